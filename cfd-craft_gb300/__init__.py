@@ -1,0 +1,10 @@
+"""GB300 pressure-projection engine for CFD-craft.
+
+Modules:
+  grid      -- Grid.build(case): the staggered grid arrays (crates/cfd-craft/src/grid.rs)
+  pressure  -- project / solve_scaled / solve / apply / center_nullspaces (pressure.rs)
+  engine    -- ctypes binding of libcfdgpu.so (include/cfdgpu.h)
+  synth     -- seeded synthetic cases of the benchmark configurations
+  build     -- in-tree build of libcfdgpu.so for sm_103a
+"""
+from . import engine, grid, pressure, synth  # noqa: F401

@@ -1,0 +1,1332 @@
+// GB300 pressure-projection engine: device kernels of the plain FP64 form and the
+// C ABI of include/cfdgpu.h.
+//
+// Build: nvcc -gencode arch=compute_103a,code=sm_103a -fmad=false (see build.py).
+//
+// Layout in HBM, per grid (N cells, F faces):
+//   flags  u16[N]   interior/outlet bits of the six faces of each cell
+//   fw     f64[F]   face weights area/(distance*volume), recomputed when faces change
+//   face_kind u8[F], face_lo/face_hi i32[F], face_dist f64[F]   (velocity correction)
+//   x r z p ap bc b terms  f64[N]   PCG and projection vectors
+//   IC(0): lower CSR (i32 off/col, f64 val), its transpose, diag, level orders
+//   multigrid: per level CSR + diag, level orders, transfer CSRs, vectors
+// The PCG loop runs as CUDA graphs of 8 iterations; every kernel first reads the
+// device Scalars and returns at once when the solve has finished, so the host only
+// synchronises between chunks, where it polls the caller's Control.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cfdgpu.h"
+#include "plain_kernels.cuh"
+#include "setup.hpp"
+
+using namespace cfdg;
+
+// ============================================================== device helpers
+
+namespace {
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (w == 0) {
+    s = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  }
+  return s;  // valid in thread 0
+}
+
+// Publishes this block's partial; true in every thread of the block that arrives last.
+__device__ __forceinline__ bool arrive(double partial, double* partials, unsigned* counter) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = partial;
+    __threadfence();
+    unsigned t = atomicAdd(counter, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  return last;
+}
+
+// Sum of the partials in a fixed order (thread 0), by the last block.
+__device__ __forceinline__ double gather_partials(const double* partials, double* sh, unsigned* counter) {
+  __threadfence();
+  double v = 0.0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) v += __ldcg(&partials[b]);
+  double s = block_sum(v, sh);
+  if (threadIdx.x == 0) *counter = 0;
+  return s;
+}
+
+__device__ __forceinline__ long long face_index(const GridDev& g, int a, int q0, int q1, int q2) {
+  return g.face_off[a] + ((long long)q2 * g.fdim[a][1] + q1) * g.fdim[a][0] + q0;
+}
+
+// (A x)_c in the reference's face order (pressure.rs:273-285, grid.rs:341-429):
+// for each axis the lower face, then the upper face, except on a periodic axis
+// where the last cell's upper face is the wrap face at coordinate 0, which comes
+// first in face order. Interior faces add d = w (x_lo - x_hi) to lo and subtract
+// it from hi; outlet faces add w x_c.
+template <bool UNIFORM>
+__device__ __forceinline__ double op_cell(const GridDev& g, const double* __restrict__ x, int c, int q0, int q1,
+                                          int q2, unsigned fl) {
+  double y = 0.0;
+  const double xc = x[c];
+  const int q[3] = {q0, q1, q2};
+  const int stride[3] = {1, g.n[0], g.n[0] * g.n[1]};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const unsigned lin = (fl >> (2 * a)) & 1u, uin = (fl >> (2 * a + 1)) & 1u;
+    const unsigned lout = (fl >> (6 + 2 * a)) & 1u, uout = (fl >> (7 + 2 * a)) & 1u;
+    if (!(lin | uin | lout | uout)) continue;
+    const int na = g.n[a];
+    double wl, wu;
+    if (UNIFORM) {
+      wl = lout ? g.w_out[a] : g.w_in[a];
+      wu = uout ? g.w_out[a] : g.w_in[a];
+    } else {
+      int p[3] = {q0, q1, q2};
+      wl = g.fw[face_index(g, a, p[0], p[1], p[2])];
+      p[a] = (g.per[a] && q[a] == na - 1) ? 0 : q[a] + 1;
+      wu = g.fw[face_index(g, a, p[0], p[1], p[2])];
+    }
+    if (g.per[a] && na == 1) {  // one face joining the cell to itself
+      if (lin) {
+        double d = wl * (xc - xc);
+        y = y + d;
+        y = y - d;
+      }
+      continue;
+    }
+    const int nl = q[a] > 0 ? c - stride[a] : c + (na - 1) * stride[a];
+    const int nu = q[a] < na - 1 ? c + stride[a] : c - (na - 1) * stride[a];
+    const bool upper_first = g.per[a] && q[a] == na - 1;
+    for (int s = 0; s < 2; ++s) {
+      const bool upper = (s == 0) == upper_first;
+      if (!upper) {
+        if (lin) {
+          double d = wl * (x[nl] - xc);
+          y = y - d;
+        } else if (lout) {
+          y = y + wl * xc;
+        }
+      } else {
+        if (uin) {
+          double d = wu * (xc - x[nu]);
+          y = y + d;
+        } else if (uout) {
+          y = y + wu * xc;
+        }
+      }
+    }
+  }
+  return y;
+}
+
+__device__ __forceinline__ void cell_coords(const GridDev& g, int c, int& q0, int& q1, int& q2) {
+  q0 = c % g.n[0];
+  int t = c / g.n[0];
+  q1 = t % g.n[1];
+  q2 = t / g.n[1];
+}
+
+// ============================================================== kernels
+
+template <bool UNIFORM>
+__global__ void k_apply(GridDev g, const double* __restrict__ x, double* __restrict__ y, int N) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+    int q0, q1, q2;
+    cell_coords(g, c, q0, q1, q2);
+    unsigned fl = g.flags[c];
+    y[c] = fl ? op_cell<UNIFORM>(g, x, c, q0, q1, q2, fl) : 0.0;
+  }
+}
+
+// Iteration start: Ap = A p, denom = p.Ap, alpha = rz/denom (pressure.rs:391-397).
+template <bool UNIFORM>
+__global__ void k_pcg_op(GridDev g, const double* __restrict__ p, double* __restrict__ ap, int N, double* partials,
+                         Scalars* S) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  if (S->it >= S->max_it) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) S->done = 3;
+    return;
+  }
+  double acc = 0.0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+    int q0, q1, q2;
+    cell_coords(g, c, q0, q1, q2);
+    unsigned fl = g.flags[c];
+    double v = fl ? op_cell<UNIFORM>(g, p, c, q0, q1, q2, fl) : 0.0;
+    ap[c] = v;
+    acc += p[c] * v;
+  }
+  double bs = block_sum(acc, sh);
+  if (arrive(bs, partials, &S->counter)) {
+    double denom = gather_partials(partials, sh, &S->counter);
+    if (threadIdx.x == 0) {
+      if (!(denom > 0.0) || !isfinite(denom)) {
+        S->done = 2;
+        S->error = CFDG_E032;
+      } else {
+        S->alpha = S->rz / denom;
+      }
+    }
+  }
+}
+
+// x += alpha p, r -= alpha Ap, rel = |r|/|b_c| (pressure.rs:398-403).
+__global__ void k_pcg_xr(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
+                         const double* __restrict__ ap, int N, double* partials, Scalars* S) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  const double alpha = S->alpha;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    x[i] = x[i] + alpha * p[i];
+    double v = r[i] - alpha * ap[i];
+    r[i] = v;
+    acc += v * v;
+  }
+  double bs = block_sum(acc, sh);
+  if (arrive(bs, partials, &S->counter)) {
+    double rr = gather_partials(partials, sh, &S->counter);
+    if (threadIdx.x == 0) {
+      S->rel = sqrt(rr) / S->norm;
+      S->check = S->rel <= S->tol;
+    }
+  }
+}
+
+// The true-residual gate (pressure.rs:403-425): |A x - b_c| / |b_c| <= 10 tol + 1e-12.
+template <bool UNIFORM>
+__global__ void k_pcg_true(GridDev g, const double* __restrict__ x, const double* __restrict__ bc, int N,
+                           double* partials, Scalars* S) {
+  __shared__ double sh[32];
+  if (S->done || !S->check) return;
+  double acc = 0.0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+    int q0, q1, q2;
+    cell_coords(g, c, q0, q1, q2);
+    unsigned fl = g.flags[c];
+    double v = fl ? op_cell<UNIFORM>(g, x, c, q0, q1, q2, fl) : 0.0;
+    double d = v - bc[c];
+    acc += d * d;
+  }
+  double bs = block_sum(acc, sh);
+  if (arrive(bs, partials, &S->counter)) {
+    double s = gather_partials(partials, sh, &S->counter);
+    if (threadIdx.x == 0) {
+      S->true_checks += 1;
+      double tr = sqrt(s) / S->norm;
+      S->true_rel = tr;
+      if (tr <= S->tol * 10.0 + 1e-12) S->done = 1;
+    }
+  }
+}
+
+// rz' = r.z, beta = rz'/rz, it += 1 (pressure.rs:428-433). init: the first rz.
+__global__ void k_pcg_rz(const double* __restrict__ r, const double* __restrict__ z, int N, double* partials,
+                         Scalars* S, int init) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) acc += r[i] * z[i];
+  double bs = block_sum(acc, sh);
+  if (arrive(bs, partials, &S->counter)) {
+    double next = gather_partials(partials, sh, &S->counter);
+    if (threadIdx.x == 0) {
+      if (init) {
+        S->rz = next;
+      } else {
+        S->beta = next / S->rz;
+        S->rz = next;
+        S->it += 1;
+      }
+    }
+  }
+}
+
+__global__ void k_pcg_p(double* __restrict__ p, const double* __restrict__ z, int N, const Scalars* S) {
+  if (S->done) return;
+  const double beta = S->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) p[i] = z[i] + beta * p[i];
+}
+
+// norm = |r|; a zero right-hand side ends the solve with x = 0 (pressure.rs:372-375).
+__global__ void k_pcg_norm(const double* __restrict__ r, int N, double* partials, Scalars* S) {
+  __shared__ double sh[32];
+  if (S->done) return;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) acc += r[i] * r[i];
+  double bs = block_sum(acc, sh);
+  if (arrive(bs, partials, &S->counter)) {
+    double rr = gather_partials(partials, sh, &S->counter);
+    if (threadIdx.x == 0) {
+      S->norm = sqrt(rr);
+      if (S->norm < 1e-24) S->done = 4;
+    }
+  }
+}
+
+__global__ void k_copy(double* __restrict__ dst, const double* __restrict__ src, int N, const Scalars* S) {
+  if (S && S->done) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) dst[i] = src[i];
+}
+__global__ void k_fill(double* __restrict__ dst, double v, int N, const Scalars* S) {
+  if (S && S->done) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) dst[i] = v;
+}
+
+// Gauge: subtract each group's mean from its members (pressure.rs:316-325,
+// masked.rs:82-89). One block per group; the sum is a fixed-order tree.
+__global__ void k_center(const int* __restrict__ off, const int* __restrict__ members, double* __restrict__ x,
+                         const Scalars* S) {
+  __shared__ double sh[32];
+  __shared__ double mean;
+  if (S && S->done) return;
+  const int gidx = blockIdx.x;
+  const int b = off[gidx], e = off[gidx + 1];
+  double acc = 0.0;
+  for (int k = b + threadIdx.x; k < e; k += blockDim.x) acc += x[members[k]];
+  double s = block_sum(acc, sh);
+  if (threadIdx.x == 0) mean = s / (double)(e - b);
+  __syncthreads();
+  const double m = mean;
+  for (int k = b + threadIdx.x; k < e; k += blockDim.x) x[members[k]] = x[members[k]] - m;
+}
+
+// Compatibility of the closed components (pressure.rs:351-362): one block per group.
+__global__ void k_compat(const int* __restrict__ off, const int* __restrict__ members, const double* __restrict__ b,
+                         const double* __restrict__ terms, int use_terms, Scalars* S) {
+  __shared__ double sh[32];
+  const int gidx = blockIdx.x;
+  const int lo = off[gidx], hi = off[gidx + 1];
+  double acc = 0.0, sc = 0.0;
+  for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+    double v = b[members[k]];
+    acc += v;
+    sc += fmax(fabs(v), use_terms ? terms[members[k]] : 0.0);
+  }
+  double s = block_sum(acc, sh);
+  double scale = block_sum(sc, sh);
+  if (threadIdx.x == 0 && fabs(s) > 1e-9 * scale) {
+    S->error = CFDG_E031;
+    S->done = 2;
+  }
+}
+
+// IC(0) forward substitution over one dependency level (pressure.rs:225-232).
+__global__ void k_ic0_fwd(const int* __restrict__ order, int begin, int end, const int* __restrict__ off,
+                          const int* __restrict__ col, const double* __restrict__ val, const double* __restrict__ diag,
+                          const double* __restrict__ r, double* __restrict__ z, const Scalars* S) {
+  if (S && S->done) return;
+  int t = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= end) return;
+  int i = order[t];
+  double v = r[i];
+  for (int k = off[i]; k < off[i + 1]; ++k) v = v - val[k] * z[col[k]];
+  z[i] = v / diag[i];
+}
+
+// IC(0) backward substitution as a gather over one level (pressure.rs:233-240):
+// z_c = (y_c - sum over rows i > c, descending, of l_ic z_i) / d_c.
+__global__ void k_ic0_bwd(const int* __restrict__ order, int begin, int end, const int* __restrict__ off,
+                          const int* __restrict__ row, const double* __restrict__ val, const double* __restrict__ diag,
+                          double* __restrict__ z, const Scalars* S) {
+  if (S && S->done) return;
+  int t = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= end) return;
+  int c = order[t];
+  double v = z[c];
+  for (int k = off[c]; k < off[c + 1]; ++k) v = v - val[k] * z[row[k]];
+  z[c] = v / diag[c];
+}
+
+// Lexicographic Gauss-Seidel over one level (multigrid.rs:272-281, masked.rs:158-172).
+__global__ void k_gs(const int* __restrict__ order, int begin, int end, const int* __restrict__ off,
+                     const int* __restrict__ col, const double* __restrict__ val, const double* __restrict__ diag,
+                     const double* __restrict__ rhs, double* __restrict__ x, const Scalars* S) {
+  if (S && S->done) return;
+  int t = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= end) return;
+  int i = order[t];
+  const double d = diag[i];
+  if (d == 0.0) {  // an isolated sealed cell: a null pressure space
+    x[i] = 0.0;
+    return;
+  }
+  double v = rhs[i];
+  for (int k = off[i]; k < off[i + 1]; ++k) v = v - val[k] * x[col[k]];
+  x[i] = v / d;
+}
+
+// res = rhs - A x (multigrid.rs:263-271 then :691-694).
+__global__ void k_residual(int n, const int* __restrict__ off, const int* __restrict__ col,
+                           const double* __restrict__ val, const double* __restrict__ diag,
+                           const double* __restrict__ rhs, const double* __restrict__ x, double* __restrict__ res,
+                           const Scalars* S) {
+  if (S && S->done) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double v = diag[i] * x[i];
+    for (int k = off[i]; k < off[i + 1]; ++k) v = v + val[k] * x[col[k]];
+    res[i] = rhs[i] - v;
+  }
+}
+
+// Coarse rhs = P^T res, per coarse row over its children in ascending order
+// (multigrid.rs:696-701, masked.rs:325-328).
+__global__ void k_restrict(int nc, const int* __restrict__ off, const int* __restrict__ child,
+                           const double* __restrict__ w, const double* __restrict__ res, double* __restrict__ rhs_c,
+                           const Scalars* S) {
+  if (S && S->done) return;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nc; j += gridDim.x * blockDim.x) {
+    double v = 0.0;
+    for (int k = off[j]; k < off[j + 1]; ++k) v = v + w[k] * res[child[k]];
+    rhs_c[j] = v;
+  }
+}
+
+// x += P x_c (multigrid.rs:703-709, masked.rs:330-332).
+__global__ void k_prolong(int n, const int* __restrict__ off, const int* __restrict__ col,
+                          const double* __restrict__ w, const double* __restrict__ xc, double* __restrict__ x,
+                          const Scalars* S) {
+  if (S && S->done) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = -0.0;
+    for (int k = off[i]; k < off[i + 1]; ++k) s = s + w[k] * xc[col[k]];
+    x[i] = x[i] + s;
+  }
+}
+
+// Dense Cholesky solves of the terminal level, one thread per block (masked.rs:52-69).
+__global__ void k_direct(int nblocks, const int* __restrict__ ioff, const int* __restrict__ idx,
+                         const long long* __restrict__ foff, const double* __restrict__ L,
+                         const double* __restrict__ rhs, double* __restrict__ x, const Scalars* S) {
+  if (S && S->done) return;
+  int bk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (bk >= nblocks) return;
+  const int* ix = idx + ioff[bk];
+  const int n = ioff[bk + 1] - ioff[bk];
+  const double* f = L + foff[bk];
+  for (int i = 0; i < n; ++i) {
+    double v = rhs[ix[i]];
+    for (int j = 0; j < i; ++j) v = v - f[i * n + j] * x[ix[j]];
+    x[ix[i]] = v / f[i * n + i];
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double v = x[ix[i]];
+    for (int j = i + 1; j < n; ++j) v = v - f[j * n + i] * x[ix[j]];
+    x[ix[i]] = v / f[i * n + i];
+  }
+}
+
+__global__ void k_gather(int n, const int* __restrict__ idx, const double* __restrict__ src, double* __restrict__ dst,
+                         const Scalars* S) {
+  if (S && S->done) return;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) dst[j] = src[idx[j]];
+}
+__global__ void k_scatter(int n, const int* __restrict__ idx, const double* __restrict__ src, double* __restrict__ dst,
+                          const Scalars* S) {
+  if (S && S->done) return;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) dst[idx[j]] = src[j];
+}
+
+// projection_rhs (pressure.rs:440-459): b = -div(u)/dt, terms = sum(|u_lo|+|u_hi|)/dx/dt.
+__global__ void k_projection_rhs(GridDev g, const uint8_t* __restrict__ fluid, const double* __restrict__ u, double dt,
+                                 double* __restrict__ b, double* __restrict__ terms, int N) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+    if (!fluid[c]) {
+      b[c] = -0.0;
+      terms[c] = 0.0;
+      continue;
+    }
+    int q[3];
+    cell_coords(g, c, q[0], q[1], q[2]);
+    double div = 0.0, scale = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      int p[3] = {q[0], q[1], q[2]};
+      long long fl = face_index(g, a, p[0], p[1], p[2]);
+      p[a] = (g.per[a] && q[a] == g.n[a] - 1) ? 0 : q[a] + 1;
+      long long fu = face_index(g, a, p[0], p[1], p[2]);
+      double ul = u[fl], uu = u[fu];
+      div = div + (uu - ul) / g.dx[a];
+      scale = scale + (fabs(ul) + fabs(uu)) / g.dx[a];
+    }
+    b[c] = -div / dt;
+    terms[c] = scale / dt;
+  }
+}
+
+// u -= dt grad(phi) on interior and outlet faces (pressure.rs:481-496).
+__global__ void k_correct_faces(const uint8_t* __restrict__ kind, const int* __restrict__ lo,
+                                const int* __restrict__ hi, const double* __restrict__ dist,
+                                const double* __restrict__ phi, double dt, double* __restrict__ u, long long F,
+                                const Scalars* S) {
+  if (S->done != 1 && S->done != 4) return;
+  for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < F; f += (long long)gridDim.x * blockDim.x) {
+    double d;
+    uint8_t k = kind[f];
+    if (k == INTERIOR) d = (phi[hi[f]] - phi[lo[f]]) / dist[f];
+    else if (k == OUTLET) d = lo[f] >= 0 ? -phi[lo[f]] / dist[f] : phi[hi[f]] / dist[f];
+    else d = 0.0;
+    u[f] = u[f] - dt * d;
+  }
+}
+
+__global__ void k_add(double* __restrict__ p, const double* __restrict__ q, int N, const Scalars* S) {
+  if (S->done != 1 && S->done != 4) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) p[i] = p[i] + q[i];
+}
+
+__global__ void k_weights(const double* __restrict__ area, const double* __restrict__ dist, double volume,
+                          double* __restrict__ w, long long F) {
+  for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < F; f += (long long)gridDim.x * blockDim.x)
+    w[f] = area[f] / (dist[f] * volume);
+}
+
+}  // namespace
+
+// ============================================================== host side
+
+namespace {
+
+thread_local std::string t_error;
+
+int fail(int code, const std::string& msg) {
+  t_error = msg;
+  return code;
+}
+
+#define CU(expr)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (expr);                                                              \
+    if (e_ != cudaSuccess) return fail(CFDG_ERR_CUDA, std::string("CUDA: ") + #expr + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+int grid_blocks(long long n) {
+  long long b = (n + BLOCK - 1) / BLOCK;
+  return (int)std::max(1LL, std::min<long long>(b, MAX_BLOCKS));
+}
+
+}  // namespace
+
+struct cfdg_context {
+  int device = 0;
+  uint64_t budget = 0;
+  std::atomic<uint64_t> used{0};
+};
+
+namespace {
+
+// Device allocation owned by a grid, counted against the context's budget.
+struct Arena {
+  cfdg_context* ctx = nullptr;
+  std::vector<void*> ptrs;
+  uint64_t bytes = 0;
+  template <class T>
+  int alloc(T** p, size_t n) {
+    size_t b = std::max<size_t>(n, 1) * sizeof(T);
+    if (ctx->used.load() + b > ctx->budget) return fail(CFDG_ERR_ADMISSION, "the grid does not fit the context's HBM budget");
+    CU(cudaMalloc((void**)p, b));
+    ptrs.push_back(*p);
+    bytes += b;
+    ctx->used += b;
+    return 0;
+  }
+  template <class T>
+  int upload(T** p, const std::vector<T>& v, cudaStream_t s) {
+    if (int e = alloc(p, v.size())) return e;
+    if (!v.empty()) CU(cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return 0;
+  }
+  void release() {
+    for (void* p : ptrs) cudaFree(p);
+    if (ctx) ctx->used -= bytes;
+    ptrs.clear();
+    bytes = 0;
+  }
+};
+
+struct DevCsr {
+  int* off = nullptr;
+  int* col = nullptr;
+  double* val = nullptr;
+  int rows = 0;
+};
+int upload_csr(Arena& A, const Csr& c, DevCsr& d, cudaStream_t s) {
+  d.rows = c.rows();
+  if (int e = A.upload(&d.off, c.off, s)) return e;
+  if (int e = A.upload(&d.col, c.col, s)) return e;
+  if (!c.val.empty() || c.col.empty())
+    if (int e = A.upload(&d.val, c.val, s)) return e;
+  return 0;
+}
+
+struct DevSchedule {
+  int* order = nullptr;
+  std::vector<int32_t> start;
+};
+
+struct DevIc0 {
+  Arena arena;
+  DevCsr lower, upper;
+  double* diag = nullptr;
+  DevSchedule fwd, bwd;
+};
+
+struct DevLevel {
+  int n = 0;
+  DevCsr a;
+  double* diag = nullptr;
+  DevSchedule fwd, bwd;
+  DevCsr groups, prolong, restrict_;
+  int ngroups = 0;
+  bool terminal = false;
+  int nblocks = 0;
+  int* d_ioff = nullptr;
+  int* d_idx = nullptr;
+  long long* d_foff = nullptr;
+  double* d_fac = nullptr;
+  double *rhs = nullptr, *x = nullptr, *res = nullptr;
+};
+
+struct DevHierarchy {
+  Arena arena;
+  bool masked = false;
+  int nfluid = 0;
+  int* fluid_idx = nullptr;
+  std::vector<DevLevel> levels;
+  std::vector<uint64_t> level_cells, level_nonzeros;
+};
+
+}  // namespace
+
+struct cfdg_grid {
+  cfdg_context* ctx = nullptr;
+  std::mutex mu;        // serialises solves on this grid
+  std::mutex stats_mu;  // guards the stats copy (readable from a poll callback)
+  std::string stats_json;
+  HostGrid h;
+  int preconditioner = 0, precision = 0;
+  cudaStream_t stream = nullptr;
+  Arena arena;  // topology, weights, vectors, scalars
+  GridDev g{};
+  bool uniform = false;
+  uint8_t* d_fluid = nullptr;
+  uint16_t* d_flags = nullptr;
+  uint8_t* d_kind = nullptr;
+  int *d_lo = nullptr, *d_hi = nullptr;
+  double *d_area = nullptr, *d_dist = nullptr, *d_fw = nullptr;
+  DevCsr comp_groups;  // closed components of the grid
+  int ncomp_groups = 0;
+  double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *ap = nullptr, *bc = nullptr, *b = nullptr,
+         *terms = nullptr, *u = nullptr, *pp = nullptr;
+  double* partials = nullptr;
+  Scalars* S = nullptr;
+  Scalars* hS = nullptr;  // pinned mirror
+  std::unique_ptr<DevIc0> ic0;
+  std::unique_ptr<DevHierarchy> mg;
+  std::unique_ptr<Signature> signature;
+  cudaGraphExec_t chunk = nullptr;  // 8 PCG iterations
+  int chunk_kind = -1;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+constexpr int CHUNK = 8;
+
+void reset_chunk(cfdg_grid* G) {
+  if (G->chunk) cudaGraphExecDestroy(G->chunk);
+  G->chunk = nullptr;
+  G->chunk_kind = -1;
+}
+
+int launch_center(cfdg_grid* G, const DevCsr& groups, int ngroups, double* x, const Scalars* S) {
+  if (ngroups == 0) return 0;
+  k_center<<<ngroups, BLOCK, 0, G->stream>>>(groups.off, groups.col, x, S);
+  return 0;
+}
+
+void launch_sweep_ic0(cfdg_grid* G, const Scalars* S) {
+  DevIc0& F = *G->ic0;
+  for (size_t l = 0; l + 1 < F.fwd.start.size(); ++l) {
+    int b = F.fwd.start[l], e = F.fwd.start[l + 1];
+    k_ic0_fwd<<<(e - b + BLOCK - 1) / BLOCK, BLOCK, 0, G->stream>>>(F.fwd.order, b, e, F.lower.off, F.lower.col,
+                                                                     F.lower.val, F.diag, G->r, G->z, S);
+  }
+  for (size_t l = 0; l + 1 < F.bwd.start.size(); ++l) {
+    int b = F.bwd.start[l], e = F.bwd.start[l + 1];
+    k_ic0_bwd<<<(e - b + BLOCK - 1) / BLOCK, BLOCK, 0, G->stream>>>(F.bwd.order, b, e, F.upper.off, F.upper.col,
+                                                                     F.upper.val, F.diag, G->z, S);
+  }
+}
+
+void launch_gs(cfdg_grid* G, DevLevel& L, bool backward, const Scalars* S) {
+  const DevSchedule& sc = backward ? L.bwd : L.fwd;
+  for (size_t l = 0; l + 1 < sc.start.size(); ++l) {
+    int b = sc.start[l], e = sc.start[l + 1];
+    k_gs<<<(e - b + BLOCK - 1) / BLOCK, BLOCK, 0, G->stream>>>(sc.order, b, e, L.a.off, L.a.col, L.a.val, L.diag,
+                                                                L.rhs, L.x, S);
+  }
+}
+
+// One symmetric V(2,2) cycle, z = M^-1 r (multigrid.rs:656-726, masked.rs:292-342).
+void launch_vcycle(cfdg_grid* G, const double* r, double* z, const Scalars* S) {
+  DevHierarchy& H = *G->mg;
+  cudaStream_t s = G->stream;
+  const int N = (int)G->h.cells;
+  DevLevel& L0 = H.levels[0];
+  if (H.masked) k_gather<<<grid_blocks(H.nfluid), BLOCK, 0, s>>>(H.nfluid, H.fluid_idx, r, L0.rhs, S);
+  else k_copy<<<grid_blocks(N), BLOCK, 0, s>>>(L0.rhs, r, N, S);
+  const int nl = (int)H.levels.size();
+  for (int l = 0; l < nl; ++l) {
+    DevLevel& L = H.levels[l];
+    launch_center(G, L.groups, L.ngroups, L.rhs, S);
+    k_fill<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.x, 0.0, L.n, S);
+    if (L.terminal) {
+      if (L.nblocks > 0)
+        k_direct<<<(L.nblocks + 63) / 64, 64, 0, s>>>(L.nblocks, L.d_ioff, L.d_idx, L.d_foff, L.d_fac, L.rhs, L.x, S);
+      launch_center(G, L.groups, L.ngroups, L.x, S);
+      break;
+    }
+    launch_gs(G, L, false, S);
+    launch_gs(G, L, false, S);
+    launch_center(G, L.groups, L.ngroups, L.x, S);
+    k_residual<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.n, L.a.off, L.a.col, L.a.val, L.diag, L.rhs, L.x, L.res, S);
+    launch_center(G, L.groups, L.ngroups, L.res, S);
+    DevLevel& C = H.levels[l + 1];
+    k_restrict<<<grid_blocks(C.n), BLOCK, 0, s>>>(C.n, L.restrict_.off, L.restrict_.col, L.restrict_.val, L.res,
+                                                  C.rhs, S);
+  }
+  for (int l = nl - 2; l >= 0; --l) {
+    DevLevel& L = H.levels[l];
+    DevLevel& C = H.levels[l + 1];
+    k_prolong<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.n, L.prolong.off, L.prolong.col, L.prolong.val, C.x, L.x, S);
+    launch_gs(G, L, true, S);
+    launch_gs(G, L, true, S);
+    launch_center(G, L.groups, L.ngroups, L.x, S);
+  }
+  if (H.masked) {
+    k_fill<<<grid_blocks(N), BLOCK, 0, s>>>(z, 0.0, N, S);
+    k_scatter<<<grid_blocks(H.nfluid), BLOCK, 0, s>>>(H.nfluid, H.fluid_idx, L0.x, z, S);
+  } else {
+    k_copy<<<grid_blocks(N), BLOCK, 0, s>>>(z, L0.x, N, S);
+  }
+}
+
+// z = M^-1 r with the grid's preconditioner, then the gauge.
+void launch_precondition(cfdg_grid* G, const Scalars* S) {
+  if (G->preconditioner == CFDG_PRECOND_MULTIGRID) launch_vcycle(G, G->r, G->z, S);
+  else launch_sweep_ic0(G, S);
+  launch_center(G, G->comp_groups, G->ncomp_groups, G->z, S);
+}
+
+template <bool U>
+void launch_iteration_t(cfdg_grid* G) {
+  const int N = (int)G->h.cells;
+  const int nb = grid_blocks(N);
+  cudaStream_t s = G->stream;
+  k_pcg_op<U><<<nb, BLOCK, 0, s>>>(G->g, G->p, G->ap, N, G->partials, G->S);
+  k_pcg_xr<<<nb, BLOCK, 0, s>>>(G->x, G->r, G->p, G->ap, N, G->partials, G->S);
+  k_pcg_true<U><<<nb, BLOCK, 0, s>>>(G->g, G->x, G->bc, N, G->partials, G->S);
+  launch_precondition(G, G->S);
+  k_pcg_rz<<<nb, BLOCK, 0, s>>>(G->r, G->z, N, G->partials, G->S, 0);
+  k_pcg_p<<<nb, BLOCK, 0, s>>>(G->p, G->z, N, G->S);
+}
+void launch_iteration(cfdg_grid* G) {
+  if (G->uniform) launch_iteration_t<true>(G);
+  else launch_iteration_t<false>(G);
+}
+
+template <bool U>
+void launch_apply_t(cfdg_grid* G, const double* x, double* y) {
+  const int N = (int)G->h.cells;
+  k_apply<U><<<grid_blocks(N), BLOCK, 0, G->stream>>>(G->g, x, y, N);
+}
+void launch_apply(cfdg_grid* G, const double* x, double* y) {
+  if (G->uniform) launch_apply_t<true>(G, x, y);
+  else launch_apply_t<false>(G, x, y);
+}
+
+// Recomputes face weights on the device and decides the uniform fast path.
+int refresh_weights(cfdg_grid* G) {
+  HostGrid& h = G->h;
+  CU(cudaMemcpyAsync(G->d_area, h.face_area.data(), h.faces * 8, cudaMemcpyHostToDevice, G->stream));
+  CU(cudaMemcpyAsync(G->d_dist, h.face_distance.data(), h.faces * 8, cudaMemcpyHostToDevice, G->stream));
+  k_weights<<<grid_blocks(h.faces), BLOCK, 0, G->stream>>>(G->d_area, G->d_dist, h.volume, G->d_fw, h.faces);
+  bool uniform = true;
+  uint64_t win[3] = {0, 0, 0}, wout[3] = {0, 0, 0};
+  bool hin[3] = {false, false, false}, hout[3] = {false, false, false};
+  for (int a = 0; a < 3 && uniform; ++a)
+    for (int64_t f = h.face_offset[a]; f < h.face_offset[a] + h.face_dims[a][0] * h.face_dims[a][1] * h.face_dims[a][2];
+         ++f) {
+      uint8_t k = h.face_kind[f];
+      if (k != INTERIOR && k != OUTLET) continue;
+      double w = h.weight(f);
+      uint64_t bits;
+      std::memcpy(&bits, &w, 8);
+      uint64_t* slot = k == INTERIOR ? &win[a] : &wout[a];
+      bool* has = k == INTERIOR ? &hin[a] : &hout[a];
+      if (!*has) {
+        *slot = bits;
+        *has = true;
+      } else if (*slot != bits) {
+        uniform = false;
+        break;
+      }
+    }
+  G->uniform = uniform;
+  for (int a = 0; a < 3; ++a) {
+    std::memcpy(&G->g.w_in[a], &win[a], 8);
+    std::memcpy(&G->g.w_out[a], &wout[a], 8);
+  }
+  CU(cudaGetLastError());
+  return 0;
+}
+
+int build_ic0_dev(cfdg_grid* G) {
+  Ic0 F;
+  build_ic0(G->h, F);
+  auto D = std::make_unique<DevIc0>();
+  D->arena.ctx = G->ctx;
+  cudaStream_t s = G->stream;
+  if (int e = upload_csr(D->arena, F.lower, D->lower, s)) return e;
+  if (int e = upload_csr(D->arena, F.upper, D->upper, s)) return e;
+  if (int e = D->arena.upload(&D->diag, F.diag, s)) return e;
+  if (int e = D->arena.upload(&D->fwd.order, F.fwd.order, s)) return e;
+  if (int e = D->arena.upload(&D->bwd.order, F.bwd.order, s)) return e;
+  D->fwd.start = F.fwd.start;
+  D->bwd.start = F.bwd.start;
+  CU(cudaStreamSynchronize(s));
+  G->ic0 = std::move(D);
+  return 0;
+}
+
+std::string stats_json_of(const DevHierarchy& H) {
+  std::string s = "{\"level_cells\":[";
+  for (size_t i = 0; i < H.level_cells.size(); ++i) s += (i ? "," : "") + std::to_string(H.level_cells[i]);
+  s += "],\"level_nonzeros\":[";
+  for (size_t i = 0; i < H.level_nonzeros.size(); ++i) s += (i ? "," : "") + std::to_string(H.level_nonzeros[i]);
+  s += "],\"allocated_bytes\":" + std::to_string(H.arena.bytes) + "}";
+  return s;
+}
+
+int build_mg_dev(cfdg_grid* G, const Poller& poll) {
+  Hierarchy H;
+  if (int e = build_hierarchy(G->h, poll, H)) {
+    if (e == CFDG_E034) return fail(e, "CFD-E034: numerics.pressure_preconditioner: multigrid requires fluid cells");
+    if (e == CFDG_E035) return fail(e, "CFD-E035: numerics.pressure_preconditioner: multigrid coarse Cholesky lost positive definiteness");
+    if (e == CFDG_CANCELLED) return fail(e, "cancelled");
+    if (e == CFDG_WALL_TIME) return fail(e, "wall_time_limit");
+    if (e == CFDG_ERR_UNSUPPORTED) return fail(e, "strongly anisotropic spacing needs line smoothing, which this engine does not implement");
+    return fail(e, "multigrid setup failed");
+  }
+  auto D = std::make_unique<DevHierarchy>();
+  D->arena.ctx = G->ctx;
+  cudaStream_t s = G->stream;
+  D->masked = H.masked;
+  D->nfluid = (int)H.fluid_indices.size();
+  if (H.masked)
+    if (int e = D->arena.upload(&D->fluid_idx, H.fluid_indices, s)) return e;
+  D->levels.resize(H.levels.size());
+  for (size_t l = 0; l < H.levels.size(); ++l) {
+    MgLevel& M = H.levels[l];
+    DevLevel& L = D->levels[l];
+    L.n = M.n;
+    if (int e = upload_csr(D->arena, M.a, L.a, s)) return e;
+    if (int e = D->arena.upload(&L.diag, M.diag, s)) return e;
+    if (int e = D->arena.upload(&L.fwd.order, M.fwd.order, s)) return e;
+    if (int e = D->arena.upload(&L.bwd.order, M.bwd.order, s)) return e;
+    L.fwd.start = M.fwd.start;
+    L.bwd.start = M.bwd.start;
+    L.ngroups = M.groups.rows();
+    if (L.ngroups)
+      if (int e = upload_csr(D->arena, M.groups, L.groups, s)) return e;
+    L.terminal = M.direct_idx.rows() > 0 || l + 1 == H.levels.size();
+    if (L.terminal) {
+      L.nblocks = M.direct_idx.rows();
+      if (int e = D->arena.upload(&L.d_ioff, M.direct_idx.off, s)) return e;
+      if (int e = D->arena.upload(&L.d_idx, M.direct_idx.col, s)) return e;
+      std::vector<long long> foff(M.direct_off.begin(), M.direct_off.end());
+      if (int e = D->arena.upload(&L.d_foff, foff, s)) return e;
+      if (int e = D->arena.upload(&L.d_fac, M.direct_factor, s)) return e;
+    } else {
+      if (int e = upload_csr(D->arena, M.prolong, L.prolong, s)) return e;
+      if (int e = upload_csr(D->arena, M.restrict, L.restrict_, s)) return e;
+    }
+    if (int e = D->arena.alloc(&L.rhs, L.n)) return e;
+    if (int e = D->arena.alloc(&L.x, L.n)) return e;
+    if (int e = D->arena.alloc(&L.res, L.n)) return e;
+  }
+  D->level_cells = H.level_cells;
+  D->level_nonzeros = H.level_nonzeros;
+  CU(cudaStreamSynchronize(s));
+  {
+    std::lock_guard<std::mutex> lk(G->stats_mu);
+    G->stats_json = stats_json_of(*D);
+  }
+  G->mg = std::move(D);
+  return 0;
+}
+
+// pressure.rs:55-97: the cached factor, or the hierarchy checked against its signature.
+int prepare_preconditioner(cfdg_grid* G, const Poller& poll, cfdg_info* info) {
+  if (G->preconditioner == CFDG_PRECOND_MULTIGRID) {
+    if (int c = poll.check()) return fail(c, c == CFDG_CANCELLED ? "cancelled" : "wall_time_limit");
+    if (G->h.n_components == 0)
+      return fail(CFDG_E034, "CFD-E034: numerics.pressure_preconditioner: multigrid requires fluid cells");
+    Signature cur;
+    int se = signature_of(G->h, cur);
+    bool rebuild = !G->mg || !G->signature || se != 0 || !(cur == *G->signature);
+    if (rebuild) {
+      if (se)
+        return fail(CFDG_E034, "CFD-E034: numerics.pressure_preconditioner: multigrid requires finite positive pressure face weights");
+      G->mg.reset();
+      reset_chunk(G);
+      if (int e = build_mg_dev(G, poll)) return e;
+      G->signature = std::make_unique<Signature>(std::move(cur));
+      if (info) info->hierarchy_builds = 1;
+    }
+    if (info) {
+      info->hierarchy_levels = G->mg->level_cells.size();
+      for (auto v : G->mg->level_cells) info->hierarchy_cells += v;
+      for (auto v : G->mg->level_nonzeros) info->hierarchy_nonzeros += v;
+    }
+  } else if (!G->ic0) {
+    reset_chunk(G);
+    if (int e = build_ic0_dev(G)) return e;
+  }
+  return 0;
+}
+
+int ensure_chunk(cfdg_grid* G) {
+  int kind = G->preconditioner * 2 + (G->uniform ? 1 : 0);
+  if (G->chunk && G->chunk_kind == kind) return 0;
+  reset_chunk(G);
+  cudaGraph_t graph;
+  CU(cudaStreamBeginCapture(G->stream, cudaStreamCaptureModeThreadLocal));
+  for (int i = 0; i < CHUNK; ++i) launch_iteration(G);
+  CU(cudaStreamEndCapture(G->stream, &graph));
+  cudaError_t e = cudaGraphInstantiate(&G->chunk, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(CFDG_ERR_CUDA, std::string("CUDA graph: ") + cudaGetErrorString(e));
+  G->chunk_kind = kind;
+  return 0;
+}
+
+int poll_code(int c) { return fail(c, c == CFDG_CANCELLED ? "cancelled" : "wall_time_limit"); }
+
+// The PCG solve of pressure.rs:342-436 on device vectors: G->b (and G->terms when
+// use_terms) in, G->x out. Returns 0 or a CFDG code; fills info.
+int solve_device(cfdg_grid* G, bool use_terms, double tol, uint64_t max_iter, const Poller& poll, cfdg_info* info) {
+  const int N = (int)G->h.cells;
+  const int nb = grid_blocks(N);
+  cudaStream_t s = G->stream;
+  cfdg_info local{};
+  cfdg_info* inf = info ? info : &local;
+  std::memset(inf, 0, sizeof(*inf));
+  Scalars init{};
+  init.tol = tol;
+  init.max_it = (long long)std::min<uint64_t>(max_iter, (uint64_t)1 << 62);
+  CU(cudaMemcpyAsync(G->S, &init, sizeof(Scalars), cudaMemcpyHostToDevice, s));
+  CU(cudaEventRecord(G->ev0, s));
+  // Compatibility of closed components (pressure.rs:351-362).
+  if (G->ncomp_groups)
+    k_compat<<<G->ncomp_groups, BLOCK, 0, s>>>(G->comp_groups.off, G->comp_groups.col, G->b, G->terms,
+                                               use_terms ? 1 : 0, G->S);
+  CU(cudaMemcpyAsync(G->hS, G->S, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  if (G->hS->done == 2) return fail(CFDG_E031, "CFD-E031: incompatible flux in a closed fluid component");
+  if (int e = prepare_preconditioner(G, poll, inf)) return e;
+  if (int e = ensure_chunk(G)) return e;
+  // Prologue: x = 0, r = centred b, norm, z = M^-1 r, p = z, rz = r.z.
+  k_fill<<<nb, BLOCK, 0, s>>>(G->x, 0.0, N, nullptr);
+  k_copy<<<nb, BLOCK, 0, s>>>(G->r, G->b, N, nullptr);
+  launch_center(G, G->comp_groups, G->ncomp_groups, G->r, nullptr);
+  k_copy<<<nb, BLOCK, 0, s>>>(G->bc, G->r, N, nullptr);
+  k_pcg_norm<<<nb, BLOCK, 0, s>>>(G->r, N, G->partials, G->S);
+  launch_precondition(G, G->S);
+  k_copy<<<nb, BLOCK, 0, s>>>(G->p, G->z, N, G->S);
+  k_pcg_rz<<<nb, BLOCK, 0, s>>>(G->r, G->z, N, G->partials, G->S, 1);
+  CU(cudaGetLastError());
+  int status = 0;
+  for (;;) {
+    CU(cudaMemcpyAsync(G->hS, G->S, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    Scalars st = *G->hS;
+    if (st.done) {
+      if (st.done == 1) status = 0;
+      else if (st.done == 4) status = 0;
+      else if (st.done == 2) status = fail(st.error, "CFD-E032: pressure CG lost positive definiteness");
+      else status = fail(CFDG_E033, "CFD-E033: pressure iteration limit " + std::to_string(max_iter));
+      inf->iterations = st.done == 1 ? (uint64_t)st.it + 1 : 0;
+      inf->relative_residual = st.done == 1 ? st.true_rel : 0.0;
+      uint64_t loop_ops = st.done == 4 ? 0 : (uint64_t)st.it + (st.done == 3 ? 0 : 1);
+      inf->work_units = loop_ops;
+      inf->true_residual_checks = (uint64_t)st.true_checks;
+      inf->operator_applications = loop_ops + (uint64_t)st.true_checks;
+      inf->preconditioner_applications = st.done == 4 ? 0 : 1 + (uint64_t)st.it;
+      break;
+    }
+    if (st.it >= (long long)max_iter) {  // not reached: the op kernel flags done = 3
+      status = fail(CFDG_E033, "CFD-E033: pressure iteration limit " + std::to_string(max_iter));
+      break;
+    }
+    if (int c = poll.check()) return poll_code(c);
+    CU(cudaGraphLaunch(G->chunk, s));
+  }
+  if (G->preconditioner == CFDG_PRECOND_MULTIGRID && G->mg) {
+    uint64_t cyc = inf->preconditioner_applications;
+    inf->cycles = cyc;
+    uint64_t inner = 0;
+    for (size_t l = 0; l + 1 < G->mg->levels.size(); ++l) inner += G->mg->levels[l].n;
+    inf->smoothing_cell_updates = 4 * inner * cyc;
+    inf->residual_cell_updates = inner * cyc;
+    inf->restriction_cell_updates = inner * cyc;
+    inf->prolongation_cell_updates = inner * cyc;
+    inf->coarse_solves = cyc;
+  }
+  if (status == 0 && G->hS->done == 1) launch_center(G, G->comp_groups, G->ncomp_groups, G->x, nullptr);
+  if (status == 0 && G->hS->done == 4) k_fill<<<nb, BLOCK, 0, s>>>(G->x, 0.0, N, nullptr);
+  CU(cudaEventRecord(G->ev1, s));
+  CU(cudaEventSynchronize(G->ev1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, G->ev0, G->ev1);
+  inf->device_seconds = ms * 1e-3;
+  return status;
+}
+
+int project_device(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol, uint64_t max_iter,
+                   const Poller& poll, cfdg_info* info) {
+  const int N = (int)G->h.cells;
+  cudaStream_t s = G->stream;
+  k_projection_rhs<<<grid_blocks(N), BLOCK, 0, s>>>(G->g, G->d_fluid, d_u, dt, G->b, G->terms, N);
+  if (int e = solve_device(G, true, tol, max_iter, poll, info)) return e;
+  k_correct_faces<<<grid_blocks(G->h.faces), BLOCK, 0, s>>>(G->d_kind, G->d_lo, G->d_hi, G->d_dist, G->x, dt, d_u,
+                                                            G->h.faces, G->S);
+  k_add<<<grid_blocks(N), BLOCK, 0, s>>>(d_p, G->x, N, G->S);
+  launch_center(G, G->comp_groups, G->ncomp_groups, d_p, nullptr);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int check_grid(cfdg_grid* G) {
+  if (!G) return fail(CFDG_ERR_INVALID, "null grid");
+  return 0;
+}
+
+}  // namespace
+
+// ============================================================== C ABI
+
+extern "C" {
+
+const char* cfdg_last_error(void) { return t_error.c_str(); }
+
+int cfdg_context_create(int device, uint64_t hbm_budget_bytes, cfdg_context** out) {
+  if (!out) return fail(CFDG_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  int count = 0;
+  CU(cudaGetDeviceCount(&count));
+  if (device < 0 || device >= count) return fail(CFDG_ERR_CUDA, "no such CUDA device");
+  CU(cudaSetDevice(device));
+  size_t free_b = 0, total_b = 0;
+  CU(cudaMemGetInfo(&free_b, &total_b));
+  auto* c = new cfdg_context();
+  c->device = device;
+  c->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)(0.9 * (double)free_b);
+  *out = c;
+  return 0;
+}
+
+void cfdg_context_destroy(cfdg_context* ctx) { delete ctx; }
+
+int cfdg_grid_open(cfdg_context* ctx, const cfdg_grid_desc* d, cfdg_grid** out) {
+  if (!ctx || !d || !out) return fail(CFDG_ERR_INVALID, "null argument");
+  *out = nullptr;
+  CU(cudaSetDevice(ctx->device));
+  auto G = std::make_unique<cfdg_grid>();
+  G->ctx = ctx;
+  HostGrid& h = G->h;
+  for (int a = 0; a < 3; ++a) {
+    h.n[a] = d->n[a];
+    h.dx[a] = d->dx[a];
+    h.periodic[a] = d->periodic[a] ? 1 : 0;
+  }
+  h.volume = d->volume;
+  h.cells = (int64_t)d->n[0] * d->n[1] * d->n[2];
+  h.faces = d->n_faces;
+  if (h.cells <= 0 || h.faces <= 0 || !d->fluid || !d->face_kind || !d->face_lo || !d->face_hi || !d->face_area ||
+      !d->face_distance || !d->component || (d->n_components && !d->anchored))
+    return fail(CFDG_ERR_INVALID, "incomplete grid description");
+  h.fluid.assign(d->fluid, d->fluid + h.cells);
+  h.face_kind.assign(d->face_kind, d->face_kind + h.faces);
+  h.face_lo.resize(h.faces);
+  h.face_hi.resize(h.faces);
+  for (int64_t f = 0; f < h.faces; ++f) {
+    h.face_lo[f] = (int32_t)d->face_lo[f];
+    h.face_hi[f] = (int32_t)d->face_hi[f];
+  }
+  h.face_area.assign(d->face_area, d->face_area + h.faces);
+  h.face_distance.assign(d->face_distance, d->face_distance + h.faces);
+  h.component.assign(d->component, d->component + h.cells);
+  h.n_components = d->n_components;
+  h.anchored.assign(d->anchored, d->anchored + d->n_components);
+  std::string why = check_layout(h);
+  if (!why.empty()) return fail(CFDG_ERR_INVALID, "grid description: " + why);
+  G->preconditioner = d->preconditioner;
+  G->precision = d->precision;
+  if (G->preconditioner != CFDG_PRECOND_IC0 && G->preconditioner != CFDG_PRECOND_MULTIGRID)
+    return fail(CFDG_ERR_INVALID, "unknown preconditioner");
+  CU(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
+  CU(cudaEventCreate(&G->ev0));
+  CU(cudaEventCreate(&G->ev1));
+  Arena& A = G->arena;
+  A.ctx = ctx;
+  cudaStream_t s = G->stream;
+  // Per-cell face flags.
+  std::vector<uint16_t> flags(h.cells, 0);
+  for (int a = 0; a < 3; ++a) {
+    const int64_t* fd = h.face_dims[a];
+    int64_t f = h.face_offset[a];
+    for (int64_t k = 0; k < fd[2]; ++k)
+      for (int64_t j = 0; j < fd[1]; ++j)
+        for (int64_t i = 0; i < fd[0]; ++i, ++f) {
+          uint8_t kind = h.face_kind[f];
+          if (kind != INTERIOR && kind != OUTLET) continue;
+          int lo = h.face_lo[f], hi = h.face_hi[f];
+          unsigned base = kind == INTERIOR ? 0 : 6;
+          if (lo >= 0) flags[lo] |= (uint16_t)(1u << (base + 2 * a + 1));  // upper face of lo
+          if (hi >= 0 && !(kind == INTERIOR && lo == hi)) flags[hi] |= (uint16_t)(1u << (base + 2 * a));
+          if (kind == INTERIOR && lo == hi) flags[lo] = (uint16_t)((flags[lo] & ~(1u << (2 * a + 1))) | (1u << (2 * a)));
+        }
+  }
+  // Closed components (their cells, ascending).
+  {
+    std::vector<std::vector<int32_t>> members(h.n_components);
+    for (int64_t c = 0; c < h.cells; ++c)
+      if (h.component[c] >= 0 && !h.anchored[h.component[c]]) members[h.component[c]].push_back((int32_t)c);
+    Csr groups;
+    groups.off.push_back(0);
+    for (auto& m : members)
+      if (!m.empty()) {
+        groups.col.insert(groups.col.end(), m.begin(), m.end());
+        groups.off.push_back((int32_t)groups.col.size());
+      }
+    G->ncomp_groups = groups.rows();
+    if (G->ncomp_groups)
+      if (int e = upload_csr(A, groups, G->comp_groups, s)) return e;
+  }
+  std::vector<int32_t> lo32(h.face_lo.begin(), h.face_lo.end()), hi32(h.face_hi.begin(), h.face_hi.end());
+  const int64_t N = h.cells, F = h.faces;
+  int e = 0;
+  if ((e = A.upload(&G->d_fluid, h.fluid, s)) || (e = A.upload(&G->d_flags, flags, s)) ||
+      (e = A.upload(&G->d_kind, h.face_kind, s)) || (e = A.upload(&G->d_lo, lo32, s)) ||
+      (e = A.upload(&G->d_hi, hi32, s)) || (e = A.alloc(&G->d_area, F)) || (e = A.alloc(&G->d_dist, F)) ||
+      (e = A.alloc(&G->d_fw, F)) || (e = A.alloc(&G->x, N)) || (e = A.alloc(&G->r, N)) || (e = A.alloc(&G->z, N)) ||
+      (e = A.alloc(&G->p, N)) || (e = A.alloc(&G->ap, N)) || (e = A.alloc(&G->bc, N)) || (e = A.alloc(&G->b, N)) ||
+      (e = A.alloc(&G->terms, N)) || (e = A.alloc(&G->u, F)) || (e = A.alloc(&G->pp, N)) ||
+      (e = A.alloc(&G->partials, MAX_BLOCKS)) || (e = A.alloc(&G->S, 1))) {
+    A.release();
+    return e;
+  }
+  CU(cudaMallocHost((void**)&G->hS, sizeof(Scalars)));
+  CU(cudaMemsetAsync(G->S, 0, sizeof(Scalars), s));
+  GridDev& g = G->g;
+  for (int a = 0; a < 3; ++a) {
+    g.n[a] = h.n[a];
+    g.per[a] = h.periodic[a];
+    g.face_off[a] = h.face_offset[a];
+    for (int dd = 0; dd < 3; ++dd) g.fdim[a][dd] = (int)h.face_dims[a][dd];
+    g.dx[a] = h.dx[a];
+  }
+  g.flags = G->d_flags;
+  g.fw = G->d_fw;
+  if ((e = refresh_weights(G.get()))) return e;
+  CU(cudaStreamSynchronize(s));
+  *out = G.release();
+  return 0;
+}
+
+void cfdg_grid_close(cfdg_grid* G) {
+  if (!G) return;
+  {
+    std::lock_guard<std::mutex> lk(G->mu);
+    cudaSetDevice(G->ctx->device);
+    reset_chunk(G);
+    if (G->stream) cudaStreamSynchronize(G->stream);
+    if (G->ic0) G->ic0->arena.release();
+    if (G->mg) G->mg->arena.release();
+    G->arena.release();
+    if (G->hS) cudaFreeHost(G->hS);
+    if (G->ev0) cudaEventDestroy(G->ev0);
+    if (G->ev1) cudaEventDestroy(G->ev1);
+    if (G->stream) cudaStreamDestroy(G->stream);
+  }
+  delete G;
+}
+
+uint64_t cfdg_grid_device_bytes(const cfdg_grid* G) {
+  if (!G) return 0;
+  uint64_t b = G->arena.bytes;
+  if (G->ic0) b += G->ic0->arena.bytes;
+  if (G->mg) b += G->mg->arena.bytes;
+  return b;
+}
+
+int cfdg_grid_update_faces(cfdg_grid* G, const double* area, const double* distance) {
+  if (int e = check_grid(G)) return e;
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  if (area) G->h.face_area.assign(area, area + G->h.faces);
+  if (distance) G->h.face_distance.assign(distance, distance + G->h.faces);
+  if (int e = refresh_weights(G)) return e;
+  reset_chunk(G);  // captured launches hold the weights by value
+  CU(cudaStreamSynchronize(G->stream));
+  return 0;
+}
+
+int cfdg_grid_configure(cfdg_grid* G, int32_t preconditioner, int32_t precision) {
+  if (int e = check_grid(G)) return e;
+  std::lock_guard<std::mutex> lk(G->mu);
+  if (preconditioner != CFDG_PRECOND_IC0 && preconditioner != CFDG_PRECOND_MULTIGRID)
+    return fail(CFDG_ERR_INVALID, "unknown preconditioner");
+  if (preconditioner != G->preconditioner) reset_chunk(G);
+  G->preconditioner = preconditioner;
+  G->precision = precision;
+  return 0;
+}
+
+int cfdg_project_device(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol, uint64_t max_iter,
+                        cfdg_poll_fn poll, void* poll_ctx, cfdg_info* info) {
+  if (int e = check_grid(G)) return e;
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  Poller P;
+  P.fn = poll;
+  P.ctx = poll_ctx;
+  return project_device(G, d_u, d_p, dt, tol, max_iter, P, info);
+}
+
+int cfdg_project(cfdg_grid* G, double* u, double* p, double dt, double tol, uint64_t max_iter, cfdg_poll_fn poll,
+                 void* poll_ctx, cfdg_info* info) {
+  if (int e = check_grid(G)) return e;
+  if (!u || !p) return fail(CFDG_ERR_INVALID, "null u or p");
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  cudaStream_t s = G->stream;
+  CU(cudaMemcpyAsync(G->u, u, G->h.faces * 8, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(G->pp, p, G->h.cells * 8, cudaMemcpyHostToDevice, s));
+  Poller P;
+  P.fn = poll;
+  P.ctx = poll_ctx;
+  if (int e = project_device(G, G->u, G->pp, dt, tol, max_iter, P, info)) return e;
+  CU(cudaMemcpyAsync(u, G->u, G->h.faces * 8, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(p, G->pp, G->h.cells * 8, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int cfdg_solve_scaled(cfdg_grid* G, const double* b, const double* roundoff_scale, double tol, uint64_t max_iter,
+                      cfdg_poll_fn poll, void* poll_ctx, double* x, cfdg_info* info) {
+  if (int e = check_grid(G)) return e;
+  if (!b || !x) return fail(CFDG_ERR_INVALID, "null b or x");
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  cudaStream_t s = G->stream;
+  CU(cudaMemcpyAsync(G->b, b, G->h.cells * 8, cudaMemcpyHostToDevice, s));
+  if (roundoff_scale) CU(cudaMemcpyAsync(G->terms, roundoff_scale, G->h.cells * 8, cudaMemcpyHostToDevice, s));
+  Poller P;
+  P.fn = poll;
+  P.ctx = poll_ctx;
+  if (int e = solve_device(G, roundoff_scale != nullptr, tol, max_iter, P, info)) return e;
+  CU(cudaMemcpyAsync(x, G->x, G->h.cells * 8, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int cfdg_apply(cfdg_grid* G, const double* x, double* y) {
+  if (int e = check_grid(G)) return e;
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  cudaStream_t s = G->stream;
+  CU(cudaMemcpyAsync(G->p, x, G->h.cells * 8, cudaMemcpyHostToDevice, s));
+  launch_apply(G, G->p, G->ap);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(y, G->ap, G->h.cells * 8, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int cfdg_center_nullspaces(cfdg_grid* G, double* x) {
+  if (int e = check_grid(G)) return e;
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  cudaStream_t s = G->stream;
+  CU(cudaMemcpyAsync(G->z, x, G->h.cells * 8, cudaMemcpyHostToDevice, s));
+  launch_center(G, G->comp_groups, G->ncomp_groups, G->z, nullptr);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(x, G->z, G->h.cells * 8, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int cfdg_multigrid_stats_json(cfdg_grid* G, char* buf, size_t cap) {
+  if (int e = check_grid(G)) return e;
+  std::lock_guard<std::mutex> lk(G->stats_mu);
+  if (G->stats_json.empty()) return CFDG_PENDING;
+  if (!buf || cap <= G->stats_json.size()) return fail(CFDG_ERR_INVALID, "buffer too small");
+  std::memcpy(buf, G->stats_json.c_str(), G->stats_json.size() + 1);
+  return 0;
+}
+
+int cfdg_debug_precondition(cfdg_grid* G, const double* r, double* z) {
+  if (int e = check_grid(G)) return e;
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  Poller P;
+  if (int e = prepare_preconditioner(G, P, nullptr)) return e;
+  cudaStream_t s = G->stream;
+  CU(cudaMemcpyAsync(G->r, r, G->h.cells * 8, cudaMemcpyHostToDevice, s));
+  if (G->preconditioner == CFDG_PRECOND_MULTIGRID) launch_vcycle(G, G->r, G->z, nullptr);
+  else launch_sweep_ic0(G, nullptr);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(z, G->z, G->h.cells * 8, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int cfdg_debug_projection_rhs(cfdg_grid* G, const double* u, double dt, double* b, double* terms) {
+  if (int e = check_grid(G)) return e;
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  cudaStream_t s = G->stream;
+  CU(cudaMemcpyAsync(G->u, u, G->h.faces * 8, cudaMemcpyHostToDevice, s));
+  k_projection_rhs<<<grid_blocks(G->h.cells), BLOCK, 0, s>>>(G->g, G->d_fluid, G->u, dt, G->b, G->terms,
+                                                             (int)G->h.cells);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(b, G->b, G->h.cells * 8, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(terms, G->terms, G->h.cells * 8, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+}  // extern "C"

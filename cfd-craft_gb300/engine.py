@@ -1,0 +1,118 @@
+"""ctypes binding of libcfdgpu.so (include/cfdgpu.h).
+
+The library is the only compute path: if it is missing or no CUDA device is
+usable, the calls raise; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libcfdgpu.so")
+
+CFDG_OK = 0
+CFDG_E031, CFDG_E032, CFDG_E033, CFDG_E034, CFDG_E035, CFDG_E036 = 31, 32, 33, 34, 35, 36
+CFDG_CANCELLED, CFDG_WALL_TIME = 100, 101
+CFDG_ERR_CUDA, CFDG_ERR_ADMISSION, CFDG_ERR_TIMEOUT, CFDG_ERR_INVALID, CFDG_ERR_UNSUPPORTED = 200, 201, 202, 203, 204
+CFDG_PENDING = 3
+PRECOND = {"ic0": 0, "multigrid": 1}
+PRECISION = {"plain": 0, "mixed": 1}
+
+# Every symbol include/cfdgpu.h declares.
+EXPORTS = (
+    "cfdg_context_create", "cfdg_context_destroy", "cfdg_grid_open", "cfdg_grid_close",
+    "cfdg_grid_update_faces", "cfdg_grid_configure", "cfdg_project", "cfdg_solve_scaled", "cfdg_apply",
+    "cfdg_center_nullspaces", "cfdg_multigrid_stats_json", "cfdg_last_error", "cfdg_project_device",
+    "cfdg_grid_device_bytes", "cfdg_debug_precondition", "cfdg_debug_projection_rhs",
+)
+
+
+class GridDesc(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32 * 3),
+        ("dx", C.c_double * 3),
+        ("volume", C.c_double),
+        ("periodic", C.c_int32 * 3),
+        ("n_faces", C.c_int64),
+        ("fluid", C.c_void_p),
+        ("face_kind", C.c_void_p),
+        ("face_lo", C.c_void_p),
+        ("face_hi", C.c_void_p),
+        ("face_area", C.c_void_p),
+        ("face_distance", C.c_void_p),
+        ("component", C.c_void_p),
+        ("n_components", C.c_int32),
+        ("anchored", C.c_void_p),
+        ("preconditioner", C.c_int32),
+        ("precision", C.c_int32),
+    ]
+
+
+class Info(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_uint64),
+        ("relative_residual", C.c_double),
+        ("work_units", C.c_uint64),
+        ("operator_applications", C.c_uint64),
+        ("preconditioner_applications", C.c_uint64),
+        ("true_residual_checks", C.c_uint64),
+        ("hierarchy_builds", C.c_uint64),
+        ("hierarchy_levels", C.c_uint64),
+        ("hierarchy_cells", C.c_uint64),
+        ("hierarchy_nonzeros", C.c_uint64),
+        ("cycles", C.c_uint64),
+        ("smoothing_cell_updates", C.c_uint64),
+        ("residual_cell_updates", C.c_uint64),
+        ("restriction_cell_updates", C.c_uint64),
+        ("prolongation_cell_updates", C.c_uint64),
+        ("coarse_solves", C.c_uint64),
+        ("refinement_steps", C.c_uint64),
+        ("device_seconds", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+POLL = C.CFUNCTYPE(C.c_int, C.c_void_p)
+_lock = threading.Lock()
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads libcfdgpu.so and declares its signatures. Raises if it was not built."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise RuntimeError(f"the CUDA engine library is missing ({path}); run __graft_entry__.build()")
+        L = C.CDLL(path)
+        P = C.c_void_p
+        L.cfdg_last_error.restype = C.c_char_p
+        L.cfdg_context_create.argtypes = [C.c_int, C.c_uint64, C.POINTER(C.c_void_p)]
+        L.cfdg_context_destroy.argtypes = [P]
+        L.cfdg_context_destroy.restype = None
+        L.cfdg_grid_open.argtypes = [P, C.POINTER(GridDesc), C.POINTER(C.c_void_p)]
+        L.cfdg_grid_close.argtypes = [P]
+        L.cfdg_grid_close.restype = None
+        L.cfdg_grid_update_faces.argtypes = [P, P, P]
+        L.cfdg_grid_configure.argtypes = [P, C.c_int32, C.c_int32]
+        L.cfdg_project.argtypes = [P, P, P, C.c_double, C.c_double, C.c_uint64, POLL, P, C.POINTER(Info)]
+        L.cfdg_project_device.argtypes = [P, P, P, C.c_double, C.c_double, C.c_uint64, POLL, P, C.POINTER(Info)]
+        L.cfdg_solve_scaled.argtypes = [P, P, P, C.c_double, C.c_uint64, POLL, P, P, C.POINTER(Info)]
+        L.cfdg_apply.argtypes = [P, P, P]
+        L.cfdg_center_nullspaces.argtypes = [P, P]
+        L.cfdg_multigrid_stats_json.argtypes = [P, C.c_char_p, C.c_size_t]
+        L.cfdg_grid_device_bytes.argtypes = [P]
+        L.cfdg_grid_device_bytes.restype = C.c_uint64
+        L.cfdg_debug_precondition.argtypes = [P, P, P]
+        L.cfdg_debug_projection_rhs.argtypes = [P, P, C.c_double, P, P]
+        _lib = L
+        return L
+
+
+def last_error() -> str:
+    return load().cfdg_last_error().decode()

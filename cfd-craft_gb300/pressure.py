@@ -1,0 +1,268 @@
+"""The pressure API of crates/cfd-craft/src/pressure.rs, served by the GB300 engine.
+
+Same names, argument meanings and error behaviour as the reference:
+
+    project(grid, u, p, dt, tol, max, control)        -> LinearInfo   (pressure.rs:469)
+    solve_scaled(grid, b, scale, tol, max, control)   -> (x, LinearInfo) (pressure.rs:342)
+    solve(grid, b, tol, max, control)                 -> (x, LinearInfo) (pressure.rs:329)
+    apply(grid, x)                                    -> y            (pressure.rs:293)
+    center_nullspaces(grid, x)                        (in place)      (pressure.rs:316)
+    multigrid_stats(grid)                             -> dict | None  (pressure.rs:100)
+
+Errors raise ``PressureError`` whose message is the reference's string
+("CFD-E031: ...", "cancelled", ...); on error ``u`` and ``p`` are unchanged.
+``grid`` is a :class:`grid.Grid`; its device state (topology, IC(0) factor,
+multigrid hierarchy) is opened on first use and cached on the grid object, the
+way the reference caches ``Grid::pressure_factor`` and the multigrid hierarchy.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import threading
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import engine as E
+
+
+class PressureError(RuntimeError):
+    """A failed pressure solve; ``code`` is the engine's return code."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+@dataclass
+class LinearInfo:
+    """pressure.rs:30-36, plus the profile work counters of the solve."""
+
+    iterations: int = 0
+    relative_residual: float = 0.0
+    work: dict = None
+
+
+class Control:
+    """solver::Control (solver.rs:75-188): cooperative cancellation and a wall-time limit.
+
+    ``poll`` is an optional callable; raising or returning a string stops the solve
+    as "cancelled" (or "wall_time_limit" when that is the text)."""
+
+    def __init__(self, seconds: float = 1e9, poll=None):
+        self.start = time.monotonic()
+        self.limit = seconds
+        self.cancelled = threading.Event()
+        self.poll = poll
+        self.polls = 0
+
+    def check(self) -> int:
+        self.polls += 1
+        if self.poll is not None:
+            try:
+                r = self.poll()
+            except Exception as e:  # an external poll error stops as cancelled
+                r = str(e) or "cancelled"
+            if r:
+                return E.CFDG_WALL_TIME if r == "wall_time_limit" else E.CFDG_CANCELLED
+        if self.cancelled.is_set():
+            return E.CFDG_CANCELLED
+        if time.monotonic() - self.start >= self.limit:
+            return E.CFDG_WALL_TIME
+        return 0
+
+
+class Context:
+    """One CUDA device with an HBM budget (cfdg_context)."""
+
+    _default = None
+    _lock = threading.Lock()
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        L = E.load()
+        h = C.c_void_p()
+        rc = L.cfdg_context_create(device, hbm_budget_bytes, C.byref(h))
+        if rc:
+            raise PressureError(rc, E.last_error())
+        self.h = h
+        self.device = device
+
+    @classmethod
+    def default(cls) -> "Context":
+        with cls._lock:
+            if cls._default is None:
+                cls._default = Context()
+            return cls._default
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and E._lib is not None:
+            E._lib.cfdg_context_destroy(h)
+            self.h = None
+
+
+def _vp(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class DeviceGrid:
+    """A grid opened on the engine (cfdg_grid): topology and caches resident in HBM."""
+
+    def __init__(self, grid, ctx: Context = None, preconditioner: str = None, precision: str = "plain"):
+        self.ctx = ctx or Context.default()
+        L = E.load()
+        self.grid = grid
+        self._keep = dict(
+            fluid=np.ascontiguousarray(grid.fluid, np.uint8),
+            kind=np.ascontiguousarray(grid.face_kind, np.uint8),
+            lo=np.ascontiguousarray(grid.face_lo, np.int64),
+            hi=np.ascontiguousarray(grid.face_hi, np.int64),
+            area=np.ascontiguousarray(grid.face_area, np.float64),
+            dist=np.ascontiguousarray(grid.face_distance, np.float64),
+            comp=np.ascontiguousarray(grid.component, np.int32),
+            anch=np.ascontiguousarray(grid.anchored, np.uint8),
+        )
+        k = self._keep
+        d = E.GridDesc()
+        for a in range(3):
+            d.n[a] = grid.n[a]
+            d.dx[a] = grid.dx[a]
+            d.periodic[a] = 1 if grid.periodic[a] else 0
+        d.volume = grid.volume
+        d.n_faces = grid.n_faces
+        d.fluid, d.face_kind, d.face_lo, d.face_hi = _vp(k["fluid"]), _vp(k["kind"]), _vp(k["lo"]), _vp(k["hi"])
+        d.face_area, d.face_distance = _vp(k["area"]), _vp(k["dist"])
+        d.component, d.n_components = _vp(k["comp"]), grid.n_components
+        d.anchored = _vp(k["anch"]) if grid.n_components else None
+        d.preconditioner = E.PRECOND[preconditioner or grid.preconditioner]
+        d.precision = E.PRECISION[precision]
+        h = C.c_void_p()
+        rc = L.cfdg_grid_open(self.ctx.h, C.byref(d), C.byref(h))
+        if rc:
+            raise PressureError(rc, E.last_error())
+        self.h = h
+        self.L = L
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cfdg_grid_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def configure(self, preconditioner: str, precision: str = "plain"):
+        self._check(self.L.cfdg_grid_configure(self.h, E.PRECOND[preconditioner], E.PRECISION[precision]))
+
+    def update_faces(self, area=None, distance=None):
+        a = None if area is None else np.ascontiguousarray(area, np.float64)
+        d = None if distance is None else np.ascontiguousarray(distance, np.float64)
+        self._check(self.L.cfdg_grid_update_faces(self.h, None if a is None else _vp(a), None if d is None else _vp(d)))
+
+    def device_bytes(self) -> int:
+        return int(self.L.cfdg_grid_device_bytes(self.h))
+
+    def _check(self, rc):
+        if rc:
+            raise PressureError(rc, E.last_error())
+
+    @staticmethod
+    def _poll_fn(control):
+        if control is None:
+            return E.POLL(0)
+
+        def cb(_ctx):
+            c = control.check()
+            return 0 if c == 0 else (2 if c == E.CFDG_WALL_TIME else 1)
+
+        return E.POLL(cb)
+
+    def project(self, u, p, dt, tol, max_iter, control=None) -> LinearInfo:
+        assert u.dtype == np.float64 and u.flags.c_contiguous and u.size == self.grid.n_faces
+        assert p.dtype == np.float64 and p.flags.c_contiguous and p.size == self.grid.count
+        info = E.Info()
+        cb = self._poll_fn(control)
+        rc = self.L.cfdg_project(self.h, _vp(u), _vp(p), float(dt), float(tol), int(max_iter), cb, None,
+                                 C.byref(info))
+        self._check(rc)
+        return LinearInfo(info.iterations, info.relative_residual, info.as_dict())
+
+    def solve_scaled(self, b, scale, tol, max_iter, control=None):
+        b = np.ascontiguousarray(b, np.float64)
+        s = None if scale is None else np.ascontiguousarray(scale, np.float64)
+        x = np.zeros(self.grid.count)
+        info = E.Info()
+        cb = self._poll_fn(control)
+        rc = self.L.cfdg_solve_scaled(self.h, _vp(b), None if s is None else _vp(s), float(tol), int(max_iter), cb,
+                                      None, _vp(x), C.byref(info))
+        self._check(rc)
+        return x, LinearInfo(info.iterations, info.relative_residual, info.as_dict())
+
+    def apply(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.empty(self.grid.count)
+        self._check(self.L.cfdg_apply(self.h, _vp(x), _vp(y)))
+        return y
+
+    def center_nullspaces(self, x):
+        assert x.dtype == np.float64 and x.flags.c_contiguous
+        self._check(self.L.cfdg_center_nullspaces(self.h, _vp(x)))
+
+    def precondition(self, r):
+        r = np.ascontiguousarray(r, np.float64)
+        z = np.empty(self.grid.count)
+        self._check(self.L.cfdg_debug_precondition(self.h, _vp(r), _vp(z)))
+        return z
+
+    def projection_rhs(self, u, dt):
+        u = np.ascontiguousarray(u, np.float64)
+        b = np.empty(self.grid.count)
+        t = np.empty(self.grid.count)
+        self._check(self.L.cfdg_debug_projection_rhs(self.h, _vp(u), float(dt), _vp(b), _vp(t)))
+        return b, t
+
+    def multigrid_stats(self):
+        buf = C.create_string_buffer(1 << 16)
+        rc = self.L.cfdg_multigrid_stats_json(self.h, buf, len(buf))
+        if rc == E.CFDG_PENDING:
+            return None
+        self._check(rc)
+        return json.loads(buf.value.decode())
+
+
+def device_grid(grid) -> DeviceGrid:
+    """The grid's engine handle, opened on first use (like Grid::pressure_factor's OnceLock)."""
+    dg = getattr(grid, "_device", None)
+    if dg is None:
+        dg = DeviceGrid(grid)
+        object.__setattr__(grid, "_device", dg)
+    return dg
+
+
+def project(grid, u, p, dt, tol, max_iter, control=None) -> LinearInfo:
+    return device_grid(grid).project(u, p, dt, tol, max_iter, control)
+
+
+def solve_scaled(grid, b, roundoff_scale, tol, max_iter, control=None):
+    return device_grid(grid).solve_scaled(b, roundoff_scale, tol, max_iter, control)
+
+
+def solve(grid, b, tol, max_iter, control=None):
+    return device_grid(grid).solve_scaled(b, None, tol, max_iter, control)
+
+
+def apply(grid, x):
+    return device_grid(grid).apply(x)
+
+
+def center_nullspaces(grid, x):
+    device_grid(grid).center_nullspaces(x)
+
+
+def multigrid_stats(grid):
+    return device_grid(grid).multigrid_stats()

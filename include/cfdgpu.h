@@ -1,0 +1,196 @@
+/*
+ * cfdgpu.h — C ABI of the GB300 pressure-projection engine for CFD-craft.
+ *
+ * The engine replaces the projection step of crates/cfd-craft: the divergence
+ * right-hand side, the IC(0)- or multigrid-preconditioned CG solve and the
+ * velocity correction. The caller keeps its grid (crates/cfd-craft/src/grid.rs)
+ * and hands the engine the grid's products once; the engine keeps the topology,
+ * the IC(0) factor and the multigrid hierarchy resident in device memory.
+ *
+ * Conventions
+ *  - Every pointer argument is caller-owned HOST memory unless the function
+ *    name ends in _device, and is only read during the call (copied in/out).
+ *  - Cell index (k*ny + j)*nx + i, x fastest (grid.rs:218-220). Face arrays hold
+ *    the x-faces, then the y-faces, then the z-faces, each x fastest over its
+ *    face dimensions (grid.rs:341-429).
+ *  - Return codes map 1:1 to the reference's error strings (see CFDG_*). On any
+ *    nonzero return, the caller's u, p and x are unchanged (pressure.rs:468).
+ *  - cfdg_last_error() gives the full message ("CFD-E033: ...") of the last
+ *    failing call on the calling thread.
+ *  - Two threads may use two different grids at once. One grid is used by one
+ *    thread at a time (its calls are serialised by an internal lock).
+ *  - No CPU fallback: without a usable CUDA device every call that computes
+ *    returns CFDG_ERR_CUDA.
+ */
+#ifndef CFDGPU_H
+#define CFDGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Return codes. */
+#define CFDG_OK 0
+#define CFDG_E031 31            /* incompatible flux in a closed fluid component (pressure.rs:359) */
+#define CFDG_E032 32            /* pressure CG lost positive definiteness (pressure.rs:395) */
+#define CFDG_E033 33            /* pressure iteration limit (pressure.rs:435) */
+#define CFDG_E034 34            /* multigrid topology or weights (multigrid.rs:152,193) */
+#define CFDG_E035 35            /* coarse Cholesky / aggregation failure (multigrid.rs:490, masked.rs:42,235) */
+#define CFDG_E036 36            /* line Cholesky (multigrid/line.rs:130) */
+#define CFDG_CANCELLED 100      /* Control::check() == "cancelled" (solver.rs:122-140) */
+#define CFDG_WALL_TIME 101      /* Control::check() == "wall_time_limit" */
+#define CFDG_ERR_CUDA 200       /* CUDA error or no usable device */
+#define CFDG_ERR_ADMISSION 201  /* the grid does not fit the context's HBM budget */
+#define CFDG_ERR_TIMEOUT 202    /* a bounded device wait gave up */
+#define CFDG_ERR_INVALID 203    /* invalid argument or inconsistent grid description */
+#define CFDG_ERR_UNSUPPORTED 204/* a configuration this engine does not implement */
+#define CFDG_PENDING 3          /* cfdg_poll_result: the ticket is not finished yet */
+
+/* Face kinds (grid.rs:60-81). */
+#define CFDG_FACE_INTERIOR 0
+#define CFDG_FACE_WALL 1
+#define CFDG_FACE_SLIP 2
+#define CFDG_FACE_INLET 3
+#define CFDG_FACE_OUTLET 4
+#define CFDG_FACE_BLOCKED 5
+
+/* Preconditioners (case.rs:860-879) and arithmetic forms. */
+#define CFDG_PRECOND_IC0 0
+#define CFDG_PRECOND_MULTIGRID 1
+#define CFDG_PRECISION_PLAIN 0 /* FP64 throughout: the parity form */
+#define CFDG_PRECISION_MIXED 1 /* FP32 inner solve, FP64 dots, true residual and refinement */
+
+typedef struct cfdg_context cfdg_context;
+typedef struct cfdg_grid cfdg_grid;
+
+/* The grid's products, as crates/cfd-craft/src/grid.rs holds them (Grid, grid.rs:114-162). */
+typedef struct {
+  int32_t n[3];                 /* cells per axis */
+  double dx[3];                 /* Grid::dx */
+  double volume;                /* Grid::volume */
+  int32_t periodic[3];          /* 1 when the axis wraps (no duplicate end face) */
+  int64_t n_faces;              /* Grid::faces.len() */
+  const uint8_t *fluid;         /* [N] 1 fluid, 0 solid */
+  const uint8_t *face_kind;     /* [F] CFDG_FACE_* */
+  const int64_t *face_lo;       /* [F] fluid cell below the face, -1 for none (Face::lo) */
+  const int64_t *face_hi;       /* [F] fluid cell above the face, -1 for none (Face::hi) */
+  const double *face_area;      /* [F] Face::area, current coefficients */
+  const double *face_distance;  /* [F] Face::distance */
+  const int32_t *component;     /* [N] fluid component per cell, -1 for solid (Grid::component) */
+  int32_t n_components;         /* Grid::components.len() */
+  const uint8_t *anchored;      /* [n_components] 1 when the component touches an outlet */
+  int32_t preconditioner;       /* CFDG_PRECOND_* (numerics.pressure_preconditioner) */
+  int32_t precision;            /* CFDG_PRECISION_* */
+} cfdg_grid_desc;
+
+/* LinearInfo (pressure.rs:30-36) plus the phase-profile work counters
+ * (profiling.rs:101-138, multigrid.rs:76-114). */
+typedef struct {
+  uint64_t iterations;          /* PCG iterations; 0 for a zero right-hand side */
+  double relative_residual;     /* recomputed residual relative to |b_compatible| */
+  uint64_t work_units;
+  uint64_t operator_applications;
+  uint64_t preconditioner_applications;
+  uint64_t true_residual_checks;
+  uint64_t hierarchy_builds;
+  uint64_t hierarchy_levels;
+  uint64_t hierarchy_cells;
+  uint64_t hierarchy_nonzeros;
+  uint64_t cycles;
+  uint64_t smoothing_cell_updates;
+  uint64_t residual_cell_updates;
+  uint64_t restriction_cell_updates;
+  uint64_t prolongation_cell_updates;
+  uint64_t coarse_solves;
+  uint64_t refinement_steps;    /* outer FP64 defect-correction steps (mixed form); 0 plain */
+  double device_seconds;        /* device time of the solve, from CUDA events */
+} cfdg_info;
+
+/* Control::check (solver.rs:122-140): 0 continue, 1 "cancelled", 2 "wall_time_limit".
+ * Polled before PCG iterations 0, 8, 16, ... like pressure.rs:387-389, and before
+ * a multigrid setup (pressure.rs:69). */
+typedef int (*cfdg_poll_fn)(void *ctx);
+
+/* ------------------------------------------------------------------ lifetime */
+
+/* Creates a context on CUDA device `device`. hbm_budget_bytes bounds the device
+ * memory of all grids opened on it (0 = 90 % of the free memory at creation).
+ * Replaces: nothing in the reference (the reference has no device). */
+int cfdg_context_create(int device, uint64_t hbm_budget_bytes, cfdg_context **out);
+void cfdg_context_destroy(cfdg_context *ctx);
+
+/* Uploads a grid's topology and face coefficients. Replaces the per-grid caches
+ * Grid::pressure_factor (grid.rs:151) and Grid::pressure_multigrid (grid.rs:155):
+ * the IC(0) factor is built by the first IC(0) solve and never rebuilt (pressure.rs:62-65);
+ * the hierarchy is rebuilt when the signature changes (pressure.rs:67-95). */
+int cfdg_grid_open(cfdg_context *ctx, const cfdg_grid_desc *desc, cfdg_grid **out);
+void cfdg_grid_close(cfdg_grid *grid);
+
+/* Replaces the public face coefficients (callers may change Grid::faces[*].area
+ * and .distance, pressure.rs:244). The operator and the true residual use them on
+ * the next solve; the IC(0) factor is kept (pressure.rs:714-743); a changed weight
+ * rebuilds the multigrid hierarchy before the next solve (multigrid.rs:173-222). */
+int cfdg_grid_update_faces(cfdg_grid *grid, const double *face_area, const double *face_distance);
+
+/* Switches the preconditioner or the arithmetic form of an open grid. */
+int cfdg_grid_configure(cfdg_grid *grid, int32_t preconditioner, int32_t precision);
+
+/* ------------------------------------------------------------------ the projection */
+
+/* pressure::project (pressure.rs:469-502): solves A phi = -div(u)/dt, subtracts
+ * dt*grad(phi) from the interior and outlet faces of u[F], adds phi to p[N] and
+ * re-centres p's gauge. Called from solver.rs:721, :767 and :1437. */
+int cfdg_project(cfdg_grid *grid, double *u, double *p, double dt, double tol, uint64_t max_iter,
+                 cfdg_poll_fn poll, void *poll_ctx, cfdg_info *info);
+
+/* pressure::solve_scaled (pressure.rs:342-436): x[N] solves A x = b with the
+ * compatibility check against roundoff_scale[N] (NULL: |b|), PCG with the grid's
+ * preconditioner and the true-residual gate. pressure::solve (pressure.rs:329) is
+ * roundoff_scale == NULL. */
+int cfdg_solve_scaled(cfdg_grid *grid, const double *b, const double *roundoff_scale, double tol,
+                      uint64_t max_iter, cfdg_poll_fn poll, void *poll_ctx, double *x, cfdg_info *info);
+
+/* pressure::apply (pressure.rs:293-312): y = A x from the current faces, bitwise equal
+ * to the reference's face-order accumulation. */
+int cfdg_apply(cfdg_grid *grid, const double *x, double *y);
+
+/* pressure::center_nullspaces (pressure.rs:316-325). */
+int cfdg_center_nullspaces(cfdg_grid *grid, double *x);
+
+/* pressure::multigrid_stats (pressure.rs:100-106) as JSON:
+ * {"level_cells":[...],"level_nonzeros":[...],"allocated_bytes":B}. Returns
+ * CFDG_PENDING when no hierarchy was built yet. Safe to call from a poll callback. */
+int cfdg_multigrid_stats_json(cfdg_grid *grid, char *buf, size_t cap);
+
+/* Last error message of the calling thread ("" when none). */
+const char *cfdg_last_error(void);
+
+/* ------------------------------------------------------------------ device-resident forms */
+
+/* cfdg_project on device pointers (u: F doubles, p: N doubles), on the grid's
+ * stream. u and p are updated only on success. */
+int cfdg_project_device(cfdg_grid *grid, double *d_u, double *d_p, double dt, double tol,
+                        uint64_t max_iter, cfdg_poll_fn poll, void *poll_ctx, cfdg_info *info);
+
+/* Device memory the grid holds, in bytes (admission accounting). */
+uint64_t cfdg_grid_device_bytes(const cfdg_grid *grid);
+
+/* ------------------------------------------------------------------ diagnostic entry points
+ * Pieces of the projection exposed for parity tests; no reference counterpart is
+ * replaced by them. */
+
+/* z = M^-1 r for the grid's preconditioner (pressure.rs:43-53): IC(0) Factor::apply
+ * (pressure.rs:223-241) or one V-cycle (multigrid.rs:656-665, masked.rs:292-302). */
+int cfdg_debug_precondition(cfdg_grid *grid, const double *r, double *z);
+
+/* projection_rhs (pressure.rs:440-459): b[N], terms[N] from u[F]. */
+int cfdg_debug_projection_rhs(cfdg_grid *grid, const double *u, double dt, double *b, double *terms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CFDGPU_H */

@@ -1,0 +1,225 @@
+"""Parity of the CUDA engine (through libcfdgpu.so's C ABI) with the oracle.
+
+Bars (from the engine's specification): bitwise for the operator, the projection
+right-hand side, the IC(0) substitutions and (on anchored grids) the multigrid
+V-cycle; pressure, corrected face velocities and post-projection divergence within
+1e-10 relative of the oracle's; PCG iteration counts within +-1.
+"""
+import copy
+import math
+
+import numpy as np
+import pytest
+
+from cases import CANYON_93K, KERNEL_ITERATIONS, LID_CAVITY, kernel_case, periodic_case, sin_field
+
+pytestmark = pytest.mark.gpu
+REL = 1e-10
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float64).view(np.uint64)
+
+
+def small_cases(pkg):
+    out = {
+        "periodic-2x3x2": periodic_case([2, 3, 2]),
+        "periodic-3x1x4": periodic_case([3, 1, 4]),
+        "periodic-1x3x1": periodic_case([1, 3, 1]),
+        "masked-open": periodic_case([6, 3, 2], "open", True, True),
+        "masked-wall": periodic_case([6, 3, 2], "wall", False, True),
+        "cavity24": kernel_case("cavity24", "ic0"),
+        "canyon93k": CANYON_93K,
+        "pocket": pkg.synth.case((12, 12, 6), 1.0, boxes=[((3, 3, 0), (9, 4, 4)), ((3, 8, 0), (9, 9, 4)),
+                                                          ((3, 3, 0), (4, 9, 4)), ((8, 3, 0), (9, 9, 4)),
+                                                          ((3, 3, 3), (9, 9, 4))]),
+        "buildings": pkg.synth.case((24, 20, 12), 2.0, boxes=[((10, 6, 0), (20, 14, 10)), ((30, 20, 0), (40, 34, 16))]),
+    }
+    c = periodic_case([18, 9, 33], "open", True)
+    c["domain"]["size_m"] = [7.15, 42.45, 38.31]
+    out["unequal-spacing"] = c
+    return out
+
+
+def open_pair(pkg, O, case, pre=None):
+    g = pkg.grid.Grid.build(case)
+    og = O.Grid(case)
+    if pre:
+        og.set_preconditioner(pre)
+    dg = pkg.pressure.DeviceGrid(g, preconditioner=pre)
+    return g, og, dg
+
+
+def test_operator_bitwise(pkg, O):
+    for name, case in small_cases(pkg).items():
+        g, og, dg = open_pair(pkg, O, case)
+        x = sin_field(g.count)
+        assert np.array_equal(bits(dg.apply(x)), bits(og.apply(x))), name
+        # Changed public face coefficients (non-uniform weights path).
+        area = g.face_area * (1.0 + (np.arange(g.n_faces) % 7) * 0.025)
+        og.set_faces(area=area)
+        dg.update_faces(area=area)
+        assert np.array_equal(bits(dg.apply(x)), bits(og.apply(x))), name + " changed"
+        dg.close()
+
+
+def test_projection_rhs_bitwise(pkg, O):
+    for name, case in small_cases(pkg).items():
+        g, og, dg = open_pair(pkg, O, case)
+        u = np.array([3.0 * math.sin(0.61 * i) - 0.4 for i in range(g.n_faces)])
+        b, t = dg.projection_rhs(u, 0.125)
+        ob, ot = og.projection_rhs(u, 0.125)
+        assert np.array_equal(bits(b), bits(ob)) and np.array_equal(bits(t), bits(ot)), name
+        dg.close()
+
+
+def test_ic0_apply_bitwise(pkg, O):
+    for name, case in small_cases(pkg).items():
+        g, og, dg = open_pair(pkg, O, case, "ic0")
+        r = np.where(g.fluid == 1, sin_field(g.count, 0.7), 0.0)
+        assert np.array_equal(bits(dg.precondition(r)), bits(og.ic0_apply(r))), name
+        dg.close()
+
+
+def test_multigrid_cycle_matches(pkg, O):
+    for name, case in small_cases(pkg).items():
+        g, og, dg = open_pair(pkg, O, case, "multigrid")
+        r = og.center_nullspaces(np.where(g.fluid == 1, sin_field(g.count, 0.7), 0.0))
+        try:
+            oz, _ = og.mg_apply(r)
+        except O.OracleError as e:
+            assert e.code == O.UNSUPPORTED  # anisotropic line smoothing is not restated
+            dg.close()
+            continue
+        z = dg.precondition(r)
+        if all(g.anchored):
+            assert np.array_equal(bits(z), bits(oz)), name  # no gauge sums: bitwise
+        else:
+            assert np.max(np.abs(z - oz)) <= 1e-12 * max(1.0, np.max(np.abs(oz))), name
+        assert dg.multigrid_stats()["level_cells"] == og.mg_levels()[0], name
+        dg.close()
+
+
+def test_published_pins_on_gpu(pkg, O):
+    for name, it in KERNEL_ITERATIONS.items():
+        for k, pre in enumerate(("ic0", "multigrid")):
+            c = kernel_case(name, pre)
+            g, og, dg = open_pair(pkg, O, c, pre)
+            exact, rhs = O.manufactured_rhs(og, c)
+            x, info = dg.solve_scaled(rhs, None, 1e-11, 10000)
+            assert abs(info.iterations - it[k]) <= 1, (name, pre, info.iterations)
+            assert info.relative_residual <= 1.01e-10
+            assert math.sqrt(float(np.sum((x - exact) ** 2)) / g.count) <= 1e-8
+            dg.close()
+    g, og, dg = open_pair(pkg, O, CANYON_93K, "ic0")
+    exact, rhs = O.manufactured_rhs(og, CANYON_93K)
+    x, info = dg.solve_scaled(rhs, None, 1e-11, 10000)
+    assert abs(info.iterations - 166) <= 1
+    assert abs(info.relative_residual - 6.9540e-12) <= 0.05e-12
+    assert abs(math.sqrt(float(np.sum((x - exact) ** 2)) / g.count) - 3.1094e-12) <= 0.05e-12
+
+
+def check_projection(pkg, O, case, pre, dt=1.0, tol=1e-8, seed=0):
+    g, og, dg = open_pair(pkg, O, case, pre)
+    u = pkg.synth.random_velocity(g, seed)
+    p = np.random.default_rng(seed + 1).uniform(-1, 1, g.count) * (g.fluid == 1)
+    code, ou, op, oinfo = og.project(u, p, dt, tol, 10000)
+    assert code == 0
+    uu, pp = u.copy(), p.copy()
+    info = dg.project(uu, pp, dt, tol, 10000)
+    assert abs(info.iterations - oinfo["iterations"]) <= 1, (case["name"], pre, info.iterations, oinfo["iterations"])
+    su = max(1.0, float(np.max(np.abs(ou))))
+    sp = max(1.0, float(np.max(np.abs(op))))
+    assert np.max(np.abs(uu - ou)) <= REL * su, case["name"]
+    assert np.max(np.abs(pp - op)) <= REL * sp, case["name"]
+    div, odiv = og.divergence(uu), og.divergence(ou)
+    assert np.max(np.abs(div - odiv)) <= REL * max(1.0, float(np.max(np.abs(og.divergence(u))))), case["name"]
+    w = info.work
+    assert w["operator_applications"] == w["work_units"] + w["true_residual_checks"]
+    for k in ("work_units", "operator_applications", "preconditioner_applications", "true_residual_checks"):
+        assert abs(w[k] - oinfo[k]) <= 1, k
+    if pre == "multigrid":
+        assert w["cycles"] == w["preconditioner_applications"]
+    dg.close()
+    return info
+
+
+@pytest.mark.parametrize("pre", ["ic0", "multigrid"])
+def test_projection_parity_small(pkg, O, pre):
+    for name, case in small_cases(pkg).items():
+        if name in ("unequal-spacing",) and pre == "multigrid":
+            continue
+        check_projection(pkg, O, case, pre, dt=0.5)
+
+
+@pytest.mark.parametrize("pre", ["ic0", "multigrid"])
+def test_projection_parity_config1_full_size(pkg, O, pre):
+    """64x64x32, open x / wall y,z, U[-1,1] faces (seed 0), tol 1e-8."""
+    c = pkg.synth.config1()
+    check_projection(pkg, O, c, pre, dt=1.0, tol=1e-8)
+
+
+def test_projection_parity_buildings_multigrid(pkg, O):
+    """A masked multigrid projection at 64x64x32 with 6 seeded buildings."""
+    rng = np.random.default_rng(11)
+    c = pkg.synth.case((64, 64, 32), 2.0, inflow=5.0,
+                       boxes=pkg.synth.random_boxes(rng, 6, (128.0, 128.0, 64.0), dx=2.0), preconditioner="multigrid")
+    check_projection(pkg, O, c, "multigrid", dt=0.1, tol=1e-8, seed=3)
+
+
+def test_contract_errors_leave_state_unchanged(pkg, O):
+    c = periodic_case([8, 6, 5], "open", True)
+    g, og, dg = open_pair(pkg, O, c, "ic0")
+    rng = np.random.default_rng(5)
+    u = g.enforce_velocity(rng.uniform(-1, 1, g.n_faces))
+    p = rng.uniform(-1, 1, g.count)
+    u0, p0 = u.copy(), p.copy()
+    with pytest.raises(pkg.pressure.PressureError) as e:
+        dg.project(u, p, 0.5, 1e-12, 1)
+    assert e.value.code == 33 and str(e.value).startswith("CFD-E033")
+    assert np.array_equal(bits(u), bits(u0)) and np.array_equal(bits(p), bits(p0))
+    calls = {"n": 0}
+
+    def poll():
+        calls["n"] += 1
+        return "cancelled" if calls["n"] >= 2 else None
+
+    with pytest.raises(pkg.pressure.PressureError) as e:
+        dg.project(u, p, 0.5, 1e-12, 1000, pkg.pressure.Control(poll=poll))
+    assert e.value.code == 100 and str(e.value) == "cancelled"
+    assert np.array_equal(bits(u), bits(u0)) and np.array_equal(bits(p), bits(p0))
+    with pytest.raises(pkg.pressure.PressureError) as e:
+        dg.project(u, p, 0.5, 1e-12, 1000, pkg.pressure.Control(poll=lambda: "wall_time_limit"))
+    assert e.value.code == 101
+    dg.close()
+    # E031: an incompatible closed right-hand side.
+    c = periodic_case([6, 3, 2], "wall")
+    g, og, dg = open_pair(pkg, O, c, "ic0")
+    with pytest.raises(pkg.pressure.PressureError) as e:
+        dg.solve_scaled(np.ones(g.count), None, 1e-10, 100)
+    assert e.value.code == 31 and str(e.value).startswith("CFD-E031")
+    # A zero right-hand side: 0 iterations, x = 0.
+    x, info = dg.solve_scaled(np.zeros(g.count), None, 1e-10, 100)
+    assert info.iterations == 0 and not x.any()
+    dg.close()
+
+
+def test_changed_faces_rebuild_multigrid_and_keep_ic0(pkg, O):
+    c = periodic_case([5, 4, 3], "open", True)
+    for pre in ("ic0", "multigrid"):
+        g, og, dg = open_pair(pkg, O, c, pre)
+        exact = sin_field(g.count)
+        for changed in (False, True):
+            if changed:
+                area = g.face_area * (1.0 + (np.arange(g.n_faces) % 7) * 0.025)
+                og.set_faces(area=area)
+                dg.update_faces(area=area)
+            b = og.apply(exact)
+            x, info = dg.solve_scaled(b, None, 1e-12, 2000)
+            code, ox, oinfo = og.solve(b, 1e-12, 2000)
+            assert info.relative_residual <= 1.1e-11
+            assert np.max(np.abs(x - exact)) < 1e-10
+            assert abs(info.iterations - oinfo["iterations"]) <= 1
+            if pre == "multigrid":
+                assert info.work["hierarchy_builds"] == (1 if changed else 1)
+        dg.close()

@@ -1,0 +1,220 @@
+"""The reference's own unit-test identities, restated against the oracle.
+
+pressure.rs:528-619 dense IC(0) reference; :621-676 compact == public operator
+(bitwise); :678-712 projection RHS and round-off scale (bitwise); :714-743 changed
+face coefficients; :745-798 fused projection == composed divergence/gradient;
+tests/regressions.rs:30-56 and numerics.rs:99-171 the closed-component contract;
+masked.rs:365-408 masked Galerkin; multigrid.rs:844-923 the cycle is symmetric.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from cases import LID_CAVITY, periodic_case, sin_field
+
+
+def dense_operator(g):
+    n = g.count
+    a = np.zeros((n, n))
+    for j in range(n):
+        e = np.zeros(n)
+        e[j] = 1.0
+        a[:, j] = -g.divergence(g.gradient(e))
+    return a
+
+
+def dense_ic0(a, rhs):
+    """pressure.rs:530-563: IC(0) of the shifted dense matrix, then two substitutions."""
+    n = a.shape[0]
+    maximum = max(1.0, max(a[i, i] for i in range(n)))
+    l = np.zeros((n, n))
+    for i in range(n):
+        for j in range(i):
+            if a[i, j] != 0.0:
+                dot = sum(l[i, k] * l[j, k] for k in range(j))
+                l[i, j] = (a[i, j] - dot) / l[j, j]
+        sq = sum(l[i, j] * l[i, j] for j in range(i))
+        l[i, i] = math.sqrt(max(a[i, i] + 1e-6 * maximum - sq, 1e-12 * maximum))
+    y = np.zeros(n)
+    for i in range(n):
+        y[i] = (rhs[i] - sum(l[i, j] * y[j] for j in range(i))) / l[i, i]
+    x = np.zeros(n)
+    for i in reversed(range(n)):
+        x[i] = (y[i] - sum(l[j, i] * x[j] for j in range(i + 1, n))) / l[i, i]
+    return x
+
+
+@pytest.mark.parametrize("n", [[2, 3, 2], [3, 3, 3], [4, 2, 3], [3, 1, 4], [1, 3, 1]])
+def test_ic0_matches_dense_reference_periodic(O, n):
+    g = O.Grid(periodic_case(n))
+    r = sin_field(g.count, 0.7)
+    expected = dense_ic0(dense_operator(g), r)
+    z = g.ic0_apply(r)
+    assert np.all(np.abs(z - expected) <= 1e-10 * np.maximum(np.abs(expected), 1.0))
+
+
+@pytest.mark.parametrize("open_", [False, True])
+def test_ic0_matches_dense_reference_masked(O, open_):
+    c = periodic_case([6, 3, 2], boundary_x="open" if open_ else "wall", open_flow=open_, barrier=True)
+    g = O.Grid(c)
+    r = np.where(g.fluid == 1, np.array([math.cos(0.73 * i) for i in range(g.count)]), 0.0)
+    expected = dense_ic0(dense_operator(g), r)
+    z = g.ic0_apply(r)
+    assert np.all(np.abs(z - expected) <= 1e-10 * np.maximum(np.abs(expected), 1.0))
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_compact_operator_equals_public_operator(O, periodic):
+    c = periodic_case([6, 3, 2], boundary_x="periodic" if periodic else "open", open_flow=not periodic,
+                      barrier=True)
+    g = O.Grid(c)
+    x = sin_field(g.count)
+    assert np.array_equal(g.apply(x).view(np.uint64), g.operator_apply(x).view(np.uint64))
+
+
+@pytest.mark.parametrize("open_", [False, True])
+def test_compact_operator_bitwise_unequal_spacing(O, open_):
+    c = periodic_case([18, 9, 33], boundary_x="open" if open_ else "periodic", open_flow=open_)
+    c["domain"]["size_m"] = [7.15, 42.45, 38.31]
+    g = O.Grid(c)
+    x = sin_field(g.count)
+    assert np.array_equal(g.apply(x).view(np.uint64), g.operator_apply(x).view(np.uint64))
+
+
+def test_projection_rhs_and_roundoff_scale(O):
+    c = periodic_case([18, 9, 33])
+    c["domain"]["size_m"] = [7.15, 42.45, 38.31]
+    c["geometry"] = [{"id": "barrier", "min_m": [2.0, 0.0, 0.0], "max_m": [3.0, 20.0, 15.0]}]
+    g = O.Grid(c)
+    u = np.array([3.0 * math.sin(0.61 * i) - 0.4 for i in range(g.n_faces)])
+    dt = 0.125
+    b, terms = g.projection_rhs(u, dt)
+    div = g.divergence(u)
+    assert np.array_equal(b, -div / dt)
+    cf = g.cell_faces
+    dx = [c["domain"]["size_m"][a] / c["grid"]["cells"][a] for a in range(3)]
+    for i in range(g.count):
+        if g.fluid[i]:
+            s = -0.0
+            for a in range(3):
+                lo, hi = cf[i, 2 * a], cf[i, 2 * a + 1]
+                s += (abs(u[lo]) + abs(u[hi])) / dx[a]
+            expected = s / dt
+        else:
+            expected = 0.0
+        assert np.float64(terms[i]).view(np.uint64) == np.float64(expected).view(np.uint64)
+    assert (g.fluid == 0).any()
+
+
+def test_second_solve_uses_changed_face_coefficients(O):
+    c = periodic_case([5, 4, 3], boundary_x="open", open_flow=True)
+    g = O.Grid(c)
+    exact = sin_field(g.count)
+    for changed in (False, True):
+        if changed:
+            area = g.face_area * (1.0 + (np.arange(g.n_faces) % 7) * 0.025)
+            g.set_faces(area=area)
+        b = g.apply(exact)
+        code, x, info = g.solve(b, 1e-12, 2000)
+        assert code == 0
+        assert info["relative_residual"] <= 1.1e-11
+        assert np.max(np.abs(x - exact)) < 1e-10
+
+
+@pytest.mark.parametrize("boundary", ["periodic", "wall", "open"])
+def test_fused_projection_matches_composed(O, boundary):
+    c = periodic_case([6, 3, 2], boundary_x=boundary, open_flow=True, barrier=True)
+    g = O.Grid(c)
+    potential = sin_field(g.count, 0.37)
+    u = g.gradient(potential)
+    dt = 0.125
+    b = -g.divergence(u) / dt
+    _, terms = g.projection_rhs(u, dt)
+    code, ref_p, ref_info = g.solve_scaled(b, terms, 1e-12, 2000)
+    assert code == 0
+    ref_u = u - dt * g.gradient(ref_p)
+    ref_p = g.center_nullspaces(ref_p)
+    code, pu, pp, info = g.project(u, np.zeros(g.count), dt, 1e-12, 2000)
+    assert code == 0
+    assert info["iterations"] == ref_info["iterations"]
+    assert info["relative_residual"] == ref_info["relative_residual"]
+    assert np.array_equal(pu, ref_u)
+    assert np.array_equal(pp, ref_p)
+
+
+def test_incompatible_closed_rhs_is_e031(O):
+    c = periodic_case([6, 3, 2], boundary_x="wall")
+    g = O.Grid(c)
+    b = np.ones(g.count)
+    code, _, _ = g.solve(b, 1e-10, 100)
+    assert code == O.E031
+    # A compatible (mean-free) closed right-hand side solves (numerics.rs:149-171).
+    b = b - b.mean()
+    b[0] += 1.0
+    b[1] -= 1.0
+    code, x, info = g.solve(b, 1e-10, 1000)
+    assert code == 0 and info["iterations"] > 0
+
+
+def test_iteration_limit_and_cancel_leave_state_unchanged(O):
+    c = periodic_case([8, 6, 5], boundary_x="open", open_flow=True)
+    g = O.Grid(c)
+    rng = np.random.default_rng(5)
+    u = rng.uniform(-1, 1, g.n_faces)
+    u = g.enforce_velocity(u)
+    p = rng.uniform(-1, 1, g.count)
+    code, u2, p2, _ = g.project(u, p, 0.5, 1e-12, 1)
+    assert code == O.E033
+    calls = {"n": 0}
+
+    def poll(_):
+        calls["n"] += 1
+        return 1 if calls["n"] >= 2 else 0
+
+    code, u3, p3, _ = g.project(u, p, 0.5, 1e-12, 1000, poll)
+    assert code == O.CANCELLED
+
+
+def _dense_masked_level(O, g, level):
+    d = g.mg_masked_level(level)
+    n = d["diagonal"].size
+    a = np.diag(d["diagonal"].copy())
+    for i in range(n):
+        for k in range(d["offsets"][i], d["offsets"][i + 1]):
+            a[i, d["columns"][k]] += d["values"][k]
+    return d, a
+
+
+def test_masked_galerkin_equals_dense_product(O):
+    c = periodic_case([9, 2, 7], boundary_x="wall")
+    c["geometry"] = [{"id": "w", "min_m": [4.0, 0.0, 0.0], "max_m": [5.0, 2.0, 5.0]}]
+    c["numerics"]["pressure_preconditioner"] = "multigrid"
+    g = O.Grid(c)
+    r = np.where(g.fluid == 1, sin_field(g.count), 0.0)
+    g.mg_apply(r)
+    cells, _ = g.mg_levels()
+    assert len(cells) >= 2
+    for level in range(len(cells) - 1):
+        d, a = _dense_masked_level(O, g, level)
+        dc, ac = _dense_masked_level(O, g, level + 1)
+        P = np.zeros((a.shape[0], ac.shape[0]))
+        P[np.arange(a.shape[0]), d["parent"]] = 1.0
+        assert np.allclose(P.T @ a @ P, ac, atol=2e-11, rtol=0)
+
+
+@pytest.mark.parametrize("masked", [False, True])
+def test_multigrid_cycle_is_symmetric(O, masked):
+    c = periodic_case([12, 2, 12], boundary_x="wall")
+    if masked:
+        c["geometry"] = [{"id": "s", "min_m": [5.0, 0.0, 5.0], "max_m": [7.0, 2.0, 7.0]}]
+    c["numerics"]["pressure_preconditioner"] = "multigrid"
+    g = O.Grid(c)
+    rng = np.random.default_rng(3)
+    f = g.fluid == 1
+    r1 = g.center_nullspaces(np.where(f, rng.standard_normal(g.count), 0.0))
+    r2 = g.center_nullspaces(np.where(f, rng.standard_normal(g.count), 0.0))
+    z1, _ = g.mg_apply(r1)
+    z2, _ = g.mg_apply(r2)
+    assert abs(z1 @ r2 - r1 @ z2) <= 1e-10 * max(abs(z1 @ r2), 1.0)
+    assert z1 @ r1 > 0
