@@ -507,6 +507,8 @@ __global__ void k_weights(const double* __restrict__ area, const double* __restr
 namespace {
 
 thread_local std::string t_error;
+std::atomic<uint64_t> g_launches{0};  // kernels enqueued by this library (graph launches count their nodes)
+inline void count(uint64_t k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
 int fail(int code, const std::string& msg) {
   t_error = msg;
@@ -530,6 +532,10 @@ struct cfdg_context {
   int device = 0;
   uint64_t budget = 0;
   std::atomic<uint64_t> used{0};
+  // Grids keep their context alive: destroy() only marks it, the last grid frees it.
+  std::mutex mu;
+  int grids = 0;
+  bool destroyed = false;
 };
 
 namespace {
@@ -585,6 +591,7 @@ struct DevSchedule {
 
 struct DevIc0 {
   Arena arena;
+  ~DevIc0() { arena.release(); }
   DevCsr lower, upper;
   double* diag = nullptr;
   DevSchedule fwd, bwd;
@@ -608,6 +615,7 @@ struct DevLevel {
 
 struct DevHierarchy {
   Arena arena;
+  ~DevHierarchy() { arena.release(); }
   bool masked = false;
   int nfluid = 0;
   int* fluid_idx = nullptr;
@@ -624,7 +632,9 @@ struct cfdg_grid {
   std::string stats_json;
   HostGrid h;
   int preconditioner = 0, precision = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;  // where work is enqueued (the grid's own stream or the caller's)
+  cudaStream_t own = nullptr;     // the grid's own stream; graphs are captured on it
+  bool capturing = false;
   Arena arena;  // topology, weights, vectors, scalars
   GridDev g{};
   bool uniform = false;
@@ -645,6 +655,7 @@ struct cfdg_grid {
   std::unique_ptr<Signature> signature;
   cudaGraphExec_t chunk = nullptr;  // 8 PCG iterations
   int chunk_kind = -1;
+  size_t chunk_nodes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -658,9 +669,13 @@ void reset_chunk(cfdg_grid* G) {
   G->chunk_kind = -1;
 }
 
+inline void tick(cfdg_grid* G) {
+  if (!G->capturing) count();
+}
+
 int launch_center(cfdg_grid* G, const DevCsr& groups, int ngroups, double* x, const Scalars* S) {
   if (ngroups == 0) return 0;
-  k_center<<<ngroups, BLOCK, 0, G->stream>>>(groups.off, groups.col, x, S);
+  k_center<<<ngroups, BLOCK, 0, G->stream>>>(groups.off, groups.col, x, S); tick(G);
   return 0;
 }
 
@@ -669,12 +684,12 @@ void launch_sweep_ic0(cfdg_grid* G, const Scalars* S) {
   for (size_t l = 0; l + 1 < F.fwd.start.size(); ++l) {
     int b = F.fwd.start[l], e = F.fwd.start[l + 1];
     k_ic0_fwd<<<(e - b + BLOCK - 1) / BLOCK, BLOCK, 0, G->stream>>>(F.fwd.order, b, e, F.lower.off, F.lower.col,
-                                                                     F.lower.val, F.diag, G->r, G->z, S);
+                                                                     F.lower.val, F.diag, G->r, G->z, S); tick(G);
   }
   for (size_t l = 0; l + 1 < F.bwd.start.size(); ++l) {
     int b = F.bwd.start[l], e = F.bwd.start[l + 1];
     k_ic0_bwd<<<(e - b + BLOCK - 1) / BLOCK, BLOCK, 0, G->stream>>>(F.bwd.order, b, e, F.upper.off, F.upper.col,
-                                                                     F.upper.val, F.diag, G->z, S);
+                                                                     F.upper.val, F.diag, G->z, S); tick(G);
   }
 }
 
@@ -683,7 +698,7 @@ void launch_gs(cfdg_grid* G, DevLevel& L, bool backward, const Scalars* S) {
   for (size_t l = 0; l + 1 < sc.start.size(); ++l) {
     int b = sc.start[l], e = sc.start[l + 1];
     k_gs<<<(e - b + BLOCK - 1) / BLOCK, BLOCK, 0, G->stream>>>(sc.order, b, e, L.a.off, L.a.col, L.a.val, L.diag,
-                                                                L.rhs, L.x, S);
+                                                                L.rhs, L.x, S); tick(G);
   }
 }
 
@@ -693,41 +708,48 @@ void launch_vcycle(cfdg_grid* G, const double* r, double* z, const Scalars* S) {
   cudaStream_t s = G->stream;
   const int N = (int)G->h.cells;
   DevLevel& L0 = H.levels[0];
-  if (H.masked) k_gather<<<grid_blocks(H.nfluid), BLOCK, 0, s>>>(H.nfluid, H.fluid_idx, r, L0.rhs, S);
-  else k_copy<<<grid_blocks(N), BLOCK, 0, s>>>(L0.rhs, r, N, S);
+  if (H.masked) {
+    k_gather<<<grid_blocks(H.nfluid), BLOCK, 0, s>>>(H.nfluid, H.fluid_idx, r, L0.rhs, S);
+    tick(G);
+  }
+  else {
+    k_copy<<<grid_blocks(N), BLOCK, 0, s>>>(L0.rhs, r, N, S);
+    tick(G);
+  }
   const int nl = (int)H.levels.size();
   for (int l = 0; l < nl; ++l) {
     DevLevel& L = H.levels[l];
     launch_center(G, L.groups, L.ngroups, L.rhs, S);
-    k_fill<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.x, 0.0, L.n, S);
+    k_fill<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.x, 0.0, L.n, S); tick(G);
     if (L.terminal) {
-      if (L.nblocks > 0)
-        k_direct<<<(L.nblocks + 63) / 64, 64, 0, s>>>(L.nblocks, L.d_ioff, L.d_idx, L.d_foff, L.d_fac, L.rhs, L.x, S);
+      if (L.nblocks > 0) {
+        k_direct<<<(L.nblocks + 63) / 64, 64, 0, s>>>(L.nblocks, L.d_ioff, L.d_idx, L.d_foff, L.d_fac, L.rhs, L.x, S); tick(G);
+      }
       launch_center(G, L.groups, L.ngroups, L.x, S);
       break;
     }
     launch_gs(G, L, false, S);
     launch_gs(G, L, false, S);
     launch_center(G, L.groups, L.ngroups, L.x, S);
-    k_residual<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.n, L.a.off, L.a.col, L.a.val, L.diag, L.rhs, L.x, L.res, S);
+    k_residual<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.n, L.a.off, L.a.col, L.a.val, L.diag, L.rhs, L.x, L.res, S); tick(G);
     launch_center(G, L.groups, L.ngroups, L.res, S);
     DevLevel& C = H.levels[l + 1];
     k_restrict<<<grid_blocks(C.n), BLOCK, 0, s>>>(C.n, L.restrict_.off, L.restrict_.col, L.restrict_.val, L.res,
-                                                  C.rhs, S);
+                                                  C.rhs, S); tick(G);
   }
   for (int l = nl - 2; l >= 0; --l) {
     DevLevel& L = H.levels[l];
     DevLevel& C = H.levels[l + 1];
-    k_prolong<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.n, L.prolong.off, L.prolong.col, L.prolong.val, C.x, L.x, S);
+    k_prolong<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.n, L.prolong.off, L.prolong.col, L.prolong.val, C.x, L.x, S); tick(G);
     launch_gs(G, L, true, S);
     launch_gs(G, L, true, S);
     launch_center(G, L.groups, L.ngroups, L.x, S);
   }
   if (H.masked) {
-    k_fill<<<grid_blocks(N), BLOCK, 0, s>>>(z, 0.0, N, S);
-    k_scatter<<<grid_blocks(H.nfluid), BLOCK, 0, s>>>(H.nfluid, H.fluid_idx, L0.x, z, S);
+    k_fill<<<grid_blocks(N), BLOCK, 0, s>>>(z, 0.0, N, S); tick(G);
+    k_scatter<<<grid_blocks(H.nfluid), BLOCK, 0, s>>>(H.nfluid, H.fluid_idx, L0.x, z, S); tick(G);
   } else {
-    k_copy<<<grid_blocks(N), BLOCK, 0, s>>>(z, L0.x, N, S);
+    k_copy<<<grid_blocks(N), BLOCK, 0, s>>>(z, L0.x, N, S); tick(G);
   }
 }
 
@@ -743,12 +765,12 @@ void launch_iteration_t(cfdg_grid* G) {
   const int N = (int)G->h.cells;
   const int nb = grid_blocks(N);
   cudaStream_t s = G->stream;
-  k_pcg_op<U><<<nb, BLOCK, 0, s>>>(G->g, G->p, G->ap, N, G->partials, G->S);
-  k_pcg_xr<<<nb, BLOCK, 0, s>>>(G->x, G->r, G->p, G->ap, N, G->partials, G->S);
-  k_pcg_true<U><<<nb, BLOCK, 0, s>>>(G->g, G->x, G->bc, N, G->partials, G->S);
+  k_pcg_op<U><<<nb, BLOCK, 0, s>>>(G->g, G->p, G->ap, N, G->partials, G->S); tick(G);
+  k_pcg_xr<<<nb, BLOCK, 0, s>>>(G->x, G->r, G->p, G->ap, N, G->partials, G->S); tick(G);
+  k_pcg_true<U><<<nb, BLOCK, 0, s>>>(G->g, G->x, G->bc, N, G->partials, G->S); tick(G);
   launch_precondition(G, G->S);
-  k_pcg_rz<<<nb, BLOCK, 0, s>>>(G->r, G->z, N, G->partials, G->S, 0);
-  k_pcg_p<<<nb, BLOCK, 0, s>>>(G->p, G->z, N, G->S);
+  k_pcg_rz<<<nb, BLOCK, 0, s>>>(G->r, G->z, N, G->partials, G->S, 0); tick(G);
+  k_pcg_p<<<nb, BLOCK, 0, s>>>(G->p, G->z, N, G->S); tick(G);
 }
 void launch_iteration(cfdg_grid* G) {
   if (G->uniform) launch_iteration_t<true>(G);
@@ -758,7 +780,7 @@ void launch_iteration(cfdg_grid* G) {
 template <bool U>
 void launch_apply_t(cfdg_grid* G, const double* x, double* y) {
   const int N = (int)G->h.cells;
-  k_apply<U><<<grid_blocks(N), BLOCK, 0, G->stream>>>(G->g, x, y, N);
+  k_apply<U><<<grid_blocks(N), BLOCK, 0, G->stream>>>(G->g, x, y, N); tick(G);
 }
 void launch_apply(cfdg_grid* G, const double* x, double* y) {
   if (G->uniform) launch_apply_t<true>(G, x, y);
@@ -770,7 +792,7 @@ int refresh_weights(cfdg_grid* G) {
   HostGrid& h = G->h;
   CU(cudaMemcpyAsync(G->d_area, h.face_area.data(), h.faces * 8, cudaMemcpyHostToDevice, G->stream));
   CU(cudaMemcpyAsync(G->d_dist, h.face_distance.data(), h.faces * 8, cudaMemcpyHostToDevice, G->stream));
-  k_weights<<<grid_blocks(h.faces), BLOCK, 0, G->stream>>>(G->d_area, G->d_dist, h.volume, G->d_fw, h.faces);
+  k_weights<<<grid_blocks(h.faces), BLOCK, 0, G->stream>>>(G->d_area, G->d_dist, h.volume, G->d_fw, h.faces); tick(G);
   bool uniform = true;
   uint64_t win[3] = {0, 0, 0}, wout[3] = {0, 0, 0};
   bool hin[3] = {false, false, false}, hout[3] = {false, false, false};
@@ -921,9 +943,19 @@ int ensure_chunk(cfdg_grid* G) {
   if (G->chunk && G->chunk_kind == kind) return 0;
   reset_chunk(G);
   cudaGraph_t graph;
-  CU(cudaStreamBeginCapture(G->stream, cudaStreamCaptureModeThreadLocal));
-  for (int i = 0; i < CHUNK; ++i) launch_iteration(G);
-  CU(cudaStreamEndCapture(G->stream, &graph));
+  cudaStream_t user = G->stream;
+  CU(cudaStreamSynchronize(user));
+  G->stream = G->own;
+  G->capturing = true;
+  cudaError_t ce = cudaStreamBeginCapture(G->stream, cudaStreamCaptureModeThreadLocal);
+  if (ce == cudaSuccess) {
+    for (int i = 0; i < CHUNK; ++i) launch_iteration(G);
+    ce = cudaStreamEndCapture(G->stream, &graph);
+  }
+  G->stream = user;
+  G->capturing = false;
+  if (ce != cudaSuccess) return fail(CFDG_ERR_CUDA, std::string("CUDA capture: ") + cudaGetErrorString(ce));
+  cudaGraphGetNodes(graph, nullptr, &G->chunk_nodes);
   cudaError_t e = cudaGraphInstantiate(&G->chunk, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return fail(CFDG_ERR_CUDA, std::string("CUDA graph: ") + cudaGetErrorString(e));
@@ -948,23 +980,25 @@ int solve_device(cfdg_grid* G, bool use_terms, double tol, uint64_t max_iter, co
   CU(cudaMemcpyAsync(G->S, &init, sizeof(Scalars), cudaMemcpyHostToDevice, s));
   CU(cudaEventRecord(G->ev0, s));
   // Compatibility of closed components (pressure.rs:351-362).
-  if (G->ncomp_groups)
+  if (G->ncomp_groups) {
     k_compat<<<G->ncomp_groups, BLOCK, 0, s>>>(G->comp_groups.off, G->comp_groups.col, G->b, G->terms,
                                                use_terms ? 1 : 0, G->S);
+    tick(G);
+  }
   CU(cudaMemcpyAsync(G->hS, G->S, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
   if (G->hS->done == 2) return fail(CFDG_E031, "CFD-E031: incompatible flux in a closed fluid component");
   if (int e = prepare_preconditioner(G, poll, inf)) return e;
   if (int e = ensure_chunk(G)) return e;
   // Prologue: x = 0, r = centred b, norm, z = M^-1 r, p = z, rz = r.z.
-  k_fill<<<nb, BLOCK, 0, s>>>(G->x, 0.0, N, nullptr);
-  k_copy<<<nb, BLOCK, 0, s>>>(G->r, G->b, N, nullptr);
+  k_fill<<<nb, BLOCK, 0, s>>>(G->x, 0.0, N, nullptr); tick(G);
+  k_copy<<<nb, BLOCK, 0, s>>>(G->r, G->b, N, nullptr); tick(G);
   launch_center(G, G->comp_groups, G->ncomp_groups, G->r, nullptr);
-  k_copy<<<nb, BLOCK, 0, s>>>(G->bc, G->r, N, nullptr);
-  k_pcg_norm<<<nb, BLOCK, 0, s>>>(G->r, N, G->partials, G->S);
+  k_copy<<<nb, BLOCK, 0, s>>>(G->bc, G->r, N, nullptr); tick(G);
+  k_pcg_norm<<<nb, BLOCK, 0, s>>>(G->r, N, G->partials, G->S); tick(G);
   launch_precondition(G, G->S);
-  k_copy<<<nb, BLOCK, 0, s>>>(G->p, G->z, N, G->S);
-  k_pcg_rz<<<nb, BLOCK, 0, s>>>(G->r, G->z, N, G->partials, G->S, 1);
+  k_copy<<<nb, BLOCK, 0, s>>>(G->p, G->z, N, G->S); tick(G);
+  k_pcg_rz<<<nb, BLOCK, 0, s>>>(G->r, G->z, N, G->partials, G->S, 1); tick(G);
   CU(cudaGetLastError());
   int status = 0;
   for (;;) {
@@ -991,6 +1025,7 @@ int solve_device(cfdg_grid* G, bool use_terms, double tol, uint64_t max_iter, co
     }
     if (int c = poll.check()) return poll_code(c);
     CU(cudaGraphLaunch(G->chunk, s));
+    count(G->chunk_nodes);
   }
   if (G->preconditioner == CFDG_PRECOND_MULTIGRID && G->mg) {
     uint64_t cyc = inf->preconditioner_applications;
@@ -1004,7 +1039,10 @@ int solve_device(cfdg_grid* G, bool use_terms, double tol, uint64_t max_iter, co
     inf->coarse_solves = cyc;
   }
   if (status == 0 && G->hS->done == 1) launch_center(G, G->comp_groups, G->ncomp_groups, G->x, nullptr);
-  if (status == 0 && G->hS->done == 4) k_fill<<<nb, BLOCK, 0, s>>>(G->x, 0.0, N, nullptr);
+  if (status == 0 && G->hS->done == 4) {
+    k_fill<<<nb, BLOCK, 0, s>>>(G->x, 0.0, N, nullptr);
+    tick(G);
+  }
   CU(cudaEventRecord(G->ev1, s));
   CU(cudaEventSynchronize(G->ev1));
   float ms = 0;
@@ -1017,11 +1055,11 @@ int project_device(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol
                    const Poller& poll, cfdg_info* info) {
   const int N = (int)G->h.cells;
   cudaStream_t s = G->stream;
-  k_projection_rhs<<<grid_blocks(N), BLOCK, 0, s>>>(G->g, G->d_fluid, d_u, dt, G->b, G->terms, N);
+  k_projection_rhs<<<grid_blocks(N), BLOCK, 0, s>>>(G->g, G->d_fluid, d_u, dt, G->b, G->terms, N); tick(G);
   if (int e = solve_device(G, true, tol, max_iter, poll, info)) return e;
   k_correct_faces<<<grid_blocks(G->h.faces), BLOCK, 0, s>>>(G->d_kind, G->d_lo, G->d_hi, G->d_dist, G->x, dt, d_u,
-                                                            G->h.faces, G->S);
-  k_add<<<grid_blocks(N), BLOCK, 0, s>>>(d_p, G->x, N, G->S);
+                                                            G->h.faces, G->S); tick(G);
+  k_add<<<grid_blocks(N), BLOCK, 0, s>>>(d_p, G->x, N, G->S); tick(G);
   launch_center(G, G->comp_groups, G->ncomp_groups, d_p, nullptr);
   CU(cudaGetLastError());
   CU(cudaStreamSynchronize(s));
@@ -1057,7 +1095,16 @@ int cfdg_context_create(int device, uint64_t hbm_budget_bytes, cfdg_context** ou
   return 0;
 }
 
-void cfdg_context_destroy(cfdg_context* ctx) { delete ctx; }
+void cfdg_context_destroy(cfdg_context* ctx) {
+  if (!ctx) return;
+  bool free_now;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->destroyed = true;
+    free_now = ctx->grids == 0;
+  }
+  if (free_now) delete ctx;
+}
 
 int cfdg_grid_open(cfdg_context* ctx, const cfdg_grid_desc* d, cfdg_grid** out) {
   if (!ctx || !d || !out) return fail(CFDG_ERR_INVALID, "null argument");
@@ -1096,7 +1143,8 @@ int cfdg_grid_open(cfdg_context* ctx, const cfdg_grid_desc* d, cfdg_grid** out) 
   G->precision = d->precision;
   if (G->preconditioner != CFDG_PRECOND_IC0 && G->preconditioner != CFDG_PRECOND_MULTIGRID)
     return fail(CFDG_ERR_INVALID, "unknown preconditioner");
-  CU(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
+  CU(cudaStreamCreateWithFlags(&G->own, cudaStreamNonBlocking));
+  G->stream = G->own;
   CU(cudaEventCreate(&G->ev0));
   CU(cudaEventCreate(&G->ev1));
   Arena& A = G->arena;
@@ -1162,26 +1210,39 @@ int cfdg_grid_open(cfdg_context* ctx, const cfdg_grid_desc* d, cfdg_grid** out) 
   g.fw = G->d_fw;
   if ((e = refresh_weights(G.get()))) return e;
   CU(cudaStreamSynchronize(s));
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->grids += 1;
+  }
   *out = G.release();
   return 0;
 }
 
 void cfdg_grid_close(cfdg_grid* G) {
   if (!G) return;
+  cfdg_context* ctx = G->ctx;
   {
     std::lock_guard<std::mutex> lk(G->mu);
     cudaSetDevice(G->ctx->device);
     reset_chunk(G);
     if (G->stream) cudaStreamSynchronize(G->stream);
+    if (G->own) cudaStreamSynchronize(G->own);
     if (G->ic0) G->ic0->arena.release();
     if (G->mg) G->mg->arena.release();
     G->arena.release();
     if (G->hS) cudaFreeHost(G->hS);
     if (G->ev0) cudaEventDestroy(G->ev0);
     if (G->ev1) cudaEventDestroy(G->ev1);
-    if (G->stream) cudaStreamDestroy(G->stream);
+    if (G->own) cudaStreamDestroy(G->own);
   }
   delete G;
+  bool free_ctx;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->grids -= 1;
+    free_ctx = ctx->destroyed && ctx->grids == 0;
+  }
+  if (free_ctx) delete ctx;
 }
 
 uint64_t cfdg_grid_device_bytes(const cfdg_grid* G) {
@@ -1314,6 +1375,70 @@ int cfdg_debug_precondition(cfdg_grid* G, const double* r, double* z) {
   return 0;
 }
 
+int cfdg_grid_set_stream(cfdg_grid* G, void* stream) {
+  if (int e = check_grid(G)) return e;
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  CU(cudaStreamSynchronize(G->stream));
+  G->stream = stream ? (cudaStream_t)stream : G->own;
+  return 0;
+}
+
+uint64_t cfdg_launch_count(void) { return g_launches.load(); }
+
+int cfdg_debug_time_kernel(cfdg_grid* G, int32_t which, int32_t reps, double* ms_per_launch,
+                           double* algorithmic_bytes) {
+  if (int e = check_grid(G)) return e;
+  if (reps < 1) return fail(CFDG_ERR_INVALID, "reps must be positive");
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  Poller P;
+  const double N = (double)G->h.cells;
+  double nfluid = 0;
+  for (auto v : G->h.fluid) nfluid += v;
+  double bytes = 0;
+  auto run = [&]() {
+    switch (which) {
+      case 0:
+        launch_apply(G, G->p, G->ap);
+        break;
+      case 1:
+        launch_gs(G, G->mg->levels[0], false, nullptr);
+        break;
+      case 2:
+        launch_sweep_ic0(G, nullptr);
+        break;
+      default:
+        launch_vcycle(G, G->r, G->z, nullptr);
+        break;
+    }
+  };
+  if (which == 0) {
+    bytes = 18.0 * N;  // read x, read the u16 face flags, write y
+  } else if (which == 1 || which == 3) {
+    if (G->preconditioner != CFDG_PRECOND_MULTIGRID) return fail(CFDG_ERR_INVALID, "needs the multigrid preconditioner");
+    if (int e = prepare_preconditioner(G, P, nullptr)) return e;
+    bytes = which == 1 ? 25.0 * nfluid : 151.0 * nfluid;  // per-unit figures of the algorithm
+  } else {
+    if (G->preconditioner != CFDG_PRECOND_IC0) return fail(CFDG_ERR_INVALID, "needs the IC(0) preconditioner");
+    if (int e = prepare_preconditioner(G, P, nullptr)) return e;
+    bytes = 58.0 * N;  // forward 25 N + backward 33 N
+  }
+  k_fill<<<grid_blocks(G->h.cells), BLOCK, 0, G->stream>>>(G->p, 1.0, (int)G->h.cells, nullptr); tick(G);
+  k_fill<<<grid_blocks(G->h.cells), BLOCK, 0, G->stream>>>(G->r, 1.0, (int)G->h.cells, nullptr); tick(G);
+  run();
+  run();
+  CU(cudaEventRecord(G->ev0, G->stream));
+  for (int i = 0; i < reps; ++i) run();
+  CU(cudaEventRecord(G->ev1, G->stream));
+  CU(cudaEventSynchronize(G->ev1));
+  float ms = 0;
+  CU(cudaEventElapsedTime(&ms, G->ev0, G->ev1));
+  if (ms_per_launch) *ms_per_launch = ms / reps;
+  if (algorithmic_bytes) *algorithmic_bytes = bytes;
+  return 0;
+}
+
 int cfdg_debug_projection_rhs(cfdg_grid* G, const double* u, double dt, double* b, double* terms) {
   if (int e = check_grid(G)) return e;
   std::lock_guard<std::mutex> lk(G->mu);
@@ -1321,7 +1446,7 @@ int cfdg_debug_projection_rhs(cfdg_grid* G, const double* u, double dt, double* 
   cudaStream_t s = G->stream;
   CU(cudaMemcpyAsync(G->u, u, G->h.faces * 8, cudaMemcpyHostToDevice, s));
   k_projection_rhs<<<grid_blocks(G->h.cells), BLOCK, 0, s>>>(G->g, G->d_fluid, G->u, dt, G->b, G->terms,
-                                                             (int)G->h.cells);
+                                                             (int)G->h.cells); tick(G);
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(b, G->b, G->h.cells * 8, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(terms, G->terms, G->h.cells * 8, cudaMemcpyDeviceToHost, s));

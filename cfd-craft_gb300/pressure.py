@@ -17,10 +17,12 @@ way the reference caches ``Grid::pressure_factor`` and the multigrid hierarchy.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import json
 import threading
 import time
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -96,15 +98,31 @@ class Context:
                 cls._default = Context()
             return cls._default
 
-    def __del__(self):
+    def close(self):
         h = getattr(self, "h", None)
         if h and E._lib is not None:
             E._lib.cfdg_context_destroy(h)
-            self.h = None
+        self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 def _vp(a):
     return a.ctypes.data_as(C.c_void_p)
+
+
+_open_grids = weakref.WeakSet()
+
+
+@atexit.register
+def _close_all():
+    # Release device state before the interpreter (and then the CUDA runtime) shut down.
+    for dg in list(_open_grids):
+        dg.close()
+    if Context._default is not None:
+        Context._default.close()
+        Context._default = None
 
 
 class DeviceGrid:
@@ -144,6 +162,7 @@ class DeviceGrid:
             raise PressureError(rc, E.last_error())
         self.h = h
         self.L = L
+        _open_grids.add(self)
 
     def close(self):
         if getattr(self, "h", None):
@@ -166,6 +185,25 @@ class DeviceGrid:
 
     def device_bytes(self) -> int:
         return int(self.L.cfdg_grid_device_bytes(self.h))
+
+    def set_stream(self, stream_handle: int):
+        """Enqueue on a caller's CUDA stream (an integer cudaStream_t; 0 = the grid's own)."""
+        self._check(self.L.cfdg_grid_set_stream(self.h, C.c_void_p(stream_handle or None)))
+
+    def project_device(self, u_ptr: int, p_ptr: int, dt, tol, max_iter, control=None) -> LinearInfo:
+        """project() on device arrays (u: F doubles, p: N doubles) given as raw pointers."""
+        info = E.Info()
+        cb = self._poll_fn(control)
+        rc = self.L.cfdg_project_device(self.h, C.c_void_p(u_ptr), C.c_void_p(p_ptr), float(dt), float(tol),
+                                        int(max_iter), cb, None, C.byref(info))
+        self._check(rc)
+        return LinearInfo(info.iterations, info.relative_residual, info.as_dict())
+
+    def time_kernel(self, which: int, reps: int = 20):
+        """(ms per launch, algorithmic bytes) of one unit of work; see cfdg_debug_time_kernel."""
+        ms, b = C.c_double(), C.c_double()
+        self._check(self.L.cfdg_debug_time_kernel(self.h, which, reps, C.byref(ms), C.byref(b)))
+        return ms.value, b.value
 
     def _check(self, rc):
         if rc:

@@ -178,6 +178,10 @@ int cfdg_project_device(cfdg_grid *grid, double *d_u, double *d_p, double dt, do
 /* Device memory the grid holds, in bytes (admission accounting). */
 uint64_t cfdg_grid_device_bytes(const cfdg_grid *grid);
 
+/* Enqueues the grid's work on `stream` (a cudaStream_t; NULL: the grid's own stream),
+ * so a caller can order it with its own kernels and time it with its own events. */
+int cfdg_grid_set_stream(cfdg_grid *grid, void *stream);
+
 /* ------------------------------------------------------------------ diagnostic entry points
  * Pieces of the projection exposed for parity tests; no reference counterpart is
  * replaced by them. */
@@ -188,6 +192,17 @@ int cfdg_debug_precondition(cfdg_grid *grid, const double *r, double *z);
 
 /* projection_rhs (pressure.rs:440-459): b[N], terms[N] from u[F]. */
 int cfdg_debug_projection_rhs(cfdg_grid *grid, const double *u, double dt, double *b, double *terms);
+
+/* Number of kernels this library has enqueued since it was loaded (a CUDA-graph
+ * launch counts its kernel nodes). */
+uint64_t cfdg_launch_count(void);
+
+/* Times one unit of work `reps` times on the grid's stream with CUDA events:
+ * which = 0 the operator y = A x, 1 one fine-level Gauss-Seidel sweep, 2 one IC(0)
+ * application (forward + backward), 3 one V-cycle. Reports the mean duration and the
+ * unit's algorithmic bytes (each logical array read or written once). */
+int cfdg_debug_time_kernel(cfdg_grid *grid, int32_t which, int32_t reps, double *ms_per_launch,
+                           double *algorithmic_bytes);
 
 #ifdef __cplusplus
 }
