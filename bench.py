@@ -219,7 +219,10 @@ def run_engine(args):
     g = pkg.grid.Grid.build(case)
     ctx = pkg.pressure.Context(device=local)
     dg = pkg.pressure.DeviceGrid(g, ctx, preconditioner="multigrid", precision=args.form)
-    stream = torch.cuda.current_stream(dev)
+    # One real stream for torch's helpers, the engine and the events (the legacy default
+    # stream's handle is NULL, which would leave the engine on its own stream).
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     dg.set_stream(stream.cuda_stream)
     K, W = args.steps, args.warmup
     u0 = pkg.synth.random_velocity(g, seed=rank)
