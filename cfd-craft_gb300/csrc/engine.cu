@@ -239,6 +239,54 @@ __global__ void k_pcg_true(GridDev g, const double* __restrict__ x, const double
   }
 }
 
+// Relative residual |A x - b| / |b| with its per-block partial sums in a caller-free
+// scratch array (see cfdg_residual_norm_noalloc). Block k sums cells
+// [k*NOALLOC_CHUNK, (k+1)*NOALLOC_CHUNK); the last block to finish adds the partials in
+// block order and writes the quotient to out[0].
+constexpr int NOALLOC_CHUNK = 2048;
+constexpr int NOALLOC_MAX_BLOCKS = 8192;  // at most NOALLOC_MAX_BLOCKS * NOALLOC_CHUNK cells
+template <bool UNIFORM>
+__global__ void k_residual_norm_noalloc(GridDev g, const double* __restrict__ x, const double* __restrict__ b, int N,
+                                        double* scratch, double* __restrict__ out) {
+  __shared__ double sh[32];
+  unsigned* counter = reinterpret_cast<unsigned*>(scratch + 2 * NOALLOC_MAX_BLOCKS);
+  const int lo = blockIdx.x * NOALLOC_CHUNK;
+  const int hi = min(N, lo + NOALLOC_CHUNK);
+  double rr = 0.0, bb = 0.0;
+  for (int c = lo + threadIdx.x; c < hi; c += blockDim.x) {
+    int q0, q1, q2;
+    cell_coords(g, c, q0, q1, q2);
+    unsigned fl = g.flags[c];
+    double v = fl ? op_cell<UNIFORM>(g, x, c, q0, q1, q2, fl) : 0.0;
+    double d = v - b[c];
+    rr += d * d;
+    bb += b[c] * b[c];
+  }
+  double s1 = block_sum(rr, sh);
+  double s2 = block_sum(bb, sh);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    scratch[blockIdx.x] = s1;
+    scratch[NOALLOC_MAX_BLOCKS + blockIdx.x] = s2;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double a1 = 0.0, a2 = 0.0;
+  for (unsigned k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
+    a1 += __ldcg(&scratch[k]);
+    a2 += __ldcg(&scratch[NOALLOC_MAX_BLOCKS + k]);
+  }
+  double t1 = block_sum(a1, sh);
+  double t2 = block_sum(a2, sh);
+  if (threadIdx.x == 0) {
+    out[0] = sqrt(t1) / sqrt(t2);
+    *counter = 0;
+  }
+}
+
 // rz' = r.z, beta = rz'/rz, it += 1 (pressure.rs:428-433). init: the first rz.
 __global__ void k_pcg_rz(const double* __restrict__ r, const double* __restrict__ z, int N, double* partials,
                          Scalars* S, int init) {
@@ -1073,6 +1121,33 @@ int check_grid(cfdg_grid* G) {
 
 }  // namespace
 
+// ------------------------------------------------------------------ no-allocation residual
+// Scratch of cfdg_residual_norm_noalloc: 2 * NOALLOC_MAX_BLOCKS partial sums and the
+// last-block counter, 128 KiB + 256 B of static device memory that every GPU loading
+// this library holds until the process exits. All calls share it.
+static __device__ __align__(256) double g_noalloc_scratch[2 * NOALLOC_MAX_BLOCKS + 32];
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[64] = {nullptr};  // device address of g_noalloc_scratch, per device
+
+// Once per device, with that device current: the device address of the scratch array.
+// In host code the symbol names a host-side stand-in, never a device address.
+int noalloc_scratch(int device, double** out) {
+  if (device < 0 || device >= 64) return fail(CFDG_ERR_INVALID, "device index out of range");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return fail(CFDG_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+    g_noalloc_ptr[device] = (double*)ptr;
+  }
+  *out = g_noalloc_ptr[device];
+  return 0;
+}
+}  // namespace
+
 // ============================================================== C ABI
 
 extern "C" {
@@ -1372,6 +1447,29 @@ int cfdg_debug_precondition(cfdg_grid* G, const double* r, double* z) {
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(z, G->z, G->h.cells * 8, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int cfdg_residual_norm_noalloc(cfdg_grid* G, const double* d_x, const double* d_b, double* d_out, void* stream) {
+  if (int e = check_grid(G)) return e;
+  if (!d_x || !d_b || !d_out) return fail(CFDG_ERR_INVALID, "null device pointer");
+  const int64_t N = G->h.cells;
+  if (N > (int64_t)NOALLOC_MAX_BLOCKS * NOALLOC_CHUNK)
+    return fail(CFDG_ERR_INVALID, "cfdg_residual_norm_noalloc: the grid has " + std::to_string(N) +
+                                      " cells; the no-allocation scratch covers at most " +
+                                      std::to_string((int64_t)NOALLOC_MAX_BLOCKS * NOALLOC_CHUNK));
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  double* scratch = nullptr;
+  if (int e = noalloc_scratch(G->ctx->device, &scratch)) return e;
+  cudaStream_t s = stream ? (cudaStream_t)stream : G->stream;
+  // The counter must start at zero; the partial sums are all rewritten by each call.
+  CU(cudaMemsetAsync(scratch + 2 * NOALLOC_MAX_BLOCKS, 0, sizeof(unsigned), s));
+  const int nb = (int)((N + NOALLOC_CHUNK - 1) / NOALLOC_CHUNK);
+  if (G->uniform) k_residual_norm_noalloc<true><<<nb, BLOCK, 0, s>>>(G->g, d_x, d_b, (int)N, scratch, d_out);
+  else k_residual_norm_noalloc<false><<<nb, BLOCK, 0, s>>>(G->g, d_x, d_b, (int)N, scratch, d_out);
+  count();
+  CU(cudaGetLastError());
   return 0;
 }
 

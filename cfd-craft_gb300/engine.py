@@ -26,7 +26,7 @@ EXPORTS = (
     "cfdg_grid_update_faces", "cfdg_grid_configure", "cfdg_project", "cfdg_solve_scaled", "cfdg_apply",
     "cfdg_center_nullspaces", "cfdg_multigrid_stats_json", "cfdg_last_error", "cfdg_project_device",
     "cfdg_grid_device_bytes", "cfdg_debug_precondition", "cfdg_debug_projection_rhs", "cfdg_grid_set_stream",
-    "cfdg_launch_count", "cfdg_debug_time_kernel",
+    "cfdg_launch_count", "cfdg_debug_time_kernel", "cfdg_residual_norm_noalloc",
 )
 
 
@@ -114,6 +114,7 @@ def load(path: str = LIB_PATH):
         L.cfdg_grid_set_stream.argtypes = [P, P]
         L.cfdg_launch_count.argtypes = []
         L.cfdg_launch_count.restype = C.c_uint64
+        L.cfdg_residual_norm_noalloc.argtypes = [P, P, P, P, P]
         L.cfdg_debug_time_kernel.argtypes = [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib = L
         return L

@@ -178,6 +178,20 @@ int cfdg_project_device(cfdg_grid *grid, double *d_u, double *d_p, double dt, do
 /* Device memory the grid holds, in bytes (admission accounting). */
 uint64_t cfdg_grid_device_bytes(const cfdg_grid *grid);
 
+/* No reference counterpart: an addition for callers that cannot allocate device memory.
+ * Writes |A x - b| / |b| (the relative residual of the solve's acceptance gate,
+ * pressure.rs:403-415) for device vectors x[N], b[N] of an open grid to d_out[0], on
+ * `stream` (NULL: the grid's stream), without waiting for it. Some callers cannot call
+ * cudaMalloc: a host that has handed the whole HBM budget to resident serving state, a
+ * step that must not block on the implicit device synchronisation an allocation can
+ * cause, or code running where an allocation failure cannot be handled. This entry
+ * point allocates nothing: its per-block partial sums live in a static device array of
+ * 128 KiB + 256 B that every GPU loading the library holds until exit, which limits it
+ * to grids of at most 16,777,216 cells (larger grids return CFDG_ERR_INVALID). The
+ * first call on a device looks up that array's address, so make it before any stream
+ * capture. All calls share the array: calls that overlap on the GPU race. */
+int cfdg_residual_norm_noalloc(cfdg_grid *grid, const double *d_x, const double *d_b, double *d_out, void *stream);
+
 /* Enqueues the grid's work on `stream` (a cudaStream_t; NULL: the grid's own stream),
  * so a caller can order it with its own kernels and time it with its own events. */
 int cfdg_grid_set_stream(cfdg_grid *grid, void *stream);
