@@ -28,6 +28,7 @@
 #include "../../include/cfdgpu.h"
 #include "plain_kernels.cuh"
 #include "setup.hpp"
+#include "wave.cuh"
 
 using namespace cfdg;
 
@@ -436,6 +437,39 @@ __global__ void k_residual(int n, const int* __restrict__ off, const int* __rest
   }
 }
 
+// Level-0 residual on the structured grid: res = rhs - (diag x + sum over the row's
+// faces in order x-lo, x-hi, y-lo, y-hi, z-lo, z-hi of (-w) x_nbr) (multigrid.rs:263-271).
+template <bool UNIFORM>
+__global__ void k_residual_struct(GridDev g, const double* __restrict__ diag, const double* __restrict__ rhs,
+                                  const double* __restrict__ x, double* __restrict__ res, int N, const Scalars* S) {
+  if (S && S->done) return;
+  const int stride[3] = {1, g.n[0], g.n[0] * g.n[1]};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+    const unsigned fl = g.flags[c];
+    double v = diag[c] * x[c];
+    if (fl & 0x3fu) {
+      int q[3];
+      cell_coords(g, c, q[0], q[1], q[2]);
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+          if (!(fl & (1u << (2 * a + side)))) continue;
+          double w;
+          if (UNIFORM) {
+            w = g.w_in[a];
+          } else {
+            int p[3] = {q[0], q[1], q[2]};
+            p[a] += side;
+            w = g.fw[face_index(g, a, p[0], p[1], p[2])];
+          }
+          v = v - w * x[side ? c + stride[a] : c - stride[a]];
+        }
+    }
+    res[c] = rhs[c] - v;
+  }
+}
+
 // Coarse rhs = P^T res, per coarse row over its children in ascending order
 // (multigrid.rs:696-701, masked.rs:325-328).
 __global__ void k_restrict(int nc, const int* __restrict__ off, const int* __restrict__ child,
@@ -642,6 +676,7 @@ struct DevIc0 {
   ~DevIc0() { arena.release(); }
   DevCsr lower, upper;
   double* diag = nullptr;
+  double *lx = nullptr, *ly = nullptr, *lz = nullptr;  // structured grids: per-cell lower coefficients
   DevSchedule fwd, bwd;
 };
 
@@ -665,6 +700,7 @@ struct DevHierarchy {
   Arena arena;
   ~DevHierarchy() { arena.release(); }
   bool masked = false;
+  bool full0 = false;  // level 0 kept in full-grid layout and swept by the wavefront kernel
   int nfluid = 0;
   int* fluid_idx = nullptr;
   std::vector<DevLevel> levels;
@@ -705,6 +741,10 @@ struct cfdg_grid {
   int chunk_kind = -1;
   size_t chunk_nodes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool structured = false;  // no periodic axis: pipelined wavefront sweeps on the fine level
+  int tiles_j = 0, tiles_k = 0;
+  int* wave_sync = nullptr;  // ticket, abort, per-tile progress of one sweep
+  int* wave_err = nullptr;   // set when a wavefront wait gave up
 };
 
 namespace {
@@ -727,8 +767,46 @@ int launch_center(cfdg_grid* G, const DevCsr& groups, int ngroups, double* x, co
   return 0;
 }
 
+WaveArgs wave_args(cfdg_grid* G, const Scalars* S) {
+  WaveArgs A{};
+  for (int a = 0; a < 3; ++a) {
+    A.n[a] = G->h.n[a];
+    A.w_in[a] = G->g.w_in[a];
+    A.face_off[a] = G->g.face_off[a];
+    for (int d = 0; d < 3; ++d) A.fdim[a][d] = G->g.fdim[a][d];
+  }
+  A.tiles_j = G->tiles_j;
+  A.tiles_k = G->tiles_k;
+  A.flags = G->d_flags;
+  A.uniform = G->uniform ? 1 : 0;
+  A.fw = G->d_fw;
+  A.sync = G->wave_sync;
+  A.error = G->wave_err;
+  A.S = S;
+  return A;
+}
+
+template <int MODE>
+void launch_wave(cfdg_grid* G, const WaveArgs& A) {
+  cudaMemsetAsync(G->wave_sync, 0, sizeof(int) * (2 + G->tiles_j * G->tiles_k), G->stream);
+  k_wave<MODE><<<G->tiles_j * G->tiles_k, WTJ * WTK, 0, G->stream>>>(A);
+  tick(G);
+}
+
 void launch_sweep_ic0(cfdg_grid* G, const Scalars* S) {
   DevIc0& F = *G->ic0;
+  if (G->structured) {
+    WaveArgs A = wave_args(G, S);
+    A.diag = F.diag;
+    A.lx = F.lx;
+    A.ly = F.ly;
+    A.lz = F.lz;
+    A.in = G->r;
+    A.x = G->z;
+    launch_wave<IC0_FWD>(G, A);
+    launch_wave<IC0_BWD>(G, A);
+    return;
+  }
   for (size_t l = 0; l + 1 < F.fwd.start.size(); ++l) {
     int b = F.fwd.start[l], e = F.fwd.start[l + 1];
     k_ic0_fwd<<<(e - b + BLOCK - 1) / BLOCK, BLOCK, 0, G->stream>>>(F.fwd.order, b, e, F.lower.off, F.lower.col,
@@ -741,7 +819,16 @@ void launch_sweep_ic0(cfdg_grid* G, const Scalars* S) {
   }
 }
 
-void launch_gs(cfdg_grid* G, DevLevel& L, bool backward, const Scalars* S) {
+void launch_gs(cfdg_grid* G, DevLevel& L, bool backward, const Scalars* S, bool full = false) {
+  if (full) {
+    WaveArgs A = wave_args(G, S);
+    A.diag = L.diag;
+    A.in = L.rhs;
+    A.x = L.x;
+    if (backward) launch_wave<GS_BWD>(G, A);
+    else launch_wave<GS_FWD>(G, A);
+    return;
+  }
   const DevSchedule& sc = backward ? L.bwd : L.fwd;
   for (size_t l = 0; l + 1 < sc.start.size(); ++l) {
     int b = sc.start[l], e = sc.start[l + 1];
@@ -756,17 +843,17 @@ void launch_vcycle(cfdg_grid* G, const double* r, double* z, const Scalars* S) {
   cudaStream_t s = G->stream;
   const int N = (int)G->h.cells;
   DevLevel& L0 = H.levels[0];
-  if (H.masked) {
+  if (H.masked && !H.full0) {
     k_gather<<<grid_blocks(H.nfluid), BLOCK, 0, s>>>(H.nfluid, H.fluid_idx, r, L0.rhs, S);
     tick(G);
-  }
-  else {
+  } else {
     k_copy<<<grid_blocks(N), BLOCK, 0, s>>>(L0.rhs, r, N, S);
     tick(G);
   }
   const int nl = (int)H.levels.size();
   for (int l = 0; l < nl; ++l) {
     DevLevel& L = H.levels[l];
+    const bool full = l == 0 && H.full0;
     launch_center(G, L.groups, L.ngroups, L.rhs, S);
     k_fill<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.x, 0.0, L.n, S); tick(G);
     if (L.terminal) {
@@ -776,10 +863,16 @@ void launch_vcycle(cfdg_grid* G, const double* r, double* z, const Scalars* S) {
       launch_center(G, L.groups, L.ngroups, L.x, S);
       break;
     }
-    launch_gs(G, L, false, S);
-    launch_gs(G, L, false, S);
+    launch_gs(G, L, false, S, full);
+    launch_gs(G, L, false, S, full);
     launch_center(G, L.groups, L.ngroups, L.x, S);
-    k_residual<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.n, L.a.off, L.a.col, L.a.val, L.diag, L.rhs, L.x, L.res, S); tick(G);
+    if (full) {
+      if (G->uniform) k_residual_struct<true><<<grid_blocks(L.n), BLOCK, 0, s>>>(G->g, L.diag, L.rhs, L.x, L.res, L.n, S);
+      else k_residual_struct<false><<<grid_blocks(L.n), BLOCK, 0, s>>>(G->g, L.diag, L.rhs, L.x, L.res, L.n, S);
+      tick(G);
+    } else {
+      k_residual<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.n, L.a.off, L.a.col, L.a.val, L.diag, L.rhs, L.x, L.res, S); tick(G);
+    }
     launch_center(G, L.groups, L.ngroups, L.res, S);
     DevLevel& C = H.levels[l + 1];
     k_restrict<<<grid_blocks(C.n), BLOCK, 0, s>>>(C.n, L.restrict_.off, L.restrict_.col, L.restrict_.val, L.res,
@@ -788,12 +881,13 @@ void launch_vcycle(cfdg_grid* G, const double* r, double* z, const Scalars* S) {
   for (int l = nl - 2; l >= 0; --l) {
     DevLevel& L = H.levels[l];
     DevLevel& C = H.levels[l + 1];
+    const bool full = l == 0 && H.full0;
     k_prolong<<<grid_blocks(L.n), BLOCK, 0, s>>>(L.n, L.prolong.off, L.prolong.col, L.prolong.val, C.x, L.x, S); tick(G);
-    launch_gs(G, L, true, S);
-    launch_gs(G, L, true, S);
+    launch_gs(G, L, true, S, full);
+    launch_gs(G, L, true, S, full);
     launch_center(G, L.groups, L.ngroups, L.x, S);
   }
-  if (H.masked) {
+  if (H.masked && !H.full0) {
     k_fill<<<grid_blocks(N), BLOCK, 0, s>>>(z, 0.0, N, S); tick(G);
     k_scatter<<<grid_blocks(H.nfluid), BLOCK, 0, s>>>(H.nfluid, H.fluid_idx, L0.x, z, S); tick(G);
   } else {
@@ -884,6 +978,22 @@ int build_ic0_dev(cfdg_grid* G) {
   if (int e = D->arena.upload(&D->bwd.order, F.bwd.order, s)) return e;
   D->fwd.start = F.fwd.start;
   D->bwd.start = F.bwd.start;
+  if (G->structured) {
+    // Each row's lower entries are its (k-1), (j-1), (i-1) neighbours (non-periodic 7-point).
+    const int64_t N = G->h.cells, nx = G->h.n[0], nxy = (int64_t)G->h.n[0] * G->h.n[1];
+    std::vector<double> lx(N, 0.0), ly(N, 0.0), lz(N, 0.0);
+    for (int64_t r = 0; r < N; ++r)
+      for (int32_t k = F.lower.off[r]; k < F.lower.off[r + 1]; ++k) {
+        int64_t c = F.lower.col[k];
+        if (c == r - 1) lx[r] = F.lower.val[k];
+        else if (c == r - nx) ly[r] = F.lower.val[k];
+        else if (c == r - nxy) lz[r] = F.lower.val[k];
+        else return fail(CFDG_ERR_INVALID, "IC(0) factor is not a 7-point lower pattern");
+      }
+    if (int e = D->arena.upload(&D->lx, lx, s)) return e;
+    if (int e = D->arena.upload(&D->ly, ly, s)) return e;
+    if (int e = D->arena.upload(&D->lz, lz, s)) return e;
+  }
   CU(cudaStreamSynchronize(s));
   G->ic0 = std::move(D);
   return 0;
@@ -916,6 +1026,36 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
   if (H.masked)
     if (int e = D->arena.upload(&D->fluid_idx, H.fluid_indices, s)) return e;
   D->levels.resize(H.levels.size());
+  D->full0 = G->structured && H.levels.size() > 1;
+  if (D->full0) {
+    // Re-index level 0 from compact fluid numbering to full-grid cells.
+    MgLevel& M = H.levels[0];
+    const int32_t N = (int32_t)G->h.cells;
+    std::vector<int32_t> full(M.n);
+    for (int32_t j = 0; j < M.n; ++j) full[j] = H.masked ? H.fluid_indices[j] : j;
+    std::vector<double> diag(N, 0.0);
+    for (int32_t j = 0; j < M.n; ++j) diag[full[j]] = M.diag[j];
+    M.diag = std::move(diag);
+    for (auto& m : M.groups.col) m = full[m];
+    for (auto& m : M.restrict.col) m = full[m];
+    Csr P;
+    P.off.assign(N + 1, 0);
+    for (int32_t j = 0; j < M.n; ++j) P.off[full[j] + 1] = M.prolong.off[j + 1] - M.prolong.off[j];
+    for (int32_t c = 0; c < N; ++c) P.off[c + 1] += P.off[c];
+    P.col.resize(M.prolong.col.size());
+    P.val.resize(M.prolong.val.size());
+    for (int32_t j = 0; j < M.n; ++j)
+      for (int32_t k = 0; k < M.prolong.off[j + 1] - M.prolong.off[j]; ++k) {
+        P.col[P.off[full[j]] + k] = M.prolong.col[M.prolong.off[j] + k];
+        P.val[P.off[full[j]] + k] = M.prolong.val[M.prolong.off[j] + k];
+      }
+    M.prolong = std::move(P);
+    M.n = N;
+    M.a = Csr();  // the wavefront kernel reads the grid's faces
+    M.a.off.assign(1, 0);
+    M.fwd = Schedule();
+    M.bwd = Schedule();
+  }
   for (size_t l = 0; l < H.levels.size(); ++l) {
     MgLevel& M = H.levels[l];
     DevLevel& L = D->levels[l];
@@ -1015,6 +1155,8 @@ int poll_code(int c) { return fail(c, c == CFDG_CANCELLED ? "cancelled" : "wall_
 
 // The PCG solve of pressure.rs:342-436 on device vectors: G->b (and G->terms when
 // use_terms) in, G->x out. Returns 0 or a CFDG code; fills info.
+int check_wave(cfdg_grid* G);
+
 int solve_device(cfdg_grid* G, bool use_terms, double tol, uint64_t max_iter, const Poller& poll, cfdg_info* info) {
   const int N = (int)G->h.cells;
   const int nb = grid_blocks(N);
@@ -1096,7 +1238,21 @@ int solve_device(cfdg_grid* G, bool use_terms, double tol, uint64_t max_iter, co
   float ms = 0;
   cudaEventElapsedTime(&ms, G->ev0, G->ev1);
   inf->device_seconds = ms * 1e-3;
+  if (int e = check_wave(G)) return e;
   return status;
+}
+
+// A wavefront wait that gave up leaves its flag set: report it once and clear it.
+int check_wave(cfdg_grid* G) {
+  int err = 0;
+  CU(cudaMemcpyAsync(&G->hS->counter, G->wave_err, sizeof(int), cudaMemcpyDeviceToHost, G->stream));
+  CU(cudaStreamSynchronize(G->stream));
+  err = (int)G->hS->counter;
+  if (err) {
+    CU(cudaMemsetAsync(G->wave_err, 0, sizeof(int), G->stream));
+    return fail(CFDG_ERR_TIMEOUT, "a wavefront sweep's bounded wait gave up; results discarded");
+  }
+  return 0;
 }
 
 int project_device(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol, uint64_t max_iter,
@@ -1283,6 +1439,11 @@ int cfdg_grid_open(cfdg_context* ctx, const cfdg_grid_desc* d, cfdg_grid** out) 
   }
   g.flags = G->d_flags;
   g.fw = G->d_fw;
+  G->structured = !h.periodic[0] && !h.periodic[1] && !h.periodic[2] && h.n[0] >= 2 && h.n[1] >= 2 && h.n[2] >= 2;
+  G->tiles_j = (h.n[1] + WTJ - 1) / WTJ;
+  G->tiles_k = (h.n[2] + WTK - 1) / WTK;
+  if ((e = A.alloc(&G->wave_sync, 2 + (size_t)G->tiles_j * G->tiles_k)) || (e = A.alloc(&G->wave_err, 1))) return e;
+  CU(cudaMemsetAsync(G->wave_err, 0, sizeof(int), s));
   if ((e = refresh_weights(G.get()))) return e;
   CU(cudaStreamSynchronize(s));
   {
@@ -1447,7 +1608,7 @@ int cfdg_debug_precondition(cfdg_grid* G, const double* r, double* z) {
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(z, G->z, G->h.cells * 8, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
-  return 0;
+  return check_wave(G);
 }
 
 int cfdg_residual_norm_noalloc(cfdg_grid* G, const double* d_x, const double* d_b, double* d_out, void* stream) {
@@ -1501,7 +1662,7 @@ int cfdg_debug_time_kernel(cfdg_grid* G, int32_t which, int32_t reps, double* ms
         launch_apply(G, G->p, G->ap);
         break;
       case 1:
-        launch_gs(G, G->mg->levels[0], false, nullptr);
+        launch_gs(G, G->mg->levels[0], false, nullptr, G->mg->full0);
         break;
       case 2:
         launch_sweep_ic0(G, nullptr);

@@ -38,6 +38,10 @@ def small_cases(pkg):
     c = periodic_case([18, 9, 33], "open", True)
     c["domain"]["size_m"] = [7.15, 42.45, 38.31]
     out["unequal-spacing"] = c
+    # Non-periodic shapes that exercise partial wavefront tiles (8x8 pencils per tile).
+    out["tiny-2x2x2"] = pkg.synth.case((2, 2, 2), 1.0)
+    out["odd-3x17x9"] = pkg.synth.case((3, 17, 9), 1.0, boundaries=("wall", "wall", "wall"))
+    out["odd-21x9x19"] = pkg.synth.case((21, 9, 19), 1.5, boxes=[((6, 3, 0), (12, 9, 9))])
     return out
 
 
