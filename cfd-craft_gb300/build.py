@@ -19,6 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # its own, like the reference (Rust does not contract a*b+c into an FMA).
 UNITS = [
     ("engine.cu", ["-fmad=false"]),
+    ("mixed.cu", []),  # FP32 inner solve: contraction allowed; its FP64 parts use explicit _rn intrinsics
     ("setup.cpp", []),
 ]
 

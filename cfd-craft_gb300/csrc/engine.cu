@@ -586,166 +586,12 @@ __global__ void k_weights(const double* __restrict__ area, const double* __restr
 
 // ============================================================== host side
 
-namespace {
-
+namespace cfdg {
 thread_local std::string t_error;
-std::atomic<uint64_t> g_launches{0};  // kernels enqueued by this library (graph launches count their nodes)
-inline void count(uint64_t k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+std::atomic<uint64_t> g_launches{0};
+}  // namespace cfdg
 
-int fail(int code, const std::string& msg) {
-  t_error = msg;
-  return code;
-}
-
-#define CU(expr)                                                                          \
-  do {                                                                                    \
-    cudaError_t e_ = (expr);                                                              \
-    if (e_ != cudaSuccess) return fail(CFDG_ERR_CUDA, std::string("CUDA: ") + #expr + ": " + cudaGetErrorString(e_)); \
-  } while (0)
-
-int grid_blocks(long long n) {
-  long long b = (n + BLOCK - 1) / BLOCK;
-  return (int)std::max(1LL, std::min<long long>(b, MAX_BLOCKS));
-}
-
-}  // namespace
-
-struct cfdg_context {
-  int device = 0;
-  uint64_t budget = 0;
-  std::atomic<uint64_t> used{0};
-  // Grids keep their context alive: destroy() only marks it, the last grid frees it.
-  std::mutex mu;
-  int grids = 0;
-  bool destroyed = false;
-};
-
-namespace {
-
-// Device allocation owned by a grid, counted against the context's budget.
-struct Arena {
-  cfdg_context* ctx = nullptr;
-  std::vector<void*> ptrs;
-  uint64_t bytes = 0;
-  template <class T>
-  int alloc(T** p, size_t n) {
-    size_t b = std::max<size_t>(n, 1) * sizeof(T);
-    if (ctx->used.load() + b > ctx->budget) return fail(CFDG_ERR_ADMISSION, "the grid does not fit the context's HBM budget");
-    CU(cudaMalloc((void**)p, b));
-    ptrs.push_back(*p);
-    bytes += b;
-    ctx->used += b;
-    return 0;
-  }
-  template <class T>
-  int upload(T** p, const std::vector<T>& v, cudaStream_t s) {
-    if (int e = alloc(p, v.size())) return e;
-    if (!v.empty()) CU(cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
-    return 0;
-  }
-  void release() {
-    for (void* p : ptrs) cudaFree(p);
-    if (ctx) ctx->used -= bytes;
-    ptrs.clear();
-    bytes = 0;
-  }
-};
-
-struct DevCsr {
-  int* off = nullptr;
-  int* col = nullptr;
-  double* val = nullptr;
-  int rows = 0;
-};
-int upload_csr(Arena& A, const Csr& c, DevCsr& d, cudaStream_t s) {
-  d.rows = c.rows();
-  if (int e = A.upload(&d.off, c.off, s)) return e;
-  if (int e = A.upload(&d.col, c.col, s)) return e;
-  if (!c.val.empty() || c.col.empty())
-    if (int e = A.upload(&d.val, c.val, s)) return e;
-  return 0;
-}
-
-struct DevSchedule {
-  int* order = nullptr;
-  std::vector<int32_t> start;
-};
-
-struct DevIc0 {
-  Arena arena;
-  ~DevIc0() { arena.release(); }
-  DevCsr lower, upper;
-  double* diag = nullptr;
-  double *lx = nullptr, *ly = nullptr, *lz = nullptr;  // structured grids: per-cell lower coefficients
-  DevSchedule fwd, bwd;
-};
-
-struct DevLevel {
-  int n = 0;
-  DevCsr a;
-  double* diag = nullptr;
-  DevSchedule fwd, bwd;
-  DevCsr groups, prolong, restrict_;
-  int ngroups = 0;
-  bool terminal = false;
-  int nblocks = 0;
-  int* d_ioff = nullptr;
-  int* d_idx = nullptr;
-  long long* d_foff = nullptr;
-  double* d_fac = nullptr;
-  double *rhs = nullptr, *x = nullptr, *res = nullptr;
-};
-
-struct DevHierarchy {
-  Arena arena;
-  ~DevHierarchy() { arena.release(); }
-  bool masked = false;
-  bool full0 = false;  // level 0 kept in full-grid layout and swept by the wavefront kernel
-  int nfluid = 0;
-  int* fluid_idx = nullptr;
-  std::vector<DevLevel> levels;
-  std::vector<uint64_t> level_cells, level_nonzeros;
-};
-
-}  // namespace
-
-struct cfdg_grid {
-  cfdg_context* ctx = nullptr;
-  std::mutex mu;        // serialises solves on this grid
-  std::mutex stats_mu;  // guards the stats copy (readable from a poll callback)
-  std::string stats_json;
-  HostGrid h;
-  int preconditioner = 0, precision = 0;
-  cudaStream_t stream = nullptr;  // where work is enqueued (the grid's own stream or the caller's)
-  cudaStream_t own = nullptr;     // the grid's own stream; graphs are captured on it
-  bool capturing = false;
-  Arena arena;  // topology, weights, vectors, scalars
-  GridDev g{};
-  bool uniform = false;
-  uint8_t* d_fluid = nullptr;
-  uint16_t* d_flags = nullptr;
-  uint8_t* d_kind = nullptr;
-  int *d_lo = nullptr, *d_hi = nullptr;
-  double *d_area = nullptr, *d_dist = nullptr, *d_fw = nullptr;
-  DevCsr comp_groups;  // closed components of the grid
-  int ncomp_groups = 0;
-  double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *ap = nullptr, *bc = nullptr, *b = nullptr,
-         *terms = nullptr, *u = nullptr, *pp = nullptr;
-  double* partials = nullptr;
-  Scalars* S = nullptr;
-  Scalars* hS = nullptr;  // pinned mirror
-  std::unique_ptr<DevIc0> ic0;
-  std::unique_ptr<DevHierarchy> mg;
-  std::unique_ptr<Signature> signature;
-  cudaGraphExec_t chunk = nullptr;  // 8 PCG iterations
-  int chunk_kind = -1;
-  size_t chunk_nodes = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  bool structured = false;  // no periodic axis: pipelined wavefront sweeps on the fine level
-  int tiles_j = 0, tiles_k = 0;
-  int* wave_sync = nullptr;  // ticket, abort, per-tile progress of one sweep
-  int* wave_err = nullptr;   // set when a wavefront wait gave up
-};
+#include "state.hpp"
 
 namespace {
 
@@ -1088,6 +934,7 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
   D->level_cells = H.level_cells;
   D->level_nonzeros = H.level_nonzeros;
   CU(cudaStreamSynchronize(s));
+  G->host_mg = std::make_shared<Hierarchy>(std::move(H));
   {
     std::lock_guard<std::mutex> lk(G->stats_mu);
     G->stats_json = stats_json_of(*D);
@@ -1096,30 +943,36 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
   return 0;
 }
 
+int prepare_mg_impl(cfdg_grid* G, const Poller& poll, cfdg_info* info) {
+  if (int c = poll.check()) return fail(c, c == CFDG_CANCELLED ? "cancelled" : "wall_time_limit");
+  if (G->h.n_components == 0)
+    return fail(CFDG_E034, "CFD-E034: numerics.pressure_preconditioner: multigrid requires fluid cells");
+  Signature cur;
+  int se = signature_of(G->h, cur);
+  bool rebuild = !G->mg || !G->signature || se != 0 || !(cur == *G->signature);
+  if (rebuild) {
+    if (se)
+      return fail(CFDG_E034, "CFD-E034: numerics.pressure_preconditioner: multigrid requires finite positive pressure face weights");
+    G->mg.reset();
+    G->mixed.reset();
+    G->solo.reset();
+    reset_chunk(G);
+    if (int e = build_mg_dev(G, poll)) return e;
+    G->signature = std::make_unique<Signature>(std::move(cur));
+    if (info) info->hierarchy_builds = 1;
+  }
+  if (info) {
+    info->hierarchy_levels = G->mg->level_cells.size();
+    for (auto v : G->mg->level_cells) info->hierarchy_cells += v;
+    for (auto v : G->mg->level_nonzeros) info->hierarchy_nonzeros += v;
+  }
+  return 0;
+}
+
 // pressure.rs:55-97: the cached factor, or the hierarchy checked against its signature.
 int prepare_preconditioner(cfdg_grid* G, const Poller& poll, cfdg_info* info) {
-  if (G->preconditioner == CFDG_PRECOND_MULTIGRID) {
-    if (int c = poll.check()) return fail(c, c == CFDG_CANCELLED ? "cancelled" : "wall_time_limit");
-    if (G->h.n_components == 0)
-      return fail(CFDG_E034, "CFD-E034: numerics.pressure_preconditioner: multigrid requires fluid cells");
-    Signature cur;
-    int se = signature_of(G->h, cur);
-    bool rebuild = !G->mg || !G->signature || se != 0 || !(cur == *G->signature);
-    if (rebuild) {
-      if (se)
-        return fail(CFDG_E034, "CFD-E034: numerics.pressure_preconditioner: multigrid requires finite positive pressure face weights");
-      G->mg.reset();
-      reset_chunk(G);
-      if (int e = build_mg_dev(G, poll)) return e;
-      G->signature = std::make_unique<Signature>(std::move(cur));
-      if (info) info->hierarchy_builds = 1;
-    }
-    if (info) {
-      info->hierarchy_levels = G->mg->level_cells.size();
-      for (auto v : G->mg->level_cells) info->hierarchy_cells += v;
-      for (auto v : G->mg->level_nonzeros) info->hierarchy_nonzeros += v;
-    }
-  } else if (!G->ic0) {
+  if (G->preconditioner == CFDG_PRECOND_MULTIGRID) return prepare_mg_impl(G, poll, info);
+  if (!G->ic0) {
     reset_chunk(G);
     if (int e = build_ic0_dev(G)) return e;
   }
@@ -1255,8 +1108,40 @@ int check_wave(cfdg_grid* G) {
   return 0;
 }
 
+int project_mixed(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol, uint64_t max_iter,
+                  const Poller& poll, cfdg_info* info) {
+  cfdg_info local{};
+  cfdg_info* inf = info ? info : &local;
+  std::memset(inf, 0, sizeof(*inf));
+  if (int e = prepare_mg_impl(G, poll, inf)) return e;
+  if (!G->solo) {
+    cfdg_batch* B = cfdg_mixed_new(G->ctx);
+    if (!B) return fail(CFDG_ERR_CUDA, "could not create the mixed-form stream");
+    std::shared_ptr<cfdg_batch> solo(B, cfdg_mixed_delete);
+    if (int e = cfdg_mixed_add_case(B, G)) return e;
+    if (int e = cfdg_mixed_pack(B)) return e;
+    G->solo = solo;
+  }
+  cfdg_mixed_set_stream(G->solo.get(), G->stream);
+  int32_t code = 0;
+  uint64_t builds = inf->hierarchy_builds, levels = inf->hierarchy_levels, cells = inf->hierarchy_cells,
+           nnz = inf->hierarchy_nonzeros;
+  if (int e = cfdg_mixed_project(G->solo.get(), &d_u, &d_p, &dt, tol, max_iter, poll.fn, poll.ctx, inf, &code))
+    return e;
+  inf->hierarchy_builds = builds, inf->hierarchy_levels = levels, inf->hierarchy_cells = cells;
+  inf->hierarchy_nonzeros = nnz;
+  if (code == CFDG_E031) return fail(code, "CFD-E031: incompatible flux in a closed fluid component");
+  if (code == CFDG_E032) return fail(code, "CFD-E032: pressure CG lost positive definiteness");
+  if (code == CFDG_E033) return fail(code, "CFD-E033: pressure iteration limit " + std::to_string(max_iter));
+  if (code) return fail(code, "mixed-form projection failed");
+  CU(cudaStreamSynchronize(G->stream));
+  return 0;
+}
+
 int project_device(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol, uint64_t max_iter,
                    const Poller& poll, cfdg_info* info) {
+  if (G->precision == CFDG_PRECISION_MIXED && G->preconditioner == CFDG_PRECOND_MULTIGRID && G->structured)
+    return project_mixed(G, d_u, d_p, dt, tol, max_iter, poll, info);
   const int N = (int)G->h.cells;
   cudaStream_t s = G->stream;
   k_projection_rhs<<<grid_blocks(N), BLOCK, 0, s>>>(G->g, G->d_fluid, d_u, dt, G->b, G->terms, N); tick(G);
@@ -1276,6 +1161,32 @@ int check_grid(cfdg_grid* G) {
 }
 
 }  // namespace
+
+namespace cfdg {
+int prepare_multigrid(cfdg_grid* G) {
+  Poller P;
+  return prepare_mg_impl(G, P, nullptr);
+}
+
+int plain_compat_center(cfdg_grid* G, cudaStream_t s) {
+  Scalars init{};
+  CU(cudaMemcpyAsync(G->S, &init, sizeof(Scalars), cudaMemcpyHostToDevice, s));
+  k_compat<<<G->ncomp_groups, BLOCK, 0, s>>>(G->comp_groups.off, G->comp_groups.col, G->b, G->terms, 1, G->S);
+  count();
+  CU(cudaMemcpyAsync(G->hS, G->S, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  if (G->hS->done == 2) return CFDG_E031;
+  CU(cudaMemcpyAsync(G->bc, G->b, G->h.cells * 8, cudaMemcpyDeviceToDevice, s));
+  plain_center(G, G->bc, s);
+  return 0;
+}
+
+void plain_center(cfdg_grid* G, double* x, cudaStream_t s) {
+  if (G->ncomp_groups == 0) return;
+  k_center<<<G->ncomp_groups, BLOCK, 0, s>>>(G->comp_groups.off, G->comp_groups.col, x, nullptr);
+  count();
+}
+}  // namespace cfdg
 
 // ------------------------------------------------------------------ no-allocation residual
 // Scratch of cfdg_residual_norm_noalloc: 2 * NOALLOC_MAX_BLOCKS partial sums and the
@@ -1497,6 +1408,8 @@ int cfdg_grid_update_faces(cfdg_grid* G, const double* area, const double* dista
   if (distance) G->h.face_distance.assign(distance, distance + G->h.faces);
   if (int e = refresh_weights(G)) return e;
   reset_chunk(G);  // captured launches hold the weights by value
+  G->mixed.reset();
+  G->solo.reset();
   CU(cudaStreamSynchronize(G->stream));
   return 0;
 }

@@ -1,0 +1,1241 @@
+// Mixed-precision, batched form of the pressure projection.
+//
+// Per case: the FP64 projection right-hand side b and its compatible (gauge-centred)
+// part b_c, then an outer FP64 defect-correction loop. Each outer step recomputes
+// r = b_c - A x with the exact FP64 operator (the reference's face order, with
+// rounded-as-written products: the true residual of pressure.rs:403-415) and stops
+// once |r|/|b_c| <= tol; otherwise it solves A e = r/|r| approximately with an inner
+// FP32 PCG (vectors, operator and the multigrid V-cycle in FP32; dot products and
+// alpha/beta accumulated in FP64) and adds |r| e to x.
+//
+// The V(2,2) cycle keeps the reference hierarchy (multigrid.rs / masked.rs: same
+// aggregates, Galerkin coarse operators, transfers and per-component gauges) but
+// smooths with parallel orderings: red-black Gauss-Seidel on the structured fine
+// level and multicolour Gauss-Seidel (greedy colouring) on the coarse levels, colours
+// reversed on the way up so the cycle stays symmetric. The coarsest level is solved
+// in FP64 with the reference's dense Cholesky factors.
+//
+// Batching: the fine-level kernels run over a work-list of 256-cell tiles drawn from
+// all cases of the batch; all coarse levels of one case run in one thread-block
+// cluster (cluster barriers between phases), one cluster per case in one launch. A
+// per-case state machine (outer step -> inner start -> inner iterations -> outer
+// step ... -> done) lets a fixed kernel sequence serve every case, so the whole
+// iteration is captured once as a CUDA graph and replayed in chunks.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "state.hpp"
+
+namespace cg = cooperative_groups;
+
+namespace cfdg {
+namespace mx {
+
+constexpr int TILE = 256;       // fine cells per block
+constexpr int FTILE = 1024;     // faces per block (velocity correction)
+constexpr int CS = 8;           // CTAs per cluster
+constexpr int CT = 512;         // threads per cluster CTA
+constexpr int MAXL = 16;        // coarse levels per case
+constexpr int CHUNK_IT = 8;     // iterations per captured graph launch
+
+enum State : int { OUTER = 0, SCALE = 1, START = 2, RUN = 3, DONE = 4, FAIL = 5, IDLE = 6 };
+
+struct MState {
+  double norm, rz, alpha, beta, scale, true_rel, tol, inner_tol;
+  double rr;
+  int state, error, inner_it, total_it, outer, max_it, max_inner, has_e;
+  unsigned counter;
+  int pad;
+};
+
+struct FineCase {
+  int n[3];
+  int N;
+  int uniform;
+  float w32[3], wo32[3];
+  double w64[3], wo64[3];
+  long long face_off[3];
+  int fdim[3][3];
+  double dx[3];
+  long long F;
+  int tile0, ntiles;     // cell tiles of this case in the work-list
+  int ftile0, nftiles;   // face tiles
+  const uint16_t* flags;
+  const uint8_t* fluid;
+  const double* fw64;    // per-face FP64 weights (the grid's)
+  const float* fw32;     // per-face FP32 weights (non-uniform grids)
+  const float* diag0;    // level-0 diagonal (full layout), 0 for solid cells
+  // FP64 outer vectors (the grid's buffers)
+  double *x64, *r64, *bc, *b, *terms;
+  // FP32 inner vectors
+  float *e, *r32, *p, *q, *x0, *rhs0, *res0;
+  double* partials;  // ntiles doubles
+  // level-0 closed groups (full indices) for the gauge
+  int ngroups;
+  const int *goff, *gmem;
+  // transfers level 0 <-> 1
+  int n1;
+  const int *r_off, *r_child;  // level-1 rows gather level-0 children
+  const float* r_w;
+  const int *p_off, *p_col;    // level-0 rows (full layout) from level-1
+  const float* p_w;
+  float *rhs1, *x1;
+  // projection I/O for this solve
+  double* u;
+  double* pfield;
+  double dt;
+  const uint8_t* fkind;
+  const int *flo, *fhi;
+  const double* fdist;
+};
+
+struct CLev {
+  int n, terminal, ncolors, ngroups;
+  const int *off, *col;
+  const float *val, *diag;
+  const int *coff, *crows;
+  const int *goff, *gmem;
+  const int *roff, *rchild;  // restriction to the next level
+  const float* rw;
+  const int *poff, *pcol;    // prolongation from the next level
+  const float* pw;
+  float *rhs, *x, *res;
+  int nblocks;
+  const int *ioff, *idx;
+  const long long* foff;
+  const double* fac;
+};
+
+struct CCase {
+  int nl;  // levels 1 .. nl (lv[0] is level 1)
+  CLev lv[MAXL];
+  double* gpart;  // group partials, max groups * CS
+};
+
+__device__ __forceinline__ bool in_state(const MState& S, int a, int b = -1) {
+  return S.state == a || S.state == b;
+}
+
+__device__ __forceinline__ double bsum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (w == 0) {
+    s = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  }
+  return s;
+}
+
+// Per-case last-block reduction: returns true in the block that finishes the case,
+// with *out the sum of the case's partials in tile order.
+__device__ __forceinline__ bool case_reduce(double v, const FineCase& F, MState& S, int lt, double* sh, double* out) {
+  __shared__ bool last;
+  double b = bsum(v, sh);
+  if (threadIdx.x == 0) {
+    F.partials[lt] = b;
+    __threadfence();
+    last = atomicAdd(&S.counter, 1u) == (unsigned)F.ntiles - 1;
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double a = 0.0;
+  for (int k = threadIdx.x; k < F.ntiles; k += blockDim.x) a += __ldcg(&F.partials[k]);
+  double s = bsum(a, sh);
+  if (threadIdx.x == 0) {
+    S.counter = 0;
+    *out = s;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void coords(const FineCase& F, int c, int& i, int& j, int& k) {
+  i = c % F.n[0];
+  int t = c / F.n[0];
+  j = t % F.n[1];
+  k = t / F.n[1];
+}
+
+__device__ __forceinline__ long long fidx(const FineCase& F, int a, int i, int j, int k) {
+  return F.face_off[a] + ((long long)k * F.fdim[a][1] + j) * F.fdim[a][0] + i;
+}
+
+// FP32 operator y = A x at cell c: sum over interior faces of w (x_c - x_n), plus w x_c on outlets.
+__device__ __forceinline__ float op32(const FineCase& F, const float* __restrict__ x, int c, unsigned fl) {
+  if (!(fl & 0x0fffu)) return 0.0f;
+  int q[3];
+  coords(F, c, q[0], q[1], q[2]);
+  const int stride[3] = {1, F.n[0], F.n[0] * F.n[1]};
+  const float xc = x[c];
+  float y = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      const unsigned ib = 1u << (2 * a + side), ob = 1u << (6 + 2 * a + side);
+      if (!(fl & (ib | ob))) continue;
+      float w;
+      if (F.uniform) {
+        w = (fl & ib) ? F.w32[a] : F.wo32[a];
+      } else {
+        int p[3] = {q[0], q[1], q[2]};
+        p[a] += side;
+        w = F.fw32[fidx(F, a, p[0], p[1], p[2])];
+      }
+      if (fl & ib) y = fmaf(w, xc - x[side ? c + stride[a] : c - stride[a]], y);
+      else y = fmaf(w, xc, y);
+    }
+  return y;
+}
+
+// FP64 operator with every product and sum rounded as written, in the reference's
+// face order (non-periodic grid): bit-identical to pressure::apply.
+__device__ __forceinline__ double op64(const FineCase& F, const double* __restrict__ x, int c, unsigned fl) {
+  if (!(fl & 0x0fffu)) return 0.0;
+  int q[3];
+  coords(F, c, q[0], q[1], q[2]);
+  const int stride[3] = {1, F.n[0], F.n[0] * F.n[1]};
+  const double xc = x[c];
+  double y = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const unsigned lin = (fl >> (2 * a)) & 1u, uin = (fl >> (2 * a + 1)) & 1u;
+    const unsigned lout = (fl >> (6 + 2 * a)) & 1u, uout = (fl >> (7 + 2 * a)) & 1u;
+    if (!(lin | uin | lout | uout)) continue;
+    double wl, wu;
+    if (F.uniform) {
+      wl = lout ? F.wo64[a] : F.w64[a];
+      wu = uout ? F.wo64[a] : F.w64[a];
+    } else {
+      int p[3] = {q[0], q[1], q[2]};
+      wl = F.fw64[fidx(F, a, p[0], p[1], p[2])];
+      p[a] += 1;
+      wu = F.fw64[fidx(F, a, p[0], p[1], p[2])];
+    }
+    if (lin) y = __dsub_rn(y, __dmul_rn(wl, __dsub_rn(x[c - stride[a]], xc)));
+    else if (lout) y = __dadd_rn(y, __dmul_rn(wl, xc));
+    if (uin) y = __dadd_rn(y, __dmul_rn(wu, __dsub_rn(xc, x[c + stride[a]])));
+    else if (uout) y = __dadd_rn(y, __dmul_rn(wu, xc));
+  }
+  return y;
+}
+
+// ----------------------------------------------------------------- fine-level kernels
+#define FINE_PROLOGUE(STATE_TEST)                 \
+  const int2 t = tiles[blockIdx.x];               \
+  const FineCase& F = FC[t.x];                    \
+  MState& S = ST[t.x];                            \
+  if (!(STATE_TEST)) return;                      \
+  const int lt = t.y;                             \
+  const int c = lt * TILE + threadIdx.x;          \
+  const bool ok = c < F.N;
+
+// A: q = A32 p, alpha = rz / (p.q) (E032 when not positive).
+__global__ void __launch_bounds__(TILE) k_op(const FineCase* FC, MState* ST, const int2* tiles) {
+  __shared__ double sh[32];
+  FINE_PROLOGUE(S.state == RUN)
+  double acc = 0.0;
+  if (ok) {
+    float v = op32(F, F.p, c, F.flags[c]);
+    F.q[c] = v;
+    acc = (double)F.p[c] * (double)v;
+  }
+  double pq;
+  if (case_reduce(acc, F, S, lt, sh, &pq) && threadIdx.x == 0) {
+    if (!(pq > 0.0) || !isfinite(pq)) {
+      S.state = FAIL;
+      S.error = CFDG_E032;
+    } else {
+      S.alpha = S.rz / pq;
+    }
+  }
+}
+
+// B: e += alpha p, r -= alpha q; |r| decides the end of the inner solve.
+__global__ void __launch_bounds__(TILE) k_update(const FineCase* FC, MState* ST, const int2* tiles) {
+  __shared__ double sh[32];
+  FINE_PROLOGUE(S.state == RUN)
+  const float alpha = (float)S.alpha;
+  double acc = 0.0;
+  if (ok) {
+    F.e[c] = fmaf(alpha, F.p[c], F.e[c]);
+    float r = fmaf(-alpha, F.q[c], F.r32[c]);
+    F.r32[c] = r;
+    acc = (double)r * (double)r;
+  }
+  double rr;
+  if (case_reduce(acc, F, S, lt, sh, &rr) && threadIdx.x == 0) {
+    S.inner_it += 1;
+    S.total_it += 1;
+    S.has_e = 1;
+    if (sqrt(rr) <= S.inner_tol || S.inner_it >= S.max_inner || S.total_it >= S.max_it) S.state = OUTER;
+  }
+}
+
+// C1: x += |r| e; r = b_c - A x in FP64; the true residual decides convergence.
+__global__ void __launch_bounds__(TILE) k_outer(const FineCase* FC, MState* ST, const int2* tiles) {
+  __shared__ double sh[32];
+  FINE_PROLOGUE(S.state == OUTER)
+  // The update of x must be complete in every block before A x is formed: this
+  // kernel only updates x; k_outer_resid forms the residual.
+  if (ok && S.has_e) F.x64[c] = F.x64[c] + S.scale * (double)F.e[c];
+  (void)sh;
+}
+
+__global__ void __launch_bounds__(TILE) k_outer_resid(const FineCase* FC, MState* ST, const int2* tiles) {
+  __shared__ double sh[32];
+  FINE_PROLOGUE(S.state == OUTER)
+  double acc = 0.0;
+  if (ok) {
+    double v = __dsub_rn(F.bc[c], op64(F, F.x64, c, F.flags[c]));
+    F.r64[c] = v;
+    acc = v * v;
+  }
+  double rr;
+  if (case_reduce(acc, F, S, lt, sh, &rr) && threadIdx.x == 0) {
+    double nr = sqrt(rr);
+    S.true_rel = nr / S.norm;
+    if (S.true_rel <= S.tol) {
+      S.state = DONE;
+    } else if (S.total_it >= S.max_it) {
+      S.state = FAIL;
+      S.error = CFDG_E033;
+    } else {
+      S.scale = nr;
+      S.outer += 1;
+      S.state = SCALE;
+    }
+  }
+}
+
+// C2: r32 = r / |r|, e = 0.
+__global__ void __launch_bounds__(TILE) k_scale(const FineCase* FC, MState* ST, const int2* tiles) {
+  FINE_PROLOGUE(S.state == SCALE)
+  if (ok) {
+    F.r32[c] = (float)(F.r64[c] / S.scale);
+    F.e[c] = 0.0f;
+  }
+}
+
+__global__ void k_start_state(MState* ST, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && ST[i].state == SCALE) {
+    ST[i].state = START;
+    ST[i].inner_it = 0;
+  }
+}
+
+// F: rz' = r.z; START: rz = rz', p = z (beta = 0) -> RUN; RUN: beta = rz'/rz.
+__global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, const int2* tiles) {
+  __shared__ double sh[32];
+  FINE_PROLOGUE(S.state == RUN || S.state == START)
+  double acc = 0.0;
+  if (ok) acc = (double)F.r32[c] * (double)F.x0[c];
+  double rz;
+  if (case_reduce(acc, F, S, lt, sh, &rz) && threadIdx.x == 0) {
+    if (S.state == START) {
+      S.beta = 0.0;
+      S.state = RUN;
+    } else {
+      S.beta = rz / S.rz;
+    }
+    S.rz = rz;
+  }
+}
+
+// G: p = z + beta p (z is the V-cycle's level-0 solution x0).
+__global__ void __launch_bounds__(TILE) k_p(const FineCase* FC, MState* ST, const int2* tiles) {
+  FINE_PROLOGUE(S.state == RUN)
+  if (ok) F.p[c] = S.beta == 0.0 ? F.x0[c] : fmaf((float)S.beta, F.p[c], F.x0[c]);
+}
+
+// ----------------------------------------------------------------- V-cycle, level 0
+// rhs0 = r32.
+__global__ void __launch_bounds__(TILE) k_v_rhs(const FineCase* FC, MState* ST, const int2* tiles) {
+  FINE_PROLOGUE(S.state == RUN || S.state == START)
+  if (ok) F.rhs0[c] = F.r32[c];
+}
+
+// Red-black Gauss-Seidel half sweep on level 0: cells with (i+j+k)%2 == color.
+// first: x is taken as zero (the cycle's initial guess); cells outside the operator
+// (solid, sealed singletons) are kept at zero.
+__global__ void __launch_bounds__(TILE) k_rb(const FineCase* FC, MState* ST, const int2* tiles, int color, int first) {
+  FINE_PROLOGUE(S.state == RUN || S.state == START)
+  if (!ok) return;
+  int q[3];
+  coords(F, c, q[0], q[1], q[2]);
+  if (((q[0] + q[1] + q[2]) & 1) != color) return;
+  const float d = F.diag0[c];
+  if (d == 0.0f) {
+    F.x0[c] = 0.0f;
+    return;
+  }
+  const unsigned fl = F.flags[c];
+  float v = F.rhs0[c];
+  if (!(first && color == 0)) {
+    const int stride[3] = {1, F.n[0], F.n[0] * F.n[1]};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {
+        if (!(fl & (1u << (2 * a + side)))) continue;
+        float w;
+        if (F.uniform) {
+          w = F.w32[a];
+        } else {
+          int p[3] = {q[0], q[1], q[2]};
+          p[a] += side;
+          w = F.fw32[fidx(F, a, p[0], p[1], p[2])];
+        }
+        v = fmaf(w, F.x0[side ? c + stride[a] : c - stride[a]], v);
+      }
+  }
+  F.x0[c] = v / d;
+}
+
+// res0 = rhs0 - A0 x0 (A0 = diag - sum w on interior faces).
+__global__ void __launch_bounds__(TILE) k_v_resid(const FineCase* FC, MState* ST, const int2* tiles) {
+  FINE_PROLOGUE(S.state == RUN || S.state == START)
+  if (!ok) return;
+  const float d = F.diag0[c];
+  if (d == 0.0f) {
+    F.res0[c] = 0.0f;
+    return;
+  }
+  const unsigned fl = F.flags[c];
+  int q[3];
+  coords(F, c, q[0], q[1], q[2]);
+  const int stride[3] = {1, F.n[0], F.n[0] * F.n[1]};
+  float v = d * F.x0[c];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      if (!(fl & (1u << (2 * a + side)))) continue;
+      float w;
+      if (F.uniform) {
+        w = F.w32[a];
+      } else {
+        int p[3] = {q[0], q[1], q[2]};
+        p[a] += side;
+        w = F.fw32[fidx(F, a, p[0], p[1], p[2])];
+      }
+      v = fmaf(-w, F.x0[side ? c + stride[a] : c - stride[a]], v);
+    }
+  F.res0[c] = F.rhs0[c] - v;
+}
+
+// rhs1 = R res0: level-1 rows gather their level-0 children. Tiles index level-1 rows.
+__global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState* ST, const int2* tiles1) {
+  const int2 t = tiles1[blockIdx.x];
+  const FineCase& F = FC[t.x];
+  const MState& S = ST[t.x];
+  if (!(S.state == RUN || S.state == START)) return;
+  const int j = t.y * TILE + threadIdx.x;
+  if (j >= F.n1) return;
+  float v = 0.0f;
+  for (int k = F.r_off[j]; k < F.r_off[j + 1]; ++k) v = fmaf(F.r_w[k], F.res0[F.r_child[k]], v);
+  F.rhs1[j] = v;
+}
+
+// x0 += P x1.
+__global__ void __launch_bounds__(TILE) k_v_prolong(const FineCase* FC, MState* ST, const int2* tiles) {
+  FINE_PROLOGUE(S.state == RUN || S.state == START)
+  if (!ok) return;
+  const int b = F.p_off[c], e = F.p_off[c + 1];
+  if (b == e) return;
+  float s = 0.0f;
+  for (int k = b; k < e; ++k) s = fmaf(F.p_w[k], F.x1[F.p_col[k]], s);
+  F.x0[c] += s;
+}
+
+// Gauge of level-0 closed groups: one block per (case, group); members strided.
+// which: 0 rhs0, 1 x0, 2 res0.
+__global__ void k_center0(const FineCase* FC, MState* ST, const int2* gtab, int which) {
+  __shared__ double sh[32];
+  __shared__ float mean;
+  const int2 t = gtab[blockIdx.x];
+  const FineCase& F = FC[t.x];
+  const MState& S = ST[t.x];
+  if (!(S.state == RUN || S.state == START)) return;
+  float* v = which == 0 ? F.rhs0 : (which == 1 ? F.x0 : F.res0);
+  const int b = F.goff[t.y], e = F.goff[t.y + 1];
+  double acc = 0.0;
+  for (int k = b + threadIdx.x; k < e; k += blockDim.x) acc += v[F.gmem[k]];
+  double s = bsum(acc, sh);
+  if (threadIdx.x == 0) mean = (float)(s / (double)(e - b));
+  __syncthreads();
+  for (int k = b + threadIdx.x; k < e; k += blockDim.x) v[F.gmem[k]] -= mean;
+}
+
+// ----------------------------------------------------------------- coarse levels, one cluster per case
+__device__ __forceinline__ void csync() { cg::this_cluster().sync(); }
+
+__device__ void c_center(const CLev& L, float* v, double* gpart, double* sh) {
+  if (L.ngroups == 0) return;
+  const int rank = (int)cg::this_cluster().block_rank();
+  for (int g = 0; g < L.ngroups; ++g) {
+    const int b = L.goff[g], e = L.goff[g + 1];
+    const int len = e - b, seg = (len + CS - 1) / CS;
+    const int sb = b + rank * seg, se = min(e, sb + seg);
+    double acc = 0.0;
+    for (int k = sb + threadIdx.x; k < se; k += blockDim.x) acc += __ldcg(&v[L.gmem[k]]);
+    double s = bsum(acc, sh);
+    if (threadIdx.x == 0) gpart[g * CS + rank] = s;
+  }
+  __threadfence();
+  csync();
+  const int tid = rank * blockDim.x + threadIdx.x, nth = CS * blockDim.x;
+  for (int g = 0; g < L.ngroups; ++g) {
+    double s = 0.0;
+    for (int r = 0; r < CS; ++r) s += __ldcg(&gpart[g * CS + r]);
+    const int b = L.goff[g], e = L.goff[g + 1];
+    const float mean = (float)(s / (double)(e - b));
+    for (int k = b + tid; k < e; k += nth) v[L.gmem[k]] = __ldcg(&v[L.gmem[k]]) - mean;
+  }
+  __threadfence();
+  csync();
+}
+
+__device__ void c_sweep(const CLev& L, bool backward) {
+  const int rank = (int)cg::this_cluster().block_rank();
+  const int tid = rank * blockDim.x + threadIdx.x, nth = CS * blockDim.x;
+  for (int cc = 0; cc < L.ncolors; ++cc) {
+    const int color = backward ? L.ncolors - 1 - cc : cc;
+    for (int k = L.coff[color] + tid; k < L.coff[color + 1]; k += nth) {
+      const int i = L.crows[k];
+      const float d = L.diag[i];
+      if (d == 0.0f) {
+        L.x[i] = 0.0f;
+        continue;
+      }
+      float v = __ldcg(&L.rhs[i]);
+      for (int a = L.off[i]; a < L.off[i + 1]; ++a) v = fmaf(-L.val[a], __ldcg(&L.x[L.col[a]]), v);
+      L.x[i] = v / d;
+    }
+    __threadfence();
+    csync();
+  }
+}
+
+__global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(CT) k_coarse(const CCase* cases, const MState* ST) {
+  __shared__ double sh[32];
+  const int ci = blockIdx.x / CS;
+  const MState& S = ST[ci];
+  if (!(S.state == RUN || S.state == START)) return;  // uniform over the cluster
+  const CCase& C = cases[ci];
+  const int rank = (int)cg::this_cluster().block_rank();
+  const int tid = rank * blockDim.x + threadIdx.x, nth = CS * blockDim.x;
+  int l = 0;
+  for (; l < C.nl; ++l) {
+    const CLev& L = C.lv[l];
+    c_center(L, L.rhs, C.gpart, sh);
+    for (int i = tid; i < L.n; i += nth) L.x[i] = 0.0f;
+    __threadfence();
+    csync();
+    if (L.terminal) {
+      // FP64 dense Cholesky solves, one warp per block (lane 0 works).
+      const int warp = tid >> 5, nw = nth >> 5;
+      if ((threadIdx.x & 31) == 0)
+        for (int bk = warp; bk < L.nblocks; bk += nw) {
+          const int* ix = L.idx + L.ioff[bk];
+          const int n = L.ioff[bk + 1] - L.ioff[bk];
+          const double* f = L.fac + L.foff[bk];
+          double y[32];
+          for (int i = 0; i < n; ++i) {
+            double v = (double)__ldcg(&L.rhs[ix[i]]);
+            for (int j = 0; j < i; ++j) v -= f[i * n + j] * y[j];
+            y[i] = v / f[i * n + i];
+          }
+          for (int i = n - 1; i >= 0; --i) {
+            double v = y[i];
+            for (int j = i + 1; j < n; ++j) v -= f[j * n + i] * y[j];
+            y[i] = v / f[i * n + i];
+          }
+          for (int i = 0; i < n; ++i) L.x[ix[i]] = (float)y[i];
+        }
+      __threadfence();
+      csync();
+      c_center(L, L.x, C.gpart, sh);
+      break;
+    }
+    c_sweep(L, false);
+    c_sweep(L, false);
+    c_center(L, L.x, C.gpart, sh);
+    for (int i = tid; i < L.n; i += nth) {
+      float v = L.diag[i] * __ldcg(&L.x[i]);
+      for (int a = L.off[i]; a < L.off[i + 1]; ++a) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
+      L.res[i] = __ldcg(&L.rhs[i]) - v;
+    }
+    __threadfence();
+    csync();
+    c_center(L, L.res, C.gpart, sh);
+    const CLev& N = C.lv[l + 1];
+    for (int j = tid; j < N.n; j += nth) {
+      float v = 0.0f;
+      for (int k = L.roff[j]; k < L.roff[j + 1]; ++k) v = fmaf(L.rw[k], __ldcg(&L.res[L.rchild[k]]), v);
+      N.rhs[j] = v;
+    }
+    __threadfence();
+    csync();
+  }
+  for (int m = min(l, C.nl - 1) - 1; m >= 0; --m) {
+    const CLev& L = C.lv[m];
+    const CLev& N = C.lv[m + 1];
+    for (int i = tid; i < L.n; i += nth) {
+      float s = 0.0f;
+      for (int k = L.poff[i]; k < L.poff[i + 1]; ++k) s = fmaf(L.pw[k], __ldcg(&N.x[L.pcol[k]]), s);
+      L.x[i] = __ldcg(&L.x[i]) + s;
+    }
+    __threadfence();
+    csync();
+    c_sweep(L, true);
+    c_sweep(L, true);
+    c_center(L, L.x, C.gpart, sh);
+  }
+}
+
+// ----------------------------------------------------------------- prologue / epilogue (FP64)
+// b = -div(u)/dt, terms (pressure.rs:440-459), rounded as written.
+__global__ void __launch_bounds__(TILE) k_rhs(const FineCase* FC, MState* ST, const int2* tiles) {
+  FINE_PROLOGUE(S.state == IDLE)
+  if (!ok) return;
+  if (!F.fluid[c]) {
+    F.b[c] = -0.0;
+    F.terms[c] = 0.0;
+    return;
+  }
+  int q[3];
+  coords(F, c, q[0], q[1], q[2]);
+  double div = 0.0, scale = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    int p[3] = {q[0], q[1], q[2]};
+    const double ul = F.u[fidx(F, a, p[0], p[1], p[2])];
+    p[a] += 1;
+    const double uu = F.u[fidx(F, a, p[0], p[1], p[2])];
+    div = __dadd_rn(div, __ddiv_rn(__dsub_rn(uu, ul), F.dx[a]));
+    scale = __dadd_rn(scale, __ddiv_rn(__dadd_rn(fabs(ul), fabs(uu)), F.dx[a]));
+  }
+  F.b[c] = __ddiv_rn(-div, F.dt);
+  F.terms[c] = __ddiv_rn(scale, F.dt);
+}
+
+// |b_c| (after the host-side gauge of closed components); x = 0.
+__global__ void __launch_bounds__(TILE) k_norm(const FineCase* FC, MState* ST, const int2* tiles) {
+  __shared__ double sh[32];
+  FINE_PROLOGUE(S.state == IDLE)
+  double acc = 0.0;
+  if (ok) {
+    double v = F.bc[c];
+    acc = v * v;
+    F.x64[c] = 0.0;
+    F.e[c] = 0.0f;
+  }
+  double bb;
+  if (case_reduce(acc, F, S, lt, sh, &bb) && threadIdx.x == 0) {
+    S.norm = sqrt(bb);
+    S.has_e = 0;
+    S.scale = 0.0;
+    S.state = S.norm < 1e-24 ? DONE : OUTER;
+  }
+}
+
+// Face correction u -= dt grad(x) (pressure.rs:481-496), face tiles.
+__global__ void k_correct(const FineCase* FC, const MState* ST, const int2* ftiles) {
+  const int2 t = ftiles[blockIdx.x];
+  const FineCase& F = FC[t.x];
+  if (ST[t.x].state != DONE) return;
+  const long long f = (long long)t.y * FTILE + threadIdx.x;
+  for (int r = 0; r < FTILE / 256; ++r) {
+    const long long ff = f + r * 256;
+    if (ff >= F.F) return;
+    double d;
+    const uint8_t k = F.fkind[ff];
+    if (k == INTERIOR) d = __ddiv_rn(__dsub_rn(F.x64[F.fhi[ff]], F.x64[F.flo[ff]]), F.fdist[ff]);
+    else if (k == OUTLET) d = F.flo[ff] >= 0 ? __ddiv_rn(-F.x64[F.flo[ff]], F.fdist[ff]) : __ddiv_rn(F.x64[F.fhi[ff]], F.fdist[ff]);
+    else d = 0.0;
+    F.u[ff] = __dsub_rn(F.u[ff], __dmul_rn(F.dt, d));
+  }
+}
+
+__global__ void __launch_bounds__(TILE) k_addp(const FineCase* FC, const MState* ST, const int2* tiles) {
+  const int2 t = tiles[blockIdx.x];
+  const FineCase& F = FC[t.x];
+  if (ST[t.x].state != DONE) return;
+  const int c = t.y * TILE + threadIdx.x;
+  if (c < F.N) F.pfield[c] = __dadd_rn(F.pfield[c], F.x64[c]);
+}
+
+// ----------------------------------------------------------------- host side
+void greedy_colors(const Csr& a, int n, std::vector<int32_t>& coff, std::vector<int32_t>& rows, int& ncolors) {
+  std::vector<int> color(n, -1);
+  ncolors = 0;
+  std::vector<char> used;
+  for (int i = 0; i < n; ++i) {
+    used.assign(ncolors + 1, 0);
+    for (int k = a.off[i]; k < a.off[i + 1]; ++k) {
+      int j = a.col[k];
+      if (j != i && color[j] >= 0) used[color[j]] = 1;
+    }
+    int c = 0;
+    while (c < ncolors && used[c]) ++c;
+    color[i] = c;
+    ncolors = std::max(ncolors, c + 1);
+  }
+  coff.assign(ncolors + 1, 0);
+  for (int i = 0; i < n; ++i) coff[color[i] + 1] += 1;
+  for (int c = 0; c < ncolors; ++c) coff[c + 1] += coff[c];
+  rows.assign(n, 0);
+  std::vector<int32_t> fill(coff.begin(), coff.end() - 1);
+  for (int i = 0; i < n; ++i) rows[fill[color[i]]++] = i;
+}
+
+template <class T>
+std::vector<float> to_f32(const std::vector<T>& v) {
+  return std::vector<float>(v.begin(), v.end());
+}
+
+struct CaseState {
+  cfdg_grid* G = nullptr;
+  Arena arena;
+  FineCase F{};
+  CCase C{};
+  int ngroups0 = 0;
+  ~CaseState() { arena.release(); }
+};
+
+// Builds the FP32 device copy of a grid's hierarchy for the mixed form (cached on the grid).
+int build_case(cfdg_grid* G, CaseState& cs) {
+  const Hierarchy& H = *G->host_mg;
+  HostGrid& h = G->h;
+  cudaStream_t s = G->stream;
+  Arena& A = cs.arena;
+  A.ctx = G->ctx;
+  FineCase& F = cs.F;
+  for (int a = 0; a < 3; ++a) {
+    F.n[a] = h.n[a];
+    F.w32[a] = (float)G->g.w_in[a];
+    F.wo32[a] = (float)G->g.w_out[a];
+    F.w64[a] = G->g.w_in[a];
+    F.wo64[a] = G->g.w_out[a];
+    F.face_off[a] = h.face_offset[a];
+    for (int d = 0; d < 3; ++d) F.fdim[a][d] = (int)h.face_dims[a][d];
+    F.dx[a] = h.dx[a];
+  }
+  F.N = (int)h.cells;
+  F.F = h.faces;
+  F.uniform = G->uniform ? 1 : 0;
+  F.flags = G->d_flags;
+  F.fluid = G->d_fluid;
+  F.fw64 = G->d_fw;
+  F.fkind = G->d_kind;
+  F.flo = G->d_lo;
+  F.fhi = G->d_hi;
+  F.fdist = G->d_dist;
+  F.x64 = G->x;
+  F.r64 = G->r;
+  F.bc = G->bc;
+  F.b = G->b;
+  F.terms = G->terms;
+  if (!G->uniform) {
+    std::vector<float> w32(h.faces);
+    for (int64_t f = 0; f < h.faces; ++f) w32[f] = (float)h.weight(f);
+    float* d;
+    if (int e = A.upload(&d, w32, s)) return e;
+    F.fw32 = d;
+  }
+  const MgLevel& M0 = H.levels[0];
+  {
+    float* d;
+    if (int e = A.upload(&d, to_f32(M0.diag), s)) return e;
+    F.diag0 = d;
+  }
+  float** fv[] = {&F.e, &F.r32, &F.p, &F.q, &F.x0, &F.rhs0, &F.res0};
+  for (float** v : fv)
+    if (int e = A.alloc(v, F.N)) return e;
+  F.ntiles = (F.N + TILE - 1) / TILE;
+  if (int e = A.alloc(&F.partials, F.ntiles)) return e;
+  cs.ngroups0 = M0.groups.rows();
+  F.ngroups = cs.ngroups0;
+  if (F.ngroups) {
+    int *o, *m;
+    if (int e = A.upload(&o, M0.groups.off, s)) return e;
+    if (int e = A.upload(&m, M0.groups.col, s)) return e;
+    F.goff = o;
+    F.gmem = m;
+  }
+  {
+    int *o, *c, *po, *pc;
+    float *w, *pw;
+    if (int e = A.upload(&o, M0.restrict.off, s)) return e;
+    if (int e = A.upload(&c, M0.restrict.col, s)) return e;
+    if (int e = A.upload(&w, to_f32(M0.restrict.val), s)) return e;
+    if (int e = A.upload(&po, M0.prolong.off, s)) return e;
+    if (int e = A.upload(&pc, M0.prolong.col, s)) return e;
+    if (int e = A.upload(&pw, to_f32(M0.prolong.val), s)) return e;
+    F.r_off = o, F.r_child = c, F.r_w = w, F.p_off = po, F.p_col = pc, F.p_w = pw;
+  }
+  // Coarse levels 1 .. L-1.
+  CCase& C = cs.C;
+  C.nl = (int)H.levels.size() - 1;
+  if (C.nl < 1 || C.nl > MAXL) return fail(CFDG_ERR_UNSUPPORTED, "mixed form: unsupported hierarchy depth");
+  int maxg = 1;
+  for (int l = 1; l <= C.nl; ++l) {
+    const MgLevel& M = H.levels[l];
+    CLev& L = C.lv[l - 1];
+    L.n = M.n;
+    L.terminal = l == C.nl;
+    L.ngroups = M.groups.rows();
+    maxg = std::max(maxg, L.ngroups);
+    int *o, *c;
+    float *v, *d;
+    if (int e = A.upload(&o, M.a.off, s)) return e;
+    if (int e = A.upload(&c, M.a.col, s)) return e;
+    if (int e = A.upload(&v, to_f32(M.a.val), s)) return e;
+    if (int e = A.upload(&d, to_f32(M.diag), s)) return e;
+    L.off = o, L.col = c, L.val = v, L.diag = d;
+    std::vector<int32_t> coff, rows;
+    greedy_colors(M.a, M.n, coff, rows, L.ncolors);
+    int *co, *cr;
+    if (int e = A.upload(&co, coff, s)) return e;
+    if (int e = A.upload(&cr, rows, s)) return e;
+    L.coff = co, L.crows = cr;
+    if (L.ngroups) {
+      int *go, *gm;
+      if (int e = A.upload(&go, M.groups.off, s)) return e;
+      if (int e = A.upload(&gm, M.groups.col, s)) return e;
+      L.goff = go, L.gmem = gm;
+    }
+    float *rhs, *x, *res;
+    if (int e = A.alloc(&rhs, L.n)) return e;
+    if (int e = A.alloc(&x, L.n)) return e;
+    if (int e = A.alloc(&res, L.n)) return e;
+    L.rhs = rhs, L.x = x, L.res = res;
+    if (L.terminal) {
+      L.nblocks = M.direct_idx.rows();
+      int *io, *ix;
+      long long* fo;
+      double* fa;
+      std::vector<long long> foff(M.direct_off.begin(), M.direct_off.end());
+      if (int e = A.upload(&io, M.direct_idx.off, s)) return e;
+      if (int e = A.upload(&ix, M.direct_idx.col, s)) return e;
+      if (int e = A.upload(&fo, foff, s)) return e;
+      if (int e = A.upload(&fa, M.direct_factor, s)) return e;
+      L.ioff = io, L.idx = ix, L.foff = fo, L.fac = fa;
+      for (int b = 0; b < L.nblocks; ++b)
+        if (M.direct_idx.off[b + 1] - M.direct_idx.off[b] > 32)
+          return fail(CFDG_ERR_UNSUPPORTED, "mixed form: coarse block larger than 32");
+    } else {
+      int *ro, *rc, *po, *pc;
+      float *rw, *pw;
+      if (int e = A.upload(&ro, M.restrict.off, s)) return e;
+      if (int e = A.upload(&rc, M.restrict.col, s)) return e;
+      if (int e = A.upload(&rw, to_f32(M.restrict.val), s)) return e;
+      if (int e = A.upload(&po, M.prolong.off, s)) return e;
+      if (int e = A.upload(&pc, M.prolong.col, s)) return e;
+      if (int e = A.upload(&pw, to_f32(M.prolong.val), s)) return e;
+      L.roff = ro, L.rchild = rc, L.rw = rw, L.poff = po, L.pcol = pc, L.pw = pw;
+    }
+  }
+  if (int e = A.alloc(&C.gpart, (size_t)maxg * CS)) return e;
+  F.n1 = C.lv[0].n;
+  F.rhs1 = C.lv[0].rhs;
+  F.x1 = C.lv[0].x;
+  CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+}  // namespace mx
+}  // namespace cfdg
+
+using namespace cfdg;
+using namespace cfdg::mx;
+
+// A set of grids solved together in the mixed form.
+struct cfdg_batch {
+  cfdg_context* ctx = nullptr;
+  std::vector<cfdg_grid*> grids;
+  std::vector<std::shared_ptr<CaseState>> cases;
+  Arena arena;
+  cudaStream_t stream = nullptr, own = nullptr;
+  FineCase* d_fc = nullptr;
+  CCase* d_cc = nullptr;
+  MState* d_st = nullptr;
+  MState* h_st = nullptr;
+  int2 *d_tiles = nullptr, *d_tiles1 = nullptr, *d_ftiles = nullptr, *d_gtab = nullptr;
+  int ntiles = 0, ntiles1 = 0, nftiles = 0, ngtab = 0;
+  std::vector<FineCase> h_fc;
+  cudaGraphExec_t chunk = nullptr;
+  size_t chunk_nodes = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  ~cfdg_batch() {
+    if (chunk) cudaGraphExecDestroy(chunk);
+    arena.release();
+    if (h_st) cudaFreeHost(h_st);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (own) cudaStreamDestroy(own);
+  }
+};
+
+namespace {
+
+void enqueue_vcycle(cfdg_batch* B, cudaStream_t s) {
+  const int nt = B->ntiles;
+  k_v_rhs<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  if (B->ngtab) k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 0);
+  // Two forward sweeps: red, black, red, black (the first red starts from x = 0).
+  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 0, 1);
+  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 1, 0);
+  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 0, 0);
+  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 1, 0);
+  if (B->ngtab) k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 1);
+  k_v_resid<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  if (B->ngtab) k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 2);
+  k_v_restrict<<<B->ntiles1, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles1);
+  k_coarse<<<(int)B->cases.size() * CS, CT, 0, s>>>(B->d_cc, B->d_st);
+  k_v_prolong<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  // Two backward sweeps: black, red, black, red.
+  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 1, 0);
+  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 0, 0);
+  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 1, 0);
+  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 0, 0);
+  if (B->ngtab) k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 1);
+}
+
+// One iteration of the per-case state machine.
+void enqueue_iteration(cfdg_batch* B, cudaStream_t s) {
+  const int nt = B->ntiles;
+  const int nc = (int)B->cases.size();
+  k_op<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  k_update<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  k_outer<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  k_outer_resid<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  k_scale<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  k_start_state<<<(nc + 127) / 128, 128, 0, s>>>(B->d_st, nc);
+  enqueue_vcycle(B, s);
+  k_rz<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  k_p<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+}
+
+int ensure_graph(cfdg_batch* B) {
+  if (B->chunk) return 0;
+  cudaGraph_t g;
+  CU(cudaStreamBeginCapture(B->own, cudaStreamCaptureModeThreadLocal));
+  for (int i = 0; i < CHUNK_IT; ++i) enqueue_iteration(B, B->own);
+  cudaError_t e = cudaStreamEndCapture(B->own, &g);
+  if (e != cudaSuccess) return fail(CFDG_ERR_CUDA, std::string("mixed capture: ") + cudaGetErrorString(e));
+  cudaGraphGetNodes(g, nullptr, &B->chunk_nodes);
+  e = cudaGraphInstantiate(&B->chunk, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(CFDG_ERR_CUDA, std::string("mixed graph: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+// Per-grid FP32 state for the mixed form, built on first use and cached on the grid.
+int case_of(cfdg_grid* G, std::shared_ptr<CaseState>& out) {
+  if (G->mixed) {
+    out = std::static_pointer_cast<CaseState>(G->mixed);
+    return 0;
+  }
+  if (!G->structured || !G->mg || !G->host_mg || !G->mg->full0)
+    return fail(CFDG_ERR_UNSUPPORTED, "the mixed form needs a non-periodic grid with a multigrid hierarchy of two or more levels");
+  auto cs = std::make_shared<CaseState>();
+  cs->G = G;
+  if (int e = build_case(G, *cs)) return e;
+  G->mixed = cs;
+  out = cs;
+  return 0;
+}
+
+}  // namespace
+
+// Called by engine.cu: (re)pack a batch's device tables after its cases are known.
+int cfdg_mixed_pack(cfdg_batch* B) {
+  cudaStream_t s = B->own;
+  B->arena.release();
+  B->arena.ctx = B->ctx;
+  std::vector<int2> tiles, tiles1, ftiles, gtab;
+  B->h_fc.clear();
+  std::vector<CCase> cc;
+  for (size_t i = 0; i < B->cases.size(); ++i) {
+    FineCase F = B->cases[i]->F;
+    F.tile0 = (int)tiles.size();
+    for (int t = 0; t < F.ntiles; ++t) tiles.push_back(make_int2((int)i, t));
+    for (int t = 0; t < (F.n1 + TILE - 1) / TILE; ++t) tiles1.push_back(make_int2((int)i, t));
+    F.ftile0 = (int)ftiles.size();
+    F.nftiles = (int)((F.F + FTILE - 1) / FTILE);
+    for (int t = 0; t < F.nftiles; ++t) ftiles.push_back(make_int2((int)i, t));
+    for (int g = 0; g < F.ngroups; ++g) gtab.push_back(make_int2((int)i, g));
+    B->h_fc.push_back(F);
+    cc.push_back(B->cases[i]->C);
+  }
+  B->ntiles = (int)tiles.size();
+  B->ntiles1 = (int)tiles1.size();
+  B->nftiles = (int)ftiles.size();
+  B->ngtab = (int)gtab.size();
+  Arena& A = B->arena;
+  if (int e = A.upload(&B->d_tiles, tiles, s)) return e;
+  if (int e = A.upload(&B->d_tiles1, tiles1, s)) return e;
+  if (int e = A.upload(&B->d_ftiles, ftiles, s)) return e;
+  if (int e = A.upload(&B->d_gtab, gtab, s)) return e;
+  if (int e = A.upload(&B->d_fc, B->h_fc, s)) return e;
+  if (int e = A.upload(&B->d_cc, cc, s)) return e;
+  if (int e = A.alloc(&B->d_st, B->cases.size())) return e;
+  CU(cudaMemsetAsync(B->d_st, 0, sizeof(MState) * B->cases.size(), s));
+  if (B->h_st) cudaFreeHost(B->h_st);
+  CU(cudaMallocHost((void**)&B->h_st, sizeof(MState) * B->cases.size()));
+  CU(cudaStreamSynchronize(s));
+  if (B->chunk) cudaGraphExecDestroy(B->chunk);
+  B->chunk = nullptr;
+  return ensure_graph(B);
+}
+
+int cfdg_mixed_add_case(cfdg_batch* B, cfdg_grid* G) {
+  std::shared_ptr<CaseState> cs;
+  if (int e = case_of(G, cs)) return e;
+  B->grids.push_back(G);
+  B->cases.push_back(cs);
+  return 0;
+}
+
+// Solves the projection of every case of the batch (device u[i], p[i]); codes[i] per case.
+int cfdg_mixed_project(cfdg_batch* B, double* const* d_u, double* const* d_p, const double* dt, double tol,
+                       uint64_t max_iter, cfdg_poll_fn poll, void* poll_ctx, cfdg_info* infos, int32_t* codes) {
+  cudaStream_t s = B->stream;
+  const int nc = (int)B->cases.size();
+  if (codes)
+    for (int i = 0; i < nc; ++i) codes[i] = 0;
+  // Per-solve I/O pointers into the case table.
+  for (int i = 0; i < nc; ++i) {
+    B->h_fc[i].u = d_u[i];
+    B->h_fc[i].pfield = d_p[i];
+    B->h_fc[i].dt = dt[i];
+  }
+  CU(cudaMemcpyAsync(B->d_fc, B->h_fc.data(), sizeof(FineCase) * nc, cudaMemcpyHostToDevice, s));
+  std::vector<MState> st(nc);
+  for (int i = 0; i < nc; ++i) {
+    std::memset(&st[i], 0, sizeof(MState));
+    st[i].state = IDLE;
+    st[i].tol = tol;
+    st[i].inner_tol = 1e-4;  // per outer step; FP32 reaches it comfortably
+    st[i].max_it = (int)std::min<uint64_t>(max_iter, 1u << 30);
+    st[i].max_inner = 200;
+  }
+  CU(cudaMemcpyAsync(B->d_st, st.data(), sizeof(MState) * nc, cudaMemcpyHostToDevice, s));
+  CU(cudaEventRecord(B->ev0, s));
+  k_rhs<<<B->ntiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  count();
+  // Compatibility and gauge of closed components: per grid, with the plain kernels.
+  CU(cudaStreamSynchronize(s));
+  for (int i = 0; i < nc; ++i) {
+    cfdg_grid* G = B->grids[i];
+    if (G->ncomp_groups == 0) {
+      CU(cudaMemcpyAsync(G->bc, G->b, G->h.cells * 8, cudaMemcpyDeviceToDevice, s));
+      continue;
+    }
+    int rc = plain_compat_center(G, s);
+    if (codes) codes[i] = rc;
+    if (rc) {
+      st[i].state = FAIL;
+      st[i].error = rc;
+    }
+  }
+  CU(cudaStreamSynchronize(s));
+  for (int i = 0; i < nc; ++i)
+    if (st[i].state == FAIL) {
+      MState f = st[i];
+      CU(cudaMemcpyAsync(&B->d_st[i], &f, sizeof(MState), cudaMemcpyHostToDevice, s));
+    }
+  k_norm<<<B->ntiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  count();
+  CU(cudaGetLastError());
+  Poller P;
+  P.fn = poll;
+  P.ctx = poll_ctx;
+  int status = 0;
+  for (;;) {
+    CU(cudaMemcpyAsync(B->h_st, B->d_st, sizeof(MState) * nc, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    bool all = true;
+    for (int i = 0; i < nc; ++i) all &= B->h_st[i].state == DONE || B->h_st[i].state == FAIL;
+    if (all) break;
+    if (int c = P.check()) {
+      status = fail(c, c == CFDG_CANCELLED ? "cancelled" : "wall_time_limit");
+      break;
+    }
+    CU(cudaGraphLaunch(B->chunk, s));
+    count(B->chunk_nodes);
+  }
+  if (status == 0) {
+    // Epilogue for converged cases: gauge of x, face correction, p += x, gauge of p.
+    for (int i = 0; i < nc; ++i) {
+      cfdg_grid* G = B->grids[i];
+      if (B->h_st[i].state == DONE && G->ncomp_groups) plain_center(G, G->x, s);
+    }
+    k_correct<<<B->nftiles, 256, 0, s>>>(B->d_fc, B->d_st, B->d_ftiles);
+    k_addp<<<B->ntiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+    count(2);
+    for (int i = 0; i < nc; ++i) {
+      cfdg_grid* G = B->grids[i];
+      if (B->h_st[i].state == DONE && G->ncomp_groups) plain_center(G, d_p[i], s);
+    }
+  }
+  CU(cudaEventRecord(B->ev1, s));
+  CU(cudaEventSynchronize(B->ev1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, B->ev0, B->ev1);
+  for (int i = 0; i < nc; ++i) {
+    const MState& m = B->h_st[i];
+    if (infos) {
+      cfdg_info& I = infos[i];
+      std::memset(&I, 0, sizeof(I));
+      I.iterations = (uint64_t)m.total_it;
+      I.relative_residual = m.state == DONE ? (m.norm < 1e-24 ? 0.0 : m.true_rel) : 0.0;
+      I.work_units = (uint64_t)m.total_it;
+      I.operator_applications = (uint64_t)m.total_it + (uint64_t)m.outer + 1;
+      I.true_residual_checks = (uint64_t)m.outer + 1;
+      I.preconditioner_applications = (uint64_t)m.total_it + (uint64_t)m.outer;
+      I.cycles = I.preconditioner_applications;
+      I.refinement_steps = (uint64_t)m.outer;
+      I.device_seconds = ms * 1e-3;
+    }
+    if (codes && codes[i] == 0) {
+      if (status) codes[i] = status;
+      else if (m.state == FAIL) codes[i] = m.error ? m.error : CFDG_E033;
+    }
+  }
+  return status;
+}
+
+// ----------------------------------------------------------------- batch lifetime and C ABI
+namespace {
+std::vector<cfdg_grid*> lock_order(const std::vector<cfdg_grid*>& g) {
+  std::vector<cfdg_grid*> v(g);
+  std::sort(v.begin(), v.end());
+  v.erase(std::unique(v.begin(), v.end()), v.end());
+  return v;
+}
+}  // namespace
+
+cfdg_batch* cfdg_mixed_new(cfdg_context* ctx) {
+  auto* B = new cfdg_batch();
+  B->ctx = ctx;
+  B->arena.ctx = ctx;
+  if (cudaStreamCreateWithFlags(&B->own, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&B->ev0) != cudaSuccess ||
+      cudaEventCreate(&B->ev1) != cudaSuccess) {
+    delete B;
+    return nullptr;
+  }
+  B->stream = B->own;
+  return B;
+}
+
+void cfdg_mixed_delete(cfdg_batch* B) {
+  if (!B) return;
+  cudaStreamSynchronize(B->stream);
+  delete B;
+}
+
+void cfdg_mixed_set_stream(cfdg_batch* B, cudaStream_t s) { B->stream = s ? s : B->own; }
+
+extern "C" {
+
+int cfdg_batch_create(cfdg_context* ctx, cfdg_grid* const* grids, int32_t n, cfdg_batch** out) {
+  if (!ctx || !grids || n < 1 || !out) return fail(CFDG_ERR_INVALID, "invalid batch arguments");
+  *out = nullptr;
+  CU(cudaSetDevice(ctx->device));
+  cfdg_batch* B = cfdg_mixed_new(ctx);
+  if (!B) return fail(CFDG_ERR_CUDA, "could not create the batch stream");
+  for (int i = 0; i < n; ++i) {
+    cfdg_grid* G = grids[i];
+    if (!G || G->ctx != ctx) {
+      cfdg_mixed_delete(B);
+      return fail(CFDG_ERR_INVALID, "every grid of a batch must be open on the batch's context");
+    }
+    std::lock_guard<std::mutex> lk(G->mu);
+    if (int e = prepare_multigrid(G)) {
+      cfdg_mixed_delete(B);
+      return e;
+    }
+    if (int e = cfdg_mixed_add_case(B, G)) {
+      cfdg_mixed_delete(B);
+      return e;
+    }
+  }
+  if (int e = cfdg_mixed_pack(B)) {
+    cfdg_mixed_delete(B);
+    return e;
+  }
+  *out = B;
+  return 0;
+}
+
+void cfdg_batch_destroy(cfdg_batch* B) { cfdg_mixed_delete(B); }
+
+int cfdg_batch_set_stream(cfdg_batch* B, void* stream) {
+  if (!B) return fail(CFDG_ERR_INVALID, "null batch");
+  CU(cudaStreamSynchronize(B->stream));
+  cfdg_mixed_set_stream(B, (cudaStream_t)stream);
+  return 0;
+}
+
+int cfdg_batch_size(const cfdg_batch* B) { return B ? (int)B->cases.size() : 0; }
+
+int cfdg_batch_project_device(cfdg_batch* B, double* const* d_u, double* const* d_p, const double* dt, double tol,
+                              uint64_t max_iter, cfdg_poll_fn poll, void* poll_ctx, cfdg_info* infos, int32_t* codes) {
+  if (!B || !d_u || !d_p || !dt) return fail(CFDG_ERR_INVALID, "invalid batch arguments");
+  CU(cudaSetDevice(B->ctx->device));
+  auto order = lock_order(B->grids);
+  std::vector<std::unique_lock<std::mutex>> locks;
+  for (auto* G : order) locks.emplace_back(G->mu);
+  return cfdg_mixed_project(B, d_u, d_p, dt, tol, max_iter, poll, poll_ctx, infos, codes);
+}
+
+int cfdg_batch_project(cfdg_batch* B, double* const* u, double* const* p, const double* dt, double tol,
+                       uint64_t max_iter, cfdg_poll_fn poll, void* poll_ctx, cfdg_info* infos, int32_t* codes) {
+  if (!B || !u || !p || !dt) return fail(CFDG_ERR_INVALID, "invalid batch arguments");
+  CU(cudaSetDevice(B->ctx->device));
+  auto order = lock_order(B->grids);
+  std::vector<std::unique_lock<std::mutex>> locks;
+  for (auto* G : order) locks.emplace_back(G->mu);
+  const int nc = (int)B->grids.size();
+  std::vector<double*> du(nc), dp(nc);
+  cudaStream_t s = B->stream;
+  for (int i = 0; i < nc; ++i) {
+    cfdg_grid* G = B->grids[i];
+    du[i] = G->u;
+    dp[i] = G->pp;
+    CU(cudaMemcpyAsync(G->u, u[i], G->h.faces * 8, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(G->pp, p[i], G->h.cells * 8, cudaMemcpyHostToDevice, s));
+  }
+  std::vector<int32_t> local(nc, 0);
+  int32_t* cd = codes ? codes : local.data();
+  int st = cfdg_mixed_project(B, du.data(), dp.data(), dt, tol, max_iter, poll, poll_ctx, infos, cd);
+  if (st) return st;
+  for (int i = 0; i < nc; ++i) {
+    if (cd[i]) continue;  // transactional: a failed case keeps its inputs
+    cfdg_grid* G = B->grids[i];
+    CU(cudaMemcpyAsync(u[i], G->u, G->h.faces * 8, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(p[i], G->pp, G->h.cells * 8, cudaMemcpyDeviceToHost, s));
+  }
+  CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+}  // extern "C"

@@ -26,7 +26,8 @@ EXPORTS = (
     "cfdg_grid_update_faces", "cfdg_grid_configure", "cfdg_project", "cfdg_solve_scaled", "cfdg_apply",
     "cfdg_center_nullspaces", "cfdg_multigrid_stats_json", "cfdg_last_error", "cfdg_project_device",
     "cfdg_grid_device_bytes", "cfdg_debug_precondition", "cfdg_debug_projection_rhs", "cfdg_grid_set_stream",
-    "cfdg_launch_count", "cfdg_debug_time_kernel", "cfdg_residual_norm_noalloc",
+    "cfdg_launch_count", "cfdg_debug_time_kernel", "cfdg_residual_norm_noalloc", "cfdg_batch_create",
+    "cfdg_batch_destroy", "cfdg_batch_set_stream", "cfdg_batch_size", "cfdg_batch_project", "cfdg_batch_project_device",
 )
 
 
@@ -115,6 +116,16 @@ def load(path: str = LIB_PATH):
         L.cfdg_launch_count.argtypes = []
         L.cfdg_launch_count.restype = C.c_uint64
         L.cfdg_residual_norm_noalloc.argtypes = [P, P, P, P, P]
+        L.cfdg_batch_create.argtypes = [P, C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]
+        L.cfdg_batch_destroy.argtypes = [P]
+        L.cfdg_batch_destroy.restype = None
+        L.cfdg_batch_set_stream.argtypes = [P, P]
+        L.cfdg_batch_size.argtypes = [P]
+        PP = C.POINTER(C.c_void_p)
+        L.cfdg_batch_project.argtypes = [P, PP, PP, C.POINTER(C.c_double), C.c_double, C.c_uint64, POLL, P,
+                                         C.POINTER(Info), C.POINTER(C.c_int32)]
+        L.cfdg_batch_project_device.argtypes = [P, PP, PP, C.POINTER(C.c_double), C.c_double, C.c_uint64, POLL, P,
+                                                C.POINTER(Info), C.POINTER(C.c_int32)]
         L.cfdg_debug_time_kernel.argtypes = [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib = L
         return L

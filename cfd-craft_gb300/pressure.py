@@ -304,3 +304,62 @@ def center_nullspaces(grid, x):
 
 def multigrid_stats(grid):
     return device_grid(grid).multigrid_stats()
+
+
+class Batch:
+    """Several grids projected together in the mixed form (cfdg_batch).
+
+    ``project(us, ps, dts, tol, max)`` returns one (code, LinearInfo) per case; a case
+    with a nonzero code keeps its inputs unchanged."""
+
+    def __init__(self, device_grids, ctx: Context = None):
+        self.ctx = ctx or device_grids[0].ctx
+        self.grids = list(device_grids)
+        L = E.load()
+        arr = (C.c_void_p * len(self.grids))(*[g.h for g in self.grids])
+        h = C.c_void_p()
+        rc = L.cfdg_batch_create(self.ctx.h, arr, len(self.grids), C.byref(h))
+        if rc:
+            raise PressureError(rc, E.last_error())
+        self.h = h
+        self.L = L
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cfdg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int):
+        rc = self.L.cfdg_batch_set_stream(self.h, C.c_void_p(stream_handle or None))
+        if rc:
+            raise PressureError(rc, E.last_error())
+
+    def _run(self, fn, us, ps, dts, tol, max_iter, control):
+        n = len(self.grids)
+        ua = (C.c_void_p * n)(*us)
+        pa = (C.c_void_p * n)(*ps)
+        da = (C.c_double * n)(*[float(d) for d in dts])
+        infos = (E.Info * n)()
+        codes = (C.c_int32 * n)()
+        cb = DeviceGrid._poll_fn(control)
+        rc = fn(self.h, ua, pa, da, float(tol), int(max_iter), cb, None, infos, codes)
+        if rc:
+            raise PressureError(rc, E.last_error())
+        return [(int(codes[i]), LinearInfo(infos[i].iterations, infos[i].relative_residual, infos[i].as_dict()))
+                for i in range(n)]
+
+    def project(self, us, ps, dts, tol, max_iter, control=None):
+        for u, p, g in zip(us, ps, self.grids):
+            assert u.dtype == np.float64 and u.flags.c_contiguous and u.size == g.grid.n_faces
+            assert p.dtype == np.float64 and p.flags.c_contiguous and p.size == g.grid.count
+        return self._run(self.L.cfdg_batch_project, [u.ctypes.data for u in us], [p.ctypes.data for p in ps], dts,
+                         tol, max_iter, control)
+
+    def project_device(self, u_ptrs, p_ptrs, dts, tol, max_iter, control=None):
+        return self._run(self.L.cfdg_batch_project_device, u_ptrs, p_ptrs, dts, tol, max_iter, control)

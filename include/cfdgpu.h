@@ -175,6 +175,29 @@ const char *cfdg_last_error(void);
 int cfdg_project_device(cfdg_grid *grid, double *d_u, double *d_p, double dt, double tol,
                         uint64_t max_iter, cfdg_poll_fn poll, void *poll_ctx, cfdg_info *info);
 
+/* ------------------------------------------------------------------ batched mixed-precision form
+ * The projection of several grids at once in the mixed form: FP32 inner PCG with an
+ * FP32 V-cycle (red-black / multicolour Gauss-Seidel on the reference hierarchy), FP64
+ * dot products, alpha/beta, true residual, outer defect correction and coarsest
+ * solve. Each case stops when its FP64 relative residual |b_c - A x|/|b_c| <= tol.
+ * Every grid must be open on the batch's context, non-periodic, and its multigrid
+ * hierarchy is built (or reused) at creation. A batch keeps its own FP32 state;
+ * the grids stay owned by the caller and must outlive the batch. */
+typedef struct cfdg_batch cfdg_batch;
+int cfdg_batch_create(cfdg_context *ctx, cfdg_grid *const *grids, int32_t n, cfdg_batch **out);
+void cfdg_batch_destroy(cfdg_batch *batch);
+int cfdg_batch_set_stream(cfdg_batch *batch, void *stream);
+int cfdg_batch_size(const cfdg_batch *batch);
+/* pressure::project for every case i (host u[i], p[i]); codes[i] is case i's return
+ * code and a failed case keeps its u[i], p[i]. Returns nonzero only for a failure of
+ * the whole call (CUDA error, cancellation). */
+int cfdg_batch_project(cfdg_batch *batch, double *const *u, double *const *p, const double *dt, double tol,
+                       uint64_t max_iter, cfdg_poll_fn poll, void *poll_ctx, cfdg_info *infos, int32_t *codes);
+/* The same on device arrays d_u[i] (F_i doubles) and d_p[i] (N_i doubles). */
+int cfdg_batch_project_device(cfdg_batch *batch, double *const *d_u, double *const *d_p, const double *dt,
+                              double tol, uint64_t max_iter, cfdg_poll_fn poll, void *poll_ctx, cfdg_info *infos,
+                              int32_t *codes);
+
 /* Device memory the grid holds, in bytes (admission accounting). */
 uint64_t cfdg_grid_device_bytes(const cfdg_grid *grid);
 

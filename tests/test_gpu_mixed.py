@@ -1,0 +1,108 @@
+"""The mixed-precision (FP32 inner / FP64 outer) and batched forms against the FP64 oracle.
+
+The mixed form is not the parity form: it stops on the same FP64 true residual
+(|b_c - A x| / |b_c| <= tol, recomputed with the exact operator) but reaches it by a
+different iteration. Bars: true relative residual <= tol; pressure and corrected
+velocities within MIXED_REL of the FP64 oracle's projection solved to the same
+tolerance; a case gives the same result alone and inside a batch.
+"""
+import numpy as np
+import pytest
+
+from cases import sin_field
+
+pytestmark = pytest.mark.gpu
+MIXED_REL = 1e-6  # relative to max|p| / max|u|, at tol 1e-8 (both solutions carry O(tol*cond) error)
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float64).view(np.uint64)
+
+
+def mixed_cases(pkg):
+    rng = np.random.default_rng(11)
+    return {
+        "c1-64x64x32": pkg.synth.case((64, 64, 32), 1.0, preconditioner="multigrid"),
+        "buildings-64x64x32": pkg.synth.case((64, 64, 32), 2.0, inflow=5.0, preconditioner="multigrid",
+                                             boxes=pkg.synth.random_boxes(rng, 6, (128.0, 128.0, 64.0), dx=2.0)),
+        "pocket": pkg.synth.case((24, 24, 12), 1.0, preconditioner="multigrid",
+                                 boxes=[((6, 6, 0), (18, 8, 8)), ((6, 16, 0), (18, 18, 8)), ((6, 6, 0), (8, 18, 8)),
+                                        ((16, 6, 0), (18, 18, 8)), ((6, 6, 6), (18, 18, 8))]),
+        "odd-37x29x21": pkg.synth.case((37, 29, 21), 1.5, preconditioner="multigrid",
+                                       boxes=[((9, 6, 0), (21, 18, 15))]),
+    }
+
+
+def run_mixed(pkg, g, u, p, dt, tol):
+    dg = pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed")
+    uu, pp = u.copy(), p.copy()
+    info = dg.project(uu, pp, dt, tol, 10000)
+    dg.close()
+    return uu, pp, info
+
+
+@pytest.mark.parametrize("name", ["c1-64x64x32", "buildings-64x64x32", "pocket", "odd-37x29x21"])
+def test_mixed_projection_against_fp64_oracle(pkg, O, name):
+    case = mixed_cases(pkg)[name]
+    g = pkg.grid.Grid.build(case)
+    og = O.Grid(case)
+    u = pkg.synth.random_velocity(g, 4)
+    p = np.zeros(g.count)
+    dt, tol = 0.1, 1e-8
+    code, ou, op, oinfo = og.project(u, p, dt, tol, 10000)
+    assert code == 0
+    uu, pp, info = run_mixed(pkg, g, u, p, dt, tol)
+    w = info.work
+    assert info.relative_residual <= tol, info.relative_residual
+    assert w["refinement_steps"] >= 1
+    # Independent check of the residual with the oracle's operator.
+    b, _ = og.projection_rhs(u, dt)
+    bc = og.center_nullspaces(b)
+    x = og.center_nullspaces(pp - p) if not all(g.anchored) else pp - p
+    true_rel = np.linalg.norm(og.apply(x) - bc) / np.linalg.norm(bc)
+    assert true_rel <= 1.5 * tol, true_rel
+    ep = np.max(np.abs(pp - op)) / max(np.max(np.abs(op)), 1e-300)
+    eu = np.max(np.abs(uu - ou)) / max(np.max(np.abs(ou)), 1e-300)
+    print(f"{name}: inner iterations {info.iterations} outer {w['refinement_steps']} "
+          f"(oracle {oinfo['iterations']}), rel err p {ep:.2e} u {eu:.2e}, true rel {true_rel:.2e}")
+    assert ep <= MIXED_REL and eu <= MIXED_REL
+    div0 = np.max(np.abs(og.divergence(u)))
+    assert np.max(np.abs(og.divergence(uu))) <= 1e-6 * max(div0, 1.0)
+
+
+def test_batch_equals_alone_and_is_transactional(pkg, O):
+    cases = mixed_cases(pkg)
+    names = ["buildings-64x64x32", "pocket", "odd-37x29x21", "c1-64x64x32"]
+    grids = [pkg.grid.Grid.build(cases[n]) for n in names]
+    us = [pkg.synth.random_velocity(g, 20 + i) for i, g in enumerate(grids)]
+    ps = [sin_field(g.count, 0.1 * (i + 1)) * (g.fluid == 1) for i, g in enumerate(grids)]
+    dts = [0.1, 0.2, 0.05, 0.1]
+    alone = [run_mixed(pkg, g, u, p, dt, 1e-8) for g, u, p, dt in zip(grids, us, ps, dts)]
+    dgs = [pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed") for g in grids]
+    batch = pkg.pressure.Batch(dgs)
+    bu = [u.copy() for u in us]
+    bp = [p.copy() for p in ps]
+    res = batch.project(bu, bp, dts, 1e-8, 10000)
+    for i, (code, info) in enumerate(res):
+        assert code == 0
+        assert info.iterations == alone[i][2].iterations
+        assert np.array_equal(bits(bu[i]), bits(alone[i][0])), names[i]
+        assert np.array_equal(bits(bp[i]), bits(alone[i][1])), names[i]
+    # An incompatible case (an inlet feeding a sealed region) fails alone; the others solve.
+    bad = pkg.synth.case((24, 12, 8), 1.0, preconditioner="multigrid", boxes=[((8, 0, 0), (9, 12, 8))])
+    gb = pkg.grid.Grid.build(bad)
+    assert not all(gb.anchored)
+    ub = pkg.synth.random_velocity(gb, 1)
+    pb = np.zeros(gb.count)
+    dgb = pkg.pressure.DeviceGrid(gb, preconditioner="multigrid", precision="mixed")
+    batch2 = pkg.pressure.Batch([dgb, dgs[0]])
+    u0, p0 = ub.copy(), pb.copy()
+    u1, p1 = us[0].copy(), ps[0].copy()
+    res = batch2.project([u0, u1], [p0, p1], [0.1, 0.1], 1e-8, 10000)
+    assert res[0][0] == 31 and res[1][0] == 0
+    assert np.array_equal(bits(u0), bits(ub)) and np.array_equal(bits(p0), bits(pb))
+    assert np.array_equal(bits(u1), bits(alone[0][0]))
+    batch.close()
+    batch2.close()
+    for d in dgs + [dgb]:
+        d.close()
