@@ -197,8 +197,110 @@ def run_reference(args):
 
 
 # ----------------------------------------------------------------------------- GPU leg
+class Form:
+    """One arithmetic form of the projection on `cases` copies of the workload (different
+    velocity seeds): plain FP64 (one grid), mixed (one grid) or batched mixed (one batch)."""
+
+    def __init__(self, pkg, torch, dev, stream, form, cases, steps, rank):
+        import numpy as np
+
+        self.pkg, self.torch, self.form = pkg, torch, form
+        self.ncases = cases
+        case = workload_case(pkg)
+        self.grids = [pkg.grid.Grid.build(case)] * 1
+        g = self.grids[0]
+        self.g = g
+        precision = "plain" if form == "plain" else "mixed"
+        self.dgs = [pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision=precision) for _ in range(cases)]
+        for d in self.dgs:
+            d.set_stream(stream.cuda_stream)
+        self.batch = None
+        if form == "batched":
+            self.batch = pkg.pressure.Batch(self.dgs)
+            self.batch.set_stream(stream.cuda_stream)
+        self.u0 = [pkg.synth.random_velocity(g, seed=100 * rank + i) for i in range(cases)]
+        self.noise = [noise_fields(pkg, g, steps, seed=1000 * rank + 10 + i) for i in range(cases)]
+        self.d_u = [torch.from_numpy(u).to(dev) for u in self.u0]
+        self.d_p = [torch.zeros(g.count, dtype=torch.float64, device=dev) for _ in range(cases)]
+        self.d_noise = [torch.from_numpy(n).to(dev) for n in self.noise]
+
+    def step(self, s):
+        for i in range(self.ncases):
+            self.d_u[i].add_(self.d_noise[i][s])
+        if self.batch is not None:
+            res = self.batch.project_device([u.data_ptr() for u in self.d_u], [p.data_ptr() for p in self.d_p],
+                                            [DT] * self.ncases, TOL, MAX_IT)
+            for code, _ in res:
+                assert code == 0, code
+            return [info for _, info in res]
+        return [d.project_device(u.data_ptr(), p.data_ptr(), DT, TOL, MAX_IT)
+                for d, u, p in zip(self.dgs, self.d_u, self.d_p)]
+
+    def e2e(self, stream, flush, K, W):
+        """Through the public C ABI with pinned host buffers (H2D + solve + D2H per step)."""
+        torch = self.torch
+        n, g = self.ncases, self.g
+        host_u = [[torch.from_numpy(self.u0[i] + self.noise[i][s]).pin_memory() for i in range(n)] for s in range(K)]
+        host_p = [[torch.zeros(g.count, dtype=torch.float64).pin_memory() for _ in range(n)] for _ in range(K)]
+
+        def one(s, copy=False):
+            us = [h.clone().numpy() if copy else h.numpy() for h in host_u[s]]
+            ps = [h.clone().numpy() if copy else h.numpy() for h in host_p[s]]
+            if self.batch is not None:
+                for code, _ in self.batch.project(us, ps, [DT] * n, TOL, MAX_IT):
+                    assert code == 0
+            else:
+                for d, u, p in zip(self.dgs, us, ps):
+                    d.project(u, p, DT, TOL, MAX_IT)
+
+        for s in range(min(W, K)):
+            one(s, copy=True)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for s in range(K):
+            flush.zero_()
+            one(s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), 2 * n * 8 * (g.n_faces + g.count)
+
+    def close(self):
+        if self.batch is not None:
+            self.batch.close()
+        for d in self.dgs:
+            d.close()
+
+
+def timed_steps(form, torch, stream, flush, W, K, dist=None):
+    for s in range(W):
+        form.step(s)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    marks = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    infos = []
+    ev0.record(stream)
+    for s in range(K):
+        flush.zero_()
+        marks[s][0].record(stream)
+        infos.extend(form.step(W + s))
+        marks[s][1].record(stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    total = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([total], device=flush.device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+    lat = sorted(a.elapsed_time(b) for a, b in marks)
+    return total, lat, infos
+
+
 def run_engine(args):
-    import numpy as np
     import torch
 
     import __graft_entry__ as entry
@@ -215,120 +317,98 @@ def run_engine(args):
 
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
-    case = workload_case(pkg)
-    g = pkg.grid.Grid.build(case)
-    ctx = pkg.pressure.Context(device=local)
-    dg = pkg.pressure.DeviceGrid(g, ctx, preconditioner="multigrid", precision=args.form)
     # One real stream for torch's helpers, the engine and the events (the legacy default
     # stream's handle is NULL, which would leave the engine on its own stream).
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
-    dg.set_stream(stream.cuda_stream)
-    K, W = args.steps, args.warmup
-    u0 = pkg.synth.random_velocity(g, seed=rank)
-    noise = noise_fields(pkg, g, K + W, seed=10 + rank)
-    d_u = torch.from_numpy(u0).to(dev)
-    d_p = torch.zeros(g.count, dtype=torch.float64, device=dev)
-    d_noise = torch.from_numpy(noise).to(dev)
     flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MiB > L2 (129 MB)
-    infos = []
-
-    def step(s):
-        d_u.add_(d_noise[s])
-        return dg.project_device(d_u.data_ptr(), d_p.data_ptr(), DT, TOL, MAX_IT)
-
-    for s in range(W):
-        step(s)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+    K, W = args.steps, args.warmup
     L = pkg.engine.load()
+    ncases = args.cases if args.form == "batched" else 1
+    form = Form(pkg, torch, dev, stream, args.form, ncases, K + W, rank)
+    g = form.g
     launches0 = L.cfdg_launch_count()
     clocks = Clocks(local)
     clocks.start()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    marks = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    for s in range(K):
-        flush.zero_()
-        marks[s][0].record(stream)
-        infos.append(step(W + s))
-        marks[s][1].record(stream)
-    ev1.record(stream)
-    torch.cuda.synchronize()
+    total_ms, lat, infos = timed_steps(form, torch, stream, flush, W, K, dist)
     clk = clocks.stop()
     launches = L.cfdg_launch_count() - launches0
-    total_ms = ev0.elapsed_time(ev1)
-    lat = sorted(a.elapsed_time(b) for a, b in marks)
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        dist.barrier()
-    value = world * K / (total_ms / 1e3)
-    its = [i.iterations for i in infos]
-
-    # e2e through the public API: pinned host inputs, H2D + solve + D2H per step.
-    host_u = [torch.from_numpy(u0 + noise[s]).pin_memory() for s in range(K)]
-    host_p = [torch.zeros(g.count, dtype=torch.float64).pin_memory() for _ in range(K)]
-    for s in range(min(W, K)):
-        uu, pp = host_u[s].clone().numpy(), host_p[s].clone().numpy()
-        dg.project(uu, pp, DT, TOL, MAX_IT)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for s in range(K):
-        flush.zero_()
-        dg.project(host_u[s].numpy(), host_p[s].numpy(), DT, TOL, MAX_IT)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
+    solves = world * K * ncases
+    value = solves / (total_ms / 1e3)
+    e2e_ms, io_bytes = form.e2e(stream, flush, K, W)
     if dist:
         t = torch.tensor([e2e_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    e2e = {"value": round(world * K / (e2e_ms / 1e3), 4), "unit": UNIT,
-           "h2d_bytes_per_step": 8 * (g.n_faces + g.count), "d2h_bytes_per_step": 8 * (g.n_faces + g.count)}
-
-    # Roofline of the dominant kernel: one fine-level Gauss-Seidel sweep (4 per V-cycle).
+    e2e = {"value": round(solves / (e2e_ms / 1e3), 4), "unit": UNIT, "h2d_bytes_per_step": io_bytes // 2,
+           "d2h_bytes_per_step": io_bytes // 2}
     peak, peak_kind = peaks()
-    sweep_ms, sweep_bytes = dg.time_kernel(1, reps=20)
-    op_ms, op_bytes = dg.time_kernel(0, reps=50)
-    cyc_ms, cyc_bytes = dg.time_kernel(3, reps=5)
-    achieved = sweep_bytes / (sweep_ms * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "fine-level lexicographic Gauss-Seidel sweep (level-scheduled)",
-                "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5),
-                "peak_source": peak_kind, "traffic": None,
-                "algorithmic_bytes": sweep_bytes, "ms_per_launch": round(sweep_ms, 4)}
-    kernels = {
-        "operator": {"ms": round(op_ms, 4), "GB/s": round(op_bytes / op_ms / 1e6, 1)},
-        "gs_sweep_fine": {"ms": round(sweep_ms, 4), "GB/s": round(achieved, 1)},
-        "vcycle": {"ms": round(cyc_ms, 4), "GB/s": round(cyc_bytes / cyc_ms / 1e6, 1)},
-    }
+    kernels = {}
+    if args.form == "plain":
+        d = form.dgs[0]
+        for name, which, reps in (("operator_fp64", 0, 50), ("gs_sweep_fine_fp64", 1, 10), ("vcycle_fp64", 3, 3)):
+            ms, b = d.time_kernel(which, reps)
+            kernels[name] = {"ms": round(ms, 4), "GB/s": round(b / ms / 1e6, 1) if b else None,
+                             "algorithmic_bytes": b}
+        dom = "gs_sweep_fine_fp64"
+        dom_desc = "fine-level lexicographic Gauss-Seidel sweep, FP64 (pipelined wavefront)"
+    else:
+        bt = form.batch if form.batch is not None else None
+        if bt is None:
+            bt = pkg.pressure.Batch(form.dgs)
+            bt.set_stream(stream.cuda_stream)
+            form.step(0)  # leave every case with live vectors
+        for name, which, reps in (("rb_half_sweep_fp32", 0, 50), ("operator_fp32", 1, 50),
+                                  ("coarse_levels_cluster", 2, 20), ("vcycle_fp32", 3, 10)):
+            ms, b = bt.time_kernel(which, reps)
+            kernels[name] = {"ms": round(ms, 4), "GB/s": round(b / ms / 1e6, 1) if b else None,
+                             "algorithmic_bytes": b}
+        if form.batch is None:
+            bt.close()
+        dom = "rb_half_sweep_fp32"
+        dom_desc = "fine-level red-black Gauss-Seidel half sweep, FP32, all cases of the batch"
+    k = kernels[dom]
+    achieved = k["algorithmic_bytes"] / (k["ms"] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom_desc, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes": k["algorithmic_bytes"], "ms_per_launch": k["ms"]}
+    # The plain FP64 form on the same workload, for the batched-mixed vs plain comparison.
+    plain = None
+    if args.form != "plain" and not args.skip_plain:
+        pf = Form(pkg, torch, dev, stream, "plain", 1, 2 + 1, rank + 7)
+        pms, plat, pinfos = timed_steps(pf, torch, stream, flush, 1, 2, dist)
+        plain = {"value": round(world * 2 / (pms / 1e3), 4), "unit": UNIT, "ms_per_solve": round(pms / 2, 2),
+                 "iterations_mean": round(statistics.mean(i.iterations for i in pinfos), 1), "steps": 2}
+        pf.close()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(case)
+        cpu = cpu_baseline(workload_case(pkg))
     if rank == 0:
-        n_it = statistics.mean(its)
+        its = [i.iterations for i in infos]
+        outer = [i.work.get("refinement_steps", 0) for i in infos]
         line = {
             "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": round(total_ms / K, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.form == "plain" else "f32+f64",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "form": f"{args.form} (multigrid PCG)", "cells": g.count,
-                       "faces": g.n_faces, "l2": "256 MiB buffer written before every step (inside the timed region)",
+            "config": {"workload": WORKLOAD, "form": {"plain": "plain FP64 multigrid PCG (parity form)",
+                                                       "mixed": "mixed FP32/FP64 multigrid PCG, one case",
+                                                       "batched": f"batched mixed FP32/FP64, {ncases} cases per step"}[args.form],
+                       "cases_per_step": ncases, "cells_per_case": g.count, "faces_per_case": g.n_faces,
+                       "l2": "256 MiB buffer written before every step (inside the timed region)",
                        "parallelism": f"replicas x{world}"},
-            "latency_ms": {"p50": round(lat[len(lat) // 2], 3), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3)},
-            "iterations_mean": round(n_it, 2),
-            "cell_updates_per_s": round(g.count * n_it * value, 1),
-            "e2e": e2e, "roofline": roofline, "kernels": kernels, "cpu_baseline": cpu,
+            "latency_ms": {"p50": round(lat[len(lat) // 2], 3), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
+                           "unit": "per step"},
+            "iterations_mean": round(statistics.mean(its), 2),
+            "refinement_steps_mean": round(statistics.mean(outer), 2),
+            "cell_updates_per_s": round(g.count * statistics.mean(its) * value, 1),
+            "e2e": e2e, "roofline": roofline, "kernels": kernels, "plain_fp64": plain, "cpu_baseline": cpu,
             "gpu_launches": int(launches), "clocks": clk,
         }
+        if plain:
+            line["batched_vs_plain"] = round(value / plain["value"], 2)
         print(json.dumps(line), flush=True)
-    dg.close()
+    form.close()
     if dist:
         dist.destroy_process_group()
     return 0
@@ -340,7 +420,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--form", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--form", default="batched", choices=["plain", "mixed", "batched"])
+    ap.add_argument("--cases", type=int, default=8, help="cases per step of the batched form")
+    ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -1371,8 +1371,10 @@ void cfdg_grid_close(cfdg_grid* G) {
   {
     std::lock_guard<std::mutex> lk(G->mu);
     cudaSetDevice(G->ctx->device);
-    reset_chunk(G);
     if (G->stream) cudaStreamSynchronize(G->stream);
+    G->solo.reset();  // before the streams go: the batch may hold the grid's stream
+    G->mixed.reset();
+    reset_chunk(G);
     if (G->own) cudaStreamSynchronize(G->own);
     if (G->ic0) G->ic0->arena.release();
     if (G->mg) G->mg->arena.release();

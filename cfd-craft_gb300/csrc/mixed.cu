@@ -1148,7 +1148,10 @@ cfdg_batch* cfdg_mixed_new(cfdg_context* ctx) {
 
 void cfdg_mixed_delete(cfdg_batch* B) {
   if (!B) return;
-  cudaStreamSynchronize(B->stream);
+  // The caller's stream may already be gone; the batch's own stream and a device-wide
+  // event wait cover its work.
+  if (B->own) cudaStreamSynchronize(B->own);
+  if (B->ev1) cudaEventSynchronize(B->ev1);
   delete B;
 }
 
@@ -1196,6 +1199,68 @@ int cfdg_batch_set_stream(cfdg_batch* B, void* stream) {
 }
 
 int cfdg_batch_size(const cfdg_batch* B) { return B ? (int)B->cases.size() : 0; }
+
+int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* ms_per_launch,
+                           double* algorithmic_bytes) {
+  if (!B || reps < 1) return fail(CFDG_ERR_INVALID, "invalid arguments");
+  CU(cudaSetDevice(B->ctx->device));
+  auto order = lock_order(B->grids);
+  std::vector<std::unique_lock<std::mutex>> locks;
+  for (auto* G : order) locks.emplace_back(G->mu);
+  const int nc = (int)B->cases.size();
+  cudaStream_t s = B->stream;
+  // Every case in the inner-iteration state, on the vectors of the last solve.
+  std::vector<MState> saved(nc), run(nc);
+  CU(cudaMemcpyAsync(saved.data(), B->d_st, sizeof(MState) * nc, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  for (int i = 0; i < nc; ++i) {
+    run[i] = saved[i];
+    run[i].state = RUN;
+    run[i].counter = 0;
+  }
+  CU(cudaMemcpyAsync(B->d_st, run.data(), sizeof(MState) * nc, cudaMemcpyHostToDevice, s));
+  double cells = 0, n1 = 0;
+  for (auto& F : B->h_fc) {
+    cells += F.N;
+    n1 += F.n1;
+  }
+  double bytes = 0;
+  auto launch = [&]() {
+    switch (which) {
+      case 0:  // one red-black half sweep over every case's fine level
+        k_rb<<<B->ntiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 1, 0);
+        break;
+      case 1:  // FP32 operator q = A p (with p.q)
+        k_op<<<B->ntiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+        break;
+      case 2:  // all coarse levels, one cluster per case
+        k_coarse<<<nc * CS, CT, 0, s>>>(B->d_cc, B->d_st);
+        break;
+      default:
+        enqueue_vcycle(B, s);
+        break;
+    }
+  };
+  if (which == 0) bytes = 9.0 * cells;       // half the cells: rhs, diag, u16 flags, x out; the other half's x in
+  else if (which == 1) bytes = 10.0 * cells; // p in, u16 flags, q out
+  else if (which == 2) bytes = 0.0;
+  else bytes = 0.0;
+  launch();
+  launch();
+  CU(cudaEventRecord(B->ev0, s));
+  for (int r = 0; r < reps; ++r) launch();
+  CU(cudaEventRecord(B->ev1, s));
+  CU(cudaEventSynchronize(B->ev1));
+  float ms = 0;
+  CU(cudaEventElapsedTime(&ms, B->ev0, B->ev1));
+  CU(cudaMemcpyAsync(B->d_st, saved.data(), sizeof(MState) * nc, cudaMemcpyHostToDevice, s));
+  CU(cudaStreamSynchronize(s));
+  CU(cudaGetLastError());
+  if (ms_per_launch) *ms_per_launch = ms / reps;
+  if (algorithmic_bytes) *algorithmic_bytes = bytes;
+  (void)n1;
+  return 0;
+}
 
 int cfdg_batch_project_device(cfdg_batch* B, double* const* d_u, double* const* d_p, const double* dt, double tol,
                               uint64_t max_iter, cfdg_poll_fn poll, void* poll_ctx, cfdg_info* infos, int32_t* codes) {

@@ -363,3 +363,11 @@ class Batch:
 
     def project_device(self, u_ptrs, p_ptrs, dts, tol, max_iter, control=None):
         return self._run(self.L.cfdg_batch_project_device, u_ptrs, p_ptrs, dts, tol, max_iter, control)
+
+    def time_kernel(self, which: int, reps: int = 20):
+        """(ms per launch, algorithmic bytes); see cfdg_batch_time_kernel."""
+        ms, b = C.c_double(), C.c_double()
+        rc = self.L.cfdg_batch_time_kernel(self.h, which, reps, C.byref(ms), C.byref(b))
+        if rc:
+            raise PressureError(rc, E.last_error())
+        return ms.value, b.value

@@ -193,6 +193,13 @@ int cfdg_batch_size(const cfdg_batch *batch);
  * the whole call (CUDA error, cancellation). */
 int cfdg_batch_project(cfdg_batch *batch, double *const *u, double *const *p, const double *dt, double tol,
                        uint64_t max_iter, cfdg_poll_fn poll, void *poll_ctx, cfdg_info *infos, int32_t *codes);
+/* Times one unit of the batch's work `reps` times with CUDA events on the batch's
+ * stream, every case in its inner-iteration state: which = 0 one red-black half sweep
+ * over all fine levels, 1 the FP32 operator, 2 the coarse-level cluster kernel, 3 one
+ * V-cycle. Reports the mean duration and the unit's algorithmic bytes (0 when not
+ * stated). Diagnostic; no reference counterpart. */
+int cfdg_batch_time_kernel(cfdg_batch *batch, int32_t which, int32_t reps, double *ms_per_launch,
+                           double *algorithmic_bytes);
 /* The same on device arrays d_u[i] (F_i doubles) and d_p[i] (N_i doubles). */
 int cfdg_batch_project_device(cfdg_batch *batch, double *const *d_u, double *const *d_p, const double *dt,
                               double tol, uint64_t max_iter, cfdg_poll_fn poll, void *poll_ctx, cfdg_info *infos,
