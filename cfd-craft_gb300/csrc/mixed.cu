@@ -43,8 +43,8 @@ namespace mx {
 
 constexpr int TILE = 256;       // fine cells per block
 constexpr int FTILE = 1024;     // faces per block (velocity correction)
-constexpr int CS = 8;           // CTAs per cluster
-constexpr int CT = 512;         // threads per cluster CTA
+constexpr int CS = 16;          // CTAs per cluster (non-portable size, opted in at pack time)
+constexpr int CT = 1024;        // threads per cluster CTA
 constexpr int MAXL = 16;        // coarse levels per case
 constexpr int CHUNK_IT = 8;     // iterations per captured graph launch
 
@@ -75,6 +75,8 @@ struct FineCase {
   const double* fw64;    // per-face FP64 weights (the grid's)
   const float* fw32;     // per-face FP32 weights (non-uniform grids)
   const float* diag0;    // level-0 diagonal (full layout), 0 for solid cells
+  const float* idiag0;   // its reciprocal, 0 where the diagonal is 0
+  int npairs, pad_pairs; // red-black work items: x-pairs of cells
   // FP64 outer vectors (the grid's buffers)
   double *x64, *r64, *bc, *b, *terms;
   // FP32 inner vectors
@@ -98,12 +100,17 @@ struct FineCase {
   const int *flo, *fhi;
   const double* fdist;
 };
+static_assert(sizeof(FineCase) % 8 == 0, "FineCase is copied to shared memory in 8-byte words");
 
 struct CLev {
   int n, terminal, ncolors, ngroups;
   const int *off, *col;
   const float *val, *diag;
   const int *coff, *crows;
+  const int *ell_off, *ell_w;  // per colour: start of its ELL block and its width
+  const int* ell_col;          // column-major ELL per colour (padding points at the row itself)
+  const float* ell_val;        // entries, 0 in padding
+  const float* idiag;          // 1/diag, 0 where diag is 0
   const int *goff, *gmem;
   const int *roff, *rchild;  // restriction to the next level
   const float* rw;
@@ -235,13 +242,21 @@ __device__ __forceinline__ double op64(const FineCase& F, const double* __restri
 }
 
 // ----------------------------------------------------------------- fine-level kernels
-#define FINE_PROLOGUE(STATE_TEST)                 \
-  const int2 t = tiles[blockIdx.x];               \
-  const FineCase& F = FC[t.x];                    \
-  MState& S = ST[t.x];                            \
-  if (!(STATE_TEST)) return;                      \
-  const int lt = t.y;                             \
-  const int c = lt * TILE + threadIdx.x;          \
+#define FINE_PROLOGUE(STATE_TEST)                                                     \
+  const int2 t = tiles[blockIdx.x];                                                   \
+  __shared__ __align__(16) FineCase sF;                                               \
+  {                                                                                   \
+    const long long* src_ = reinterpret_cast<const long long*>(&FC[t.x]);             \
+    long long* dst_ = reinterpret_cast<long long*>(&sF);                              \
+    for (int w_ = threadIdx.x; w_ < (int)(sizeof(FineCase) / 8); w_ += blockDim.x)     \
+      dst_[w_] = src_[w_];                                                            \
+  }                                                                                   \
+  __syncthreads();                                                                    \
+  const FineCase& F = sF;                                                             \
+  MState& S = ST[t.x];                                                                \
+  if (!(STATE_TEST)) return;                                                          \
+  const int lt = t.y;                                                                 \
+  const int c = lt * TILE + threadIdx.x;                                              \
   const bool ok = c < F.N;
 
 // A: q = A32 p, alpha = rz / (p.q) (E032 when not positive).
@@ -370,41 +385,54 @@ __global__ void __launch_bounds__(TILE) k_v_rhs(const FineCase* FC, MState* ST, 
   if (ok) F.rhs0[c] = F.r32[c];
 }
 
-// Red-black Gauss-Seidel half sweep on level 0: cells with (i+j+k)%2 == color.
-// first: x is taken as zero (the cycle's initial guess); cells outside the operator
-// (solid, sealed singletons) are kept at zero.
+// Red-black Gauss-Seidel half sweep on level 0: cells with (i+j+k)%2 == color. Work
+// item p is the pair of cells (2m, 2m+1) of one x-row, of which exactly one has the
+// colour. first: x is taken as zero (the cycle's initial guess). Cells outside the
+// operator (solid, sealed singletons) are kept at zero. Tiles index pairs.
 __global__ void __launch_bounds__(TILE) k_rb(const FineCase* FC, MState* ST, const int2* tiles, int color, int first) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
-  if (!ok) return;
-  int q[3];
-  coords(F, c, q[0], q[1], q[2]);
-  if (((q[0] + q[1] + q[2]) & 1) != color) return;
-  const float d = F.diag0[c];
-  if (d == 0.0f) {
-    F.x0[c] = 0.0f;
+  (void)ok;
+  const int nx = F.n[0], ny = F.n[1];
+  const int pr = lt * TILE + threadIdx.x;
+  if (pr >= F.npairs) return;
+  const int px = (nx + 1) >> 1;
+  const int row = pr / px, m = pr - row * px;
+  const int j = row % ny, k = row / ny;
+  const int i = 2 * m + ((j + k + color) & 1);
+  if (i >= nx) return;
+  const int cc = row * nx + i;
+  float* __restrict__ x = F.x0;
+  const float id = F.idiag0[cc];
+  if (id == 0.0f) {
+    x[cc] = 0.0f;
     return;
   }
-  const unsigned fl = F.flags[c];
-  float v = F.rhs0[c];
+  float v = F.rhs0[cc];
   if (!(first && color == 0)) {
-    const int stride[3] = {1, F.n[0], F.n[0] * F.n[1]};
+    const unsigned fl = F.flags[cc];
+    const int sy = nx, sz = nx * ny;
+    if (F.uniform) {
+      if (fl & 1u) v = fmaf(F.w32[0], x[cc - 1], v);
+      if (fl & 2u) v = fmaf(F.w32[0], x[cc + 1], v);
+      if (fl & 4u) v = fmaf(F.w32[1], x[cc - sy], v);
+      if (fl & 8u) v = fmaf(F.w32[1], x[cc + sy], v);
+      if (fl & 16u) v = fmaf(F.w32[2], x[cc - sz], v);
+      if (fl & 32u) v = fmaf(F.w32[2], x[cc + sz], v);
+    } else {
+      const int q[3] = {i, j, k};
+      const int stride[3] = {1, sy, sz};
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+      for (int a = 0; a < 3; ++a)
 #pragma unroll
-      for (int side = 0; side < 2; ++side) {
-        if (!(fl & (1u << (2 * a + side)))) continue;
-        float w;
-        if (F.uniform) {
-          w = F.w32[a];
-        } else {
+        for (int side = 0; side < 2; ++side) {
+          if (!(fl & (1u << (2 * a + side)))) continue;
           int p[3] = {q[0], q[1], q[2]};
           p[a] += side;
-          w = F.fw32[fidx(F, a, p[0], p[1], p[2])];
+          v = fmaf(F.fw32[fidx(F, a, p[0], p[1], p[2])], x[side ? cc + stride[a] : cc - stride[a]], v);
         }
-        v = fmaf(w, F.x0[side ? c + stride[a] : c - stride[a]], v);
-      }
+    }
   }
-  F.x0[c] = v / d;
+  x[cc] = v * id;
 }
 
 // res0 = rhs0 - A0 x0 (A0 = diag - sum w on interior faces).
@@ -488,21 +516,22 @@ __device__ __forceinline__ void csync() { cg::this_cluster().sync(); }
 __device__ void c_center(const CLev& L, float* v, double* gpart, double* sh) {
   if (L.ngroups == 0) return;
   const int rank = (int)cg::this_cluster().block_rank();
+  const int CSZ = (int)cg::this_cluster().num_blocks();
   for (int g = 0; g < L.ngroups; ++g) {
     const int b = L.goff[g], e = L.goff[g + 1];
-    const int len = e - b, seg = (len + CS - 1) / CS;
+    const int len = e - b, seg = (len + CSZ - 1) / CSZ;
     const int sb = b + rank * seg, se = min(e, sb + seg);
     double acc = 0.0;
     for (int k = sb + threadIdx.x; k < se; k += blockDim.x) acc += __ldcg(&v[L.gmem[k]]);
     double s = bsum(acc, sh);
-    if (threadIdx.x == 0) gpart[g * CS + rank] = s;
+    if (threadIdx.x == 0) gpart[g * CSZ + rank] = s;
   }
   __threadfence();
   csync();
-  const int tid = rank * blockDim.x + threadIdx.x, nth = CS * blockDim.x;
+  const int tid = rank * blockDim.x + threadIdx.x, nth = CSZ * blockDim.x;
   for (int g = 0; g < L.ngroups; ++g) {
     double s = 0.0;
-    for (int r = 0; r < CS; ++r) s += __ldcg(&gpart[g * CS + r]);
+    for (int r = 0; r < CSZ; ++r) s += __ldcg(&gpart[g * CSZ + r]);
     const int b = L.goff[g], e = L.goff[g + 1];
     const float mean = (float)(s / (double)(e - b));
     for (int k = b + tid; k < e; k += nth) v[L.gmem[k]] = __ldcg(&v[L.gmem[k]]) - mean;
@@ -513,33 +542,35 @@ __device__ void c_center(const CLev& L, float* v, double* gpart, double* sh) {
 
 __device__ void c_sweep(const CLev& L, bool backward) {
   const int rank = (int)cg::this_cluster().block_rank();
-  const int tid = rank * blockDim.x + threadIdx.x, nth = CS * blockDim.x;
+  const int tid = rank * blockDim.x + threadIdx.x, nth = (int)cg::this_cluster().num_blocks() * blockDim.x;
   for (int cc = 0; cc < L.ncolors; ++cc) {
     const int color = backward ? L.ncolors - 1 - cc : cc;
-    for (int k = L.coff[color] + tid; k < L.coff[color + 1]; k += nth) {
-      const int i = L.crows[k];
-      const float d = L.diag[i];
-      if (d == 0.0f) {
-        L.x[i] = 0.0f;
-        continue;
-      }
+    const int b = L.coff[color], nrow = L.coff[color + 1] - b;
+    const int base = L.ell_off[color], w = L.ell_w[color];
+    for (int t = tid; t < nrow; t += nth) {
+      const int i = L.crows[b + t];
+      const float id = L.idiag[i];
       float v = __ldcg(&L.rhs[i]);
-      for (int a = L.off[i]; a < L.off[i + 1]; ++a) v = fmaf(-L.val[a], __ldcg(&L.x[L.col[a]]), v);
-      L.x[i] = v / d;
+      for (int a = 0; a < w; ++a) {
+        const int e = base + a * nrow + t;
+        v = fmaf(-L.ell_val[e], __ldcg(&L.x[L.ell_col[e]]), v);
+      }
+      L.x[i] = v * id;
     }
     __threadfence();
     csync();
   }
 }
 
-__global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(CT) k_coarse(const CCase* cases, const MState* ST) {
+__global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState* ST) {
   __shared__ double sh[32];
-  const int ci = blockIdx.x / CS;
+  const int csz = (int)cg::this_cluster().num_blocks();
+  const int ci = blockIdx.x / csz;
   const MState& S = ST[ci];
   if (!(S.state == RUN || S.state == START)) return;  // uniform over the cluster
   const CCase& C = cases[ci];
   const int rank = (int)cg::this_cluster().block_rank();
-  const int tid = rank * blockDim.x + threadIdx.x, nth = CS * blockDim.x;
+  const int tid = rank * blockDim.x + threadIdx.x, nth = csz * blockDim.x;
   int l = 0;
   for (; l < C.nl; ++l) {
     const CLev& L = C.lv[l];
@@ -761,10 +792,15 @@ int build_case(cfdg_grid* G, CaseState& cs) {
   }
   const MgLevel& M0 = H.levels[0];
   {
-    float* d;
-    if (int e = A.upload(&d, to_f32(M0.diag), s)) return e;
+    float *d, *id;
+    std::vector<float> d32 = to_f32(M0.diag), i32(d32.size());
+    for (size_t i = 0; i < d32.size(); ++i) i32[i] = d32[i] == 0.0f ? 0.0f : 1.0f / d32[i];
+    if (int e = A.upload(&d, d32, s)) return e;
+    if (int e = A.upload(&id, i32, s)) return e;
     F.diag0 = d;
+    F.idiag0 = id;
   }
+  F.npairs = ((h.n[0] + 1) / 2) * h.n[1] * h.n[2];
   float** fv[] = {&F.e, &F.r32, &F.p, &F.q, &F.x0, &F.rhs0, &F.res0};
   for (float** v : fv)
     if (int e = A.alloc(v, F.N)) return e;
@@ -815,6 +851,40 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     if (int e = A.upload(&co, coff, s)) return e;
     if (int e = A.upload(&cr, rows, s)) return e;
     L.coff = co, L.crows = cr;
+    {
+      // Column-major ELL per colour: entry a of the colour's t-th row at base + a*nrow + t.
+      std::vector<int32_t> eoff(L.ncolors), ew(L.ncolors), ecol;
+      std::vector<float> eval, idg(M.n);
+      for (int i = 0; i < M.n; ++i) idg[i] = M.diag[i] == 0.0 ? 0.0f : 1.0f / (float)M.diag[i];
+      for (int c = 0; c < L.ncolors; ++c) {
+        int nrow = coff[c + 1] - coff[c], w = 0;
+        for (int t = 0; t < nrow; ++t) {
+          int r = rows[coff[c] + t];
+          w = std::max(w, M.a.off[r + 1] - M.a.off[r]);
+        }
+        eoff[c] = (int32_t)ecol.size();
+        ew[c] = w;
+        ecol.resize(ecol.size() + (size_t)w * nrow);
+        eval.resize(eval.size() + (size_t)w * nrow);
+        for (int t = 0; t < nrow; ++t) {
+          int r = rows[coff[c] + t];
+          int len = M.a.off[r + 1] - M.a.off[r];
+          for (int a = 0; a < w; ++a) {
+            size_t e = (size_t)eoff[c] + (size_t)a * nrow + t;
+            ecol[e] = a < len ? M.a.col[M.a.off[r] + a] : r;
+            eval[e] = a < len ? (float)M.a.val[M.a.off[r] + a] : 0.0f;
+          }
+        }
+      }
+      int *eo, *ewp, *ec;
+      float *ev, *idp;
+      if (int e = A.upload(&eo, eoff, s)) return e;
+      if (int e = A.upload(&ewp, ew, s)) return e;
+      if (int e = A.upload(&ec, ecol, s)) return e;
+      if (int e = A.upload(&ev, eval, s)) return e;
+      if (int e = A.upload(&idp, idg, s)) return e;
+      L.ell_off = eo, L.ell_w = ewp, L.ell_col = ec, L.ell_val = ev, L.idiag = idp;
+    }
     if (L.ngroups) {
       int *go, *gm;
       if (int e = A.upload(&go, M.groups.off, s)) return e;
@@ -877,8 +947,9 @@ struct cfdg_batch {
   CCase* d_cc = nullptr;
   MState* d_st = nullptr;
   MState* h_st = nullptr;
-  int2 *d_tiles = nullptr, *d_tiles1 = nullptr, *d_ftiles = nullptr, *d_gtab = nullptr;
-  int ntiles = 0, ntiles1 = 0, nftiles = 0, ngtab = 0;
+  int2 *d_tiles = nullptr, *d_tiles1 = nullptr, *d_ftiles = nullptr, *d_gtab = nullptr, *d_ptiles = nullptr;
+  int ntiles = 0, ntiles1 = 0, nftiles = 0, ngtab = 0, nptiles = 0;
+  int csize = CS;  // CTAs per cluster of the coarse-level kernel
   std::vector<FineCase> h_fc;
   cudaGraphExec_t chunk = nullptr;
   size_t chunk_nodes = 0;
@@ -895,26 +966,41 @@ struct cfdg_batch {
 
 namespace {
 
+void launch_coarse(cfdg_batch* B, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(B->cases.size() * B->csize), 1, 1);
+  cfg.blockDim = dim3(CT, 1, 1);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)B->csize;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_coarse, (const CCase*)B->d_cc, (const MState*)B->d_st);
+}
+
 void enqueue_vcycle(cfdg_batch* B, cudaStream_t s) {
   const int nt = B->ntiles;
   k_v_rhs<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
   if (B->ngtab) k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 0);
   // Two forward sweeps: red, black, red, black (the first red starts from x = 0).
-  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 0, 1);
-  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 1, 0);
-  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 0, 0);
-  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 1, 0);
+  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 0, 1);
+  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 1, 0);
+  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 0, 0);
+  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 1, 0);
   if (B->ngtab) k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 1);
   k_v_resid<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
   if (B->ngtab) k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 2);
   k_v_restrict<<<B->ntiles1, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles1);
-  k_coarse<<<(int)B->cases.size() * CS, CT, 0, s>>>(B->d_cc, B->d_st);
+  launch_coarse(B, s);
   k_v_prolong<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
   // Two backward sweeps: black, red, black, red.
-  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 1, 0);
-  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 0, 0);
-  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 1, 0);
-  k_rb<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 0, 0);
+  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 1, 0);
+  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 0, 0);
+  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 1, 0);
+  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 0, 0);
   if (B->ngtab) k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 1);
 }
 
@@ -970,7 +1056,7 @@ int cfdg_mixed_pack(cfdg_batch* B) {
   cudaStream_t s = B->own;
   B->arena.release();
   B->arena.ctx = B->ctx;
-  std::vector<int2> tiles, tiles1, ftiles, gtab;
+  std::vector<int2> tiles, tiles1, ftiles, gtab, ptiles;
   B->h_fc.clear();
   std::vector<CCase> cc;
   for (size_t i = 0; i < B->cases.size(); ++i) {
@@ -978,6 +1064,7 @@ int cfdg_mixed_pack(cfdg_batch* B) {
     F.tile0 = (int)tiles.size();
     for (int t = 0; t < F.ntiles; ++t) tiles.push_back(make_int2((int)i, t));
     for (int t = 0; t < (F.n1 + TILE - 1) / TILE; ++t) tiles1.push_back(make_int2((int)i, t));
+    for (int t = 0; t < (F.npairs + TILE - 1) / TILE; ++t) ptiles.push_back(make_int2((int)i, t));
     F.ftile0 = (int)ftiles.size();
     F.nftiles = (int)((F.F + FTILE - 1) / FTILE);
     for (int t = 0; t < F.nftiles; ++t) ftiles.push_back(make_int2((int)i, t));
@@ -989,7 +1076,31 @@ int cfdg_mixed_pack(cfdg_batch* B) {
   B->ntiles1 = (int)tiles1.size();
   B->nftiles = (int)ftiles.size();
   B->ngtab = (int)gtab.size();
+  B->nptiles = (int)ptiles.size();
   Arena& A = B->arena;
+  if (int e = A.upload(&B->d_ptiles, ptiles, s)) return e;
+  // Coarse-level clusters: 16 CTAs when the device allows that non-portable size, else 8.
+  B->csize = CS;
+  if (cudaFuncSetAttribute(k_coarse, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    B->csize = 8;
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(B->csize, 1, 1);
+    cfg.blockDim = dim3(CT, 1, 1);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = B->csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_coarse, &cfg) != cudaSuccess || nclusters < 1) {
+      cudaGetLastError();
+      B->csize = 8;
+    }
+  }
   if (int e = A.upload(&B->d_tiles, tiles, s)) return e;
   if (int e = A.upload(&B->d_tiles1, tiles1, s)) return e;
   if (int e = A.upload(&B->d_ftiles, ftiles, s)) return e;
@@ -1228,13 +1339,13 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
   auto launch = [&]() {
     switch (which) {
       case 0:  // one red-black half sweep over every case's fine level
-        k_rb<<<B->ntiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles, 1, 0);
+        k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 1, 0);
         break;
       case 1:  // FP32 operator q = A p (with p.q)
         k_op<<<B->ntiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
         break;
       case 2:  // all coarse levels, one cluster per case
-        k_coarse<<<nc * CS, CT, 0, s>>>(B->d_cc, B->d_st);
+        launch_coarse(B, s);
         break;
       default:
         enqueue_vcycle(B, s);
