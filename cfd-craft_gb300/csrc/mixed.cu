@@ -244,6 +244,8 @@ __device__ __forceinline__ double op64(const FineCase& F, const double* __restri
 // ----------------------------------------------------------------- fine-level kernels
 #define FINE_PROLOGUE(STATE_TEST)                                                     \
   const int2 t = tiles[blockIdx.x];                                                   \
+  MState& S = ST[t.x];                                                                \
+  if (!(STATE_TEST)) return;                                                          \
   __shared__ __align__(16) FineCase sF;                                               \
   {                                                                                   \
     const long long* src_ = reinterpret_cast<const long long*>(&FC[t.x]);             \
@@ -253,24 +255,44 @@ __device__ __forceinline__ double op64(const FineCase& F, const double* __restri
   }                                                                                   \
   __syncthreads();                                                                    \
   const FineCase& F = sF;                                                             \
-  MState& S = ST[t.x];                                                                \
-  if (!(STATE_TEST)) return;                                                          \
   const int lt = t.y;                                                                 \
   const int c = lt * TILE + threadIdx.x;                                              \
   const bool ok = c < F.N;
+
+// Reduction kernels cover DOT cells per block, DOT / TILE per thread (cell c0 + r*TILE).
+constexpr int DOT = 4 * TILE;
+
+// FP32 error-free transformations: a running sum (hi, lo) of exact products keeps
+// about twice the FP32 significand, so a thread's few terms convert to FP64 once.
+__device__ __forceinline__ void dd_add_prod(float a, float b, float& hi, float& lo) {
+  const float p = a * b;
+  const float pe = fmaf(a, b, -p);
+  const float s = hi + p;
+  const float bb = s - hi;
+  const float se = (hi - (s - bb)) + (p - bb);
+  hi = s;
+  lo += se + pe;
+}
 
 // A: q = A32 p, alpha = rz / (p.q) (E032 when not positive).
 __global__ void __launch_bounds__(TILE) k_op(const FineCase* FC, MState* ST, const int2* tiles) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN)
-  double acc = 0.0;
-  if (ok) {
-    float v = op32(F, F.p, c, F.flags[c]);
-    F.q[c] = v;
-    acc = (double)F.p[c] * (double)v;
+  (void)c;
+  (void)ok;
+  float hi = 0.0f, lo = 0.0f;
+#pragma unroll
+  for (int r = 0; r < DOT / TILE; ++r) {
+    const int cc = lt * DOT + r * TILE + threadIdx.x;
+    if (cc < F.N) {
+      const float pv = F.p[cc];
+      const float v = op32(F, F.p, cc, F.flags[cc]);
+      F.q[cc] = v;
+      dd_add_prod(pv, v, hi, lo);
+    }
   }
   double pq;
-  if (case_reduce(acc, F, S, lt, sh, &pq) && threadIdx.x == 0) {
+  if (case_reduce((double)hi + (double)lo, F, S, lt, sh, &pq) && threadIdx.x == 0) {
     if (!(pq > 0.0) || !isfinite(pq)) {
       S.state = FAIL;
       S.error = CFDG_E032;
@@ -284,20 +306,26 @@ __global__ void __launch_bounds__(TILE) k_op(const FineCase* FC, MState* ST, con
 __global__ void __launch_bounds__(TILE) k_update(const FineCase* FC, MState* ST, const int2* tiles) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN)
+  (void)c;
+  (void)ok;
   const float alpha = (float)S.alpha;
-  double acc = 0.0;
-  if (ok) {
-    F.e[c] = fmaf(alpha, F.p[c], F.e[c]);
-    float r = fmaf(-alpha, F.q[c], F.r32[c]);
-    F.r32[c] = r;
-    acc = (double)r * (double)r;
+  float hi = 0.0f, lo = 0.0f;
+#pragma unroll
+  for (int rr = 0; rr < DOT / TILE; ++rr) {
+    const int cc = lt * DOT + rr * TILE + threadIdx.x;
+    if (cc < F.N) {
+      F.e[cc] = fmaf(alpha, F.p[cc], F.e[cc]);
+      const float r = fmaf(-alpha, F.q[cc], F.r32[cc]);
+      F.r32[cc] = r;
+      dd_add_prod(r, r, hi, lo);
+    }
   }
-  double rr;
-  if (case_reduce(acc, F, S, lt, sh, &rr) && threadIdx.x == 0) {
+  double rr2;
+  if (case_reduce((double)hi + (double)lo, F, S, lt, sh, &rr2) && threadIdx.x == 0) {
     S.inner_it += 1;
     S.total_it += 1;
     S.has_e = 1;
-    if (sqrt(rr) <= S.inner_tol || S.inner_it >= S.max_inner || S.total_it >= S.max_it) S.state = OUTER;
+    if (sqrt(rr2) <= S.inner_tol || S.inner_it >= S.max_inner || S.total_it >= S.max_it) S.state = OUTER;
   }
 }
 
@@ -314,11 +342,17 @@ __global__ void __launch_bounds__(TILE) k_outer(const FineCase* FC, MState* ST, 
 __global__ void __launch_bounds__(TILE) k_outer_resid(const FineCase* FC, MState* ST, const int2* tiles) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == OUTER)
+  (void)c;
+  (void)ok;
   double acc = 0.0;
-  if (ok) {
-    double v = __dsub_rn(F.bc[c], op64(F, F.x64, c, F.flags[c]));
-    F.r64[c] = v;
-    acc = v * v;
+#pragma unroll
+  for (int r = 0; r < DOT / TILE; ++r) {
+    const int cc = lt * DOT + r * TILE + threadIdx.x;
+    if (cc < F.N) {
+      const double v = __dsub_rn(F.bc[cc], op64(F, F.x64, cc, F.flags[cc]));
+      F.r64[cc] = v;
+      acc = __fma_rn(v, v, acc);
+    }
   }
   double rr;
   if (case_reduce(acc, F, S, lt, sh, &rr) && threadIdx.x == 0) {
@@ -358,10 +392,16 @@ __global__ void k_start_state(MState* ST, int n) {
 __global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, const int2* tiles) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN || S.state == START)
-  double acc = 0.0;
-  if (ok) acc = (double)F.r32[c] * (double)F.x0[c];
+  (void)c;
+  (void)ok;
+  float hi = 0.0f, lo = 0.0f;
+#pragma unroll
+  for (int r = 0; r < DOT / TILE; ++r) {
+    const int cc = lt * DOT + r * TILE + threadIdx.x;
+    if (cc < F.N) dd_add_prod(F.r32[cc], F.x0[cc], hi, lo);
+  }
   double rz;
-  if (case_reduce(acc, F, S, lt, sh, &rz) && threadIdx.x == 0) {
+  if (case_reduce((double)hi + (double)lo, F, S, lt, sh, &rz) && threadIdx.x == 0) {
     if (S.state == START) {
       S.beta = 0.0;
       S.state = RUN;
@@ -382,7 +422,7 @@ __global__ void __launch_bounds__(TILE) k_p(const FineCase* FC, MState* ST, cons
 // rhs0 = r32.
 __global__ void __launch_bounds__(TILE) k_v_rhs(const FineCase* FC, MState* ST, const int2* tiles) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
-  if (ok) F.rhs0[c] = F.r32[c];
+  if (ok && F.rhs0 != F.r32) F.rhs0[c] = F.r32[c];
 }
 
 // Red-black Gauss-Seidel half sweep on level 0: cells with (i+j+k)%2 == color. Work
@@ -640,6 +680,187 @@ __global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState*
   }
 }
 
+// ----------------------------------------------------------------- coarse levels, whole grid
+// All coarse levels of every case in one cooperative launch: each phase of the cycle
+// spreads the rows of all cases over the whole grid (a global index space of per-case
+// row ranges) and the phases are separated by grid-wide barriers.
+constexpr int MAXC = 32;  // colours per level
+
+struct CoarseTab {
+  int nc, nlev;
+  int maxc[MAXL];
+  int anyg[MAXL];
+  const int* rows;   // [nlev][nc+1] prefix over cases of the rows of level l
+  const int* term;   // [nlev][nc+1] terminal blocks at level l
+  const int* fwd;    // [nlev][MAXC][nc+1] rows of colour c (non-terminal levels)
+  const int* bwd;    // [nlev][MAXC][nc+1] rows of colour C_case-1-c
+  const int* next;   // [nlev][nc+1] rows of level l+1 (restriction targets; non-terminal at l)
+  const int* live;   // [nlev][nc+1] rows of level l when non-terminal (residual, prolongation)
+  const int* grp;    // [nlev][nc+1] closed groups at level l
+};
+
+__device__ __forceinline__ int find_case(const int* off, int nc, int t) {
+  int lo = 0, hi = nc;  // off[lo] <= t < off[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(&off[mid]) <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ bool active(const MState* ST, int ci) {
+  const int st = ST[ci].state;
+  return st == RUN || st == START;
+}
+
+// Subtracts each closed group's mean, one CTA per (case, group) pair.
+__device__ void g_center(const CCase* cases, const MState* ST, const CoarseTab& T, int l, int which,
+                         double* sh, cg::grid_group& grid) {
+  const int* off = T.grp + l * (T.nc + 1);
+  const int total = __ldg(&off[T.nc]);
+  __shared__ float mean;
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int ci = find_case(off, T.nc, t);
+    if (!active(ST, ci)) continue;
+    const CLev& L = cases[ci].lv[l];
+    float* v = which == 0 ? L.rhs : (which == 1 ? L.x : L.res);
+    const int g = t - off[ci];
+    const int b = L.goff[g], e = L.goff[g + 1];
+    double acc = 0.0;
+    for (int k = b + threadIdx.x; k < e; k += blockDim.x) acc += __ldcg(&v[L.gmem[k]]);
+    double s = bsum(acc, sh);
+    if (threadIdx.x == 0) mean = (float)(s / (double)(e - b));
+    __syncthreads();
+    const float m = mean;
+    for (int k = b + threadIdx.x; k < e; k += blockDim.x) v[L.gmem[k]] = __ldcg(&v[L.gmem[k]]) - m;
+    __syncthreads();
+  }
+  grid.sync();
+}
+
+__device__ void g_sweep(const CCase* cases, const MState* ST, const CoarseTab& T, int l, bool backward,
+                        cg::grid_group& grid) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  for (int cc = 0; cc < T.maxc[l]; ++cc) {
+    const int* off = (backward ? T.bwd : T.fwd) + (l * MAXC + cc) * (T.nc + 1);
+    const int total = __ldg(&off[T.nc]);
+    for (int t = gt; t < total; t += nth) {
+      const int ci = find_case(off, T.nc, t);
+      if (!active(ST, ci)) continue;
+      const CLev& L = cases[ci].lv[l];
+      const int color = backward ? L.ncolors - 1 - cc : cc;
+      const int k = t - off[ci];
+      const int nrow = L.coff[color + 1] - L.coff[color];
+      const int i = L.crows[L.coff[color] + k];
+      const int base = L.ell_off[color], w = L.ell_w[color];
+      float v = __ldcg(&L.rhs[i]);
+      for (int a = 0; a < w; ++a) {
+        const int e = base + a * nrow + k;
+        v = fmaf(-L.ell_val[e], __ldcg(&L.x[L.ell_col[e]]), v);
+      }
+      L.x[i] = v * L.idiag[i];
+    }
+    grid.sync();
+  }
+}
+
+__global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MState* ST, CoarseTab T) {
+  __shared__ double sh[32];
+  cg::grid_group grid = cg::this_grid();
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  const int nc = T.nc;
+  for (int l = 0; l < T.nlev; ++l) {
+    if (T.anyg[l]) g_center(cases, ST, T, l, 0, sh, grid);
+    {
+      const int* off = T.rows + l * (nc + 1);
+      for (int t = gt; t < off[nc]; t += nth) {
+        const int ci = find_case(off, nc, t);
+        if (active(ST, ci)) cases[ci].lv[l].x[t - off[ci]] = 0.0f;
+      }
+    }
+    grid.sync();
+    {
+      // Terminal levels: FP64 dense Cholesky solves, one warp per block (lane 0 works).
+      const int* off = T.term + l * (nc + 1);
+      const int warp = gt >> 5, nw = nth >> 5;
+      if ((threadIdx.x & 31) == 0)
+        for (int t = warp; t < off[nc]; t += nw) {
+          const int ci = find_case(off, nc, t);
+          if (!active(ST, ci)) continue;
+          const CLev& L = cases[ci].lv[l];
+          const int bk = t - off[ci];
+          const int* ix = L.idx + L.ioff[bk];
+          const int n = L.ioff[bk + 1] - L.ioff[bk];
+          const double* f = L.fac + L.foff[bk];
+          double y[32];
+          for (int i = 0; i < n; ++i) {
+            double v = (double)__ldcg(&L.rhs[ix[i]]);
+            for (int j = 0; j < i; ++j) v -= f[i * n + j] * y[j];
+            y[i] = v / f[i * n + i];
+          }
+          for (int i = n - 1; i >= 0; --i) {
+            double v = y[i];
+            for (int j = i + 1; j < n; ++j) v -= f[j * n + i] * y[j];
+            y[i] = v / f[i * n + i];
+          }
+          for (int i = 0; i < n; ++i) L.x[ix[i]] = (float)y[i];
+        }
+    }
+    grid.sync();
+    g_sweep(cases, ST, T, l, false, grid);
+    g_sweep(cases, ST, T, l, false, grid);
+    if (T.anyg[l]) g_center(cases, ST, T, l, 1, sh, grid);
+    {
+      const int* off = T.live + l * (nc + 1);
+      for (int t = gt; t < off[nc]; t += nth) {
+        const int ci = find_case(off, nc, t);
+        if (!active(ST, ci)) continue;
+        const CLev& L = cases[ci].lv[l];
+        const int i = t - off[ci];
+        float v = L.diag[i] * __ldcg(&L.x[i]);
+        for (int a = L.off[i]; a < L.off[i + 1]; ++a) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
+        L.res[i] = __ldcg(&L.rhs[i]) - v;
+      }
+    }
+    grid.sync();
+    if (T.anyg[l]) g_center(cases, ST, T, l, 2, sh, grid);
+    {
+      const int* off = T.next + l * (nc + 1);
+      for (int t = gt; t < off[nc]; t += nth) {
+        const int ci = find_case(off, nc, t);
+        if (!active(ST, ci)) continue;
+        const CLev& L = cases[ci].lv[l];
+        const CLev& N = cases[ci].lv[l + 1];
+        const int j = t - off[ci];
+        float v = 0.0f;
+        for (int k = L.roff[j]; k < L.roff[j + 1]; ++k) v = fmaf(L.rw[k], __ldcg(&L.res[L.rchild[k]]), v);
+        N.rhs[j] = v;
+      }
+    }
+    grid.sync();
+  }
+  for (int l = T.nlev - 2; l >= 0; --l) {
+    {
+      const int* off = T.live + l * (nc + 1);
+      for (int t = gt; t < off[nc]; t += nth) {
+        const int ci = find_case(off, nc, t);
+        if (!active(ST, ci)) continue;
+        const CLev& L = cases[ci].lv[l];
+        const CLev& N = cases[ci].lv[l + 1];
+        const int i = t - off[ci];
+        float s = 0.0f;
+        for (int k = L.poff[i]; k < L.poff[i + 1]; ++k) s = fmaf(L.pw[k], __ldcg(&N.x[L.pcol[k]]), s);
+        L.x[i] = __ldcg(&L.x[i]) + s;
+      }
+    }
+    grid.sync();
+    g_sweep(cases, ST, T, l, true, grid);
+    g_sweep(cases, ST, T, l, true, grid);
+    if (T.anyg[l]) g_center(cases, ST, T, l, 1, sh, grid);
+  }
+}
+
 // ----------------------------------------------------------------- prologue / epilogue (FP64)
 // b = -div(u)/dt, terms (pressure.rs:440-459), rounded as written.
 __global__ void __launch_bounds__(TILE) k_rhs(const FineCase* FC, MState* ST, const int2* tiles) {
@@ -670,12 +891,18 @@ __global__ void __launch_bounds__(TILE) k_rhs(const FineCase* FC, MState* ST, co
 __global__ void __launch_bounds__(TILE) k_norm(const FineCase* FC, MState* ST, const int2* tiles) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == IDLE)
+  (void)c;
+  (void)ok;
   double acc = 0.0;
-  if (ok) {
-    double v = F.bc[c];
-    acc = v * v;
-    F.x64[c] = 0.0;
-    F.e[c] = 0.0f;
+#pragma unroll
+  for (int r = 0; r < DOT / TILE; ++r) {
+    const int cc = lt * DOT + r * TILE + threadIdx.x;
+    if (cc < F.N) {
+      const double v = F.bc[cc];
+      acc = __fma_rn(v, v, acc);
+      F.x64[cc] = 0.0;
+      F.e[cc] = 0.0f;
+    }
   }
   double bb;
   if (case_reduce(acc, F, S, lt, sh, &bb) && threadIdx.x == 0) {
@@ -746,6 +973,7 @@ struct CaseState {
   Arena arena;
   FineCase F{};
   CCase C{};
+  std::vector<std::vector<int32_t>> colors;  // per coarse level: colour offsets (host copy)
   int ngroups0 = 0;
   ~CaseState() { arena.release(); }
 };
@@ -801,10 +1029,17 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     F.idiag0 = id;
   }
   F.npairs = ((h.n[0] + 1) / 2) * h.n[1] * h.n[2];
-  float** fv[] = {&F.e, &F.r32, &F.p, &F.q, &F.x0, &F.rhs0, &F.res0};
+  float** fv[] = {&F.e, &F.r32, &F.p, &F.q, &F.x0, &F.res0};
   for (float** v : fv)
     if (int e = A.alloc(v, F.N)) return e;
-  F.ntiles = (F.N + TILE - 1) / TILE;
+  // The cycle's right-hand side is the inner residual itself unless level 0 has
+  // closed groups, whose gauge it would modify in place.
+  if (M0.groups.rows() > 0) {
+    if (int e = A.alloc(&F.rhs0, F.N)) return e;
+  } else {
+    F.rhs0 = F.r32;
+  }
+  F.ntiles = (F.N + DOT - 1) / DOT;  // reduction tiles (partials per case)
   if (int e = A.alloc(&F.partials, F.ntiles)) return e;
   cs.ngroups0 = M0.groups.rows();
   F.ngroups = cs.ngroups0;
@@ -847,6 +1082,7 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     L.off = o, L.col = c, L.val = v, L.diag = d;
     std::vector<int32_t> coff, rows;
     greedy_colors(M.a, M.n, coff, rows, L.ncolors);
+    cs.colors.push_back(coff);
     int *co, *cr;
     if (int e = A.upload(&co, coff, s)) return e;
     if (int e = A.upload(&cr, rows, s)) return e;
@@ -947,9 +1183,13 @@ struct cfdg_batch {
   CCase* d_cc = nullptr;
   MState* d_st = nullptr;
   MState* h_st = nullptr;
-  int2 *d_tiles = nullptr, *d_tiles1 = nullptr, *d_ftiles = nullptr, *d_gtab = nullptr, *d_ptiles = nullptr;
-  int ntiles = 0, ntiles1 = 0, nftiles = 0, ngtab = 0, nptiles = 0;
+  int2 *d_tiles = nullptr, *d_tiles1 = nullptr, *d_ftiles = nullptr, *d_gtab = nullptr, *d_ptiles = nullptr,
+       *d_dtiles = nullptr;
+  int ntiles = 0, ntiles1 = 0, nftiles = 0, ngtab = 0, nptiles = 0, ndtiles = 0;
   int csize = CS;  // CTAs per cluster of the coarse-level kernel
+  CoarseTab tab{};   // phase tables of the cooperative coarse-level kernel
+  int coop_blocks = 0;
+  bool coop = true;  // the cooperative whole-grid coarse kernel (else one cluster per case)
   std::vector<FineCase> h_fc;
   cudaGraphExec_t chunk = nullptr;
   size_t chunk_nodes = 0;
@@ -967,6 +1207,19 @@ struct cfdg_batch {
 namespace {
 
 void launch_coarse(cfdg_batch* B, cudaStream_t s) {
+  if (B->coop) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)B->coop_blocks, 1, 1);
+    cfg.blockDim = dim3(512, 1, 1);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_coarse_all, (const CCase*)B->d_cc, (const MState*)B->d_st, B->tab);
+    return;
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(B->cases.size() * B->csize), 1, 1);
   cfg.blockDim = dim3(CT, 1, 1);
@@ -983,8 +1236,10 @@ void launch_coarse(cfdg_batch* B, cudaStream_t s) {
 
 void enqueue_vcycle(cfdg_batch* B, cudaStream_t s) {
   const int nt = B->ntiles;
-  k_v_rhs<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
-  if (B->ngtab) k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 0);
+  if (B->ngtab) {
+    k_v_rhs<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+    k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 0);
+  }
   // Two forward sweeps: red, black, red, black (the first red starts from x = 0).
   k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 0, 1);
   k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 1, 0);
@@ -1008,14 +1263,14 @@ void enqueue_vcycle(cfdg_batch* B, cudaStream_t s) {
 void enqueue_iteration(cfdg_batch* B, cudaStream_t s) {
   const int nt = B->ntiles;
   const int nc = (int)B->cases.size();
-  k_op<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
-  k_update<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  k_op<<<B->ndtiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_dtiles);
+  k_update<<<B->ndtiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_dtiles);
   k_outer<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
-  k_outer_resid<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  k_outer_resid<<<B->ndtiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_dtiles);
   k_scale<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
   k_start_state<<<(nc + 127) / 128, 128, 0, s>>>(B->d_st, nc);
   enqueue_vcycle(B, s);
-  k_rz<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  k_rz<<<B->ndtiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_dtiles);
   k_p<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
 }
 
@@ -1056,13 +1311,14 @@ int cfdg_mixed_pack(cfdg_batch* B) {
   cudaStream_t s = B->own;
   B->arena.release();
   B->arena.ctx = B->ctx;
-  std::vector<int2> tiles, tiles1, ftiles, gtab, ptiles;
+  std::vector<int2> tiles, tiles1, ftiles, gtab, ptiles, dtiles;
   B->h_fc.clear();
   std::vector<CCase> cc;
   for (size_t i = 0; i < B->cases.size(); ++i) {
     FineCase F = B->cases[i]->F;
     F.tile0 = (int)tiles.size();
-    for (int t = 0; t < F.ntiles; ++t) tiles.push_back(make_int2((int)i, t));
+    for (int t = 0; t < (F.N + TILE - 1) / TILE; ++t) tiles.push_back(make_int2((int)i, t));
+    for (int t = 0; t < F.ntiles; ++t) dtiles.push_back(make_int2((int)i, t));
     for (int t = 0; t < (F.n1 + TILE - 1) / TILE; ++t) tiles1.push_back(make_int2((int)i, t));
     for (int t = 0; t < (F.npairs + TILE - 1) / TILE; ++t) ptiles.push_back(make_int2((int)i, t));
     F.ftile0 = (int)ftiles.size();
@@ -1077,8 +1333,83 @@ int cfdg_mixed_pack(cfdg_batch* B) {
   B->nftiles = (int)ftiles.size();
   B->ngtab = (int)gtab.size();
   B->nptiles = (int)ptiles.size();
+  B->ndtiles = (int)dtiles.size();
   Arena& A = B->arena;
+  if (int e = A.upload(&B->d_dtiles, dtiles, s)) return e;
   if (int e = A.upload(&B->d_ptiles, ptiles, s)) return e;
+  // Phase tables of the cooperative coarse-level kernel.
+  {
+    const int nc = (int)B->cases.size();
+    int nlev = 0;
+    for (auto& c : B->cases) nlev = std::max(nlev, c->C.nl);
+    CoarseTab T{};
+    T.nc = nc;
+    T.nlev = nlev;
+    std::vector<int32_t> rows, term, fwd, bwd, next, live, grp;
+    auto prefix = [&](std::vector<int32_t>& v, auto count) {
+      int acc = 0;
+      v.push_back(0);
+      for (int i = 0; i < nc; ++i) {
+        acc += count(i);
+        v.push_back(acc);
+      }
+    };
+    for (int l = 0; l < nlev; ++l) {
+      int maxc = 0, anyg = 0;
+      for (auto& c : B->cases)
+        if (l < c->C.nl) {
+          const CLev& L = c->C.lv[l];
+          if (!L.terminal) maxc = std::max(maxc, L.ncolors);
+          anyg |= L.ngroups > 0;
+        }
+      if (maxc > MAXC) return fail(CFDG_ERR_UNSUPPORTED, "mixed form: too many colours on a coarse level");
+      T.maxc[l] = maxc;
+      T.anyg[l] = anyg;
+      auto lev = [&](int i) -> const CLev* { return l < B->cases[i]->C.nl ? &B->cases[i]->C.lv[l] : nullptr; };
+      prefix(rows, [&](int i) { return lev(i) ? lev(i)->n : 0; });
+      prefix(term, [&](int i) { return lev(i) && lev(i)->terminal ? lev(i)->nblocks : 0; });
+      prefix(next, [&](int i) { return lev(i) && !lev(i)->terminal ? B->cases[i]->C.lv[l + 1].n : 0; });
+      prefix(live, [&](int i) { return lev(i) && !lev(i)->terminal ? lev(i)->n : 0; });
+      prefix(grp, [&](int i) { return lev(i) ? lev(i)->ngroups : 0; });
+      for (int c = 0; c < MAXC; ++c) {
+        prefix(fwd, [&](int i) {
+          const CLev* L = lev(i);
+          if (!L || L->terminal || c >= L->ncolors) return 0;
+          return B->cases[i]->colors[l][c + 1] - B->cases[i]->colors[l][c];
+        });
+        prefix(bwd, [&](int i) {
+          const CLev* L = lev(i);
+          if (!L || L->terminal || c >= L->ncolors) return 0;
+          const int cb = L->ncolors - 1 - c;
+          return B->cases[i]->colors[l][cb + 1] - B->cases[i]->colors[l][cb];
+        });
+      }
+    }
+    int *d;
+    if (int e = A.upload(&d, rows, s)) return e;
+    T.rows = d;
+    if (int e = A.upload(&d, term, s)) return e;
+    T.term = d;
+    if (int e = A.upload(&d, fwd, s)) return e;
+    T.fwd = d;
+    if (int e = A.upload(&d, bwd, s)) return e;
+    T.bwd = d;
+    if (int e = A.upload(&d, next, s)) return e;
+    T.next = d;
+    if (int e = A.upload(&d, live, s)) return e;
+    T.live = d;
+    if (int e = A.upload(&d, grp, s)) return e;
+    T.grp = d;
+    B->tab = T;
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_coarse_all, 512, 0) != cudaSuccess || per < 1) {
+      cudaGetLastError();
+      B->coop = false;
+    }
+    B->coop_blocks = sms * std::min(per, 2);
+  }
   // Coarse-level clusters: 16 CTAs when the device allows that non-portable size, else 8.
   B->csize = CS;
   if (cudaFuncSetAttribute(k_coarse, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
@@ -1173,7 +1504,7 @@ int cfdg_mixed_project(cfdg_batch* B, double* const* d_u, double* const* d_p, co
       MState f = st[i];
       CU(cudaMemcpyAsync(&B->d_st[i], &f, sizeof(MState), cudaMemcpyHostToDevice, s));
     }
-  k_norm<<<B->ntiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  k_norm<<<B->ndtiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_dtiles);
   count();
   CU(cudaGetLastError());
   Poller P;
@@ -1342,7 +1673,7 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
         k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 1, 0);
         break;
       case 1:  // FP32 operator q = A p (with p.q)
-        k_op<<<B->ntiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+        k_op<<<B->ndtiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_dtiles);
         break;
       case 2:  // all coarse levels, one cluster per case
         launch_coarse(B, s);
