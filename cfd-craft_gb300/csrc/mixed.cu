@@ -123,6 +123,8 @@ struct CLev {
   const double* fac;
 };
 
+static_assert(sizeof(CLev) % 8 == 0, "CLev is copied to shared memory in 8-byte words");
+
 struct CCase {
   int nl;  // levels 1 .. nl (lv[0] is level 1)
   CLev lv[MAXL];
@@ -242,6 +244,12 @@ __device__ __forceinline__ double op64(const FineCase& F, const double* __restri
 }
 
 // ----------------------------------------------------------------- fine-level kernels
+// Fine-level kernels run over row tiles: tile (case, rt) holds the x-rows
+// [rt*RT, rt*RT + RT) of that case's grid, i.e. the cells [rt*RT*nx, (rt*RT+RT)*nx).
+// Stencil kernels give each warp one row (no index divisions per cell); element-wise
+// kernels stride the tile's cells. Reductions keep one partial per row tile.
+constexpr int RT = TILE / 32;  // rows per tile: one warp per row
+
 #define FINE_PROLOGUE(STATE_TEST)                                                     \
   const int2 t = tiles[blockIdx.x];                                                   \
   MState& S = ST[t.x];                                                                \
@@ -256,11 +264,24 @@ __device__ __forceinline__ double op64(const FineCase& F, const double* __restri
   __syncthreads();                                                                    \
   const FineCase& F = sF;                                                             \
   const int lt = t.y;                                                                 \
-  const int c = lt * TILE + threadIdx.x;                                              \
-  const bool ok = c < F.N;
+  const int nx_ = F.n[0];                                                             \
+  const int cb = lt * RT * nx_;                                                       \
+  const int ce = min(F.N, cb + RT * nx_);                                             \
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;                         \
+  (void)cb;                                                                           \
+  (void)ce;                                                                           \
+  (void)warp;                                                                         \
+  (void)lane;
 
-// Reduction kernels cover DOT cells per block, DOT / TILE per thread (cell c0 + r*TILE).
-constexpr int DOT = 4 * TILE;
+// The row of this warp: returns false when the tile has fewer rows.
+__device__ __forceinline__ bool warp_row(const FineCase& F, int lt, int warp, int& j, int& k, int& rowbase) {
+  const int r = lt * RT + warp;
+  if (r >= F.n[1] * F.n[2]) return false;
+  j = r % F.n[1];
+  k = r / F.n[1];
+  rowbase = r * F.n[0];
+  return true;
+}
 
 // FP32 error-free transformations: a running sum (hi, lo) of exact products keeps
 // about twice the FP32 significand, so a thread's few terms convert to FP64 once.
@@ -274,21 +295,46 @@ __device__ __forceinline__ void dd_add_prod(float a, float b, float& hi, float& 
   lo += se + pe;
 }
 
+// FP32 operator at cell c = rowbase + i of row (j, k).
+__device__ __forceinline__ float op32r(const FineCase& F, const float* __restrict__ x, int c, int i, int j, int k,
+                                       unsigned fl) {
+  if (!(fl & 0x0fffu)) return 0.0f;
+  const int stride[3] = {1, F.n[0], F.n[0] * F.n[1]};
+  const int q[3] = {i, j, k};
+  const float xc = x[c];
+  float y = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      const unsigned ib = 1u << (2 * a + side), ob = 1u << (6 + 2 * a + side);
+      if (!(fl & (ib | ob))) continue;
+      float w;
+      if (F.uniform) {
+        w = (fl & ib) ? F.w32[a] : F.wo32[a];
+      } else {
+        int p[3] = {q[0], q[1], q[2]};
+        p[a] += side;
+        w = F.fw32[fidx(F, a, p[0], p[1], p[2])];
+      }
+      if (fl & ib) y = fmaf(w, xc - x[side ? c + stride[a] : c - stride[a]], y);
+      else y = fmaf(w, xc, y);
+    }
+  return y;
+}
+
 // A: q = A32 p, alpha = rz / (p.q) (E032 when not positive).
 __global__ void __launch_bounds__(TILE) k_op(const FineCase* FC, MState* ST, const int2* tiles) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN)
-  (void)c;
-  (void)ok;
   float hi = 0.0f, lo = 0.0f;
-#pragma unroll
-  for (int r = 0; r < DOT / TILE; ++r) {
-    const int cc = lt * DOT + r * TILE + threadIdx.x;
-    if (cc < F.N) {
-      const float pv = F.p[cc];
-      const float v = op32(F, F.p, cc, F.flags[cc]);
-      F.q[cc] = v;
-      dd_add_prod(pv, v, hi, lo);
+  int j, k, rb;
+  if (warp_row(F, lt, warp, j, k, rb)) {
+    for (int i = lane; i < nx_; i += 32) {
+      const int c = rb + i;
+      const float v = op32r(F, F.p, c, i, j, k, F.flags[c]);
+      F.q[c] = v;
+      dd_add_prod(F.p[c], v, hi, lo);
     }
   }
   double pq;
@@ -306,53 +352,40 @@ __global__ void __launch_bounds__(TILE) k_op(const FineCase* FC, MState* ST, con
 __global__ void __launch_bounds__(TILE) k_update(const FineCase* FC, MState* ST, const int2* tiles) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN)
-  (void)c;
-  (void)ok;
   const float alpha = (float)S.alpha;
   float hi = 0.0f, lo = 0.0f;
-#pragma unroll
-  for (int rr = 0; rr < DOT / TILE; ++rr) {
-    const int cc = lt * DOT + rr * TILE + threadIdx.x;
-    if (cc < F.N) {
-      F.e[cc] = fmaf(alpha, F.p[cc], F.e[cc]);
-      const float r = fmaf(-alpha, F.q[cc], F.r32[cc]);
-      F.r32[cc] = r;
-      dd_add_prod(r, r, hi, lo);
-    }
+  for (int c = cb + threadIdx.x; c < ce; c += TILE) {
+    F.e[c] = fmaf(alpha, F.p[c], F.e[c]);
+    const float r = fmaf(-alpha, F.q[c], F.r32[c]);
+    F.r32[c] = r;
+    dd_add_prod(r, r, hi, lo);
   }
-  double rr2;
-  if (case_reduce((double)hi + (double)lo, F, S, lt, sh, &rr2) && threadIdx.x == 0) {
+  double rr;
+  if (case_reduce((double)hi + (double)lo, F, S, lt, sh, &rr) && threadIdx.x == 0) {
     S.inner_it += 1;
     S.total_it += 1;
     S.has_e = 1;
-    if (sqrt(rr2) <= S.inner_tol || S.inner_it >= S.max_inner || S.total_it >= S.max_it) S.state = OUTER;
+    if (sqrt(rr) <= S.inner_tol || S.inner_it >= S.max_inner || S.total_it >= S.max_it) S.state = OUTER;
   }
 }
 
-// C1: x += |r| e; r = b_c - A x in FP64; the true residual decides convergence.
+// C1: x += |r| e (the residual is formed by k_outer_resid once every block has updated x).
 __global__ void __launch_bounds__(TILE) k_outer(const FineCase* FC, MState* ST, const int2* tiles) {
-  __shared__ double sh[32];
   FINE_PROLOGUE(S.state == OUTER)
-  // The update of x must be complete in every block before A x is formed: this
-  // kernel only updates x; k_outer_resid forms the residual.
-  if (ok && S.has_e) F.x64[c] = F.x64[c] + S.scale * (double)F.e[c];
-  (void)sh;
+  if (!S.has_e) return;
+  const double scale = S.scale;
+  for (int c = cb + threadIdx.x; c < ce; c += TILE) F.x64[c] = F.x64[c] + scale * (double)F.e[c];
 }
 
+// r = b_c - A x in FP64; the true residual decides convergence.
 __global__ void __launch_bounds__(TILE) k_outer_resid(const FineCase* FC, MState* ST, const int2* tiles) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == OUTER)
-  (void)c;
-  (void)ok;
   double acc = 0.0;
-#pragma unroll
-  for (int r = 0; r < DOT / TILE; ++r) {
-    const int cc = lt * DOT + r * TILE + threadIdx.x;
-    if (cc < F.N) {
-      const double v = __dsub_rn(F.bc[cc], op64(F, F.x64, cc, F.flags[cc]));
-      F.r64[cc] = v;
-      acc = __fma_rn(v, v, acc);
-    }
+  for (int c = cb + threadIdx.x; c < ce; c += TILE) {
+    const double v = __dsub_rn(F.bc[c], op64(F, F.x64, c, F.flags[c]));
+    F.r64[c] = v;
+    acc = __fma_rn(v, v, acc);
   }
   double rr;
   if (case_reduce(acc, F, S, lt, sh, &rr) && threadIdx.x == 0) {
@@ -374,8 +407,9 @@ __global__ void __launch_bounds__(TILE) k_outer_resid(const FineCase* FC, MState
 // C2: r32 = r / |r|, e = 0.
 __global__ void __launch_bounds__(TILE) k_scale(const FineCase* FC, MState* ST, const int2* tiles) {
   FINE_PROLOGUE(S.state == SCALE)
-  if (ok) {
-    F.r32[c] = (float)(F.r64[c] / S.scale);
+  const double inv = 1.0 / S.scale;
+  for (int c = cb + threadIdx.x; c < ce; c += TILE) {
+    F.r32[c] = (float)(F.r64[c] * inv);
     F.e[c] = 0.0f;
   }
 }
@@ -392,14 +426,8 @@ __global__ void k_start_state(MState* ST, int n) {
 __global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, const int2* tiles) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN || S.state == START)
-  (void)c;
-  (void)ok;
   float hi = 0.0f, lo = 0.0f;
-#pragma unroll
-  for (int r = 0; r < DOT / TILE; ++r) {
-    const int cc = lt * DOT + r * TILE + threadIdx.x;
-    if (cc < F.N) dd_add_prod(F.r32[cc], F.x0[cc], hi, lo);
-  }
+  for (int c = cb + threadIdx.x; c < ce; c += TILE) dd_add_prod(F.r32[c], F.x0[c], hi, lo);
   double rz;
   if (case_reduce((double)hi + (double)lo, F, S, lt, sh, &rz) && threadIdx.x == 0) {
     if (S.state == START) {
@@ -415,49 +443,94 @@ __global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, con
 // G: p = z + beta p (z is the V-cycle's level-0 solution x0).
 __global__ void __launch_bounds__(TILE) k_p(const FineCase* FC, MState* ST, const int2* tiles) {
   FINE_PROLOGUE(S.state == RUN)
-  if (ok) F.p[c] = S.beta == 0.0 ? F.x0[c] : fmaf((float)S.beta, F.p[c], F.x0[c]);
+  const float beta = (float)S.beta;
+  if (S.beta == 0.0) {
+    for (int c = cb + threadIdx.x; c < ce; c += TILE) F.p[c] = F.x0[c];
+  } else {
+    for (int c = cb + threadIdx.x; c < ce; c += TILE) F.p[c] = fmaf(beta, F.p[c], F.x0[c]);
+  }
 }
 
 // ----------------------------------------------------------------- V-cycle, level 0
-// rhs0 = r32.
+// rhs0 = r32 (only when level 0 has closed groups; otherwise rhs0 is r32 itself).
 __global__ void __launch_bounds__(TILE) k_v_rhs(const FineCase* FC, MState* ST, const int2* tiles) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
-  if (ok && F.rhs0 != F.r32) F.rhs0[c] = F.r32[c];
+  if (F.rhs0 == F.r32) return;
+  for (int c = cb + threadIdx.x; c < ce; c += TILE) F.rhs0[c] = F.r32[c];
 }
 
-// Red-black Gauss-Seidel half sweep on level 0: cells with (i+j+k)%2 == color. Work
-// item p is the pair of cells (2m, 2m+1) of one x-row, of which exactly one has the
-// colour. first: x is taken as zero (the cycle's initial guess). Cells outside the
-// operator (solid, sealed singletons) are kept at zero. Tiles index pairs.
+// Red-black Gauss-Seidel half sweep on level 0: cells with (i+j+k)%2 == color. Lanes
+// walk the x-pairs (2m, 2m+1) of the warp's row, of which exactly one has the colour.
+// first: x is taken as zero (the cycle's initial guess). Cells outside the operator
+// (solid, sealed singletons) are kept at zero.
 __global__ void __launch_bounds__(TILE) k_rb(const FineCase* FC, MState* ST, const int2* tiles, int color, int first) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
-  (void)ok;
-  const int nx = F.n[0], ny = F.n[1];
-  const int pr = lt * TILE + threadIdx.x;
-  if (pr >= F.npairs) return;
-  const int px = (nx + 1) >> 1;
-  const int row = pr / px, m = pr - row * px;
-  const int j = row % ny, k = row / ny;
-  const int i = 2 * m + ((j + k + color) & 1);
-  if (i >= nx) return;
-  const int cc = row * nx + i;
+  int j, k, rb;
+  if (!warp_row(F, lt, warp, j, k, rb)) return;
+  const int px = (nx_ + 1) >> 1;
+  const int par = (j + k + color) & 1;
   float* __restrict__ x = F.x0;
-  const float id = F.idiag0[cc];
-  if (id == 0.0f) {
-    x[cc] = 0.0f;
-    return;
+  const int sy = nx_, sz = nx_ * F.n[1];
+  for (int m = lane; m < px; m += 32) {
+    const int i = 2 * m + par;
+    if (i >= nx_) break;
+    const int cc = rb + i;
+    const float id = F.idiag0[cc];
+    if (id == 0.0f) {
+      x[cc] = 0.0f;
+      continue;
+    }
+    float v = F.rhs0[cc];
+    if (!(first && color == 0)) {
+      const unsigned fl = F.flags[cc];
+      if (F.uniform) {
+        if (fl & 1u) v = fmaf(F.w32[0], x[cc - 1], v);
+        if (fl & 2u) v = fmaf(F.w32[0], x[cc + 1], v);
+        if (fl & 4u) v = fmaf(F.w32[1], x[cc - sy], v);
+        if (fl & 8u) v = fmaf(F.w32[1], x[cc + sy], v);
+        if (fl & 16u) v = fmaf(F.w32[2], x[cc - sz], v);
+        if (fl & 32u) v = fmaf(F.w32[2], x[cc + sz], v);
+      } else {
+        const int q[3] = {i, j, k};
+        const int stride[3] = {1, sy, sz};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int side = 0; side < 2; ++side) {
+            if (!(fl & (1u << (2 * a + side)))) continue;
+            int pp[3] = {q[0], q[1], q[2]};
+            pp[a] += side;
+            v = fmaf(F.fw32[fidx(F, a, pp[0], pp[1], pp[2])], x[side ? cc + stride[a] : cc - stride[a]], v);
+          }
+      }
+    }
+    x[cc] = v * id;
   }
-  float v = F.rhs0[cc];
-  if (!(first && color == 0)) {
+}
+
+// res0 = rhs0 - A0 x0 (A0 = diag - sum w on interior faces).
+__global__ void __launch_bounds__(TILE) k_v_resid(const FineCase* FC, MState* ST, const int2* tiles) {
+  FINE_PROLOGUE(S.state == RUN || S.state == START)
+  int j, k, rb;
+  if (!warp_row(F, lt, warp, j, k, rb)) return;
+  const int sy = nx_, sz = nx_ * F.n[1];
+  const float* __restrict__ x = F.x0;
+  for (int i = lane; i < nx_; i += 32) {
+    const int cc = rb + i;
+    const float d = F.diag0[cc];
+    if (d == 0.0f) {
+      F.res0[cc] = 0.0f;
+      continue;
+    }
     const unsigned fl = F.flags[cc];
-    const int sy = nx, sz = nx * ny;
+    float v = d * x[cc];
     if (F.uniform) {
-      if (fl & 1u) v = fmaf(F.w32[0], x[cc - 1], v);
-      if (fl & 2u) v = fmaf(F.w32[0], x[cc + 1], v);
-      if (fl & 4u) v = fmaf(F.w32[1], x[cc - sy], v);
-      if (fl & 8u) v = fmaf(F.w32[1], x[cc + sy], v);
-      if (fl & 16u) v = fmaf(F.w32[2], x[cc - sz], v);
-      if (fl & 32u) v = fmaf(F.w32[2], x[cc + sz], v);
+      if (fl & 1u) v = fmaf(-F.w32[0], x[cc - 1], v);
+      if (fl & 2u) v = fmaf(-F.w32[0], x[cc + 1], v);
+      if (fl & 4u) v = fmaf(-F.w32[1], x[cc - sy], v);
+      if (fl & 8u) v = fmaf(-F.w32[1], x[cc + sy], v);
+      if (fl & 16u) v = fmaf(-F.w32[2], x[cc - sz], v);
+      if (fl & 32u) v = fmaf(-F.w32[2], x[cc + sz], v);
     } else {
       const int q[3] = {i, j, k};
       const int stride[3] = {1, sy, sz};
@@ -466,45 +539,13 @@ __global__ void __launch_bounds__(TILE) k_rb(const FineCase* FC, MState* ST, con
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
           if (!(fl & (1u << (2 * a + side)))) continue;
-          int p[3] = {q[0], q[1], q[2]};
-          p[a] += side;
-          v = fmaf(F.fw32[fidx(F, a, p[0], p[1], p[2])], x[side ? cc + stride[a] : cc - stride[a]], v);
+          int pp[3] = {q[0], q[1], q[2]};
+          pp[a] += side;
+          v = fmaf(-F.fw32[fidx(F, a, pp[0], pp[1], pp[2])], x[side ? cc + stride[a] : cc - stride[a]], v);
         }
     }
+    F.res0[cc] = F.rhs0[cc] - v;
   }
-  x[cc] = v * id;
-}
-
-// res0 = rhs0 - A0 x0 (A0 = diag - sum w on interior faces).
-__global__ void __launch_bounds__(TILE) k_v_resid(const FineCase* FC, MState* ST, const int2* tiles) {
-  FINE_PROLOGUE(S.state == RUN || S.state == START)
-  if (!ok) return;
-  const float d = F.diag0[c];
-  if (d == 0.0f) {
-    F.res0[c] = 0.0f;
-    return;
-  }
-  const unsigned fl = F.flags[c];
-  int q[3];
-  coords(F, c, q[0], q[1], q[2]);
-  const int stride[3] = {1, F.n[0], F.n[0] * F.n[1]};
-  float v = d * F.x0[c];
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int side = 0; side < 2; ++side) {
-      if (!(fl & (1u << (2 * a + side)))) continue;
-      float w;
-      if (F.uniform) {
-        w = F.w32[a];
-      } else {
-        int p[3] = {q[0], q[1], q[2]};
-        p[a] += side;
-        w = F.fw32[fidx(F, a, p[0], p[1], p[2])];
-      }
-      v = fmaf(-w, F.x0[side ? c + stride[a] : c - stride[a]], v);
-    }
-  F.res0[c] = F.rhs0[c] - v;
 }
 
 // rhs1 = R res0: level-1 rows gather their level-0 children. Tiles index level-1 rows.
@@ -523,12 +564,13 @@ __global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState*
 // x0 += P x1.
 __global__ void __launch_bounds__(TILE) k_v_prolong(const FineCase* FC, MState* ST, const int2* tiles) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
-  if (!ok) return;
-  const int b = F.p_off[c], e = F.p_off[c + 1];
-  if (b == e) return;
-  float s = 0.0f;
-  for (int k = b; k < e; ++k) s = fmaf(F.p_w[k], F.x1[F.p_col[k]], s);
-  F.x0[c] += s;
+  for (int c = cb + threadIdx.x; c < ce; c += TILE) {
+    const int b = F.p_off[c], e = F.p_off[c + 1];
+    if (b == e) continue;
+    float sum = 0.0f;
+    for (int kk = b; kk < e; ++kk) sum = fmaf(F.p_w[kk], F.x1[F.p_col[kk]], sum);
+    F.x0[c] += sum;
+  }
 }
 
 // Gauge of level-0 closed groups: one block per (case, group); members strided.
@@ -714,16 +756,33 @@ __device__ __forceinline__ bool active(const MState* ST, int ci) {
   return st == RUN || st == START;
 }
 
+// The descriptors of the current level (sl[0..nc)) and of the next (sl[nc..2nc)) are
+// copied into shared memory at each level, so the phases read them without global
+// round trips.
+__device__ void load_levels(const CCase* cases, int nc, int l, int nlev_max, CLev* sl) {
+  __syncthreads();
+  const int words = (int)(sizeof(CLev) / 8);
+  for (int w = threadIdx.x; w < 2 * nc * words; w += blockDim.x) {
+    const int which = w / (nc * words), rem = w % (nc * words);
+    const int ci = rem / words, k = rem % words;
+    const int lev = l + which;
+    long long v = 0;
+    if (lev < nlev_max) v = reinterpret_cast<const long long*>(&cases[ci].lv[lev])[k];
+    reinterpret_cast<long long*>(&sl[which * nc + ci])[k] = v;
+  }
+  __syncthreads();
+}
+
 // Subtracts each closed group's mean, one CTA per (case, group) pair.
-__device__ void g_center(const CCase* cases, const MState* ST, const CoarseTab& T, int l, int which,
-                         double* sh, cg::grid_group& grid) {
+__device__ void g_center(const CLev* sl, const MState* ST, const CoarseTab& T, int l, int which, double* sh,
+                         cg::grid_group& grid) {
   const int* off = T.grp + l * (T.nc + 1);
   const int total = __ldg(&off[T.nc]);
   __shared__ float mean;
   for (int t = blockIdx.x; t < total; t += gridDim.x) {
     const int ci = find_case(off, T.nc, t);
     if (!active(ST, ci)) continue;
-    const CLev& L = cases[ci].lv[l];
+    const CLev& L = sl[ci];
     float* v = which == 0 ? L.rhs : (which == 1 ? L.x : L.res);
     const int g = t - off[ci];
     const int b = L.goff[g], e = L.goff[g + 1];
@@ -739,7 +798,7 @@ __device__ void g_center(const CCase* cases, const MState* ST, const CoarseTab& 
   grid.sync();
 }
 
-__device__ void g_sweep(const CCase* cases, const MState* ST, const CoarseTab& T, int l, bool backward,
+__device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, int l, bool backward,
                         cg::grid_group& grid) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
   for (int cc = 0; cc < T.maxc[l]; ++cc) {
@@ -748,17 +807,29 @@ __device__ void g_sweep(const CCase* cases, const MState* ST, const CoarseTab& T
     for (int t = gt; t < total; t += nth) {
       const int ci = find_case(off, T.nc, t);
       if (!active(ST, ci)) continue;
-      const CLev& L = cases[ci].lv[l];
+      const CLev& L = sl[ci];
       const int color = backward ? L.ncolors - 1 - cc : cc;
-      const int k = t - off[ci];
-      const int nrow = L.coff[color + 1] - L.coff[color];
-      const int i = L.crows[L.coff[color] + k];
+      const int k = t - __ldg(&off[ci]);
+      const int c0 = L.coff[color];
+      const int nrow = L.coff[color + 1] - c0;
+      const int i = L.crows[c0 + k];
       const int base = L.ell_off[color], w = L.ell_w[color];
       float v = __ldcg(&L.rhs[i]);
-      for (int a = 0; a < w; ++a) {
-        const int e = base + a * nrow + k;
-        v = fmaf(-L.ell_val[e], __ldcg(&L.x[L.ell_col[e]]), v);
+      const int* ec = L.ell_col + base + k;
+      const float* ev = L.ell_val + base + k;
+      int a = 0;
+      for (; a + 4 <= w; a += 4) {
+        const int c_0 = ec[(a + 0) * nrow], c_1 = ec[(a + 1) * nrow], c_2 = ec[(a + 2) * nrow],
+                  c_3 = ec[(a + 3) * nrow];
+        const float v0 = ev[(a + 0) * nrow], v1 = ev[(a + 1) * nrow], v2 = ev[(a + 2) * nrow],
+                    v3 = ev[(a + 3) * nrow];
+        const float x0 = __ldcg(&L.x[c_0]), x1 = __ldcg(&L.x[c_1]), x2 = __ldcg(&L.x[c_2]), x3 = __ldcg(&L.x[c_3]);
+        v = fmaf(-v0, x0, v);
+        v = fmaf(-v1, x1, v);
+        v = fmaf(-v2, x2, v);
+        v = fmaf(-v3, x3, v);
       }
+      for (; a < w; ++a) v = fmaf(-ev[a * nrow], __ldcg(&L.x[ec[a * nrow]]), v);
       L.x[i] = v * L.idiag[i];
     }
     grid.sync();
@@ -767,29 +838,32 @@ __device__ void g_sweep(const CCase* cases, const MState* ST, const CoarseTab& T
 
 __global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MState* ST, CoarseTab T) {
   __shared__ double sh[32];
+  extern __shared__ __align__(16) unsigned char smem[];
+  CLev* sl = reinterpret_cast<CLev*>(smem);
   cg::grid_group grid = cg::this_grid();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
   const int nc = T.nc;
   for (int l = 0; l < T.nlev; ++l) {
-    if (T.anyg[l]) g_center(cases, ST, T, l, 0, sh, grid);
+    load_levels(cases, nc, l, MAXL, sl);
+    if (T.anyg[l]) g_center(sl, ST, T, l, 0, sh, grid);
     {
       const int* off = T.rows + l * (nc + 1);
-      for (int t = gt; t < off[nc]; t += nth) {
+      for (int t = gt; t < __ldg(&off[nc]); t += nth) {
         const int ci = find_case(off, nc, t);
-        if (active(ST, ci)) cases[ci].lv[l].x[t - off[ci]] = 0.0f;
+        if (active(ST, ci)) sl[ci].x[t - __ldg(&off[ci])] = 0.0f;
       }
     }
     grid.sync();
     {
       // Terminal levels: FP64 dense Cholesky solves, one warp per block (lane 0 works).
       const int* off = T.term + l * (nc + 1);
-      const int warp = gt >> 5, nw = nth >> 5;
+      const int wp = gt >> 5, nw = nth >> 5;
       if ((threadIdx.x & 31) == 0)
-        for (int t = warp; t < off[nc]; t += nw) {
+        for (int t = wp; t < __ldg(&off[nc]); t += nw) {
           const int ci = find_case(off, nc, t);
           if (!active(ST, ci)) continue;
-          const CLev& L = cases[ci].lv[l];
-          const int bk = t - off[ci];
+          const CLev& L = sl[ci];
+          const int bk = t - __ldg(&off[ci]);
           const int* ix = L.idx + L.ioff[bk];
           const int n = L.ioff[bk + 1] - L.ioff[bk];
           const double* f = L.fac + L.foff[bk];
@@ -808,31 +882,31 @@ __global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MS
         }
     }
     grid.sync();
-    g_sweep(cases, ST, T, l, false, grid);
-    g_sweep(cases, ST, T, l, false, grid);
-    if (T.anyg[l]) g_center(cases, ST, T, l, 1, sh, grid);
+    g_sweep(sl, ST, T, l, false, grid);
+    g_sweep(sl, ST, T, l, false, grid);
+    if (T.anyg[l]) g_center(sl, ST, T, l, 1, sh, grid);
     {
       const int* off = T.live + l * (nc + 1);
-      for (int t = gt; t < off[nc]; t += nth) {
+      for (int t = gt; t < __ldg(&off[nc]); t += nth) {
         const int ci = find_case(off, nc, t);
         if (!active(ST, ci)) continue;
-        const CLev& L = cases[ci].lv[l];
-        const int i = t - off[ci];
+        const CLev& L = sl[ci];
+        const int i = t - __ldg(&off[ci]);
         float v = L.diag[i] * __ldcg(&L.x[i]);
         for (int a = L.off[i]; a < L.off[i + 1]; ++a) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
         L.res[i] = __ldcg(&L.rhs[i]) - v;
       }
     }
     grid.sync();
-    if (T.anyg[l]) g_center(cases, ST, T, l, 2, sh, grid);
+    if (T.anyg[l]) g_center(sl, ST, T, l, 2, sh, grid);
     {
       const int* off = T.next + l * (nc + 1);
-      for (int t = gt; t < off[nc]; t += nth) {
+      for (int t = gt; t < __ldg(&off[nc]); t += nth) {
         const int ci = find_case(off, nc, t);
         if (!active(ST, ci)) continue;
-        const CLev& L = cases[ci].lv[l];
-        const CLev& N = cases[ci].lv[l + 1];
-        const int j = t - off[ci];
+        const CLev& L = sl[ci];
+        const CLev& N = sl[nc + ci];
+        const int j = t - __ldg(&off[ci]);
         float v = 0.0f;
         for (int k = L.roff[j]; k < L.roff[j + 1]; ++k) v = fmaf(L.rw[k], __ldcg(&L.res[L.rchild[k]]), v);
         N.rhs[j] = v;
@@ -841,23 +915,24 @@ __global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MS
     grid.sync();
   }
   for (int l = T.nlev - 2; l >= 0; --l) {
+    load_levels(cases, nc, l, MAXL, sl);
     {
       const int* off = T.live + l * (nc + 1);
-      for (int t = gt; t < off[nc]; t += nth) {
+      for (int t = gt; t < __ldg(&off[nc]); t += nth) {
         const int ci = find_case(off, nc, t);
         if (!active(ST, ci)) continue;
-        const CLev& L = cases[ci].lv[l];
-        const CLev& N = cases[ci].lv[l + 1];
-        const int i = t - off[ci];
+        const CLev& L = sl[ci];
+        const CLev& N = sl[nc + ci];
+        const int i = t - __ldg(&off[ci]);
         float s = 0.0f;
         for (int k = L.poff[i]; k < L.poff[i + 1]; ++k) s = fmaf(L.pw[k], __ldcg(&N.x[L.pcol[k]]), s);
         L.x[i] = __ldcg(&L.x[i]) + s;
       }
     }
     grid.sync();
-    g_sweep(cases, ST, T, l, true, grid);
-    g_sweep(cases, ST, T, l, true, grid);
-    if (T.anyg[l]) g_center(cases, ST, T, l, 1, sh, grid);
+    g_sweep(sl, ST, T, l, true, grid);
+    g_sweep(sl, ST, T, l, true, grid);
+    if (T.anyg[l]) g_center(sl, ST, T, l, 1, sh, grid);
   }
 }
 
@@ -865,44 +940,41 @@ __global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MS
 // b = -div(u)/dt, terms (pressure.rs:440-459), rounded as written.
 __global__ void __launch_bounds__(TILE) k_rhs(const FineCase* FC, MState* ST, const int2* tiles) {
   FINE_PROLOGUE(S.state == IDLE)
-  if (!ok) return;
-  if (!F.fluid[c]) {
-    F.b[c] = -0.0;
-    F.terms[c] = 0.0;
-    return;
-  }
-  int q[3];
-  coords(F, c, q[0], q[1], q[2]);
-  double div = 0.0, scale = 0.0;
+  int j, k, rb;
+  if (!warp_row(F, lt, warp, j, k, rb)) return;
+  for (int i = lane; i < nx_; i += 32) {
+    const int c = rb + i;
+    if (!F.fluid[c]) {
+      F.b[c] = -0.0;
+      F.terms[c] = 0.0;
+      continue;
+    }
+    const int q[3] = {i, j, k};
+    double div = 0.0, scale = 0.0;
 #pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    int p[3] = {q[0], q[1], q[2]};
-    const double ul = F.u[fidx(F, a, p[0], p[1], p[2])];
-    p[a] += 1;
-    const double uu = F.u[fidx(F, a, p[0], p[1], p[2])];
-    div = __dadd_rn(div, __ddiv_rn(__dsub_rn(uu, ul), F.dx[a]));
-    scale = __dadd_rn(scale, __ddiv_rn(__dadd_rn(fabs(ul), fabs(uu)), F.dx[a]));
+    for (int a = 0; a < 3; ++a) {
+      int p[3] = {q[0], q[1], q[2]};
+      const double ul = F.u[fidx(F, a, p[0], p[1], p[2])];
+      p[a] += 1;
+      const double uu = F.u[fidx(F, a, p[0], p[1], p[2])];
+      div = __dadd_rn(div, __ddiv_rn(__dsub_rn(uu, ul), F.dx[a]));
+      scale = __dadd_rn(scale, __ddiv_rn(__dadd_rn(fabs(ul), fabs(uu)), F.dx[a]));
+    }
+    F.b[c] = __ddiv_rn(-div, F.dt);
+    F.terms[c] = __ddiv_rn(scale, F.dt);
   }
-  F.b[c] = __ddiv_rn(-div, F.dt);
-  F.terms[c] = __ddiv_rn(scale, F.dt);
 }
 
 // |b_c| (after the host-side gauge of closed components); x = 0.
 __global__ void __launch_bounds__(TILE) k_norm(const FineCase* FC, MState* ST, const int2* tiles) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == IDLE)
-  (void)c;
-  (void)ok;
   double acc = 0.0;
-#pragma unroll
-  for (int r = 0; r < DOT / TILE; ++r) {
-    const int cc = lt * DOT + r * TILE + threadIdx.x;
-    if (cc < F.N) {
-      const double v = F.bc[cc];
-      acc = __fma_rn(v, v, acc);
-      F.x64[cc] = 0.0;
-      F.e[cc] = 0.0f;
-    }
+  for (int c = cb + threadIdx.x; c < ce; c += TILE) {
+    const double v = F.bc[c];
+    acc = __fma_rn(v, v, acc);
+    F.x64[c] = 0.0;
+    F.e[c] = 0.0f;
   }
   double bb;
   if (case_reduce(acc, F, S, lt, sh, &bb) && threadIdx.x == 0) {
@@ -931,12 +1003,9 @@ __global__ void k_correct(const FineCase* FC, const MState* ST, const int2* ftil
   }
 }
 
-__global__ void __launch_bounds__(TILE) k_addp(const FineCase* FC, const MState* ST, const int2* tiles) {
-  const int2 t = tiles[blockIdx.x];
-  const FineCase& F = FC[t.x];
-  if (ST[t.x].state != DONE) return;
-  const int c = t.y * TILE + threadIdx.x;
-  if (c < F.N) F.pfield[c] = __dadd_rn(F.pfield[c], F.x64[c]);
+__global__ void __launch_bounds__(TILE) k_addp(const FineCase* FC, MState* ST, const int2* tiles) {
+  FINE_PROLOGUE(S.state == DONE)
+  for (int c = cb + threadIdx.x; c < ce; c += TILE) F.pfield[c] = __dadd_rn(F.pfield[c], F.x64[c]);
 }
 
 // ----------------------------------------------------------------- host side
@@ -1039,7 +1108,7 @@ int build_case(cfdg_grid* G, CaseState& cs) {
   } else {
     F.rhs0 = F.r32;
   }
-  F.ntiles = (F.N + DOT - 1) / DOT;  // reduction tiles (partials per case)
+  F.ntiles = (h.n[1] * h.n[2] + RT - 1) / RT;  // row tiles (one reduction partial each)
   if (int e = A.alloc(&F.partials, F.ntiles)) return e;
   cs.ngroups0 = M0.groups.rows();
   F.ngroups = cs.ngroups0;
@@ -1211,6 +1280,7 @@ void launch_coarse(cfdg_batch* B, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)B->coop_blocks, 1, 1);
     cfg.blockDim = dim3(512, 1, 1);
+    cfg.dynamicSmemBytes = 2 * B->cases.size() * sizeof(CLev);
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeCooperative;
@@ -1317,10 +1387,10 @@ int cfdg_mixed_pack(cfdg_batch* B) {
   for (size_t i = 0; i < B->cases.size(); ++i) {
     FineCase F = B->cases[i]->F;
     F.tile0 = (int)tiles.size();
-    for (int t = 0; t < (F.N + TILE - 1) / TILE; ++t) tiles.push_back(make_int2((int)i, t));
+    for (int t = 0; t < F.ntiles; ++t) tiles.push_back(make_int2((int)i, t));
     for (int t = 0; t < F.ntiles; ++t) dtiles.push_back(make_int2((int)i, t));
     for (int t = 0; t < (F.n1 + TILE - 1) / TILE; ++t) tiles1.push_back(make_int2((int)i, t));
-    for (int t = 0; t < (F.npairs + TILE - 1) / TILE; ++t) ptiles.push_back(make_int2((int)i, t));
+    for (int t = 0; t < F.ntiles; ++t) ptiles.push_back(make_int2((int)i, t));
     F.ftile0 = (int)ftiles.size();
     F.nftiles = (int)((F.F + FTILE - 1) / FTILE);
     for (int t = 0; t < F.nftiles; ++t) ftiles.push_back(make_int2((int)i, t));
@@ -1404,7 +1474,9 @@ int cfdg_mixed_pack(cfdg_batch* B) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_coarse_all, 512, 0) != cudaSuccess || per < 1) {
+    const size_t dsm = 2 * B->cases.size() * sizeof(CLev);
+    if (dsm > 48 * 1024) cudaFuncSetAttribute(k_coarse_all, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_coarse_all, 512, dsm) != cudaSuccess || per < 1) {
       cudaGetLastError();
       B->coop = false;
     }
