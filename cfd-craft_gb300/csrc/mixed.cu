@@ -661,26 +661,17 @@ __global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState*
     __threadfence();
     csync();
     if (L.terminal) {
-      // FP64 dense Cholesky solves, one warp per block (lane 0 works).
-      const int warp = tid >> 5, nw = nth >> 5;
-      if ((threadIdx.x & 31) == 0)
-        for (int bk = warp; bk < L.nblocks; bk += nw) {
-          const int* ix = L.idx + L.ioff[bk];
-          const int n = L.ioff[bk + 1] - L.ioff[bk];
-          const double* f = L.fac + L.foff[bk];
-          double y[32];
-          for (int i = 0; i < n; ++i) {
-            double v = (double)__ldcg(&L.rhs[ix[i]]);
-            for (int j = 0; j < i; ++j) v -= f[i * n + j] * y[j];
-            y[i] = v / f[i * n + i];
-          }
-          for (int i = n - 1; i >= 0; --i) {
-            double v = y[i];
-            for (int j = i + 1; j < n; ++j) v -= f[j * n + i] * y[j];
-            y[i] = v / f[i * n + i];
-          }
-          for (int i = 0; i < n; ++i) L.x[ix[i]] = (float)y[i];
-        }
+      // x_idx = (L L^T)^-1 rhs_idx in FP64 (the block inverses formed on the host).
+      for (int q = tid; q < L.nblocks * 32; q += nth) {
+        const int bk = q >> 5, ln = q & 31;
+        const int* ix = L.idx + L.ioff[bk];
+        const int n = L.ioff[bk + 1] - L.ioff[bk];
+        if (ln >= n) continue;
+        const double* m = L.fac + L.foff[bk];
+        double acc = 0.0;
+        for (int j = 0; j < n; ++j) acc = fma(m[ln * n + j], (double)__ldcg(&L.rhs[ix[j]]), acc);
+        L.x[ix[ln]] = (float)acc;
+      }
       __threadfence();
       csync();
       c_center(L, L.x, C.gpart, sh);
@@ -855,31 +846,33 @@ __global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MS
     }
     grid.sync();
     {
-      // Terminal levels: FP64 dense Cholesky solves, one warp per block (lane 0 works).
+      // Terminal levels: x_idx = (L L^T)^-1 rhs_idx in FP64, one warp per block.
       const int* off = T.term + l * (nc + 1);
-      const int wp = gt >> 5, nw = nth >> 5;
-      if ((threadIdx.x & 31) == 0)
-        for (int t = wp; t < __ldg(&off[nc]); t += nw) {
-          const int ci = find_case(off, nc, t);
-          if (!active(ST, ci)) continue;
-          const CLev& L = sl[ci];
-          const int bk = t - __ldg(&off[ci]);
-          const int* ix = L.idx + L.ioff[bk];
-          const int n = L.ioff[bk + 1] - L.ioff[bk];
-          const double* f = L.fac + L.foff[bk];
-          double y[32];
-          for (int i = 0; i < n; ++i) {
-            double v = (double)__ldcg(&L.rhs[ix[i]]);
-            for (int j = 0; j < i; ++j) v -= f[i * n + j] * y[j];
-            y[i] = v / f[i * n + i];
+      const int wp = gt >> 5, nw = nth >> 5, ln = threadIdx.x & 31;
+      for (int t = wp; t < __ldg(&off[nc]); t += nw) {
+        const int ci = find_case(off, nc, t);
+        if (!active(ST, ci)) continue;
+        const CLev& L = sl[ci];
+        const int bk = t - __ldg(&off[ci]);
+        const int* ix = L.idx + L.ioff[bk];
+        const int n = L.ioff[bk + 1] - L.ioff[bk];
+        const double* m = L.fac + L.foff[bk];
+        const double rj = ln < n ? (double)__ldcg(&L.rhs[ix[ln]]) : 0.0;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        for (int j = 0; j < n; j += 4) {
+          const double r0 = __shfl_sync(0xffffffffu, rj, j);
+          const double r1 = __shfl_sync(0xffffffffu, rj, j + 1 < 32 ? j + 1 : 31);
+          const double r2 = __shfl_sync(0xffffffffu, rj, j + 2 < 32 ? j + 2 : 31);
+          const double r3 = __shfl_sync(0xffffffffu, rj, j + 3 < 32 ? j + 3 : 31);
+          if (ln < n) {
+            a0 = fma(m[ln * n + j], r0, a0);
+            if (j + 1 < n) a1 = fma(m[ln * n + j + 1], r1, a1);
+            if (j + 2 < n) a2 = fma(m[ln * n + j + 2], r2, a2);
+            if (j + 3 < n) a3 = fma(m[ln * n + j + 3], r3, a3);
           }
-          for (int i = n - 1; i >= 0; --i) {
-            double v = y[i];
-            for (int j = i + 1; j < n; ++j) v -= f[j * n + i] * y[j];
-            y[i] = v / f[i * n + i];
-          }
-          for (int i = 0; i < n; ++i) L.x[ix[i]] = (float)y[i];
         }
+        if (ln < n) L.x[ix[ln]] = (float)((a0 + a1) + (a2 + a3));
+      }
     }
     grid.sync();
     g_sweep(sl, ST, T, l, false, grid);
@@ -1210,7 +1203,30 @@ int build_case(cfdg_grid* G, CaseState& cs) {
       if (int e = A.upload(&io, M.direct_idx.off, s)) return e;
       if (int e = A.upload(&ix, M.direct_idx.col, s)) return e;
       if (int e = A.upload(&fo, foff, s)) return e;
-      if (int e = A.upload(&fa, M.direct_factor, s)) return e;
+      // The coarsest solve as an FP64 mat-vec with (L L^T)^-1 of each block, formed on
+      // the host from the reference's Cholesky factor: one warp per block, no FP64
+      // dependency chain of substitution steps.
+      std::vector<double> inv(M.direct_factor.size());
+      for (int b = 0; b < L.nblocks; ++b) {
+        const int n = M.direct_idx.off[b + 1] - M.direct_idx.off[b];
+        const double* f = M.direct_factor.data() + M.direct_off[b];
+        double* out = inv.data() + M.direct_off[b];
+        std::vector<double> y(n);
+        for (int col = 0; col < n; ++col) {
+          for (int i = 0; i < n; ++i) {
+            double v = i == col ? 1.0 : 0.0;
+            for (int j = 0; j < i; ++j) v -= f[i * n + j] * y[j];
+            y[i] = v / f[i * n + i];
+          }
+          for (int i = n - 1; i >= 0; --i) {
+            double v = y[i];
+            for (int j = i + 1; j < n; ++j) v -= f[j * n + i] * y[j];
+            y[i] = v / f[i * n + i];
+          }
+          for (int i = 0; i < n; ++i) out[i * n + col] = y[i];
+        }
+      }
+      if (int e = A.upload(&fa, inv, s)) return e;
       L.ioff = io, L.idx = ix, L.foff = fo, L.fac = fa;
       for (int b = 0; b < L.nblocks; ++b)
         if (M.direct_idx.off[b + 1] - M.direct_idx.off[b] > 32)
