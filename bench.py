@@ -401,6 +401,9 @@ def run_engine(args):
                            "unit": "per step"},
             "iterations_mean": round(statistics.mean(its), 2),
             "refinement_steps_mean": round(statistics.mean(outer), 2),
+            "solve_breakdown": {"device_ms": round(1e3 * statistics.mean(i.work.get("device_seconds", 0) for i in infos), 3),
+                                "loop_ms": round(1e3 * statistics.mean(i.work.get("loop_seconds", 0) for i in infos), 3),
+                                "graph_chunks": round(statistics.mean(i.work.get("graph_launches", 0) for i in infos), 2)},
             "cell_updates_per_s": round(g.count * statistics.mean(its) * value, 1),
             "e2e": e2e, "roofline": roofline, "kernels": kernels, "plain_fp64": plain, "cpu_baseline": cpu,
             "gpu_launches": int(launches), "clocks": clk,

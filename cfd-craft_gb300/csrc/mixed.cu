@@ -1599,6 +1599,11 @@ int cfdg_mixed_project(cfdg_batch* B, double* const* d_u, double* const* d_p, co
   P.fn = poll;
   P.ctx = poll_ctx;
   int status = 0;
+  uint64_t chunks = 0;
+  cudaEvent_t lp0, lp1;
+  cudaEventCreate(&lp0);
+  cudaEventCreate(&lp1);
+  cudaEventRecord(lp0, s);
   for (;;) {
     CU(cudaMemcpyAsync(B->h_st, B->d_st, sizeof(MState) * nc, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
@@ -1611,7 +1616,9 @@ int cfdg_mixed_project(cfdg_batch* B, double* const* d_u, double* const* d_p, co
     }
     CU(cudaGraphLaunch(B->chunk, s));
     count(B->chunk_nodes);
+    chunks += 1;
   }
+  cudaEventRecord(lp1, s);
   if (status == 0) {
     // Epilogue for converged cases: gauge of x, face correction, p += x, gauge of p.
     for (int i = 0; i < nc; ++i) {
@@ -1628,8 +1635,11 @@ int cfdg_mixed_project(cfdg_batch* B, double* const* d_u, double* const* d_p, co
   }
   CU(cudaEventRecord(B->ev1, s));
   CU(cudaEventSynchronize(B->ev1));
-  float ms = 0;
+  float ms = 0, lms = 0;
   cudaEventElapsedTime(&ms, B->ev0, B->ev1);
+  cudaEventElapsedTime(&lms, lp0, lp1);
+  cudaEventDestroy(lp0);
+  cudaEventDestroy(lp1);
   for (int i = 0; i < nc; ++i) {
     const MState& m = B->h_st[i];
     if (infos) {
@@ -1644,6 +1654,8 @@ int cfdg_mixed_project(cfdg_batch* B, double* const* d_u, double* const* d_p, co
       I.cycles = I.preconditioner_applications;
       I.refinement_steps = (uint64_t)m.outer;
       I.device_seconds = ms * 1e-3;
+      I.graph_launches = chunks;
+      I.loop_seconds = lms * 1e-3;
     }
     if (codes && codes[i] == 0) {
       if (status) codes[i] = status;

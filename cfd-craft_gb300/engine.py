@@ -73,6 +73,8 @@ class Info(C.Structure):
         ("coarse_solves", C.c_uint64),
         ("refinement_steps", C.c_uint64),
         ("device_seconds", C.c_double),
+        ("graph_launches", C.c_uint64),
+        ("loop_seconds", C.c_double),
     ]
 
     def as_dict(self):

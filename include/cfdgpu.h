@@ -107,6 +107,8 @@ typedef struct {
   uint64_t coarse_solves;
   uint64_t refinement_steps;    /* outer FP64 defect-correction steps (mixed form); 0 plain */
   double device_seconds;        /* device time of the solve, from CUDA events */
+  uint64_t graph_launches;      /* captured iteration chunks replayed by the solve */
+  double loop_seconds;          /* device time of the iteration loop alone */
 } cfdg_info;
 
 /* Control::check (solver.rs:122-140): 0 continue, 1 "cancelled", 2 "wall_time_limit".
