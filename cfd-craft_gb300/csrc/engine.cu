@@ -947,6 +947,15 @@ int prepare_mg_impl(cfdg_grid* G, const Poller& poll, cfdg_info* info) {
   if (int c = poll.check()) return fail(c, c == CFDG_CANCELLED ? "cancelled" : "wall_time_limit");
   if (G->h.n_components == 0)
     return fail(CFDG_E034, "CFD-E034: numerics.pressure_preconditioner: multigrid requires fluid cells");
+  if (G->mg && G->signature && G->sig_version == G->faces_version) {
+    // Faces unchanged since the hierarchy was last checked against them.
+    if (info) {
+      info->hierarchy_levels = G->mg->level_cells.size();
+      for (auto v : G->mg->level_cells) info->hierarchy_cells += v;
+      for (auto v : G->mg->level_nonzeros) info->hierarchy_nonzeros += v;
+    }
+    return 0;
+  }
   Signature cur;
   int se = signature_of(G->h, cur);
   bool rebuild = !G->mg || !G->signature || se != 0 || !(cur == *G->signature);
@@ -961,6 +970,7 @@ int prepare_mg_impl(cfdg_grid* G, const Poller& poll, cfdg_info* info) {
     G->signature = std::make_unique<Signature>(std::move(cur));
     if (info) info->hierarchy_builds = 1;
   }
+  G->sig_version = G->faces_version;
   if (info) {
     info->hierarchy_levels = G->mg->level_cells.size();
     for (auto v : G->mg->level_cells) info->hierarchy_cells += v;
@@ -1410,6 +1420,7 @@ int cfdg_grid_update_faces(cfdg_grid* G, const double* area, const double* dista
   if (distance) G->h.face_distance.assign(distance, distance + G->h.faces);
   if (int e = refresh_weights(G)) return e;
   reset_chunk(G);  // captured launches hold the weights by value
+  G->faces_version += 1;
   G->mixed.reset();
   G->solo.reset();
   CU(cudaStreamSynchronize(G->stream));

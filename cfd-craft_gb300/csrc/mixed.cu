@@ -1032,6 +1032,7 @@ std::vector<float> to_f32(const std::vector<T>& v) {
 
 struct CaseState {
   cfdg_grid* G = nullptr;
+  uint64_t version = 0;  // the grid's faces_version this state was built from
   Arena arena;
   FineCase F{};
   CCase C{};
@@ -1384,6 +1385,7 @@ int case_of(cfdg_grid* G, std::shared_ptr<CaseState>& out) {
     return fail(CFDG_ERR_UNSUPPORTED, "the mixed form needs a non-periodic grid with a multigrid hierarchy of two or more levels");
   auto cs = std::make_shared<CaseState>();
   cs->G = G;
+  cs->version = G->faces_version;
   if (int e = build_case(G, *cs)) return e;
   G->mixed = cs;
   out = cs;
@@ -1667,6 +1669,22 @@ int cfdg_mixed_project(cfdg_batch* B, double* const* d_u, double* const* d_p, co
 
 // ----------------------------------------------------------------- batch lifetime and C ABI
 namespace {
+// A grid whose faces changed since the batch was packed gets a fresh hierarchy and FP32
+// state, and the batch's tables are packed again (the grids' locks are held).
+int refresh_batch(cfdg_batch* B) {
+  bool stale = false;
+  for (size_t i = 0; i < B->cases.size(); ++i) {
+    cfdg_grid* G = B->grids[i];
+    if (B->cases[i]->version == G->faces_version && G->mixed == B->cases[i]) continue;
+    if (int e = prepare_multigrid(G)) return e;
+    std::shared_ptr<CaseState> cs;
+    if (int e = case_of(G, cs)) return e;
+    B->cases[i] = cs;
+    stale = true;
+  }
+  return stale ? cfdg_mixed_pack(B) : 0;
+}
+
 std::vector<cfdg_grid*> lock_order(const std::vector<cfdg_grid*>& g) {
   std::vector<cfdg_grid*> v(g);
   std::sort(v.begin(), v.end());
@@ -1811,6 +1829,7 @@ int cfdg_batch_project_device(cfdg_batch* B, double* const* d_u, double* const* 
   auto order = lock_order(B->grids);
   std::vector<std::unique_lock<std::mutex>> locks;
   for (auto* G : order) locks.emplace_back(G->mu);
+  if (int e = refresh_batch(B)) return e;
   return cfdg_mixed_project(B, d_u, d_p, dt, tol, max_iter, poll, poll_ctx, infos, codes);
 }
 
@@ -1821,6 +1840,7 @@ int cfdg_batch_project(cfdg_batch* B, double* const* u, double* const* p, const 
   auto order = lock_order(B->grids);
   std::vector<std::unique_lock<std::mutex>> locks;
   for (auto* G : order) locks.emplace_back(G->mu);
+  if (int e = refresh_batch(B)) return e;
   const int nc = (int)B->grids.size();
   std::vector<double*> du(nc), dp(nc);
   cudaStream_t s = B->stream;

@@ -179,6 +179,10 @@ struct cfdg_grid {
   std::shared_ptr<cfdg::Hierarchy> host_mg;  // the hierarchy as uploaded (level 0 re-indexed when full0)
   std::shared_ptr<void> mixed;               // the mixed-precision form's device state (mixed.cu)
   std::shared_ptr<struct cfdg_batch> solo;   // a one-grid batch for cfdg_project in the mixed form
+  // Face coefficients change only through cfdg_grid_update_faces, which bumps
+  // faces_version; the hierarchy's signature is re-compared only after a change.
+  uint64_t faces_version = 0;
+  uint64_t sig_version = ~0ull;
 };
 
 struct cfdg_batch;

@@ -106,3 +106,29 @@ def test_batch_equals_alone_and_is_transactional(pkg, O):
     batch2.close()
     for d in dgs + [dgb]:
         d.close()
+
+
+def test_batch_follows_changed_face_coefficients(pkg):
+    """After cfdg_grid_update_faces the batch rebuilds that grid's hierarchy and FP32 state."""
+    cases = mixed_cases(pkg)
+    g1 = pkg.grid.Grid.build(cases["odd-37x29x21"])
+    g2 = pkg.grid.Grid.build(cases["pocket"])
+    d1 = pkg.pressure.DeviceGrid(g1, preconditioner="multigrid", precision="mixed")
+    d2 = pkg.pressure.DeviceGrid(g2, preconditioner="multigrid", precision="mixed")
+    batch = pkg.pressure.Batch([d1, d2])
+    u1, u2 = pkg.synth.random_velocity(g1, 5), pkg.synth.random_velocity(g2, 6)
+    p1, p2 = np.zeros(g1.count), np.zeros(g2.count)
+    area = g1.face_area * (1.0 + (np.arange(g1.n_faces) % 5) * 0.01)
+    d1.update_faces(area=area)
+    bu = [u1.copy(), u2.copy()]
+    bp = [p1.copy(), p2.copy()]
+    res = batch.project(bu, bp, [0.1, 0.1], 1e-8, 10000)
+    assert [c for c, _ in res] == [0, 0]
+    # Alone, on a grid built with the same changed coefficients.
+    g1b = pkg.grid.Grid.build(cases["odd-37x29x21"])
+    g1b.face_area = area
+    au, ap_, _ = run_mixed(pkg, g1b, u1, p1, 0.1, 1e-8)
+    assert np.array_equal(bits(bu[0]), bits(au)) and np.array_equal(bits(bp[0]), bits(ap_))
+    batch.close()
+    d1.close()
+    d2.close()
