@@ -28,6 +28,7 @@
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -251,10 +252,10 @@ __device__ __forceinline__ double op64(const FineCase& F, const double* __restri
 constexpr int RT = TILE / 32;  // rows per tile: one warp per row
 
 #define FINE_PROLOGUE(STATE_TEST)                                                     \
-  const int2 t = tiles[blockIdx.x];                                                   \
   MState& S = ST[t.x];                                                                \
   if (!(STATE_TEST)) return;                                                          \
   __shared__ __align__(16) FineCase sF;                                               \
+  __syncthreads(); /* the previous tile's readers of sF are done */                   \
   {                                                                                   \
     const long long* src_ = reinterpret_cast<const long long*>(&FC[t.x]);             \
     long long* dst_ = reinterpret_cast<long long*>(&sF);                              \
@@ -324,7 +325,7 @@ __device__ __forceinline__ float op32r(const FineCase& F, const float* __restric
 }
 
 // A: q = A32 p, alpha = rz / (p.q) (E032 when not positive).
-__global__ void __launch_bounds__(TILE) k_op(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_op(const FineCase* FC, MState* ST, const int2 t) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN)
   float hi = 0.0f, lo = 0.0f;
@@ -347,9 +348,13 @@ __global__ void __launch_bounds__(TILE) k_op(const FineCase* FC, MState* ST, con
     }
   }
 }
+__global__ void __launch_bounds__(TILE) k_op(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_op(FC, ST, tiles[ti]);
+}
 
 // B: e += alpha p, r -= alpha q; |r| decides the end of the inner solve.
-__global__ void __launch_bounds__(TILE) k_update(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_update(const FineCase* FC, MState* ST, const int2 t) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN)
   const float alpha = (float)S.alpha;
@@ -368,17 +373,25 @@ __global__ void __launch_bounds__(TILE) k_update(const FineCase* FC, MState* ST,
     if (sqrt(rr) <= S.inner_tol || S.inner_it >= S.max_inner || S.total_it >= S.max_it) S.state = OUTER;
   }
 }
+__global__ void __launch_bounds__(TILE) k_update(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_update(FC, ST, tiles[ti]);
+}
 
 // C1: x += |r| e (the residual is formed by k_outer_resid once every block has updated x).
-__global__ void __launch_bounds__(TILE) k_outer(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_outer(const FineCase* FC, MState* ST, const int2 t) {
   FINE_PROLOGUE(S.state == OUTER)
   if (!S.has_e) return;
   const double scale = S.scale;
   for (int c = cb + threadIdx.x; c < ce; c += TILE) F.x64[c] = F.x64[c] + scale * (double)F.e[c];
 }
+__global__ void __launch_bounds__(TILE) k_outer(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_outer(FC, ST, tiles[ti]);
+}
 
 // r = b_c - A x in FP64; the true residual decides convergence.
-__global__ void __launch_bounds__(TILE) k_outer_resid(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_outer_resid(const FineCase* FC, MState* ST, const int2 t) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == OUTER)
   double acc = 0.0;
@@ -403,15 +416,23 @@ __global__ void __launch_bounds__(TILE) k_outer_resid(const FineCase* FC, MState
     }
   }
 }
+__global__ void __launch_bounds__(TILE) k_outer_resid(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_outer_resid(FC, ST, tiles[ti]);
+}
 
 // C2: r32 = r / |r|, e = 0.
-__global__ void __launch_bounds__(TILE) k_scale(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_scale(const FineCase* FC, MState* ST, const int2 t) {
   FINE_PROLOGUE(S.state == SCALE)
   const double inv = 1.0 / S.scale;
   for (int c = cb + threadIdx.x; c < ce; c += TILE) {
     F.r32[c] = (float)(F.r64[c] * inv);
     F.e[c] = 0.0f;
   }
+}
+__global__ void __launch_bounds__(TILE) k_scale(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_scale(FC, ST, tiles[ti]);
 }
 
 __global__ void k_start_state(MState* ST, int n) {
@@ -423,7 +444,7 @@ __global__ void k_start_state(MState* ST, int n) {
 }
 
 // F: rz' = r.z; START: rz = rz', p = z (beta = 0) -> RUN; RUN: beta = rz'/rz.
-__global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_rz(const FineCase* FC, MState* ST, const int2 t) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   float hi = 0.0f, lo = 0.0f;
@@ -439,9 +460,13 @@ __global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, con
     S.rz = rz;
   }
 }
+__global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_rz(FC, ST, tiles[ti]);
+}
 
 // G: p = z + beta p (z is the V-cycle's level-0 solution x0).
-__global__ void __launch_bounds__(TILE) k_p(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_p(const FineCase* FC, MState* ST, const int2 t) {
   FINE_PROLOGUE(S.state == RUN)
   const float beta = (float)S.beta;
   if (S.beta == 0.0) {
@@ -450,20 +475,28 @@ __global__ void __launch_bounds__(TILE) k_p(const FineCase* FC, MState* ST, cons
     for (int c = cb + threadIdx.x; c < ce; c += TILE) F.p[c] = fmaf(beta, F.p[c], F.x0[c]);
   }
 }
+__global__ void __launch_bounds__(TILE) k_p(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_p(FC, ST, tiles[ti]);
+}
 
 // ----------------------------------------------------------------- V-cycle, level 0
 // rhs0 = r32 (only when level 0 has closed groups; otherwise rhs0 is r32 itself).
-__global__ void __launch_bounds__(TILE) k_v_rhs(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_v_rhs(const FineCase* FC, MState* ST, const int2 t) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   if (F.rhs0 == F.r32) return;
   for (int c = cb + threadIdx.x; c < ce; c += TILE) F.rhs0[c] = F.r32[c];
+}
+__global__ void __launch_bounds__(TILE) k_v_rhs(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_rhs(FC, ST, tiles[ti]);
 }
 
 // Red-black Gauss-Seidel half sweep on level 0: cells with (i+j+k)%2 == color. Lanes
 // walk the x-pairs (2m, 2m+1) of the warp's row, of which exactly one has the colour.
 // first: x is taken as zero (the cycle's initial guess). Cells outside the operator
 // (solid, sealed singletons) are kept at zero.
-__global__ void __launch_bounds__(TILE) k_rb(const FineCase* FC, MState* ST, const int2* tiles, int color, int first) {
+__device__ __forceinline__ void b_rb(const FineCase* FC, MState* ST, const int2 t, int color, int first) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   int j, k, rb;
   if (!warp_row(F, lt, warp, j, k, rb)) return;
@@ -507,9 +540,13 @@ __global__ void __launch_bounds__(TILE) k_rb(const FineCase* FC, MState* ST, con
     x[cc] = v * id;
   }
 }
+__global__ void __launch_bounds__(TILE) k_rb(const FineCase* FC, MState* ST, const int2* tiles, const int* count, int color, int first) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_rb(FC, ST, tiles[ti], color, first);
+}
 
 // res0 = rhs0 - A0 x0 (A0 = diag - sum w on interior faces).
-__global__ void __launch_bounds__(TILE) k_v_resid(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_v_resid(const FineCase* FC, MState* ST, const int2 t) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   int j, k, rb;
   if (!warp_row(F, lt, warp, j, k, rb)) return;
@@ -547,22 +584,30 @@ __global__ void __launch_bounds__(TILE) k_v_resid(const FineCase* FC, MState* ST
     F.res0[cc] = F.rhs0[cc] - v;
   }
 }
+__global__ void __launch_bounds__(TILE) k_v_resid(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_resid(FC, ST, tiles[ti]);
+}
 
 // rhs1 = R res0: level-1 rows gather their level-0 children. Tiles index level-1 rows.
-__global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState* ST, const int2* tiles1) {
-  const int2 t = tiles1[blockIdx.x];
-  const FineCase& F = FC[t.x];
-  const MState& S = ST[t.x];
-  if (!(S.state == RUN || S.state == START)) return;
-  const int j = t.y * TILE + threadIdx.x;
-  if (j >= F.n1) return;
-  float v = 0.0f;
-  for (int k = F.r_off[j]; k < F.r_off[j + 1]; ++k) v = fmaf(F.r_w[k], F.res0[F.r_child[k]], v);
-  F.rhs1[j] = v;
+__global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState* ST, const int2* tiles1,
+                                                     const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) {
+    const int2 t = tiles1[ti];
+    const FineCase& F = FC[t.x];
+    const MState& S = ST[t.x];
+    if (!(S.state == RUN || S.state == START)) continue;
+    const int j = t.y * TILE + threadIdx.x;
+    if (j >= F.n1) continue;
+    float v = 0.0f;
+    for (int k = F.r_off[j]; k < F.r_off[j + 1]; ++k) v = fmaf(F.r_w[k], F.res0[F.r_child[k]], v);
+    F.rhs1[j] = v;
+  }
 }
 
 // x0 += P x1.
-__global__ void __launch_bounds__(TILE) k_v_prolong(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, const int2 t) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   for (int c = cb + threadIdx.x; c < ce; c += TILE) {
     const int b = F.p_off[c], e = F.p_off[c + 1];
@@ -572,24 +617,33 @@ __global__ void __launch_bounds__(TILE) k_v_prolong(const FineCase* FC, MState* 
     F.x0[c] += sum;
   }
 }
+__global__ void __launch_bounds__(TILE) k_v_prolong(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_prolong(FC, ST, tiles[ti]);
+}
 
 // Gauge of level-0 closed groups: one block per (case, group); members strided.
 // which: 0 rhs0, 1 x0, 2 res0.
-__global__ void k_center0(const FineCase* FC, MState* ST, const int2* gtab, int which) {
+__global__ void k_center0(const FineCase* FC, MState* ST, const int2* gtab, const int* count, int which) {
   __shared__ double sh[32];
   __shared__ float mean;
-  const int2 t = gtab[blockIdx.x];
-  const FineCase& F = FC[t.x];
-  const MState& S = ST[t.x];
-  if (!(S.state == RUN || S.state == START)) return;
-  float* v = which == 0 ? F.rhs0 : (which == 1 ? F.x0 : F.res0);
-  const int b = F.goff[t.y], e = F.goff[t.y + 1];
-  double acc = 0.0;
-  for (int k = b + threadIdx.x; k < e; k += blockDim.x) acc += v[F.gmem[k]];
-  double s = bsum(acc, sh);
-  if (threadIdx.x == 0) mean = (float)(s / (double)(e - b));
-  __syncthreads();
-  for (int k = b + threadIdx.x; k < e; k += blockDim.x) v[F.gmem[k]] -= mean;
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) {
+    const int2 t = gtab[ti];
+    const FineCase& F = FC[t.x];
+    const MState& S = ST[t.x];
+    if (!(S.state == RUN || S.state == START)) continue;
+    float* v = which == 0 ? F.rhs0 : (which == 1 ? F.x0 : F.res0);
+    const int b = F.goff[t.y], e = F.goff[t.y + 1];
+    double acc = 0.0;
+    for (int k = b + threadIdx.x; k < e; k += blockDim.x) acc += v[F.gmem[k]];
+    double s = bsum(acc, sh);
+    if (threadIdx.x == 0) mean = (float)(s / (double)(e - b));
+    __syncthreads();
+    const float m = mean;
+    for (int k = b + threadIdx.x; k < e; k += blockDim.x) v[F.gmem[k]] -= m;
+    __syncthreads();
+  }
 }
 
 // ----------------------------------------------------------------- coarse levels, one cluster per case
@@ -827,7 +881,8 @@ __device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, in
   }
 }
 
-__global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MState* ST, CoarseTab T) {
+__global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MState* ST, const CoarseTab* Tp) {
+  const CoarseTab T = *Tp;
   __shared__ double sh[32];
   extern __shared__ __align__(16) unsigned char smem[];
   CLev* sl = reinterpret_cast<CLev*>(smem);
@@ -931,7 +986,7 @@ __global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MS
 
 // ----------------------------------------------------------------- prologue / epilogue (FP64)
 // b = -div(u)/dt, terms (pressure.rs:440-459), rounded as written.
-__global__ void __launch_bounds__(TILE) k_rhs(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_rhs(const FineCase* FC, MState* ST, const int2 t) {
   FINE_PROLOGUE(S.state == IDLE)
   int j, k, rb;
   if (!warp_row(F, lt, warp, j, k, rb)) return;
@@ -957,9 +1012,13 @@ __global__ void __launch_bounds__(TILE) k_rhs(const FineCase* FC, MState* ST, co
     F.terms[c] = __ddiv_rn(scale, F.dt);
   }
 }
+__global__ void __launch_bounds__(TILE) k_rhs(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_rhs(FC, ST, tiles[ti]);
+}
 
 // |b_c| (after the host-side gauge of closed components); x = 0.
-__global__ void __launch_bounds__(TILE) k_norm(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_norm(const FineCase* FC, MState* ST, const int2 t) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == IDLE)
   double acc = 0.0;
@@ -977,28 +1036,39 @@ __global__ void __launch_bounds__(TILE) k_norm(const FineCase* FC, MState* ST, c
     S.state = S.norm < 1e-24 ? DONE : OUTER;
   }
 }
+__global__ void __launch_bounds__(TILE) k_norm(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_norm(FC, ST, tiles[ti]);
+}
 
 // Face correction u -= dt grad(x) (pressure.rs:481-496), face tiles.
-__global__ void k_correct(const FineCase* FC, const MState* ST, const int2* ftiles) {
-  const int2 t = ftiles[blockIdx.x];
-  const FineCase& F = FC[t.x];
-  if (ST[t.x].state != DONE) return;
-  const long long f = (long long)t.y * FTILE + threadIdx.x;
-  for (int r = 0; r < FTILE / 256; ++r) {
-    const long long ff = f + r * 256;
-    if (ff >= F.F) return;
-    double d;
-    const uint8_t k = F.fkind[ff];
-    if (k == INTERIOR) d = __ddiv_rn(__dsub_rn(F.x64[F.fhi[ff]], F.x64[F.flo[ff]]), F.fdist[ff]);
-    else if (k == OUTLET) d = F.flo[ff] >= 0 ? __ddiv_rn(-F.x64[F.flo[ff]], F.fdist[ff]) : __ddiv_rn(F.x64[F.fhi[ff]], F.fdist[ff]);
-    else d = 0.0;
-    F.u[ff] = __dsub_rn(F.u[ff], __dmul_rn(F.dt, d));
+__global__ void k_correct(const FineCase* FC, const MState* ST, const int2* ftiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) {
+    const int2 t = ftiles[ti];
+    const FineCase& F = FC[t.x];
+    if (ST[t.x].state != DONE) continue;
+    const long long f0 = (long long)t.y * FTILE + threadIdx.x;
+    for (int r = 0; r < FTILE / 256; ++r) {
+      const long long ff = f0 + r * 256;
+      if (ff >= F.F) break;
+      double d;
+      const uint8_t k = F.fkind[ff];
+      if (k == INTERIOR) d = __ddiv_rn(__dsub_rn(F.x64[F.fhi[ff]], F.x64[F.flo[ff]]), F.fdist[ff]);
+      else if (k == OUTLET) d = F.flo[ff] >= 0 ? __ddiv_rn(-F.x64[F.flo[ff]], F.fdist[ff]) : __ddiv_rn(F.x64[F.fhi[ff]], F.fdist[ff]);
+      else d = 0.0;
+      F.u[ff] = __dsub_rn(F.u[ff], __dmul_rn(F.dt, d));
+    }
   }
 }
 
-__global__ void __launch_bounds__(TILE) k_addp(const FineCase* FC, MState* ST, const int2* tiles) {
+__device__ __forceinline__ void b_addp(const FineCase* FC, MState* ST, const int2 t) {
   FINE_PROLOGUE(S.state == DONE)
   for (int c = cb + threadIdx.x; c < ce; c += TILE) F.pfield[c] = __dadd_rn(F.pfield[c], F.x64[c]);
+}
+__global__ void __launch_bounds__(TILE) k_addp(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+  const int n = *count;
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_addp(FC, ST, tiles[ti]);
 }
 
 // ----------------------------------------------------------------- host side
@@ -1258,6 +1328,15 @@ int build_case(cfdg_grid* G, CaseState& cs) {
 using namespace cfdg;
 using namespace cfdg::mx;
 
+// Work-lists of the persistent fine-level kernels: the row tiles, level-1 row tiles,
+// face tiles and level-0 group entries of the cases a list covers. Kernels loop over
+// the first counts[k] entries, so the lists change between graph replays without
+// touching the graph.
+struct WorkLists {
+  int2 *tiles = nullptr, *tiles1 = nullptr, *ftiles = nullptr, *gtab = nullptr;
+  int* counts = nullptr;  // [4]
+};
+
 // A set of grids solved together in the mixed form.
 struct cfdg_batch {
   cfdg_context* ctx = nullptr;
@@ -1269,14 +1348,22 @@ struct cfdg_batch {
   CCase* d_cc = nullptr;
   MState* d_st = nullptr;
   MState* h_st = nullptr;
-  int2 *d_tiles = nullptr, *d_tiles1 = nullptr, *d_ftiles = nullptr, *d_gtab = nullptr, *d_ptiles = nullptr,
-       *d_dtiles = nullptr;
-  int ntiles = 0, ntiles1 = 0, nftiles = 0, ngtab = 0, nptiles = 0, ndtiles = 0;
-  int csize = CS;  // CTAs per cluster of the coarse-level kernel
-  CoarseTab tab{};   // phase tables of the cooperative coarse-level kernel
-  int coop_blocks = 0;
-  bool coop = true;  // the cooperative whole-grid coarse kernel (else one cluster per case)
   std::vector<FineCase> h_fc;
+  // All work items of all cases (host), and three device lists: the graph's (run),
+  // the prologue's and the epilogue's.
+  std::vector<int2> tiles, tiles1, ftiles, gtab;
+  WorkLists run, pro, epi;
+  int g_fine = 1, g_1 = 1, g_f = 1, g_g = 1;  // persistent grid sizes
+  bool any_groups = false;
+  // Coarse-level phase tables (device), refilled for each active set.
+  CoarseTab h_tab{};
+  CoarseTab* d_tab = nullptr;
+  int* tab_buf = nullptr;
+  int nlev_all = 0;
+  int coop_blocks = 0;
+  bool coop = true;
+  int csize = CS;
+  std::vector<char> active;
   cudaGraphExec_t chunk = nullptr;
   size_t chunk_nodes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1292,6 +1379,91 @@ struct cfdg_batch {
 
 namespace {
 
+int fill_lists(cfdg_batch* B, WorkLists& W, const std::vector<char>& on, cudaStream_t s) {
+  static thread_local std::vector<int2> a, b, c, d;
+  a.clear(), b.clear(), c.clear(), d.clear();
+  for (auto& t : B->tiles)
+    if (on[t.x]) a.push_back(t);
+  for (auto& t : B->tiles1)
+    if (on[t.x]) b.push_back(t);
+  for (auto& t : B->ftiles)
+    if (on[t.x]) c.push_back(t);
+  for (auto& t : B->gtab)
+    if (on[t.x]) d.push_back(t);
+  int counts[4] = {(int)a.size(), (int)b.size(), (int)c.size(), (int)d.size()};
+  if (!a.empty()) CU(cudaMemcpyAsync(W.tiles, a.data(), a.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+  if (!b.empty()) CU(cudaMemcpyAsync(W.tiles1, b.data(), b.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+  if (!c.empty()) CU(cudaMemcpyAsync(W.ftiles, c.data(), c.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+  if (!d.empty()) CU(cudaMemcpyAsync(W.gtab, d.data(), d.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(W.counts, counts, sizeof(counts), cudaMemcpyHostToDevice, s));
+  CU(cudaStreamSynchronize(s));  // the staging vectors are reused
+  return 0;
+}
+
+// Coarse phase tables for the active cases (inactive ones contribute no rows).
+int fill_tab(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
+  const int nc = (int)B->cases.size(), nlev = B->nlev_all, w = nc + 1;
+  CoarseTab& T = B->h_tab;
+  static thread_local std::vector<int32_t> buf;
+  const size_t words = (size_t)nlev * w * (5 + 2 * MAXC);
+  buf.assign(words, 0);
+  int32_t *rows = buf.data(), *term = rows + nlev * w, *next = term + nlev * w, *live = next + nlev * w,
+          *grp = live + nlev * w, *fwd = grp + nlev * w, *bwd = fwd + (size_t)nlev * MAXC * w;
+  T.nc = nc;
+  T.nlev = 0;
+  for (int l = 0; l < nlev; ++l) {
+    int maxc = 0, anyg = 0;
+    auto lev = [&](int i) -> const CLev* {
+      return on[i] && l < B->cases[i]->C.nl ? &B->cases[i]->C.lv[l] : nullptr;
+    };
+    for (int i = 0; i < nc; ++i)
+      if (const CLev* L = lev(i)) {
+        if (!L->terminal) maxc = std::max(maxc, L->ncolors);
+        anyg |= L->ngroups > 0;
+        T.nlev = std::max(T.nlev, l + 1);
+      }
+    T.maxc[l] = maxc;
+    T.anyg[l] = anyg;
+    for (int i = 0; i < nc; ++i) {
+      const CLev* L = lev(i);
+      const bool nt = L && !L->terminal;
+      rows[l * w + i + 1] = rows[l * w + i] + (L ? L->n : 0);
+      term[l * w + i + 1] = term[l * w + i] + (L && L->terminal ? L->nblocks : 0);
+      next[l * w + i + 1] = next[l * w + i] + (nt ? B->cases[i]->C.lv[l + 1].n : 0);
+      live[l * w + i + 1] = live[l * w + i] + (nt ? L->n : 0);
+      grp[l * w + i + 1] = grp[l * w + i] + (L ? L->ngroups : 0);
+      for (int c = 0; c < MAXC; ++c) {
+        int nf = 0, nb = 0;
+        if (nt && c < L->ncolors) {
+          const auto& co = B->cases[i]->colors[l];
+          nf = co[c + 1] - co[c];
+          const int cb = L->ncolors - 1 - c;
+          nb = co[cb + 1] - co[cb];
+        }
+        fwd[(l * MAXC + c) * w + i + 1] = fwd[(l * MAXC + c) * w + i] + nf;
+        bwd[(l * MAXC + c) * w + i + 1] = bwd[(l * MAXC + c) * w + i] + nb;
+      }
+    }
+  }
+  T.rows = B->tab_buf;
+  T.term = T.rows + nlev * w;
+  T.next = T.term + nlev * w;
+  T.live = T.next + nlev * w;
+  T.grp = T.live + nlev * w;
+  T.fwd = T.grp + nlev * w;
+  T.bwd = T.fwd + (size_t)nlev * MAXC * w;
+  CU(cudaMemcpyAsync(B->tab_buf, buf.data(), words * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(B->d_tab, &T, sizeof(CoarseTab), cudaMemcpyHostToDevice, s));
+  CU(cudaStreamSynchronize(s));
+  return 0;
+}
+
+// The graph's lists and tables cover the cases marked in B->active.
+int set_active(cfdg_batch* B, cudaStream_t s) {
+  if (int e = fill_lists(B, B->run, B->active, s)) return e;
+  return fill_tab(B, B->active, s);
+}
+
 void launch_coarse(cfdg_batch* B, cudaStream_t s) {
   if (B->coop) {
     cudaLaunchConfig_t cfg = {};
@@ -1304,7 +1476,7 @@ void launch_coarse(cfdg_batch* B, cudaStream_t s) {
     at[0].val.cooperative = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, k_coarse_all, (const CCase*)B->d_cc, (const MState*)B->d_st, B->tab);
+    cudaLaunchKernelEx(&cfg, k_coarse_all, (const CCase*)B->d_cc, (const MState*)B->d_st, (const CoarseTab*)B->d_tab);
     return;
   }
   cudaLaunchConfig_t cfg = {};
@@ -1321,44 +1493,46 @@ void launch_coarse(cfdg_batch* B, cudaStream_t s) {
   cudaLaunchKernelEx(&cfg, k_coarse, (const CCase*)B->d_cc, (const MState*)B->d_st);
 }
 
+#define FINE(K, W, ...) K<<<B->g_fine, TILE, 0, s>>>(B->d_fc, B->d_st, (W).tiles, (W).counts, ##__VA_ARGS__)
+
 void enqueue_vcycle(cfdg_batch* B, cudaStream_t s) {
-  const int nt = B->ntiles;
-  if (B->ngtab) {
-    k_v_rhs<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
-    k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 0);
+  const WorkLists& W = B->run;
+  if (B->any_groups) {
+    FINE(k_v_rhs, W);
+    k_center0<<<B->g_g, 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 0);
   }
   // Two forward sweeps: red, black, red, black (the first red starts from x = 0).
-  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 0, 1);
-  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 1, 0);
-  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 0, 0);
-  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 1, 0);
-  if (B->ngtab) k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 1);
-  k_v_resid<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
-  if (B->ngtab) k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 2);
-  k_v_restrict<<<B->ntiles1, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles1);
+  FINE(k_rb, W, 0, 1);
+  FINE(k_rb, W, 1, 0);
+  FINE(k_rb, W, 0, 0);
+  FINE(k_rb, W, 1, 0);
+  if (B->any_groups) k_center0<<<B->g_g, 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 1);
+  FINE(k_v_resid, W);
+  if (B->any_groups) k_center0<<<B->g_g, 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 2);
+  k_v_restrict<<<B->g_1, TILE, 0, s>>>(B->d_fc, B->d_st, W.tiles1, W.counts + 1);
   launch_coarse(B, s);
-  k_v_prolong<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  FINE(k_v_prolong, W);
   // Two backward sweeps: black, red, black, red.
-  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 1, 0);
-  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 0, 0);
-  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 1, 0);
-  k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 0, 0);
-  if (B->ngtab) k_center0<<<B->ngtab, 256, 0, s>>>(B->d_fc, B->d_st, B->d_gtab, 1);
+  FINE(k_rb, W, 1, 0);
+  FINE(k_rb, W, 0, 0);
+  FINE(k_rb, W, 1, 0);
+  FINE(k_rb, W, 0, 0);
+  if (B->any_groups) k_center0<<<B->g_g, 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 1);
 }
 
 // One iteration of the per-case state machine.
 void enqueue_iteration(cfdg_batch* B, cudaStream_t s) {
-  const int nt = B->ntiles;
+  const WorkLists& W = B->run;
   const int nc = (int)B->cases.size();
-  k_op<<<B->ndtiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_dtiles);
-  k_update<<<B->ndtiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_dtiles);
-  k_outer<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
-  k_outer_resid<<<B->ndtiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_dtiles);
-  k_scale<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  FINE(k_op, W);
+  FINE(k_update, W);
+  FINE(k_outer, W);
+  FINE(k_outer_resid, W);
+  FINE(k_scale, W);
   k_start_state<<<(nc + 127) / 128, 128, 0, s>>>(B->d_st, nc);
   enqueue_vcycle(B, s);
-  k_rz<<<B->ndtiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_dtiles);
-  k_p<<<nt, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
+  FINE(k_rz, W);
+  FINE(k_p, W);
 }
 
 int ensure_graph(cfdg_batch* B) {
@@ -1392,149 +1566,151 @@ int case_of(cfdg_grid* G, std::shared_ptr<CaseState>& out) {
   return 0;
 }
 
+MState initial_state(double tol, uint64_t max_iter) {
+  MState m;
+  std::memset(&m, 0, sizeof(m));
+  m.state = IDLE;
+  m.tol = tol;
+  m.inner_tol = 1e-4;  // per outer step; FP32 reaches it comfortably
+  m.max_it = (int)std::min<uint64_t>(max_iter, 1u << 30);
+  m.max_inner = 200;
+  return m;
+}
+
+// Prologue of the cases marked in `on` (their states IDLE): b, terms, the closed
+// components' compatibility and gauge, |b_c|. A failed check sets FAIL/E031.
+int prologue(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
+  if (int e = fill_lists(B, B->pro, on, s)) return e;
+  FINE(k_rhs, B->pro);
+  count();
+  CU(cudaStreamSynchronize(s));
+  for (size_t i = 0; i < B->cases.size(); ++i) {
+    if (!on[i]) continue;
+    cfdg_grid* G = B->grids[i];
+    if (G->ncomp_groups == 0) {
+      CU(cudaMemcpyAsync(G->bc, G->b, G->h.cells * 8, cudaMemcpyDeviceToDevice, s));
+      continue;
+    }
+    int rc = plain_compat_center(G, s);
+    if (rc) {
+      MState f = initial_state(0, 0);
+      f.state = FAIL;
+      f.error = rc;
+      CU(cudaMemcpyAsync(&B->d_st[i], &f, sizeof(MState), cudaMemcpyHostToDevice, s));
+      CU(cudaStreamSynchronize(s));
+    }
+  }
+  FINE(k_norm, B->pro);
+  count();
+  CU(cudaGetLastError());
+  return 0;
+}
+
+// Epilogue of the converged cases marked in `on`: gauge of x, u -= dt grad x, p += x,
+// gauge of p.
+int epilogue(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
+  if (int e = fill_lists(B, B->epi, on, s)) return e;
+  for (size_t i = 0; i < B->cases.size(); ++i)
+    if (on[i] && B->grids[i]->ncomp_groups) plain_center(B->grids[i], B->grids[i]->x, s);
+  k_correct<<<B->g_f, 256, 0, s>>>(B->d_fc, B->d_st, B->epi.ftiles, B->epi.counts + 2);
+  FINE(k_addp, B->epi);
+  count(2);
+  for (size_t i = 0; i < B->cases.size(); ++i)
+    if (on[i] && B->grids[i]->ncomp_groups) plain_center(B->grids[i], B->h_fc[i].pfield, s);
+  CU(cudaGetLastError());
+  return 0;
+}
+
+void fill_info(const MState& m, cfdg_info& I) {
+  std::memset(&I, 0, sizeof(I));
+  I.iterations = (uint64_t)m.total_it;
+  I.relative_residual = m.state == DONE ? (m.norm < 1e-24 ? 0.0 : m.true_rel) : 0.0;
+  I.work_units = (uint64_t)m.total_it;
+  I.operator_applications = (uint64_t)m.total_it + (uint64_t)m.outer + 1;
+  I.true_residual_checks = (uint64_t)m.outer + 1;
+  I.preconditioner_applications = (uint64_t)m.total_it + (uint64_t)m.outer;
+  I.cycles = I.preconditioner_applications;
+  I.refinement_steps = (uint64_t)m.outer;
+}
+
 }  // namespace
 
-// Called by engine.cu: (re)pack a batch's device tables after its cases are known.
+// (Re)packs a batch's device tables after its cases are known.
 int cfdg_mixed_pack(cfdg_batch* B) {
   cudaStream_t s = B->own;
+  if (B->chunk) cudaGraphExecDestroy(B->chunk);
+  B->chunk = nullptr;
   B->arena.release();
   B->arena.ctx = B->ctx;
-  std::vector<int2> tiles, tiles1, ftiles, gtab, ptiles, dtiles;
+  B->tiles.clear(), B->tiles1.clear(), B->ftiles.clear(), B->gtab.clear();
   B->h_fc.clear();
   std::vector<CCase> cc;
-  for (size_t i = 0; i < B->cases.size(); ++i) {
+  const int nc = (int)B->cases.size();
+  B->any_groups = false;
+  B->nlev_all = 0;
+  for (int i = 0; i < nc; ++i) {
     FineCase F = B->cases[i]->F;
-    F.tile0 = (int)tiles.size();
-    for (int t = 0; t < F.ntiles; ++t) tiles.push_back(make_int2((int)i, t));
-    for (int t = 0; t < F.ntiles; ++t) dtiles.push_back(make_int2((int)i, t));
-    for (int t = 0; t < (F.n1 + TILE - 1) / TILE; ++t) tiles1.push_back(make_int2((int)i, t));
-    for (int t = 0; t < F.ntiles; ++t) ptiles.push_back(make_int2((int)i, t));
-    F.ftile0 = (int)ftiles.size();
+    for (int t = 0; t < F.ntiles; ++t) B->tiles.push_back(make_int2(i, t));
+    for (int t = 0; t < (F.n1 + TILE - 1) / TILE; ++t) B->tiles1.push_back(make_int2(i, t));
     F.nftiles = (int)((F.F + FTILE - 1) / FTILE);
-    for (int t = 0; t < F.nftiles; ++t) ftiles.push_back(make_int2((int)i, t));
-    for (int g = 0; g < F.ngroups; ++g) gtab.push_back(make_int2((int)i, g));
+    for (int t = 0; t < F.nftiles; ++t) B->ftiles.push_back(make_int2(i, t));
+    for (int g = 0; g < F.ngroups; ++g) B->gtab.push_back(make_int2(i, g));
+    B->any_groups |= F.ngroups > 0;
+    B->nlev_all = std::max(B->nlev_all, B->cases[i]->C.nl);
+    for (int l = 0; l < B->cases[i]->C.nl; ++l)
+      if (!B->cases[i]->C.lv[l].terminal && B->cases[i]->C.lv[l].ncolors > MAXC)
+        return fail(CFDG_ERR_UNSUPPORTED, "mixed form: too many colours on a coarse level");
     B->h_fc.push_back(F);
     cc.push_back(B->cases[i]->C);
   }
-  B->ntiles = (int)tiles.size();
-  B->ntiles1 = (int)tiles1.size();
-  B->nftiles = (int)ftiles.size();
-  B->ngtab = (int)gtab.size();
-  B->nptiles = (int)ptiles.size();
-  B->ndtiles = (int)dtiles.size();
   Arena& A = B->arena;
-  if (int e = A.upload(&B->d_dtiles, dtiles, s)) return e;
-  if (int e = A.upload(&B->d_ptiles, ptiles, s)) return e;
-  // Phase tables of the cooperative coarse-level kernel.
+  for (WorkLists* W : {&B->run, &B->pro, &B->epi}) {
+    if (int e = A.alloc(&W->tiles, B->tiles.size())) return e;
+    if (int e = A.alloc(&W->tiles1, B->tiles1.size())) return e;
+    if (int e = A.alloc(&W->ftiles, B->ftiles.size())) return e;
+    if (int e = A.alloc(&W->gtab, B->gtab.size())) return e;
+    if (int e = A.alloc(&W->counts, 4)) return e;
+  }
+  auto clamp = [](size_t n) { return (int)std::max<size_t>(1, std::min<size_t>(n, 152 * 8)); };
+  B->g_fine = clamp(B->tiles.size());
+  B->g_1 = clamp(B->tiles1.size());
+  B->g_f = clamp(B->ftiles.size());
+  B->g_g = clamp(B->gtab.size());
+  if (int e = A.upload(&B->d_fc, B->h_fc, s)) return e;
+  if (int e = A.upload(&B->d_cc, cc, s)) return e;
+  if (int e = A.alloc(&B->d_st, nc)) return e;
+  std::vector<MState> idle(nc, initial_state(0, 0));
+  for (auto& m : idle) m.state = DONE;  // nothing runs before a solve sets its cases
+  CU(cudaMemcpyAsync(B->d_st, idle.data(), sizeof(MState) * nc, cudaMemcpyHostToDevice, s));
+  if (B->h_st) cudaFreeHost(B->h_st);
+  CU(cudaMallocHost((void**)&B->h_st, sizeof(MState) * nc));
+  if (int e = A.alloc(&B->tab_buf, (size_t)B->nlev_all * (nc + 1) * (5 + 2 * MAXC) + 1)) return e;
+  if (int e = A.alloc(&B->d_tab, 1)) return e;
+  B->active.assign(nc, 1);
+  if (int e = set_active(B, s)) return e;
+  // Grid of the cooperative coarse-level kernel: all blocks co-resident.
   {
-    const int nc = (int)B->cases.size();
-    int nlev = 0;
-    for (auto& c : B->cases) nlev = std::max(nlev, c->C.nl);
-    CoarseTab T{};
-    T.nc = nc;
-    T.nlev = nlev;
-    std::vector<int32_t> rows, term, fwd, bwd, next, live, grp;
-    auto prefix = [&](std::vector<int32_t>& v, auto count) {
-      int acc = 0;
-      v.push_back(0);
-      for (int i = 0; i < nc; ++i) {
-        acc += count(i);
-        v.push_back(acc);
-      }
-    };
-    for (int l = 0; l < nlev; ++l) {
-      int maxc = 0, anyg = 0;
-      for (auto& c : B->cases)
-        if (l < c->C.nl) {
-          const CLev& L = c->C.lv[l];
-          if (!L.terminal) maxc = std::max(maxc, L.ncolors);
-          anyg |= L.ngroups > 0;
-        }
-      if (maxc > MAXC) return fail(CFDG_ERR_UNSUPPORTED, "mixed form: too many colours on a coarse level");
-      T.maxc[l] = maxc;
-      T.anyg[l] = anyg;
-      auto lev = [&](int i) -> const CLev* { return l < B->cases[i]->C.nl ? &B->cases[i]->C.lv[l] : nullptr; };
-      prefix(rows, [&](int i) { return lev(i) ? lev(i)->n : 0; });
-      prefix(term, [&](int i) { return lev(i) && lev(i)->terminal ? lev(i)->nblocks : 0; });
-      prefix(next, [&](int i) { return lev(i) && !lev(i)->terminal ? B->cases[i]->C.lv[l + 1].n : 0; });
-      prefix(live, [&](int i) { return lev(i) && !lev(i)->terminal ? lev(i)->n : 0; });
-      prefix(grp, [&](int i) { return lev(i) ? lev(i)->ngroups : 0; });
-      for (int c = 0; c < MAXC; ++c) {
-        prefix(fwd, [&](int i) {
-          const CLev* L = lev(i);
-          if (!L || L->terminal || c >= L->ncolors) return 0;
-          return B->cases[i]->colors[l][c + 1] - B->cases[i]->colors[l][c];
-        });
-        prefix(bwd, [&](int i) {
-          const CLev* L = lev(i);
-          if (!L || L->terminal || c >= L->ncolors) return 0;
-          const int cb = L->ncolors - 1 - c;
-          return B->cases[i]->colors[l][cb + 1] - B->cases[i]->colors[l][cb];
-        });
-      }
-    }
-    int *d;
-    if (int e = A.upload(&d, rows, s)) return e;
-    T.rows = d;
-    if (int e = A.upload(&d, term, s)) return e;
-    T.term = d;
-    if (int e = A.upload(&d, fwd, s)) return e;
-    T.fwd = d;
-    if (int e = A.upload(&d, bwd, s)) return e;
-    T.bwd = d;
-    if (int e = A.upload(&d, next, s)) return e;
-    T.next = d;
-    if (int e = A.upload(&d, live, s)) return e;
-    T.live = d;
-    if (int e = A.upload(&d, grp, s)) return e;
-    T.grp = d;
-    B->tab = T;
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const size_t dsm = 2 * B->cases.size() * sizeof(CLev);
+    const size_t dsm = 2 * (size_t)nc * sizeof(CLev);
     if (dsm > 48 * 1024) cudaFuncSetAttribute(k_coarse_all, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+    B->coop = true;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_coarse_all, 512, dsm) != cudaSuccess || per < 1) {
       cudaGetLastError();
       B->coop = false;
     }
-    B->coop_blocks = sms * std::min(per, 2);
+    B->coop_blocks = sms * std::max(1, std::min(per, 2));
   }
-  // Coarse-level clusters: 16 CTAs when the device allows that non-portable size, else 8.
-  B->csize = CS;
-  if (cudaFuncSetAttribute(k_coarse, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
-    cudaGetLastError();
-    B->csize = 8;
-  } else {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(B->csize, 1, 1);
-    cfg.blockDim = dim3(CT, 1, 1);
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = B->csize;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, k_coarse, &cfg) != cudaSuccess || nclusters < 1) {
+  if (!B->coop) {
+    // One cluster per case: 16 CTAs when that non-portable size is allowed, else 8.
+    B->csize = CS;
+    if (cudaFuncSetAttribute(k_coarse, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
       cudaGetLastError();
       B->csize = 8;
     }
   }
-  if (int e = A.upload(&B->d_tiles, tiles, s)) return e;
-  if (int e = A.upload(&B->d_tiles1, tiles1, s)) return e;
-  if (int e = A.upload(&B->d_ftiles, ftiles, s)) return e;
-  if (int e = A.upload(&B->d_gtab, gtab, s)) return e;
-  if (int e = A.upload(&B->d_fc, B->h_fc, s)) return e;
-  if (int e = A.upload(&B->d_cc, cc, s)) return e;
-  if (int e = A.alloc(&B->d_st, B->cases.size())) return e;
-  CU(cudaMemsetAsync(B->d_st, 0, sizeof(MState) * B->cases.size(), s));
-  if (B->h_st) cudaFreeHost(B->h_st);
-  CU(cudaMallocHost((void**)&B->h_st, sizeof(MState) * B->cases.size()));
   CU(cudaStreamSynchronize(s));
-  if (B->chunk) cudaGraphExecDestroy(B->chunk);
-  B->chunk = nullptr;
   return ensure_graph(B);
 }
 
@@ -1553,50 +1729,19 @@ int cfdg_mixed_project(cfdg_batch* B, double* const* d_u, double* const* d_p, co
   const int nc = (int)B->cases.size();
   if (codes)
     for (int i = 0; i < nc; ++i) codes[i] = 0;
-  // Per-solve I/O pointers into the case table.
   for (int i = 0; i < nc; ++i) {
     B->h_fc[i].u = d_u[i];
     B->h_fc[i].pfield = d_p[i];
     B->h_fc[i].dt = dt[i];
   }
   CU(cudaMemcpyAsync(B->d_fc, B->h_fc.data(), sizeof(FineCase) * nc, cudaMemcpyHostToDevice, s));
-  std::vector<MState> st(nc);
-  for (int i = 0; i < nc; ++i) {
-    std::memset(&st[i], 0, sizeof(MState));
-    st[i].state = IDLE;
-    st[i].tol = tol;
-    st[i].inner_tol = 1e-4;  // per outer step; FP32 reaches it comfortably
-    st[i].max_it = (int)std::min<uint64_t>(max_iter, 1u << 30);
-    st[i].max_inner = 200;
-  }
+  std::vector<MState> st(nc, initial_state(tol, max_iter));
   CU(cudaMemcpyAsync(B->d_st, st.data(), sizeof(MState) * nc, cudaMemcpyHostToDevice, s));
   CU(cudaEventRecord(B->ev0, s));
-  k_rhs<<<B->ntiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
-  count();
-  // Compatibility and gauge of closed components: per grid, with the plain kernels.
-  CU(cudaStreamSynchronize(s));
-  for (int i = 0; i < nc; ++i) {
-    cfdg_grid* G = B->grids[i];
-    if (G->ncomp_groups == 0) {
-      CU(cudaMemcpyAsync(G->bc, G->b, G->h.cells * 8, cudaMemcpyDeviceToDevice, s));
-      continue;
-    }
-    int rc = plain_compat_center(G, s);
-    if (codes) codes[i] = rc;
-    if (rc) {
-      st[i].state = FAIL;
-      st[i].error = rc;
-    }
-  }
-  CU(cudaStreamSynchronize(s));
-  for (int i = 0; i < nc; ++i)
-    if (st[i].state == FAIL) {
-      MState f = st[i];
-      CU(cudaMemcpyAsync(&B->d_st[i], &f, sizeof(MState), cudaMemcpyHostToDevice, s));
-    }
-  k_norm<<<B->ndtiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_dtiles);
-  count();
-  CU(cudaGetLastError());
+  std::vector<char> all(nc, 1);
+  if (int e = prologue(B, all, s)) return e;
+  B->active = all;
+  if (int e = set_active(B, s)) return e;
   Poller P;
   P.fn = poll;
   P.ctx = poll_ctx;
@@ -1609,31 +1754,31 @@ int cfdg_mixed_project(cfdg_batch* B, double* const* d_u, double* const* d_p, co
   for (;;) {
     CU(cudaMemcpyAsync(B->h_st, B->d_st, sizeof(MState) * nc, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
-    bool all = true;
-    for (int i = 0; i < nc; ++i) all &= B->h_st[i].state == DONE || B->h_st[i].state == FAIL;
-    if (all) break;
+    bool all_done = true, shrink = false;
+    for (int i = 0; i < nc; ++i) {
+      const bool fin = B->h_st[i].state == DONE || B->h_st[i].state == FAIL;
+      all_done &= fin;
+      if (fin && B->active[i]) {
+        B->active[i] = 0;  // finished cases leave the work-lists
+        shrink = true;
+      }
+    }
+    if (all_done) break;
     if (int c = P.check()) {
       status = fail(c, c == CFDG_CANCELLED ? "cancelled" : "wall_time_limit");
       break;
     }
+    if (shrink)
+      if (int e = set_active(B, s)) return e;
     CU(cudaGraphLaunch(B->chunk, s));
     count(B->chunk_nodes);
     chunks += 1;
   }
   cudaEventRecord(lp1, s);
   if (status == 0) {
-    // Epilogue for converged cases: gauge of x, face correction, p += x, gauge of p.
-    for (int i = 0; i < nc; ++i) {
-      cfdg_grid* G = B->grids[i];
-      if (B->h_st[i].state == DONE && G->ncomp_groups) plain_center(G, G->x, s);
-    }
-    k_correct<<<B->nftiles, 256, 0, s>>>(B->d_fc, B->d_st, B->d_ftiles);
-    k_addp<<<B->ntiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_tiles);
-    count(2);
-    for (int i = 0; i < nc; ++i) {
-      cfdg_grid* G = B->grids[i];
-      if (B->h_st[i].state == DONE && G->ncomp_groups) plain_center(G, d_p[i], s);
-    }
+    std::vector<char> done(nc, 0);
+    for (int i = 0; i < nc; ++i) done[i] = B->h_st[i].state == DONE;
+    if (int e = epilogue(B, done, s)) return e;
   }
   CU(cudaEventRecord(B->ev1, s));
   CU(cudaEventSynchronize(B->ev1));
@@ -1645,19 +1790,10 @@ int cfdg_mixed_project(cfdg_batch* B, double* const* d_u, double* const* d_p, co
   for (int i = 0; i < nc; ++i) {
     const MState& m = B->h_st[i];
     if (infos) {
-      cfdg_info& I = infos[i];
-      std::memset(&I, 0, sizeof(I));
-      I.iterations = (uint64_t)m.total_it;
-      I.relative_residual = m.state == DONE ? (m.norm < 1e-24 ? 0.0 : m.true_rel) : 0.0;
-      I.work_units = (uint64_t)m.total_it;
-      I.operator_applications = (uint64_t)m.total_it + (uint64_t)m.outer + 1;
-      I.true_residual_checks = (uint64_t)m.outer + 1;
-      I.preconditioner_applications = (uint64_t)m.total_it + (uint64_t)m.outer;
-      I.cycles = I.preconditioner_applications;
-      I.refinement_steps = (uint64_t)m.outer;
-      I.device_seconds = ms * 1e-3;
-      I.graph_launches = chunks;
-      I.loop_seconds = lms * 1e-3;
+      fill_info(m, infos[i]);
+      infos[i].device_seconds = ms * 1e-3;
+      infos[i].graph_launches = chunks;
+      infos[i].loop_seconds = lms * 1e-3;
     }
     if (codes && codes[i] == 0) {
       if (status) codes[i] = status;
@@ -1691,6 +1827,13 @@ std::vector<cfdg_grid*> lock_order(const std::vector<cfdg_grid*>& g) {
   v.erase(std::unique(v.begin(), v.end()), v.end());
   return v;
 }
+
+struct Locks {
+  std::vector<std::unique_lock<std::mutex>> held;
+  explicit Locks(const std::vector<cfdg_grid*>& grids) {
+    for (auto* G : lock_order(grids)) held.emplace_back(G->mu);
+  }
+};
 }  // namespace
 
 cfdg_batch* cfdg_mixed_new(cfdg_context* ctx) {
@@ -1708,14 +1851,43 @@ cfdg_batch* cfdg_mixed_new(cfdg_context* ctx) {
 
 void cfdg_mixed_delete(cfdg_batch* B) {
   if (!B) return;
-  // The caller's stream may already be gone; the batch's own stream and a device-wide
-  // event wait cover its work.
+  // The caller's stream may already be gone; the batch's own stream and its last
+  // event cover its work.
   if (B->own) cudaStreamSynchronize(B->own);
   if (B->ev1) cudaEventSynchronize(B->ev1);
   delete B;
 }
 
 void cfdg_mixed_set_stream(cfdg_batch* B, cudaStream_t s) { B->stream = s ? s : B->own; }
+
+// ----------------------------------------------------------------- serving: continuous batching
+// A server keeps a set of resident grids (one slot each) and a queue of projection
+// requests. Each progress() round finishes the cases that converged (epilogue, result
+// recorded), admits queued requests into free slots up to `max_active` (prologue), points
+// the work-lists at the active cases and replays one chunk of the iteration graph, so a
+// request that arrives while others run joins them at the next chunk boundary. A grid
+// serves its requests in order, one at a time (a time step needs the previous one).
+struct cfdg_server {
+  cfdg_batch* B = nullptr;
+  int max_active = 0;
+  struct Req {
+    uint64_t ticket;
+    int grid;
+    double *u, *p;
+    double dt, tol;
+    uint64_t max_iter;
+  };
+  std::deque<Req> queue;
+  std::vector<uint64_t> running;  // ticket per case, 0 when idle
+  struct Done {
+    cfdg_info info;
+    int32_t code;
+  };
+  std::map<uint64_t, Done> results;
+  uint64_t next_ticket = 1;
+  bool launched = false;
+  std::mutex mu;
+};
 
 extern "C" {
 
@@ -1731,6 +1903,11 @@ int cfdg_batch_create(cfdg_context* ctx, cfdg_grid* const* grids, int32_t n, cfd
       cfdg_mixed_delete(B);
       return fail(CFDG_ERR_INVALID, "every grid of a batch must be open on the batch's context");
     }
+    for (int j = 0; j < i; ++j)
+      if (grids[j] == G) {
+        cfdg_mixed_delete(B);
+        return fail(CFDG_ERR_INVALID, "a grid can appear once in a batch");
+      }
     std::lock_guard<std::mutex> lk(G->mu);
     if (int e = prepare_multigrid(G)) {
       cfdg_mixed_delete(B);
@@ -1764,9 +1941,7 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
                            double* algorithmic_bytes) {
   if (!B || reps < 1) return fail(CFDG_ERR_INVALID, "invalid arguments");
   CU(cudaSetDevice(B->ctx->device));
-  auto order = lock_order(B->grids);
-  std::vector<std::unique_lock<std::mutex>> locks;
-  for (auto* G : order) locks.emplace_back(G->mu);
+  Locks locks(B->grids);
   const int nc = (int)B->cases.size();
   cudaStream_t s = B->stream;
   // Every case in the inner-iteration state, on the vectors of the last solve.
@@ -1779,21 +1954,20 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
     run[i].counter = 0;
   }
   CU(cudaMemcpyAsync(B->d_st, run.data(), sizeof(MState) * nc, cudaMemcpyHostToDevice, s));
-  double cells = 0, n1 = 0;
-  for (auto& F : B->h_fc) {
-    cells += F.N;
-    n1 += F.n1;
-  }
+  B->active.assign(nc, 1);
+  if (int e = set_active(B, s)) return e;
+  double cells = 0;
+  for (auto& F : B->h_fc) cells += F.N;
   double bytes = 0;
   auto launch = [&]() {
     switch (which) {
       case 0:  // one red-black half sweep over every case's fine level
-        k_rb<<<B->nptiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_ptiles, 1, 0);
+        FINE(k_rb, B->run, 1, 0);
         break;
       case 1:  // FP32 operator q = A p (with p.q)
-        k_op<<<B->ndtiles, TILE, 0, s>>>(B->d_fc, B->d_st, B->d_dtiles);
+        FINE(k_op, B->run);
         break;
-      case 2:  // all coarse levels, one cluster per case
+      case 2:  // all coarse levels of all cases
         launch_coarse(B, s);
         break;
       default:
@@ -1801,10 +1975,8 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
         break;
     }
   };
-  if (which == 0) bytes = 9.0 * cells;       // half the cells: rhs, diag, u16 flags, x out; the other half's x in
+  if (which == 0) bytes = 9.0 * cells;       // half the cells: rhs, 1/diag, u16 flags, x out; the other half's x in
   else if (which == 1) bytes = 10.0 * cells; // p in, u16 flags, q out
-  else if (which == 2) bytes = 0.0;
-  else bytes = 0.0;
   launch();
   launch();
   CU(cudaEventRecord(B->ev0, s));
@@ -1818,7 +1990,6 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
   CU(cudaGetLastError());
   if (ms_per_launch) *ms_per_launch = ms / reps;
   if (algorithmic_bytes) *algorithmic_bytes = bytes;
-  (void)n1;
   return 0;
 }
 
@@ -1826,9 +1997,7 @@ int cfdg_batch_project_device(cfdg_batch* B, double* const* d_u, double* const* 
                               uint64_t max_iter, cfdg_poll_fn poll, void* poll_ctx, cfdg_info* infos, int32_t* codes) {
   if (!B || !d_u || !d_p || !dt) return fail(CFDG_ERR_INVALID, "invalid batch arguments");
   CU(cudaSetDevice(B->ctx->device));
-  auto order = lock_order(B->grids);
-  std::vector<std::unique_lock<std::mutex>> locks;
-  for (auto* G : order) locks.emplace_back(G->mu);
+  Locks locks(B->grids);
   if (int e = refresh_batch(B)) return e;
   return cfdg_mixed_project(B, d_u, d_p, dt, tol, max_iter, poll, poll_ctx, infos, codes);
 }
@@ -1837,9 +2006,7 @@ int cfdg_batch_project(cfdg_batch* B, double* const* u, double* const* p, const 
                        uint64_t max_iter, cfdg_poll_fn poll, void* poll_ctx, cfdg_info* infos, int32_t* codes) {
   if (!B || !u || !p || !dt) return fail(CFDG_ERR_INVALID, "invalid batch arguments");
   CU(cudaSetDevice(B->ctx->device));
-  auto order = lock_order(B->grids);
-  std::vector<std::unique_lock<std::mutex>> locks;
-  for (auto* G : order) locks.emplace_back(G->mu);
+  Locks locks(B->grids);
   if (int e = refresh_batch(B)) return e;
   const int nc = (int)B->grids.size();
   std::vector<double*> du(nc), dp(nc);
@@ -1863,6 +2030,146 @@ int cfdg_batch_project(cfdg_batch* B, double* const* u, double* const* p, const 
   }
   CU(cudaStreamSynchronize(s));
   return 0;
+}
+
+// ------------------------------------------------------------------ server
+int cfdg_server_create(cfdg_context* ctx, cfdg_grid* const* grids, int32_t n, int32_t max_active,
+                       cfdg_server** out) {
+  if (!out || max_active < 1) return fail(CFDG_ERR_INVALID, "invalid server arguments");
+  *out = nullptr;
+  cfdg_batch* B = nullptr;
+  if (int e = cfdg_batch_create(ctx, grids, n, &B)) return e;
+  auto* S = new cfdg_server();
+  S->B = B;
+  S->max_active = max_active;
+  S->running.assign(n, 0);
+  B->active.assign(n, 0);
+  {
+    Locks locks(B->grids);
+    if (int e = set_active(B, B->stream)) {
+      cfdg_batch_destroy(B);
+      delete S;
+      return e;
+    }
+  }
+  *out = S;
+  return 0;
+}
+
+void cfdg_server_destroy(cfdg_server* S) {
+  if (!S) return;
+  cfdg_batch_destroy(S->B);
+  delete S;
+}
+
+int cfdg_server_set_stream(cfdg_server* S, void* stream) {
+  if (!S) return fail(CFDG_ERR_INVALID, "null server");
+  return cfdg_batch_set_stream(S->B, stream);
+}
+
+int cfdg_server_submit(cfdg_server* S, int32_t grid, double* d_u, double* d_p, double dt, double tol,
+                       uint64_t max_iter, uint64_t* ticket) {
+  if (!S || grid < 0 || grid >= (int)S->B->grids.size() || !d_u || !d_p || !ticket)
+    return fail(CFDG_ERR_INVALID, "invalid submit arguments");
+  std::lock_guard<std::mutex> lk(S->mu);
+  *ticket = S->next_ticket++;
+  S->queue.push_back({*ticket, grid, d_u, d_p, dt, tol, max_iter});
+  return 0;
+}
+
+int cfdg_server_progress(cfdg_server* S, int32_t* finished) {
+  if (!S) return fail(CFDG_ERR_INVALID, "null server");
+  std::lock_guard<std::mutex> lk(S->mu);
+  cfdg_batch* B = S->B;
+  CU(cudaSetDevice(B->ctx->device));
+  Locks locks(B->grids);
+  cudaStream_t s = B->stream;
+  const int nc = (int)B->cases.size();
+  int nfin = 0;
+  // 1. Finish the cases that converged or failed in the last chunk.
+  CU(cudaMemcpyAsync(B->h_st, B->d_st, sizeof(MState) * nc, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  std::vector<char> done(nc, 0), fin(nc, 0);
+  bool changed = false;
+  for (int i = 0; i < nc; ++i) {
+    if (!S->running[i]) continue;
+    const int st = B->h_st[i].state;
+    if (st == DONE || st == FAIL) {
+      fin[i] = 1;
+      done[i] = st == DONE;
+    }
+  }
+  bool any_done = false;
+  for (int i = 0; i < nc; ++i) any_done |= done[i] != 0;
+  if (any_done)
+    if (int e = epilogue(B, done, s)) return e;
+  if (any_done) CU(cudaStreamSynchronize(s));
+  for (int i = 0; i < nc; ++i) {
+    if (!fin[i]) continue;
+    cfdg_server::Done d;
+    fill_info(B->h_st[i], d.info);
+    d.code = B->h_st[i].state == DONE ? 0 : (B->h_st[i].error ? B->h_st[i].error : CFDG_E033);
+    S->results[S->running[i]] = d;
+    S->running[i] = 0;
+    B->active[i] = 0;
+    changed = true;
+    ++nfin;
+  }
+  // 2. Admit queued requests into free slots (in arrival order; one per grid at a time).
+  int nactive = 0;
+  for (int i = 0; i < nc; ++i) nactive += S->running[i] != 0;
+  std::vector<char> admit(nc, 0);
+  bool any_admit = false;
+  for (auto it = S->queue.begin(); it != S->queue.end() && nactive < S->max_active;) {
+    if (S->running[it->grid] || admit[it->grid]) {
+      ++it;
+      continue;
+    }
+    const int i = it->grid;
+    B->h_fc[i].u = it->u;
+    B->h_fc[i].pfield = it->p;
+    B->h_fc[i].dt = it->dt;
+    CU(cudaMemcpyAsync(&B->d_fc[i], &B->h_fc[i], sizeof(FineCase), cudaMemcpyHostToDevice, s));
+    MState m = initial_state(it->tol, it->max_iter);
+    CU(cudaMemcpyAsync(&B->d_st[i], &m, sizeof(MState), cudaMemcpyHostToDevice, s));
+    S->running[i] = it->ticket;
+    admit[i] = 1;
+    any_admit = true;
+    B->active[i] = 1;
+    ++nactive;
+    changed = true;
+    it = S->queue.erase(it);
+  }
+  if (any_admit)
+    if (int e = prologue(B, admit, s)) return e;
+  // 3. Point the work-lists at the active cases and run one chunk.
+  if (changed)
+    if (int e = set_active(B, s)) return e;
+  if (nactive > 0) {
+    CU(cudaGraphLaunch(B->chunk, s));
+    count(B->chunk_nodes);
+  }
+  if (finished) *finished = nfin;
+  return 0;
+}
+
+int cfdg_server_result(cfdg_server* S, uint64_t ticket, cfdg_info* info, int32_t* code) {
+  if (!S) return fail(CFDG_ERR_INVALID, "null server");
+  std::lock_guard<std::mutex> lk(S->mu);
+  auto it = S->results.find(ticket);
+  if (it == S->results.end()) return CFDG_PENDING;
+  if (info) *info = it->second.info;
+  if (code) *code = it->second.code;
+  S->results.erase(it);
+  return 0;
+}
+
+int cfdg_server_pending(cfdg_server* S) {
+  if (!S) return 0;
+  std::lock_guard<std::mutex> lk(S->mu);
+  int n = (int)S->queue.size();
+  for (auto t : S->running) n += t != 0;
+  return n;
 }
 
 }  // extern "C"

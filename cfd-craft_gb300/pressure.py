@@ -371,3 +371,61 @@ class Batch:
         if rc:
             raise PressureError(rc, E.last_error())
         return ms.value, b.value
+
+
+class Server:
+    """Continuous-batching projection server over resident grids (cfdg_server)."""
+
+    def __init__(self, device_grids, max_active: int, ctx: Context = None):
+        self.ctx = ctx or device_grids[0].ctx
+        self.grids = list(device_grids)
+        L = E.load()
+        arr = (C.c_void_p * len(self.grids))(*[g.h for g in self.grids])
+        h = C.c_void_p()
+        rc = L.cfdg_server_create(self.ctx.h, arr, len(self.grids), int(max_active), C.byref(h))
+        if rc:
+            raise PressureError(rc, E.last_error())
+        self.h = h
+        self.L = L
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cfdg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise PressureError(rc, E.last_error())
+
+    def set_stream(self, stream_handle: int):
+        self._check(self.L.cfdg_server_set_stream(self.h, C.c_void_p(stream_handle or None)))
+
+    def submit(self, grid_index: int, u_ptr: int, p_ptr: int, dt, tol, max_iter) -> int:
+        t = C.c_uint64()
+        self._check(self.L.cfdg_server_submit(self.h, int(grid_index), C.c_void_p(u_ptr), C.c_void_p(p_ptr),
+                                              float(dt), float(tol), int(max_iter), C.byref(t)))
+        return t.value
+
+    def progress(self) -> int:
+        n = C.c_int32()
+        self._check(self.L.cfdg_server_progress(self.h, C.byref(n)))
+        return n.value
+
+    def result(self, ticket: int):
+        """(code, LinearInfo) when finished, None while pending."""
+        info = E.Info()
+        code = C.c_int32()
+        rc = self.L.cfdg_server_result(self.h, int(ticket), C.byref(info), C.byref(code))
+        if rc == E.CFDG_PENDING:
+            return None
+        self._check(rc)
+        return int(code.value), LinearInfo(info.iterations, info.relative_residual, info.as_dict())
+
+    def pending(self) -> int:
+        return int(self.L.cfdg_server_pending(self.h))

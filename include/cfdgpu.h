@@ -207,6 +207,32 @@ int cfdg_batch_project_device(cfdg_batch *batch, double *const *d_u, double *con
                               double tol, uint64_t max_iter, cfdg_poll_fn poll, void *poll_ctx, cfdg_info *infos,
                               int32_t *codes);
 
+/* ------------------------------------------------------------------ serving (continuous batching)
+ * A server keeps `n` resident grids (their topology, hierarchy and FP32 state stay in HBM
+ * across requests; cfdg_grid_open already refused grids beyond the context's HBM budget)
+ * and runs projection requests on them in the mixed form. cfdg_server_progress() is one
+ * scheduling round: it finishes the requests whose cases converged in the previous round
+ * (face correction, p update, result recorded), admits queued requests into free slots
+ * (at most max_active running at once; one request per grid at a time, in arrival order),
+ * and replays one chunk of the batched iteration over the running cases, so requests that
+ * arrive while others are on the GPU join them at the next chunk. Results are
+ * bit-identical to the same request solved alone. No reference counterpart: the
+ * reference runs one case per process. */
+typedef struct cfdg_server cfdg_server;
+int cfdg_server_create(cfdg_context *ctx, cfdg_grid *const *grids, int32_t n, int32_t max_active,
+                       cfdg_server **out);
+void cfdg_server_destroy(cfdg_server *server);
+int cfdg_server_set_stream(cfdg_server *server, void *stream);
+/* Queues pressure::project on grid `grid` for device arrays d_u (F doubles), d_p (N doubles),
+ * which must stay valid until the ticket's result is read. */
+int cfdg_server_submit(cfdg_server *server, int32_t grid, double *d_u, double *d_p, double dt, double tol,
+                       uint64_t max_iter, uint64_t *ticket);
+int cfdg_server_progress(cfdg_server *server, int32_t *finished);
+/* 0 and the result (consumed) when the ticket finished, CFDG_PENDING otherwise. */
+int cfdg_server_result(cfdg_server *server, uint64_t ticket, cfdg_info *info, int32_t *code);
+/* Requests queued or running. */
+int cfdg_server_pending(cfdg_server *server);
+
 /* Device memory the grid holds, in bytes (admission accounting). */
 uint64_t cfdg_grid_device_bytes(const cfdg_grid *grid);
 
