@@ -255,14 +255,15 @@ constexpr int RT = TILE / 32;  // rows per tile: one warp per row
   MState& S = ST[t.x];                                                                \
   if (!(STATE_TEST)) return;                                                          \
   __shared__ __align__(16) FineCase sF;                                               \
-  __syncthreads(); /* the previous tile's readers of sF are done */                   \
-  {                                                                                   \
+  if (cached_ != t.x) { /* block-uniform: copy the case descriptor */                 \
+    __syncthreads(); /* the previous tile's readers of sF are done */                 \
     const long long* src_ = reinterpret_cast<const long long*>(&FC[t.x]);             \
     long long* dst_ = reinterpret_cast<long long*>(&sF);                              \
     for (int w_ = threadIdx.x; w_ < (int)(sizeof(FineCase) / 8); w_ += blockDim.x)     \
       dst_[w_] = src_[w_];                                                            \
+    cached_ = t.x;                                                                    \
+    __syncthreads();                                                                  \
   }                                                                                   \
-  __syncthreads();                                                                    \
   const FineCase& F = sF;                                                             \
   const int lt = t.y;                                                                 \
   const int nx_ = F.n[0];                                                             \
@@ -325,7 +326,7 @@ __device__ __forceinline__ float op32r(const FineCase& F, const float* __restric
 }
 
 // A: q = A32 p, alpha = rz / (p.q) (E032 when not positive).
-__device__ __forceinline__ void b_op(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_op(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN)
   float hi = 0.0f, lo = 0.0f;
@@ -350,11 +351,12 @@ __device__ __forceinline__ void b_op(const FineCase* FC, MState* ST, const int2 
 }
 __global__ void __launch_bounds__(TILE) k_op(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_op(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_op(FC, ST, tiles[ti], cached_);
 }
 
 // B: e += alpha p, r -= alpha q; |r| decides the end of the inner solve.
-__device__ __forceinline__ void b_update(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_update(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN)
   const float alpha = (float)S.alpha;
@@ -375,11 +377,12 @@ __device__ __forceinline__ void b_update(const FineCase* FC, MState* ST, const i
 }
 __global__ void __launch_bounds__(TILE) k_update(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_update(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_update(FC, ST, tiles[ti], cached_);
 }
 
 // C1: x += |r| e (the residual is formed by k_outer_resid once every block has updated x).
-__device__ __forceinline__ void b_outer(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_outer(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == OUTER)
   if (!S.has_e) return;
   const double scale = S.scale;
@@ -387,11 +390,12 @@ __device__ __forceinline__ void b_outer(const FineCase* FC, MState* ST, const in
 }
 __global__ void __launch_bounds__(TILE) k_outer(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_outer(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_outer(FC, ST, tiles[ti], cached_);
 }
 
 // r = b_c - A x in FP64; the true residual decides convergence.
-__device__ __forceinline__ void b_outer_resid(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_outer_resid(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == OUTER)
   double acc = 0.0;
@@ -418,11 +422,12 @@ __device__ __forceinline__ void b_outer_resid(const FineCase* FC, MState* ST, co
 }
 __global__ void __launch_bounds__(TILE) k_outer_resid(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_outer_resid(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_outer_resid(FC, ST, tiles[ti], cached_);
 }
 
 // C2: r32 = r / |r|, e = 0.
-__device__ __forceinline__ void b_scale(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_scale(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == SCALE)
   const double inv = 1.0 / S.scale;
   for (int c = cb + threadIdx.x; c < ce; c += TILE) {
@@ -432,7 +437,8 @@ __device__ __forceinline__ void b_scale(const FineCase* FC, MState* ST, const in
 }
 __global__ void __launch_bounds__(TILE) k_scale(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_scale(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_scale(FC, ST, tiles[ti], cached_);
 }
 
 __global__ void k_start_state(MState* ST, int n) {
@@ -444,7 +450,7 @@ __global__ void k_start_state(MState* ST, int n) {
 }
 
 // F: rz' = r.z; START: rz = rz', p = z (beta = 0) -> RUN; RUN: beta = rz'/rz.
-__device__ __forceinline__ void b_rz(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_rz(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   float hi = 0.0f, lo = 0.0f;
@@ -462,11 +468,12 @@ __device__ __forceinline__ void b_rz(const FineCase* FC, MState* ST, const int2 
 }
 __global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_rz(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_rz(FC, ST, tiles[ti], cached_);
 }
 
 // G: p = z + beta p (z is the V-cycle's level-0 solution x0).
-__device__ __forceinline__ void b_p(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_p(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == RUN)
   const float beta = (float)S.beta;
   if (S.beta == 0.0) {
@@ -477,26 +484,28 @@ __device__ __forceinline__ void b_p(const FineCase* FC, MState* ST, const int2 t
 }
 __global__ void __launch_bounds__(TILE) k_p(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_p(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_p(FC, ST, tiles[ti], cached_);
 }
 
 // ----------------------------------------------------------------- V-cycle, level 0
 // rhs0 = r32 (only when level 0 has closed groups; otherwise rhs0 is r32 itself).
-__device__ __forceinline__ void b_v_rhs(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_v_rhs(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   if (F.rhs0 == F.r32) return;
   for (int c = cb + threadIdx.x; c < ce; c += TILE) F.rhs0[c] = F.r32[c];
 }
 __global__ void __launch_bounds__(TILE) k_v_rhs(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_rhs(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_rhs(FC, ST, tiles[ti], cached_);
 }
 
 // Red-black Gauss-Seidel half sweep on level 0: cells with (i+j+k)%2 == color. Lanes
 // walk the x-pairs (2m, 2m+1) of the warp's row, of which exactly one has the colour.
 // first: x is taken as zero (the cycle's initial guess). Cells outside the operator
 // (solid, sealed singletons) are kept at zero.
-__device__ __forceinline__ void b_rb(const FineCase* FC, MState* ST, const int2 t, int color, int first) {
+__device__ __forceinline__ void b_rb(const FineCase* FC, MState* ST, const int2 t, int& cached_, int color, int first) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   int j, k, rb;
   if (!warp_row(F, lt, warp, j, k, rb)) return;
@@ -542,11 +551,12 @@ __device__ __forceinline__ void b_rb(const FineCase* FC, MState* ST, const int2 
 }
 __global__ void __launch_bounds__(TILE) k_rb(const FineCase* FC, MState* ST, const int2* tiles, const int* count, int color, int first) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_rb(FC, ST, tiles[ti], color, first);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_rb(FC, ST, tiles[ti], cached_, color, first);
 }
 
 // res0 = rhs0 - A0 x0 (A0 = diag - sum w on interior faces).
-__device__ __forceinline__ void b_v_resid(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_v_resid(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   int j, k, rb;
   if (!warp_row(F, lt, warp, j, k, rb)) return;
@@ -586,7 +596,8 @@ __device__ __forceinline__ void b_v_resid(const FineCase* FC, MState* ST, const 
 }
 __global__ void __launch_bounds__(TILE) k_v_resid(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_resid(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_resid(FC, ST, tiles[ti], cached_);
 }
 
 // rhs1 = R res0: level-1 rows gather their level-0 children. Tiles index level-1 rows.
@@ -607,7 +618,7 @@ __global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState*
 }
 
 // x0 += P x1.
-__device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   for (int c = cb + threadIdx.x; c < ce; c += TILE) {
     const int b = F.p_off[c], e = F.p_off[c + 1];
@@ -619,7 +630,8 @@ __device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, cons
 }
 __global__ void __launch_bounds__(TILE) k_v_prolong(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_prolong(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_prolong(FC, ST, tiles[ti], cached_);
 }
 
 // Gauge of level-0 closed groups: one block per (case, group); members strided.
@@ -986,7 +998,7 @@ __global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MS
 
 // ----------------------------------------------------------------- prologue / epilogue (FP64)
 // b = -div(u)/dt, terms (pressure.rs:440-459), rounded as written.
-__device__ __forceinline__ void b_rhs(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_rhs(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == IDLE)
   int j, k, rb;
   if (!warp_row(F, lt, warp, j, k, rb)) return;
@@ -1014,11 +1026,12 @@ __device__ __forceinline__ void b_rhs(const FineCase* FC, MState* ST, const int2
 }
 __global__ void __launch_bounds__(TILE) k_rhs(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_rhs(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_rhs(FC, ST, tiles[ti], cached_);
 }
 
 // |b_c| (after the host-side gauge of closed components); x = 0.
-__device__ __forceinline__ void b_norm(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_norm(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == IDLE)
   double acc = 0.0;
@@ -1038,7 +1051,8 @@ __device__ __forceinline__ void b_norm(const FineCase* FC, MState* ST, const int
 }
 __global__ void __launch_bounds__(TILE) k_norm(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_norm(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_norm(FC, ST, tiles[ti], cached_);
 }
 
 // Face correction u -= dt grad(x) (pressure.rs:481-496), face tiles.
@@ -1062,13 +1076,14 @@ __global__ void k_correct(const FineCase* FC, const MState* ST, const int2* ftil
   }
 }
 
-__device__ __forceinline__ void b_addp(const FineCase* FC, MState* ST, const int2 t) {
+__device__ __forceinline__ void b_addp(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == DONE)
   for (int c = cb + threadIdx.x; c < ce; c += TILE) F.pfield[c] = __dadd_rn(F.pfield[c], F.x64[c]);
 }
 __global__ void __launch_bounds__(TILE) k_addp(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_addp(FC, ST, tiles[ti]);
+  int cached_ = -1;  // case whose descriptor is in shared memory
+  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_addp(FC, ST, tiles[ti], cached_);
 }
 
 // ----------------------------------------------------------------- host side

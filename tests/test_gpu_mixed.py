@@ -132,3 +132,40 @@ def test_batch_follows_changed_face_coefficients(pkg):
     batch.close()
     d1.close()
     d2.close()
+
+
+def test_batch_with_several_tiles_per_block(pkg, O):
+    """Uneven cases whose row tiles outnumber the persistent grid (1216 blocks), so each block
+    walks tiles of several cases, some of them already converged; results equal alone."""
+    rng = np.random.default_rng(23)
+    shapes = [(128, 128, 64), (96, 96, 48), (128, 128, 64), (24, 24, 12)]
+    cases = [pkg.synth.case(sh, 2.0, inflow=5.0, preconditioner="multigrid",
+                            boxes=pkg.synth.random_boxes(rng, 4, [v * 2.0 for v in sh], side=(6.0, 20.0),
+                                                         height=(6.0, 40.0), dx=2.0)) for sh in shapes]
+    grids = [pkg.grid.Grid.build(c) for c in cases]
+    assert sum((g.n[1] * g.n[2] + 7) // 8 for g in grids) > 2 * 1216
+    us = [pkg.synth.random_velocity(g, 40 + i) for i, g in enumerate(grids)]
+    ps = [np.zeros(g.count) for g in grids]
+    dts = [0.1, 0.1, 0.05, 0.1]
+    alone = [run_mixed(pkg, g, u, p, dt, 1e-8) for g, u, p, dt in zip(grids, us, ps, dts)]
+    dgs = [pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed") for g in grids]
+    batch = pkg.pressure.Batch(dgs)
+    for rep in range(2):
+        bu = [u.copy() for u in us]
+        bp = [p.copy() for p in ps]
+        res = batch.project(bu, bp, dts, 1e-8, 10000)
+        for i, (code, info) in enumerate(res):
+            assert code == 0
+            assert info.iterations == alone[i][2].iterations
+            assert np.array_equal(bits(bu[i]), bits(alone[i][0])), (rep, i)
+            assert np.array_equal(bits(bp[i]), bits(alone[i][1])), (rep, i)
+    # The 96x96x48 case against the FP64 oracle.
+    og = O.Grid(cases[1])
+    code, ou, op, _ = og.project(us[1], ps[1], dts[1], 1e-8, 10000)
+    assert code == 0
+    ep = np.max(np.abs(alone[1][1] - op)) / np.max(np.abs(op))
+    eu = np.max(np.abs(alone[1][0] - ou)) / np.max(np.abs(ou))
+    assert ep <= MIXED_REL and eu <= MIXED_REL, (ep, eu)
+    batch.close()
+    for d in dgs:
+        d.close()
