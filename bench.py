@@ -38,6 +38,15 @@ WORKLOAD = ("128x128x64 grid, dx=2 m, 12 seeded box buildings, open x (inflow 5 
             "masked multigrid V(2,2)-PCG to 1e-8")
 
 
+def max_over_ranks(value, dist, device):
+    """The largest of every rank's `value` (the job's time is its slowest replica's)."""
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -114,6 +123,7 @@ class CpuPool:
     grid, so each thread keeps its own), solving concurrently; ctypes releases the GIL."""
 
     def __init__(self, case, threads):
+        """`case`: one case for every thread, or a list with one case per thread."""
         from oracle import oracle as O
         import numpy as np
 
@@ -121,12 +131,13 @@ class CpuPool:
 
         pkg = entry.package()
         self.np = np
-        self.case = case
+        self.cases = list(case) if isinstance(case, (list, tuple)) else [case] * threads
+        assert len(self.cases) == threads
         self.threads = threads
-        self.g = pkg.grid.Grid.build(case)
+        self.gs = [pkg.grid.Grid.build(c) for c in self.cases]
         self.pkg = pkg
         self.grids = [None] * threads
-        self._each(lambda t: self.grids.__setitem__(t, O.Grid(case)))
+        self._each(lambda t: self.grids.__setitem__(t, O.Grid(self.cases[t])))
 
     def _each(self, fn):
         ths = [threading.Thread(target=fn, args=(t,)) for t in range(self.threads)]
@@ -139,10 +150,10 @@ class CpuPool:
         """One projection per thread on velocity seed seeds[t]; returns per-solve seconds."""
         times = [None] * self.threads
         codes = [None] * self.threads
-        us = [self.pkg.synth.random_velocity(self.g, s) for s in seeds]
+        us = [self.pkg.synth.random_velocity(self.gs[t], s) for t, s in enumerate(seeds)]
 
         def work(t):
-            p = self.np.zeros(self.g.count)
+            p = self.np.zeros(self.gs[t].count)
             t0 = time.perf_counter()
             codes[t], _, _, _ = self.grids[t].project(us[t], p, DT, TOL, MAX_IT)
             times[t] = time.perf_counter() - t0
@@ -163,6 +174,28 @@ def cpu_baseline(case):
                       f"untimed cold solve each); median {med:.2f} s per solve"}
 
 
+def mix_sample(pkg, threads):
+    """One case of the serving mix per host thread, spread over the mix in order (the 36 large
+    wind-direction cases come first, then the 16 smaller ones)."""
+    mix = pkg.synth.config5()
+    return [mix[(t * len(mix)) // threads] for t in range(threads)]
+
+
+def cpu_baseline_mix(pkg):
+    threads = os.cpu_count() or 1
+    cases = mix_sample(pkg, threads)
+    pool = CpuPool(cases, threads)
+    pool.solve([500 + t for t in range(threads)])  # cold: hierarchy build, untimed
+    t0 = time.perf_counter()
+    times = pool.solve([1000 + t for t in range(threads)])
+    wall = time.perf_counter() - t0
+    small = sum(1 for c in cases if c["grid"]["cells"][0] == 96)
+    return {"value": round(threads / wall, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{threads} concurrent warm solves, one per host thread, over cases of the mix "
+                      f"({threads - small} at 128x128x64, {small} at 96x96x48), after one untimed cold solve "
+                      f"each; {wall:.2f} s wall, median {statistics.median(times):.2f} s per solve"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -173,8 +206,9 @@ def run_reference(args):
     from oracle import oracle as O
 
     O.build()
-    case = workload_case(pkg)
     threads = os.cpu_count() or 1
+    serving = args.form == "serving"
+    case = mix_sample(pkg, threads) if serving else workload_case(pkg)
     pool = CpuPool(case, threads)
     pool.solve(list(range(threads)))  # warm-up: the cold solve that builds each thread's hierarchy
     t0 = time.perf_counter()
@@ -186,8 +220,10 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "form": "CPU restatement of the reference (oracle), warm solves",
-                       "threads": threads},
+            "config": {"workload": SERVE_WORKLOAD if serving else WORKLOAD,
+                       "form": "CPU restatement of the reference (oracle), warm solves", "threads": threads,
+                       "sample": ("one case of the mix per host thread, spread over the mix in order"
+                                  if serving else "the workload's grid on every host thread")},
             "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"each step: {threads} concurrent warm solves (one per host thread), "
                                        f"median {statistics.median(per):.2f} s per solve; one cold warm-up step"},
@@ -293,11 +329,285 @@ def timed_steps(form, torch, stream, flush, W, K, dist=None):
     torch.cuda.synchronize()
     total = ev0.elapsed_time(ev1)
     if dist:
-        t = torch.tensor([total], device=flush.device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total = float(t.item())
+        total = max_over_ranks(total, dist, flush.device)
     lat = sorted(a.elapsed_time(b) for a, b in marks)
     return total, lat, infos
+
+
+SERVE_WORKLOAD = ("serving mix: 36 wind-direction cases (0..350 deg, 10 deg steps) on a 128x128x64 grid, dx=2 m, "
+                  "30 seeded buildings, open x/y, ground_open_top z, neutral_rans 5 m/s; plus 16 cases at 96x96x48 "
+                  "with 0-20 buildings; each case's u* sequence as above, state resident across steps; "
+                  "mixed FP32/FP64 multigrid PCG to 1e-8 through the continuous-batching server")
+
+
+class Serving:
+    """The serving mix through cfdg_server: every case's fields, hierarchy and FP32 state stay
+    resident; a case's next step is its projected field plus the seeded perturbation."""
+
+    def __init__(self, pkg, torch, dev, stream, slots, rank):
+        import numpy as np
+
+        self.pkg, self.torch, self.dev, self.stream = pkg, torch, dev, stream
+        self.cases = pkg.synth.config5()
+        self.grids = [pkg.grid.Grid.build(c) for c in self.cases]
+        self.n = len(self.grids)
+        self.dgs = [pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed") for g in self.grids]
+        for d in self.dgs:
+            d.set_stream(stream.cuda_stream)
+        self.server = pkg.pressure.Server(self.dgs, slots or self.n)
+        self.server.set_stream(stream.cuda_stream)
+        self.u0 = [pkg.synth.random_velocity(g, seed=5000 + 100 * rank + i) for i, g in enumerate(self.grids)]
+        self.d_u = [torch.from_numpy(u).to(dev) for u in self.u0]
+        self.d_p = [torch.zeros(g.count, dtype=torch.float64, device=dev) for g in self.grids]
+        self.free = []
+        for g in self.grids:
+            m = ((g.face_kind == pkg.grid.INTERIOR) | (g.face_kind == pkg.grid.OUTLET)).astype(np.float64)
+            self.free.append(torch.from_numpy(m).to(dev))
+        self.gen = [torch.Generator(device=dev) for _ in self.grids]
+        for i, gn in enumerate(self.gen):
+            gn.manual_seed(7000 + 100 * rank + i)
+        self.cells = [g.count for g in self.grids]
+
+    def perturb(self, c):
+        """u*_{s+1} = project(u*_s) + 0.05 U[-1,1] on the free faces (on the device)."""
+        torch = self.torch
+        noise = torch.rand(self.d_u[c].numel(), dtype=torch.float64, device=self.dev, generator=self.gen[c])
+        self.d_u[c].add_(noise.mul_(0.1).sub_(0.05).mul_(self.free[c]))
+
+    def submit(self, c):
+        return self.server.submit(c, self.d_u[c].data_ptr(), self.d_p[c].data_ptr(), DT, TOL, MAX_IT)
+
+    def closed_loop(self, steps):
+        """Every case runs `steps` consecutive time steps; a case's next step is submitted as soon
+        as its previous one is finished. Returns (per-request latency s, infos, cell updates)."""
+        srv = self.server
+        left = [steps] * self.n
+        inflight = {}
+        lat, infos = [], []
+        for c in range(self.n):
+            self.perturb(c)
+            inflight[self.submit(c)] = (c, time.perf_counter())
+            left[c] -= 1
+        while inflight:
+            if srv.progress() == 0:
+                continue
+            for t in list(inflight):
+                r = srv.result(t)
+                if r is None:
+                    continue
+                code, info = r
+                assert code == 0, code
+                c, t0 = inflight.pop(t)
+                lat.append(time.perf_counter() - t0)
+                infos.append((c, info))
+                if left[c] > 0:
+                    self.perturb(c)
+                    inflight[self.submit(c)] = (c, time.perf_counter())
+                    left[c] -= 1
+        return lat, infos
+
+    def poisson(self, requests, rate, seed):
+        """Open loop: `requests` arrivals with exponential gaps (mean 1/rate), each for a case drawn
+        uniformly; a case's arrivals are served in order, one at a time. Latency = completion -
+        arrival, as the client sees it."""
+        import numpy as np
+
+        rng = np.random.default_rng(seed)
+        arrive = np.cumsum(rng.exponential(1.0 / rate, size=requests))
+        which = rng.integers(0, self.n, size=requests)
+        srv = self.server
+        backlog = [[] for _ in range(self.n)]
+        inflight, busy = {}, [False] * self.n
+        lat = []
+        nxt = 0
+        t_start = time.perf_counter()
+        done = 0
+        while done < requests:
+            now = time.perf_counter() - t_start
+            while nxt < requests and arrive[nxt] <= now:
+                backlog[which[nxt]].append(arrive[nxt])
+                nxt += 1
+            for c in range(self.n):
+                if backlog[c] and not busy[c]:
+                    self.perturb(c)
+                    inflight[self.submit(c)] = (c, backlog[c].pop(0))
+                    busy[c] = True
+            if not inflight:
+                if nxt < requests:
+                    time.sleep(max(0.0, min(arrive[nxt] - (time.perf_counter() - t_start), 0.002)))
+                continue
+            if srv.progress() == 0:
+                continue
+            for t in list(inflight):
+                r = srv.result(t)
+                if r is None:
+                    continue
+                assert r[0] == 0, r[0]
+                c, a = inflight.pop(t)
+                lat.append(time.perf_counter() - t_start - a)
+                busy[c] = False
+                done += 1
+        span = time.perf_counter() - t_start
+        return lat, span, float(arrive[-1])
+
+    def close(self):
+        self.server.close()
+        for d in self.dgs:
+            d.close()
+
+
+def coarse_summary(stats):
+    """Per coarse level over all cases: rows, max smoother colours, ELL entries per
+    nonzero, closed groups."""
+    out = []
+    depth = max(len(c["levels"]) for c in stats["cases"])
+    for l in range(depth):
+        lv = [c["levels"][l] for c in stats["cases"] if len(c["levels"]) > l]
+        nnz = sum(v["nnz"] for v in lv)
+        out.append({"rows": sum(v["rows"] for v in lv), "max_colors": max(v["colors"] for v in lv),
+                    "jacobi_cases": sum(1 for v in lv if v.get("smoother") == "l1-jacobi"),
+                    "ell_per_nnz": round(sum(v["ell_entries"] for v in lv) / max(nnz, 1), 2),
+                    "groups": sum(v["groups"] for v in lv), "blocks": sum(v["blocks"] for v in lv)})
+    return out
+
+
+def pct(xs, q):
+    xs = sorted(xs)
+    return xs[min(len(xs) - 1, int(q * len(xs)))]
+
+
+def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
+    import numpy as np
+
+    K, W = args.steps, args.warmup
+    sv = Serving(pkg, torch, dev, stream, args.slots, rank)
+    n = sv.n
+    t_setup = time.perf_counter()
+    sv.closed_loop(W)  # first solves build every hierarchy and FP32 state
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t_setup
+    if dist:
+        dist.barrier()
+    launches0 = L.cfdg_launch_count()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    lat, infos = sv.closed_loop(K)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = L.cfdg_launch_count() - launches0
+    total_ms = ev0.elapsed_time(ev1)
+    if dist:
+        total_ms = max_over_ranks(total_ms, dist, dev)
+    solves = world * K * n
+    value = solves / (total_ms / 1e3)
+    cell_updates = sum(sv.cells[c] * i.iterations for c, i in infos)
+    # Open loop at the stated arrival rate.
+    plat, span, last_arrival = sv.poisson(args.requests, args.rate, seed=5)
+    serving = {"arrivals": "Poisson, seed 5", "offered_per_s": args.rate, "requests": args.requests,
+               "throughput": round(args.requests / span, 2), "arrival_span_s": round(last_arrival, 3),
+               "p50_ms": round(1e3 * pct(plat, 0.50), 2), "p99_ms": round(1e3 * pct(plat, 0.99), 2),
+               "max_ms": round(1e3 * max(plat), 2), "slots": args.slots or n}
+    # End to end through the host-buffer batch call: every case of the mix per step, H2D + D2H inside.
+    bt = pkg.pressure.Batch(sv.dgs)
+    bt.set_stream(stream.cuda_stream)
+    coarse = coarse_summary(bt.stats())
+    host_u = [torch.from_numpy(u).pin_memory() for u in sv.u0]
+    work_u = [torch.empty_like(h).pin_memory() for h in host_u]
+    work_p = [torch.zeros(g.count, dtype=torch.float64).pin_memory() for g in sv.grids]
+    e2e_steps = max(1, min(K, 3))
+    e2e_ms = 0.0
+    for s in range(e2e_steps + 1):
+        for w, h, p in zip(work_u, host_u, work_p):
+            w.copy_(h)
+            p.zero_()
+        torch.cuda.synchronize()
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for code, _ in bt.project([w.numpy() for w in work_u], [p.numpy() for p in work_p], [DT] * n, TOL, MAX_IT):
+            assert code == 0
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if s > 0:  # the first call builds the batch's state
+            e2e_ms += e0.elapsed_time(e1)
+    io = sum(8 * (g.n_faces + g.count) for g in sv.grids)
+    e2e = {"value": round(world * e2e_steps * n / (e2e_ms / 1e3), 4), "unit": UNIT, "h2d_bytes_per_step": io,
+           "d2h_bytes_per_step": io,
+           "call": "cfdg_batch_project (host buffers) over all cases of the mix per step"}
+    kernels = {}
+    for name, which, reps in (("rb_half_sweep_fp32", 0, 20), ("operator_fp32", 1, 20),
+                              ("coarse_levels_cluster", 2, 10), ("vcycle_fp32", 3, 5)):
+        ms, b = bt.time_kernel(which, reps)
+        kernels[name] = {"ms": round(ms, 4), "GB/s": round(b / ms / 1e6, 1) if b else None, "algorithmic_bytes": b}
+    bt.close()
+    peak, peak_kind = peaks()
+    k = kernels["rb_half_sweep_fp32"]
+    achieved = k["algorithmic_bytes"] / (k["ms"] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "fine-level red-black Gauss-Seidel half sweep, FP32, all cases of the mix",
+                "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "peak_source": peak_kind, "traffic": None, "algorithmic_bytes": k["algorithmic_bytes"],
+                "ms_per_launch": k["ms"]}
+    # Plain FP64 on the same mix: one large and one small case, weighted 36:16.
+    plain = None
+    if not args.skip_plain:
+        per = {}
+        for c in (0, 36):
+            d = pkg.pressure.DeviceGrid(sv.grids[c], preconditioner="multigrid", precision="plain")
+            d.set_stream(stream.cuda_stream)
+            u = torch.from_numpy(sv.u0[c]).to(dev)
+            p = torch.zeros(sv.grids[c].count, dtype=torch.float64, device=dev)
+            d.project_device(u.data_ptr(), p.data_ptr(), DT, TOL, MAX_IT)  # cold: setup
+            torch.cuda.synchronize()
+            u.copy_(torch.from_numpy(sv.u0[c]))
+            p.zero_()
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            info = d.project_device(u.data_ptr(), p.data_ptr(), DT, TOL, MAX_IT)
+            b.record(stream)
+            torch.cuda.synchronize()
+            per[c] = (a.elapsed_time(b), info.iterations)
+            d.close()
+        mix_ms = (36 * per[0][0] + 16 * per[36][0]) / 52
+        plain = {"value": round(world * 1e3 / mix_ms, 4), "unit": UNIT, "ms_per_solve_128x128x64": round(per[0][0], 2),
+                 "ms_per_solve_96x96x48": round(per[36][0], 2), "iterations": [per[0][1], per[36][1]],
+                 "sample": "one warm solve of wind direction 0 and of the first 96x96x48 case, weighted 36:16"}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_mix(pkg)
+    if rank == 0:
+        its = [i.iterations for _, i in infos]
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": round(total_ms / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": SERVE_WORKLOAD, "form": "serving (continuous batching, cfdg_server)",
+                       "cases": n, "step": f"one time step of every case ({n} solves)",
+                       "cells_per_step": sum(sv.cells), "l2": "inputs larger than L2: the mix holds "
+                       f"{sum(sv.cells) * 8 * 10 / 1e9:.1f} GB of FP64 fields alone",
+                       "parallelism": f"replicas x{world}"},
+            "latency_ms": {"p50": serving["p50_ms"], "p99": serving["p99_ms"],
+                           "unit": "per request, open loop at the offered rate",
+                           "closed_loop_p50": round(1e3 * pct(lat, 0.5), 2),
+                           "closed_loop_p99": round(1e3 * pct(lat, 0.99), 2)},
+            "serving": serving, "setup_s": round(setup_s, 2), "coarse_levels": coarse,
+            "iterations_mean": round(statistics.mean(its), 2),
+            "cell_updates_per_s": round(world * cell_updates / (total_ms / 1e3), 1),
+            "e2e": e2e, "roofline": roofline, "kernels": kernels, "plain_fp64": plain, "cpu_baseline": cpu,
+            "gpu_launches": int(launches), "clocks": clk,
+        }
+        if plain:
+            line["serving_vs_plain"] = round(value / plain["value"], 2)
+        print(json.dumps(line), flush=True)
+    sv.close()
+    return 0
 
 
 def run_engine(args):
@@ -324,6 +634,11 @@ def run_engine(args):
     flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MiB > L2 (129 MB)
     K, W = args.steps, args.warmup
     L = pkg.engine.load()
+    if args.form == "serving":
+        rc = run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L)
+        if dist:
+            dist.destroy_process_group()
+        return rc
     ncases = args.cases if args.form == "batched" else 1
     form = Form(pkg, torch, dev, stream, args.form, ncases, K + W, rank)
     g = form.g
@@ -337,9 +652,7 @@ def run_engine(args):
     value = solves / (total_ms / 1e3)
     e2e_ms, io_bytes = form.e2e(stream, flush, K, W)
     if dist:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+        e2e_ms = max_over_ranks(e2e_ms, dist, dev)
     e2e = {"value": round(solves / (e2e_ms / 1e3), 4), "unit": UNIT, "h2d_bytes_per_step": io_bytes // 2,
            "d2h_bytes_per_step": io_bytes // 2}
     peak, peak_kind = peaks()
@@ -423,7 +736,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--form", default="batched", choices=["plain", "mixed", "batched"])
+    ap.add_argument("--form", default="batched", choices=["plain", "mixed", "batched", "serving"])
+    ap.add_argument("--slots", type=int, default=0, help="serving: cases on the GPU at once (0: all)")
+    ap.add_argument("--requests", type=int, default=520, help="serving: open-loop requests")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")
     ap.add_argument("--cases", type=int, default=8, help="cases per step of the batched form")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

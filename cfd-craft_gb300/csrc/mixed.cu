@@ -75,12 +75,14 @@ struct FineCase {
   const uint8_t* fluid;
   const double* fw64;    // per-face FP64 weights (the grid's)
   const float* fw32;     // per-face FP32 weights (non-uniform grids)
-  const float* diag0;    // level-0 diagonal (full layout), 0 for solid cells
+  // Level-0 FP32 arrays use the colour-split row layout (slot lay(r, colour, nxh, i>>1)).
+  const float* diag0;    // level-0 diagonal, 0 for solid cells
   const float* idiag0;   // its reciprocal, 0 where the diagonal is 0
-  int npairs, pad_pairs; // red-black work items: x-pairs of cells
-  // FP64 outer vectors (the grid's buffers)
+  const uint16_t* flags0;  // face flags
+  int nxh, N2;           // slots per colour and row (ceil(nx/2)); slots in all (2 * rows * nxh)
+  // FP64 outer vectors (the grid's buffers, natural cell order)
   double *x64, *r64, *bc, *b, *terms;
-  // FP32 inner vectors
+  // FP32 inner vectors (split layout; padding slots stay zero)
   float *e, *r32, *p, *q, *x0, *rhs0, *res0;
   double* partials;  // ntiles doubles
   // level-0 closed groups (full indices) for the gauge
@@ -105,6 +107,11 @@ static_assert(sizeof(FineCase) % 8 == 0, "FineCase is copied to shared memory in
 
 struct CLev {
   int n, terminal, ncolors, ngroups;
+  // Smoother: 0 multicolour Gauss-Seidel, 1 l1-Jacobi (levels whose graph needs many
+  // colours: the wide Galerkin stencils of linear-interpolation hierarchies).
+  int jacobi, pad_;
+  const float* il1;  // l1-Jacobi: 1 / (diag + sum |a_ij|), 0 where diag is 0
+  float* x2;         // l1-Jacobi: the second iterate of a sweep pair
   const int *off, *col;
   const float *val, *diag;
   const int *coff, *crows;
@@ -184,34 +191,6 @@ __device__ __forceinline__ long long fidx(const FineCase& F, int a, int i, int j
   return F.face_off[a] + ((long long)k * F.fdim[a][1] + j) * F.fdim[a][0] + i;
 }
 
-// FP32 operator y = A x at cell c: sum over interior faces of w (x_c - x_n), plus w x_c on outlets.
-__device__ __forceinline__ float op32(const FineCase& F, const float* __restrict__ x, int c, unsigned fl) {
-  if (!(fl & 0x0fffu)) return 0.0f;
-  int q[3];
-  coords(F, c, q[0], q[1], q[2]);
-  const int stride[3] = {1, F.n[0], F.n[0] * F.n[1]};
-  const float xc = x[c];
-  float y = 0.0f;
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int side = 0; side < 2; ++side) {
-      const unsigned ib = 1u << (2 * a + side), ob = 1u << (6 + 2 * a + side);
-      if (!(fl & (ib | ob))) continue;
-      float w;
-      if (F.uniform) {
-        w = (fl & ib) ? F.w32[a] : F.wo32[a];
-      } else {
-        int p[3] = {q[0], q[1], q[2]};
-        p[a] += side;
-        w = F.fw32[fidx(F, a, p[0], p[1], p[2])];
-      }
-      if (fl & ib) y = fmaf(w, xc - x[side ? c + stride[a] : c - stride[a]], y);
-      else y = fmaf(w, xc, y);
-    }
-  return y;
-}
-
 // FP64 operator with every product and sum rounded as written, in the reference's
 // face order (non-periodic grid): bit-identical to pressure::apply.
 __device__ __forceinline__ double op64(const FineCase& F, const double* __restrict__ x, int c, unsigned fl) {
@@ -270,8 +249,13 @@ constexpr int RT = TILE / 32;  // rows per tile: one warp per row
   const int cb = lt * RT * nx_;                                                       \
   const int ce = min(F.N, cb + RT * nx_);                                             \
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;                         \
+  const int nxh_ = F.nxh;                                                             \
+  const int sb = lt * RT * 2 * nxh_;                                                  \
+  const int se = min(F.N2, sb + RT * 2 * nxh_);                                       \
   (void)cb;                                                                           \
   (void)ce;                                                                           \
+  (void)sb;                                                                           \
+  (void)se;                                                                           \
   (void)warp;                                                                         \
   (void)lane;
 
@@ -297,13 +281,67 @@ __device__ __forceinline__ void dd_add_prod(float a, float b, float& hi, float& 
   lo += se + pe;
 }
 
-// FP32 operator at cell c = rowbase + i of row (j, k).
-__device__ __forceinline__ float op32r(const FineCase& F, const float* __restrict__ x, int c, int i, int j, int k,
-                                       unsigned fl) {
+// Level-0 FP32 layout. Row r = k*ny + j keeps its colour-0 cells ((i+j+k) even) in the
+// slots [2r*nxh, 2r*nxh + nxh) and its colour-1 cells in the next nxh slots, cell i in
+// slot i>>1 (nxh = ceil(nx/2); an odd nx leaves one zero padding slot in one half). A
+// red-black half sweep then reads and writes one contiguous half-row per row, and every
+// neighbour of a cell has the other colour: the x-neighbours sit in the same row's other
+// half at slots (i-1)>>1 and (i+1)>>1, the y- and z-neighbours at slot i>>1 of the other
+// half of rows r-1, r+1, r-ny and r+ny.
+__host__ __device__ __forceinline__ int lay(int r, int col, int nxh, int s) { return (2 * r + col) * nxh + s; }
+
+// Offsets of the six neighbours of cell i (slot s) whose other-colour half-row starts at
+// oth: x-lo, x-hi, y-lo, y-hi, z-lo, z-hi (only those with a face bit are read).
+struct Nbr {
+  int o[6];
+  __device__ __forceinline__ Nbr(int oth, int i, int s, int sy, int sz) {
+    o[0] = oth + ((i - 1) >> 1);
+    o[1] = oth + ((i + 1) >> 1);
+    o[2] = oth + s - sy;
+    o[3] = oth + s + sy;
+    o[4] = oth + s - sz;
+    o[5] = oth + s + sz;
+  }
+};
+
+// The neighbours of the two cells in slots s2 and s2+1 (s2 even, nxh even) of one
+// colour half-row, loaded as float2 before any is used: the other half of the same row
+// (plus the edge slot s2-1 or s2+2) and of rows r-1, r+1, r-ny, r+ny. Rows outside the
+// grid are replaced by the same row (their faces are absent, so the values are unused).
+struct Pair {
+  float2 xo, yl, yh, zl, zh;
+  float xe;
+  __device__ __forceinline__ void load(const float* __restrict__ x, int oth, int s2, int par, int nxh, int sy,
+                                       int sz, bool hy0, bool hy1, bool hz0, bool hz1) {
+    xo = *reinterpret_cast<const float2*>(x + oth + s2);
+    yl = *reinterpret_cast<const float2*>(x + (hy0 ? oth - sy : oth) + s2);
+    yh = *reinterpret_cast<const float2*>(x + (hy1 ? oth + sy : oth) + s2);
+    zl = *reinterpret_cast<const float2*>(x + (hz0 ? oth - sz : oth) + s2);
+    zh = *reinterpret_cast<const float2*>(x + (hz1 ? oth + sz : oth) + s2);
+    const int e = par ? s2 + 2 : s2 - 1;
+    xe = (e >= 0 && e < nxh) ? x[oth + e] : 0.0f;
+  }
+  // Neighbour values of cell h (0: slot s2, 1: slot s2+1) in face order.
+  __device__ __forceinline__ void of(int h, int par, float nb[6]) const {
+    if (h == 0) {
+      nb[0] = par ? xo.x : xe;
+      nb[1] = par ? xo.y : xo.x;
+      nb[2] = yl.x, nb[3] = yh.x, nb[4] = zl.x, nb[5] = zh.x;
+    } else {
+      nb[0] = par ? xo.y : xo.x;
+      nb[1] = par ? xe : xo.y;
+      nb[2] = yl.y, nb[3] = yh.y, nb[4] = zl.y, nb[5] = zh.y;
+    }
+  }
+};
+
+// FP32 operator at cell (i, j, k) in the split layout: sum over interior faces of
+// w (x_c - x_n), plus w x_c on outlet faces, faces in x-lo, x-hi, y-lo, ... order.
+__device__ __forceinline__ float op32s(const FineCase& F, const float* __restrict__ x, int own, const Nbr& nb, int i,
+                                       int j, int k, unsigned fl) {
   if (!(fl & 0x0fffu)) return 0.0f;
-  const int stride[3] = {1, F.n[0], F.n[0] * F.n[1]};
   const int q[3] = {i, j, k};
-  const float xc = x[c];
+  const float xc = x[own];
   float y = 0.0f;
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -319,10 +357,33 @@ __device__ __forceinline__ float op32r(const FineCase& F, const float* __restric
         p[a] += side;
         w = F.fw32[fidx(F, a, p[0], p[1], p[2])];
       }
-      if (fl & ib) y = fmaf(w, xc - x[side ? c + stride[a] : c - stride[a]], y);
+      if (fl & ib) y = fmaf(w, xc - x[nb.o[2 * a + side]], y);
       else y = fmaf(w, xc, y);
     }
   return y;
+}
+
+// Sum over interior faces of w x_n in face order, starting from v (Gauss-Seidel update
+// and residual of the level-0 matrix, whose off-diagonal entries are -w).
+__device__ __forceinline__ float nbsum32(const FineCase& F, const float* __restrict__ x, const Nbr& nb, int i, int j,
+                                         int k, unsigned fl, float v, float sign) {
+  if (F.uniform) {
+#pragma unroll
+    for (int f = 0; f < 6; ++f)
+      if (fl & (1u << f)) v = fmaf(sign * F.w32[f >> 1], x[nb.o[f]], v);
+  } else {
+    const int q[3] = {i, j, k};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {
+        if (!(fl & (1u << (2 * a + side)))) continue;
+        int pp[3] = {q[0], q[1], q[2]};
+        pp[a] += side;
+        v = fmaf(sign * F.fw32[fidx(F, a, pp[0], pp[1], pp[2])], x[nb.o[2 * a + side]], v);
+      }
+  }
+  return v;
 }
 
 // A: q = A32 p, alpha = rz / (p.q) (E032 when not positive).
@@ -331,12 +392,48 @@ __device__ __forceinline__ void b_op(const FineCase* FC, MState* ST, const int2 
   FINE_PROLOGUE(S.state == RUN)
   float hi = 0.0f, lo = 0.0f;
   int j, k, rb;
-  if (warp_row(F, lt, warp, j, k, rb)) {
-    for (int i = lane; i < nx_; i += 32) {
-      const int c = rb + i;
-      const float v = op32r(F, F.p, c, i, j, k, F.flags[c]);
-      F.q[c] = v;
-      dd_add_prod(F.p[c], v, hi, lo);
+  if (warp_row(F, lt, warp, j, k, rb) && F.uniform && !(nxh_ & 1)) {
+    const int r = lt * RT + warp, sy = 2 * nxh_, sz = sy * F.n[1];
+    const bool hy0 = j > 0, hy1 = j + 1 < F.n[1], hz0 = k > 0, hz1 = k + 1 < F.n[2];
+    for (int col = 0; col < 2; ++col) {
+      const int par = (j + k + col) & 1;
+      const int own = lay(r, col, nxh_, 0), oth = lay(r, col ^ 1, nxh_, 0);
+      for (int s2 = 2 * lane; s2 < nxh_; s2 += 64) {
+        const float2 pc = *reinterpret_cast<const float2*>(F.p + own + s2);
+        const unsigned fl2 = *reinterpret_cast<const unsigned*>(F.flags0 + own + s2);
+        Pair P;
+        P.load(F.p, oth, s2, par, nxh_, sy, sz, hy0, hy1, hz0, hz1);
+        float nb[6];
+        float2 y = make_float2(0.0f, 0.0f);
+        P.of(0, par, nb);
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+          if (fl2 & (1u << f)) y.x = fmaf(F.w32[f >> 1], pc.x - nb[f], y.x);
+          else if (fl2 & (1u << (6 + f))) y.x = fmaf(F.wo32[f >> 1], pc.x, y.x);
+        }
+        P.of(1, par, nb);
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+          if (fl2 & (1u << (16 + f))) y.y = fmaf(F.w32[f >> 1], pc.y - nb[f], y.y);
+          else if (fl2 & (1u << (22 + f))) y.y = fmaf(F.wo32[f >> 1], pc.y, y.y);
+        }
+        *reinterpret_cast<float2*>(F.q + own + s2) = y;
+        dd_add_prod(pc.x, y.x, hi, lo);
+        dd_add_prod(pc.y, y.y, hi, lo);
+      }
+    }
+  } else if (warp_row(F, lt, warp, j, k, rb)) {
+    const int r = lt * RT + warp, sy = 2 * nxh_, sz = sy * F.n[1];
+    for (int col = 0; col < 2; ++col) {
+      const int par = (j + k + col) & 1;
+      const int own = lay(r, col, nxh_, 0), oth = lay(r, col ^ 1, nxh_, 0);
+      for (int s = lane; s < nxh_; s += 32) {
+        const int i = 2 * s + par;
+        if (i >= nx_) break;
+        const float v = op32s(F, F.p, own + s, Nbr(oth, i, s, sy, sz), i, j, k, F.flags0[own + s]);
+        F.q[own + s] = v;
+        dd_add_prod(F.p[own + s], v, hi, lo);
+      }
     }
   }
   double pq;
@@ -361,7 +458,7 @@ __device__ __forceinline__ void b_update(const FineCase* FC, MState* ST, const i
   FINE_PROLOGUE(S.state == RUN)
   const float alpha = (float)S.alpha;
   float hi = 0.0f, lo = 0.0f;
-  for (int c = cb + threadIdx.x; c < ce; c += TILE) {
+  for (int c = sb + threadIdx.x; c < se; c += TILE) {
     F.e[c] = fmaf(alpha, F.p[c], F.e[c]);
     const float r = fmaf(-alpha, F.q[c], F.r32[c]);
     F.r32[c] = r;
@@ -386,7 +483,11 @@ __device__ __forceinline__ void b_outer(const FineCase* FC, MState* ST, const in
   FINE_PROLOGUE(S.state == OUTER)
   if (!S.has_e) return;
   const double scale = S.scale;
-  for (int c = cb + threadIdx.x; c < ce; c += TILE) F.x64[c] = F.x64[c] + scale * (double)F.e[c];
+  int j, k, rb;
+  if (!warp_row(F, lt, warp, j, k, rb)) return;
+  const int r = lt * RT + warp, rp = (j + k) & 1;
+  for (int i = lane; i < nx_; i += 32)
+    F.x64[rb + i] = F.x64[rb + i] + scale * (double)F.e[lay(r, (i + rp) & 1, nxh_, i >> 1)];
 }
 __global__ void __launch_bounds__(TILE) k_outer(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
@@ -430,10 +531,11 @@ __global__ void __launch_bounds__(TILE) k_outer_resid(const FineCase* FC, MState
 __device__ __forceinline__ void b_scale(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == SCALE)
   const double inv = 1.0 / S.scale;
-  for (int c = cb + threadIdx.x; c < ce; c += TILE) {
-    F.r32[c] = (float)(F.r64[c] * inv);
-    F.e[c] = 0.0f;
-  }
+  for (int c = sb + threadIdx.x; c < se; c += TILE) F.e[c] = 0.0f;
+  int j, k, rb;
+  if (!warp_row(F, lt, warp, j, k, rb)) return;
+  const int r = lt * RT + warp, rp = (j + k) & 1;
+  for (int i = lane; i < nx_; i += 32) F.r32[lay(r, (i + rp) & 1, nxh_, i >> 1)] = (float)(F.r64[rb + i] * inv);
 }
 __global__ void __launch_bounds__(TILE) k_scale(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
@@ -454,7 +556,7 @@ __device__ __forceinline__ void b_rz(const FineCase* FC, MState* ST, const int2 
   __shared__ double sh[32];
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   float hi = 0.0f, lo = 0.0f;
-  for (int c = cb + threadIdx.x; c < ce; c += TILE) dd_add_prod(F.r32[c], F.x0[c], hi, lo);
+  for (int c = sb + threadIdx.x; c < se; c += TILE) dd_add_prod(F.r32[c], F.x0[c], hi, lo);
   double rz;
   if (case_reduce((double)hi + (double)lo, F, S, lt, sh, &rz) && threadIdx.x == 0) {
     if (S.state == START) {
@@ -477,9 +579,9 @@ __device__ __forceinline__ void b_p(const FineCase* FC, MState* ST, const int2 t
   FINE_PROLOGUE(S.state == RUN)
   const float beta = (float)S.beta;
   if (S.beta == 0.0) {
-    for (int c = cb + threadIdx.x; c < ce; c += TILE) F.p[c] = F.x0[c];
+    for (int c = sb + threadIdx.x; c < se; c += TILE) F.p[c] = F.x0[c];
   } else {
-    for (int c = cb + threadIdx.x; c < ce; c += TILE) F.p[c] = fmaf(beta, F.p[c], F.x0[c]);
+    for (int c = sb + threadIdx.x; c < se; c += TILE) F.p[c] = fmaf(beta, F.p[c], F.x0[c]);
   }
 }
 __global__ void __launch_bounds__(TILE) k_p(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
@@ -493,7 +595,7 @@ __global__ void __launch_bounds__(TILE) k_p(const FineCase* FC, MState* ST, cons
 __device__ __forceinline__ void b_v_rhs(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   if (F.rhs0 == F.r32) return;
-  for (int c = cb + threadIdx.x; c < ce; c += TILE) F.rhs0[c] = F.r32[c];
+  for (int c = sb + threadIdx.x; c < se; c += TILE) F.rhs0[c] = F.r32[c];
 }
 __global__ void __launch_bounds__(TILE) k_v_rhs(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   const int n = *count;
@@ -501,52 +603,56 @@ __global__ void __launch_bounds__(TILE) k_v_rhs(const FineCase* FC, MState* ST, 
   for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_rhs(FC, ST, tiles[ti], cached_);
 }
 
-// Red-black Gauss-Seidel half sweep on level 0: cells with (i+j+k)%2 == color. Lanes
-// walk the x-pairs (2m, 2m+1) of the warp's row, of which exactly one has the colour.
+// Red-black Gauss-Seidel half sweep on level 0: cells with (i+j+k)%2 == color, the
+// contiguous colour half of the warp's row in the split layout.
 // first: x is taken as zero (the cycle's initial guess). Cells outside the operator
 // (solid, sealed singletons) are kept at zero.
 __device__ __forceinline__ void b_rb(const FineCase* FC, MState* ST, const int2 t, int& cached_, int color, int first) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   int j, k, rb;
   if (!warp_row(F, lt, warp, j, k, rb)) return;
-  const int px = (nx_ + 1) >> 1;
+  const int r = lt * RT + warp, sy = 2 * nxh_, sz = sy * F.n[1];
   const int par = (j + k + color) & 1;
+  const int own = lay(r, color, nxh_, 0), oth = lay(r, color ^ 1, nxh_, 0);
   float* __restrict__ x = F.x0;
-  const int sy = nx_, sz = nx_ * F.n[1];
-  for (int m = lane; m < px; m += 32) {
-    const int i = 2 * m + par;
+  if (F.uniform && !(nxh_ & 1)) {
+    const bool hy0 = j > 0, hy1 = j + 1 < F.n[1], hz0 = k > 0, hz1 = k + 1 < F.n[2];
+    const bool skip = first && color == 0;
+    for (int s2 = 2 * lane; s2 < nxh_; s2 += 64) {
+      const float2 id = *reinterpret_cast<const float2*>(F.idiag0 + own + s2);
+      float2 v = *reinterpret_cast<const float2*>(F.rhs0 + own + s2);
+      const unsigned fl2 = *reinterpret_cast<const unsigned*>(F.flags0 + own + s2);
+      if (!skip) {
+        Pair P;
+        P.load(x, oth, s2, par, nxh_, sy, sz, hy0, hy1, hz0, hz1);
+        float nb[6];
+        P.of(0, par, nb);
+#pragma unroll
+        for (int f = 0; f < 6; ++f)
+          if (fl2 & (1u << f)) v.x = fmaf(F.w32[f >> 1], nb[f], v.x);
+        P.of(1, par, nb);
+#pragma unroll
+        for (int f = 0; f < 6; ++f)
+          if (fl2 & (1u << (16 + f))) v.y = fmaf(F.w32[f >> 1], nb[f], v.y);
+      }
+      float2 out;
+      out.x = id.x == 0.0f ? 0.0f : v.x * id.x;
+      out.y = id.y == 0.0f ? 0.0f : v.y * id.y;
+      *reinterpret_cast<float2*>(x + own + s2) = out;
+    }
+    return;
+  }
+  for (int s = lane; s < nxh_; s += 32) {
+    const int i = 2 * s + par;
     if (i >= nx_) break;
-    const int cc = rb + i;
-    const float id = F.idiag0[cc];
+    const float id = F.idiag0[own + s];
     if (id == 0.0f) {
-      x[cc] = 0.0f;
+      x[own + s] = 0.0f;
       continue;
     }
-    float v = F.rhs0[cc];
-    if (!(first && color == 0)) {
-      const unsigned fl = F.flags[cc];
-      if (F.uniform) {
-        if (fl & 1u) v = fmaf(F.w32[0], x[cc - 1], v);
-        if (fl & 2u) v = fmaf(F.w32[0], x[cc + 1], v);
-        if (fl & 4u) v = fmaf(F.w32[1], x[cc - sy], v);
-        if (fl & 8u) v = fmaf(F.w32[1], x[cc + sy], v);
-        if (fl & 16u) v = fmaf(F.w32[2], x[cc - sz], v);
-        if (fl & 32u) v = fmaf(F.w32[2], x[cc + sz], v);
-      } else {
-        const int q[3] = {i, j, k};
-        const int stride[3] = {1, sy, sz};
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int side = 0; side < 2; ++side) {
-            if (!(fl & (1u << (2 * a + side)))) continue;
-            int pp[3] = {q[0], q[1], q[2]};
-            pp[a] += side;
-            v = fmaf(F.fw32[fidx(F, a, pp[0], pp[1], pp[2])], x[side ? cc + stride[a] : cc - stride[a]], v);
-          }
-      }
-    }
-    x[cc] = v * id;
+    float v = F.rhs0[own + s];
+    if (!(first && color == 0)) v = nbsum32(F, x, Nbr(oth, i, s, sy, sz), i, j, k, F.flags0[own + s], v, 1.0f);
+    x[own + s] = v * id;
   }
 }
 __global__ void __launch_bounds__(TILE) k_rb(const FineCase* FC, MState* ST, const int2* tiles, const int* count, int color, int first) {
@@ -560,38 +666,52 @@ __device__ __forceinline__ void b_v_resid(const FineCase* FC, MState* ST, const 
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   int j, k, rb;
   if (!warp_row(F, lt, warp, j, k, rb)) return;
-  const int sy = nx_, sz = nx_ * F.n[1];
+  const int r = lt * RT + warp, sy = 2 * nxh_, sz = sy * F.n[1];
   const float* __restrict__ x = F.x0;
-  for (int i = lane; i < nx_; i += 32) {
-    const int cc = rb + i;
-    const float d = F.diag0[cc];
-    if (d == 0.0f) {
-      F.res0[cc] = 0.0f;
-      continue;
-    }
-    const unsigned fl = F.flags[cc];
-    float v = d * x[cc];
-    if (F.uniform) {
-      if (fl & 1u) v = fmaf(-F.w32[0], x[cc - 1], v);
-      if (fl & 2u) v = fmaf(-F.w32[0], x[cc + 1], v);
-      if (fl & 4u) v = fmaf(-F.w32[1], x[cc - sy], v);
-      if (fl & 8u) v = fmaf(-F.w32[1], x[cc + sy], v);
-      if (fl & 16u) v = fmaf(-F.w32[2], x[cc - sz], v);
-      if (fl & 32u) v = fmaf(-F.w32[2], x[cc + sz], v);
-    } else {
-      const int q[3] = {i, j, k};
-      const int stride[3] = {1, sy, sz};
+  if (F.uniform && !(nxh_ & 1)) {
+    const bool hy0 = j > 0, hy1 = j + 1 < F.n[1], hz0 = k > 0, hz1 = k + 1 < F.n[2];
+    for (int col = 0; col < 2; ++col) {
+      const int par = (j + k + col) & 1;
+      const int own = lay(r, col, nxh_, 0), oth = lay(r, col ^ 1, nxh_, 0);
+      for (int s2 = 2 * lane; s2 < nxh_; s2 += 64) {
+        const float2 d = *reinterpret_cast<const float2*>(F.diag0 + own + s2);
+        const float2 xc = *reinterpret_cast<const float2*>(x + own + s2);
+        const float2 rh = *reinterpret_cast<const float2*>(F.rhs0 + own + s2);
+        const unsigned fl2 = *reinterpret_cast<const unsigned*>(F.flags0 + own + s2);
+        Pair P;
+        P.load(x, oth, s2, par, nxh_, sy, sz, hy0, hy1, hz0, hz1);
+        float nb[6];
+        float va = d.x * xc.x, vb = d.y * xc.y;
+        P.of(0, par, nb);
 #pragma unroll
-      for (int a = 0; a < 3; ++a)
+        for (int f = 0; f < 6; ++f)
+          if (fl2 & (1u << f)) va = fmaf(-F.w32[f >> 1], nb[f], va);
+        P.of(1, par, nb);
 #pragma unroll
-        for (int side = 0; side < 2; ++side) {
-          if (!(fl & (1u << (2 * a + side)))) continue;
-          int pp[3] = {q[0], q[1], q[2]};
-          pp[a] += side;
-          v = fmaf(-F.fw32[fidx(F, a, pp[0], pp[1], pp[2])], x[side ? cc + stride[a] : cc - stride[a]], v);
-        }
+        for (int f = 0; f < 6; ++f)
+          if (fl2 & (1u << (16 + f))) vb = fmaf(-F.w32[f >> 1], nb[f], vb);
+        float2 out;
+        out.x = d.x == 0.0f ? 0.0f : rh.x - va;
+        out.y = d.y == 0.0f ? 0.0f : rh.y - vb;
+        *reinterpret_cast<float2*>(F.res0 + own + s2) = out;
+      }
     }
-    F.res0[cc] = F.rhs0[cc] - v;
+    return;
+  }
+  for (int col = 0; col < 2; ++col) {
+    const int par = (j + k + col) & 1;
+    const int own = lay(r, col, nxh_, 0), oth = lay(r, col ^ 1, nxh_, 0);
+    for (int s = lane; s < nxh_; s += 32) {
+      const int i = 2 * s + par;
+      if (i >= nx_) break;
+      const float d = F.diag0[own + s];
+      if (d == 0.0f) {
+        F.res0[own + s] = 0.0f;
+        continue;
+      }
+      const float v = nbsum32(F, x, Nbr(oth, i, s, sy, sz), i, j, k, F.flags0[own + s], d * x[own + s], -1.0f);
+      F.res0[own + s] = F.rhs0[own + s] - v;
+    }
   }
 }
 __global__ void __launch_bounds__(TILE) k_v_resid(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
@@ -617,10 +737,10 @@ __global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState*
   }
 }
 
-// x0 += P x1.
+// x0 += P x1 (the prolongation's rows are the split layout's slots; padding rows are empty).
 __device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
-  for (int c = cb + threadIdx.x; c < ce; c += TILE) {
+  for (int c = sb + threadIdx.x; c < se; c += TILE) {
     const int b = F.p_off[c], e = F.p_off[c + 1];
     if (b == e) continue;
     float sum = 0.0f;
@@ -688,9 +808,23 @@ __device__ void c_center(const CLev& L, float* v, double* gpart, double* sh) {
   csync();
 }
 
-__device__ void c_sweep(const CLev& L, bool backward) {
+__device__ void c_sweep(const CLev& L, bool backward, int pass) {
   const int rank = (int)cg::this_cluster().block_rank();
   const int tid = rank * blockDim.x + threadIdx.x, nth = (int)cg::this_cluster().num_blocks() * blockDim.x;
+  if (L.jacobi) {  // l1-Jacobi, x -> x2 (pass 0) -> x (pass 1)
+    const float* xin = pass ? L.x2 : L.x;
+    float* xout = pass ? L.x : L.x2;
+    const int w = L.ell_w[0];
+    for (int i = tid; i < L.n; i += nth) {
+      float v = 0.0f;
+      for (int a = 0; a < w; ++a) v = fmaf(L.ell_val[a * L.n + i], __ldcg(&xin[L.ell_col[a * L.n + i]]), v);
+      const float xi = __ldcg(&xin[i]);
+      xout[i] = fmaf(L.il1[i], __ldcg(&L.rhs[i]) - fmaf(L.diag[i], xi, v), xi);
+    }
+    __threadfence();
+    csync();
+    return;
+  }
   for (int cc = 0; cc < L.ncolors; ++cc) {
     const int color = backward ? L.ncolors - 1 - cc : cc;
     const int b = L.coff[color], nrow = L.coff[color + 1] - b;
@@ -743,8 +877,8 @@ __global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState*
       c_center(L, L.x, C.gpart, sh);
       break;
     }
-    c_sweep(L, false);
-    c_sweep(L, false);
+    c_sweep(L, false, 0);
+    c_sweep(L, false, 1);
     c_center(L, L.x, C.gpart, sh);
     for (int i = tid; i < L.n; i += nth) {
       float v = L.diag[i] * __ldcg(&L.x[i]);
@@ -773,8 +907,8 @@ __global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState*
     }
     __threadfence();
     csync();
-    c_sweep(L, true);
-    c_sweep(L, true);
+    c_sweep(L, true, 0);
+    c_sweep(L, true, 1);
     c_center(L, L.x, C.gpart, sh);
   }
 }
@@ -794,7 +928,8 @@ struct CoarseTab {
   const int* fwd;    // [nlev][MAXC][nc+1] rows of colour c (non-terminal levels)
   const int* bwd;    // [nlev][MAXC][nc+1] rows of colour C_case-1-c
   const int* next;   // [nlev][nc+1] rows of level l+1 (restriction targets; non-terminal at l)
-  const int* live;   // [nlev][nc+1] rows of level l when non-terminal (residual, prolongation)
+  const int* live;   // [nlev][nc+1] rows of level l when non-terminal (prolongation)
+  const int* res;    // [nlev][nc+1] residual work items: rows, or 8 lanes per row (l1-Jacobi levels)
   const int* grp;    // [nlev][nc+1] closed groups at level l
 };
 
@@ -855,7 +990,7 @@ __device__ void g_center(const CLev* sl, const MState* ST, const CoarseTab& T, i
   grid.sync();
 }
 
-__device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, int l, bool backward,
+__device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, int l, bool backward, int pass,
                         cg::grid_group& grid) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
   for (int cc = 0; cc < T.maxc[l]; ++cc) {
@@ -865,10 +1000,32 @@ __device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, in
       const int ci = find_case(off, T.nc, t);
       if (!active(ST, ci)) continue;
       const CLev& L = sl[ci];
-      const int color = backward ? L.ncolors - 1 - cc : cc;
       const int k = t - __ldg(&off[ci]);
+      if (L.jacobi) {
+        // One sweep x_out = x_in + (rhs - A x_in) / (diag + sum |a_ij|); eight lanes per
+        // row (the ranges of such cases start at multiples of eight), x -> x2 -> x.
+        const int i = k >> 3, sub = k & 7;
+        const float* xin = pass ? L.x2 : L.x;
+        float* xout = pass ? L.x : L.x2;
+        const int w = L.ell_w[0];
+        const int* ec = L.ell_col + i;
+        const float* ev = L.ell_val + i;
+        float v = 0.0f;
+        for (int a = sub; a < w; a += 8) v = fmaf(ev[a * L.n], __ldcg(&xin[ec[a * L.n]]), v);
+        const unsigned mask = 0xffu << (threadIdx.x & 24);
+        v += __shfl_xor_sync(mask, v, 4, 8);
+        v += __shfl_xor_sync(mask, v, 2, 8);
+        v += __shfl_xor_sync(mask, v, 1, 8);
+        if (sub == 0) {
+          const float xi = __ldcg(&xin[i]);
+          xout[i] = fmaf(L.il1[i], __ldcg(&L.rhs[i]) - fmaf(L.diag[i], xi, v), xi);
+        }
+        continue;
+      }
+      const int color = backward ? L.ncolors - 1 - cc : cc;
       const int c0 = L.coff[color];
       const int nrow = L.coff[color + 1] - c0;
+      if (k >= nrow) continue;  // ranges are rounded up to multiples of eight
       const int i = L.crows[c0 + k];
       const int base = L.ell_off[color], w = L.ell_w[color];
       float v = __ldcg(&L.rhs[i]);
@@ -893,7 +1050,7 @@ __device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, in
   }
 }
 
-__global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MState* ST, const CoarseTab* Tp) {
+__global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const MState* ST, const CoarseTab* Tp) {
   const CoarseTab T = *Tp;
   __shared__ double sh[32];
   extern __shared__ __align__(16) unsigned char smem[];
@@ -942,16 +1099,29 @@ __global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MS
       }
     }
     grid.sync();
-    g_sweep(sl, ST, T, l, false, grid);
-    g_sweep(sl, ST, T, l, false, grid);
+    g_sweep(sl, ST, T, l, false, 0, grid);
+    g_sweep(sl, ST, T, l, false, 1, grid);
     if (T.anyg[l]) g_center(sl, ST, T, l, 1, sh, grid);
     {
-      const int* off = T.live + l * (nc + 1);
+      const int* off = T.res + l * (nc + 1);
       for (int t = gt; t < __ldg(&off[nc]); t += nth) {
         const int ci = find_case(off, nc, t);
         if (!active(ST, ci)) continue;
         const CLev& L = sl[ci];
-        const int i = t - __ldg(&off[ci]);
+        const int k = t - __ldg(&off[ci]);
+        if (L.jacobi) {  // eight lanes per (wide) row
+          const int i = k >> 3, sub = k & 7;
+          float v = 0.0f;
+          for (int a = L.off[i] + sub; a < L.off[i + 1]; a += 8) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
+          const unsigned mask = 0xffu << (threadIdx.x & 24);
+          v += __shfl_xor_sync(mask, v, 4, 8);
+          v += __shfl_xor_sync(mask, v, 2, 8);
+          v += __shfl_xor_sync(mask, v, 1, 8);
+          if (sub == 0) L.res[i] = __ldcg(&L.rhs[i]) - fmaf(L.diag[i], __ldcg(&L.x[i]), v);
+          continue;
+        }
+        if (k >= L.n) continue;
+        const int i = k;
         float v = L.diag[i] * __ldcg(&L.x[i]);
         for (int a = L.off[i]; a < L.off[i + 1]; ++a) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
         L.res[i] = __ldcg(&L.rhs[i]) - v;
@@ -990,8 +1160,8 @@ __global__ void __launch_bounds__(512) k_coarse_all(const CCase* cases, const MS
       }
     }
     grid.sync();
-    g_sweep(sl, ST, T, l, true, grid);
-    g_sweep(sl, ST, T, l, true, grid);
+    g_sweep(sl, ST, T, l, true, 0, grid);
+    g_sweep(sl, ST, T, l, true, 1, grid);
     if (T.anyg[l]) g_center(sl, ST, T, l, 1, sh, grid);
   }
 }
@@ -1039,8 +1209,8 @@ __device__ __forceinline__ void b_norm(const FineCase* FC, MState* ST, const int
     const double v = F.bc[c];
     acc = __fma_rn(v, v, acc);
     F.x64[c] = 0.0;
-    F.e[c] = 0.0f;
   }
+  for (int c = sb + threadIdx.x; c < se; c += TILE) F.e[c] = 0.0f;
   double bb;
   if (case_reduce(acc, F, S, lt, sh, &bb) && threadIdx.x == 0) {
     S.norm = sqrt(bb);
@@ -1110,6 +1280,25 @@ void greedy_colors(const Csr& a, int n, std::vector<int32_t>& coff, std::vector<
   for (int i = 0; i < n; ++i) rows[fill[color[i]]++] = i;
 }
 
+// Two colours from a level's bin parity when it colours the graph properly (masked
+// hierarchies); false otherwise (the caller falls back to the greedy colouring).
+bool parity_colors(const Csr& a, const std::vector<uint8_t>& parity, int n, std::vector<int32_t>& coff,
+                   std::vector<int32_t>& rows, int& ncolors) {
+  if ((int)parity.size() != n) return false;
+  for (int i = 0; i < n; ++i)
+    for (int k = a.off[i]; k < a.off[i + 1]; ++k)
+      if (a.col[k] != i && parity[a.col[k]] == parity[i]) return false;
+  coff.assign(3, 0);
+  for (int i = 0; i < n; ++i) coff[parity[i] + 1] += 1;
+  coff[2] += coff[1];
+  rows.assign(n, 0);
+  int fill[2] = {0, coff[1]};
+  for (int i = 0; i < n; ++i) rows[fill[parity[i]]++] = i;
+  ncolors = coff[1] > 0 && coff[2] > coff[1] ? 2 : 1;
+  if (ncolors == 1) coff.resize(2), coff[1] = n;
+  return true;
+}
+
 template <class T>
 std::vector<float> to_f32(const std::vector<T>& v) {
   return std::vector<float>(v.begin(), v.end());
@@ -1122,6 +1311,11 @@ struct CaseState {
   FineCase F{};
   CCase C{};
   std::vector<std::vector<int32_t>> colors;  // per coarse level: colour offsets (host copy)
+  struct LevelStats {
+    long long rows, nnz, ell, groups, blocks;
+    int colors, jacobi;
+  };
+  std::vector<LevelStats> stats;  // per coarse level (diagnostics)
   int ngroups0 = 0;
   ~CaseState() { arena.release(); }
 };
@@ -1167,23 +1361,51 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     F.fw32 = d;
   }
   const MgLevel& M0 = H.levels[0];
+  if ((int64_t)M0.diag.size() != (int64_t)h.cells)
+    return fail(CFDG_ERR_UNSUPPORTED, "mixed form: level 0 must cover every cell");
+  // The split layout of the level-0 FP32 arrays (slot of each cell, cell of each slot).
+  const int nx = h.n[0], ny = h.n[1], rows = h.n[1] * h.n[2];
+  F.nxh = (nx + 1) / 2;
+  F.N2 = 2 * rows * F.nxh;
+  std::vector<int32_t> slot(F.N), cell_of(F.N2, -1);
+  for (int r = 0; r < rows; ++r) {
+    const int rp = (r % ny + r / ny) & 1;
+    for (int i = 0; i < nx; ++i) {
+      const int c = r * nx + i, sl = lay(r, (i + rp) & 1, F.nxh, i >> 1);
+      slot[c] = sl;
+      cell_of[sl] = c;
+    }
+  }
   {
+    std::vector<uint16_t> fl(F.N), fl2(F.N2, 0);
+    CU(cudaMemcpyAsync(fl.data(), G->d_flags, sizeof(uint16_t) * F.N, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    std::vector<float> d32(F.N2, 0.0f), i32(F.N2, 0.0f);
+    for (int c = 0; c < F.N; ++c) {
+      const float d = (float)M0.diag[c];
+      d32[slot[c]] = d;
+      i32[slot[c]] = d == 0.0f ? 0.0f : 1.0f / d;
+      fl2[slot[c]] = fl[c];
+    }
     float *d, *id;
-    std::vector<float> d32 = to_f32(M0.diag), i32(d32.size());
-    for (size_t i = 0; i < d32.size(); ++i) i32[i] = d32[i] == 0.0f ? 0.0f : 1.0f / d32[i];
+    uint16_t* f2;
     if (int e = A.upload(&d, d32, s)) return e;
     if (int e = A.upload(&id, i32, s)) return e;
+    if (int e = A.upload(&f2, fl2, s)) return e;
     F.diag0 = d;
     F.idiag0 = id;
+    F.flags0 = f2;
   }
-  F.npairs = ((h.n[0] + 1) / 2) * h.n[1] * h.n[2];
   float** fv[] = {&F.e, &F.r32, &F.p, &F.q, &F.x0, &F.res0};
-  for (float** v : fv)
-    if (int e = A.alloc(v, F.N)) return e;
+  for (float** v : fv) {
+    if (int e = A.alloc(v, F.N2)) return e;
+    CU(cudaMemsetAsync(*v, 0, sizeof(float) * F.N2, s));  // padding slots stay zero
+  }
   // The cycle's right-hand side is the inner residual itself unless level 0 has
   // closed groups, whose gauge it would modify in place.
   if (M0.groups.rows() > 0) {
-    if (int e = A.alloc(&F.rhs0, F.N)) return e;
+    if (int e = A.alloc(&F.rhs0, F.N2)) return e;
+    CU(cudaMemsetAsync(F.rhs0, 0, sizeof(float) * F.N2, s));
   } else {
     F.rhs0 = F.r32;
   }
@@ -1193,20 +1415,38 @@ int build_case(cfdg_grid* G, CaseState& cs) {
   F.ngroups = cs.ngroups0;
   if (F.ngroups) {
     int *o, *m;
+    std::vector<int32_t> mem(M0.groups.col.size());
+    for (size_t q = 0; q < mem.size(); ++q) mem[q] = slot[M0.groups.col[q]];
     if (int e = A.upload(&o, M0.groups.off, s)) return e;
-    if (int e = A.upload(&m, M0.groups.col, s)) return e;
+    if (int e = A.upload(&m, mem, s)) return e;
     F.goff = o;
     F.gmem = m;
   }
   {
+    // Restriction gathers level-0 slots; the prolongation's rows follow the slots.
+    std::vector<int32_t> child(M0.restrict.col.size());
+    for (size_t q = 0; q < child.size(); ++q) child[q] = slot[M0.restrict.col[q]];
+    std::vector<int32_t> poff(F.N2 + 1, 0), pcol;
+    std::vector<float> pw32;
+    pcol.reserve(M0.prolong.col.size());
+    pw32.reserve(M0.prolong.col.size());
+    for (int sl = 0; sl < F.N2; ++sl) {
+      const int c = cell_of[sl];
+      if (c >= 0)
+        for (int q = M0.prolong.off[c]; q < M0.prolong.off[c + 1]; ++q) {
+          pcol.push_back(M0.prolong.col[q]);
+          pw32.push_back((float)M0.prolong.val[q]);
+        }
+      poff[sl + 1] = (int32_t)pcol.size();
+    }
     int *o, *c, *po, *pc;
     float *w, *pw;
     if (int e = A.upload(&o, M0.restrict.off, s)) return e;
-    if (int e = A.upload(&c, M0.restrict.col, s)) return e;
+    if (int e = A.upload(&c, child, s)) return e;
     if (int e = A.upload(&w, to_f32(M0.restrict.val), s)) return e;
-    if (int e = A.upload(&po, M0.prolong.off, s)) return e;
-    if (int e = A.upload(&pc, M0.prolong.col, s)) return e;
-    if (int e = A.upload(&pw, to_f32(M0.prolong.val), s)) return e;
+    if (int e = A.upload(&po, poff, s)) return e;
+    if (int e = A.upload(&pc, pcol, s)) return e;
+    if (int e = A.upload(&pw, pw32, s)) return e;
     F.r_off = o, F.r_child = c, F.r_w = w, F.p_off = po, F.p_col = pc, F.p_w = pw;
   }
   // Coarse levels 1 .. L-1.
@@ -1229,7 +1469,27 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     if (int e = A.upload(&d, to_f32(M.diag), s)) return e;
     L.off = o, L.col = c, L.val = v, L.diag = d;
     std::vector<int32_t> coff, rows;
-    greedy_colors(M.a, M.n, coff, rows, L.ncolors);
+    if (!parity_colors(M.a, M.parity, M.n, coff, rows, L.ncolors)) greedy_colors(M.a, M.n, coff, rows, L.ncolors);
+    // A level whose graph needs many colours (the wide stencils of linear-interpolation
+    // coarse operators) is smoothed by l1-Jacobi instead: one phase per sweep.
+    L.jacobi = !L.terminal && L.ncolors > 8 ? 1 : 0;
+    if (L.jacobi) {
+      L.ncolors = 1;
+      coff = {0, M.n};
+      rows.resize(M.n);
+      for (int i = 0; i < M.n; ++i) rows[i] = i;
+      std::vector<float> il1(M.n, 0.0f);
+      for (int i = 0; i < M.n; ++i) {
+        double sum = std::fabs(M.diag[i]);
+        for (int k = M.a.off[i]; k < M.a.off[i + 1]; ++k) sum += std::fabs(M.a.val[k]);
+        il1[i] = M.diag[i] == 0.0 ? 0.0f : (float)(1.0 / sum);
+      }
+      float *pl, *x2;
+      if (int e = A.upload(&pl, il1, s)) return e;
+      if (int e = A.alloc(&x2, M.n)) return e;
+      L.il1 = pl;
+      L.x2 = x2;
+    }
     cs.colors.push_back(coff);
     int *co, *cr;
     if (int e = A.upload(&co, coff, s)) return e;
@@ -1268,6 +1528,8 @@ int build_case(cfdg_grid* G, CaseState& cs) {
       if (int e = A.upload(&ev, eval, s)) return e;
       if (int e = A.upload(&idp, idg, s)) return e;
       L.ell_off = eo, L.ell_w = ewp, L.ell_col = ec, L.ell_val = ev, L.idiag = idp;
+      cs.stats.push_back({M.n, (long long)M.a.col.size(), (long long)ecol.size(), M.groups.rows(),
+                          L.terminal ? M.direct_idx.rows() : 0, L.ncolors, L.jacobi});
     }
     if (L.ngroups) {
       int *go, *gm;
@@ -1368,7 +1630,7 @@ struct cfdg_batch {
   // the prologue's and the epilogue's.
   std::vector<int2> tiles, tiles1, ftiles, gtab;
   WorkLists run, pro, epi;
-  int g_fine = 1, g_1 = 1, g_f = 1, g_g = 1;  // persistent grid sizes
+  int g_fine = 1, g_1 = 1, g_f = 1, g_g = 1;  // work items per list: caps on the persistent grids
   bool any_groups = false;
   // Coarse-level phase tables (device), refilled for each active set.
   CoarseTab h_tab{};
@@ -1420,10 +1682,13 @@ int fill_tab(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
   const int nc = (int)B->cases.size(), nlev = B->nlev_all, w = nc + 1;
   CoarseTab& T = B->h_tab;
   static thread_local std::vector<int32_t> buf;
-  const size_t words = (size_t)nlev * w * (5 + 2 * MAXC);
+  const size_t words = (size_t)nlev * w * (6 + 2 * MAXC);
   buf.assign(words, 0);
   int32_t *rows = buf.data(), *term = rows + nlev * w, *next = term + nlev * w, *live = next + nlev * w,
-          *grp = live + nlev * w, *fwd = grp + nlev * w, *bwd = fwd + (size_t)nlev * MAXC * w;
+          *grp = live + nlev * w, *res = grp + nlev * w, *fwd = res + nlev * w, *bwd = fwd + (size_t)nlev * MAXC * w;
+  // Sweep and residual ranges are rounded up to multiples of eight, so the eight-lane
+  // groups of l1-Jacobi rows never straddle two cases.
+  auto r8 = [](int v) { return (v + 7) & ~7; };
   T.nc = nc;
   T.nlev = 0;
   for (int l = 0; l < nlev; ++l) {
@@ -1447,13 +1712,16 @@ int fill_tab(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
       next[l * w + i + 1] = next[l * w + i] + (nt ? B->cases[i]->C.lv[l + 1].n : 0);
       live[l * w + i + 1] = live[l * w + i] + (nt ? L->n : 0);
       grp[l * w + i + 1] = grp[l * w + i] + (L ? L->ngroups : 0);
+      res[l * w + i + 1] = res[l * w + i] + (nt ? r8(L->jacobi ? 8 * L->n : L->n) : 0);
       for (int c = 0; c < MAXC; ++c) {
         int nf = 0, nb = 0;
-        if (nt && c < L->ncolors) {
+        if (nt && L->jacobi) {
+          nf = nb = c == 0 ? 8 * L->n : 0;
+        } else if (nt && c < L->ncolors) {
           const auto& co = B->cases[i]->colors[l];
-          nf = co[c + 1] - co[c];
+          nf = r8(co[c + 1] - co[c]);
           const int cb = L->ncolors - 1 - c;
-          nb = co[cb + 1] - co[cb];
+          nb = r8(co[cb + 1] - co[cb]);
         }
         fwd[(l * MAXC + c) * w + i + 1] = fwd[(l * MAXC + c) * w + i] + nf;
         bwd[(l * MAXC + c) * w + i + 1] = bwd[(l * MAXC + c) * w + i] + nb;
@@ -1465,7 +1733,8 @@ int fill_tab(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
   T.next = T.term + nlev * w;
   T.live = T.next + nlev * w;
   T.grp = T.live + nlev * w;
-  T.fwd = T.grp + nlev * w;
+  T.res = T.grp + nlev * w;
+  T.fwd = T.res + nlev * w;
   T.bwd = T.fwd + (size_t)nlev * MAXC * w;
   CU(cudaMemcpyAsync(B->tab_buf, buf.data(), words * sizeof(int32_t), cudaMemcpyHostToDevice, s));
   CU(cudaMemcpyAsync(B->d_tab, &T, sizeof(CoarseTab), cudaMemcpyHostToDevice, s));
@@ -1508,23 +1777,46 @@ void launch_coarse(cfdg_batch* B, cudaStream_t s) {
   cudaLaunchKernelEx(&cfg, k_coarse, (const CCase*)B->d_cc, (const MState*)B->d_st);
 }
 
-#define FINE(K, W, ...) K<<<B->g_fine, TILE, 0, s>>>(B->d_fc, B->d_st, (W).tiles, (W).counts, ##__VA_ARGS__)
+// Persistent grids: every block resident at once (the SM count times the kernel's
+// occupancy), and no more blocks than work items.
+int resident_grid(const void* fn, int threads) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find({dev, fn});
+  if (it != cache.end()) return it->second;
+  int sms = 0, per = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0) != cudaSuccess || per < 1) {
+    cudaGetLastError();
+    per = 1;
+  }
+  return cache[{dev, fn}] = std::max(1, sms) * per;
+}
+template <class K>
+int grid_of(K kernel, int threads, int items) {
+  return std::max(1, std::min(items, resident_grid((const void*)kernel, threads)));
+}
+#define FINE(K, W, ...) \
+  K<<<grid_of(K, TILE, B->g_fine), TILE, 0, s>>>(B->d_fc, B->d_st, (W).tiles, (W).counts, ##__VA_ARGS__)
 
 void enqueue_vcycle(cfdg_batch* B, cudaStream_t s) {
   const WorkLists& W = B->run;
   if (B->any_groups) {
     FINE(k_v_rhs, W);
-    k_center0<<<B->g_g, 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 0);
+    k_center0<<<grid_of(k_center0, 256, B->g_g), 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 0);
   }
   // Two forward sweeps: red, black, red, black (the first red starts from x = 0).
   FINE(k_rb, W, 0, 1);
   FINE(k_rb, W, 1, 0);
   FINE(k_rb, W, 0, 0);
   FINE(k_rb, W, 1, 0);
-  if (B->any_groups) k_center0<<<B->g_g, 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 1);
+  if (B->any_groups) k_center0<<<grid_of(k_center0, 256, B->g_g), 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 1);
   FINE(k_v_resid, W);
-  if (B->any_groups) k_center0<<<B->g_g, 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 2);
-  k_v_restrict<<<B->g_1, TILE, 0, s>>>(B->d_fc, B->d_st, W.tiles1, W.counts + 1);
+  if (B->any_groups) k_center0<<<grid_of(k_center0, 256, B->g_g), 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 2);
+  k_v_restrict<<<grid_of(k_v_restrict, TILE, B->g_1), TILE, 0, s>>>(B->d_fc, B->d_st, W.tiles1, W.counts + 1);
   launch_coarse(B, s);
   FINE(k_v_prolong, W);
   // Two backward sweeps: black, red, black, red.
@@ -1532,7 +1824,7 @@ void enqueue_vcycle(cfdg_batch* B, cudaStream_t s) {
   FINE(k_rb, W, 0, 0);
   FINE(k_rb, W, 1, 0);
   FINE(k_rb, W, 0, 0);
-  if (B->any_groups) k_center0<<<B->g_g, 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 1);
+  if (B->any_groups) k_center0<<<grid_of(k_center0, 256, B->g_g), 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 1);
 }
 
 // One iteration of the per-case state machine.
@@ -1627,7 +1919,7 @@ int epilogue(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
   if (int e = fill_lists(B, B->epi, on, s)) return e;
   for (size_t i = 0; i < B->cases.size(); ++i)
     if (on[i] && B->grids[i]->ncomp_groups) plain_center(B->grids[i], B->grids[i]->x, s);
-  k_correct<<<B->g_f, 256, 0, s>>>(B->d_fc, B->d_st, B->epi.ftiles, B->epi.counts + 2);
+  k_correct<<<grid_of(k_correct, 256, B->g_f), 256, 0, s>>>(B->d_fc, B->d_st, B->epi.ftiles, B->epi.counts + 2);
   FINE(k_addp, B->epi);
   count(2);
   for (size_t i = 0; i < B->cases.size(); ++i)
@@ -1686,7 +1978,7 @@ int cfdg_mixed_pack(cfdg_batch* B) {
     if (int e = A.alloc(&W->gtab, B->gtab.size())) return e;
     if (int e = A.alloc(&W->counts, 4)) return e;
   }
-  auto clamp = [](size_t n) { return (int)std::max<size_t>(1, std::min<size_t>(n, 152 * 8)); };
+  auto clamp = [](size_t n) { return (int)std::max<size_t>(1, std::min<size_t>(n, 1 << 30)); };
   B->g_fine = clamp(B->tiles.size());
   B->g_1 = clamp(B->tiles1.size());
   B->g_f = clamp(B->ftiles.size());
@@ -1699,7 +1991,7 @@ int cfdg_mixed_pack(cfdg_batch* B) {
   CU(cudaMemcpyAsync(B->d_st, idle.data(), sizeof(MState) * nc, cudaMemcpyHostToDevice, s));
   if (B->h_st) cudaFreeHost(B->h_st);
   CU(cudaMallocHost((void**)&B->h_st, sizeof(MState) * nc));
-  if (int e = A.alloc(&B->tab_buf, (size_t)B->nlev_all * (nc + 1) * (5 + 2 * MAXC) + 1)) return e;
+  if (int e = A.alloc(&B->tab_buf, (size_t)B->nlev_all * (nc + 1) * (6 + 2 * MAXC) + 1)) return e;
   if (int e = A.alloc(&B->d_tab, 1)) return e;
   B->active.assign(nc, 1);
   if (int e = set_active(B, s)) return e;
@@ -1951,6 +2243,38 @@ int cfdg_batch_set_stream(cfdg_batch* B, void* stream) {
 }
 
 int cfdg_batch_size(const cfdg_batch* B) { return B ? (int)B->cases.size() : 0; }
+
+int64_t cfdg_batch_stats_json(cfdg_batch* B, char* buf, int64_t cap) {
+  if (!B) return -(int64_t)fail(CFDG_ERR_INVALID, "null batch");
+  Locks locks(B->grids);
+  char tmp[256];
+  snprintf(tmp, sizeof tmp, "{\"coarse_kernel\": \"%s\", \"coarse_blocks\": %d, \"cases\": [",
+           B->coop ? "cooperative" : "cluster", B->coop ? B->coop_blocks : (int)B->cases.size() * B->csize);
+  std::string out = tmp;
+  for (size_t i = 0; i < B->cases.size(); ++i) {
+    const CaseState& cs = *B->cases[i];
+    snprintf(tmp, sizeof tmp, "%s{\"cells\": %d, \"groups0\": %d, \"levels\": [", i ? ", " : "", cs.F.N,
+             cs.ngroups0);
+    out += tmp;
+    for (size_t l = 0; l < cs.stats.size(); ++l) {
+      const auto& v = cs.stats[l];
+      snprintf(tmp, sizeof tmp,
+               "%s{\"rows\": %lld, \"nnz\": %lld, \"smoother\": \"%s\", \"colors\": %d, \"ell_entries\": %lld, "
+               "\"groups\": %lld, \"blocks\": %lld}",
+               l ? ", " : "", v.rows, v.nnz, v.jacobi ? "l1-jacobi" : "gauss-seidel", v.colors, v.ell, v.groups,
+               v.blocks);
+      out += tmp;
+    }
+    out += "]}";
+  }
+  out += "]}";
+  if (buf && cap > 0) {
+    const size_t k = std::min((size_t)cap - 1, out.size());
+    memcpy(buf, out.data(), k);
+    buf[k] = 0;
+  }
+  return (int64_t)out.size() + 1;
+}
 
 int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* ms_per_launch,
                            double* algorithmic_bytes) {

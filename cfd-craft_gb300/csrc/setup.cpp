@@ -384,6 +384,7 @@ static int build_masked(const HostGrid& g, const Poller& poll, Hierarchy& h) {
         factors.push_back(std::move(l));
       }
       finish_terminal(lev, blocks, factors);
+      for (auto& p : coords) lev.parity.push_back((uint8_t)((p[0] + p[1] + p[2]) & 1));
       h.levels.push_back(std::move(lev));
       break;
     }
@@ -445,6 +446,7 @@ static int build_masked(const HostGrid& g, const Poller& poll, Hierarchy& h) {
     std::vector<double> ac(nc, 0.0);
     for (size_t i = 0; i < anchors.size(); ++i) ac[parent[i]] += anchors[i];
     aggregation_transfer(parent, nc, lev);
+    for (auto& p : coords) lev.parity.push_back((uint8_t)((p[0] + p[1] + p[2]) & 1));
     h.levels.push_back(std::move(lev));
     edges = std::move(next);
     anchors = std::move(ac);

@@ -80,6 +80,10 @@ struct MgLevel {
   Csr groups;    // closed groups centred at this level: members per group
   Csr prolong;   // fine row -> (coarse column, weight), columns ascending
   Csr restrict;  // coarse row -> (fine child, weight), children ascending
+  // Masked levels: parity of the node's bin coordinates. Aggregates are connected sets
+  // inside one bin, so neighbouring nodes sit in face-adjacent bins and the parity is
+  // a two-colouring of the level's graph (used by the parallel smoothers).
+  std::vector<uint8_t> parity;
   // Terminal level: dense lower Cholesky blocks (masked.rs:16-70, multigrid.rs:468-520).
   Csr direct_idx;                   // block -> solved indices
   std::vector<int64_t> direct_off;  // block -> offset of its n*n factor in direct_factor

@@ -364,6 +364,17 @@ class Batch:
     def project_device(self, u_ptrs, p_ptrs, dts, tol, max_iter, control=None):
         return self._run(self.L.cfdg_batch_project_device, u_ptrs, p_ptrs, dts, tol, max_iter, control)
 
+    def stats(self) -> dict:
+        """Per case and coarse level: rows, nonzeros, colours, ELL entries, groups, blocks."""
+        import json
+
+        n = self.L.cfdg_batch_stats_json(self.h, None, 0)
+        if n < 0:
+            raise PressureError(int(-n), E.last_error())
+        buf = C.create_string_buffer(int(n))
+        self.L.cfdg_batch_stats_json(self.h, buf, int(n))
+        return json.loads(buf.value.decode())
+
     def time_kernel(self, which: int, reps: int = 20):
         """(ms per launch, algorithmic bytes); see cfdg_batch_time_kernel."""
         ms, b = C.c_double(), C.c_double()

@@ -202,6 +202,11 @@ int cfdg_batch_project(cfdg_batch *batch, double *const *u, double *const *p, co
  * stated). Diagnostic; no reference counterpart. */
 int cfdg_batch_time_kernel(cfdg_batch *batch, int32_t which, int32_t reps, double *ms_per_launch,
                            double *algorithmic_bytes);
+/* Per case and coarse level of the batch's FP32 hierarchies, as JSON: rows, nonzeros,
+ * smoother colours, ELL entries (with padding), closed groups and terminal blocks. Writes
+ * at most cap bytes (NUL-terminated) and returns the length the full text needs, or a
+ * negative error code. Diagnostic; no reference counterpart. */
+int64_t cfdg_batch_stats_json(cfdg_batch *batch, char *buf, int64_t cap);
 /* The same on device arrays d_u[i] (F_i doubles) and d_p[i] (N_i doubles). */
 int cfdg_batch_project_device(cfdg_batch *batch, double *const *d_u, double *const *d_p, const double *dt,
                               double tol, uint64_t max_iter, cfdg_poll_fn poll, void *poll_ctx, cfdg_info *infos,
