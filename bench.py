@@ -1,19 +1,27 @@
 #!/usr/bin/env python3
 """Pressure-projection benchmark of the GB300 engine: Poisson solves/s at 1e-8.
 
-Workload (one step = one projection solve): the 128x128x64 grid (dx = 2 m) with 12
-seeded box buildings, open x / wall y,z, inflow 5 m/s; the projection of the
-seeded u* sequence u*_{s+1} = project(u*_s) + 0.05 U[-1,1] (fixed faces untouched),
-dt = 0.1 s, multigrid V(2,2)-preconditioned CG to 1e-8 relative residual. Inputs
-are synthetic (numpy PCG64 seeds); the reference publishes no dataset.
+Default (serving form): the wind-direction campaign mix - 36 cases on a 128x128x64 grid
+(dx = 2 m, 30 seeded buildings, open x/y, ground_open_top z, neutral_rans 5 m/s, one case
+per 10-degree wind direction) plus 16 cases at 96x96x48 with 0-20 buildings - served
+through the continuous-batching server (cfdg_server) with every case's state resident.
+One step is one time step of every case: the projection of its seeded u* sequence
+(u*_{s+1} = project(u*_s) + 0.05 U[-1,1] on the free faces), dt = 0.1 s, mixed
+FP32/FP64 multigrid PCG to 1e-8 relative residual. `value` is the closed-loop
+throughput (a case's next step is submitted when its last one finishes); `serving`
+adds an open-loop run with Poisson arrivals (mean 200/s, seed 5) and its p50/p99
+latency; `plain_fp64` times the plain FP64 form on the same mix and `cpu_baseline` the
+CPU restatement of the reference on all host cores. Inputs are synthetic (numpy PCG64
+seeds); the reference publishes no dataset.
 
-  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--form plain]
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+                  [--form serving|batched|mixed|plain]
 
-Prints one JSON line (rank 0). `value` is device-resident throughput; `e2e` is the
-same metric through the public C ABI (cfdg_project) with pinned host buffers, the
-host<->device copies inside the timed region. `--impl reference` times the
-reference algorithm's CPU restatement (the oracle; the Rust reference cannot be
-built here) on all host cores.
+`--form batched|mixed|plain` measure the 128x128x64 grid with 12 buildings (one case per
+step, or 8 cases per batched step). Prints one JSON line (rank 0). `e2e` is the same
+metric through the public C ABI with pinned host buffers, the host<->device copies
+inside the timed region. `--impl reference` times the reference algorithm's CPU
+restatement (the oracle; the Rust reference cannot be built here) on all host cores.
 """
 from __future__ import annotations
 
@@ -344,7 +352,7 @@ class Serving:
     """The serving mix through cfdg_server: every case's fields, hierarchy and FP32 state stay
     resident; a case's next step is its projected field plus the seeded perturbation."""
 
-    def __init__(self, pkg, torch, dev, stream, slots, rank):
+    def __init__(self, pkg, torch, dev, stream, slots, rank, autotune=True, chunk=0):
         import numpy as np
 
         self.pkg, self.torch, self.dev, self.stream = pkg, torch, dev, stream
@@ -354,11 +362,30 @@ class Serving:
         self.dgs = [pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed") for g in self.grids]
         for d in self.dgs:
             d.set_stream(stream.cuda_stream)
-        self.server = pkg.pressure.Server(self.dgs, slots or self.n)
-        self.server.set_stream(stream.cuda_stream)
         self.u0 = [pkg.synth.random_velocity(g, seed=5000 + 100 * rank + i) for i, g in enumerate(self.grids)]
         self.d_u = [torch.from_numpy(u).to(dev) for u in self.u0]
         self.d_p = [torch.zeros(g.count, dtype=torch.float64, device=dev) for g in self.grids]
+        self.tuned = None
+        if autotune:
+            # The sweep counts with the shortest time to 1e-8 on this mix (first step's inputs).
+            d_u0 = [u.clone() for u in self.d_u]
+
+            def reset():
+                for u, u0, p in zip(self.d_u, d_u0, self.d_p):
+                    u.copy_(u0)
+                    p.zero_()
+
+            t0 = time.perf_counter()
+            self.tuned = pkg.pressure.autotune(self.dgs, [u.data_ptr() for u in self.d_u],
+                                               [p.data_ptr() for p in self.d_p], reset, [DT] * self.n, TOL, MAX_IT,
+                                               stream_handle=stream.cuda_stream)
+            torch.cuda.synchronize()
+            self.tuned["seconds"] = round(time.perf_counter() - t0, 2)
+            del d_u0
+        self.server = pkg.pressure.Server(self.dgs, slots or self.n)
+        self.server.set_stream(stream.cuda_stream)
+        if chunk:
+            self.server.set_chunk(chunk)
         self.free = []
         for g in self.grids:
             m = ((g.face_kind == pkg.grid.INTERIOR) | (g.face_kind == pkg.grid.OUTLET)).astype(np.float64)
@@ -480,7 +507,7 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     import numpy as np
 
     K, W = args.steps, args.warmup
-    sv = Serving(pkg, torch, dev, stream, args.slots, rank)
+    sv = Serving(pkg, torch, dev, stream, args.slots, rank, autotune=not args.no_autotune, chunk=args.chunk)
     n = sv.n
     t_setup = time.perf_counter()
     sv.closed_loop(W)  # first solves build every hierarchy and FP32 state
@@ -495,9 +522,14 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     ev1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     ev0.record(stream)
+    st0 = sv.server.stats()
     lat, infos = sv.closed_loop(K)
     ev1.record(stream)
     torch.cuda.synchronize()
+    st1 = sv.server.stats()
+    loop = {k: round(st1[k] - st0[k], 3) for k in ("rounds", "chunks", "chunk_device_ms", "progress_host_ms",
+                                                   "finished", "admitted")}
+    loop["iterations_per_chunk"] = st1["iterations_per_chunk"]
     clk = clocks.stop()
     launches = L.cfdg_launch_count() - launches0
     total_ms = ev0.elapsed_time(ev1)
@@ -506,12 +538,14 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     solves = world * K * n
     value = solves / (total_ms / 1e3)
     cell_updates = sum(sv.cells[c] * i.iterations for c, i in infos)
-    # Open loop at the stated arrival rate.
-    plat, span, last_arrival = sv.poisson(args.requests, args.rate, seed=5)
-    serving = {"arrivals": "Poisson, seed 5", "offered_per_s": args.rate, "requests": args.requests,
-               "throughput": round(args.requests / span, 2), "arrival_span_s": round(last_arrival, 3),
-               "p50_ms": round(1e3 * pct(plat, 0.50), 2), "p99_ms": round(1e3 * pct(plat, 0.99), 2),
-               "max_ms": round(1e3 * max(plat), 2), "slots": args.slots or n}
+    # Open loop at the stated arrival rate (skipped with --requests 0).
+    serving = None
+    if args.requests > 0:
+        plat, span, last_arrival = sv.poisson(args.requests, args.rate, seed=5)
+        serving = {"arrivals": "Poisson, seed 5", "offered_per_s": args.rate, "requests": args.requests,
+                   "throughput": round(args.requests / span, 2), "arrival_span_s": round(last_arrival, 3),
+                   "p50_ms": round(1e3 * pct(plat, 0.50), 2), "p99_ms": round(1e3 * pct(plat, 0.99), 2),
+                   "max_ms": round(1e3 * max(plat), 2), "slots": args.slots or n}
     # End to end through the host-buffer batch call: every case of the mix per step, H2D + D2H inside.
     bt = pkg.pressure.Batch(sv.dgs)
     bt.set_stream(stream.cuda_stream)
@@ -593,11 +627,12 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
                        "cells_per_step": sum(sv.cells), "l2": "inputs larger than L2: the mix holds "
                        f"{sum(sv.cells) * 8 * 10 / 1e9:.1f} GB of FP64 fields alone",
                        "parallelism": f"replicas x{world}"},
-            "latency_ms": {"p50": serving["p50_ms"], "p99": serving["p99_ms"],
+            "latency_ms": {"p50": serving["p50_ms"] if serving else None, "p99": serving["p99_ms"] if serving else None,
                            "unit": "per request, open loop at the offered rate",
                            "closed_loop_p50": round(1e3 * pct(lat, 0.5), 2),
                            "closed_loop_p99": round(1e3 * pct(lat, 0.99), 2)},
-            "serving": serving, "setup_s": round(setup_s, 2), "coarse_levels": coarse,
+            "serving": serving, "setup_s": round(setup_s, 2), "server_loop": loop, "autotune": sv.tuned,
+            "coarse_levels": coarse,
             "iterations_mean": round(statistics.mean(its), 2),
             "cell_updates_per_s": round(world * cell_updates / (total_ms / 1e3), 1),
             "e2e": e2e, "roofline": roofline, "kernels": kernels, "plain_fp64": plain, "cpu_baseline": cpu,
@@ -736,10 +771,12 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--form", default="batched", choices=["plain", "mixed", "batched", "serving"])
+    ap.add_argument("--form", default="serving", choices=["plain", "mixed", "batched", "serving"])
     ap.add_argument("--slots", type=int, default=0, help="serving: cases on the GPU at once (0: all)")
     ap.add_argument("--requests", type=int, default=520, help="serving: open-loop requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")
+    ap.add_argument("--chunk", type=int, default=0, help="serving: iterations per graph chunk (0: the engine's)")
+    ap.add_argument("--no-autotune", action="store_true", help="serving: keep the default V(2,2) sweeps")
     ap.add_argument("--cases", type=int, default=8, help="cases per step of the batched form")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

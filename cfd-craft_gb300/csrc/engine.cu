@@ -1438,6 +1438,17 @@ int cfdg_grid_configure(cfdg_grid* G, int32_t preconditioner, int32_t precision)
   return 0;
 }
 
+int cfdg_grid_set_cycle(cfdg_grid* G, int32_t nu_fine, int32_t nu_coarse) {
+  if (int e = check_grid(G)) return e;
+  if (nu_fine < 1 || nu_fine > 4 || nu_coarse < 1 || nu_coarse > 4)
+    return fail(CFDG_ERR_INVALID, "sweep counts must be 1..4");
+  std::lock_guard<std::mutex> lk(G->mu);
+  if (G->mx_nu0 != nu_fine || G->mx_nuc != nu_coarse) G->solo.reset();
+  G->mx_nu0 = nu_fine;
+  G->mx_nuc = nu_coarse;
+  return 0;
+}
+
 int cfdg_project_device(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol, uint64_t max_iter,
                         cfdg_poll_fn poll, void* poll_ctx, cfdg_info* info) {
   if (int e = check_grid(G)) return e;

@@ -24,6 +24,7 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -114,7 +115,7 @@ struct CLev {
   float* x2;         // l1-Jacobi: the second iterate of a sweep pair
   const int *off, *col;
   const float *val, *diag;
-  const int *coff, *crows;
+  const int* coff;  // colour c owns rows coff[c] .. coff[c+1]-1
   const int *ell_off, *ell_w;  // per colour: start of its ELL block and its width
   const int* ell_col;          // column-major ELL per colour (padding points at the row itself)
   const float* ell_val;        // entries, 0 in padding
@@ -157,28 +158,50 @@ __device__ __forceinline__ double bsum(double v, double* sh) {
   return s;
 }
 
-// Per-case last-block reduction: returns true in the block that finishes the case,
-// with *out the sum of the case's partials in tile order.
-__device__ __forceinline__ bool case_reduce(double v, const FineCase& F, MState& S, int lt, double* sh, double* out) {
+// Reductions of the fine-level kernels. Every tile stores its block sum in the case's
+// partials (slot = tile index); a block counts a case's tiles once per run of
+// consecutive tiles of that case, and the block that completes a case sums the partials
+// in tile order (the same bits whatever the grid size) and applies the case's scalar
+// update.
+__device__ __forceinline__ void tile_partial(double v, const FineCase& F, int lt, double* sh, int& seg_n) {
+  const double b = bsum(v, sh);
+  if (threadIdx.x == 0) F.partials[lt] = b;
+  ++seg_n;
+}
+
+struct Seg {
+  int ci = -1, n = 0;  // case of the current run of tiles, tiles with a stored partial
+};
+
+template <class Fin>
+__device__ __forceinline__ void close_seg(const FineCase* FC, MState* ST, Seg& g, double* sh, Fin fin) {
+  if (g.n == 0) return;
   __shared__ bool last;
-  double b = bsum(v, sh);
   if (threadIdx.x == 0) {
-    F.partials[lt] = b;
     __threadfence();
-    last = atomicAdd(&S.counter, 1u) == (unsigned)F.ntiles - 1;
+    last = atomicAdd(&ST[g.ci].counter, (unsigned)g.n) + (unsigned)g.n == (unsigned)FC[g.ci].ntiles;
   }
   __syncthreads();
-  if (!last) return false;
+  g.n = 0;
+  if (!last) return;
   __threadfence();
+  const int nt = FC[g.ci].ntiles;
+  const double* part = FC[g.ci].partials;
   double a = 0.0;
-  for (int k = threadIdx.x; k < F.ntiles; k += blockDim.x) a += __ldcg(&F.partials[k]);
-  double s = bsum(a, sh);
+  for (int k = threadIdx.x; k < nt; k += blockDim.x) a += __ldcg(&part[k]);
+  const double s = bsum(a, sh);
   if (threadIdx.x == 0) {
-    S.counter = 0;
-    *out = s;
+    ST[g.ci].counter = 0;
+    fin(ST[g.ci], s);
   }
-  return true;
 }
+
+// Persistent fine-level kernels: block b takes the contiguous tile range
+// [b*per, (b+1)*per) of the work-list (neighbouring rows stay in one block's cache).
+#define TILE_RANGE                                   \
+  const int n_ = *count;                             \
+  const int per_ = (n_ + gridDim.x - 1) / gridDim.x; \
+  const int t0_ = blockIdx.x * per_, t1_ = min(n_, t0_ + per_);
 
 __device__ __forceinline__ void coords(const FineCase& F, int c, int& i, int& j, int& k) {
   i = c % F.n[0];
@@ -386,9 +409,20 @@ __device__ __forceinline__ float nbsum32(const FineCase& F, const float* __restr
   return v;
 }
 
+struct FinOp {
+  __device__ void operator()(MState& S, double pq) const {
+    if (!(pq > 0.0) || !isfinite(pq)) {
+      S.state = FAIL;
+      S.error = CFDG_E032;
+    } else {
+      S.alpha = S.rz / pq;
+    }
+  }
+};
+
 // A: q = A32 p, alpha = rz / (p.q) (E032 when not positive).
-__device__ __forceinline__ void b_op(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
-  __shared__ double sh[32];
+__device__ __forceinline__ void b_op(const FineCase* FC, MState* ST, const int2 t, int& cached_, double* sh,
+                                    int& seg_n) {
   FINE_PROLOGUE(S.state == RUN)
   float hi = 0.0f, lo = 0.0f;
   int j, k, rb;
@@ -436,25 +470,36 @@ __device__ __forceinline__ void b_op(const FineCase* FC, MState* ST, const int2 
       }
     }
   }
-  double pq;
-  if (case_reduce((double)hi + (double)lo, F, S, lt, sh, &pq) && threadIdx.x == 0) {
-    if (!(pq > 0.0) || !isfinite(pq)) {
-      S.state = FAIL;
-      S.error = CFDG_E032;
-    } else {
-      S.alpha = S.rz / pq;
-    }
-  }
+  tile_partial((double)hi + (double)lo, F, lt, sh, seg_n);
 }
 __global__ void __launch_bounds__(TILE) k_op(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  __shared__ double sh[32];
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_op(FC, ST, tiles[ti], cached_);
+  Seg g;
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    if (t.x != g.ci) {
+      close_seg(FC, ST, g, sh, FinOp());
+      g.ci = t.x;
+    }
+    b_op(FC, ST, t, cached_, sh, g.n);
+  }
+  close_seg(FC, ST, g, sh, FinOp());
 }
 
+struct FinUpdate {
+  __device__ void operator()(MState& S, double rr) const {
+    S.inner_it += 1;
+    S.total_it += 1;
+    S.has_e = 1;
+    if (sqrt(rr) <= S.inner_tol || S.inner_it >= S.max_inner || S.total_it >= S.max_it) S.state = OUTER;
+  }
+};
+
 // B: e += alpha p, r -= alpha q; |r| decides the end of the inner solve.
-__device__ __forceinline__ void b_update(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
-  __shared__ double sh[32];
+__device__ __forceinline__ void b_update(const FineCase* FC, MState* ST, const int2 t, int& cached_, double* sh,
+                                    int& seg_n) {
   FINE_PROLOGUE(S.state == RUN)
   const float alpha = (float)S.alpha;
   float hi = 0.0f, lo = 0.0f;
@@ -464,18 +509,22 @@ __device__ __forceinline__ void b_update(const FineCase* FC, MState* ST, const i
     F.r32[c] = r;
     dd_add_prod(r, r, hi, lo);
   }
-  double rr;
-  if (case_reduce((double)hi + (double)lo, F, S, lt, sh, &rr) && threadIdx.x == 0) {
-    S.inner_it += 1;
-    S.total_it += 1;
-    S.has_e = 1;
-    if (sqrt(rr) <= S.inner_tol || S.inner_it >= S.max_inner || S.total_it >= S.max_it) S.state = OUTER;
-  }
+  tile_partial((double)hi + (double)lo, F, lt, sh, seg_n);
 }
 __global__ void __launch_bounds__(TILE) k_update(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  __shared__ double sh[32];
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_update(FC, ST, tiles[ti], cached_);
+  Seg g;
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    if (t.x != g.ci) {
+      close_seg(FC, ST, g, sh, FinUpdate());
+      g.ci = t.x;
+    }
+    b_update(FC, ST, t, cached_, sh, g.n);
+  }
+  close_seg(FC, ST, g, sh, FinUpdate());
 }
 
 // C1: x += |r| e (the residual is formed by k_outer_resid once every block has updated x).
@@ -490,23 +539,13 @@ __device__ __forceinline__ void b_outer(const FineCase* FC, MState* ST, const in
     F.x64[rb + i] = F.x64[rb + i] + scale * (double)F.e[lay(r, (i + rp) & 1, nxh_, i >> 1)];
 }
 __global__ void __launch_bounds__(TILE) k_outer(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_outer(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) b_outer(FC, ST, tiles[ti], cached_);
 }
 
-// r = b_c - A x in FP64; the true residual decides convergence.
-__device__ __forceinline__ void b_outer_resid(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
-  __shared__ double sh[32];
-  FINE_PROLOGUE(S.state == OUTER)
-  double acc = 0.0;
-  for (int c = cb + threadIdx.x; c < ce; c += TILE) {
-    const double v = __dsub_rn(F.bc[c], op64(F, F.x64, c, F.flags[c]));
-    F.r64[c] = v;
-    acc = __fma_rn(v, v, acc);
-  }
-  double rr;
-  if (case_reduce(acc, F, S, lt, sh, &rr) && threadIdx.x == 0) {
+struct FinOuterResid {
+  __device__ void operator()(MState& S, double rr) const {
     double nr = sqrt(rr);
     S.true_rel = nr / S.norm;
     if (S.true_rel <= S.tol) {
@@ -520,11 +559,34 @@ __device__ __forceinline__ void b_outer_resid(const FineCase* FC, MState* ST, co
       S.state = SCALE;
     }
   }
+};
+
+// r = b_c - A x in FP64; the true residual decides convergence.
+__device__ __forceinline__ void b_outer_resid(const FineCase* FC, MState* ST, const int2 t, int& cached_, double* sh,
+                                    int& seg_n) {
+  FINE_PROLOGUE(S.state == OUTER)
+  double acc = 0.0;
+  for (int c = cb + threadIdx.x; c < ce; c += TILE) {
+    const double v = __dsub_rn(F.bc[c], op64(F, F.x64, c, F.flags[c]));
+    F.r64[c] = v;
+    acc = __fma_rn(v, v, acc);
+  }
+  tile_partial(acc, F, lt, sh, seg_n);
 }
 __global__ void __launch_bounds__(TILE) k_outer_resid(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  __shared__ double sh[32];
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_outer_resid(FC, ST, tiles[ti], cached_);
+  Seg g;
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    if (t.x != g.ci) {
+      close_seg(FC, ST, g, sh, FinOuterResid());
+      g.ci = t.x;
+    }
+    b_outer_resid(FC, ST, t, cached_, sh, g.n);
+  }
+  close_seg(FC, ST, g, sh, FinOuterResid());
 }
 
 // C2: r32 = r / |r|, e = 0.
@@ -538,9 +600,9 @@ __device__ __forceinline__ void b_scale(const FineCase* FC, MState* ST, const in
   for (int i = lane; i < nx_; i += 32) F.r32[lay(r, (i + rp) & 1, nxh_, i >> 1)] = (float)(F.r64[rb + i] * inv);
 }
 __global__ void __launch_bounds__(TILE) k_scale(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_scale(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) b_scale(FC, ST, tiles[ti], cached_);
 }
 
 __global__ void k_start_state(MState* ST, int n) {
@@ -551,14 +613,8 @@ __global__ void k_start_state(MState* ST, int n) {
   }
 }
 
-// F: rz' = r.z; START: rz = rz', p = z (beta = 0) -> RUN; RUN: beta = rz'/rz.
-__device__ __forceinline__ void b_rz(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
-  __shared__ double sh[32];
-  FINE_PROLOGUE(S.state == RUN || S.state == START)
-  float hi = 0.0f, lo = 0.0f;
-  for (int c = sb + threadIdx.x; c < se; c += TILE) dd_add_prod(F.r32[c], F.x0[c], hi, lo);
-  double rz;
-  if (case_reduce((double)hi + (double)lo, F, S, lt, sh, &rz) && threadIdx.x == 0) {
+struct FinRz {
+  __device__ void operator()(MState& S, double rz) const {
     if (S.state == START) {
       S.beta = 0.0;
       S.state = RUN;
@@ -567,11 +623,30 @@ __device__ __forceinline__ void b_rz(const FineCase* FC, MState* ST, const int2 
     }
     S.rz = rz;
   }
+};
+
+// F: rz' = r.z; START: rz = rz', p = z (beta = 0) -> RUN; RUN: beta = rz'/rz.
+__device__ __forceinline__ void b_rz(const FineCase* FC, MState* ST, const int2 t, int& cached_, double* sh,
+                                    int& seg_n) {
+  FINE_PROLOGUE(S.state == RUN || S.state == START)
+  float hi = 0.0f, lo = 0.0f;
+  for (int c = sb + threadIdx.x; c < se; c += TILE) dd_add_prod(F.r32[c], F.x0[c], hi, lo);
+  tile_partial((double)hi + (double)lo, F, lt, sh, seg_n);
 }
 __global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  __shared__ double sh[32];
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_rz(FC, ST, tiles[ti], cached_);
+  Seg g;
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    if (t.x != g.ci) {
+      close_seg(FC, ST, g, sh, FinRz());
+      g.ci = t.x;
+    }
+    b_rz(FC, ST, t, cached_, sh, g.n);
+  }
+  close_seg(FC, ST, g, sh, FinRz());
 }
 
 // G: p = z + beta p (z is the V-cycle's level-0 solution x0).
@@ -585,9 +660,9 @@ __device__ __forceinline__ void b_p(const FineCase* FC, MState* ST, const int2 t
   }
 }
 __global__ void __launch_bounds__(TILE) k_p(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_p(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) b_p(FC, ST, tiles[ti], cached_);
 }
 
 // ----------------------------------------------------------------- V-cycle, level 0
@@ -598,9 +673,9 @@ __device__ __forceinline__ void b_v_rhs(const FineCase* FC, MState* ST, const in
   for (int c = sb + threadIdx.x; c < se; c += TILE) F.rhs0[c] = F.r32[c];
 }
 __global__ void __launch_bounds__(TILE) k_v_rhs(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_rhs(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) b_v_rhs(FC, ST, tiles[ti], cached_);
 }
 
 // Red-black Gauss-Seidel half sweep on level 0: cells with (i+j+k)%2 == color, the
@@ -656,9 +731,9 @@ __device__ __forceinline__ void b_rb(const FineCase* FC, MState* ST, const int2 
   }
 }
 __global__ void __launch_bounds__(TILE) k_rb(const FineCase* FC, MState* ST, const int2* tiles, const int* count, int color, int first) {
-  const int n = *count;
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_rb(FC, ST, tiles[ti], cached_, color, first);
+  for (int ti = t0_; ti < t1_; ++ti) b_rb(FC, ST, tiles[ti], cached_, color, first);
 }
 
 // res0 = rhs0 - A0 x0 (A0 = diag - sum w on interior faces).
@@ -715,9 +790,9 @@ __device__ __forceinline__ void b_v_resid(const FineCase* FC, MState* ST, const 
   }
 }
 __global__ void __launch_bounds__(TILE) k_v_resid(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_resid(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) b_v_resid(FC, ST, tiles[ti], cached_);
 }
 
 // rhs1 = R res0: level-1 rows gather their level-0 children. Tiles index level-1 rows.
@@ -749,9 +824,9 @@ __device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, cons
   }
 }
 __global__ void __launch_bounds__(TILE) k_v_prolong(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_v_prolong(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) b_v_prolong(FC, ST, tiles[ti], cached_);
 }
 
 // Gauge of level-0 closed groups: one block per (case, group); members strided.
@@ -808,9 +883,10 @@ __device__ void c_center(const CLev& L, float* v, double* gpart, double* sh) {
   csync();
 }
 
-__device__ void c_sweep(const CLev& L, bool backward, int pass) {
+__device__ void c_sweep(const CLev& L, bool backward, int pass, bool gs_on) {
   const int rank = (int)cg::this_cluster().block_rank();
   const int tid = rank * blockDim.x + threadIdx.x, nth = (int)cg::this_cluster().num_blocks() * blockDim.x;
+  if (!L.jacobi && !gs_on) return;
   if (L.jacobi) {  // l1-Jacobi, x -> x2 (pass 0) -> x (pass 1)
     const float* xin = pass ? L.x2 : L.x;
     float* xout = pass ? L.x : L.x2;
@@ -830,7 +906,7 @@ __device__ void c_sweep(const CLev& L, bool backward, int pass) {
     const int b = L.coff[color], nrow = L.coff[color + 1] - b;
     const int base = L.ell_off[color], w = L.ell_w[color];
     for (int t = tid; t < nrow; t += nth) {
-      const int i = L.crows[b + t];
+      const int i = b + t;  // colour blocks are contiguous
       const float id = L.idiag[i];
       float v = __ldcg(&L.rhs[i]);
       for (int a = 0; a < w; ++a) {
@@ -844,7 +920,9 @@ __device__ void c_sweep(const CLev& L, bool backward, int pass) {
   }
 }
 
-__global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState* ST) {
+// nu: Gauss-Seidel sweeps before and after the coarse correction (l1-Jacobi levels run
+// the next even count, so their iterate ends in x).
+__global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState* ST, int nu) {
   __shared__ double sh[32];
   const int csz = (int)cg::this_cluster().num_blocks();
   const int ci = blockIdx.x / csz;
@@ -877,8 +955,7 @@ __global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState*
       c_center(L, L.x, C.gpart, sh);
       break;
     }
-    c_sweep(L, false, 0);
-    c_sweep(L, false, 1);
+    for (int sw = 0; sw < nu + (nu & 1); ++sw) c_sweep(L, false, sw & 1, sw < nu);
     c_center(L, L.x, C.gpart, sh);
     for (int i = tid; i < L.n; i += nth) {
       float v = L.diag[i] * __ldcg(&L.x[i]);
@@ -907,8 +984,7 @@ __global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState*
     }
     __threadfence();
     csync();
-    c_sweep(L, true, 0);
-    c_sweep(L, true, 1);
+    for (int sw = 0; sw < nu + (nu & 1); ++sw) c_sweep(L, true, sw & 1, sw < nu);
     c_center(L, L.x, C.gpart, sh);
   }
 }
@@ -921,6 +997,7 @@ constexpr int MAXC = 32;  // colours per level
 
 struct CoarseTab {
   int nc, nlev;
+  int nu, pad_;  // sweeps before and after the coarse correction
   int maxc[MAXL];
   int anyg[MAXL];
   const int* rows;   // [nlev][nc+1] prefix over cases of the rows of level l
@@ -941,6 +1018,19 @@ __device__ __forceinline__ int find_case(const int* off, int nc, int t) {
     else hi = mid;
   }
   return lo;
+}
+
+// The case of global item t, remembering the last case's range (a thread's items
+// advance by the grid size, so consecutive ones usually share a case).
+struct CaseCursor {
+  int ci = -1, lo = 0, hi = 0;
+};
+__device__ __forceinline__ int case_at(const int* off, int nc, int t, CaseCursor& cur) {
+  if (t >= cur.lo && t < cur.hi) return cur.ci;
+  cur.ci = find_case(off, nc, t);
+  cur.lo = __ldg(&off[cur.ci]);
+  cur.hi = __ldg(&off[cur.ci + 1]);
+  return cur.ci;
 }
 
 __device__ __forceinline__ bool active(const MState* ST, int ci) {
@@ -991,16 +1081,21 @@ __device__ void g_center(const CLev* sl, const MState* ST, const CoarseTab& T, i
 }
 
 __device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, int l, bool backward, int pass,
-                        cg::grid_group& grid) {
+                        bool gs_on, cg::grid_group& grid) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
   for (int cc = 0; cc < T.maxc[l]; ++cc) {
     const int* off = (backward ? T.bwd : T.fwd) + (l * MAXC + cc) * (T.nc + 1);
     const int total = __ldg(&off[T.nc]);
+    CaseCursor cur;
+    bool on = false;
     for (int t = gt; t < total; t += nth) {
-      const int ci = find_case(off, T.nc, t);
-      if (!active(ST, ci)) continue;
+      const int prev = cur.ci;
+      const int ci = case_at(off, T.nc, t, cur);
+      if (ci != prev) on = active(ST, ci);
+      if (!on) continue;
       const CLev& L = sl[ci];
-      const int k = t - __ldg(&off[ci]);
+      const int k = t - cur.lo;
+      if (!L.jacobi && !gs_on) continue;
       if (L.jacobi) {
         // One sweep x_out = x_in + (rhs - A x_in) / (diag + sum |a_ij|); eight lanes per
         // row (the ranges of such cases start at multiples of eight), x -> x2 -> x.
@@ -1026,7 +1121,7 @@ __device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, in
       const int c0 = L.coff[color];
       const int nrow = L.coff[color + 1] - c0;
       if (k >= nrow) continue;  // ranges are rounded up to multiples of eight
-      const int i = L.crows[c0 + k];
+      const int i = c0 + k;  // colour blocks are contiguous
       const int base = L.ell_off[color], w = L.ell_w[color];
       float v = __ldcg(&L.rhs[i]);
       const int* ec = L.ell_col + base + k;
@@ -1050,7 +1145,7 @@ __device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, in
   }
 }
 
-__global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const MState* ST, const CoarseTab* Tp) {
+__global__ void __launch_bounds__(512, 3) k_coarse_all(const CCase* cases, const MState* ST, const CoarseTab* Tp) {
   const CoarseTab T = *Tp;
   __shared__ double sh[32];
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1099,8 +1194,7 @@ __global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const
       }
     }
     grid.sync();
-    g_sweep(sl, ST, T, l, false, 0, grid);
-    g_sweep(sl, ST, T, l, false, 1, grid);
+    for (int sw = 0; sw < T.nu + (T.nu & 1); ++sw) g_sweep(sl, ST, T, l, false, sw & 1, sw < T.nu, grid);
     if (T.anyg[l]) g_center(sl, ST, T, l, 1, sh, grid);
     {
       const int* off = T.res + l * (nc + 1);
@@ -1160,8 +1254,7 @@ __global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const
       }
     }
     grid.sync();
-    g_sweep(sl, ST, T, l, true, 0, grid);
-    g_sweep(sl, ST, T, l, true, 1, grid);
+    for (int sw = 0; sw < T.nu + (T.nu & 1); ++sw) g_sweep(sl, ST, T, l, true, sw & 1, sw < T.nu, grid);
     if (T.anyg[l]) g_center(sl, ST, T, l, 1, sh, grid);
   }
 }
@@ -1195,14 +1288,23 @@ __device__ __forceinline__ void b_rhs(const FineCase* FC, MState* ST, const int2
   }
 }
 __global__ void __launch_bounds__(TILE) k_rhs(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_rhs(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) b_rhs(FC, ST, tiles[ti], cached_);
 }
 
+struct FinNorm {
+  __device__ void operator()(MState& S, double bb) const {
+    S.norm = sqrt(bb);
+    S.has_e = 0;
+    S.scale = 0.0;
+    S.state = S.norm < 1e-24 ? DONE : OUTER;
+  }
+};
+
 // |b_c| (after the host-side gauge of closed components); x = 0.
-__device__ __forceinline__ void b_norm(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
-  __shared__ double sh[32];
+__device__ __forceinline__ void b_norm(const FineCase* FC, MState* ST, const int2 t, int& cached_, double* sh,
+                                    int& seg_n) {
   FINE_PROLOGUE(S.state == IDLE)
   double acc = 0.0;
   for (int c = cb + threadIdx.x; c < ce; c += TILE) {
@@ -1211,18 +1313,22 @@ __device__ __forceinline__ void b_norm(const FineCase* FC, MState* ST, const int
     F.x64[c] = 0.0;
   }
   for (int c = sb + threadIdx.x; c < se; c += TILE) F.e[c] = 0.0f;
-  double bb;
-  if (case_reduce(acc, F, S, lt, sh, &bb) && threadIdx.x == 0) {
-    S.norm = sqrt(bb);
-    S.has_e = 0;
-    S.scale = 0.0;
-    S.state = S.norm < 1e-24 ? DONE : OUTER;
-  }
+  tile_partial(acc, F, lt, sh, seg_n);
 }
 __global__ void __launch_bounds__(TILE) k_norm(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  __shared__ double sh[32];
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_norm(FC, ST, tiles[ti], cached_);
+  Seg g;
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    if (t.x != g.ci) {
+      close_seg(FC, ST, g, sh, FinNorm());
+      g.ci = t.x;
+    }
+    b_norm(FC, ST, t, cached_, sh, g.n);
+  }
+  close_seg(FC, ST, g, sh, FinNorm());
 }
 
 // Face correction u -= dt grad(x) (pressure.rs:481-496), face tiles.
@@ -1251,9 +1357,9 @@ __device__ __forceinline__ void b_addp(const FineCase* FC, MState* ST, const int
   for (int c = cb + threadIdx.x; c < ce; c += TILE) F.pfield[c] = __dadd_rn(F.pfield[c], F.x64[c]);
 }
 __global__ void __launch_bounds__(TILE) k_addp(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
-  const int n = *count;
+  TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = blockIdx.x; ti < n; ti += gridDim.x) b_addp(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) b_addp(FC, ST, tiles[ti], cached_);
 }
 
 // ----------------------------------------------------------------- host side
@@ -1320,7 +1426,30 @@ struct CaseState {
   ~CaseState() { arena.release(); }
 };
 
+// Row r of `a` becomes row prow[r] (entry order kept), columns c become pcol[c]; an
+// empty map is the identity.
+Csr permute_csr(const Csr& a, const std::vector<int32_t>& prow, const std::vector<int32_t>& pcol) {
+  Csr out;
+  const int n = a.rows();
+  out.off.assign(n + 1, 0);
+  for (int r = 0; r < n; ++r) out.off[(prow.empty() ? r : prow[r]) + 1] = a.off[r + 1] - a.off[r];
+  for (int r = 0; r < n; ++r) out.off[r + 1] += out.off[r];
+  out.col.resize(a.col.size());
+  if (!a.val.empty()) out.val.resize(a.val.size());
+  for (int r = 0; r < n; ++r) {
+    int dst = out.off[prow.empty() ? r : prow[r]];
+    for (int k = a.off[r]; k < a.off[r + 1]; ++k, ++dst) {
+      out.col[dst] = pcol.empty() ? a.col[k] : pcol[a.col[k]];
+      if (!a.val.empty()) out.val[dst] = a.val[k];
+    }
+  }
+  return out;
+}
+
 // Builds the FP32 device copy of a grid's hierarchy for the mixed form (cached on the grid).
+// Each coarse level is renumbered so that the rows of every smoother colour are
+// contiguous (colour c owns rows [coff[c], coff[c+1])): sweeps then read the right-hand
+// side, 1/diag and x of consecutive rows without an index list.
 int build_case(cfdg_grid* G, CaseState& cs) {
   const Hierarchy& H = *G->host_mg;
   HostGrid& h = G->h;
@@ -1422,10 +1551,60 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     F.goff = o;
     F.gmem = m;
   }
+  // Coarse levels 1 .. L-1: colouring (bin parity, else greedy; l1-Jacobi when more than
+  // 8 colours), then every level renumbered colour by colour.
+  CCase& C = cs.C;
+  C.nl = (int)H.levels.size() - 1;
+  if (C.nl < 1 || C.nl > MAXL) return fail(CFDG_ERR_UNSUPPORTED, "mixed form: unsupported hierarchy depth");
+  std::vector<std::vector<int32_t>> perm(C.nl + 2), lcoff(C.nl + 1);
+  std::vector<int> lcolors(C.nl + 1, 1), ljacobi(C.nl + 1, 0);
+  for (int l = 1; l <= C.nl; ++l) {
+    const MgLevel& M = H.levels[l];
+    const bool terminal = l == C.nl;
+    std::vector<int32_t> rows;
+    int nco = 1;
+    if (terminal) {
+      lcoff[l] = {0, M.n};
+      rows.resize(M.n);
+      for (int i = 0; i < M.n; ++i) rows[i] = i;
+    } else {
+      if (!parity_colors(M.a, M.parity, M.n, lcoff[l], rows, nco)) greedy_colors(M.a, M.n, lcoff[l], rows, nco);
+      if (nco > 8) {
+        ljacobi[l] = 1;
+        nco = 1;
+        lcoff[l] = {0, M.n};
+        for (int i = 0; i < M.n; ++i) rows[i] = i;
+      }
+    }
+    lcolors[l] = nco;
+    perm[l].assign(M.n, 0);
+    for (int k = 0; k < M.n; ++k) perm[l][rows[k]] = k;
+  }
+  std::vector<MgLevel> PL(C.nl + 1);
+  for (int l = 1; l <= C.nl; ++l) {
+    const MgLevel& M = H.levels[l];
+    MgLevel& Q = PL[l];
+    const std::vector<int32_t>& P = perm[l];
+    const std::vector<int32_t> none;
+    Q.n = M.n;
+    Q.a = permute_csr(M.a, P, P);
+    Q.diag.assign(M.n, 0.0);
+    for (int i = 0; i < M.n; ++i) Q.diag[P[i]] = M.diag[i];
+    Q.groups = permute_csr(M.groups, none, P);
+    Q.direct_idx = permute_csr(M.direct_idx, none, P);
+    Q.direct_off = M.direct_off;
+    Q.direct_factor = M.direct_factor;
+    if (l < C.nl) {
+      Q.restrict = permute_csr(M.restrict, perm[l + 1], P);
+      Q.prolong = permute_csr(M.prolong, P, perm[l + 1]);
+    }
+  }
   {
-    // Restriction gathers level-0 slots; the prolongation's rows follow the slots.
-    std::vector<int32_t> child(M0.restrict.col.size());
-    for (size_t q = 0; q < child.size(); ++q) child[q] = slot[M0.restrict.col[q]];
+    // Restriction gathers level-0 slots; the prolongation's rows follow the slots; level
+    // 1 in its colour-by-colour numbering.
+    const Csr R0 = permute_csr(M0.restrict, perm[1], {});
+    std::vector<int32_t> child(R0.col.size());
+    for (size_t q = 0; q < child.size(); ++q) child[q] = slot[R0.col[q]];
     std::vector<int32_t> poff(F.N2 + 1, 0), pcol;
     std::vector<float> pw32;
     pcol.reserve(M0.prolong.col.size());
@@ -1434,28 +1613,24 @@ int build_case(cfdg_grid* G, CaseState& cs) {
       const int c = cell_of[sl];
       if (c >= 0)
         for (int q = M0.prolong.off[c]; q < M0.prolong.off[c + 1]; ++q) {
-          pcol.push_back(M0.prolong.col[q]);
+          pcol.push_back(perm[1][M0.prolong.col[q]]);
           pw32.push_back((float)M0.prolong.val[q]);
         }
       poff[sl + 1] = (int32_t)pcol.size();
     }
     int *o, *c, *po, *pc;
     float *w, *pw;
-    if (int e = A.upload(&o, M0.restrict.off, s)) return e;
+    if (int e = A.upload(&o, R0.off, s)) return e;
     if (int e = A.upload(&c, child, s)) return e;
-    if (int e = A.upload(&w, to_f32(M0.restrict.val), s)) return e;
+    if (int e = A.upload(&w, to_f32(R0.val), s)) return e;
     if (int e = A.upload(&po, poff, s)) return e;
     if (int e = A.upload(&pc, pcol, s)) return e;
     if (int e = A.upload(&pw, pw32, s)) return e;
     F.r_off = o, F.r_child = c, F.r_w = w, F.p_off = po, F.p_col = pc, F.p_w = pw;
   }
-  // Coarse levels 1 .. L-1.
-  CCase& C = cs.C;
-  C.nl = (int)H.levels.size() - 1;
-  if (C.nl < 1 || C.nl > MAXL) return fail(CFDG_ERR_UNSUPPORTED, "mixed form: unsupported hierarchy depth");
   int maxg = 1;
   for (int l = 1; l <= C.nl; ++l) {
-    const MgLevel& M = H.levels[l];
+    const MgLevel& M = PL[l];
     CLev& L = C.lv[l - 1];
     L.n = M.n;
     L.terminal = l == C.nl;
@@ -1468,16 +1643,13 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     if (int e = A.upload(&v, to_f32(M.a.val), s)) return e;
     if (int e = A.upload(&d, to_f32(M.diag), s)) return e;
     L.off = o, L.col = c, L.val = v, L.diag = d;
-    std::vector<int32_t> coff, rows;
-    if (!parity_colors(M.a, M.parity, M.n, coff, rows, L.ncolors)) greedy_colors(M.a, M.n, coff, rows, L.ncolors);
+    std::vector<int32_t> coff = lcoff[l], rows(M.n);
+    for (int i = 0; i < M.n; ++i) rows[i] = i;  // colour c owns rows coff[c] .. coff[c+1]-1
+    L.ncolors = lcolors[l];
     // A level whose graph needs many colours (the wide stencils of linear-interpolation
     // coarse operators) is smoothed by l1-Jacobi instead: one phase per sweep.
-    L.jacobi = !L.terminal && L.ncolors > 8 ? 1 : 0;
+    L.jacobi = ljacobi[l];
     if (L.jacobi) {
-      L.ncolors = 1;
-      coff = {0, M.n};
-      rows.resize(M.n);
-      for (int i = 0; i < M.n; ++i) rows[i] = i;
       std::vector<float> il1(M.n, 0.0f);
       for (int i = 0; i < M.n; ++i) {
         double sum = std::fabs(M.diag[i]);
@@ -1491,10 +1663,9 @@ int build_case(cfdg_grid* G, CaseState& cs) {
       L.x2 = x2;
     }
     cs.colors.push_back(coff);
-    int *co, *cr;
+    int* co;
     if (int e = A.upload(&co, coff, s)) return e;
-    if (int e = A.upload(&cr, rows, s)) return e;
-    L.coff = co, L.crows = cr;
+    L.coff = co;
     {
       // Column-major ELL per colour: entry a of the colour's t-th row at base + a*nrow + t.
       std::vector<int32_t> eoff(L.ncolors), ew(L.ncolors), ecol;
@@ -1612,7 +1783,28 @@ using namespace cfdg::mx;
 struct WorkLists {
   int2 *tiles = nullptr, *tiles1 = nullptr, *ftiles = nullptr, *gtab = nullptr;
   int* counts = nullptr;  // [4]
+  int* pos = nullptr;     // [4][cases]: where a case's items start in each list, -1 when absent
 };
+
+// Builds work-lists on the device from the case-contiguous master lists: item e of case
+// c goes to pos[k][c] + (e - moff[k][c]) when the case is in the list.
+struct ListBuild {
+  const int2* m[4];
+  int2* out[4];
+  int total[4];
+  const int* moff;  // [4][nc+1]
+  const int* pos;   // [4][nc]
+  int nc;
+};
+__global__ void k_build_lists(ListBuild L) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int k = 0; k < 4; ++k)
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < L.total[k]; e += stride) {
+      const int2 t = L.m[k][e];
+      const int p = L.pos[k * L.nc + t.x];
+      if (p >= 0) L.out[k][p + e - L.moff[k * (L.nc + 1) + t.x]] = t;
+    }
+}
 
 // A set of grids solved together in the mixed form.
 struct cfdg_batch {
@@ -1644,36 +1836,121 @@ struct cfdg_batch {
   cudaGraphExec_t chunk = nullptr;
   size_t chunk_nodes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // V-cycle sweeps before and after the coarse correction on level 0 and on the coarse
+  // levels (from the grids' settings), and iterations per graph chunk.
+  int nu0 = 2, nuc = 2, chunk_it = CHUNK_IT;
+  // Device copies of the master lists and their per-case offsets [4][nc+1].
+  int2 *m_tiles = nullptr, *m_tiles1 = nullptr, *m_ftiles = nullptr, *m_gtab = nullptr;
+  int* d_moff = nullptr;
+  std::vector<int> moff;
+  // Pinned staging ring: host->device copies that return without waiting for the stream.
+  struct Stage {
+    void* h = nullptr;
+    size_t cap = 0;
+    cudaEvent_t ev = nullptr;
+    bool pending = false;
+  };
+  std::vector<Stage> ring = std::vector<Stage>(16);
+  size_t ring_next = 0;
   ~cfdg_batch() {
     if (chunk) cudaGraphExecDestroy(chunk);
     arena.release();
     if (h_st) cudaFreeHost(h_st);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    for (auto& r : ring) {
+      if (r.pending) cudaEventSynchronize(r.ev);
+      if (r.h) cudaFreeHost(r.h);
+      if (r.ev) cudaEventDestroy(r.ev);
+    }
     if (own) cudaStreamDestroy(own);
   }
 };
 
 namespace {
 
+// Persistent grids: every block resident at once (the SM count times the kernel's
+// occupancy), and no more blocks than work items.
+int resident_grid(const void* fn, int threads) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find({dev, fn});
+  if (it != cache.end()) return it->second;
+  int sms = 0, per = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0) != cudaSuccess || per < 1) {
+    cudaGetLastError();
+    per = 1;
+  }
+  return cache[{dev, fn}] = std::max(1, sms) * per;
+}
+template <class K>
+int grid_of(K kernel, int threads, int items) {
+  return std::max(1, std::min(items, resident_grid((const void*)kernel, threads)));
+}
+// Copies `bytes` from host memory to the device through a pinned staging slot, so the
+// call returns without waiting for the work queued on `s` (the slot is reused once the
+// copy that last used it has completed).
+int staged_h2d(cfdg_batch* B, void* d_dst, const void* h_src, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return 0;
+  cfdg_batch::Stage& st = B->ring[B->ring_next];
+  B->ring_next = (B->ring_next + 1) % B->ring.size();
+  if (st.pending) CU(cudaEventSynchronize(st.ev));
+  st.pending = false;
+  if (!st.ev) CU(cudaEventCreateWithFlags(&st.ev, cudaEventDisableTiming));
+  if (st.cap < bytes) {
+    if (st.h) CU(cudaFreeHost(st.h));
+    st.h = nullptr;
+    st.cap = 0;
+    CU(cudaMallocHost(&st.h, bytes));
+    st.cap = bytes;
+  }
+  std::memcpy(st.h, h_src, bytes);
+  CU(cudaMemcpyAsync(d_dst, st.h, bytes, cudaMemcpyHostToDevice, s));
+  CU(cudaEventRecord(st.ev, s));
+  st.pending = true;
+  return 0;
+}
+
+// Points work-list W at the cases marked in `on`: the host computes where each case's
+// items go, one kernel gathers them from the master lists (no host pass over the items,
+// no wait for the stream).
 int fill_lists(cfdg_batch* B, WorkLists& W, const std::vector<char>& on, cudaStream_t s) {
-  static thread_local std::vector<int2> a, b, c, d;
-  a.clear(), b.clear(), c.clear(), d.clear();
-  for (auto& t : B->tiles)
-    if (on[t.x]) a.push_back(t);
-  for (auto& t : B->tiles1)
-    if (on[t.x]) b.push_back(t);
-  for (auto& t : B->ftiles)
-    if (on[t.x]) c.push_back(t);
-  for (auto& t : B->gtab)
-    if (on[t.x]) d.push_back(t);
-  int counts[4] = {(int)a.size(), (int)b.size(), (int)c.size(), (int)d.size()};
-  if (!a.empty()) CU(cudaMemcpyAsync(W.tiles, a.data(), a.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
-  if (!b.empty()) CU(cudaMemcpyAsync(W.tiles1, b.data(), b.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
-  if (!c.empty()) CU(cudaMemcpyAsync(W.ftiles, c.data(), c.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
-  if (!d.empty()) CU(cudaMemcpyAsync(W.gtab, d.data(), d.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
-  CU(cudaMemcpyAsync(W.counts, counts, sizeof(counts), cudaMemcpyHostToDevice, s));
-  CU(cudaStreamSynchronize(s));  // the staging vectors are reused
+  const int nc = (int)B->cases.size();
+  static thread_local std::vector<int> pos;
+  pos.assign(4 * nc + 4, -1);
+  int counts[4] = {0, 0, 0, 0};
+  for (int k = 0; k < 4; ++k)
+    for (int c = 0; c < nc; ++c) {
+      if (!on[c]) continue;
+      const int n = B->moff[k * (nc + 1) + c + 1] - B->moff[k * (nc + 1) + c];
+      pos[k * nc + c] = counts[k];
+      counts[k] += n;
+    }
+  for (int k = 0; k < 4; ++k) pos[4 * nc + k] = counts[k];
+  if (int e = staged_h2d(B, W.pos, pos.data(), sizeof(int) * 4 * nc, s)) return e;
+  if (int e = staged_h2d(B, W.counts, pos.data() + 4 * nc, sizeof(int) * 4, s)) return e;
+  ListBuild L;
+  const int2* m[4] = {B->m_tiles, B->m_tiles1, B->m_ftiles, B->m_gtab};
+  int2* out[4] = {W.tiles, W.tiles1, W.ftiles, W.gtab};
+  int most = 0;
+  for (int k = 0; k < 4; ++k) {
+    L.m[k] = m[k];
+    L.out[k] = out[k];
+    L.total[k] = B->moff[k * (nc + 1) + nc];
+    most = std::max(most, L.total[k]);
+  }
+  L.moff = B->d_moff;
+  L.pos = W.pos;
+  L.nc = nc;
+  if (most > 0) {
+    k_build_lists<<<grid_of(k_build_lists, 256, (most + 255) / 256), 256, 0, s>>>(L);
+    count();
+  }
+  CU(cudaGetLastError());
   return 0;
 }
 
@@ -1691,6 +1968,7 @@ int fill_tab(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
   auto r8 = [](int v) { return (v + 7) & ~7; };
   T.nc = nc;
   T.nlev = 0;
+  T.nu = B->nuc;
   for (int l = 0; l < nlev; ++l) {
     int maxc = 0, anyg = 0;
     auto lev = [&](int i) -> const CLev* {
@@ -1736,10 +2014,8 @@ int fill_tab(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
   T.res = T.grp + nlev * w;
   T.fwd = T.res + nlev * w;
   T.bwd = T.fwd + (size_t)nlev * MAXC * w;
-  CU(cudaMemcpyAsync(B->tab_buf, buf.data(), words * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-  CU(cudaMemcpyAsync(B->d_tab, &T, sizeof(CoarseTab), cudaMemcpyHostToDevice, s));
-  CU(cudaStreamSynchronize(s));
-  return 0;
+  if (int e = staged_h2d(B, B->tab_buf, buf.data(), words * sizeof(int32_t), s)) return e;
+  return staged_h2d(B, B->d_tab, &T, sizeof(CoarseTab), s);
 }
 
 // The graph's lists and tables cover the cases marked in B->active.
@@ -1774,31 +2050,9 @@ void launch_coarse(cfdg_batch* B, cudaStream_t s) {
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k_coarse, (const CCase*)B->d_cc, (const MState*)B->d_st);
+  cudaLaunchKernelEx(&cfg, k_coarse, (const CCase*)B->d_cc, (const MState*)B->d_st, B->nuc);
 }
 
-// Persistent grids: every block resident at once (the SM count times the kernel's
-// occupancy), and no more blocks than work items.
-int resident_grid(const void* fn, int threads) {
-  static std::mutex mu;
-  static std::map<std::pair<int, const void*>, int> cache;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  std::lock_guard<std::mutex> lk(mu);
-  auto it = cache.find({dev, fn});
-  if (it != cache.end()) return it->second;
-  int sms = 0, per = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0) != cudaSuccess || per < 1) {
-    cudaGetLastError();
-    per = 1;
-  }
-  return cache[{dev, fn}] = std::max(1, sms) * per;
-}
-template <class K>
-int grid_of(K kernel, int threads, int items) {
-  return std::max(1, std::min(items, resident_grid((const void*)kernel, threads)));
-}
 #define FINE(K, W, ...) \
   K<<<grid_of(K, TILE, B->g_fine), TILE, 0, s>>>(B->d_fc, B->d_st, (W).tiles, (W).counts, ##__VA_ARGS__)
 
@@ -1808,22 +2062,22 @@ void enqueue_vcycle(cfdg_batch* B, cudaStream_t s) {
     FINE(k_v_rhs, W);
     k_center0<<<grid_of(k_center0, 256, B->g_g), 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 0);
   }
-  // Two forward sweeps: red, black, red, black (the first red starts from x = 0).
-  FINE(k_rb, W, 0, 1);
-  FINE(k_rb, W, 1, 0);
-  FINE(k_rb, W, 0, 0);
-  FINE(k_rb, W, 1, 0);
+  // nu0 forward sweeps: red, black, red, black, ... (the first red starts from x = 0).
+  for (int sw = 0; sw < B->nu0; ++sw) {
+    FINE(k_rb, W, 0, sw == 0 ? 1 : 0);
+    FINE(k_rb, W, 1, 0);
+  }
   if (B->any_groups) k_center0<<<grid_of(k_center0, 256, B->g_g), 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 1);
   FINE(k_v_resid, W);
   if (B->any_groups) k_center0<<<grid_of(k_center0, 256, B->g_g), 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 2);
   k_v_restrict<<<grid_of(k_v_restrict, TILE, B->g_1), TILE, 0, s>>>(B->d_fc, B->d_st, W.tiles1, W.counts + 1);
   launch_coarse(B, s);
   FINE(k_v_prolong, W);
-  // Two backward sweeps: black, red, black, red.
-  FINE(k_rb, W, 1, 0);
-  FINE(k_rb, W, 0, 0);
-  FINE(k_rb, W, 1, 0);
-  FINE(k_rb, W, 0, 0);
+  // nu0 backward sweeps: black, red, ...
+  for (int sw = 0; sw < B->nu0; ++sw) {
+    FINE(k_rb, W, 1, 0);
+    FINE(k_rb, W, 0, 0);
+  }
   if (B->any_groups) k_center0<<<grid_of(k_center0, 256, B->g_g), 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 1);
 }
 
@@ -1846,7 +2100,7 @@ int ensure_graph(cfdg_batch* B) {
   if (B->chunk) return 0;
   cudaGraph_t g;
   CU(cudaStreamBeginCapture(B->own, cudaStreamCaptureModeThreadLocal));
-  for (int i = 0; i < CHUNK_IT; ++i) enqueue_iteration(B, B->own);
+  for (int i = 0; i < B->chunk_it; ++i) enqueue_iteration(B, B->own);
   cudaError_t e = cudaStreamEndCapture(B->own, &g);
   if (e != cudaSuccess) return fail(CFDG_ERR_CUDA, std::string("mixed capture: ") + cudaGetErrorString(e));
   cudaGraphGetNodes(g, nullptr, &B->chunk_nodes);
@@ -1890,7 +2144,9 @@ int prologue(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
   if (int e = fill_lists(B, B->pro, on, s)) return e;
   FINE(k_rhs, B->pro);
   count();
-  CU(cudaStreamSynchronize(s));
+  bool groups = false;
+  for (size_t i = 0; i < B->cases.size(); ++i) groups |= on[i] && B->grids[i]->ncomp_groups > 0;
+  if (groups) CU(cudaStreamSynchronize(s));  // the compatibility check (E031) is decided on the host
   for (size_t i = 0; i < B->cases.size(); ++i) {
     if (!on[i]) continue;
     cfdg_grid* G = B->grids[i];
@@ -1977,6 +2233,22 @@ int cfdg_mixed_pack(cfdg_batch* B) {
     if (int e = A.alloc(&W->ftiles, B->ftiles.size())) return e;
     if (int e = A.alloc(&W->gtab, B->gtab.size())) return e;
     if (int e = A.alloc(&W->counts, 4)) return e;
+    if (int e = A.alloc(&W->pos, 4 * (size_t)nc)) return e;
+  }
+  // Master lists (case-contiguous) on the device and the offset of each case's items.
+  B->moff.assign(4 * (nc + 1), 0);
+  {
+    const std::vector<int2>* lists[4] = {&B->tiles, &B->tiles1, &B->ftiles, &B->gtab};
+    for (int k = 0; k < 4; ++k) {
+      int* o = B->moff.data() + k * (nc + 1);
+      for (const int2& t : *lists[k]) o[t.x + 1] += 1;
+      for (int c = 0; c < nc; ++c) o[c + 1] += o[c];
+    }
+    if (int e = A.upload(&B->m_tiles, B->tiles, s)) return e;
+    if (int e = A.upload(&B->m_tiles1, B->tiles1, s)) return e;
+    if (int e = A.upload(&B->m_ftiles, B->ftiles, s)) return e;
+    if (int e = A.upload(&B->m_gtab, B->gtab, s)) return e;
+    if (int e = A.upload(&B->d_moff, B->moff, s)) return e;
   }
   auto clamp = [](size_t n) { return (int)std::max<size_t>(1, std::min<size_t>(n, 1 << 30)); };
   B->g_fine = clamp(B->tiles.size());
@@ -2007,7 +2279,7 @@ int cfdg_mixed_pack(cfdg_batch* B) {
       cudaGetLastError();
       B->coop = false;
     }
-    B->coop_blocks = sms * std::max(1, std::min(per, 2));
+    B->coop_blocks = sms * std::max(1, std::min(per, 4));
   }
   if (!B->coop) {
     // One cluster per case: 16 CTAs when that non-portable size is allowed, else 8.
@@ -2024,6 +2296,12 @@ int cfdg_mixed_pack(cfdg_batch* B) {
 int cfdg_mixed_add_case(cfdg_batch* B, cfdg_grid* G) {
   std::shared_ptr<CaseState> cs;
   if (int e = case_of(G, cs)) return e;
+  if (B->grids.empty()) {
+    B->nu0 = G->mx_nu0;
+    B->nuc = G->mx_nuc;
+  } else if (B->nu0 != G->mx_nu0 || B->nuc != G->mx_nuc) {
+    return fail(CFDG_ERR_INVALID, "the grids of a batch must share their V-cycle sweep counts");
+  }
   B->grids.push_back(G);
   B->cases.push_back(cs);
   return 0;
@@ -2194,6 +2472,17 @@ struct cfdg_server {
   uint64_t next_ticket = 1;
   bool launched = false;
   std::mutex mu;
+  // Observability: graph chunks, their device time (events around each launch, read at
+  // the next progress), host time inside progress, cases finished and admitted.
+  cudaEvent_t ca = nullptr, cb = nullptr, epi = nullptr;
+  bool timing = false;
+  uint64_t chunks = 0, finished = 0, admitted = 0, rounds = 0;
+  double chunk_ms = 0.0, host_ms = 0.0;
+  ~cfdg_server() {
+    if (ca) cudaEventDestroy(ca);
+    if (cb) cudaEventDestroy(cb);
+    if (epi) cudaEventDestroy(epi);
+  }
 };
 
 extern "C" {
@@ -2381,6 +2670,12 @@ int cfdg_server_create(cfdg_context* ctx, cfdg_grid* const* grids, int32_t n, in
   auto* S = new cfdg_server();
   S->B = B;
   S->max_active = max_active;
+  if (cudaEventCreate(&S->ca) != cudaSuccess || cudaEventCreate(&S->cb) != cudaSuccess ||
+      cudaEventCreateWithFlags(&S->epi, cudaEventDisableTiming) != cudaSuccess) {
+    cfdg_batch_destroy(B);
+    delete S;
+    return fail(CFDG_ERR_CUDA, "could not create the server's events");
+  }
   S->running.assign(n, 0);
   B->active.assign(n, 0);
   {
@@ -2406,6 +2701,20 @@ int cfdg_server_set_stream(cfdg_server* S, void* stream) {
   return cfdg_batch_set_stream(S->B, stream);
 }
 
+int cfdg_server_set_chunk(cfdg_server* S, int32_t iterations) {
+  if (!S || iterations < 1 || iterations > 64) return fail(CFDG_ERR_INVALID, "chunk iterations must be 1..64");
+  std::lock_guard<std::mutex> lk(S->mu);
+  cfdg_batch* B = S->B;
+  CU(cudaSetDevice(B->ctx->device));
+  if (iterations == B->chunk_it) return 0;
+  CU(cudaStreamSynchronize(B->stream));
+  if (B->chunk) cudaGraphExecDestroy(B->chunk);
+  B->chunk = nullptr;
+  B->chunk_it = iterations;
+  Locks locks(B->grids);
+  return ensure_graph(B);
+}
+
 int cfdg_server_submit(cfdg_server* S, int32_t grid, double* d_u, double* d_p, double dt, double tol,
                        uint64_t max_iter, uint64_t* ticket) {
   if (!S || grid < 0 || grid >= (int)S->B->grids.size() || !d_u || !d_p || !ticket)
@@ -2425,9 +2734,23 @@ int cfdg_server_progress(cfdg_server* S, int32_t* finished) {
   cudaStream_t s = B->stream;
   const int nc = (int)B->cases.size();
   int nfin = 0;
+  const auto h0 = std::chrono::steady_clock::now();
+  struct HostClock {
+    cfdg_server* S;
+    std::chrono::steady_clock::time_point t0;
+    ~HostClock() {
+      S->host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+  } host_clock{S, h0};
+  ++S->rounds;
   // 1. Finish the cases that converged or failed in the last chunk.
   CU(cudaMemcpyAsync(B->h_st, B->d_st, sizeof(MState) * nc, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
+  if (S->timing) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, S->ca, S->cb) == cudaSuccess) S->chunk_ms += ms;
+    S->timing = false;
+  }
   std::vector<char> done(nc, 0), fin(nc, 0);
   bool changed = false;
   for (int i = 0; i < nc; ++i) {
@@ -2438,21 +2761,27 @@ int cfdg_server_progress(cfdg_server* S, int32_t* finished) {
       done[i] = st == DONE;
     }
   }
+  // The epilogue of the converged cases is queued first (it reads their descriptors
+  // before an admission below may point them at a new request); their results are
+  // published once it has run, after the next chunk is queued.
   bool any_done = false;
   for (int i = 0; i < nc; ++i) any_done |= done[i] != 0;
-  if (any_done)
+  if (any_done) {
     if (int e = epilogue(B, done, s)) return e;
-  if (any_done) CU(cudaStreamSynchronize(s));
+    CU(cudaEventRecord(S->epi, s));
+  }
+  std::vector<std::pair<uint64_t, cfdg_server::Done>> out;
   for (int i = 0; i < nc; ++i) {
     if (!fin[i]) continue;
     cfdg_server::Done d;
     fill_info(B->h_st[i], d.info);
     d.code = B->h_st[i].state == DONE ? 0 : (B->h_st[i].error ? B->h_st[i].error : CFDG_E033);
-    S->results[S->running[i]] = d;
+    out.push_back({S->running[i], d});
     S->running[i] = 0;
     B->active[i] = 0;
     changed = true;
     ++nfin;
+    ++S->finished;
   }
   // 2. Admit queued requests into free slots (in arrival order; one per grid at a time).
   int nactive = 0;
@@ -2468,10 +2797,9 @@ int cfdg_server_progress(cfdg_server* S, int32_t* finished) {
     B->h_fc[i].u = it->u;
     B->h_fc[i].pfield = it->p;
     B->h_fc[i].dt = it->dt;
-    CU(cudaMemcpyAsync(&B->d_fc[i], &B->h_fc[i], sizeof(FineCase), cudaMemcpyHostToDevice, s));
-    MState m = initial_state(it->tol, it->max_iter);
-    CU(cudaMemcpyAsync(&B->d_st[i], &m, sizeof(MState), cudaMemcpyHostToDevice, s));
+    B->h_st[i] = initial_state(it->tol, it->max_iter);
     S->running[i] = it->ticket;
+    ++S->admitted;
     admit[i] = 1;
     any_admit = true;
     B->active[i] = 1;
@@ -2479,15 +2807,26 @@ int cfdg_server_progress(cfdg_server* S, int32_t* finished) {
     changed = true;
     it = S->queue.erase(it);
   }
-  if (any_admit)
+  if (any_admit) {
+    // Nothing has run since the states were read, so the other cases' device states
+    // equal h_st and whole-array copies are exact.
+    if (int e = staged_h2d(B, B->d_fc, B->h_fc.data(), sizeof(FineCase) * nc, s)) return e;
+    if (int e = staged_h2d(B, B->d_st, B->h_st, sizeof(MState) * nc, s)) return e;
     if (int e = prologue(B, admit, s)) return e;
+  }
   // 3. Point the work-lists at the active cases and run one chunk.
   if (changed)
     if (int e = set_active(B, s)) return e;
   if (nactive > 0) {
+    CU(cudaEventRecord(S->ca, s));
     CU(cudaGraphLaunch(B->chunk, s));
+    CU(cudaEventRecord(S->cb, s));
+    S->timing = true;
+    ++S->chunks;
     count(B->chunk_nodes);
   }
+  if (any_done) CU(cudaEventSynchronize(S->epi));
+  for (auto& r : out) S->results[r.first] = r.second;
   if (finished) *finished = nfin;
   return 0;
 }
@@ -2501,6 +2840,24 @@ int cfdg_server_result(cfdg_server* S, uint64_t ticket, cfdg_info* info, int32_t
   if (code) *code = it->second.code;
   S->results.erase(it);
   return 0;
+}
+
+int64_t cfdg_server_stats_json(cfdg_server* S, char* buf, int64_t cap) {
+  if (!S) return -(int64_t)fail(CFDG_ERR_INVALID, "null server");
+  std::lock_guard<std::mutex> lk(S->mu);
+  char tmp[512];
+  snprintf(tmp, sizeof tmp,
+           "{\"rounds\": %llu, \"chunks\": %llu, \"iterations_per_chunk\": %d, \"chunk_device_ms\": %.3f, "
+           "\"progress_host_ms\": %.3f, \"finished\": %llu, \"admitted\": %llu}",
+           (unsigned long long)S->rounds, (unsigned long long)S->chunks, S->B->chunk_it, S->chunk_ms, S->host_ms,
+           (unsigned long long)S->finished, (unsigned long long)S->admitted);
+  const std::string out = tmp;
+  if (buf && cap > 0) {
+    const size_t k = std::min((size_t)cap - 1, out.size());
+    memcpy(buf, out.data(), k);
+    buf[k] = 0;
+  }
+  return (int64_t)out.size() + 1;
 }
 
 int cfdg_server_pending(cfdg_server* S) {

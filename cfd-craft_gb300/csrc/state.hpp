@@ -182,6 +182,9 @@ struct cfdg_grid {
   // Face coefficients change only through cfdg_grid_update_faces, which bumps
   // faces_version; the hierarchy's signature is re-compared only after a change.
   uint64_t faces_version = 0;
+  // Mixed form: V-cycle sweeps before and after the coarse correction on level 0 and on
+  // the coarse levels (cfdg_grid_set_cycle); a batch takes them from its grids.
+  int mx_nu0 = 2, mx_nuc = 2;
   uint64_t sig_version = ~0ull;
 };
 

@@ -29,7 +29,7 @@ EXPORTS = (
     "cfdg_launch_count", "cfdg_debug_time_kernel", "cfdg_residual_norm_noalloc", "cfdg_batch_create",
     "cfdg_batch_destroy", "cfdg_batch_set_stream", "cfdg_batch_size", "cfdg_batch_project", "cfdg_batch_project_device",
     "cfdg_batch_time_kernel", "cfdg_batch_stats_json", "cfdg_server_create", "cfdg_server_destroy", "cfdg_server_set_stream",
-    "cfdg_server_submit", "cfdg_server_progress", "cfdg_server_result", "cfdg_server_pending",
+    "cfdg_server_submit", "cfdg_server_progress", "cfdg_server_result", "cfdg_server_pending", "cfdg_server_stats_json", "cfdg_server_set_chunk", "cfdg_grid_set_cycle",
 )
 
 
@@ -137,6 +137,10 @@ def load(path: str = LIB_PATH):
         L.cfdg_batch_size.argtypes = [P]
         L.cfdg_batch_stats_json.argtypes = [P, C.c_char_p, C.c_int64]
         L.cfdg_batch_stats_json.restype = C.c_int64
+        L.cfdg_server_stats_json.argtypes = [P, C.c_char_p, C.c_int64]
+        L.cfdg_server_stats_json.restype = C.c_int64
+        L.cfdg_server_set_chunk.argtypes = [P, C.c_int32]
+        L.cfdg_grid_set_cycle.argtypes = [P, C.c_int32, C.c_int32]
         PP = C.POINTER(C.c_void_p)
         L.cfdg_batch_project.argtypes = [P, PP, PP, C.POINTER(C.c_double), C.c_double, C.c_uint64, POLL, P,
                                          C.POINTER(Info), C.POINTER(C.c_int32)]

@@ -183,6 +183,10 @@ class DeviceGrid:
         d = None if distance is None else np.ascontiguousarray(distance, np.float64)
         self._check(self.L.cfdg_grid_update_faces(self.h, None if a is None else _vp(a), None if d is None else _vp(d)))
 
+    def set_cycle(self, nu_fine: int, nu_coarse: int):
+        """Mixed form: V-cycle sweeps on level 0 and on the coarse levels (cfdg_grid_set_cycle)."""
+        self._check(self.L.cfdg_grid_set_cycle(self.h, int(nu_fine), int(nu_coarse)))
+
     def device_bytes(self) -> int:
         return int(self.L.cfdg_grid_device_bytes(self.h))
 
@@ -423,6 +427,10 @@ class Server:
                                               float(dt), float(tol), int(max_iter), C.byref(t)))
         return t.value
 
+    def set_chunk(self, iterations: int):
+        """Iterations per graph chunk (cfdg_server_set_chunk)."""
+        self._check(self.L.cfdg_server_set_chunk(self.h, int(iterations)))
+
     def progress(self) -> int:
         n = C.c_int32()
         self._check(self.L.cfdg_server_progress(self.h, C.byref(n)))
@@ -440,3 +448,65 @@ class Server:
 
     def pending(self) -> int:
         return int(self.L.cfdg_server_pending(self.h))
+
+    def stats(self) -> dict:
+        """Rounds, chunks, chunk device ms, progress host ms, finished, admitted."""
+        import json
+
+        n = self.L.cfdg_server_stats_json(self.h, None, 0)
+        if n < 0:
+            raise PressureError(int(-n), E.last_error())
+        buf = C.create_string_buffer(int(n))
+        self.L.cfdg_server_stats_json(self.h, buf, int(n))
+        return json.loads(buf.value.decode())
+
+
+# Candidate (level-0 sweeps, coarse-level sweeps) pairs of the mixed form's V-cycle.
+CYCLE_CANDIDATES = ((1, 1), (1, 2), (1, 3), (1, 4), (2, 2), (2, 3))
+
+
+def autotune(device_grids, u_ptrs, p_ptrs, reset, dts, tol=1e-8, max_iter=10000, candidates=CYCLE_CANDIDATES,
+             stream_handle=None):
+    """Picks the mixed form's V-cycle sweep counts with the shortest time to `tol` on these
+    grids and applies them (cfdg_grid_set_cycle).
+
+    For each candidate a batch of all the grids projects the device velocities u_ptrs /
+    p_ptrs twice (the first call builds the batch's graph and is not timed); `reset()`
+    restores the inputs before every call. More sweeps make a cycle dearer and the
+    iteration count smaller; the optimum depends on the case mix (stencil anisotropy,
+    buildings, the share of wide-stencil coarse levels), which is why it is measured.
+    Returns {"choice": (nu_fine, nu_coarse), "ms": {...}, "iterations": {...}}."""
+    import time
+
+    timing, iters = {}, {}
+    for cand in candidates:
+        for d in device_grids:
+            d.set_cycle(*cand)
+        b = Batch(device_grids)
+        if stream_handle:
+            b.set_stream(stream_handle)
+        try:
+            best = None
+            for rep in range(2):
+                reset()
+                t0 = time.perf_counter()
+                res = b.project_device(u_ptrs, p_ptrs, dts, tol, max_iter)
+                dt_s = time.perf_counter() - t0
+                if any(code != 0 for code, _ in res):
+                    best = None
+                    break
+                if rep:
+                    best = dt_s
+                    iters[cand] = sum(i.iterations for _, i in res) / len(res)
+        finally:
+            b.close()
+        if best is not None:
+            timing[cand] = best
+    if not timing:
+        raise PressureError(E.CFDG_ERR_INVALID, "no candidate cycle converged")
+    choice = min(timing, key=timing.get)
+    for d in device_grids:
+        d.set_cycle(*choice)
+    reset()
+    return {"choice": list(choice), "ms": {f"{a},{b}": round(1e3 * t, 2) for (a, b), t in timing.items()},
+            "iterations": {f"{a},{b}": round(v, 2) for (a, b), v in iters.items()}}

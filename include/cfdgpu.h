@@ -139,6 +139,12 @@ int cfdg_grid_update_faces(cfdg_grid *grid, const double *face_area, const doubl
 
 /* Switches the preconditioner or the arithmetic form of an open grid. */
 int cfdg_grid_configure(cfdg_grid *grid, int32_t preconditioner, int32_t precision);
+/* Mixed form: Gauss-Seidel sweeps before and after the coarse correction of the V-cycle,
+ * on level 0 and on the coarse levels (1..4 each; default 2 and 2, the reference's
+ * V(2,2)). Batches and servers created afterwards take the counts from their grids (all
+ * grids of one batch must agree), so a grid gives the same result alone and in a batch.
+ * The bench's autotuner picks them per case mix. No reference counterpart. */
+int cfdg_grid_set_cycle(cfdg_grid *grid, int32_t nu_fine, int32_t nu_coarse);
 
 /* ------------------------------------------------------------------ the projection */
 
@@ -230,6 +236,9 @@ void cfdg_server_destroy(cfdg_server *server);
 int cfdg_server_set_stream(cfdg_server *server, void *stream);
 /* Queues pressure::project on grid `grid` for device arrays d_u (F doubles), d_p (N doubles),
  * which must stay valid until the ticket's result is read. */
+/* Iterations per graph chunk (1..64, default 8): requests join and leave the running set
+ * at chunk boundaries, so shorter chunks lower latency at more host rounds. */
+int cfdg_server_set_chunk(cfdg_server *server, int32_t iterations);
 int cfdg_server_submit(cfdg_server *server, int32_t grid, double *d_u, double *d_p, double dt, double tol,
                        uint64_t max_iter, uint64_t *ticket);
 int cfdg_server_progress(cfdg_server *server, int32_t *finished);
@@ -237,6 +246,12 @@ int cfdg_server_progress(cfdg_server *server, int32_t *finished);
 int cfdg_server_result(cfdg_server *server, uint64_t ticket, cfdg_info *info, int32_t *code);
 /* Requests queued or running. */
 int cfdg_server_pending(cfdg_server *server);
+/* Counters of the server since its creation, as JSON: progress rounds, graph chunks
+ * launched and their device time (CUDA events around each launch), host time spent in
+ * cfdg_server_progress (it includes waiting for the previous chunk), requests finished
+ * and admitted. Same buffer convention as cfdg_batch_stats_json. No reference
+ * counterpart. */
+int64_t cfdg_server_stats_json(cfdg_server *server, char *buf, int64_t cap);
 
 /* Device memory the grid holds, in bytes (admission accounting). */
 uint64_t cfdg_grid_device_bytes(const cfdg_grid *grid);

@@ -79,3 +79,76 @@ def test_server_results_equal_alone(pkg):
     server.close()
     for d in dgs:
         d.close()
+
+
+def test_cycle_settings_chunks_and_autotune(pkg):
+    """Sweep counts set on the grids apply alike to solo solves, batches and servers (same
+    bits), a server with a shorter chunk gives the same results, and the autotuner applies
+    its fastest candidate."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(9)
+    shapes = [(32, 32, 16), (48, 32, 16)]
+    cases = [pkg.synth.case(sh, 2.0, inflow=5.0, preconditioner="multigrid",
+                            boxes=pkg.synth.random_boxes(rng, 3, [v * 2.0 for v in sh], side=(6.0, 14.0),
+                                                         height=(6.0, 20.0), dx=2.0)) for sh in shapes]
+    grids = [pkg.grid.Grid.build(c) for c in cases]
+    us = [pkg.synth.random_velocity(g, 60 + i) for i, g in enumerate(grids)]
+    dev = torch.device("cuda", 0)
+    alone = []
+    for g, u in zip(grids, us):
+        dg = pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed")
+        dg.set_cycle(1, 3)
+        uu, pp = u.copy(), np.zeros(g.count)
+        info = dg.project(uu, pp, 0.1, 1e-8, 10000)
+        assert info.relative_residual <= 1e-8
+        alone.append((uu, pp, info.iterations))
+        dg.close()
+    dgs = [pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed") for g in grids]
+    for d in dgs:
+        d.set_cycle(1, 3)
+    batch = pkg.pressure.Batch(dgs)
+    bu, bp = [u.copy() for u in us], [np.zeros(g.count) for g in grids]
+    res = batch.project(bu, bp, [0.1, 0.1], 1e-8, 10000)
+    batch.close()
+    for i, (code, info) in enumerate(res):
+        assert code == 0 and info.iterations == alone[i][2]
+        assert np.array_equal(bits(bu[i]), bits(alone[i][0])) and np.array_equal(bits(bp[i]), bits(alone[i][1]))
+    server = pkg.pressure.Server(dgs, max_active=2)
+    server.set_chunk(3)
+    d_u = [torch.from_numpy(u).to(dev) for u in us]
+    d_p = [torch.zeros(g.count, dtype=torch.float64, device=dev) for g in grids]
+    torch.cuda.synchronize()
+    tickets = [server.submit(i, d_u[i].data_ptr(), d_p[i].data_ptr(), 0.1, 1e-8, 10000) for i in range(2)]
+    done = {}
+    for _ in range(100000):
+        server.progress()
+        for i, t in enumerate(tickets):
+            if i not in done:
+                r = server.result(t)
+                if r is not None:
+                    done[i] = r
+        if len(done) == 2:
+            break
+    assert len(done) == 2
+    st = server.stats()
+    assert st["iterations_per_chunk"] == 3 and st["finished"] == 2
+    for i in range(2):
+        assert done[i][0] == 0
+        assert np.array_equal(bits(d_u[i].cpu().numpy()), bits(alone[i][0]))
+        assert np.array_equal(bits(d_p[i].cpu().numpy()), bits(alone[i][1]))
+    server.close()
+    # Autotuning over two candidates picks the faster and sets it on the grids.
+    d_u0 = [u.clone() for u in d_u]
+
+    def reset():
+        for u, u0, p in zip(d_u, d_u0, d_p):
+            u.copy_(u0)
+            p.zero_()
+
+    out = pkg.pressure.autotune(dgs, [u.data_ptr() for u in d_u], [p.data_ptr() for p in d_p], reset, [0.1, 0.1],
+                                candidates=((2, 2), (1, 2)))
+    assert tuple(out["choice"]) in ((2, 2), (1, 2)) and len(out["ms"]) == 2
+    best = min(out["ms"], key=out["ms"].get)
+    assert best == "%d,%d" % tuple(out["choice"])
+    for d in dgs:
+        d.close()
