@@ -538,6 +538,13 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     solves = world * K * n
     value = solves / (total_ms / 1e3)
     cell_updates = sum(sv.cells[c] * i.iterations for c, i in infos)
+    if args.only_loop:  # profiling runs: the closed loop alone
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": K,
+                              "warmup": W, "ms_per_step": round(total_ms / K, 4), "only_loop": True,
+                              "gpu_launches": int(launches), "server_loop": loop}), flush=True)
+        sv.close()
+        return 0
     # Open loop at the stated arrival rate (skipped with --requests 0).
     serving = None
     if args.requests > 0:
@@ -645,6 +652,119 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     return 0
 
 
+UNEVEN_WORKLOAD = ("64 uneven cases: shapes uniform over 48^3, 64x64x32, 96x96x48, 128x128x64, 160x160x80 (seeds "
+                   "100-163), 0-20 seeded buildings, dx=2 m, inflow 5 m/s; each case's u* sequence as above; all 64 "
+                   "projected by one batched call per step (mixed FP32/FP64 multigrid PCG to 1e-8)")
+
+
+def run_uneven(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
+    """Survey configuration 4: 64 uneven cases in one batch (one graph-captured projection per step)."""
+    import numpy as np
+
+    K, W = args.steps, args.warmup
+    cases = pkg.synth.config4()
+    grids = [pkg.grid.Grid.build(c) for c in cases]
+    n = len(grids)
+    dgs = [pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed") for g in grids]
+    for d in dgs:
+        d.set_stream(stream.cuda_stream)
+    u0 = [pkg.synth.random_velocity(g, seed=8000 + 100 * rank + i) for i, g in enumerate(grids)]
+    d_u = [torch.from_numpy(u).to(dev) for u in u0]
+    d_p = [torch.zeros(g.count, dtype=torch.float64, device=dev) for g in grids]
+    free = [torch.from_numpy(((g.face_kind == pkg.grid.INTERIOR) | (g.face_kind == pkg.grid.OUTLET))
+                             .astype(np.float64)).to(dev) for g in grids]
+    gens = [torch.Generator(device=dev) for _ in grids]
+    for i, gn in enumerate(gens):
+        gn.manual_seed(9000 + 100 * rank + i)
+    tuned = None
+    if not args.no_autotune:
+        d_u0 = [u.clone() for u in d_u]
+
+        def reset():
+            for u, v, p in zip(d_u, d_u0, d_p):
+                u.copy_(v)
+                p.zero_()
+
+        t0 = time.perf_counter()
+        tuned = pkg.pressure.autotune(dgs, [u.data_ptr() for u in d_u], [p.data_ptr() for p in d_p], reset,
+                                      [DT] * n, TOL, MAX_IT, stream_handle=stream.cuda_stream)
+        tuned["seconds"] = round(time.perf_counter() - t0, 2)
+        del d_u0
+    batch = pkg.pressure.Batch(dgs)
+    batch.set_stream(stream.cuda_stream)
+
+    def step():
+        for i in range(n):
+            noise = torch.rand(d_u[i].numel(), dtype=torch.float64, device=dev, generator=gens[i])
+            d_u[i].add_(noise.mul_(0.1).sub_(0.05).mul_(free[i]))
+        res = batch.project_device([u.data_ptr() for u in d_u], [p.data_ptr() for p in d_p], [DT] * n, TOL, MAX_IT)
+        assert all(c == 0 for c, _ in res), [c for c, _ in res]
+        return [i for _, i in res]
+
+    for _ in range(W):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches0 = L.cfdg_launch_count()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    infos = []
+    ev0.record(stream)
+    for _ in range(K):
+        infos.extend(step())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = L.cfdg_launch_count() - launches0
+    total_ms = ev0.elapsed_time(ev1)
+    if dist:
+        total_ms = max_over_ranks(total_ms, dist, dev)
+    value = world * K * n / (total_ms / 1e3)
+    # End to end: the same batch on pinned host buffers, H2D and D2H inside the timed region.
+    host_u = [torch.from_numpy(u).pin_memory() for u in u0]
+    work_u = [torch.empty_like(h).pin_memory() for h in host_u]
+    work_p = [torch.zeros(g.count, dtype=torch.float64).pin_memory() for g in grids]
+    e2e_ms = 0.0
+    e2e_steps = 2
+    for s_ in range(e2e_steps):
+        for w, h, p in zip(work_u, host_u, work_p):
+            w.copy_(h)
+            p.zero_()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for code, _ in batch.project([w.numpy() for w in work_u], [p.numpy() for p in work_p], [DT] * n, TOL, MAX_IT):
+            assert code == 0
+        b.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms += a.elapsed_time(b)
+    io = sum(8 * (g.n_faces + g.count) for g in grids)
+    batch.close()
+    if rank == 0:
+        shapes = {}
+        for g in grids:
+            shapes[str(tuple(g.n))] = shapes.get(str(tuple(g.n)), 0) + 1
+        its = [i.iterations for i in infos]
+        line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+                "ms_per_step": round(total_ms / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32+f64", "data": "synthetic",
+                "config": {"workload": UNEVEN_WORKLOAD, "form": "batched mixed, one call per step", "cases": n,
+                           "shapes": shapes, "cells_per_step": sum(g.count for g in grids),
+                           "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
+                "iterations_mean": round(statistics.mean(its), 2), "iterations_max": max(its),
+                "e2e": {"value": round(world * e2e_steps * n / (e2e_ms / 1e3), 4), "unit": UNIT,
+                        "h2d_bytes_per_step": io, "d2h_bytes_per_step": io},
+                "autotune": tuned, "gpu_launches": int(launches), "clocks": clk}
+        print(json.dumps(line), flush=True)
+    for d in dgs:
+        d.close()
+    return 0
+
+
 def run_engine(args):
     import torch
 
@@ -669,8 +789,9 @@ def run_engine(args):
     flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MiB > L2 (129 MB)
     K, W = args.steps, args.warmup
     L = pkg.engine.load()
-    if args.form == "serving":
-        rc = run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L)
+    if args.form in ("serving", "uneven"):
+        run = run_serving if args.form == "serving" else run_uneven
+        rc = run(args, pkg, torch, dev, stream, flush, rank, world, dist, L)
         if dist:
             dist.destroy_process_group()
         return rc
@@ -771,12 +892,13 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--form", default="serving", choices=["plain", "mixed", "batched", "serving"])
+    ap.add_argument("--form", default="serving", choices=["plain", "mixed", "batched", "serving", "uneven"])
     ap.add_argument("--slots", type=int, default=0, help="serving: cases on the GPU at once (0: all)")
     ap.add_argument("--requests", type=int, default=520, help="serving: open-loop requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")
     ap.add_argument("--chunk", type=int, default=0, help="serving: iterations per graph chunk (0: the engine's)")
     ap.add_argument("--no-autotune", action="store_true", help="serving: keep the default V(2,2) sweeps")
+    ap.add_argument("--only-loop", action="store_true", help="serving: the closed loop only (for launch lists)")
     ap.add_argument("--cases", type=int, default=8, help="cases per step of the batched form")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

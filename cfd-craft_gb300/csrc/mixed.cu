@@ -95,6 +95,7 @@ struct FineCase {
   const float* r_w;
   const int *p_off, *p_col;    // level-0 rows (full layout) from level-1
   const float* p_w;
+  const int* pinj;             // injection prolongation (aggregation): level-1 parent per slot, -1 none
   float *rhs1, *x1;
   // projection I/O for this solve
   double* u;
@@ -198,17 +199,22 @@ __device__ __forceinline__ void close_seg(const FineCase* FC, MState* ST, Seg& g
 
 // Persistent fine-level kernels: block b takes the contiguous tile range
 // [b*per, (b+1)*per) of the work-list (neighbouring rows stay in one block's cache).
+// A tile whose case is not in the kernel's state: skip the rest of that case's tiles in
+// this block's range (a case's tiles are consecutive in every list, in tile order), so
+// idle cases cost one state read per block instead of one per tile.
+#define SKIP_CASE(T_, TEST_)                \
+  {                                         \
+    const MState& S_ = ST[(T_).x];          \
+    if (!(TEST_)) {                         \
+      ti += FC[(T_).x].ntiles - 1 - (T_).y; \
+      continue;                             \
+    }                                       \
+  }
+
 #define TILE_RANGE                                   \
   const int n_ = *count;                             \
   const int per_ = (n_ + gridDim.x - 1) / gridDim.x; \
   const int t0_ = blockIdx.x * per_, t1_ = min(n_, t0_ + per_);
-
-__device__ __forceinline__ void coords(const FineCase& F, int c, int& i, int& j, int& k) {
-  i = c % F.n[0];
-  int t = c / F.n[0];
-  j = t % F.n[1];
-  k = t / F.n[1];
-}
 
 __device__ __forceinline__ long long fidx(const FineCase& F, int a, int i, int j, int k) {
   return F.face_off[a] + ((long long)k * F.fdim[a][1] + j) * F.fdim[a][0] + i;
@@ -216,10 +222,10 @@ __device__ __forceinline__ long long fidx(const FineCase& F, int a, int i, int j
 
 // FP64 operator with every product and sum rounded as written, in the reference's
 // face order (non-periodic grid): bit-identical to pressure::apply.
-__device__ __forceinline__ double op64(const FineCase& F, const double* __restrict__ x, int c, unsigned fl) {
+__device__ __forceinline__ double op64r(const FineCase& F, const double* __restrict__ x, int c, int i, int j, int k,
+                                        unsigned fl) {
   if (!(fl & 0x0fffu)) return 0.0;
-  int q[3];
-  coords(F, c, q[0], q[1], q[2]);
+  const int q[3] = {i, j, k};
   const int stride[3] = {1, F.n[0], F.n[0] * F.n[1]};
   const double xc = x[c];
   double y = 0.0;
@@ -479,6 +485,7 @@ __global__ void __launch_bounds__(TILE) k_op(const FineCase* FC, MState* ST, con
   Seg g;
   for (int ti = t0_; ti < t1_; ++ti) {
     const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == RUN)
     if (t.x != g.ci) {
       close_seg(FC, ST, g, sh, FinOp());
       g.ci = t.x;
@@ -518,6 +525,7 @@ __global__ void __launch_bounds__(TILE) k_update(const FineCase* FC, MState* ST,
   Seg g;
   for (int ti = t0_; ti < t1_; ++ti) {
     const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == RUN)
     if (t.x != g.ci) {
       close_seg(FC, ST, g, sh, FinUpdate());
       g.ci = t.x;
@@ -541,7 +549,11 @@ __device__ __forceinline__ void b_outer(const FineCase* FC, MState* ST, const in
 __global__ void __launch_bounds__(TILE) k_outer(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = t0_; ti < t1_; ++ti) b_outer(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == OUTER)
+    b_outer(FC, ST, t, cached_);
+  }
 }
 
 struct FinOuterResid {
@@ -566,10 +578,20 @@ __device__ __forceinline__ void b_outer_resid(const FineCase* FC, MState* ST, co
                                     int& seg_n) {
   FINE_PROLOGUE(S.state == OUTER)
   double acc = 0.0;
-  for (int c = cb + threadIdx.x; c < ce; c += TILE) {
-    const double v = __dsub_rn(F.bc[c], op64(F, F.x64, c, F.flags[c]));
-    F.r64[c] = v;
-    acc = __fma_rn(v, v, acc);
+  int j, k, rb;
+  if (warp_row(F, lt, warp, j, k, rb)) {
+    // One warp per row, several cells per lane: the cells' FP64 chains are independent.
+    const double* __restrict__ x = F.x64;
+    const double* __restrict__ bc = F.bc;
+    const uint16_t* __restrict__ fl = F.flags;
+    double* __restrict__ r = F.r64;
+#pragma unroll 4
+    for (int i = lane; i < nx_; i += 32) {
+      const int c = rb + i;
+      const double v = __dsub_rn(bc[c], op64r(F, x, c, i, j, k, fl[c]));
+      r[c] = v;
+      acc = __fma_rn(v, v, acc);
+    }
   }
   tile_partial(acc, F, lt, sh, seg_n);
 }
@@ -580,6 +602,7 @@ __global__ void __launch_bounds__(TILE) k_outer_resid(const FineCase* FC, MState
   Seg g;
   for (int ti = t0_; ti < t1_; ++ti) {
     const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == OUTER)
     if (t.x != g.ci) {
       close_seg(FC, ST, g, sh, FinOuterResid());
       g.ci = t.x;
@@ -602,7 +625,11 @@ __device__ __forceinline__ void b_scale(const FineCase* FC, MState* ST, const in
 __global__ void __launch_bounds__(TILE) k_scale(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = t0_; ti < t1_; ++ti) b_scale(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == SCALE)
+    b_scale(FC, ST, t, cached_);
+  }
 }
 
 __global__ void k_start_state(MState* ST, int n) {
@@ -640,6 +667,7 @@ __global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, con
   Seg g;
   for (int ti = t0_; ti < t1_; ++ti) {
     const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == RUN || S_.state == START)
     if (t.x != g.ci) {
       close_seg(FC, ST, g, sh, FinRz());
       g.ci = t.x;
@@ -662,7 +690,11 @@ __device__ __forceinline__ void b_p(const FineCase* FC, MState* ST, const int2 t
 __global__ void __launch_bounds__(TILE) k_p(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = t0_; ti < t1_; ++ti) b_p(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == RUN)
+    b_p(FC, ST, t, cached_);
+  }
 }
 
 // ----------------------------------------------------------------- V-cycle, level 0
@@ -675,7 +707,11 @@ __device__ __forceinline__ void b_v_rhs(const FineCase* FC, MState* ST, const in
 __global__ void __launch_bounds__(TILE) k_v_rhs(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = t0_; ti < t1_; ++ti) b_v_rhs(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == RUN || S_.state == START)
+    b_v_rhs(FC, ST, t, cached_);
+  }
 }
 
 // Red-black Gauss-Seidel half sweep on level 0: cells with (i+j+k)%2 == color, the
@@ -733,7 +769,11 @@ __device__ __forceinline__ void b_rb(const FineCase* FC, MState* ST, const int2 
 __global__ void __launch_bounds__(TILE) k_rb(const FineCase* FC, MState* ST, const int2* tiles, const int* count, int color, int first) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = t0_; ti < t1_; ++ti) b_rb(FC, ST, tiles[ti], cached_, color, first);
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == RUN || S_.state == START)
+    b_rb(FC, ST, t, cached_, color, first);
+  }
 }
 
 // res0 = rhs0 - A0 x0 (A0 = diag - sum w on interior faces).
@@ -792,7 +832,11 @@ __device__ __forceinline__ void b_v_resid(const FineCase* FC, MState* ST, const 
 __global__ void __launch_bounds__(TILE) k_v_resid(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = t0_; ti < t1_; ++ti) b_v_resid(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == RUN || S_.state == START)
+    b_v_resid(FC, ST, t, cached_);
+  }
 }
 
 // rhs1 = R res0: level-1 rows gather their level-0 children. Tiles index level-1 rows.
@@ -815,6 +859,13 @@ __global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState*
 // x0 += P x1 (the prolongation's rows are the split layout's slots; padding rows are empty).
 __device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
+  if (F.pinj) {  // x0 += x1[parent]: the same value as the weight-1 row below
+    for (int c = sb + threadIdx.x; c < se; c += TILE) {
+      const int q = F.pinj[c];
+      if (q >= 0) F.x0[c] += F.x1[q];
+    }
+    return;
+  }
   for (int c = sb + threadIdx.x; c < se; c += TILE) {
     const int b = F.p_off[c], e = F.p_off[c + 1];
     if (b == e) continue;
@@ -826,7 +877,11 @@ __device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, cons
 __global__ void __launch_bounds__(TILE) k_v_prolong(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = t0_; ti < t1_; ++ti) b_v_prolong(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == RUN || S_.state == START)
+    b_v_prolong(FC, ST, t, cached_);
+  }
 }
 
 // Gauge of level-0 closed groups: one block per (case, group); members strided.
@@ -994,10 +1049,12 @@ __global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState*
 // spreads the rows of all cases over the whole grid (a global index space of per-case
 // row ranges) and the phases are separated by grid-wide barriers.
 constexpr int MAXC = 32;  // colours per level
+constexpr long long BLK_WORK = 24576;  // rows + stencil entries a single block smooths (block-local levels)
 
 struct CoarseTab {
   int nc, nlev;
-  int nu, pad_;  // sweeps before and after the coarse correction
+  int nu;  // sweeps before and after the coarse correction
+  int lb;  // first level (lv index) that every case runs inside one block
   int maxc[MAXL];
   int anyg[MAXL];
   const int* rows;   // [nlev][nc+1] prefix over cases of the rows of level l
@@ -1145,7 +1202,156 @@ __device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, in
   }
 }
 
-__global__ void __launch_bounds__(512, 3) k_coarse_all(const CCase* cases, const MState* ST, const CoarseTab* Tp) {
+// ----------------------------------------------------------------- block-local coarse levels
+// The small coarse levels of one case, smoothed by one block with block barriers. Every
+// row sees the same operations in the same order as in the grid-wide phases, so a case
+// gives the same bits whichever levels run block-locally.
+__device__ void blk_center(const CLev& L, float* v, double* sh) {
+  __shared__ float mean;
+  for (int g = 0; g < L.ngroups; ++g) {
+    const int b = L.goff[g], e = L.goff[g + 1];
+    double acc = 0.0;
+    for (int k = b + threadIdx.x; k < e; k += blockDim.x) acc += __ldcg(&v[L.gmem[k]]);
+    const double s = bsum(acc, sh);
+    if (threadIdx.x == 0) mean = (float)(s / (double)(e - b));
+    __syncthreads();
+    const float m = mean;
+    for (int k = b + threadIdx.x; k < e; k += blockDim.x) v[L.gmem[k]] = __ldcg(&v[L.gmem[k]]) - m;
+    __syncthreads();
+  }
+}
+
+__device__ void blk_sweep(const CLev& L, bool backward, int pass, bool gs_on) {
+  if (L.jacobi) {
+    const float* xin = pass ? L.x2 : L.x;
+    float* xout = pass ? L.x : L.x2;
+    const int w = L.ell_w[0];
+    // Eight lanes per row, as in the grid-wide phase.
+    for (int k = threadIdx.x; k < 8 * L.n; k += blockDim.x) {
+      const int i = k >> 3, sub = k & 7;
+      float v = 0.0f;
+      for (int a = sub; a < w; a += 8) v = fmaf(L.ell_val[a * L.n + i], __ldcg(&xin[L.ell_col[a * L.n + i]]), v);
+      const unsigned mask = 0xffu << (threadIdx.x & 24);
+      v += __shfl_xor_sync(mask, v, 4, 8);
+      v += __shfl_xor_sync(mask, v, 2, 8);
+      v += __shfl_xor_sync(mask, v, 1, 8);
+      if (sub == 0) {
+        const float xi = __ldcg(&xin[i]);
+        xout[i] = fmaf(L.il1[i], __ldcg(&L.rhs[i]) - fmaf(L.diag[i], xi, v), xi);
+      }
+    }
+    __syncthreads();
+    return;
+  }
+  if (!gs_on) return;
+  for (int cc = 0; cc < L.ncolors; ++cc) {
+    const int color = backward ? L.ncolors - 1 - cc : cc;
+    const int c0 = L.coff[color], nrow = L.coff[color + 1] - c0;
+    const int base = L.ell_off[color], w = L.ell_w[color];
+    for (int k = threadIdx.x; k < nrow; k += blockDim.x) {
+      const int i = c0 + k;
+      float v = __ldcg(&L.rhs[i]);
+      const int* ec = L.ell_col + base + k;
+      const float* ev = L.ell_val + base + k;
+      int a = 0;
+      for (; a + 4 <= w; a += 4) {
+        const int c_0 = ec[(a + 0) * nrow], c_1 = ec[(a + 1) * nrow], c_2 = ec[(a + 2) * nrow],
+                  c_3 = ec[(a + 3) * nrow];
+        const float v0 = ev[(a + 0) * nrow], v1 = ev[(a + 1) * nrow], v2 = ev[(a + 2) * nrow],
+                    v3 = ev[(a + 3) * nrow];
+        const float x0 = __ldcg(&L.x[c_0]), x1 = __ldcg(&L.x[c_1]), x2 = __ldcg(&L.x[c_2]), x3 = __ldcg(&L.x[c_3]);
+        v = fmaf(-v0, x0, v);
+        v = fmaf(-v1, x1, v);
+        v = fmaf(-v2, x2, v);
+        v = fmaf(-v3, x3, v);
+      }
+      for (; a < w; ++a) v = fmaf(-ev[a * nrow], __ldcg(&L.x[ec[a * nrow]]), v);
+      L.x[i] = v * L.idiag[i];
+    }
+    __syncthreads();
+  }
+}
+
+// Terminal level: x_idx = (L L^T)^-1 rhs_idx in FP64, one warp per block (as the grid-wide phase).
+__device__ __forceinline__ void terminal_block(const CLev& L, int bk, int ln) {
+  const int* ix = L.idx + L.ioff[bk];
+  const int n = L.ioff[bk + 1] - L.ioff[bk];
+  const double* m = L.fac + L.foff[bk];
+  const double rj = ln < n ? (double)__ldcg(&L.rhs[ix[ln]]) : 0.0;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  for (int j = 0; j < n; j += 4) {
+    const double r0 = __shfl_sync(0xffffffffu, rj, j);
+    const double r1 = __shfl_sync(0xffffffffu, rj, j + 1 < 32 ? j + 1 : 31);
+    const double r2 = __shfl_sync(0xffffffffu, rj, j + 2 < 32 ? j + 2 : 31);
+    const double r3 = __shfl_sync(0xffffffffu, rj, j + 3 < 32 ? j + 3 : 31);
+    if (ln < n) {
+      a0 = fma(m[ln * n + j], r0, a0);
+      if (j + 1 < n) a1 = fma(m[ln * n + j + 1], r1, a1);
+      if (j + 2 < n) a2 = fma(m[ln * n + j + 2], r2, a2);
+      if (j + 3 < n) a3 = fma(m[ln * n + j + 3], r3, a3);
+    }
+  }
+  if (ln < n) L.x[ix[ln]] = (float)((a0 + a1) + (a2 + a3));
+}
+
+// Levels l0 .. of case C, down to the terminal level and back up to l0.
+__device__ void blk_cycle(const CCase& C, int l0, int nu, double* sh) {
+  int l = l0;
+  for (; l < C.nl; ++l) {
+    const CLev& L = C.lv[l];
+    blk_center(L, L.rhs, sh);
+    for (int i = threadIdx.x; i < L.n; i += blockDim.x) L.x[i] = 0.0f;
+    __syncthreads();
+    if (L.terminal) {
+      for (int t = threadIdx.x >> 5; t < L.nblocks; t += blockDim.x >> 5) terminal_block(L, t, threadIdx.x & 31);
+      __syncthreads();
+      blk_center(L, L.x, sh);
+      break;
+    }
+    for (int sw = 0; sw < nu + (nu & 1); ++sw) blk_sweep(L, false, sw & 1, sw < nu);
+    blk_center(L, L.x, sh);
+    for (int k = threadIdx.x; k < (L.jacobi ? 8 : 1) * L.n; k += blockDim.x) {
+      if (L.jacobi) {
+        const int i = k >> 3, sub = k & 7;
+        float v = 0.0f;
+        for (int a = L.off[i] + sub; a < L.off[i + 1]; a += 8) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
+        const unsigned mask = 0xffu << (threadIdx.x & 24);
+        v += __shfl_xor_sync(mask, v, 4, 8);
+        v += __shfl_xor_sync(mask, v, 2, 8);
+        v += __shfl_xor_sync(mask, v, 1, 8);
+        if (sub == 0) L.res[i] = __ldcg(&L.rhs[i]) - fmaf(L.diag[i], __ldcg(&L.x[i]), v);
+      } else {
+        const int i = k;
+        float v = L.diag[i] * __ldcg(&L.x[i]);
+        for (int a = L.off[i]; a < L.off[i + 1]; ++a) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
+        L.res[i] = __ldcg(&L.rhs[i]) - v;
+      }
+    }
+    __syncthreads();
+    blk_center(L, L.res, sh);
+    const CLev& N = C.lv[l + 1];
+    for (int j = threadIdx.x; j < N.n; j += blockDim.x) {
+      float v = 0.0f;
+      for (int k = L.roff[j]; k < L.roff[j + 1]; ++k) v = fmaf(L.rw[k], __ldcg(&L.res[L.rchild[k]]), v);
+      N.rhs[j] = v;
+    }
+    __syncthreads();
+  }
+  for (int m = min(l, C.nl - 1) - 1; m >= l0; --m) {
+    const CLev& L = C.lv[m];
+    const CLev& N = C.lv[m + 1];
+    for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+      float s = 0.0f;
+      for (int k = L.poff[i]; k < L.poff[i + 1]; ++k) s = fmaf(L.pw[k], __ldcg(&N.x[L.pcol[k]]), s);
+      L.x[i] = __ldcg(&L.x[i]) + s;
+    }
+    __syncthreads();
+    for (int sw = 0; sw < nu + (nu & 1); ++sw) blk_sweep(L, true, sw & 1, sw < nu);
+    blk_center(L, L.x, sh);
+  }
+}
+
+__global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const MState* ST, const CoarseTab* Tp) {
   const CoarseTab T = *Tp;
   __shared__ double sh[32];
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1153,7 +1359,8 @@ __global__ void __launch_bounds__(512, 3) k_coarse_all(const CCase* cases, const
   cg::grid_group grid = cg::this_grid();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
   const int nc = T.nc;
-  for (int l = 0; l < T.nlev; ++l) {
+  const int gl = min(T.nlev, T.lb);  // levels 0 .. gl-1 grid-wide
+  for (int l = 0; l < gl; ++l) {
     load_levels(cases, nc, l, MAXL, sl);
     if (T.anyg[l]) g_center(sl, ST, T, l, 0, sh, grid);
     {
@@ -1164,36 +1371,17 @@ __global__ void __launch_bounds__(512, 3) k_coarse_all(const CCase* cases, const
       }
     }
     grid.sync();
-    {
+    if (__ldg(&T.term[l * (nc + 1) + nc]) > 0) {  // the same for every block
       // Terminal levels: x_idx = (L L^T)^-1 rhs_idx in FP64, one warp per block.
       const int* off = T.term + l * (nc + 1);
       const int wp = gt >> 5, nw = nth >> 5, ln = threadIdx.x & 31;
       for (int t = wp; t < __ldg(&off[nc]); t += nw) {
         const int ci = find_case(off, nc, t);
         if (!active(ST, ci)) continue;
-        const CLev& L = sl[ci];
-        const int bk = t - __ldg(&off[ci]);
-        const int* ix = L.idx + L.ioff[bk];
-        const int n = L.ioff[bk + 1] - L.ioff[bk];
-        const double* m = L.fac + L.foff[bk];
-        const double rj = ln < n ? (double)__ldcg(&L.rhs[ix[ln]]) : 0.0;
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-        for (int j = 0; j < n; j += 4) {
-          const double r0 = __shfl_sync(0xffffffffu, rj, j);
-          const double r1 = __shfl_sync(0xffffffffu, rj, j + 1 < 32 ? j + 1 : 31);
-          const double r2 = __shfl_sync(0xffffffffu, rj, j + 2 < 32 ? j + 2 : 31);
-          const double r3 = __shfl_sync(0xffffffffu, rj, j + 3 < 32 ? j + 3 : 31);
-          if (ln < n) {
-            a0 = fma(m[ln * n + j], r0, a0);
-            if (j + 1 < n) a1 = fma(m[ln * n + j + 1], r1, a1);
-            if (j + 2 < n) a2 = fma(m[ln * n + j + 2], r2, a2);
-            if (j + 3 < n) a3 = fma(m[ln * n + j + 3], r3, a3);
-          }
-        }
-        if (ln < n) L.x[ix[ln]] = (float)((a0 + a1) + (a2 + a3));
+        terminal_block(sl[ci], t - __ldg(&off[ci]), ln);
       }
+      grid.sync();
     }
-    grid.sync();
     for (int sw = 0; sw < T.nu + (T.nu & 1); ++sw) g_sweep(sl, ST, T, l, false, sw & 1, sw < T.nu, grid);
     if (T.anyg[l]) g_center(sl, ST, T, l, 1, sh, grid);
     {
@@ -1238,7 +1426,14 @@ __global__ void __launch_bounds__(512, 3) k_coarse_all(const CCase* cases, const
     }
     grid.sync();
   }
-  for (int l = T.nlev - 2; l >= 0; --l) {
+  if (gl < T.nlev) {
+    // The remaining levels of every case inside one block each.
+    for (int ci = blockIdx.x; ci < nc; ci += gridDim.x)
+      if (active(ST, ci) && cases[ci].nl > gl) blk_cycle(cases[ci], gl, T.nu, sh);
+    __threadfence();
+    grid.sync();
+  }
+  for (int l = min(T.nlev - 2, gl - 1); l >= 0; --l) {
     load_levels(cases, nc, l, MAXL, sl);
     {
       const int* off = T.live + l * (nc + 1);
@@ -1290,7 +1485,11 @@ __device__ __forceinline__ void b_rhs(const FineCase* FC, MState* ST, const int2
 __global__ void __launch_bounds__(TILE) k_rhs(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = t0_; ti < t1_; ++ti) b_rhs(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == IDLE)
+    b_rhs(FC, ST, t, cached_);
+  }
 }
 
 struct FinNorm {
@@ -1322,6 +1521,7 @@ __global__ void __launch_bounds__(TILE) k_norm(const FineCase* FC, MState* ST, c
   Seg g;
   for (int ti = t0_; ti < t1_; ++ti) {
     const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == IDLE)
     if (t.x != g.ci) {
       close_seg(FC, ST, g, sh, FinNorm());
       g.ci = t.x;
@@ -1359,7 +1559,11 @@ __device__ __forceinline__ void b_addp(const FineCase* FC, MState* ST, const int
 __global__ void __launch_bounds__(TILE) k_addp(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = t0_; ti < t1_; ++ti) b_addp(FC, ST, tiles[ti], cached_);
+  for (int ti = t0_; ti < t1_; ++ti) {
+    const int2 t = tiles[ti];
+    SKIP_CASE(t, S_.state == DONE)
+    b_addp(FC, ST, t, cached_);
+  }
 }
 
 // ----------------------------------------------------------------- host side
@@ -1617,6 +1821,21 @@ int build_case(cfdg_grid* G, CaseState& cs) {
           pw32.push_back((float)M0.prolong.val[q]);
         }
       poff[sl + 1] = (int32_t)pcol.size();
+    }
+    // Aggregation hierarchies prolong by injection (one weight-1 entry per row): keep the
+    // parent per slot only.
+    bool inj = true;
+    for (int sl = 0; sl < F.N2 && inj; ++sl) {
+      const int n = poff[sl + 1] - poff[sl];
+      inj = n == 0 || (n == 1 && pw32[poff[sl]] == 1.0f);
+    }
+    if (inj) {
+      std::vector<int32_t> par(F.N2, -1);
+      for (int sl = 0; sl < F.N2; ++sl)
+        if (poff[sl + 1] > poff[sl]) par[sl] = pcol[poff[sl]];
+      int* pp;
+      if (int e = A.upload(&pp, par, s)) return e;
+      F.pinj = pp;
     }
     int *o, *c, *po, *pc;
     float *w, *pw;
@@ -1969,6 +2188,20 @@ int fill_tab(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
   T.nc = nc;
   T.nlev = 0;
   T.nu = B->nuc;
+  // Levels on which every active case has at most BLK_WORK rows plus stencil entries run
+  // block-locally (one block per case, block barriers) instead of one grid barrier per
+  // phase; wide-stencil levels stay grid-wide even when they have few rows.
+  T.lb = nlev;
+  for (int l = nlev - 1; l >= 0; --l) {
+    long long most = 0;
+    for (int i = 0; i < nc; ++i)
+      if (on[i] && l < B->cases[i]->C.nl) {
+        const auto& st = B->cases[i]->stats[l];
+        most = std::max(most, st.rows + st.ell);
+      }
+    if (most > BLK_WORK) break;
+    T.lb = l;
+  }
   for (int l = 0; l < nlev; ++l) {
     int maxc = 0, anyg = 0;
     auto lev = [&](int i) -> const CLev* {
