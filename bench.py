@@ -41,6 +41,8 @@ sys.path.insert(0, ROOT)
 METRIC = "Poisson solves/s at 1e-8 resid: batched mixed vs plain FP64; p50/p99 latency"
 UNIT = "solves/s"
 DT, TOL, MAX_IT = 0.1, 1e-8, 10000
+LARGE_WORKLOAD = ("256x256x128 grid (8,388,608 cells), dx=2 m, 40 seeded box buildings, open x (inflow 5 m/s) / "
+                  "wall y,z; projection of the seeded u* sequence, dt=0.1 s; mixed FP32/FP64 multigrid PCG to 1e-8")
 WORKLOAD = ("128x128x64 grid, dx=2 m, 12 seeded box buildings, open x (inflow 5 m/s) / wall y,z; "
             "projection of the seeded u* sequence (0.05 U[-1,1] perturbation per step), dt=0.1 s; "
             "masked multigrid V(2,2)-PCG to 1e-8")
@@ -245,12 +247,12 @@ class Form:
     """One arithmetic form of the projection on `cases` copies of the workload (different
     velocity seeds): plain FP64 (one grid), mixed (one grid) or batched mixed (one batch)."""
 
-    def __init__(self, pkg, torch, dev, stream, form, cases, steps, rank):
+    def __init__(self, pkg, torch, dev, stream, form, cases, steps, rank, case=None):
         import numpy as np
 
         self.pkg, self.torch, self.form = pkg, torch, form
         self.ncases = cases
-        case = workload_case(pkg)
+        case = case or workload_case(pkg)
         self.grids = [pkg.grid.Grid.build(case)] * 1
         g = self.grids[0]
         self.g = g
@@ -796,7 +798,10 @@ def run_engine(args):
             dist.destroy_process_group()
         return rc
     ncases = args.cases if args.form == "batched" else 1
-    form = Form(pkg, torch, dev, stream, args.form, ncases, K + W, rank)
+    # --form large: the mixed form on the 256x256x128 grid with 40 buildings (8.4 M cells).
+    big = pkg.synth.config3() if args.form == "large" else None
+    fname = "mixed" if args.form == "large" else args.form
+    form = Form(pkg, torch, dev, stream, fname, ncases, K + W, rank, case=big)
     g = form.g
     launches0 = L.cfdg_launch_count()
     clocks = Clocks(local)
@@ -844,13 +849,13 @@ def run_engine(args):
     # The plain FP64 form on the same workload, for the batched-mixed vs plain comparison.
     plain = None
     if args.form != "plain" and not args.skip_plain:
-        pf = Form(pkg, torch, dev, stream, "plain", 1, 2 + 1, rank + 7)
+        pf = Form(pkg, torch, dev, stream, "plain", 1, 2 + 1, rank + 7, case=big)
         pms, plat, pinfos = timed_steps(pf, torch, stream, flush, 1, 2, dist)
         plain = {"value": round(world * 2 / (pms / 1e3), 4), "unit": UNIT, "ms_per_solve": round(pms / 2, 2),
                  "iterations_mean": round(statistics.mean(i.iterations for i in pinfos), 1), "steps": 2}
         pf.close()
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.form != "large":
         cpu = cpu_baseline(workload_case(pkg))
     if rank == 0:
         its = [i.iterations for i in infos]
@@ -860,9 +865,11 @@ def run_engine(args):
             "ms_per_step": round(total_ms / K, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.form == "plain" else "f32+f64",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "form": {"plain": "plain FP64 multigrid PCG (parity form)",
-                                                       "mixed": "mixed FP32/FP64 multigrid PCG, one case",
-                                                       "batched": f"batched mixed FP32/FP64, {ncases} cases per step"}[args.form],
+            "config": {"workload": LARGE_WORKLOAD if args.form == "large" else WORKLOAD,
+                       "form": {"plain": "plain FP64 multigrid PCG (parity form)",
+                                "mixed": "mixed FP32/FP64 multigrid PCG, one case",
+                                "large": "mixed FP32/FP64 multigrid PCG, one 8.4 M-cell case",
+                                "batched": f"batched mixed FP32/FP64, {ncases} cases per step"}[args.form],
                        "cases_per_step": ncases, "cells_per_case": g.count, "faces_per_case": g.n_faces,
                        "l2": "256 MiB buffer written before every step (inside the timed region)",
                        "parallelism": f"replicas x{world}"},
@@ -892,7 +899,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--form", default="serving", choices=["plain", "mixed", "batched", "serving", "uneven"])
+    ap.add_argument("--form", default="serving", choices=["plain", "mixed", "batched", "serving", "uneven", "large"])
     ap.add_argument("--slots", type=int, default=0, help="serving: cases on the GPU at once (0: all)")
     ap.add_argument("--requests", type=int, default=520, help="serving: open-loop requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")

@@ -13,6 +13,7 @@
 // The PCG loop runs as CUDA graphs of 8 iterations; every kernel first reads the
 // device Scalars and returns at once when the solve has finished, so the host only
 // synchronises between chunks, where it polls the caller's Control.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -406,6 +407,71 @@ __global__ void k_ic0_bwd(const int* __restrict__ order, int begin, int end, con
   z[c] = v / diag[c];
 }
 
+// Row bodies shared by the level-by-level kernels and the cooperative coarse kernel
+// (same operations, same order; L2 loads for vectors another block may have written).
+__device__ __forceinline__ void gs_row(int i, const int* __restrict__ off, const int* __restrict__ col,
+                                       const double* __restrict__ val, const double* __restrict__ diag,
+                                       const double* rhs, double* x) {
+  const double d = diag[i];
+  if (d == 0.0) {  // an isolated sealed cell: a null pressure space
+    x[i] = 0.0;
+    return;
+  }
+  double v = __ldcg(&rhs[i]);
+  for (int k = off[i]; k < off[i + 1]; ++k) v = v - val[k] * __ldcg(&x[col[k]]);
+  x[i] = v / d;
+}
+__device__ __forceinline__ void residual_row(int i, const int* __restrict__ off, const int* __restrict__ col,
+                                             const double* __restrict__ val, const double* __restrict__ diag,
+                                             const double* rhs, const double* x, double* res) {
+  double v = diag[i] * __ldcg(&x[i]);
+  for (int k = off[i]; k < off[i + 1]; ++k) v = v + val[k] * __ldcg(&x[col[k]]);
+  res[i] = __ldcg(&rhs[i]) - v;
+}
+__device__ __forceinline__ void restrict_row(int j, const int* __restrict__ off, const int* __restrict__ child,
+                                             const double* __restrict__ w, const double* res, double* rhs_c) {
+  double v = 0.0;
+  for (int k = off[j]; k < off[j + 1]; ++k) v = v + w[k] * __ldcg(&res[child[k]]);
+  rhs_c[j] = v;
+}
+__device__ __forceinline__ void prolong_row(int i, const int* __restrict__ off, const int* __restrict__ col,
+                                            const double* __restrict__ w, const double* xc, double* x) {
+  double s = -0.0;
+  for (int k = off[i]; k < off[i + 1]; ++k) s = s + w[k] * __ldcg(&xc[col[k]]);
+  x[i] = __ldcg(&x[i]) + s;
+}
+// Dense Cholesky solve of one terminal block by one thread (masked.rs:52-69).
+__device__ __forceinline__ void direct_block(int bk, const int* __restrict__ ioff, const int* __restrict__ idx,
+                                             const long long* __restrict__ foff, const double* __restrict__ L,
+                                             const double* rhs, double* x) {
+  const int* ix = idx + ioff[bk];
+  const int n = ioff[bk + 1] - ioff[bk];
+  const double* f = L + foff[bk];
+  for (int i = 0; i < n; ++i) {
+    double v = __ldcg(&rhs[ix[i]]);
+    for (int j = 0; j < i; ++j) v = v - f[i * n + j] * __ldcg(&x[ix[j]]);
+    x[ix[i]] = v / f[i * n + i];
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double v = __ldcg(&x[ix[i]]);
+    for (int j = i + 1; j < n; ++j) v = v - f[j * n + i] * __ldcg(&x[ix[j]]);
+    x[ix[i]] = v / f[i * n + i];
+  }
+}
+// Gauge of group g by one block: subtract the members' mean (fixed-order tree sum).
+__device__ __forceinline__ void center_group(int g, const int* __restrict__ off, const int* __restrict__ members,
+                                             double* x, double* sh, double* mean) {
+  const int b = off[g], e = off[g + 1];
+  double acc = 0.0;
+  for (int k = b + threadIdx.x; k < e; k += blockDim.x) acc += __ldcg(&x[members[k]]);
+  double s = block_sum(acc, sh);
+  if (threadIdx.x == 0) *mean = s / (double)(e - b);
+  __syncthreads();
+  const double m = *mean;
+  for (int k = b + threadIdx.x; k < e; k += blockDim.x) x[members[k]] = __ldcg(&x[members[k]]) - m;
+  __syncthreads();
+}
+
 // Lexicographic Gauss-Seidel over one level (multigrid.rs:272-281, masked.rs:158-172).
 __global__ void k_gs(const int* __restrict__ order, int begin, int end, const int* __restrict__ off,
                      const int* __restrict__ col, const double* __restrict__ val, const double* __restrict__ diag,
@@ -413,15 +479,7 @@ __global__ void k_gs(const int* __restrict__ order, int begin, int end, const in
   if (S && S->done) return;
   int t = begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= end) return;
-  int i = order[t];
-  const double d = diag[i];
-  if (d == 0.0) {  // an isolated sealed cell: a null pressure space
-    x[i] = 0.0;
-    return;
-  }
-  double v = rhs[i];
-  for (int k = off[i]; k < off[i + 1]; ++k) v = v - val[k] * x[col[k]];
-  x[i] = v / d;
+  gs_row(order[t], off, col, val, diag, rhs, x);
 }
 
 // res = rhs - A x (multigrid.rs:263-271 then :691-694).
@@ -514,6 +572,107 @@ __global__ void k_direct(int nblocks, const int* __restrict__ ioff, const int* _
     double v = x[ix[i]];
     for (int j = i + 1; j < n; ++j) v = v - f[j * n + i] * x[ix[j]];
     x[ix[i]] = v / f[i * n + i];
+  }
+}
+
+// ----------------------------------------------------------------- coarse levels, one launch
+// Levels 1 .. L-1 of the V-cycle in one cooperative kernel: each dependency level of a
+// lexicographic sweep, the residual, the restriction, the prolongation and the gauges is
+// a phase separated by a grid barrier (level-by-level launches cost a launch each: about
+// 1,300 per cycle on a 128x128x64 grid). Levels whose dependency levels have at most one
+// block of rows sweep inside block 0 with block barriers. Every row runs the row body of
+// the level-by-level kernels, so the bits are the same.
+struct PLev {
+  int n, terminal, ngroups, nblocks;
+  int nfwd, nbwd, blocal, pad_;
+  const int *off, *col;
+  const double *val, *diag;
+  const int *fo, *fs, *bo, *bs;  // sweep orders and dependency-level starts
+  const int *goff, *gmem;
+  const int *roff, *rcol;        // restriction to the next level (rows of the next level)
+  const double* rval;
+  const int *poff, *pcol;        // prolongation from the next level
+  const double* pval;
+  double *rhs, *x, *res;
+  const int *ioff, *idx;
+  const long long* foff;
+  const double* fac;
+};
+
+namespace cg = cooperative_groups;
+
+__device__ void pc_center(const PLev& L, double* v, double* sh, double* mean, cg::grid_group& grid) {
+  if (L.ngroups == 0) return;
+  for (int g = blockIdx.x; g < L.ngroups; g += gridDim.x) center_group(g, L.goff, L.gmem, v, sh, mean);
+  __threadfence();
+  grid.sync();
+}
+
+__device__ void pc_sweep(const PLev& L, bool backward, cg::grid_group& grid) {
+  const int* order = backward ? L.bo : L.fo;
+  const int* start = backward ? L.bs : L.fs;
+  const int nlev = backward ? L.nbwd : L.nfwd;
+  if (L.blocal) {
+    if (blockIdx.x == 0)
+      for (int dl = 0; dl < nlev; ++dl) {
+        for (int t = start[dl] + threadIdx.x; t < start[dl + 1]; t += blockDim.x)
+          gs_row(order[t], L.off, L.col, L.val, L.diag, L.rhs, L.x);
+        __threadfence();
+        __syncthreads();
+      }
+    __threadfence();
+    grid.sync();
+    return;
+  }
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  for (int dl = 0; dl < nlev; ++dl) {
+    for (int t = start[dl] + gt; t < start[dl + 1]; t += nth) gs_row(order[t], L.off, L.col, L.val, L.diag, L.rhs, L.x);
+    __threadfence();
+    grid.sync();
+  }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_plain_coarse(const PLev* lv, int nl, const Scalars* S) {
+  if (S && S->done) return;  // read once; nothing in this kernel changes it
+  __shared__ double sh[32];
+  __shared__ double mean;
+  cg::grid_group grid = cg::this_grid();
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  int l = 0;
+  for (; l < nl; ++l) {
+    const PLev& L = lv[l];
+    pc_center(L, L.rhs, sh, &mean, grid);
+    for (int i = gt; i < L.n; i += nth) L.x[i] = 0.0;
+    __threadfence();
+    grid.sync();
+    if (L.terminal) {
+      for (int bk = gt; bk < L.nblocks; bk += nth) direct_block(bk, L.ioff, L.idx, L.foff, L.fac, L.rhs, L.x);
+      __threadfence();
+      grid.sync();
+      pc_center(L, L.x, sh, &mean, grid);
+      break;
+    }
+    pc_sweep(L, false, grid);
+    pc_sweep(L, false, grid);
+    pc_center(L, L.x, sh, &mean, grid);
+    for (int i = gt; i < L.n; i += nth) residual_row(i, L.off, L.col, L.val, L.diag, L.rhs, L.x, L.res);
+    __threadfence();
+    grid.sync();
+    pc_center(L, L.res, sh, &mean, grid);
+    const PLev& N = lv[l + 1];
+    for (int j = gt; j < N.n; j += nth) restrict_row(j, L.roff, L.rcol, L.rval, L.res, N.rhs);
+    __threadfence();
+    grid.sync();
+  }
+  for (int m = min(l, nl - 1) - 1; m >= 0; --m) {
+    const PLev& L = lv[m];
+    const PLev& N = lv[m + 1];
+    for (int i = gt; i < L.n; i += nth) prolong_row(i, L.poff, L.pcol, L.pval, N.x, L.x);
+    __threadfence();
+    grid.sync();
+    pc_sweep(L, true, grid);
+    pc_sweep(L, true, grid);
+    pc_center(L, L.x, sh, &mean, grid);
   }
 }
 
@@ -697,7 +856,9 @@ void launch_vcycle(cfdg_grid* G, const double* r, double* z, const Scalars* S) {
     tick(G);
   }
   const int nl = (int)H.levels.size();
-  for (int l = 0; l < nl; ++l) {
+  // Levels 1 .. L-1 in one cooperative launch when available, else level by level.
+  const bool coop = H.coop_blocks > 0 && nl > 1;
+  for (int l = 0; l < (coop ? 1 : nl); ++l) {
     DevLevel& L = H.levels[l];
     const bool full = l == 0 && H.full0;
     launch_center(G, L.groups, L.ngroups, L.rhs, S);
@@ -724,7 +885,20 @@ void launch_vcycle(cfdg_grid* G, const double* r, double* z, const Scalars* S) {
     k_restrict<<<grid_blocks(C.n), BLOCK, 0, s>>>(C.n, L.restrict_.off, L.restrict_.col, L.restrict_.val, L.res,
                                                   C.rhs, S); tick(G);
   }
-  for (int l = nl - 2; l >= 0; --l) {
+  if (coop) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)H.coop_blocks, 1, 1);
+    cfg.blockDim = dim3(BLOCK, 1, 1);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_plain_coarse, (const PLev*)H.d_plev, nl - 1, S);
+    tick(G);
+  }
+  for (int l = coop ? 0 : nl - 2; l >= 0; --l) {
     DevLevel& L = H.levels[l];
     DevLevel& C = H.levels[l + 1];
     const bool full = l == 0 && H.full0;
@@ -912,6 +1086,8 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
     if (int e = D->arena.upload(&L.bwd.order, M.bwd.order, s)) return e;
     L.fwd.start = M.fwd.start;
     L.bwd.start = M.bwd.start;
+    if (int e = D->arena.upload(&L.fwd.d_start, M.fwd.start, s)) return e;
+    if (int e = D->arena.upload(&L.bwd.d_start, M.bwd.start, s)) return e;
     L.ngroups = M.groups.rows();
     if (L.ngroups)
       if (int e = upload_csr(D->arena, M.groups, L.groups, s)) return e;
@@ -933,6 +1109,48 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
   }
   D->level_cells = H.level_cells;
   D->level_nonzeros = H.level_nonzeros;
+  // Levels 1 .. L-1 for the cooperative coarse kernel, when its grid can be co-resident.
+  if (D->levels.size() > 1) {
+    std::vector<PLev> pl;
+    int widest = 1;
+    for (size_t l = 1; l < D->levels.size(); ++l) {
+      const DevLevel& L = D->levels[l];
+      PLev P{};
+      P.n = L.n;
+      P.terminal = L.terminal ? 1 : 0;
+      P.ngroups = L.ngroups;
+      P.nblocks = L.nblocks;
+      P.nfwd = (int)L.fwd.start.size() - 1;
+      P.nbwd = (int)L.bwd.start.size() - 1;
+      int dl_max = 0;
+      for (int q = 0; q < P.nfwd; ++q) dl_max = std::max(dl_max, L.fwd.start[q + 1] - L.fwd.start[q]);
+      for (int q = 0; q < P.nbwd; ++q) dl_max = std::max(dl_max, L.bwd.start[q + 1] - L.bwd.start[q]);
+      P.blocal = dl_max <= BLOCK ? 1 : 0;
+      widest = std::max(widest, dl_max);
+      P.off = L.a.off, P.col = L.a.col, P.val = L.a.val, P.diag = L.diag;
+      P.fo = L.fwd.order, P.fs = L.fwd.d_start, P.bo = L.bwd.order, P.bs = L.bwd.d_start;
+      P.goff = L.groups.off, P.gmem = L.groups.col;
+      P.roff = L.restrict_.off, P.rcol = L.restrict_.col, P.rval = L.restrict_.val;
+      P.poff = L.prolong.off, P.pcol = L.prolong.col, P.pval = L.prolong.val;
+      P.rhs = L.rhs, P.x = L.x, P.res = L.res;
+      P.ioff = L.d_ioff, P.idx = L.d_idx, P.foff = L.d_foff, P.fac = L.d_fac;
+      pl.push_back(P);
+    }
+    PLev* dp = nullptr;
+    if (int e = D->arena.upload(&dp, pl, s)) return e;
+    D->d_plev = dp;
+    // A small grid: the widest dependency level fits it in one pass, and fewer blocks make
+    // the grid barrier cheaper.
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_plain_coarse, BLOCK, 0) != cudaSuccess || per < 1) {
+      cudaGetLastError();
+      per = 0;
+    }
+    const int want = std::max(8, std::min(64, (widest + BLOCK - 1) / BLOCK));
+    D->coop_blocks = per > 0 ? std::min(want, sms * per) : 0;
+  }
   CU(cudaStreamSynchronize(s));
   G->host_mg = std::make_shared<Hierarchy>(std::move(H));
   {

@@ -478,7 +478,7 @@ __device__ __forceinline__ void b_op(const FineCase* FC, MState* ST, const int2 
   }
   tile_partial((double)hi + (double)lo, F, lt, sh, seg_n);
 }
-__global__ void __launch_bounds__(TILE) k_op(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+__global__ void __launch_bounds__(TILE, 6) k_op(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   __shared__ double sh[32];
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory

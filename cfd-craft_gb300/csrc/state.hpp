@@ -98,6 +98,7 @@ inline int upload_csr(Arena& A, const Csr& c, DevCsr& d, cudaStream_t s) {
 struct DevSchedule {
   int* order = nullptr;
   std::vector<int32_t> start;
+  int* d_start = nullptr;  // device copy of start (the cooperative coarse kernel walks it)
 };
 
 struct DevIc0 {
@@ -134,6 +135,10 @@ struct DevHierarchy {
   int* fluid_idx = nullptr;
   std::vector<DevLevel> levels;
   std::vector<uint64_t> level_cells, level_nonzeros;
+  // Levels 1 .. L-1 as one cooperative kernel's descriptors (engine.cu PLev), and its grid
+  // (0: not co-resident, the level-by-level launches are used instead).
+  void* d_plev = nullptr;
+  int coop_blocks = 0;
 };
 
 }  // namespace cfdg
