@@ -1112,7 +1112,6 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
   // Levels 1 .. L-1 for the cooperative coarse kernel, when its grid can be co-resident.
   if (D->levels.size() > 1) {
     std::vector<PLev> pl;
-    int widest = 1;
     for (size_t l = 1; l < D->levels.size(); ++l) {
       const DevLevel& L = D->levels[l];
       PLev P{};
@@ -1126,7 +1125,6 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
       for (int q = 0; q < P.nfwd; ++q) dl_max = std::max(dl_max, L.fwd.start[q + 1] - L.fwd.start[q]);
       for (int q = 0; q < P.nbwd; ++q) dl_max = std::max(dl_max, L.bwd.start[q + 1] - L.bwd.start[q]);
       P.blocal = dl_max <= BLOCK ? 1 : 0;
-      widest = std::max(widest, dl_max);
       P.off = L.a.off, P.col = L.a.col, P.val = L.a.val, P.diag = L.diag;
       P.fo = L.fwd.order, P.fs = L.fwd.d_start, P.bo = L.bwd.order, P.bs = L.bwd.d_start;
       P.goff = L.groups.off, P.gmem = L.groups.col;
@@ -1139,8 +1137,8 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
     PLev* dp = nullptr;
     if (int e = D->arena.upload(&dp, pl, s)) return e;
     D->d_plev = dp;
-    // A small grid: the widest dependency level fits it in one pass, and fewer blocks make
-    // the grid barrier cheaper.
+    // One block per SM: a dependency level fits in one pass and whole-level phases
+    // (residual, transfers) have a few rows per thread.
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1148,8 +1146,7 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
       cudaGetLastError();
       per = 0;
     }
-    const int want = std::max(8, std::min(64, (widest + BLOCK - 1) / BLOCK));
-    D->coop_blocks = per > 0 ? std::min(want, sms * per) : 0;
+    D->coop_blocks = per > 0 ? sms : 0;
   }
   CU(cudaStreamSynchronize(s));
   G->host_mg = std::make_shared<Hierarchy>(std::move(H));

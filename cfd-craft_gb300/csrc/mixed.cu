@@ -48,7 +48,8 @@ constexpr int FTILE = 1024;     // faces per block (velocity correction)
 constexpr int CS = 16;          // CTAs per cluster (non-portable size, opted in at pack time)
 constexpr int CT = 1024;        // threads per cluster CTA
 constexpr int MAXL = 16;        // coarse levels per case
-constexpr int CHUNK_IT = 8;     // iterations per captured graph launch
+constexpr int CHUNK_IT = 8;     // iterations per captured graph launch (batched projections)
+constexpr int SERVER_CHUNK_IT = 4;  // the same for servers: requests join and leave at chunk ends
 
 enum State : int { OUTER = 0, SCALE = 1, START = 2, RUN = 3, DONE = 4, FAIL = 5, IDLE = 6 };
 
@@ -159,14 +160,15 @@ __device__ __forceinline__ double bsum(double v, double* sh) {
   return s;
 }
 
-// Reductions of the fine-level kernels. Every tile stores its block sum in the case's
-// partials (slot = tile index); a block counts a case's tiles once per run of
-// consecutive tiles of that case, and the block that completes a case sums the partials
-// in tile order (the same bits whatever the grid size) and applies the case's scalar
-// update.
+// Reductions of the fine-level kernels. Every warp stores its sum in the case's partials
+// (slot = tile * RT + warp, no block barrier); a block counts a case's tiles once per run
+// of consecutive tiles of that case, and the block that completes a case sums the
+// partials in slot order (the same bits whatever the grid size) and applies the case's
+// scalar update.
 __device__ __forceinline__ void tile_partial(double v, const FineCase& F, int lt, double* sh, int& seg_n) {
-  const double b = bsum(v, sh);
-  if (threadIdx.x == 0) F.partials[lt] = b;
+  (void)sh;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) F.partials[lt * (TILE / 32) + (threadIdx.x >> 5)] = v;
   ++seg_n;
 }
 
@@ -178,6 +180,7 @@ template <class Fin>
 __device__ __forceinline__ void close_seg(const FineCase* FC, MState* ST, Seg& g, double* sh, Fin fin) {
   if (g.n == 0) return;
   __shared__ bool last;
+  __syncthreads();  // every warp's partials of the run are stored
   if (threadIdx.x == 0) {
     __threadfence();
     last = atomicAdd(&ST[g.ci].counter, (unsigned)g.n) + (unsigned)g.n == (unsigned)FC[g.ci].ntiles;
@@ -186,7 +189,7 @@ __device__ __forceinline__ void close_seg(const FineCase* FC, MState* ST, Seg& g
   g.n = 0;
   if (!last) return;
   __threadfence();
-  const int nt = FC[g.ci].ntiles;
+  const int nt = FC[g.ci].ntiles * (TILE / 32);
   const double* part = FC[g.ci].partials;
   double a = 0.0;
   for (int k = threadIdx.x; k < nt; k += blockDim.x) a += __ldcg(&part[k]);
@@ -1174,29 +1177,43 @@ __device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, in
         }
         continue;
       }
+      // Two consecutive rows of the colour block per item: both rows' loads are in flight
+      // before either is stored (rows of one colour never read each other). Each row sums
+      // its entries in ELL order, as every other path does.
       const int color = backward ? L.ncolors - 1 - cc : cc;
       const int c0 = L.coff[color];
       const int nrow = L.coff[color + 1] - c0;
-      if (k >= nrow) continue;  // ranges are rounded up to multiples of eight
-      const int i = c0 + k;  // colour blocks are contiguous
+      const int q = 2 * k;
+      if (q >= nrow) continue;  // ranges are rounded up to multiples of eight
+      const bool two = q + 1 < nrow;
+      const int i = c0 + q;  // colour blocks are contiguous
       const int base = L.ell_off[color], w = L.ell_w[color];
-      float v = __ldcg(&L.rhs[i]);
-      const int* ec = L.ell_col + base + k;
-      const float* ev = L.ell_val + base + k;
+      float v0 = __ldcg(&L.rhs[i]);
+      float v1 = two ? __ldcg(&L.rhs[i + 1]) : 0.0f;
+      const float d0 = L.idiag[i], d1 = two ? L.idiag[i + 1] : 0.0f;
+      const int* ec = L.ell_col + base + q;
+      const float* ev = L.ell_val + base + q;
       int a = 0;
-      for (; a + 4 <= w; a += 4) {
-        const int c_0 = ec[(a + 0) * nrow], c_1 = ec[(a + 1) * nrow], c_2 = ec[(a + 2) * nrow],
-                  c_3 = ec[(a + 3) * nrow];
-        const float v0 = ev[(a + 0) * nrow], v1 = ev[(a + 1) * nrow], v2 = ev[(a + 2) * nrow],
-                    v3 = ev[(a + 3) * nrow];
-        const float x0 = __ldcg(&L.x[c_0]), x1 = __ldcg(&L.x[c_1]), x2 = __ldcg(&L.x[c_2]), x3 = __ldcg(&L.x[c_3]);
-        v = fmaf(-v0, x0, v);
-        v = fmaf(-v1, x1, v);
-        v = fmaf(-v2, x2, v);
-        v = fmaf(-v3, x3, v);
+      for (; a + 2 <= w; a += 2) {
+        const int ca0 = ec[a * nrow], ca1 = ec[(a + 1) * nrow];
+        const int cb0 = two ? ec[a * nrow + 1] : ca0, cb1 = two ? ec[(a + 1) * nrow + 1] : ca1;
+        const float wa0 = ev[a * nrow], wa1 = ev[(a + 1) * nrow];
+        const float wb0 = two ? ev[a * nrow + 1] : 0.0f, wb1 = two ? ev[(a + 1) * nrow + 1] : 0.0f;
+        const float xa0 = __ldcg(&L.x[ca0]), xa1 = __ldcg(&L.x[ca1]);
+        const float xb0 = __ldcg(&L.x[cb0]), xb1 = __ldcg(&L.x[cb1]);
+        v0 = fmaf(-wa0, xa0, v0);
+        v0 = fmaf(-wa1, xa1, v0);
+        v1 = fmaf(-wb0, xb0, v1);
+        v1 = fmaf(-wb1, xb1, v1);
       }
-      for (; a < w; ++a) v = fmaf(-ev[a * nrow], __ldcg(&L.x[ec[a * nrow]]), v);
-      L.x[i] = v * L.idiag[i];
+      if (a < w) {
+        const int ca = ec[a * nrow], cb = two ? ec[a * nrow + 1] : ca;
+        const float wa = ev[a * nrow], wb = two ? ev[a * nrow + 1] : 0.0f;
+        v0 = fmaf(-wa, __ldcg(&L.x[ca]), v0);
+        v1 = fmaf(-wb, __ldcg(&L.x[cb]), v1);
+      }
+      L.x[i] = v0 * d0;
+      if (two) L.x[i + 1] = v1 * d1;
     }
     grid.sync();
   }
@@ -1365,9 +1382,13 @@ __global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const
     if (T.anyg[l]) g_center(sl, ST, T, l, 0, sh, grid);
     {
       const int* off = T.rows + l * (nc + 1);
+      CaseCursor cur;
+      bool on = false;
       for (int t = gt; t < __ldg(&off[nc]); t += nth) {
-        const int ci = find_case(off, nc, t);
-        if (active(ST, ci)) sl[ci].x[t - __ldg(&off[ci])] = 0.0f;
+        const int prev = cur.ci;
+        const int ci = case_at(off, nc, t, cur);
+        if (ci != prev) on = active(ST, ci);
+        if (on) sl[ci].x[t - cur.lo] = 0.0f;
       }
     }
     grid.sync();
@@ -1386,11 +1407,15 @@ __global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const
     if (T.anyg[l]) g_center(sl, ST, T, l, 1, sh, grid);
     {
       const int* off = T.res + l * (nc + 1);
+      CaseCursor cur;
+      bool on = false;
       for (int t = gt; t < __ldg(&off[nc]); t += nth) {
-        const int ci = find_case(off, nc, t);
-        if (!active(ST, ci)) continue;
+        const int prev = cur.ci;
+        const int ci = case_at(off, nc, t, cur);
+        if (ci != prev) on = active(ST, ci);
+        if (!on) continue;
         const CLev& L = sl[ci];
-        const int k = t - __ldg(&off[ci]);
+        const int k = t - cur.lo;
         if (L.jacobi) {  // eight lanes per (wide) row
           const int i = k >> 3, sub = k & 7;
           float v = 0.0f;
@@ -1413,12 +1438,16 @@ __global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const
     if (T.anyg[l]) g_center(sl, ST, T, l, 2, sh, grid);
     {
       const int* off = T.next + l * (nc + 1);
+      CaseCursor cur;
+      bool on = false;
       for (int t = gt; t < __ldg(&off[nc]); t += nth) {
-        const int ci = find_case(off, nc, t);
-        if (!active(ST, ci)) continue;
+        const int prev = cur.ci;
+        const int ci = case_at(off, nc, t, cur);
+        if (ci != prev) on = active(ST, ci);
+        if (!on) continue;
         const CLev& L = sl[ci];
         const CLev& N = sl[nc + ci];
-        const int j = t - __ldg(&off[ci]);
+        const int j = t - cur.lo;
         float v = 0.0f;
         for (int k = L.roff[j]; k < L.roff[j + 1]; ++k) v = fmaf(L.rw[k], __ldcg(&L.res[L.rchild[k]]), v);
         N.rhs[j] = v;
@@ -1437,12 +1466,16 @@ __global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const
     load_levels(cases, nc, l, MAXL, sl);
     {
       const int* off = T.live + l * (nc + 1);
+      CaseCursor cur;
+      bool on = false;
       for (int t = gt; t < __ldg(&off[nc]); t += nth) {
-        const int ci = find_case(off, nc, t);
-        if (!active(ST, ci)) continue;
+        const int prev = cur.ci;
+        const int ci = case_at(off, nc, t, cur);
+        if (ci != prev) on = active(ST, ci);
+        if (!on) continue;
         const CLev& L = sl[ci];
         const CLev& N = sl[nc + ci];
-        const int i = t - __ldg(&off[ci]);
+        const int i = t - cur.lo;
         float s = 0.0f;
         for (int k = L.poff[i]; k < L.poff[i + 1]; ++k) s = fmaf(L.pw[k], __ldcg(&N.x[L.pcol[k]]), s);
         L.x[i] = __ldcg(&L.x[i]) + s;
@@ -1743,7 +1776,7 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     F.rhs0 = F.r32;
   }
   F.ntiles = (h.n[1] * h.n[2] + RT - 1) / RT;  // row tiles (one reduction partial each)
-  if (int e = A.alloc(&F.partials, F.ntiles)) return e;
+  if (int e = A.alloc(&F.partials, (size_t)F.ntiles * (TILE / 32))) return e;
   cs.ngroups0 = M0.groups.rows();
   F.ngroups = cs.ngroups0;
   if (F.ngroups) {
@@ -2228,11 +2261,11 @@ int fill_tab(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
         int nf = 0, nb = 0;
         if (nt && L->jacobi) {
           nf = nb = c == 0 ? 8 * L->n : 0;
-        } else if (nt && c < L->ncolors) {
+        } else if (nt && c < L->ncolors) {  // two rows per item
           const auto& co = B->cases[i]->colors[l];
-          nf = r8(co[c + 1] - co[c]);
+          nf = r8((co[c + 1] - co[c] + 1) / 2);
           const int cb = L->ncolors - 1 - c;
-          nb = r8(co[cb + 1] - co[cb]);
+          nb = r8((co[cb + 1] - co[cb] + 1) / 2);
         }
         fwd[(l * MAXC + c) * w + i + 1] = fwd[(l * MAXC + c) * w + i] + nf;
         bwd[(l * MAXC + c) * w + i + 1] = bwd[(l * MAXC + c) * w + i] + nb;
@@ -2911,13 +2944,19 @@ int cfdg_server_create(cfdg_context* ctx, cfdg_grid* const* grids, int32_t n, in
   }
   S->running.assign(n, 0);
   B->active.assign(n, 0);
+  int e = 0;
   {
     Locks locks(B->grids);
-    if (int e = set_active(B, B->stream)) {
-      cfdg_batch_destroy(B);
-      delete S;
-      return e;
-    }
+    if (B->chunk) cudaGraphExecDestroy(B->chunk);
+    B->chunk = nullptr;
+    B->chunk_it = SERVER_CHUNK_IT;
+    e = ensure_graph(B);
+    if (!e) e = set_active(B, B->stream);
+  }
+  if (e) {
+    cfdg_batch_destroy(B);
+    delete S;
+    return e;
   }
   *out = S;
   return 0;

@@ -236,7 +236,7 @@ void cfdg_server_destroy(cfdg_server *server);
 int cfdg_server_set_stream(cfdg_server *server, void *stream);
 /* Queues pressure::project on grid `grid` for device arrays d_u (F doubles), d_p (N doubles),
  * which must stay valid until the ticket's result is read. */
-/* Iterations per graph chunk (1..64, default 8): requests join and leave the running set
+/* Iterations per graph chunk (1..64, default 4): requests join and leave the running set
  * at chunk boundaries, so shorter chunks lower latency at more host rounds. */
 int cfdg_server_set_chunk(cfdg_server *server, int32_t iterations);
 int cfdg_server_submit(cfdg_server *server, int32_t grid, double *d_u, double *d_p, double dt, double tol,
