@@ -582,7 +582,14 @@ __device__ __forceinline__ void b_outer_resid(const FineCase* FC, MState* ST, co
   FINE_PROLOGUE(S.state == OUTER)
   double acc = 0.0;
   int j, k, rb;
-  if (warp_row(F, lt, warp, j, k, rb)) {
+  if (!S.has_e) {
+    // First outer step: x = 0 exactly, so A x = 0 and r = b_c bit for bit.
+    for (int c = cb + threadIdx.x; c < ce; c += TILE) {
+      const double v = F.bc[c];
+      F.r64[c] = v;
+      acc = __fma_rn(v, v, acc);
+    }
+  } else if (warp_row(F, lt, warp, j, k, rb)) {
     // One warp per row, several cells per lane: the cells' FP64 chains are independent.
     const double* __restrict__ x = F.x64;
     const double* __restrict__ bc = F.bc;

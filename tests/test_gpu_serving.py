@@ -152,3 +152,61 @@ def test_cycle_settings_chunks_and_autotune(pkg):
     assert best == "%d,%d" % tuple(out["choice"])
     for d in dgs:
         d.close()
+
+
+def test_admission_by_hbm_budget_and_failed_requests(pkg):
+    """Grids are admitted against the context's HBM budget (CFDG_ERR_ADMISSION beyond it,
+    room again after a grid closes); a request that fails (E031, an inflow into a sealed
+    region) returns its code with its arrays untouched while the others complete."""
+    torch = pytest.importorskip("torch")
+    case = pkg.synth.case((24, 24, 12), 1.0, preconditioner="multigrid")
+    g = pkg.grid.Grid.build(case)
+    probe = pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed")
+    one = probe.device_bytes()
+    probe.close()
+    assert one > 0
+    ctx = pkg.pressure.Context(0, hbm_budget_bytes=int(2.5 * one))
+    a = pkg.pressure.DeviceGrid(g, ctx=ctx, preconditioner="multigrid", precision="mixed")
+    b = pkg.pressure.DeviceGrid(g, ctx=ctx, preconditioner="multigrid", precision="mixed")
+    with pytest.raises(pkg.pressure.PressureError) as e:
+        pkg.pressure.DeviceGrid(g, ctx=ctx, preconditioner="multigrid", precision="mixed")
+    assert e.value.code == pkg.engine.CFDG_ERR_ADMISSION
+    a.close()
+    c = pkg.pressure.DeviceGrid(g, ctx=ctx, preconditioner="multigrid", precision="mixed")
+    b.close()
+    c.close()
+    ctx.close()
+    # A failing request next to a good one in one server.
+    bad = pkg.grid.Grid.build(pkg.synth.case((24, 12, 8), 1.0, preconditioner="multigrid",
+                                             boxes=[((8, 0, 0), (9, 12, 8))]))
+    good = pkg.grid.Grid.build(pkg.synth.case((32, 16, 16), 1.0, preconditioner="multigrid"))
+    ub, ug = pkg.synth.random_velocity(bad, 1), pkg.synth.random_velocity(good, 2)
+    dgood = pkg.pressure.DeviceGrid(good, preconditioner="multigrid", precision="mixed")
+    au, ap = ug.copy(), np.zeros(good.count)
+    dgood.project(au, ap, 0.1, 1e-8, 10000)
+    dgs = [pkg.pressure.DeviceGrid(bad, preconditioner="multigrid", precision="mixed"), dgood]
+    server = pkg.pressure.Server(dgs, max_active=2)
+    dev = torch.device("cuda", 0)
+    d_u = [torch.from_numpy(ub).to(dev), torch.from_numpy(ug).to(dev)]
+    d_p = [torch.full((bad.count,), 7.0, dtype=torch.float64, device=dev),
+           torch.zeros(good.count, dtype=torch.float64, device=dev)]
+    torch.cuda.synchronize()
+    tickets = [server.submit(i, d_u[i].data_ptr(), d_p[i].data_ptr(), 0.1, 1e-8, 10000) for i in range(2)]
+    done = {}
+    for _ in range(100000):
+        server.progress()
+        for i, t in enumerate(tickets):
+            if i not in done:
+                r = server.result(t)
+                if r is not None:
+                    done[i] = r
+        if len(done) == 2:
+            break
+    assert done[0][0] == 31 and done[1][0] == 0
+    assert np.array_equal(bits(d_u[0].cpu().numpy()), bits(ub))
+    assert np.all(d_p[0].cpu().numpy() == 7.0)
+    assert np.array_equal(bits(d_u[1].cpu().numpy()), bits(au))
+    assert np.array_equal(bits(d_p[1].cpu().numpy()), bits(ap))
+    server.close()
+    for d in dgs:
+        d.close()
