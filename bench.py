@@ -655,7 +655,7 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
                    "every request (on the server's stream)", "steps": srv_steps}
     kernels = {}
     for name, which, reps in (("rb_half_sweep_fp32", 0, 20), ("operator_fp32", 1, 20),
-                              ("coarse_levels_cluster", 2, 10), ("vcycle_fp32", 3, 5)):
+                              ("coarse_levels", 2, 10), ("vcycle_fp32", 3, 5)):
         ms, b = bt.time_kernel(which, reps)
         kernels[name] = {"ms": round(ms, 4), "GB/s": round(b / ms / 1e6, 1) if b else None, "algorithmic_bytes": b}
     bt.close()
@@ -908,7 +908,7 @@ def run_engine(args):
             bt.set_stream(stream.cuda_stream)
             form.step(0)  # leave every case with live vectors
         for name, which, reps in (("rb_half_sweep_fp32", 0, 50), ("operator_fp32", 1, 50),
-                                  ("coarse_levels_cluster", 2, 20), ("vcycle_fp32", 3, 10)):
+                                  ("coarse_levels", 2, 20), ("vcycle_fp32", 3, 10)):
             ms, b = bt.time_kernel(which, reps)
             kernels[name] = {"ms": round(ms, 4), "GB/s": round(b / ms / 1e6, 1) if b else None,
                              "algorithmic_bytes": b}

@@ -203,7 +203,7 @@ int cfdg_batch_project(cfdg_batch *batch, double *const *u, double *const *p, co
                        uint64_t max_iter, cfdg_poll_fn poll, void *poll_ctx, cfdg_info *infos, int32_t *codes);
 /* Times one unit of the batch's work `reps` times with CUDA events on the batch's
  * stream, every case in its inner-iteration state: which = 0 one red-black half sweep
- * over all fine levels, 1 the FP32 operator, 2 the coarse-level cluster kernel, 3 one
+ * over all fine levels, 1 the FP32 operator, 2 all coarse levels (one cooperative launch), 3 one
  * V-cycle. Reports the mean duration and the unit's algorithmic bytes (0 when not
  * stated). Diagnostic; no reference counterpart. */
 int cfdg_batch_time_kernel(cfdg_batch *batch, int32_t which, int32_t reps, double *ms_per_launch,
