@@ -842,6 +842,97 @@ def run_uneven(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     return 0
 
 
+STEP_WORKLOAD = ("128x128x64 grid, dx=2 m, 12 seeded box buildings, laminar inflow 5 m/s, open x / wall y,z; "
+                 "SSPRK2 time steps of dt=0.1 s from the projected initial flow, two projections per step "
+                 "(multigrid PCG to 1e-8), u and p resident on the device")
+
+
+def run_stepping(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
+    """Survey configuration 2 as true laminar time stepping (cfdg_step_device)."""
+    K, W = args.steps, args.warmup
+    case = workload_case(pkg)
+    g = pkg.grid.Grid.build(case)
+
+    def stepper(precision):
+        d = pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision=precision)
+        d.set_stream(stream.cuda_stream)
+        d.set_flow(case)
+        u0, p0 = g.initial_velocity(), torch.zeros(g.count, dtype=torch.float64).numpy()
+        d.project(u0, p0, DT, TOL, MAX_IT)  # the initial projection (solver.rs:1437)
+        return d, torch.from_numpy(u0).to(dev), torch.from_numpy(p0).to(dev)
+
+    d, d_u, d_p = stepper("mixed")
+    for _ in range(W):
+        d.step_device(d_u.data_ptr(), d_p.data_ptr(), DT, TOL, MAX_IT)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches0 = L.cfdg_launch_count()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    its = []
+    ev0.record(stream)
+    for _ in range(K):
+        flush.zero_()
+        its.append(d.step_device(d_u.data_ptr(), d_p.data_ptr(), DT, TOL, MAX_IT).iterations)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = L.cfdg_launch_count() - launches0
+    total_ms = ev0.elapsed_time(ev1)
+    if dist:
+        total_ms = max_over_ranks(total_ms, dist, dev)
+    value = world * 2 * K / (total_ms / 1e3)
+    # End to end: u and p from pinned host memory each step, back after it.
+    h_u = torch.from_numpy(d_u.cpu().numpy()).pin_memory()
+    h_p = torch.from_numpy(d_p.cpu().numpy()).pin_memory()
+    e2e_steps = max(1, min(K, 3))
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(e2e_steps):
+        d_u.copy_(h_u, non_blocking=True)
+        d_p.copy_(h_p, non_blocking=True)
+        d.step_device(d_u.data_ptr(), d_p.data_ptr(), DT, TOL, MAX_IT)
+        h_u.copy_(d_u, non_blocking=True)
+        h_p.copy_(d_p, non_blocking=True)
+    b.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = a.elapsed_time(b)
+    io = 8 * (g.n_faces + g.count)
+    d.close()
+    plain = None
+    if not args.skip_plain:
+        dp_, pu, pp = stepper("plain")
+        dp_.step_device(pu.data_ptr(), pp.data_ptr(), DT, TOL, MAX_IT)
+        torch.cuda.synchronize()
+        a.record(stream)
+        pits = [dp_.step_device(pu.data_ptr(), pp.data_ptr(), DT, TOL, MAX_IT).iterations for _ in range(2)]
+        b.record(stream)
+        torch.cuda.synchronize()
+        pms = a.elapsed_time(b)
+        plain = {"value": round(world * 4 / (pms / 1e3), 4), "unit": UNIT, "ms_per_step": round(pms / 2, 2),
+                 "iterations_per_step": pits}
+        dp_.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+                "ms_per_step": round(total_ms / K, 4), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                "config": {"workload": STEP_WORKLOAD, "form": "laminar SSPRK2 stepping, mixed-form projections",
+                           "cells": g.count, "faces": g.n_faces, "l2": "256 MiB buffer written before every step",
+                           "parallelism": f"replicas x{world}"},
+                "time_steps_per_s": round(world * K / (total_ms / 1e3), 4),
+                "iterations_per_step_mean": round(statistics.mean(its), 2),
+                "e2e": {"value": round(world * 2 * e2e_steps / (e2e_ms / 1e3), 4), "unit": UNIT,
+                        "h2d_bytes_per_step": io, "d2h_bytes_per_step": io},
+                "plain_fp64": plain, "gpu_launches": int(launches), "clocks": clk}
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_engine(args):
     import torch
 
@@ -866,8 +957,8 @@ def run_engine(args):
     flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MiB > L2 (129 MB)
     K, W = args.steps, args.warmup
     L = pkg.engine.load()
-    if args.form in ("serving", "uneven"):
-        run = run_serving if args.form == "serving" else run_uneven
+    if args.form in ("serving", "uneven", "stepping"):
+        run = {"serving": run_serving, "uneven": run_uneven, "stepping": run_stepping}[args.form]
         rc = run(args, pkg, torch, dev, stream, flush, rank, world, dist, L)
         if dist:
             dist.destroy_process_group()
@@ -974,7 +1065,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--form", default="serving", choices=["plain", "mixed", "batched", "serving", "uneven", "large"])
+    ap.add_argument("--form", default="serving",
+                    choices=["plain", "mixed", "batched", "serving", "uneven", "large", "stepping"])
     ap.add_argument("--slots", type=int, default=0, help="serving: cases on the GPU at once (0: all)")
     ap.add_argument("--requests", type=int, default=520, help="serving: open-loop requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")

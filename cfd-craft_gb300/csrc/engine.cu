@@ -1385,6 +1385,169 @@ int check_grid(cfdg_grid* G) {
   return 0;
 }
 
+// ----------------------------------------------------------------- laminar time stepping
+// One SSPRK2 step of the laminar flow with a projection per stage (solver.rs:879-960,
+// flow_euler solver.rs:671-732): u1 = P(u + dt (R(u) - grad p)), u2 = P(u1 + dt (R(u1) -
+// grad p1)), u <- (u + u2) / 2 with the fixed faces re-applied, p <- p2. R is the steady
+// momentum right-hand side of laminar flow with the default donor-cell advection
+// (flow.rs:426-525). Every face evaluates the reference's expression in its order
+// (-fmad=false), so a step is bit-identical to the reference algorithm on the same grid.
+struct FlowDev {
+  int n[3];
+  long long face_off[3];
+  int fdim[3][3];
+  double dx[3], size[3], vel[3], nu, acc[3];
+  int bnd[3];
+  const uint8_t* kind;
+  const int *lo, *hi;
+  const double* dist;
+  const uint8_t* fluid;
+};
+
+__device__ __forceinline__ long long fface(const FlowDev& D, int a, int i, int j, int k) {
+  return D.face_off[a] + ((long long)k * D.fdim[a][1] + j) * D.fdim[a][0] + i;
+}
+
+// grid.rs:631-645 cell_velocity, one array per axis.
+__global__ void k_cell_velocity(FlowDev D, const double* __restrict__ u, double* __restrict__ cu, int N) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+    const int i = c % D.n[0], j = (c / D.n[0]) % D.n[1], k = c / (D.n[0] * D.n[1]);
+    const int q[3] = {i, j, k};
+    for (int a = 0; a < 3; ++a) {
+      if (!D.fluid[c]) {
+        cu[(long long)a * N + c] = 0.0;
+        continue;
+      }
+      int p[3] = {q[0], q[1], q[2]};
+      const double lo = u[fface(D, a, p[0], p[1], p[2])];
+      p[a] += 1;
+      const double hi = u[fface(D, a, p[0], p[1], p[2])];
+      cu[(long long)a * N + c] = 0.5 * (lo + hi);
+    }
+  }
+}
+
+// flow.rs:66-154 ghost_values, laminar flow without moving walls.
+__device__ __forceinline__ double ghost(const FlowDev& D, int a, const double center[3], int d, int side,
+                                        double value) {
+  const bool at_domain = side < 0 ? center[d] < D.dx[d] : center[d] > D.size[d] - D.dx[d];
+  const int bc = D.bnd[d];
+  if (at_domain && bc == 3) return value;  // slip
+  if (at_domain && bc == 1) {              // open
+    const double speed = D.vel[d] * (double)side;
+    if (speed < -1e-12) return 2.0 * D.vel[a] - value;
+    return value;
+  }
+  const double target = 0.0;
+  return 2.0 * target - value;
+}
+
+// flow.rs:426-525 momentum_rhs (laminar, donor cell), then u + dt (rhs - grad p) and the
+// fixed face values (solver.rs:695-719, grid.rs:683-691).
+__global__ void k_momentum_update(FlowDev D, const double* __restrict__ u, const double* __restrict__ p,
+                                  const double* __restrict__ cu, double dt, double* __restrict__ out, long long F,
+                                  int N) {
+  for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < F; f += (long long)gridDim.x * blockDim.x) {
+    const int a = f >= D.face_off[2] ? 2 : (f >= D.face_off[1] ? 1 : 0);
+    long long r = f - D.face_off[a];
+    const int q[3] = {(int)(r % D.fdim[a][0]), (int)((r / D.fdim[a][0]) % D.fdim[a][1]),
+                      (int)(r / ((long long)D.fdim[a][0] * D.fdim[a][1]))};
+    const uint8_t kd = D.kind[f];
+    if (kd == WALL || kd == SLIP || kd == BLOCKED) {
+      out[f] = 0.0;
+      continue;
+    }
+    if (kd == INLET) {
+      out[f] = D.vel[a];
+      continue;
+    }
+    const int lo = D.lo[f], hi = D.hi[f];
+    double velocity[3];
+    for (int d = 0; d < 3; ++d) {
+      if (lo >= 0 && hi >= 0) velocity[d] = 0.5 * (cu[(long long)d * N + lo] + cu[(long long)d * N + hi]);
+      else if (lo >= 0) velocity[d] = cu[(long long)d * N + lo];
+      else if (hi >= 0) velocity[d] = cu[(long long)d * N + hi];
+      else velocity[d] = 0.0;
+    }
+    double center[3];
+    for (int d = 0; d < 3; ++d) center[d] = ((double)q[d] + (d == a ? 0.0 : 0.5)) * D.dx[d];
+    const double uf = u[f];
+    double rhs = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      double vlo, vhi;
+      for (int side = 0; side < 2; ++side) {
+        int pq[3] = {q[0], q[1], q[2]};
+        pq[d] += side ? 1 : -1;
+        const bool exists = pq[d] >= 0 && pq[d] < D.fdim[a][d];
+        double v;
+        if (exists) {
+          const long long nb = fface(D, a, pq[0], pq[1], pq[2]);
+          const uint8_t nk = D.kind[nb];
+          v = ((nk == WALL || nk == BLOCKED) && d != a) ? ghost(D, a, center, d, side ? 1 : -1, uf) : u[nb];
+        } else {
+          v = d == a ? uf : ghost(D, a, center, d, side ? 1 : -1, uf);
+        }
+        if (side) vhi = v;
+        else vlo = v;
+      }
+      rhs = rhs - velocity[d] * (velocity[d] >= 0.0 ? (uf - vlo) / D.dx[d] : (vhi - uf) / D.dx[d]);
+      const double mu = D.nu + 0.0;
+      rhs = rhs + (mu * (vhi - uf) - mu * (uf - vlo)) / (D.dx[d] * D.dx[d]);
+    }
+    rhs = rhs + D.acc[a];
+    rhs = rhs + (lo >= 0 && hi >= 0 ? 0.5 * (0.0 + 0.0) : 0.0);  // the RANS cross term, zero here
+    double grad;
+    if (kd == INTERIOR) grad = (p[hi] - p[lo]) / D.dist[f];
+    else grad = lo >= 0 ? -p[lo] / D.dist[f] : p[hi] / D.dist[f];  // outlet
+    out[f] = uf + dt * (rhs - grad);
+  }
+}
+
+// SSPRK2 combination u <- (u + u2) / 2, then the fixed face values (solver.rs:937-946).
+__global__ void k_ssprk_combine(FlowDev D, double* __restrict__ u, const double* __restrict__ u2, long long F) {
+  for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < F; f += (long long)gridDim.x * blockDim.x) {
+    const uint8_t kd = D.kind[f];
+    const int a = f >= D.face_off[2] ? 2 : (f >= D.face_off[1] ? 1 : 0);
+    if (kd == WALL || kd == SLIP || kd == BLOCKED) u[f] = 0.0;
+    else if (kd == INLET) u[f] = D.vel[a];
+    else u[f] = 0.5 * (u[f] + u2[f]);
+  }
+}
+
+FlowDev flow_dev(cfdg_grid* G) {
+  FlowDev D{};
+  for (int a = 0; a < 3; ++a) {
+    D.n[a] = G->h.n[a];
+    D.face_off[a] = G->g.face_off[a];
+    for (int d = 0; d < 3; ++d) D.fdim[a][d] = G->g.fdim[a][d];
+    D.dx[a] = G->h.dx[a];
+    D.size[a] = G->flow_size[a];
+    D.vel[a] = G->flow_vel[a];
+    D.acc[a] = G->flow_acc[a];
+    D.bnd[a] = G->flow_bnd[a];
+  }
+  D.nu = G->flow_nu;
+  D.kind = G->d_kind;
+  D.lo = G->d_lo;
+  D.hi = G->d_hi;
+  D.dist = G->d_dist;
+  D.fluid = G->d_fluid;
+  return D;
+}
+
+// One stage: out = u + dt (R(u) - grad p) with the fixed faces, then the projection of
+// out with p1 (= p on entry) accumulating the pressure.
+int flow_stage(cfdg_grid* G, const FlowDev& D, const double* u, double* out, double* p1, double dt, double tol,
+               uint64_t max_iter, const Poller& P, cfdg_info* info) {
+  const int N = (int)G->h.cells;
+  const long long F = G->h.faces;
+  cudaStream_t s = G->stream;
+  k_cell_velocity<<<grid_blocks(N), BLOCK, 0, s>>>(D, u, G->st_cu, N); tick(G);
+  k_momentum_update<<<grid_blocks((int)std::min<long long>(F, 1LL << 30)), BLOCK, 0, s>>>(D, u, p1, G->st_cu, dt, out, F, N);
+  tick(G);
+  return project_device(G, out, p1, dt, tol, max_iter, P, info);
+}
+
 }  // namespace
 
 namespace cfdg {
@@ -1650,6 +1813,88 @@ int cfdg_grid_configure(cfdg_grid* G, int32_t preconditioner, int32_t precision)
   if (preconditioner != G->preconditioner) reset_chunk(G);
   G->preconditioner = preconditioner;
   G->precision = precision;
+  return 0;
+}
+
+int cfdg_grid_set_flow(cfdg_grid* G, const cfdg_flow_desc* flow) {
+  if (int e = check_grid(G)) return e;
+  if (!flow) return fail(CFDG_ERR_INVALID, "null flow");
+  for (int a = 0; a < 3; ++a)
+    if (flow->boundary[a] == 0 || flow->boundary[a] == 4)
+      return fail(CFDG_ERR_UNSUPPORTED, "laminar stepping supports open, wall and slip boundaries");
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  if (!G->st_cu) {
+    Arena& A = G->arena;
+    if (int e = A.alloc(&G->st_cu, 3 * (size_t)G->h.cells)) return e;
+    if (int e = A.alloc(&G->st_v, (size_t)G->h.faces)) return e;
+    if (int e = A.alloc(&G->st_v2, (size_t)G->h.faces)) return e;
+    if (int e = A.alloc(&G->st_p1, (size_t)G->h.cells)) return e;
+  }
+  for (int a = 0; a < 3; ++a) {
+    G->flow_bnd[a] = flow->boundary[a];
+    G->flow_size[a] = flow->size_m[a];
+    G->flow_vel[a] = flow->velocity[a];
+    G->flow_acc[a] = flow->acceleration[a];
+  }
+  G->flow_nu = flow->viscosity;
+  G->has_flow = true;
+  return 0;
+}
+
+int cfdg_step_device(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol, uint64_t max_iter,
+                     cfdg_poll_fn poll, void* poll_ctx, cfdg_info* info) {
+  if (int e = check_grid(G)) return e;
+  if (!d_u || !d_p) return fail(CFDG_ERR_INVALID, "null u or p");
+  std::lock_guard<std::mutex> lk(G->mu);
+  if (!G->has_flow) return fail(CFDG_ERR_INVALID, "cfdg_grid_set_flow has not been called for this grid");
+  CU(cudaSetDevice(G->ctx->device));
+  cudaStream_t s = G->stream;
+  Poller P;
+  P.fn = poll;
+  P.ctx = poll_ctx;
+  const FlowDev D = flow_dev(G);
+  const size_t N = G->h.cells;
+  cfdg_info i1{}, i2{};
+  // Stage outputs live in the grid's buffers until the step succeeds (the caller's u and
+  // p stay unchanged on any error, as solver::step builds the next state beside it).
+  CU(cudaMemcpyAsync(G->st_p1, d_p, N * 8, cudaMemcpyDeviceToDevice, s));
+  if (int e = flow_stage(G, D, d_u, G->st_v, G->st_p1, dt, tol, max_iter, P, &i1)) return e;
+  if (int e = flow_stage(G, D, G->st_v, G->st_v2, G->st_p1, dt, tol, max_iter, P, &i2)) return e;
+  k_ssprk_combine<<<grid_blocks((int)std::min<long long>(G->h.faces, 1LL << 30)), BLOCK, 0, s>>>(D, d_u, G->st_v2,
+                                                                                                 G->h.faces);
+  tick(G);
+  CU(cudaMemcpyAsync(d_p, G->st_p1, N * 8, cudaMemcpyDeviceToDevice, s));
+  CU(cudaStreamSynchronize(s));
+  if (info) {
+    *info = i2;
+    info->iterations = i1.iterations + i2.iterations;
+    info->work_units = i1.work_units + i2.work_units;
+    info->operator_applications = i1.operator_applications + i2.operator_applications;
+    info->preconditioner_applications = i1.preconditioner_applications + i2.preconditioner_applications;
+    info->true_residual_checks = i1.true_residual_checks + i2.true_residual_checks;
+    info->device_seconds = i1.device_seconds + i2.device_seconds;
+  }
+  return 0;
+}
+
+int cfdg_debug_momentum_update(cfdg_grid* G, const double* u, const double* p, double dt, double* out) {
+  if (int e = check_grid(G)) return e;
+  if (!u || !p || !out) return fail(CFDG_ERR_INVALID, "null array");
+  std::lock_guard<std::mutex> lk(G->mu);
+  if (!G->has_flow) return fail(CFDG_ERR_INVALID, "cfdg_grid_set_flow has not been called for this grid");
+  CU(cudaSetDevice(G->ctx->device));
+  cudaStream_t s = G->stream;
+  const size_t N = G->h.cells, F = G->h.faces;
+  CU(cudaMemcpyAsync(G->st_v2, u, F * 8, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(G->st_p1, p, N * 8, cudaMemcpyHostToDevice, s));
+  const FlowDev D = flow_dev(G);
+  k_cell_velocity<<<grid_blocks((int)N), BLOCK, 0, s>>>(D, G->st_v2, G->st_cu, (int)N); tick(G);
+  k_momentum_update<<<grid_blocks((int)std::min<size_t>(F, 1u << 30)), BLOCK, 0, s>>>(D, G->st_v2, G->st_p1, G->st_cu, dt,
+                                                                                     G->st_v, (long long)F, (int)N);
+  tick(G);
+  CU(cudaMemcpyAsync(out, G->st_v, F * 8, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
   return 0;
 }
 

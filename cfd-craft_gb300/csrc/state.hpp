@@ -190,6 +190,12 @@ struct cfdg_grid {
   // Mixed form: V-cycle sweeps before and after the coarse correction on level 0 and on
   // the coarse levels (cfdg_grid_set_cycle); a batch takes them from its grids.
   int mx_nu0 = 2, mx_nuc = 2;
+  // Laminar time stepping (cfdg_grid_set_flow / cfdg_step_device): the case flow and the
+  // stage buffers (cell velocities, the two stage velocities, the stage pressure).
+  bool has_flow = false;
+  int flow_bnd[3] = {0, 0, 0};
+  double flow_size[3] = {0, 0, 0}, flow_vel[3] = {0, 0, 0}, flow_nu = 0, flow_acc[3] = {0, 0, 0};
+  double *st_cu = nullptr, *st_v = nullptr, *st_v2 = nullptr, *st_p1 = nullptr;
   uint64_t sig_version = ~0ull;
 };
 

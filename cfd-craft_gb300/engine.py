@@ -29,7 +29,7 @@ EXPORTS = (
     "cfdg_launch_count", "cfdg_debug_time_kernel", "cfdg_residual_norm_noalloc", "cfdg_batch_create",
     "cfdg_batch_destroy", "cfdg_batch_set_stream", "cfdg_batch_size", "cfdg_batch_project", "cfdg_batch_project_device",
     "cfdg_batch_time_kernel", "cfdg_batch_stats_json", "cfdg_server_create", "cfdg_server_destroy", "cfdg_server_set_stream",
-    "cfdg_server_submit", "cfdg_server_progress", "cfdg_server_result", "cfdg_server_pending", "cfdg_server_stats_json", "cfdg_server_set_chunk", "cfdg_grid_set_cycle",
+    "cfdg_server_submit", "cfdg_server_progress", "cfdg_server_result", "cfdg_server_pending", "cfdg_server_stats_json", "cfdg_server_set_chunk", "cfdg_grid_set_cycle", "cfdg_grid_set_flow", "cfdg_step_device", "cfdg_debug_momentum_update",
 )
 
 
@@ -80,6 +80,18 @@ class Info(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class FlowDesc(C.Structure):
+    """cfdg_flow_desc: the laminar flow terms of a case (cfdg_grid_set_flow)."""
+
+    _fields_ = [
+        ("boundary", C.c_int32 * 3),
+        ("size_m", C.c_double * 3),
+        ("velocity", C.c_double * 3),
+        ("viscosity", C.c_double),
+        ("acceleration", C.c_double * 3),
+    ]
 
 
 POLL = C.CFUNCTYPE(C.c_int, C.c_void_p)
@@ -141,6 +153,9 @@ def load(path: str = LIB_PATH):
         L.cfdg_server_stats_json.restype = C.c_int64
         L.cfdg_server_set_chunk.argtypes = [P, C.c_int32]
         L.cfdg_grid_set_cycle.argtypes = [P, C.c_int32, C.c_int32]
+        L.cfdg_grid_set_flow.argtypes = [P, C.POINTER(FlowDesc)]
+        L.cfdg_step_device.argtypes = [P, P, P, C.c_double, C.c_double, C.c_uint64, POLL, P, C.POINTER(Info)]
+        L.cfdg_debug_momentum_update.argtypes = [P, P, P, C.c_double, P]
         PP = C.POINTER(C.c_void_p)
         L.cfdg_batch_project.argtypes = [P, PP, PP, C.POINTER(C.c_double), C.c_double, C.c_uint64, POLL, P,
                                          C.POINTER(Info), C.POINTER(C.c_int32)]

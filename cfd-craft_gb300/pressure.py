@@ -183,6 +183,38 @@ class DeviceGrid:
         d = None if distance is None else np.ascontiguousarray(distance, np.float64)
         self._check(self.L.cfdg_grid_update_faces(self.h, None if a is None else _vp(a), None if d is None else _vp(d)))
 
+    def set_flow(self, case: dict):
+        """The case's laminar flow terms for step_device (cfdg_grid_set_flow)."""
+        bnd = {"periodic": 0, "open": 1, "wall": 2, "slip": 3, "ground_open_top": 4}
+        flow = case["flow"]
+        if flow["kind"] != "laminar":
+            raise PressureError(E.CFDG_ERR_UNSUPPORTED, "laminar stepping: the case flow is not laminar")
+        d = E.FlowDesc()
+        for a in range(3):
+            d.boundary[a] = bnd[case["boundaries"]["xyz"[a]]]
+            d.size_m[a] = float(case["domain"]["size_m"][a])
+            d.velocity[a] = float(flow.get("initial_velocity_m_s", [0.0, 0.0, 0.0])[a])
+            d.acceleration[a] = float(flow.get("acceleration_m_s2", [0.0, 0.0, 0.0])[a])
+        d.viscosity = float(flow.get("viscosity_m2_s", 1.5e-5))
+        self._check(self.L.cfdg_grid_set_flow(self.h, C.byref(d)))
+
+    def step_device(self, u_ptr: int, p_ptr: int, dt, tol, max_iter, control=None) -> LinearInfo:
+        """One SSPRK2 step with a projection per stage, in place on device arrays (cfdg_step_device)."""
+        info = E.Info()
+        cb = self._poll_fn(control)
+        rc = self.L.cfdg_step_device(self.h, C.c_void_p(u_ptr), C.c_void_p(p_ptr), float(dt), float(tol),
+                                     int(max_iter), cb, None, C.byref(info))
+        self._check(rc)
+        return LinearInfo(info.iterations, info.relative_residual, info.as_dict())
+
+    def momentum_update(self, u, p, dt):
+        """u + dt (R(u) - grad p) with the fixed face values, before a stage's projection."""
+        u = np.ascontiguousarray(u, np.float64)
+        p = np.ascontiguousarray(p, np.float64)
+        out = np.zeros_like(u)
+        self._check(self.L.cfdg_debug_momentum_update(self.h, _vp(u), _vp(p), float(dt), _vp(out)))
+        return out
+
     def set_cycle(self, nu_fine: int, nu_coarse: int):
         """Mixed form: V-cycle sweeps on level 0 and on the coarse levels (cfdg_grid_set_cycle)."""
         self._check(self.L.cfdg_grid_set_cycle(self.h, int(nu_fine), int(nu_coarse)))

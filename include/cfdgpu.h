@@ -139,6 +139,28 @@ int cfdg_grid_update_faces(cfdg_grid *grid, const double *face_area, const doubl
 
 /* Switches the preconditioner or the arithmetic form of an open grid. */
 int cfdg_grid_configure(cfdg_grid *grid, int32_t preconditioner, int32_t precision);
+/* ------------------------------------------------------------------ laminar time stepping
+ * The flow terms of the case that the projection does not read (case.rs Flow::Laminar,
+ * boundaries, domain size), for cfdg_step_device. Open, wall and slip boundaries. */
+typedef struct {
+  int32_t boundary[3];     /* per axis: 1 open, 2 wall, 3 slip (case.rs Boundary) */
+  double size_m[3];        /* domain size */
+  double velocity[3];      /* initial_velocity_m_s: the inflow (Flow::vector) */
+  double viscosity;        /* viscosity_m2_s */
+  double acceleration[3];  /* acceleration_m_s2 */
+} cfdg_flow_desc;
+int cfdg_grid_set_flow(cfdg_grid *grid, const cfdg_flow_desc *flow);
+/* One SSPRK2 step of laminar flow with a projection per stage, in place on device arrays
+ * d_u (F) and d_p (N) (solver.rs:879-960 with flow_euler solver.rs:671-732; the momentum
+ * right-hand side flow.rs:426-525 with donor-cell advection). Each stage projects in the
+ * grid's precision (plain: bit-identical to the reference algorithm). On any error u and
+ * p are unchanged. info: the second projection's, with iterations and work summed. */
+int cfdg_step_device(cfdg_grid *grid, double *d_u, double *d_p, double dt, double tol, uint64_t max_iter,
+                     cfdg_poll_fn poll, void *poll_ctx, cfdg_info *info);
+/* Diagnostic: one stage's velocity before its projection, out = u + dt (R(u) - grad p) with
+ * the fixed face values, on host arrays (F, N, F doubles). No reference counterpart. */
+int cfdg_debug_momentum_update(cfdg_grid *grid, const double *u, const double *p, double dt, double *out);
+
 /* Mixed form: Gauss-Seidel sweeps before and after the coarse correction of the V-cycle,
  * on level 0 and on the coarse levels (1..4 each; default 2 and 2, the reference's
  * V(2,2)). Batches and servers created afterwards take the counts from their grids (all

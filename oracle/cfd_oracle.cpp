@@ -449,7 +449,10 @@ struct Hierarchy {
 struct Grid {
   size_t n[3];
   double dx[3];
+  double size_m[3];  // the case's domain size (ghost_values' boundary test)
   double volume;
+  double viscosity = 1.5e-5;            // laminar kinematic viscosity (case flow)
+  double acceleration[3] = {0, 0, 0};   // laminar body acceleration (case flow)
   int boundary[3];
   Flow flow;
   int preconditioner = 0;  // 0 ic0, 1 multigrid
@@ -477,6 +480,7 @@ static int grid_build(Grid& g, const size_t n[3], const double size_m[3], const 
   for (int a = 0; a < 3; ++a) {
     g.n[a] = n[a];
     g.dx[a] = size_m[a] / (double)n[a];
+    g.size_m[a] = size_m[a];
     g.boundary[a] = boundary[a];
   }
   g.flow = flow;
@@ -1457,6 +1461,160 @@ void ora_gradient(void* gp, const double* p, double* out) {
     else out[f] = 0.0;
   }
 }
+}  // extern "C" (momentum below is C++)
+
+// ---------------------------------------------------------------- laminar momentum (next row)
+// grid.rs:593-607 face_at: the axis-a face at position q; periodic axes wrap.
+static size_t face_at(const Grid& g, int a, long q[3]) {
+  for (int d = 0; d < 3; ++d) {
+    if (g.boundary[d] == B_PERIODIC) {
+      long n = (long)g.n[d];
+      q[d] = ((q[d] % n) + n) % n;
+    } else if (q[d] < 0 || q[d] >= (long)g.face_dims[a][d]) {
+      return NONE;
+    }
+  }
+  return g.offsets[a] + ((size_t)q[2] * g.face_dims[a][1] + (size_t)q[1]) * g.face_dims[a][0] + (size_t)q[0];
+}
+
+// flow.rs:66-154 ghost_values for laminar flow without moving walls: slip and outflow
+// mirror the face value, an inflowing open side reflects about the inflow, walls and
+// buildings reflect about zero.
+static double ghost_value(const Grid& g, const Face& f, int d, int side, double value) {
+  const bool at_domain = side < 0 ? f.center[d] < g.dx[d] : f.center[d] > g.size_m[d] - g.dx[d];
+  const int bc = g.boundary[d];
+  if (at_domain && bc == B_SLIP) return value;
+  if (at_domain && bc == B_OPEN) {
+    double v[3];
+    g.flow.vector(f.center[2], v);
+    const double speed = v[d] * (double)side;
+    if (speed < -1e-12) {
+      const double inflow = v[f.axis];
+      return 2.0 * inflow - value;
+    }
+    return value;
+  }
+  const double target = 0.0;
+  return 2.0 * target - value;
+}
+
+// flow.rs:156-180 sample
+static double sample(const Grid& g, size_t fi, int d, int side, size_t nb, const double* u) {
+  const Face& f = g.faces[fi];
+  if (nb != NONE) {
+    const int k = g.faces[nb].kind;
+    if ((k == K_WALL || k == K_BLOCKED) && d != f.axis) return ghost_value(g, f, d, side, u[fi]);
+    return u[nb];
+  }
+  if (d == f.axis) return u[fi];
+  return ghost_value(g, f, d, side, u[fi]);
+}
+
+// flow.rs:426-525 momentum_rhs, laminar flow with the default donor-cell advection and no
+// vegetation: zero on faces without an equation.
+static int momentum_rhs(const Grid& g, const double* u, double* out) {
+  if (g.flow.kind == F_RANS) return UNSUPPORTED;
+  const size_t N = g.count();
+  // grid.rs:631-645 cell_velocity
+  std::vector<std::array<double, 3>> cu(N);
+  for (size_t i = 0; i < N; ++i)
+    for (int a = 0; a < 3; ++a)
+      cu[i][a] = g.fluid[i] ? 0.5 * (u[g.cell_faces[i][a * 2]] + u[g.cell_faces[i][a * 2 + 1]]) : 0.0;
+  const double nu = g.viscosity;
+  for (size_t fi = 0; fi < g.faces.size(); ++fi) {
+    const Face& f = g.faces[fi];
+    if (f.kind != K_INTERIOR && f.kind != K_OUTLET) {
+      out[fi] = 0.0;
+      continue;
+    }
+    double velocity[3];
+    for (int a = 0; a < 3; ++a) {
+      if (f.lo != NONE && f.hi != NONE) velocity[a] = 0.5 * (cu[f.lo][a] + cu[f.hi][a]);
+      else if (f.lo != NONE) velocity[a] = cu[f.lo][a];
+      else if (f.hi != NONE) velocity[a] = cu[f.hi][a];
+      else velocity[a] = 0.0;
+    }
+    double rhs = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      long ql[3] = {(long)f.coord[0], (long)f.coord[1], (long)f.coord[2]};
+      long qh[3] = {(long)f.coord[0], (long)f.coord[1], (long)f.coord[2]};
+      ql[d] -= 1;
+      qh[d] += 1;
+      const size_t lo_face = face_at(g, f.axis, ql), hi_face = face_at(g, f.axis, qh);
+      const double lo = sample(g, fi, d, -1, lo_face, u);
+      const double hi = sample(g, fi, d, 1, hi_face, u);
+      rhs = rhs - velocity[d] * (velocity[d] >= 0.0 ? (u[fi] - lo) / g.dx[d] : (hi - u[fi]) / g.dx[d]);
+      const double mu = nu + 0.0;
+      const double mu_lo = mu, mu_hi = mu;
+      rhs = rhs + (mu_hi * (hi - u[fi]) - mu_lo * (u[fi] - lo)) / (g.dx[d] * g.dx[d]);
+    }
+    rhs = rhs + g.acceleration[f.axis];
+    rhs = rhs + (f.lo != NONE && f.hi != NONE ? 0.5 * (0.0 + 0.0) : 0.0);  // the RANS cross term, zero
+    out[fi] = rhs;
+  }
+  return OK;
+}
+
+static void enforce_velocity(const Grid& g, double* u) {
+  for (size_t f = 0; f < g.faces.size(); ++f) {
+    const Face& x = g.faces[f];
+    if (x.kind == K_WALL || x.kind == K_SLIP || x.kind == K_BLOCKED) u[f] = 0.0;
+    else if (x.kind == K_INLET) {
+      double v[3];
+      g.flow.vector(x.center[2], v);
+      u[f] = v[x.axis];
+    }
+  }
+}
+
+// solver.rs:671-732 flow_euler (explicit algorithm, no vegetation drag).
+static int flow_euler(Grid& g, const double* u, const double* p, double dt, double tol, uint64_t max,
+                      std::vector<double>& v, std::vector<double>& pp, uint64_t& iterations) {
+  const size_t F = g.faces.size();
+  std::vector<double> rhs(F), grad(F);
+  if (int c = momentum_rhs(g, u, rhs.data())) return c;
+  for (size_t f = 0; f < F; ++f) {
+    const Face& x = g.faces[f];
+    if (x.kind == K_INTERIOR) grad[f] = (p[x.hi] - p[x.lo]) / x.distance;
+    else if (x.kind == K_OUTLET) grad[f] = x.lo != NONE ? -p[x.lo] / x.distance : p[x.hi] / x.distance;
+    else grad[f] = 0.0;
+  }
+  v.resize(F);
+  for (size_t f = 0; f < F; ++f) v[f] = u[f] + dt * (rhs[f] - grad[f]);
+  enforce_velocity(g, v.data());
+  pp.assign(p, p + g.count());
+  Control control;
+  Info info;
+  if (int c = project(g, v.data(), pp.data(), dt, tol, max, control, info)) return c;
+  iterations += info.iterations;
+  enforce_velocity(g, v.data());
+  return OK;
+}
+
+extern "C" {
+
+// Laminar flow terms the projection does not need (case flow: viscosity_m2_s, acceleration_m_s2).
+void ora_grid_set_flow_terms(void* gp, double viscosity, const double* acceleration) {
+  Grid* g = (Grid*)gp;
+  g->viscosity = viscosity;
+  for (int a = 0; a < 3; ++a) g->acceleration[a] = acceleration ? acceleration[a] : 0.0;
+}
+int32_t ora_momentum_rhs(void* gp, const double* u, double* out) { return momentum_rhs(*(Grid*)gp, u, out); }
+// solver.rs:879-960: one SSPRK2 step of the laminar flow, a projection per stage, in place.
+int32_t ora_step(void* gp, double* u, double* p, double dt, double tol, uint64_t max, uint64_t* iterations) {
+  Grid& g = *(Grid*)gp;
+  const size_t F = g.faces.size();
+  std::vector<double> v, p1, v2, p2;
+  uint64_t it = 0;
+  if (int c = flow_euler(g, u, p, dt, tol, max, v, p1, it)) return c;
+  if (int c = flow_euler(g, v.data(), p1.data(), dt, tol, max, v2, p2, it)) return c;
+  for (size_t f = 0; f < F; ++f) u[f] = 0.5 * (u[f] + v2[f]);
+  std::copy(p2.begin(), p2.end(), p);
+  enforce_velocity(g, u);
+  if (iterations) *iterations = it;
+  return OK;
+}
+
 // grid.rs:683-691
 void ora_enforce_velocity(void* gp, double* u) {
   Grid* g = (Grid*)gp;

@@ -113,6 +113,11 @@ def lib():
             L.ora_mg_levels.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int32]
             L.ora_mg_masked_level.restype = C.c_int64
             L.ora_mg_masked_level.argtypes = [P, C.c_int32] + [C.c_void_p] * 6
+            L.ora_grid_set_flow_terms.argtypes = [P, C.c_double, dp]
+            L.ora_momentum_rhs.restype = C.c_int32
+            L.ora_momentum_rhs.argtypes = [P, dp, dp]
+            L.ora_step.restype = C.c_int32
+            L.ora_step.argtypes = [P, dp, dp, C.c_double, C.c_double, C.c_uint64, C.POINTER(C.c_uint64)]
             _lib = L
     return _lib
 
@@ -186,12 +191,32 @@ class Grid:
         L.ora_grid_export(self.h, _vp(self.fluid), _vp(self.face_kind), _vp(self.face_lo), _vp(self.face_hi),
                           _vp(self.face_area), _vp(self.face_distance), _vp(self.component), _vp(self.anchored),
                           _vp(self.cell_faces), _vp(self.face_center), _vp(self.face_axis))
+        acc = np.ascontiguousarray(flow.get("acceleration_m_s2", [0.0, 0.0, 0.0]), dtype=np.float64)
+        L.ora_grid_set_flow_terms(self.h, float(flow.get("viscosity_m2_s", 1.5e-5)), _ptr(acc))
 
     def __del__(self):
         h = getattr(self, "h", None)
         if h is not None and _lib is not None:
             _lib.ora_grid_free(h)
             self.h = None
+
+    def momentum_rhs(self, u):
+        """flow::momentum_rhs for laminar flow (flow.rs:426-525), per face."""
+        u = np.ascontiguousarray(u, np.float64)
+        out = np.zeros(self.n_faces)
+        code = lib().ora_momentum_rhs(self.h, _ptr(u), _ptr(out))
+        if code:
+            raise OracleError(code, "momentum_rhs")
+        return out
+
+    def step(self, u, p, dt, tol=1e-8, max_iter=10000):
+        """One SSPRK2 step of laminar flow with a projection per stage (solver.rs:879-960).
+        Returns (code, u, p, pressure iterations)."""
+        uu = np.array(u, dtype=np.float64, copy=True)
+        pp = np.array(p, dtype=np.float64, copy=True)
+        it = C.c_uint64()
+        code = lib().ora_step(self.h, _ptr(uu), _ptr(pp), float(dt), float(tol), int(max_iter), C.byref(it))
+        return code, uu, pp, it.value
 
     def set_preconditioner(self, name):
         lib().ora_grid_set_preconditioner(self.h, PRECONDITIONER[name])
