@@ -50,6 +50,9 @@ WORKLOAD = ("128x128x64 grid, dx=2 m, 12 seeded box buildings, open x (inflow 5 
 
 # DRAM bytes per cell of one red-black half sweep (ncu: 29,417,728 B over 4,194,304 cells).
 RB_DRAM_BYTES_PER_CELL = (29406720 + 11008) / 4194304
+# DRAM bytes of one scalar transport step (both passes) per cell, from one ncu capture of
+# k_scalar_pass on the 128x128x64 transport workload (profiles/k_scalar_pass_transport_128x128x64.md).
+TRANSPORT_DRAM_BYTES_PER_CELL = (54496768 + 337408 + 62883584 + 301824) / 1048576
 
 
 def max_over_ranks(value, dist, device):
@@ -935,6 +938,160 @@ def run_stepping(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     return 0
 
 
+TRANSPORT_WORKLOAD = ("128x128x64 grid, dx=2 m, 12 seeded box buildings, laminar inflow 5 m/s, open x / wall y,z; "
+                      "one constituent on the flow projected from the initial velocity, linear upwind, cell "
+                      "diffusivities 0.05-0.15 m2/s, a release of 1e-3 kg/m3/s in 64 cells near the inflow, "
+                      "dt at CFL 0.4")
+TRANSPORT_METRIC = "scalar transport SSPRK2 steps/s (linear upwind, bit-identical to the reference arithmetic)"
+
+
+def transport_fields(pkg, g, seed):
+    """Diffusivity, source and a starting concentration of the transport workload."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    fluid = g.fluid.astype(bool)
+    d = np.where(fluid, rng.uniform(0.05, 0.15, g.count), 0.0)
+    source = np.zeros(g.count)
+    nx, ny = int(g.n[0]), int(g.n[1])
+    cell = np.arange(g.count)
+    near = np.nonzero(fluid & (cell % nx < 8) & (np.abs((cell // nx) % ny - ny // 2) < 4))[0]
+    source[rng.choice(near, 64, replace=False)] = 1e-3
+    c = np.where(fluid, rng.uniform(0.0, 1e-3, g.count), 0.0)
+    return d, source, c
+
+
+def transport_cpu_baseline(case, u, d, source, c, dt):
+    """The oracle's advance_scalar on every host thread, each on its own grid and copy."""
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    grids = [None] * threads
+    steps = 10
+
+    def build(t):
+        grids[t] = O.Grid(case)
+
+    def work(t):
+        x = c
+        for _ in range(steps):
+            x = grids[t].scalar_step(x, u, d, source, dt)
+
+    for fn in (build, work):
+        ths = [threading.Thread(target=fn, args=(t,)) for t in range(threads)]
+        t0 = time.perf_counter()
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        wall = time.perf_counter() - t0
+    return {"value": round(threads * steps / wall, 4), "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"{threads} host threads, each {steps} SSPRK2 steps of the workload on its own oracle grid; "
+                      f"{wall:.2f} s wall"}
+
+
+def run_transport(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
+    """Survey row f2: receptor transport on the device (cfdg_scalar_step_device)."""
+    import numpy as np
+
+    K, W = args.steps, args.warmup
+    case = workload_case(pkg)
+    g = pkg.grid.Grid.build(case)
+    dg = pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed")
+    dg.set_stream(stream.cuda_stream)
+    u, p = g.initial_velocity(), np.zeros(g.count)
+    dg.project(u, p, DT, TOL, MAX_IT)
+    d, source, c = transport_fields(pkg, g, 7)
+    # CFL 0.4 on the largest transporting-face speed, and the explicit diffusion limit.
+    moving = np.isin(g.face_kind, (pkg.grid.INTERIOR, pkg.grid.INLET, pkg.grid.OUTLET))
+    dmin = float(min(g.dx))
+    dt = min(0.4 * dmin / float(np.max(np.abs(u[moving]))), 0.1 * dmin * dmin / float(np.max(d)))
+    d_u = torch.from_numpy(u).to(dev)
+    d_d, d_s = torch.from_numpy(d).to(dev), torch.from_numpy(source).to(dev)
+    d_c = torch.from_numpy(c.copy()).to(dev)
+
+    def step():
+        dg.scalar_step_device(d_u.data_ptr(), d_c.data_ptr(), d_d.data_ptr(), d_s.data_ptr(), dt)
+
+    for _ in range(W):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches0 = L.cfdg_launch_count()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for k in range(K):
+        flush.zero_()
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = L.cfdg_launch_count() - launches0
+    total_ms = ev0.elapsed_time(ev1)
+    kern_ms = sum(a.elapsed_time(b) for a, b in ev) / K
+    if dist:
+        total_ms = max_over_ranks(total_ms, dist, dev)
+    value = world * K / (total_ms / 1e3)
+    # End to end: the step's inputs (u, d, source, c) from pinned host memory, c back.
+    h_u, h_d, h_s = (torch.from_numpy(x).pin_memory() for x in (u, d, source))
+    h_c = torch.from_numpy(d_c.cpu().numpy()).pin_memory()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(K):
+        flush.zero_()
+        d_u.copy_(h_u, non_blocking=True)
+        d_d.copy_(h_d, non_blocking=True)
+        d_s.copy_(h_s, non_blocking=True)
+        d_c.copy_(h_c, non_blocking=True)
+        step()
+        h_c.copy_(d_c, non_blocking=True)
+    b.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = a.elapsed_time(b)
+    if dist:
+        e2e_ms = max_over_ranks(e2e_ms, dist, dev)
+    n, f = g.count, g.n_faces
+    # Algorithmic bytes of one step (two passes): per cell c, d, source, the stage or c
+    # written, the fluid flag, and three faces' velocity and kind; the second pass also
+    # reads the cell's own c.
+    step_bytes = (60 + 68) * n
+    peak, peak_kind = peaks()
+    achieved = step_bytes / (kern_ms / 1e3) / 1e9
+    dg.close()
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            cpu = transport_cpu_baseline(case, u, d, source, c, dt)
+        line = {"metric": TRANSPORT_METRIC, "value": round(value, 4), "unit": "steps/s", "n_gpus": world,
+                "steps": K, "warmup": W, "ms_per_step": round(total_ms / K, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": TRANSPORT_WORKLOAD, "cells": n, "faces": f, "dt_s": dt,
+                           "l2": "256 MiB buffer written before every step", "parallelism": f"replicas x{world}"},
+                "cell_updates_per_s": round(world * K * n / (total_ms / 1e3), 1),
+                "e2e": {"value": round(world * K / (e2e_ms / 1e3), 4), "unit": "steps/s",
+                        "h2d_bytes_per_step": 8 * (f + 3 * n), "d2h_bytes_per_step": 8 * n},
+                "roofline": {"bound": "hbm", "kernel": "k_scalar_pass stage + combine (one step)",
+                             "limiter": "FP64 pipe (72 % active under ncu; about 24 FP64 adds and multiplies "
+                                        "per cell and pass)",
+                             "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                             "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                             "algorithmic_bytes_per_step": step_bytes, "kernel_ms_per_step": round(kern_ms, 4),
+                             "traffic": round(TRANSPORT_DRAM_BYTES_PER_CELL * n, 0)},
+                "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk}
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_engine(args):
     import torch
 
@@ -959,8 +1116,9 @@ def run_engine(args):
     flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MiB > L2 (129 MB)
     K, W = args.steps, args.warmup
     L = pkg.engine.load()
-    if args.form in ("serving", "uneven", "stepping"):
-        run = {"serving": run_serving, "uneven": run_uneven, "stepping": run_stepping}[args.form]
+    if args.form in ("serving", "uneven", "stepping", "transport"):
+        run = {"serving": run_serving, "uneven": run_uneven, "stepping": run_stepping,
+               "transport": run_transport}[args.form]
         rc = run(args, pkg, torch, dev, stream, flush, rank, world, dist, L)
         if dist:
             dist.destroy_process_group()
@@ -1068,7 +1226,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--form", default="serving",
-                    choices=["plain", "mixed", "batched", "serving", "uneven", "large", "stepping"])
+                    choices=["plain", "mixed", "batched", "serving", "uneven", "large", "stepping", "transport"])
     ap.add_argument("--slots", type=int, default=0, help="serving: cases on the GPU at once (0: all)")
     ap.add_argument("--requests", type=int, default=520, help="serving: open-loop requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")

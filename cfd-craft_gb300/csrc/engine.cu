@@ -981,6 +981,35 @@ int refresh_weights(cfdg_grid* G) {
     std::memcpy(&G->g.w_in[a], &win[a], 8);
     std::memcpy(&G->g.w_out[a], &wout[a], 8);
   }
+  // Scalar transport: area and distance of the transporting faces per axis and kind.
+  bool sc_uniform = true;
+  uint64_t sa[3][3] = {}, sd[3][3] = {};
+  bool sh[3][3] = {};
+  for (int a = 0; a < 3 && sc_uniform; ++a)
+    for (int64_t f = h.face_offset[a]; f < h.face_offset[a] + h.face_dims[a][0] * h.face_dims[a][1] * h.face_dims[a][2];
+         ++f) {
+      const uint8_t k = h.face_kind[f];
+      if (k != INTERIOR && k != INLET && k != OUTLET) continue;
+      const int t = k == INTERIOR ? 0 : (k == INLET ? 1 : 2);
+      uint64_t ab, db;
+      std::memcpy(&ab, &h.face_area[f], 8);
+      std::memcpy(&db, &h.face_distance[f], 8);
+      if (!sh[a][t]) {
+        sa[a][t] = ab;
+        sd[a][t] = db;
+        sh[a][t] = true;
+      } else if (sa[a][t] != ab || sd[a][t] != db) {
+        sc_uniform = false;
+        break;
+      }
+    }
+  G->sc_uniform = sc_uniform;
+  for (int a = 0; a < 3; ++a)
+    for (int t = 0; t < 3; ++t) {
+      G->sc_used[a][t] = sh[a][t];
+      std::memcpy(&G->sc_area[a][t], &sa[a][t], 8);
+      std::memcpy(&G->sc_dist[a][t], &sd[a][t], 8);
+    }
   CU(cudaGetLastError());
   return 0;
 }
@@ -1514,6 +1543,205 @@ __global__ void k_ssprk_combine(FlowDev D, double* __restrict__ u, const double*
   }
 }
 
+// ----------------------------------------------------------------- scalar transport
+// transport.rs:651-699 rhs_into (linear upwind, zero inlet concentration) and
+// solver.rs:808-855 advance_scalar. The reference loops over faces and applies each
+// transporting face's flux / volume to its lo cell (subtracted) and hi cell (added); a
+// cell therefore receives its faces in face order: x-lo, x-hi, y-lo, y-hi, z-lo, z-hi.
+// Here each face's value is computed once by one thread of a 32x8 tile marching in z
+// (x neighbours through warp shuffles, y neighbours through shared memory, z in
+// registers) and each cell sums its six faces in that order: the same bits without
+// atomics. The kernels are bound by the FP64 pipe (one FP64 add or multiply per SM and
+// clock on this part), so FP64 operations that are exact in integer arithmetic are done
+// there: a product with, or a quotient by, a power of two (0.5, and the face area,
+// distance and cell volume of grids with power-of-two spacing) is an addition to the
+// exponent field while the operand and result are normal numbers (the same real value,
+// so the same bits; zeros, subnormals, infinities and NaNs take the FP64 instruction),
+// and `x + 0.0` only turns -0.0 into +0.0.
+// A factor 2^e (value v) when `ok`; otherwise the factor is not a power of two.
+struct Pow2 {
+  double v;
+  int e;
+  int ok;
+};
+
+struct ScalarDev {
+  int n[3];
+  long long face_off[3];
+  int fdim[3][3];
+  double volume;
+  Pow2 inv_volume;  // 1/volume
+  const uint8_t* kind;
+  const uint8_t* fluid;
+  const int *lo, *hi;
+  const double *area, *dist;
+  // Uniform grids: the area and distance of the transporting faces per axis and kind
+  // (interior, inlet, outlet), equal bit for bit on every such face.
+  double area_k[3][3], dist_k[3][3];
+  Pow2 area_p[3][3], inv_dist_p[3][3];
+};
+
+constexpr int STX = 32, STY = 8, STZ = 8;  // cells of one transport tile (x, y, z)
+
+__device__ __forceinline__ int transport_slot(uint8_t k) { return k == INTERIOR ? 0 : (k == INLET ? 1 : 2); }
+
+__device__ __forceinline__ double plus_zero(double x) {  // x + 0.0
+  return __double_as_longlong(x) == (long long)0x8000000000000000ull ? 0.0 : x;
+}
+
+// The rare FP64 paths, out of line: an if-converted FP64 instruction whose lanes are all
+// predicated off still takes its turn on the FP64 pipe.
+__device__ __noinline__ double fp64_mul(double x, double y) { return x * y; }
+
+// x * 2^e, the exponent field moved when x and the result are normal (bit-identical to the
+// FP64 product, which is exact there), the FP64 product otherwise.
+__device__ __forceinline__ double mul_pow2(double x, const Pow2& p) {
+  const long long b = __double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  const int r = e + p.e;
+  if (e != 0 && e != 0x7ff && r >= 1 && r <= 2046) return __longlong_as_double(b + ((long long)p.e << 52));
+  if ((b & 0x7fffffffffffffffLL) == 0) return x;  // a signed zero stays itself
+  return fp64_mul(x, p.v);
+}
+
+// x >= 0.0 on the bits: +0.0 and -0.0, and positive numbers up to +infinity; not NaN.
+__device__ __forceinline__ bool nonneg(double x) {
+  const long long b = __double_as_longlong(x);
+  return (b & 0x7fffffffffffffffLL) == 0 || (b >= 0 && b <= 0x7ff0000000000000LL);
+}
+__device__ __forceinline__ double half(double x) { return mul_pow2(x, Pow2{0.5, -1, 1}); }
+
+// The flux / volume of face f on axis a between cells lo_cell and hi_cell (its structural
+// neighbours, -1 outside the domain), evaluated on the field x; false if the face does not
+// transport. UNI: the layout's lo/hi (interior iff both are fluid) and per-axis constants.
+// P2 (with UNI): the volume and every transporting face's area and distance are powers of
+// two, so the products and quotients by them go through the exponent field.
+template <bool UNI, bool P2>
+__device__ __forceinline__ bool face_eval(const ScalarDev& D, int a, long long f, long long lo_cell,
+                                          long long hi_cell, const double* __restrict__ x,
+                                          const double* __restrict__ u, const double* __restrict__ d, double& pv) {
+  const uint8_t k = D.kind[f];
+  if (k != INTERIOR && k != INLET && k != OUTLET) return false;
+  bool hl, hh;
+  double area = 0.0, dist = 0.0;
+  Pow2 area_p{0.0, 0, 0}, inv_dist_p{0.0, 0, 0};
+  if (UNI) {
+    if (k == INTERIOR) {
+      hl = hh = true;
+    } else {
+      hl = lo_cell >= 0 && D.fluid[lo_cell];
+      hh = hi_cell >= 0 && D.fluid[hi_cell];
+    }
+    const int t = transport_slot(k);
+    if (P2) {
+      area_p = D.area_p[a][t];
+      inv_dist_p = D.inv_dist_p[a][t];
+    } else {
+      area = D.area_k[a][t];
+      dist = D.dist_k[a][t];
+    }
+  } else {
+    hl = D.lo[f] >= 0;
+    hh = D.hi[f] >= 0;
+    area = D.area[f];
+    dist = D.dist[f];
+  }
+  const double cl = hl ? x[lo_cell] : 0.0, cr = hh ? x[hi_cell] : 0.0;
+  const double uf = u[f];
+  // Donor: the upwind cell's value (+ 0.0 when it exists; the inlet value 0.0 otherwise,
+  // whose + 0.0 is the same bits); `cr - 0.0` is cr for every cr.
+  const double donor = nonneg(uf) ? plus_zero(cl) : cr;
+  double diffusivity;
+  if (hl && hh) diffusivity = half(d[lo_cell] + d[hi_cell]);
+  else if (hl) diffusivity = d[lo_cell];
+  else if (hh) diffusivity = d[hi_cell];
+  else diffusivity = 0.0;
+  if (P2) {
+    const double diff = k == OUTLET ? 0.0 : mul_pow2(diffusivity * (cl - cr), inv_dist_p);
+    pv = mul_pow2(mul_pow2(uf * donor + diff, area_p), D.inv_volume);
+  } else {
+    const double diff = k == OUTLET ? 0.0 : diffusivity * (cl - cr) / dist;
+    pv = (uf * donor + diff) * area / D.volume;
+  }
+  return true;
+}
+
+// One pass of the SSPRK2 step over a (32, 8, 8) tile of cells. MODE 0 (solver.rs:845-847):
+// stage = c + dt rhs(c). MODE 1 (solver.rs:848-850): c = (c + stage + dt rhs(stage)) / 2, in
+// place (a thread reads c only at its own cell). Blocks are (32, 8); every thread reaches
+// every barrier and shuffle.
+template <bool UNI, bool P2, int MODE>
+__global__ void __launch_bounds__(STX * STY) k_scalar_pass(ScalarDev D, double* __restrict__ c,
+                                                          double* __restrict__ stage, const double* __restrict__ u,
+                                                          const double* __restrict__ d,
+                                                          const double* __restrict__ source, double dt) {
+  __shared__ double s_pv[STY][STX];
+  __shared__ uint8_t s_on[STY][STX];
+  const double* __restrict__ x = MODE == 0 ? c : stage;  // the field the right-hand side reads
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int nx = D.n[0], ny = D.n[1], nz = D.n[2];
+  const int i = blockIdx.x * STX + tx, j = blockIdx.y * STY + ty;
+  const int z0 = blockIdx.z * STZ, z1 = min(z0 + STZ, nz);
+  const bool valid = i < nx && j < ny;
+  const long long sx = nx, sxy = (long long)nx * ny;
+  double zlo = 0.0;
+  bool zlo_on = false;
+  if (valid) {  // the z-lo face of the first slice
+    const long long cell = z0 * sxy + j * sx + i;
+    const long long f = D.face_off[2] + ((long long)z0 * D.fdim[2][1] + j) * D.fdim[2][0] + i;
+    zlo_on = face_eval<UNI, P2>(D, 2, f, z0 > 0 ? cell - sxy : -1, cell, x, u, d, zlo);
+  }
+  for (int z = z0; z < z1; ++z) {
+    const long long cell = z * sxy + j * sx + i;
+    double xlo = 0.0, xhi = 0.0, ylo = 0.0, yhi = 0.0, zhi = 0.0;
+    bool xlo_on = false, xhi_on = false, ylo_on = false, yhi_on = false, zhi_on = false;
+    if (valid) {
+      const long long fx = D.face_off[0] + ((long long)z * D.fdim[0][1] + j) * D.fdim[0][0] + i;
+      xlo_on = face_eval<UNI, P2>(D, 0, fx, i > 0 ? cell - 1 : -1, cell, x, u, d, xlo);
+      const long long fy = D.face_off[1] + ((long long)z * D.fdim[1][1] + j) * D.fdim[1][0] + i;
+      ylo_on = face_eval<UNI, P2>(D, 1, fy, j > 0 ? cell - sx : -1, cell, x, u, d, ylo);
+      const long long fz = D.face_off[2] + ((long long)(z + 1) * D.fdim[2][1] + j) * D.fdim[2][0] + i;
+      zhi_on = face_eval<UNI, P2>(D, 2, fz, cell, z + 1 < nz ? cell + sxy : -1, x, u, d, zhi);
+    }
+    // x-hi: the next lane's x-lo, or computed here at the tile's or the domain's edge.
+    const double nxt = __shfl_down_sync(0xffffffffu, xlo, 1);
+    const int nxt_on = __shfl_down_sync(0xffffffffu, (int)xlo_on, 1);
+    s_pv[ty][tx] = ylo;
+    s_on[ty][tx] = ylo_on;
+    __syncthreads();
+    if (valid) {
+      if (tx == STX - 1 || i == nx - 1) {
+        const long long fx = D.face_off[0] + ((long long)z * D.fdim[0][1] + j) * D.fdim[0][0] + i + 1;
+        xhi_on = face_eval<UNI, P2>(D, 0, fx, cell, i + 1 < nx ? cell + 1 : -1, x, u, d, xhi);
+      } else {
+        xhi = nxt;
+        xhi_on = nxt_on != 0;
+      }
+      if (ty == STY - 1 || j == ny - 1) {
+        const long long fy = D.face_off[1] + ((long long)z * D.fdim[1][1] + j + 1) * D.fdim[1][0] + i;
+        yhi_on = face_eval<UNI, P2>(D, 1, fy, cell, j + 1 < ny ? cell + sx : -1, x, u, d, yhi);
+      } else {
+        yhi = s_pv[ty + 1][tx];
+        yhi_on = s_on[ty + 1][tx] != 0;
+      }
+      double acc = source[cell];
+      if (D.fluid[cell]) {  // a solid cell is on no face: its rate is its source
+        if (xlo_on) acc = acc + xlo;
+        if (xhi_on) acc = acc - xhi;
+        if (ylo_on) acc = acc + ylo;
+        if (yhi_on) acc = acc - yhi;
+        if (zlo_on) acc = acc + zlo;
+        if (zhi_on) acc = acc - zhi;
+      }
+      if (MODE == 0) stage[cell] = c[cell] + dt * acc;
+      else c[cell] = half(c[cell] + stage[cell] + dt * acc);
+    }
+    zlo = zhi;
+    zlo_on = zhi_on;
+    __syncthreads();  // s_pv is rewritten by the next slice
+  }
+}
+
 FlowDev flow_dev(cfdg_grid* G) {
   FlowDev D{};
   for (int a = 0; a < 3; ++a) {
@@ -1875,6 +2103,73 @@ int cfdg_step_device(cfdg_grid* G, double* d_u, double* d_p, double dt, double t
     info->true_residual_checks = i1.true_residual_checks + i2.true_residual_checks;
     info->device_seconds = i1.device_seconds + i2.device_seconds;
   }
+  return 0;
+}
+
+// y (inverse: 1/y) as a power-of-two factor when y is a positive normal power of two whose
+// reciprocal is normal too (a product with 1/y is then the quotient by y, rounding included).
+static Pow2 pow2_of(double y, bool inverse) {
+  Pow2 p{0.0, 0, 0};
+  if (!(y > 0.0) || !std::isnormal(y)) return p;
+  int e = 0;
+  if (std::frexp(y, &e) != 0.5) return p;
+  const int k = inverse ? 1 - e : e - 1;
+  const double v = std::ldexp(1.0, k);
+  if (!std::isnormal(v) || !std::isnormal(1.0 / v)) return p;
+  return Pow2{v, k, 1};
+}
+
+int cfdg_scalar_step_device(cfdg_grid* G, const double* d_u, double* d_c, const double* d_diff, const double* d_source,
+                            double dt) {
+  if (int e = check_grid(G)) return e;
+  if (!d_u || !d_c || !d_diff || !d_source) return fail(CFDG_ERR_INVALID, "null array");
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  for (int a = 0; a < 3; ++a)
+    if (G->h.periodic[a]) return fail(CFDG_ERR_UNSUPPORTED, "scalar transport on the device: periodic axes");
+  const int N = (int)G->h.cells;
+  if (!G->st_sc) {
+    if (int e = G->arena.alloc(&G->st_sc, (size_t)N)) return e;
+  }
+  ScalarDev D{};
+  for (int a = 0; a < 3; ++a) {
+    D.n[a] = G->h.n[a];
+    D.face_off[a] = G->g.face_off[a];
+    for (int d = 0; d < 3; ++d) D.fdim[a][d] = G->g.fdim[a][d];
+  }
+  D.volume = G->h.volume;
+  D.inv_volume = pow2_of(G->h.volume, true);
+  D.kind = G->d_kind;
+  D.fluid = G->d_fluid;
+  D.lo = G->d_lo;
+  D.hi = G->d_hi;
+  D.area = G->d_area;
+  D.dist = G->d_dist;
+  for (int a = 0; a < 3; ++a)
+    for (int t = 0; t < 3; ++t) {
+      D.area_k[a][t] = G->sc_area[a][t];
+      D.dist_k[a][t] = G->sc_dist[a][t];
+      D.area_p[a][t] = pow2_of(G->sc_area[a][t], false);
+      D.inv_dist_p[a][t] = pow2_of(G->sc_dist[a][t], true);
+    }
+  double* stage = G->st_sc;
+  cudaStream_t s = G->stream;
+  const dim3 blk(STX, STY), grd((G->h.n[0] + STX - 1) / STX, (G->h.n[1] + STY - 1) / STY, (G->h.n[2] + STZ - 1) / STZ);
+  bool p2 = G->sc_uniform && D.inv_volume.ok;
+  for (int a = 0; a < 3; ++a)
+    for (int t = 0; t < 3; ++t)
+      if (G->sc_used[a][t]) p2 = p2 && D.area_p[a][t].ok && D.inv_dist_p[a][t].ok;
+  if (p2) {
+    k_scalar_pass<true, true, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+    k_scalar_pass<true, true, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+  } else if (G->sc_uniform) {
+    k_scalar_pass<true, false, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+    k_scalar_pass<true, false, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+  } else {
+    k_scalar_pass<false, false, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+    k_scalar_pass<false, false, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+  }
+  CU(cudaGetLastError());
   return 0;
 }
 

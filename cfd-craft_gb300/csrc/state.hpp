@@ -196,6 +196,12 @@ struct cfdg_grid {
   int flow_bnd[3] = {0, 0, 0};
   double flow_size[3] = {0, 0, 0}, flow_vel[3] = {0, 0, 0}, flow_nu = 0, flow_acc[3] = {0, 0, 0};
   double *st_cu = nullptr, *st_v = nullptr, *st_v2 = nullptr, *st_p1 = nullptr;
+  double* st_sc = nullptr;  // scalar transport: the SSPRK2 stage (N)
+  // Scalar transport on a uniform grid: per axis and transporting kind (interior, inlet,
+  // outlet) the one face area and distance, bit for bit (refresh_weights).
+  bool sc_uniform = false;
+  bool sc_used[3][3] = {};
+  double sc_area[3][3] = {}, sc_dist[3][3] = {};
   uint64_t sig_version = ~0ull;
 };
 

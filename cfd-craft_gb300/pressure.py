@@ -207,6 +207,11 @@ class DeviceGrid:
         self._check(rc)
         return LinearInfo(info.iterations, info.relative_residual, info.as_dict())
 
+    def scalar_step_device(self, u_ptr: int, c_ptr: int, d_ptr: int, source_ptr: int, dt):
+        """One SSPRK2 step of a constituent on device arrays (cfdg_scalar_step_device)."""
+        self._check(self.L.cfdg_scalar_step_device(self.h, C.c_void_p(u_ptr), C.c_void_p(c_ptr), C.c_void_p(d_ptr),
+                                                   C.c_void_p(source_ptr), float(dt)))
+
     def momentum_update(self, u, p, dt):
         """u + dt (R(u) - grad p) with the fixed face values, before a stage's projection."""
         u = np.ascontiguousarray(u, np.float64)

@@ -157,6 +157,13 @@ int cfdg_grid_set_flow(cfdg_grid *grid, const cfdg_flow_desc *flow);
  * p are unchanged. info: the second projection's, with iterations and work summed. */
 int cfdg_step_device(cfdg_grid *grid, double *d_u, double *d_p, double dt, double tol, uint64_t max_iter,
                      cfdg_poll_fn poll, void *poll_ctx, cfdg_info *info);
+/* One SSPRK2 step of a constituent's concentration d_c (N, kg/m3) in place on the face
+ * velocities d_u (F), with cell diffusivities d_diff (N, m2/s: the constituent's plus
+ * nu_t / Sc) and source densities d_source (N, kg/m3/s): advance_scalar
+ * (solver.rs:808-855) with linear upwind (transport.rs:651-699) and zero inflow
+ * concentration, bit-identical to it; the budgets are not kept. Non-periodic grids. */
+int cfdg_scalar_step_device(cfdg_grid *grid, const double *d_u, double *d_c, const double *d_diff,
+                            const double *d_source, double dt);
 /* Diagnostic: one stage's velocity before its projection, out = u + dt (R(u) - grad p) with
  * the fixed face values, on host arrays (F, N, F doubles). No reference counterpart. */
 int cfdg_debug_momentum_update(cfdg_grid *grid, const double *u, const double *p, double dt, double *out);

@@ -1591,7 +1591,46 @@ static int flow_euler(Grid& g, const double* u, const double* p, double dt, doub
   return OK;
 }
 
+// transport.rs:651-699 rhs_into with linear upwind (no MUSCL slope) and a zero inlet
+// concentration (solver.rs:823-832 passes |_| 0.0), in face order.
+static void scalar_rhs(const Grid& g, const double* c, const double* u, const double* d, const double* source,
+                       double* v) {
+  const size_t N = g.count();
+  for (size_t i = 0; i < N; ++i) v[i] = source[i];
+  for (size_t fi = 0; fi < g.faces.size(); ++fi) {
+    const Face& f = g.faces[fi];
+    if (f.kind != K_INTERIOR && f.kind != K_INLET && f.kind != K_OUTLET) continue;
+    const double cl = f.lo != NONE ? c[f.lo] : 0.0;
+    const double cr = f.hi != NONE ? c[f.hi] : 0.0;
+    double donor;
+    if (u[fi] >= 0.0) donor = f.lo != NONE ? cl + 0.0 : cl;
+    else donor = f.hi != NONE ? cr - 0.0 : cr;
+    double diffusivity;
+    if (f.lo != NONE && f.hi != NONE) diffusivity = 0.5 * (d[f.lo] + d[f.hi]);
+    else if (f.lo != NONE) diffusivity = d[f.lo];
+    else if (f.hi != NONE) diffusivity = d[f.hi];
+    else diffusivity = 0.0;
+    const double diff = f.kind == K_OUTLET ? 0.0 : diffusivity * (cl - cr) / f.distance;
+    const double flux = (u[fi] * donor + diff) * f.area;
+    const double per_volume = flux / g.volume;
+    if (f.lo != NONE) v[f.lo] = v[f.lo] - per_volume;
+    if (f.hi != NONE) v[f.hi] = v[f.hi] + per_volume;
+  }
+}
+
 extern "C" {
+
+// solver.rs:808-855 advance_scalar: one SSPRK2 step of a constituent in place (linear
+// upwind, no particle terms; the budgets are not kept).
+void ora_scalar_step(void* gp, double* c, const double* u, const double* d, const double* source, double dt) {
+  const Grid& g = *(Grid*)gp;
+  const size_t N = g.count();
+  std::vector<double> r1(N), stage(N), r2(N);
+  scalar_rhs(g, c, u, d, source, r1.data());
+  for (size_t i = 0; i < N; ++i) stage[i] = c[i] + dt * r1[i];
+  scalar_rhs(g, stage.data(), u, d, source, r2.data());
+  for (size_t i = 0; i < N; ++i) c[i] = 0.5 * (c[i] + stage[i] + dt * r2[i]);
+}
 
 // Laminar flow terms the projection does not need (case flow: viscosity_m2_s, acceleration_m_s2).
 void ora_grid_set_flow_terms(void* gp, double viscosity, const double* acceleration) {

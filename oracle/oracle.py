@@ -116,6 +116,7 @@ def lib():
             L.ora_grid_set_flow_terms.argtypes = [P, C.c_double, dp]
             L.ora_momentum_rhs.restype = C.c_int32
             L.ora_momentum_rhs.argtypes = [P, dp, dp]
+            L.ora_scalar_step.argtypes = [P, dp, dp, dp, dp, C.c_double]
             L.ora_step.restype = C.c_int32
             L.ora_step.argtypes = [P, dp, dp, C.c_double, C.c_double, C.c_uint64, C.POINTER(C.c_uint64)]
             _lib = L
@@ -217,6 +218,14 @@ class Grid:
         it = C.c_uint64()
         code = lib().ora_step(self.h, _ptr(uu), _ptr(pp), float(dt), float(tol), int(max_iter), C.byref(it))
         return code, uu, pp, it.value
+
+    def scalar_step(self, c, u, d, source, dt):
+        """advance_scalar (solver.rs:808-855): one SSPRK2 step of a constituent, linear upwind."""
+        cc = np.array(c, dtype=np.float64, copy=True)
+        lib().ora_scalar_step(self.h, _ptr(cc), _ptr(np.ascontiguousarray(u, np.float64)),
+                              _ptr(np.ascontiguousarray(d, np.float64)),
+                              _ptr(np.ascontiguousarray(source, np.float64)), float(dt))
+        return cc
 
     def set_preconditioner(self, name):
         lib().ora_grid_set_preconditioner(self.h, PRECONDITIONER[name])

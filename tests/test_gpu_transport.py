@@ -1,0 +1,137 @@
+"""Scalar transport on the device (cfdg_scalar_step_device): SSPRK2 steps of a constituent
+with linear upwind advection, bit-identical to the oracle's sequential restatement of
+advance_scalar (solver.rs:808-855) and rhs_into (transport.rs:651-699), and mass
+conservation in a closed box at a larger size."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float64).view(np.uint64)
+
+
+def flow_case(pkg, name):
+    if name == "buildings-open-wall":
+        return pkg.synth.case((24, 20, 12), 2.0, inflow=5.0, preconditioner="multigrid",
+                              boxes=[((16.0, 10.0, 0.0), (26.0, 22.0, 10.0)), ((30.0, 4.0, 0.0), (36.0, 10.0, 16.0))])
+    if name == "spacing-1.5m":  # face areas, distances and the volume not powers of two
+        return pkg.synth.case((40, 14, 9), 1.5, inflow=4.0, preconditioner="multigrid",
+                              boxes=[((15.0, 6.0, 0.0), (24.0, 15.0, 7.5))])
+    if name == "wide-tiles":  # several x and y tiles, ragged in every axis
+        return pkg.synth.case((70, 19, 11), 1.0, inflow=3.0, preconditioner="multigrid",
+                              boxes=[((20.0, 5.0, 0.0), (31.0, 12.0, 6.0)), ((50.0, 0.0, 0.0), (64.0, 4.0, 9.0))])
+    return pkg.synth.case((20, 12, 10), 1.0, boundaries=("open", "slip", "wall"), inflow=2.0,
+                          preconditioner="ic0", boxes=[((6.0, 0.0, 0.0), (9.0, 5.0, 4.0))])
+
+
+@pytest.mark.parametrize("name,perturb", [("buildings-open-wall", False), ("slip-channel", False),
+                                          ("wide-tiles", False), ("spacing-1.5m", False),
+                                          ("buildings-open-wall", True), ("wide-tiles", True)])
+def test_scalar_steps_bit_identical(pkg, O, name, perturb):
+    """perturb: face areas and distances scaled per face (the general gather that reads
+    each face's lo, hi, area and distance); otherwise the structured fast path."""
+    torch = pytest.importorskip("torch")
+    case = flow_case(pkg, name)
+    g = pkg.grid.Grid.build(case)
+    og = O.Grid(case)
+    rng = np.random.default_rng(11)
+    # A projected flow with noise on the interior faces (backflow through the outlet included).
+    code, u, _, _ = og.project(g.initial_velocity(), np.zeros(g.count), 0.1, 1e-8, 10000)
+    assert code == 0
+    u = u + np.where(g.face_kind == pkg.grid.INTERIOR, rng.uniform(-1.0, 1.0, g.n_faces), 0.0)
+    u[g.face_kind == pkg.grid.OUTLET] *= rng.choice([1.0, -0.5], int((g.face_kind == pkg.grid.OUTLET).sum()))
+    fluid = g.fluid.astype(bool)
+    d = np.where(fluid, rng.uniform(0.01, 0.5, g.count), 0.0)
+    source = np.zeros(g.count)
+    src_cells = rng.choice(np.nonzero(fluid)[0], 5, replace=False)
+    source[src_cells] = rng.uniform(1e-4, 1e-2, 5)
+    c = np.where(fluid, rng.uniform(0.0, 1e-3, g.count), 0.0)
+    dt = 0.02
+    dg = pkg.pressure.DeviceGrid(g, preconditioner=case["numerics"]["pressure_preconditioner"])
+    if perturb:
+        area = np.asarray(g.face_area) * rng.uniform(0.8, 1.2, g.n_faces)
+        dist = np.asarray(g.face_distance) * rng.uniform(0.9, 1.1, g.n_faces)
+        og.set_faces(area, dist)
+        dg.update_faces(area, dist)
+    dev = torch.device("cuda", 0)
+    d_u, d_c = torch.from_numpy(u.copy()).to(dev), torch.from_numpy(c.copy()).to(dev)
+    d_d, d_s = torch.from_numpy(d).to(dev), torch.from_numpy(source).to(dev)
+    ref = c.copy()
+    for step in range(6):
+        ref = og.scalar_step(ref, u, d, source, dt)
+        dg.scalar_step_device(d_u.data_ptr(), d_c.data_ptr(), d_d.data_ptr(), d_s.data_ptr(), dt)
+        torch.cuda.synchronize()
+        got = d_c.cpu().numpy()
+        assert np.array_equal(bits(got), bits(ref)), f"step {step}: max diff {np.max(np.abs(got - ref)):.3e}"
+    dg.close()
+
+
+@pytest.mark.parametrize("name,perturb", [("wide-tiles", False), ("buildings-open-wall", False),
+                                          ("spacing-1.5m", False), ("wide-tiles", True)])
+def test_scalar_steps_extreme_values_bit_identical(pkg, O, name, perturb):
+    """Signed zeros, subnormals and values near the top of the range in the concentration,
+    diffusivity and source: the exponent-field products and the `+ 0.0` on bits must give
+    the FP64 operations' bits there too."""
+    torch = pytest.importorskip("torch")
+    case = flow_case(pkg, name)
+    g = pkg.grid.Grid.build(case)
+    og = O.Grid(case)
+    rng = np.random.default_rng(5)
+    u = np.where(np.isin(g.face_kind, (pkg.grid.INTERIOR, pkg.grid.INLET, pkg.grid.OUTLET)),
+                 rng.uniform(-3.0, 3.0, g.n_faces), 0.0)
+    pool = np.array([0.0, -0.0, 5e-324, -5e-324, 3e-310, -2.2e-308, 1e-300, 1.0, -7.5, 1e300, -3e299, 2.5e-16])
+    c = rng.choice(pool, g.count)
+    d = rng.choice(np.array([0.0, 1e-310, 0.1, 2.0, 1e-300]), g.count)
+    source = rng.choice(np.array([0.0, -0.0, 1e-320, 1e-3, -1e290]), g.count)
+    dt = 0.01
+    dg = pkg.pressure.DeviceGrid(g, preconditioner="multigrid")
+    if perturb:
+        area = np.asarray(g.face_area) * rng.uniform(0.8, 1.2, g.n_faces)
+        dist = np.asarray(g.face_distance) * rng.uniform(0.9, 1.1, g.n_faces)
+        og.set_faces(area, dist)
+        dg.update_faces(area, dist)
+    dev = torch.device("cuda", 0)
+    d_u, d_c = torch.from_numpy(u).to(dev), torch.from_numpy(c.copy()).to(dev)
+    d_d, d_s = torch.from_numpy(d).to(dev), torch.from_numpy(source).to(dev)
+    ref = c.copy()
+    for step in range(3):
+        ref = og.scalar_step(ref, u, d, source, dt)
+        dg.scalar_step_device(d_u.data_ptr(), d_c.data_ptr(), d_d.data_ptr(), d_s.data_ptr(), dt)
+        torch.cuda.synchronize()
+        got = d_c.cpu().numpy()
+        assert np.all(np.isfinite(ref))
+        bad = np.nonzero(bits(got) != bits(ref))[0]
+        assert bad.size == 0, f"step {step}: {bad.size} cells differ, first {bad[:4]}: {got[bad[:4]]} vs {ref[bad[:4]]}"
+    dg.close()
+
+
+def test_scalar_mass_conserved_in_closed_box(pkg):
+    """Walls on every side: no face leaves, so the mass grows by dt * emission per step."""
+    torch = pytest.importorskip("torch")
+    case = pkg.synth.case((96, 80, 48), 2.0, boundaries=("wall", "wall", "wall"), inflow=0.0,
+                          preconditioner="multigrid", boxes=[((60.0, 40.0, 0.0), (90.0, 100.0, 50.0))])
+    g = pkg.grid.Grid.build(case)
+    rng = np.random.default_rng(3)
+    interior = g.face_kind == pkg.grid.INTERIOR
+    u = np.where(interior, rng.uniform(-2.0, 2.0, g.n_faces), 0.0)
+    fluid = g.fluid.astype(bool)
+    c = np.where(fluid, rng.uniform(0.0, 1.0, g.count), 0.0)
+    source = np.where(fluid, rng.uniform(0.0, 1e-3, g.count), 0.0)
+    d = np.where(fluid, 0.1, 0.0)
+    dt = 0.01
+    dg = pkg.pressure.DeviceGrid(g, preconditioner="multigrid")
+    dev = torch.device("cuda", 0)
+    d_u, d_c = torch.from_numpy(u).to(dev), torch.from_numpy(c.copy()).to(dev)
+    d_d, d_s = torch.from_numpy(d).to(dev), torch.from_numpy(source).to(dev)
+    steps = 20
+    for _ in range(steps):
+        dg.scalar_step_device(d_u.data_ptr(), d_c.data_ptr(), d_d.data_ptr(), d_s.data_ptr(), dt)
+    torch.cuda.synchronize()
+    dg.close()
+    got = d_c.cpu().numpy()
+    m0, m1 = c.sum() * g.volume, got.sum() * g.volume
+    emitted = steps * dt * source.sum() * g.volume
+    assert abs(m1 - (m0 + emitted)) <= 1e-11 * m1
+    assert np.all(got[~fluid] == 0.0)

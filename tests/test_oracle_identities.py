@@ -218,3 +218,29 @@ def test_multigrid_cycle_is_symmetric(O, masked):
     z2, _ = g.mg_apply(r2)
     assert abs(z1 @ r2 - r1 @ z2) <= 1e-10 * max(abs(z1 @ r2), 1.0)
     assert z1 @ r1 > 0
+
+
+def test_scalar_step_matches_vectorised_restatement(pkg, O):
+    """advance_scalar (solver.rs:808-855) in the oracle's sequential form against an SSPRK2
+    composed from oracle/transport.py's vectorised rhs (which sums a cell's faces in
+    another order, hence 1e-13 relative, not bitwise)."""
+    from oracle import transport as T
+
+    case = pkg.synth.case((14, 10, 8), 1.0, inflow=2.0, boxes=[((4.0, 3.0, 0.0), (7.0, 6.0, 4.0))])
+    g = pkg.grid.Grid.build(case)
+    og = O.Grid(case)
+    rng = np.random.default_rng(2)
+    fluid = g.fluid.astype(bool)
+    u = np.where(g.face_kind != pkg.grid.WALL, rng.uniform(-2.0, 2.0, g.n_faces), 0.0)
+    d = np.where(fluid, rng.uniform(0.01, 0.3, g.count), 0.0)
+    source = np.where(fluid, rng.uniform(0.0, 1e-2, g.count), 0.0)
+    c = np.where(fluid, rng.uniform(0.0, 1.0, g.count), 0.0)
+    tr = T.Transport(g, d)
+    dt = 0.01
+    ref = c.copy()
+    for _ in range(3):
+        r1 = tr.rhs(ref, u, source)
+        stage = ref + dt * r1
+        ref = 0.5 * (ref + stage + dt * tr.rhs(stage, u, source))
+        c = og.scalar_step(c, u, d, source, dt)
+    assert np.max(np.abs(c - ref)) <= 1e-13 * np.max(np.abs(ref))
