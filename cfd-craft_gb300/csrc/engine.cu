@@ -2173,6 +2173,64 @@ int cfdg_scalar_step_device(cfdg_grid* G, const double* d_u, double* d_c, const 
   return 0;
 }
 
+// solver.rs:1035-1037: a receptor's value is Σ c[cell] w over its weights in order, an
+// Iterator::sum (from -0.0); one thread per receptor keeps that order.
+__global__ void k_receptors(const int64_t* __restrict__ off, const int32_t* __restrict__ cell,
+                            const double* __restrict__ w, const double* __restrict__ c, double* __restrict__ out,
+                            int n) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  double acc = -0.0;
+  for (long long k = off[r]; k < off[r + 1]; ++k) acc = acc + c[cell[k]] * w[k];
+  out[r] = acc;
+}
+
+int cfdg_receptors_set(cfdg_grid* G, int32_t n, const int64_t* offsets, const int64_t* cells,
+                       const double* weights) {
+  if (int e = check_grid(G)) return e;
+  if (n < 0 || (n > 0 && (!offsets || !cells || !weights))) return fail(CFDG_ERR_INVALID, "receptor arrays");
+  if (n > 0 && offsets[0] != 0) return fail(CFDG_ERR_INVALID, "receptor offsets must start at 0");
+  for (int32_t r = 0; r < n; ++r)
+    if (offsets[r + 1] <= offsets[r]) return fail(CFDG_ERR_INVALID, "a receptor has no weight");
+  const int64_t m = n > 0 ? offsets[n] : 0;
+  for (int64_t k = 0; k < m; ++k)
+    if (cells[k] < 0 || cells[k] >= G->h.cells) return fail(CFDG_ERR_INVALID, "a receptor cell is outside the grid");
+  std::lock_guard<std::mutex> lk(G->mu);
+  CU(cudaSetDevice(G->ctx->device));
+  // Grown arrays come from the grid's arena (released with the grid); smaller sets reuse them.
+  if (n + 1 > G->rc_cap_n) {
+    if (int e = G->arena.alloc(&G->rc_off, (size_t)n + 1)) return e;
+    G->rc_cap_n = n + 1;
+  }
+  if (m > G->rc_cap_entries) {
+    if (int e = G->arena.alloc(&G->rc_cell, (size_t)m)) return e;
+    if (int e = G->arena.alloc(&G->rc_w, (size_t)m)) return e;
+    G->rc_cap_entries = m;
+  }
+  std::vector<int32_t> c32(cells, cells + m);
+  cudaStream_t s = G->stream;
+  if (n > 0) {
+    CU(cudaMemcpyAsync(G->rc_off, offsets, ((size_t)n + 1) * 8, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(G->rc_cell, c32.data(), (size_t)m * 4, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(G->rc_w, weights, (size_t)m * 8, cudaMemcpyHostToDevice, s));
+  }
+  CU(cudaStreamSynchronize(s));  // the host arrays may go away after the return
+  G->rc_n = n;
+  return 0;
+}
+
+int cfdg_receptors_sample(cfdg_grid* G, const double* d_c, double* d_out) {
+  if (int e = check_grid(G)) return e;
+  std::lock_guard<std::mutex> lk(G->mu);
+  if (G->rc_n == 0) return 0;
+  if (!d_c || !d_out) return fail(CFDG_ERR_INVALID, "null array");
+  CU(cudaSetDevice(G->ctx->device));
+  const int n = G->rc_n;
+  k_receptors<<<(n + 127) / 128, 128, 0, G->stream>>>(G->rc_off, G->rc_cell, G->rc_w, d_c, d_out, n); tick(G);
+  CU(cudaGetLastError());
+  return 0;
+}
+
 int cfdg_debug_momentum_update(cfdg_grid* G, const double* u, const double* p, double dt, double* out) {
   if (int e = check_grid(G)) return e;
   if (!u || !p || !out) return fail(CFDG_ERR_INVALID, "null array");

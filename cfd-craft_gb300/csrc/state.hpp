@@ -197,6 +197,12 @@ struct cfdg_grid {
   double flow_size[3] = {0, 0, 0}, flow_vel[3] = {0, 0, 0}, flow_nu = 0, flow_acc[3] = {0, 0, 0};
   double *st_cu = nullptr, *st_v = nullptr, *st_v2 = nullptr, *st_p1 = nullptr;
   double* st_sc = nullptr;  // scalar transport: the SSPRK2 stage (N)
+  // Receptors (cfdg_receptors_set): CSR of cells and weights, in receptor order.
+  int32_t rc_n = 0, rc_cap_n = 0;
+  int64_t rc_cap_entries = 0;
+  int64_t* rc_off = nullptr;
+  int32_t* rc_cell = nullptr;
+  double* rc_w = nullptr;
   // Scalar transport on a uniform grid: per axis and transporting kind (interior, inlet,
   // outlet) the one face area and distance, bit for bit (refresh_weights).
   bool sc_uniform = false;

@@ -212,6 +212,20 @@ class DeviceGrid:
         self._check(self.L.cfdg_scalar_step_device(self.h, C.c_void_p(u_ptr), C.c_void_p(c_ptr), C.c_void_p(d_ptr),
                                                    C.c_void_p(source_ptr), float(dt)))
 
+    def set_receptors(self, weights):
+        """Receptor weights for sample_receptors (cfdg_receptors_set): one list of
+        (cell, weight) pairs per receptor, as receptors.receptor_weights returns them."""
+        off = np.zeros(len(weights) + 1, dtype=np.int64)
+        for r, w in enumerate(weights):
+            off[r + 1] = off[r] + len(w)
+        cells = np.array([c for w in weights for c, _ in w], dtype=np.int64)
+        vals = np.array([v for w in weights for _, v in w], dtype=np.float64)
+        self._check(self.L.cfdg_receptors_set(self.h, len(weights), _vp(off), _vp(cells), _vp(vals)))
+
+    def sample_receptors(self, c_ptr: int, out_ptr: int):
+        """The receptor values of the device concentration at c_ptr into out_ptr (device)."""
+        self._check(self.L.cfdg_receptors_sample(self.h, C.c_void_p(c_ptr), C.c_void_p(out_ptr)))
+
     def momentum_update(self, u, p, dt):
         """u + dt (R(u) - grad p) with the fixed face values, before a stage's projection."""
         u = np.ascontiguousarray(u, np.float64)

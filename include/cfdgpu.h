@@ -164,6 +164,17 @@ int cfdg_step_device(cfdg_grid *grid, double *d_u, double *d_p, double dt, doubl
  * concentration, bit-identical to it; the budgets are not kept. Non-periodic grids. */
 int cfdg_scalar_step_device(cfdg_grid *grid, const double *d_u, double *d_c, const double *d_diff,
                             const double *d_source, double dt);
+/* Receptors of a grid for cfdg_receptors_sample: n receptors' normalised weights as
+ * receptor_weights (transport.rs:374-436) returns them, in CSR form: receptor r holds
+ * cells[offsets[r] .. offsets[r+1]) with weights[...] in that order (host arrays, copied).
+ * Cells must lie in the grid; an empty receptor is CFDG_ERR_INVALID (the reference's E042
+ * is raised where the weights are made). Replaces the receptors set before. */
+int cfdg_receptors_set(cfdg_grid *grid, int32_t n, const int64_t *offsets, const int64_t *cells,
+                       const double *weights);
+/* The receptor values of the concentration d_c (device, N doubles) into d_out (device, n
+ * doubles), on the grid's stream: each the sum of c[cell] w in weight order, as the monitor
+ * row of solver.rs:1024-1041 computes it, bit-identical. */
+int cfdg_receptors_sample(cfdg_grid *grid, const double *d_c, double *d_out);
 /* Diagnostic: one stage's velocity before its projection, out = u + dt (R(u) - grad p) with
  * the fixed face values, on host arrays (F, N, F doubles). No reference counterpart. */
 int cfdg_debug_momentum_update(cfdg_grid *grid, const double *u, const double *p, double dt, double *out);

@@ -135,3 +135,53 @@ def test_scalar_mass_conserved_in_closed_box(pkg):
     emitted = steps * dt * source.sum() * g.volume
     assert abs(m1 - (m0 + emitted)) <= 1e-11 * m1
     assert np.all(got[~fluid] == 0.0)
+
+
+def test_receptor_values_bit_identical(pkg, O):
+    """cfdg_receptors_sample after device transport steps: each receptor's value is the
+    sum of c[cell] w in weight order (solver.rs:1035-1037), bit for bit."""
+    torch = pytest.importorskip("torch")
+    from importlib import import_module
+
+    R = import_module(pkg.__name__ + ".receptors")
+    case = flow_case(pkg, "wide-tiles")
+    g = pkg.grid.Grid.build(case)
+    og = O.Grid(case)
+    code, u, _, _ = og.project(g.initial_velocity(), np.zeros(g.count), 0.1, 1e-8, 10000)
+    assert code == 0
+    fluid = g.fluid.astype(bool)
+    rng = np.random.default_rng(9)
+    d = np.where(fluid, 0.05, 0.0)
+    source = np.zeros(g.count)
+    source[np.nonzero(fluid)[0][:40]] = 1e-3
+    receptors = [{"kind": "point", "point_m": [x, y, 3.3]} for x in (12.2, 40.0, 66.6) for y in (3.1, 9.5, 16.0)]
+    receptors += [{"kind": "volume_average", "min_m": [35.2, 2.0, 0.5], "max_m": [48.7, 17.5, 6.0]},
+                  {"kind": "point", "point_m": [0.2, 0.3, 10.8]}]
+    weights = []
+    for r in receptors:
+        try:
+            weights.append(R.receptor_weights(g, r))
+        except R.ReceptorError:
+            pass  # inside a building
+    assert len(weights) >= 6
+    dg = pkg.pressure.DeviceGrid(g, preconditioner="multigrid")
+    dg.set_receptors(weights)
+    dev = torch.device("cuda", 0)
+    d_u, d_c = torch.from_numpy(u).to(dev), torch.zeros(g.count, dtype=torch.float64, device=dev)
+    d_d, d_s = torch.from_numpy(d).to(dev), torch.from_numpy(source).to(dev)
+    out = torch.empty(len(weights), dtype=torch.float64, device=dev)
+    for _ in range(30):
+        dg.scalar_step_device(d_u.data_ptr(), d_c.data_ptr(), d_d.data_ptr(), d_s.data_ptr(), 0.05)
+    dg.sample_receptors(d_c.data_ptr(), out.data_ptr())
+    torch.cuda.synchronize()
+    c = d_c.cpu().numpy()
+    ref = []
+    for w in weights:
+        acc = -0.0
+        for cell, v in w:
+            acc = acc + c[cell] * v
+        ref.append(acc)
+    got = out.cpu().numpy()
+    dg.close()
+    assert np.array_equal(bits(got), bits(np.array(ref))), (got, ref)
+    assert np.count_nonzero(got) >= 3

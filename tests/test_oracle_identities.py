@@ -244,3 +244,25 @@ def test_scalar_step_matches_vectorised_restatement(pkg, O):
         ref = 0.5 * (ref + stage + dt * tr.rhs(stage, u, source))
         c = og.scalar_step(c, u, d, source, dt)
     assert np.max(np.abs(c - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+def test_receptor_point_weights_match_oracle(pkg):
+    """The package's receptor_weights (transport.rs:374-436) against the oracle's restatement."""
+    from importlib import import_module
+
+    from oracle import transport as T
+
+    R = import_module(pkg.__name__ + ".receptors")
+    case = pkg.synth.case((14, 10, 8), 2.0, inflow=2.0, boxes=[((8.0, 6.0, 0.0), (14.0, 12.0, 8.0))])
+    g = pkg.grid.Grid.build(case)
+    for p in ((1.0, 1.0, 1.0), (27.9, 19.5, 15.2), (5.3, 17.7, 3.9), (20.0, 3.0, 12.0)):
+        w = R.receptor_weights(g, {"kind": "point", "point_m": list(p)})
+        ref = T.point_weights(g, p)
+        assert [c for c, _ in w] == [c for c, _ in ref]
+        assert np.array_equal(np.array([v for _, v in w]), np.array([v for _, v in ref]))
+    with pytest.raises(R.ReceptorError):
+        R.receptor_weights(g, {"kind": "point", "point_m": [11.0, 9.0, 3.0]})  # a solid cell's centre
+    vol = R.receptor_weights(g, {"kind": "volume_average", "min_m": [0.5, 0.5, 0.5], "max_m": [3.0, 2.0, 1.5]})
+    # Overlaps 1.5 x 1.5 x 1.0 with cell (0,0,0) and 1.0 x 1.5 x 1.0 with cell (1,0,0).
+    assert [c for c, _ in vol] == [0, 1]
+    assert [v for _, v in vol] == [2.25 / 3.75, 1.5 / 3.75]
