@@ -288,9 +288,131 @@ static void center_plain(double* x, size_t n, bool anchored) {
 }
 
 // multigrid.rs:434-521
+// multigrid/line.rs:26-201: exact line (or small plane) solves for block Gauss-Seidel.
+// The blocks are the cells sharing their coordinates off `axes`; a periodic axis is folded
+// (0, n-1, 1, n-2, ...) so its cycle has a narrow band. Each block holds a banded Cholesky
+// factor with the diagonal replaced by its reciprocal; outside-block entries are kept as
+// rows of (column, value) in block order.
+struct BlockSmoother {
+  std::vector<int> axes;
+  size_t length = 0, bandwidth = 0;
+  std::vector<size_t> nodes, outside_offsets, outside_columns;
+  std::vector<double> outside_values, factor, scratch;
+
+  int build(const Matrix& m, const size_t n[3], const std::vector<int>& ax, const bool periodic[3], Control& control) {
+    axes = ax;
+    const size_t count = m.diagonal.size();
+    length = 1;
+    for (int a : axes) length *= n[a];
+    nodes.clear();
+    nodes.reserve(count);
+    for (size_t i = 0; i < count; ++i) {
+      size_t q[3] = {i % n[0], i / n[0] % n[1], i / (n[0] * n[1])};
+      bool skip = false;
+      for (int a : axes) skip |= q[a] != 0;
+      if (skip) continue;
+      for (size_t at = 0; at < length; ++at) {
+        size_t remainder = at;
+        for (int axis : axes) {
+          const size_t v = remainder % n[axis];
+          remainder /= n[axis];
+          q[axis] = !periodic[axis] ? v : (v % 2 == 0 ? v / 2 : n[axis] - 1 - v / 2);
+        }
+        nodes.push_back((q[2] * n[1] + q[1]) * n[0] + q[0]);
+      }
+    }
+    std::vector<size_t> position(count, 0);
+    for (size_t at = 0; at < nodes.size(); ++at) position[nodes[at]] = at;
+    bandwidth = 0;
+    for (size_t i = 0; i < count; ++i) {
+      const size_t pi = position[i];
+      for (size_t at = m.offsets[i]; at < m.offsets[i + 1]; ++at) {
+        const size_t pj = position[m.columns[at]];
+        if (pi / length == pj / length) bandwidth = std::max(bandwidth, pi > pj ? pi - pj : pj - pi);
+      }
+    }
+    const size_t stride = bandwidth + 1;
+    outside_offsets.assign(1, 0);
+    outside_columns.clear();
+    outside_values.clear();
+    for (size_t at = 0; at < nodes.size(); ++at) {
+      const size_t cell = nodes[at];
+      for (size_t e = m.offsets[cell]; e < m.offsets[cell + 1]; ++e) {
+        const size_t col = m.columns[e];
+        if (position[col] / length != at / length) {
+          outside_columns.push_back(col);
+          outside_values.push_back(m.values[e]);
+        }
+      }
+      outside_offsets.push_back(outside_columns.size());
+    }
+    factor.assign(count * stride, 0.0);
+    for (size_t at = 0; at < nodes.size(); ++at) {
+      const size_t cell = nodes[at];
+      factor[at * stride] = m.diagonal[cell];
+      for (size_t e = m.offsets[cell]; e < m.offsets[cell + 1]; ++e) {
+        const size_t col = position[m.columns[e]];
+        if (col / length == at / length && col < at) factor[at * stride + at - col] += m.values[e];
+      }
+    }
+    for (size_t line = 0; line < count / length; ++line) {
+      if (line % 128 == 0) {
+        int c = control.check();
+        if (c) return c;
+      }
+      const size_t base = line * length * stride;
+      for (size_t i = 0; i < length; ++i)
+        for (size_t j = i > bandwidth ? i - bandwidth : 0; j <= i; ++j) {
+          const size_t row = base + i * stride, other = base + j * stride;
+          double value = factor[row + i - j];
+          for (size_t k = i > bandwidth ? i - bandwidth : 0; k < j; ++k)
+            value -= factor[row + i - k] * factor[other + j - k];
+          if (i == j) {
+            if (!std::isfinite(value) || value <= 0.0) return E036;
+            factor[row] = std::sqrt(value);
+          } else {
+            factor[row + i - j] = value / factor[other];
+          }
+        }
+    }
+    for (size_t row = 0; row < count; ++row) factor[row * stride] = 1.0 / factor[row * stride];
+    scratch.assign(length, 0.0);
+    return OK;
+  }
+
+  // line.rs:155-190
+  void sweep(const double* rhs, double* x, bool backward) {
+    const size_t count = nodes.size() / length, stride = bandwidth + 1;
+    for (size_t at = 0; at < count; ++at) {
+      const size_t line = backward ? count - 1 - at : at;
+      const size_t start = line * length, base = start * stride;
+      for (size_t i = 0; i < length; ++i) {
+        double value = rhs[nodes[start + i]];
+        for (size_t e = outside_offsets[start + i]; e < outside_offsets[start + i + 1]; ++e)
+          value -= outside_values[e] * x[outside_columns[e]];
+        scratch[i] = value;
+      }
+      for (size_t i = 0; i < length; ++i) {
+        const size_t row = base + i * stride;
+        double value = scratch[i];
+        for (size_t j = i > bandwidth ? i - bandwidth : 0; j < i; ++j) value -= factor[row + i - j] * scratch[j];
+        scratch[i] = value * factor[row];
+      }
+      for (size_t i = length; i-- > 0;) {
+        double value = scratch[i];
+        for (size_t j = i + 1; j < std::min(length, i + bandwidth + 1); ++j)
+          value -= factor[base + j * stride + j - i] * scratch[j];
+        scratch[i] = value * factor[base + i * stride];
+      }
+      for (size_t i = 0; i < length; ++i) x[nodes[start + i]] = scratch[i];
+    }
+  }
+};
+
 struct Level {
   Matrix matrix;
   Transfer transfer;
+  std::vector<BlockSmoother> lines;  // anisotropic levels: replaces the point sweeps
   std::vector<double> rhs, x, residual, cholesky;
   bool anchored = true;
   bool terminal = false;
@@ -953,13 +1075,13 @@ static int masked_build(const Grid& g, Control& control, Hierarchy& h) {
   return OK;
 }
 
-// multigrid.rs:530-645 (point smoothing only; line smoothing is not restated)
+// multigrid.rs:530-645, with the line/plane block smoothers of anisotropic grids (:573-607)
 static int hierarchy_build(const Grid& g, Control& control, Hierarchy& h) {
   bool any_solid = false;
   for (auto v : g.fluid) any_solid |= !v;
   if (any_solid || g.components.size() != 1) return masked_build(g, control, h);
   size_t n[3] = {g.n[0], g.n[1], g.n[2]};
-  if (!line_axes(g.n, g.dx).empty()) return UNSUPPORTED;
+  const std::vector<int> axes = line_axes(g.n, g.dx);
   std::vector<double> centers[3];
   for (int a = 0; a < 3; ++a)
     for (size_t i = 0; i < n[a]; ++i) centers[a].push_back((double)i + 0.5);
@@ -996,8 +1118,38 @@ static int hierarchy_build(const Grid& g, Control& control, Hierarchy& h) {
       break;
     }
     bool coarsen[3] = {n[0] > 2, n[1] > 2, n[2] > 2};
+    if (!axes.empty()) {
+      // Weak-axis modes are kept until the stiff directions have collapsed (:575-581).
+      bool stiff_can_coarsen = false;
+      for (int a : axes) stiff_can_coarsen |= n[a] > 2;
+      for (int a = 0; a < 3; ++a) {
+        const bool in_axes = std::find(axes.begin(), axes.end(), a) != axes.end();
+        coarsen[a] = n[a] > 2 && (!stiff_can_coarsen || in_axes);
+      }
+    }
     std::vector<double> coarse[3];
     level.transfer = transfer_build(n, centers, periodic, extent, coarsen, coarse);
+    // :584-599: one plane block over all stiff axes when it holds at most 16 cells, else
+    // lines along the stiff axis of smallest spacing (the first of equals).
+    std::vector<std::vector<int>> groups;
+    if (!axes.empty()) {
+      size_t plane = 1;
+      for (int a : axes) plane *= n[a];
+      if (axes.size() > 1 && plane <= 16) {
+        groups.push_back(axes);
+      } else {
+        int best = axes[0];
+        for (int a : axes)
+          if (g.dx[a] < g.dx[best]) best = a;
+        groups.push_back({best});
+      }
+    }
+    for (auto& grp : groups) {
+      BlockSmoother b;
+      int e = b.build(level.matrix, n, grp, periodic, control);
+      if (e) return e;
+      level.lines.push_back(std::move(b));
+    }
     for (int a = 0; a < 3; ++a) n[a] = coarse[a].size();
     std::vector<Edge> ce;
     std::vector<double> ca;
@@ -1025,7 +1177,11 @@ static void cycle(std::vector<Level>& levels, size_t at, Info& w) {
   }
   size_t n = level.x.size();
   std::fill(level.x.begin(), level.x.end(), 0.0);
-  for (int pass = 0; pass < 2; ++pass) level.matrix.sweep(level.rhs.data(), level.x.data(), n, false);
+  const int sweeps = level.lines.empty() ? 2 : 1;
+  for (int pass = 0; pass < sweeps; ++pass) {
+    if (level.lines.empty()) level.matrix.sweep(level.rhs.data(), level.x.data(), n, false);
+    else level.lines[pass % level.lines.size()].sweep(level.rhs.data(), level.x.data(), false);
+  }
   center_plain(level.x.data(), n, level.anchored);
   level.matrix.product(level.x.data(), level.residual.data(), n);
   for (size_t i = 0; i < n; ++i) level.residual[i] = level.rhs[i] - level.residual[i];
@@ -1044,9 +1200,12 @@ static void cycle(std::vector<Level>& levels, size_t at, Info& w) {
       s += level.transfer.weights[k] * next.x[level.transfer.columns[k]];
     level.x[i] += s;
   }
-  for (int pass = 0; pass < 2; ++pass) level.matrix.sweep(level.rhs.data(), level.x.data(), n, true);
+  for (int pass = 0; pass < sweeps; ++pass) {
+    if (level.lines.empty()) level.matrix.sweep(level.rhs.data(), level.x.data(), n, true);
+    else level.lines[(sweeps - 1 - pass) % level.lines.size()].sweep(level.rhs.data(), level.x.data(), true);
+  }
   center_plain(level.x.data(), n, level.anchored);
-  w.smoothing_cell_updates += 4 * n;
+  w.smoothing_cell_updates += 2 * sweeps * n;
   w.residual_cell_updates += n;
   w.restriction_cell_updates += n;
   w.prolongation_cell_updates += n;
