@@ -597,9 +597,46 @@ struct PLev {
   const int *ioff, *idx;
   const long long* foff;
   const double* fac;
+  // Sweeps each way (2, or 1 with block smoothing) and the block smoother, if any.
+  int nsweep, lines, llen, lbw;
+  int lnfwd, lnbwd, lblocal, pad2_;
+  const int *lnodes, *looff, *locol;
+  const double *loval, *lfac;
+  double* lscr;
+  const int *lfo, *lfs, *lbo, *lbs;
 };
 
 namespace cg = cooperative_groups;
+
+// multigrid/line.rs:155-190, one block: the right-hand side less the outside entries, the
+// banded forward and backward substitutions (the diagonal stored as its reciprocal), then
+// the block's values written to x. One thread, in the reference's order (bit-identical);
+// x and rhs come through L2 (other blocks of the launch write them).
+__device__ __noinline__ void line_block(int b, const PLev& L, const double* rhs, double* x) {
+  const int len = L.llen, bw = L.lbw;
+  const long long stride = bw + 1;
+  const int start = b * len;
+  const long long base = (long long)start * stride;
+  double* __restrict__ scr = L.lscr + start;
+  const double* __restrict__ fac = L.lfac;
+  for (int i = 0; i < len; ++i) {
+    double v = __ldcg(&rhs[L.lnodes[start + i]]);
+    for (int e = L.looff[start + i]; e < L.looff[start + i + 1]; ++e) v = v - L.loval[e] * __ldcg(&x[L.locol[e]]);
+    scr[i] = v;
+  }
+  for (int i = 0; i < len; ++i) {
+    const long long row = base + i * stride;
+    double v = scr[i];
+    for (int j = max(0, i - bw); j < i; ++j) v = v - fac[row + i - j] * scr[j];
+    scr[i] = v * fac[row];
+  }
+  for (int i = len - 1; i >= 0; --i) {
+    double v = scr[i];
+    for (int j = i + 1; j < min(len, i + bw + 1); ++j) v = v - fac[base + j * stride + j - i] * scr[j];
+    scr[i] = v * fac[base + i * stride];
+  }
+  for (int i = 0; i < len; ++i) x[L.lnodes[start + i]] = scr[i];
+}
 
 __device__ void pc_center(const PLev& L, double* v, double* sh, double* mean, cg::grid_group& grid) {
   if (L.ngroups == 0) return;
@@ -608,7 +645,36 @@ __device__ void pc_center(const PLev& L, double* v, double* sh, double* mean, cg
   grid.sync();
 }
 
+// A block Gauss-Seidel sweep over the block dependency levels (blocks of one level share
+// no entry, so they run in parallel; the reference's block order is kept where it matters).
+__device__ void pc_lines(const PLev& L, bool backward, cg::grid_group& grid) {
+  const int* order = backward ? L.lbo : L.lfo;
+  const int* start = backward ? L.lbs : L.lfs;
+  const int nlev = backward ? L.lnbwd : L.lnfwd;
+  if (L.lblocal) {
+    if (blockIdx.x == 0)
+      for (int dl = 0; dl < nlev; ++dl) {
+        for (int t = start[dl] + threadIdx.x; t < start[dl + 1]; t += blockDim.x) line_block(order[t], L, L.rhs, L.x);
+        __threadfence();
+        __syncthreads();
+      }
+    __threadfence();
+    grid.sync();
+    return;
+  }
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  for (int dl = 0; dl < nlev; ++dl) {
+    for (int t = start[dl] + gt; t < start[dl + 1]; t += nth) line_block(order[t], L, L.rhs, L.x);
+    __threadfence();
+    grid.sync();
+  }
+}
+
 __device__ void pc_sweep(const PLev& L, bool backward, cg::grid_group& grid) {
+  if (L.lines) {
+    pc_lines(L, backward, grid);
+    return;
+  }
   const int* order = backward ? L.bo : L.fo;
   const int* start = backward ? L.bs : L.fs;
   const int nlev = backward ? L.nbwd : L.nfwd;
@@ -652,8 +718,7 @@ __global__ void __launch_bounds__(BLOCK) k_plain_coarse(const PLev* lv, int nl, 
       pc_center(L, L.x, sh, &mean, grid);
       break;
     }
-    pc_sweep(L, false, grid);
-    pc_sweep(L, false, grid);
+    for (int sw = 0; sw < L.nsweep; ++sw) pc_sweep(L, false, grid);
     pc_center(L, L.x, sh, &mean, grid);
     for (int i = gt; i < L.n; i += nth) residual_row(i, L.off, L.col, L.val, L.diag, L.rhs, L.x, L.res);
     __threadfence();
@@ -670,8 +735,7 @@ __global__ void __launch_bounds__(BLOCK) k_plain_coarse(const PLev* lv, int nl, 
     for (int i = gt; i < L.n; i += nth) prolong_row(i, L.poff, L.pcol, L.pval, N.x, L.x);
     __threadfence();
     grid.sync();
-    pc_sweep(L, true, grid);
-    pc_sweep(L, true, grid);
+    for (int sw = 0; sw < L.nsweep; ++sw) pc_sweep(L, true, grid);
     pc_center(L, L.x, sh, &mean, grid);
   }
 }
@@ -858,7 +922,8 @@ void launch_vcycle(cfdg_grid* G, const double* r, double* z, const Scalars* S) {
   const int nl = (int)H.levels.size();
   // Levels 1 .. L-1 in one cooperative launch when available, else level by level.
   const bool coop = H.coop_blocks > 0 && nl > 1;
-  for (int l = 0; l < (coop ? 1 : nl); ++l) {
+  const int first = H.coop0 ? 0 : 1;  // the first level of the cooperative launch
+  for (int l = 0; l < (coop ? first : nl); ++l) {
     DevLevel& L = H.levels[l];
     const bool full = l == 0 && H.full0;
     launch_center(G, L.groups, L.ngroups, L.rhs, S);
@@ -895,10 +960,10 @@ void launch_vcycle(cfdg_grid* G, const double* r, double* z, const Scalars* S) {
     at[0].val.cooperative = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, k_plain_coarse, (const PLev*)H.d_plev, nl - 1, S);
+    cudaLaunchKernelEx(&cfg, k_plain_coarse, (const PLev*)H.d_plev, nl - first, S);
     tick(G);
   }
-  for (int l = coop ? 0 : nl - 2; l >= 0; --l) {
+  for (int l = coop ? first - 1 : nl - 2; l >= 0; --l) {
     DevLevel& L = H.levels[l];
     DevLevel& C = H.levels[l + 1];
     const bool full = l == 0 && H.full0;
@@ -1064,7 +1129,8 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
     if (e == CFDG_E035) return fail(e, "CFD-E035: numerics.pressure_preconditioner: multigrid coarse Cholesky lost positive definiteness");
     if (e == CFDG_CANCELLED) return fail(e, "cancelled");
     if (e == CFDG_WALL_TIME) return fail(e, "wall_time_limit");
-    if (e == CFDG_ERR_UNSUPPORTED) return fail(e, "strongly anisotropic spacing needs line smoothing, which this engine does not implement");
+    if (e == CFDG_E036)
+      return fail(e, "CFD-E036: numerics.pressure_preconditioner: multigrid line Cholesky lost positive definiteness");
     return fail(e, "multigrid setup failed");
   }
   auto D = std::make_unique<DevHierarchy>();
@@ -1075,7 +1141,9 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
   if (H.masked)
     if (int e = D->arena.upload(&D->fluid_idx, H.fluid_indices, s)) return e;
   D->levels.resize(H.levels.size());
-  D->full0 = G->structured && H.levels.size() > 1;
+  const bool lines = !H.levels.empty() && !H.levels[0].lines.empty();
+  D->full0 = G->structured && H.levels.size() > 1 && !lines;
+  D->coop0 = lines && H.levels.size() > 1;
   if (D->full0) {
     // Re-index level 0 from compact fluid numbering to full-grid cells.
     MgLevel& M = H.levels[0];
@@ -1135,13 +1203,33 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
     if (int e = D->arena.alloc(&L.rhs, L.n)) return e;
     if (int e = D->arena.alloc(&L.x, L.n)) return e;
     if (int e = D->arena.alloc(&L.res, L.n)) return e;
+    if (!M.lines.empty()) {
+      const LineBlocks& B = M.lines[0];  // the reference builds one block group per level
+      L.lines = true;
+      L.llen = B.length;
+      L.lbw = B.bandwidth;
+      L.lcount = B.count();
+      if (int e = D->arena.upload(&L.lnodes, B.nodes, s)) return e;
+      if (int e = D->arena.upload(&L.looff, B.outside.off, s)) return e;
+      if (int e = D->arena.upload(&L.locol, B.outside.col, s)) return e;
+      if (int e = D->arena.upload(&L.loval, B.outside.val, s)) return e;
+      if (int e = D->arena.upload(&L.lfac, B.factor, s)) return e;
+      if (int e = D->arena.alloc(&L.lscr, B.nodes.size())) return e;
+      if (int e = D->arena.upload(&L.lfwd.order, B.fwd.order, s)) return e;
+      if (int e = D->arena.upload(&L.lbwd.order, B.bwd.order, s)) return e;
+      L.lfwd.start = B.fwd.start;
+      L.lbwd.start = B.bwd.start;
+      if (int e = D->arena.upload(&L.lfwd.d_start, B.fwd.start, s)) return e;
+      if (int e = D->arena.upload(&L.lbwd.d_start, B.bwd.start, s)) return e;
+    }
   }
   D->level_cells = H.level_cells;
   D->level_nonzeros = H.level_nonzeros;
-  // Levels 1 .. L-1 for the cooperative coarse kernel, when its grid can be co-resident.
+  // Levels 1 .. L-1 (0 .. L-1 for block-smoothed hierarchies) for the cooperative kernel,
+  // when its grid can be co-resident.
   if (D->levels.size() > 1) {
     std::vector<PLev> pl;
-    for (size_t l = 1; l < D->levels.size(); ++l) {
+    for (size_t l = D->coop0 ? 0 : 1; l < D->levels.size(); ++l) {
       const DevLevel& L = D->levels[l];
       PLev P{};
       P.n = L.n;
@@ -1161,6 +1249,20 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
       P.poff = L.prolong.off, P.pcol = L.prolong.col, P.pval = L.prolong.val;
       P.rhs = L.rhs, P.x = L.x, P.res = L.res;
       P.ioff = L.d_ioff, P.idx = L.d_idx, P.foff = L.d_foff, P.fac = L.d_fac;
+      P.nsweep = L.lines ? 1 : 2;  // multigrid.rs:676
+      P.lines = L.lines ? 1 : 0;
+      if (L.lines) {
+        P.llen = L.llen, P.lbw = L.lbw;
+        P.lnfwd = (int)L.lfwd.start.size() - 1;
+        P.lnbwd = (int)L.lbwd.start.size() - 1;
+        int lmax = 0;
+        for (int q = 0; q < P.lnfwd; ++q) lmax = std::max(lmax, L.lfwd.start[q + 1] - L.lfwd.start[q]);
+        for (int q = 0; q < P.lnbwd; ++q) lmax = std::max(lmax, L.lbwd.start[q + 1] - L.lbwd.start[q]);
+        P.lblocal = lmax <= BLOCK ? 1 : 0;
+        P.lnodes = L.lnodes, P.looff = L.looff, P.locol = L.locol, P.loval = L.loval, P.lfac = L.lfac;
+        P.lscr = L.lscr;
+        P.lfo = L.lfwd.order, P.lfs = L.lfwd.d_start, P.lbo = L.lbwd.order, P.lbs = L.lbwd.d_start;
+      }
       pl.push_back(P);
     }
     PLev* dp = nullptr;
@@ -1176,6 +1278,8 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
       per = 0;
     }
     D->coop_blocks = per > 0 ? sms : 0;
+    if (D->coop0 && D->coop_blocks == 0)
+      return fail(CFDG_ERR_UNSUPPORTED, "block-smoothed multigrid needs a co-resident cooperative launch");
   }
   CU(cudaStreamSynchronize(s));
   G->host_mg = std::make_shared<Hierarchy>(std::move(H));
@@ -1327,9 +1431,12 @@ int solve_device(cfdg_grid* G, bool use_terms, double tol, uint64_t max_iter, co
   if (G->preconditioner == CFDG_PRECOND_MULTIGRID && G->mg) {
     uint64_t cyc = inf->preconditioner_applications;
     inf->cycles = cyc;
-    uint64_t inner = 0;
-    for (size_t l = 0; l + 1 < G->mg->levels.size(); ++l) inner += G->mg->levels[l].n;
-    inf->smoothing_cell_updates = 4 * inner * cyc;
+    uint64_t inner = 0, smooth = 0;
+    for (size_t l = 0; l + 1 < G->mg->levels.size(); ++l) {
+      inner += G->mg->levels[l].n;
+      smooth += (G->mg->levels[l].lines ? 2 : 4) * (uint64_t)G->mg->levels[l].n;  // 2 x sweeps
+    }
+    inf->smoothing_cell_updates = smooth * cyc;
     inf->residual_cell_updates = inner * cyc;
     inf->restriction_cell_updates = inner * cyc;
     inf->prolongation_cell_updates = inner * cyc;

@@ -1734,6 +1734,9 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     F.fw32 = d;
   }
   const MgLevel& M0 = H.levels[0];
+  if (!M0.lines.empty())
+    return fail(CFDG_ERR_UNSUPPORTED,
+                "mixed form: the line/plane block smoothers of anisotropic grids run in the plain form only");
   if ((int64_t)M0.diag.size() != (int64_t)h.cells)
     return fail(CFDG_ERR_UNSUPPORTED, "mixed form: level 0 must cover every cell");
   // The split layout of the level-0 FP32 arrays (slot of each cell, cell of each slot).

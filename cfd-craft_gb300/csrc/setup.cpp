@@ -498,10 +498,108 @@ static std::vector<int> line_axes(const int32_t n[3], const double dx[3]) {
   return out;
 }
 
-// multigrid.rs:530-645 with point smoothing (tensor-linear P, Galerkin coarse operators).
+// multigrid/line.rs:39-150 BlockSmoother::build: node order (a periodic axis folded to
+// 0, n-1, 1, n-2, ...), bandwidth from the entries, outside-block rows, banded Cholesky per
+// block with reciprocal diagonals; CFD-E036 on a non-positive pivot. The block-level
+// dependency schedules are the engine's (blocks that share an outside entry).
+static int build_lines(const Csr& a, const std::vector<double>& diag, const int32_t n[3], const std::vector<int>& axes,
+                       const bool periodic[3], const Poller& poll, LineBlocks& out) {
+  const int32_t count = (int32_t)diag.size();
+  out.axes.assign(axes.begin(), axes.end());
+  int32_t length = 1;
+  for (int ax : axes) length *= n[ax];
+  out.length = length;
+  out.nodes.clear();
+  out.nodes.reserve(count);
+  for (int32_t i = 0; i < count; ++i) {
+    int32_t q[3] = {i % n[0], i / n[0] % n[1], i / (n[0] * n[1])};
+    bool skip = false;
+    for (int ax : axes) skip |= q[ax] != 0;
+    if (skip) continue;
+    for (int32_t at = 0; at < length; ++at) {
+      int32_t remainder = at;
+      for (int ax : axes) {
+        const int32_t v = remainder % n[ax];
+        remainder /= n[ax];
+        q[ax] = !periodic[ax] ? v : (v % 2 == 0 ? v / 2 : n[ax] - 1 - v / 2);
+      }
+      out.nodes.push_back((q[2] * n[1] + q[1]) * n[0] + q[0]);
+    }
+  }
+  std::vector<int32_t> position(count, 0);
+  for (int32_t at = 0; at < (int32_t)out.nodes.size(); ++at) position[out.nodes[at]] = at;
+  int32_t bw = 0;
+  for (int32_t i = 0; i < count; ++i)
+    for (int32_t k = a.off[i]; k < a.off[i + 1]; ++k) {
+      const int32_t pi = position[i], pj = position[a.col[k]];
+      if (pi / length == pj / length) bw = std::max(bw, pi > pj ? pi - pj : pj - pi);
+    }
+  out.bandwidth = bw;
+  const int64_t stride = bw + 1;
+  out.outside.off.assign(1, 0);
+  out.outside.col.clear();
+  out.outside.val.clear();
+  for (int32_t at = 0; at < (int32_t)out.nodes.size(); ++at) {
+    const int32_t cell = out.nodes[at];
+    for (int32_t k = a.off[cell]; k < a.off[cell + 1]; ++k)
+      if (position[a.col[k]] / length != at / length) {
+        out.outside.col.push_back(a.col[k]);
+        out.outside.val.push_back(a.val[k]);
+      }
+    out.outside.off.push_back((int32_t)out.outside.col.size());
+  }
+  std::vector<double>& f = out.factor;
+  f.assign((size_t)count * stride, 0.0);
+  for (int32_t at = 0; at < (int32_t)out.nodes.size(); ++at) {
+    const int32_t cell = out.nodes[at];
+    f[at * stride] = diag[cell];
+    for (int32_t k = a.off[cell]; k < a.off[cell + 1]; ++k) {
+      const int32_t col = position[a.col[k]];
+      if (col / length == at / length && col < at) f[at * stride + at - col] += a.val[k];
+    }
+  }
+  for (int32_t line = 0; line < count / length; ++line) {
+    if (line % 128 == 0)
+      if (int c = poll.check()) return c;
+    const int64_t base = (int64_t)line * length * stride;
+    for (int32_t i = 0; i < length; ++i)
+      for (int32_t j = std::max(0, i - bw); j <= i; ++j) {
+        const int64_t row = base + i * stride, other = base + j * stride;
+        double value = f[row + i - j];
+        for (int32_t k = std::max(0, i - bw); k < j; ++k) value -= f[row + i - k] * f[other + j - k];
+        if (i == j) {
+          if (!std::isfinite(value) || value <= 0.0) return CFDG_E036;
+          f[row] = std::sqrt(value);
+        } else {
+          f[row + i - j] = value / f[other];
+        }
+      }
+  }
+  for (int32_t row = 0; row < count; ++row) f[row * stride] = 1.0 / f[row * stride];
+  // Block dependency pattern: block b reads the cells of the blocks its outside entries name.
+  const int32_t nb = count / length;
+  std::vector<std::vector<int32_t>> adj(nb);
+  for (int32_t at = 0; at < (int32_t)out.nodes.size(); ++at)
+    for (int32_t k = out.outside.off[at]; k < out.outside.off[at + 1]; ++k)
+      adj[at / length].push_back(position[out.outside.col[k]] / length);
+  Csr pattern;
+  pattern.off.assign(1, 0);
+  for (auto& v : adj) {
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    pattern.col.insert(pattern.col.end(), v.begin(), v.end());
+    pattern.off.push_back((int32_t)pattern.col.size());
+  }
+  out.fwd = schedule(pattern, false);
+  out.bwd = schedule(pattern, true);
+  return 0;
+}
+
+// multigrid.rs:530-645 (tensor-linear P, Galerkin coarse operators), with the line/plane
+// block smoothers and semicoarsening of anisotropic grids (:573-607).
 static int build_unmasked(const HostGrid& g, const Poller& poll, Hierarchy& h) {
   h.masked = false;
-  if (!line_axes(g.n, g.dx).empty()) return CFDG_ERR_UNSUPPORTED;
+  const std::vector<int> axes = line_axes(g.n, g.dx);
   int32_t n[3] = {g.n[0], g.n[1], g.n[2]};
   std::vector<double> centers[3];
   for (int a = 0; a < 3; ++a)
@@ -551,11 +649,38 @@ static int build_unmasked(const HostGrid& g, const Poller& poll, Hierarchy& h) {
       h.levels.push_back(std::move(lev));
       break;
     }
+    // Which axes coarsen: all with more than two cells, or on anisotropic grids only the
+    // stiff ones until they are down to two cells (multigrid.rs:575-581).
+    bool coarsen[3] = {n[0] > 2, n[1] > 2, n[2] > 2};
+    if (!axes.empty()) {
+      bool stiff_can_coarsen = false;
+      for (int a : axes) stiff_can_coarsen |= n[a] > 2;
+      for (int a = 0; a < 3; ++a) {
+        const bool in_axes = std::find(axes.begin(), axes.end(), a) != axes.end();
+        coarsen[a] = n[a] > 2 && (!stiff_can_coarsen || in_axes);
+      }
+      // :584-599: one plane block over all stiff axes when it holds at most 16 cells,
+      // else lines along the stiff axis of smallest spacing (the first of equals).
+      std::vector<int> group;
+      int32_t plane = 1;
+      for (int a : axes) plane *= n[a];
+      if (axes.size() > 1 && plane <= 16) {
+        group = axes;
+      } else {
+        int best = axes[0];
+        for (int a : axes)
+          if (g.dx[a] < g.dx[best]) best = a;
+        group = {best};
+      }
+      LineBlocks lb;
+      if (int e = build_lines(lev.a, lev.diag, n, group, periodic, poll, lb)) return e;
+      lev.lines.push_back(std::move(lb));
+    }
     // Tensor-linear interpolation (multigrid.rs:330-371).
     std::vector<double> coarse[3];
     std::vector<std::vector<std::pair<int32_t, double>>> wts[3];
     for (int a = 0; a < 3; ++a) {
-      size_t step = n[a] > 2 ? 2 : 1;
+      size_t step = coarsen[a] ? 2 : 1;
       for (size_t s = 0; s < centers[a].size(); s += step) {
         size_t e = std::min(s + step, centers[a].size());
         double sum = -0.0;

@@ -71,7 +71,24 @@ struct Poller {
   int check() const;  // 0, or CFDG_CANCELLED / CFDG_WALL_TIME
 };
 
-// One level of the symmetric V(2,2) cycle (multigrid.rs:667-726, masked.rs:304-342).
+// The line (or small plane) block smoother of an anisotropic level (multigrid/line.rs:
+// 26-150): block b is nodes[b*length .. (b+1)*length); `outside` holds, per node position,
+// the level's entries whose column lies in another block (value, column); `factor` holds
+// each block's banded Cholesky factor (stride bandwidth+1, entry [pos*stride + d] = L(pos,
+// pos-d)) with the diagonal replaced by its reciprocal. fwd/bwd: the blocks grouped by
+// dependency level for a forward / backward block Gauss-Seidel sweep.
+struct LineBlocks {
+  int32_t length = 0, bandwidth = 0;
+  std::vector<int32_t> axes;
+  std::vector<int32_t> nodes;
+  Csr outside;
+  std::vector<double> factor;
+  Schedule fwd, bwd;
+  int32_t count() const { return length ? (int32_t)(nodes.size() / length) : 0; }
+};
+
+// One level of the symmetric V(2,2) cycle (multigrid.rs:667-726, masked.rs:304-342), or
+// V(1,1) with block smoothers on anisotropic grids.
 struct MgLevel {
   int32_t n = 0;
   Csr a;  // off-diagonal entries in the reference's row order (multigrid.rs:233-262)
@@ -84,6 +101,9 @@ struct MgLevel {
   // inside one bin, so neighbouring nodes sit in face-adjacent bins and the parity is
   // a two-colouring of the level's graph (used by the parallel smoothers).
   std::vector<uint8_t> parity;
+  // Anisotropic unmasked levels: the block smoothers, used in turn by the cycle's sweeps
+  // (one sweep each way, multigrid.rs:676-718); empty for point Gauss-Seidel.
+  std::vector<LineBlocks> lines;
   // Terminal level: dense lower Cholesky blocks (masked.rs:16-70, multigrid.rs:468-520).
   Csr direct_idx;                   // block -> solved indices
   std::vector<int64_t> direct_off;  // block -> offset of its n*n factor in direct_factor

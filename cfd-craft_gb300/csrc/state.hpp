@@ -124,6 +124,12 @@ struct DevLevel {
   long long* d_foff = nullptr;
   double* d_fac = nullptr;
   double *rhs = nullptr, *x = nullptr, *res = nullptr;
+  // Anisotropic levels: the block smoother (setup.hpp LineBlocks) and its scratch.
+  bool lines = false;
+  int llen = 0, lbw = 0, lcount = 0;
+  int *lnodes = nullptr, *looff = nullptr, *locol = nullptr;
+  double *loval = nullptr, *lfac = nullptr, *lscr = nullptr;
+  DevSchedule lfwd, lbwd;
 };
 
 struct DevHierarchy {
@@ -139,6 +145,9 @@ struct DevHierarchy {
   // (0: not co-resident, the level-by-level launches are used instead).
   void* d_plev = nullptr;
   int coop_blocks = 0;
+  // Block-smoothed (anisotropic) hierarchies: d_plev starts at level 0 and the whole cycle
+  // is the cooperative launch.
+  bool coop0 = false;
 };
 
 }  // namespace cfdg

@@ -88,3 +88,55 @@ def sin_field(n, k=0.73):
     import numpy as np
 
     return np.array([math.sin(k * float(i)) for i in range(n)])
+
+
+# docs/evidence/anisotropic-pressure.md:122-141 (shapes) and :41-60 (iterations IC(0) /
+# point MG / candidate MG): the rough manufactured pressure sin(0.73 i) + 0.3 cos(0.17 i),
+# centred, its operator image as the RHS (examples/pressure_probe.rs:60-68), tol 1e-14,
+# at most 1200 iterations. The oracle's multigrid is the candidate (line/plane block
+# smoothing with semicoarsening on anisotropic grids, multigrid/line.rs); on the three
+# shapes below the anisotropy threshold it is the point cycle, whose counts equal the
+# candidate's there.
+ANISOTROPIC = {
+    "isotropic": ([24, 2, 24], [1.0, 1.0, 1.0], "wall", 60, 8),
+    "near-isotropic": ([96, 2, 24], [4.0, 0.1, 1.0], "wall", 122, 13),
+    "threshold25": ([64, 2, 64], [1.0, 0.1, 0.2], "wall", 108, 24),
+    "thin100": ([64, 2, 64], [1.0, 0.1, 0.1], "wall", 92, 5),
+    "thin400": ([64, 2, 64], [1.0, 0.1, 0.05], "wall", 86, 5),
+    "cube100": ([48, 48, 48], [1.0, 1.0, 0.1], "wall", 147, 5),
+    "slab100": ([32, 32, 16], [1.0, 1.0, 0.05], "wall", 118, 6),
+    "plate64": ([64, 8, 64], [1.0, 1.0, 1.0], "wall", 126, 11),
+    "plate256": ([64, 16, 64], [1.0, 4.0, 1.0], "wall", 199, 12),
+    "thin1600": ([64, 8, 64], [1.0, 1.0, 0.2], "wall", 152, 19),
+    "thin6400": ([64, 8, 64], [1.0, 1.0, 0.1], "wall", 162, 18),
+    "review-stretched": ([64, 8, 64], [1.0, 1.0, 0.02], "wall", 161, 17),
+    "odd": ([33, 5, 17], [1.0, 1.0, 0.1], "wall", 87, 14),
+    "periodic": ([31, 5, 17], [0.05, 1.0, 1.0], "periodic", 145, 7),
+    "outlet": ([33, 5, 17], [1.0, 1.0, 0.1], "open", 92, 13),
+    "stiff-two-cell": ([32, 2, 32], [1.0, 0.001, 1.0], "wall", 95, 9),
+    "long-domain": ([128, 2, 16], [100.0, 1.0, 1.0], "wall", 220, 23),
+    "short-stiff-axis": ([64, 64, 8], [1.0, 1.0, 0.01], "wall", 204, 6),
+}
+
+
+def anisotropic_case(name, pre):
+    n, size, bx, _, _ = ANISOTROPIC[name]
+    c = copy.deepcopy(LID_CAVITY)
+    c["grid"]["cells"] = list(n)
+    c["domain"]["size_m"] = list(size)
+    c["boundaries"]["x"] = bx
+    if bx == "open":
+        c["flow"]["initial_velocity_m_s"] = [1.0, 0.0, 0.0]
+    c["numerics"]["pressure_preconditioner"] = pre
+    return c
+
+
+def rough_rhs(g):
+    """pressure_probe.rs:60-68: the rough exact pressure, centred, and its operator image."""
+    import math
+
+    import numpy as np
+
+    exact = np.array([math.sin(0.73 * v) + 0.3 * math.cos(0.17 * v) for v in range(g.count)])
+    exact = g.center_nullspaces(exact)
+    return exact, g.apply(exact)

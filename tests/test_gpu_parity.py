@@ -11,7 +11,8 @@ import math
 import numpy as np
 import pytest
 
-from cases import CANYON_93K, KERNEL_ITERATIONS, LID_CAVITY, kernel_case, periodic_case, sin_field
+from cases import (ANISOTROPIC, CANYON_93K, KERNEL_ITERATIONS, LID_CAVITY, anisotropic_case, kernel_case,
+                   periodic_case, rough_rhs, sin_field)
 
 pytestmark = pytest.mark.gpu
 REL = 1e-10
@@ -89,12 +90,7 @@ def test_multigrid_cycle_matches(pkg, O):
     for name, case in small_cases(pkg).items():
         g, og, dg = open_pair(pkg, O, case, "multigrid")
         r = og.center_nullspaces(np.where(g.fluid == 1, sin_field(g.count, 0.7), 0.0))
-        try:
-            oz, _ = og.mg_apply(r)
-        except O.OracleError as e:
-            assert e.code == O.UNSUPPORTED  # anisotropic line smoothing is not restated
-            dg.close()
-            continue
+        oz, _ = og.mg_apply(r)
         z = dg.precondition(r)
         if all(g.anchored):
             assert np.array_equal(bits(z), bits(oz)), name  # no gauge sums: bitwise
@@ -234,3 +230,39 @@ def test_changed_faces_rebuild_multigrid_and_keep_ic0(pkg, O):
             if pre == "multigrid":
                 assert info.work["hierarchy_builds"] == (1 if changed else 1)
         dg.close()
+
+
+# The 18 anisotropic shapes of docs/evidence/anisotropic-pressure.md (line/plane block
+# smoothing and semicoarsening, multigrid/line.rs) through the plain form's multigrid.
+
+
+@pytest.mark.parametrize("name", list(ANISOTROPIC))
+def test_anisotropic_pins_on_gpu(pkg, O, name):
+    c = anisotropic_case(name, "multigrid")
+    g, og, dg = open_pair(pkg, O, c, "multigrid")
+    exact, rhs = rough_rhs(og)
+    x, info = dg.solve_scaled(rhs, None, 1e-14, 1200)
+    code, ox, oinfo = og.solve(rhs, 1e-14, 1200)
+    dg.close()
+    assert code == 0
+    assert abs(info.iterations - ANISOTROPIC[name][4]) <= 1, (name, info.iterations)
+    assert info.relative_residual <= 1.1e-12
+    assert math.sqrt(float(np.mean((x - exact) ** 2))) <= 1e-8
+    assert np.max(np.abs(x - ox)) <= REL * max(1.0, np.max(np.abs(ox)))
+
+
+@pytest.mark.parametrize("name", ["outlet", "thin100", "plate64", "periodic", "stiff-two-cell", "long-domain"])
+def test_block_smoothed_cycle_matches(pkg, O, name):
+    """One V(1,1) cycle with line/plane block Gauss-Seidel against the oracle's: bitwise on
+    an anchored grid (no gauge sums), else within 1e-12."""
+    c = anisotropic_case(name, "multigrid")
+    g, og, dg = open_pair(pkg, O, c, "multigrid")
+    r = og.center_nullspaces(sin_field(g.count, 0.7))
+    oz, _ = og.mg_apply(r)
+    z = dg.precondition(r)
+    assert dg.multigrid_stats()["level_cells"] == og.mg_levels()[0]
+    dg.close()
+    if all(g.anchored):
+        assert np.array_equal(bits(z), bits(oz))
+    else:
+        assert np.max(np.abs(z - oz)) <= 1e-12 * max(1.0, np.max(np.abs(oz)))
