@@ -608,34 +608,90 @@ struct PLev {
 
 namespace cg = cooperative_groups;
 
-// multigrid/line.rs:155-190, one block: the right-hand side less the outside entries, the
-// banded forward and backward substitutions (the diagonal stored as its reciprocal), then
-// the block's values written to x. One thread, in the reference's order (bit-identical);
-// x and rhs come through L2 (other blocks of the launch write them).
-__device__ __noinline__ void line_block(int b, const PLev& L, const double* rhs, double* x) {
-  const int len = L.llen, bw = L.lbw;
-  const long long stride = bw + 1;
-  const int start = b * len;
-  const long long base = (long long)start * stride;
-  double* __restrict__ scr = L.lscr + start;
-  const double* __restrict__ fac = L.lfac;
+// The banded forward and backward substitutions of one block (multigrid/line.rs:172-185)
+// for a half-bandwidth BW: the last BW results stay in registers and the factor entries of
+// a row are independent of the chain, so only the multiply-subtract chain is serial. The
+// operations and their order are the reference's (bit-identical).
+template <int BW>
+__device__ __forceinline__ void line_subst(double* s, const double* __restrict__ fac, long long base, int len) {
+  constexpr int stride = BW + 1;
+  double w[BW + 1];  // w[d]: the result d rows back (forward) or ahead (backward)
+#pragma unroll
+  for (int d = 0; d <= BW; ++d) w[d] = 0.0;
   for (int i = 0; i < len; ++i) {
+    const double* f = fac + base + (long long)i * stride;
+    double v = s[i];
+#pragma unroll
+    for (int d = BW; d >= 1; --d)  // columns i-BW .. i-1, ascending
+      if (i - d >= 0) v = v - f[d] * w[d];
+    v = v * f[0];
+    s[i] = v;
+#pragma unroll
+    for (int d = BW; d >= 2; --d) w[d] = w[d - 1];
+    w[1] = v;
+  }
+#pragma unroll
+  for (int d = 0; d <= BW; ++d) w[d] = 0.0;
+  for (int i = len - 1; i >= 0; --i) {
+    double v = s[i];
+#pragma unroll
+    for (int d = 1; d <= BW; ++d)  // columns i+1 .. i+BW, ascending
+      if (i + d < len) v = v - fac[base + (long long)(i + d) * stride + d] * w[d];
+    v = v * fac[base + (long long)i * stride];
+    s[i] = v;
+#pragma unroll
+    for (int d = BW; d >= 2; --d) w[d] = w[d - 1];
+    w[1] = v;
+  }
+}
+
+// Any half-bandwidth, as line.rs:172-185 writes it.
+__device__ __noinline__ void line_subst_any(double* s, const double* __restrict__ fac, long long base, int len, int bw) {
+  const long long stride = bw + 1;
+  for (int i = 0; i < len; ++i) {
+    const long long row = base + i * stride;
+    double v = s[i];
+    for (int j = max(0, i - bw); j < i; ++j) v = v - fac[row + i - j] * s[j];
+    s[i] = v * fac[row];
+  }
+  for (int i = len - 1; i >= 0; --i) {
+    double v = s[i];
+    for (int j = i + 1; j < min(len, i + bw + 1); ++j) v = v - fac[base + j * stride + j - i] * s[j];
+    s[i] = v * fac[base + i * stride];
+  }
+}
+
+constexpr int LSCR = 256;  // block lengths up to this keep their scratch in shared memory
+
+// multigrid/line.rs:155-190, one block, by one warp: the lanes gather the right-hand side
+// less the outside entries for the block's nodes (each node's entries in the reference's
+// order), lane 0 runs the substitutions, the lanes write the block's values to x.
+// Bit-identical to the sequential sweep. x and rhs come through L2 (other blocks of the
+// launch write them); the scratch is the warp's shared row or the block's global slice.
+__device__ __forceinline__ void line_block(int b, const PLev& L, const double* rhs, double* x, int lane,
+                                           double* wsh) {
+  const int len = L.llen, bw = L.lbw;
+  const int start = b * len;
+  const long long base = (long long)start * (bw + 1);
+  double* scr = len <= LSCR ? wsh : L.lscr + start;
+  for (int i = lane; i < len; i += 32) {
     double v = __ldcg(&rhs[L.lnodes[start + i]]);
     for (int e = L.looff[start + i]; e < L.looff[start + i + 1]; ++e) v = v - L.loval[e] * __ldcg(&x[L.locol[e]]);
     scr[i] = v;
   }
-  for (int i = 0; i < len; ++i) {
-    const long long row = base + i * stride;
-    double v = scr[i];
-    for (int j = max(0, i - bw); j < i; ++j) v = v - fac[row + i - j] * scr[j];
-    scr[i] = v * fac[row];
+  __syncwarp();
+  if (lane == 0) {
+    switch (bw) {
+      case 1: line_subst<1>(scr, L.lfac, base, len); break;
+      case 2: line_subst<2>(scr, L.lfac, base, len); break;
+      case 3: line_subst<3>(scr, L.lfac, base, len); break;
+      case 4: line_subst<4>(scr, L.lfac, base, len); break;
+      default: line_subst_any(scr, L.lfac, base, len, bw); break;
+    }
   }
-  for (int i = len - 1; i >= 0; --i) {
-    double v = scr[i];
-    for (int j = i + 1; j < min(len, i + bw + 1); ++j) v = v - fac[base + j * stride + j - i] * scr[j];
-    scr[i] = v * fac[base + i * stride];
-  }
-  for (int i = 0; i < len; ++i) x[L.lnodes[start + i]] = scr[i];
+  __syncwarp();
+  for (int i = lane; i < len; i += 32) x[L.lnodes[start + i]] = scr[i];
+  __syncwarp();  // the row is reused by the warp's next block
 }
 
 __device__ void pc_center(const PLev& L, double* v, double* sh, double* mean, cg::grid_group& grid) {
@@ -647,14 +703,16 @@ __device__ void pc_center(const PLev& L, double* v, double* sh, double* mean, cg
 
 // A block Gauss-Seidel sweep over the block dependency levels (blocks of one level share
 // no entry, so they run in parallel; the reference's block order is kept where it matters).
-__device__ void pc_lines(const PLev& L, bool backward, cg::grid_group& grid) {
+__device__ void pc_lines(const PLev& L, bool backward, cg::grid_group& grid, double* lsh) {
   const int* order = backward ? L.lbo : L.lfo;
   const int* start = backward ? L.lbs : L.lfs;
   const int nlev = backward ? L.lnbwd : L.lnfwd;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  double* wsh = lsh + warp * LSCR;
   if (L.lblocal) {
     if (blockIdx.x == 0)
       for (int dl = 0; dl < nlev; ++dl) {
-        for (int t = start[dl] + threadIdx.x; t < start[dl + 1]; t += blockDim.x) line_block(order[t], L, L.rhs, L.x);
+        for (int t = start[dl] + warp; t < start[dl + 1]; t += wpb) line_block(order[t], L, L.rhs, L.x, lane, wsh);
         __threadfence();
         __syncthreads();
       }
@@ -662,17 +720,17 @@ __device__ void pc_lines(const PLev& L, bool backward, cg::grid_group& grid) {
     grid.sync();
     return;
   }
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  const int gw = blockIdx.x * wpb + warp, nw = gridDim.x * wpb;
   for (int dl = 0; dl < nlev; ++dl) {
-    for (int t = start[dl] + gt; t < start[dl + 1]; t += nth) line_block(order[t], L, L.rhs, L.x);
+    for (int t = start[dl] + gw; t < start[dl + 1]; t += nw) line_block(order[t], L, L.rhs, L.x, lane, wsh);
     __threadfence();
     grid.sync();
   }
 }
 
-__device__ void pc_sweep(const PLev& L, bool backward, cg::grid_group& grid) {
+__device__ void pc_sweep(const PLev& L, bool backward, cg::grid_group& grid, double* lsh) {
   if (L.lines) {
-    pc_lines(L, backward, grid);
+    pc_lines(L, backward, grid, lsh);
     return;
   }
   const int* order = backward ? L.bo : L.fo;
@@ -702,6 +760,7 @@ __global__ void __launch_bounds__(BLOCK) k_plain_coarse(const PLev* lv, int nl, 
   if (S && S->done) return;  // read once; nothing in this kernel changes it
   __shared__ double sh[32];
   __shared__ double mean;
+  __shared__ double lsh[(BLOCK / 32) * LSCR];  // one scratch row per warp (block smoothers)
   cg::grid_group grid = cg::this_grid();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
   int l = 0;
@@ -718,7 +777,7 @@ __global__ void __launch_bounds__(BLOCK) k_plain_coarse(const PLev* lv, int nl, 
       pc_center(L, L.x, sh, &mean, grid);
       break;
     }
-    for (int sw = 0; sw < L.nsweep; ++sw) pc_sweep(L, false, grid);
+    for (int sw = 0; sw < L.nsweep; ++sw) pc_sweep(L, false, grid, lsh);
     pc_center(L, L.x, sh, &mean, grid);
     for (int i = gt; i < L.n; i += nth) residual_row(i, L.off, L.col, L.val, L.diag, L.rhs, L.x, L.res);
     __threadfence();
@@ -735,7 +794,7 @@ __global__ void __launch_bounds__(BLOCK) k_plain_coarse(const PLev* lv, int nl, 
     for (int i = gt; i < L.n; i += nth) prolong_row(i, L.poff, L.pcol, L.pval, N.x, L.x);
     __threadfence();
     grid.sync();
-    for (int sw = 0; sw < L.nsweep; ++sw) pc_sweep(L, true, grid);
+    for (int sw = 0; sw < L.nsweep; ++sw) pc_sweep(L, true, grid, lsh);
     pc_center(L, L.x, sh, &mean, grid);
   }
 }
@@ -1258,7 +1317,7 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
         int lmax = 0;
         for (int q = 0; q < P.lnfwd; ++q) lmax = std::max(lmax, L.lfwd.start[q + 1] - L.lfwd.start[q]);
         for (int q = 0; q < P.lnbwd; ++q) lmax = std::max(lmax, L.lbwd.start[q + 1] - L.lbwd.start[q]);
-        P.lblocal = lmax <= BLOCK ? 1 : 0;
+        P.lblocal = lmax <= BLOCK / 32 ? 1 : 0;  // one warp per block solve
         P.lnodes = L.lnodes, P.looff = L.looff, P.locol = L.locol, P.loval = L.loval, P.lfac = L.lfac;
         P.lscr = L.lscr;
         P.lfo = L.lfwd.order, P.lfs = L.lfwd.d_start, P.lbo = L.lbwd.order, P.lbs = L.lbwd.d_start;
