@@ -2428,6 +2428,18 @@ int cfdg_grid_set_cycle(cfdg_grid* G, int32_t nu_fine, int32_t nu_coarse) {
   return 0;
 }
 
+int cfdg_grid_set_coarse_scale(cfdg_grid* G, double alpha) {
+  if (int e = check_grid(G)) return e;
+  if (!(alpha > 0.0 && alpha < 2.0)) return fail(CFDG_ERR_INVALID, "the coarse-correction scale must lie in (0, 2)");
+  std::lock_guard<std::mutex> lk(G->mu);
+  if (G->mx_alpha != (float)alpha) {
+    G->mixed.reset();  // the case state holds the scaled prolongation
+    G->solo.reset();
+  }
+  G->mx_alpha = (float)alpha;
+  return 0;
+}
+
 int cfdg_project_device(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol, uint64_t max_iter,
                         cfdg_poll_fn poll, void* poll_ctx, cfdg_info* info) {
   if (int e = check_grid(G)) return e;

@@ -97,6 +97,7 @@ struct FineCase {
   const int *p_off, *p_col;    // level-0 rows (full layout) from level-1
   const float* p_w;
   const int* pinj;             // injection prolongation (aggregation): level-1 parent per slot, -1 none
+  float pscale;                // the coarse-correction scale of the injection path
   float *rhs1, *x1;
   // projection I/O for this solve
   double* u;
@@ -872,7 +873,7 @@ __device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, cons
   if (F.pinj) {  // x0 += x1[parent]: the same value as the weight-1 row below
     for (int c = sb + threadIdx.x; c < se; c += TILE) {
       const int q = F.pinj[c];
-      if (q >= 0) F.x0[c] += F.x1[q];
+      if (q >= 0) F.x0[c] += F.pscale * F.x1[q];
     }
     return;
   }
@@ -1696,6 +1697,11 @@ Csr permute_csr(const Csr& a, const std::vector<int32_t>& prow, const std::vecto
 // side, 1/diag and x of consecutive rows without an index list.
 int build_case(cfdg_grid* G, CaseState& cs) {
   const Hierarchy& H = *G->host_mg;
+  // Coarse corrections of an aggregation (masked) hierarchy are scaled by the grid's
+  // over-correction factor (cfdg_grid_set_coarse_scale): the piecewise-constant
+  // prolongation under-corrects smooth errors, and the scaled correction stays symmetric
+  // (restriction unchanged) and positive definite for factors below 2.
+  const float alpha = H.masked ? G->mx_alpha : 1.0f;
   HostGrid& h = G->h;
   cudaStream_t s = G->stream;
   Arena& A = cs.arena;
@@ -1872,6 +1878,8 @@ int build_case(cfdg_grid* G, CaseState& cs) {
       const int n = poff[sl + 1] - poff[sl];
       inj = n == 0 || (n == 1 && pw32[poff[sl]] == 1.0f);
     }
+    F.pscale = alpha;
+    for (auto& w : pw32) w *= alpha;
     if (inj) {
       std::vector<int32_t> par(F.N2, -1);
       for (int sl = 0; sl < F.N2; ++sl)
@@ -2020,7 +2028,9 @@ int build_case(cfdg_grid* G, CaseState& cs) {
       if (int e = A.upload(&rw, to_f32(M.restrict.val), s)) return e;
       if (int e = A.upload(&po, M.prolong.off, s)) return e;
       if (int e = A.upload(&pc, M.prolong.col, s)) return e;
-      if (int e = A.upload(&pw, to_f32(M.prolong.val), s)) return e;
+      std::vector<float> pw32 = to_f32(M.prolong.val);
+      for (auto& w : pw32) w *= alpha;
+      if (int e = A.upload(&pw, pw32, s)) return e;
       L.roff = ro, L.rchild = rc, L.rw = rw, L.poff = po, L.pcol = pc, L.pw = pw;
     }
   }

@@ -238,6 +238,11 @@ class DeviceGrid:
         """Mixed form: V-cycle sweeps on level 0 and on the coarse levels (cfdg_grid_set_cycle)."""
         self._check(self.L.cfdg_grid_set_cycle(self.h, int(nu_fine), int(nu_coarse)))
 
+    def set_coarse_scale(self, alpha: float):
+        """Mixed form: scale of the coarse corrections on aggregation hierarchies
+        (cfdg_grid_set_coarse_scale; default 1.7, 1 is the reference's cycle)."""
+        self._check(self.L.cfdg_grid_set_coarse_scale(self.h, float(alpha)))
+
     def device_bytes(self) -> int:
         return int(self.L.cfdg_grid_device_bytes(self.h))
 
@@ -513,26 +518,33 @@ class Server:
 
 
 # Candidate (level-0 sweeps, coarse-level sweeps) pairs of the mixed form's V-cycle.
-CYCLE_CANDIDATES = ((1, 1), (1, 2), (1, 3), (1, 4), (2, 2), (2, 3))
+# (sweeps on level 0, sweeps on the coarse levels, coarse-correction scale)
+CYCLE_CANDIDATES = ((1, 1, 1.7), (1, 2, 1.5), (1, 2, 1.7), (1, 2, 1.85), (1, 3, 1.7), (2, 2, 1.7))
 
 
 def autotune(device_grids, u_ptrs, p_ptrs, reset, dts, tol=1e-8, max_iter=10000, candidates=CYCLE_CANDIDATES,
              stream_handle=None):
-    """Picks the mixed form's V-cycle sweep counts with the shortest time to `tol` on these
-    grids and applies them (cfdg_grid_set_cycle).
+    """Picks the mixed form's V-cycle sweep counts and coarse-correction scale with the
+    shortest time to `tol` on these grids and applies them (cfdg_grid_set_cycle,
+    cfdg_grid_set_coarse_scale; a candidate without a scale keeps the grids' own).
 
     For each candidate a batch of all the grids projects the device velocities u_ptrs /
     p_ptrs twice (the first call builds the batch's graph and is not timed); `reset()`
     restores the inputs before every call. More sweeps make a cycle dearer and the
     iteration count smaller; the optimum depends on the case mix (stencil anisotropy,
     buildings, the share of wide-stencil coarse levels), which is why it is measured.
-    Returns {"choice": (nu_fine, nu_coarse), "ms": {...}, "iterations": {...}}."""
+    Returns {"choice": [nu_fine, nu_coarse(, scale)], "ms": {...}, "iterations": {...}}."""
     import time
 
     timing, iters = {}, {}
-    for cand in candidates:
+    def apply(cand):
         for d in device_grids:
-            d.set_cycle(*cand)
+            d.set_cycle(cand[0], cand[1])
+            if len(cand) > 2:
+                d.set_coarse_scale(cand[2])
+
+    for cand in candidates:
+        apply(cand)
         b = Batch(device_grids)
         if stream_handle:
             b.set_stream(stream_handle)
@@ -556,8 +568,11 @@ def autotune(device_grids, u_ptrs, p_ptrs, reset, dts, tol=1e-8, max_iter=10000,
     if not timing:
         raise PressureError(E.CFDG_ERR_INVALID, "no candidate cycle converged")
     choice = min(timing, key=timing.get)
-    for d in device_grids:
-        d.set_cycle(*choice)
+    apply(choice)
     reset()
-    return {"choice": list(choice), "ms": {f"{a},{b}": round(1e3 * t, 2) for (a, b), t in timing.items()},
-            "iterations": {f"{a},{b}": round(v, 2) for (a, b), v in iters.items()}}
+
+    def key(c):
+        return ",".join(str(v) for v in c)
+
+    return {"choice": list(choice), "ms": {key(c): round(1e3 * t, 2) for c, t in timing.items()},
+            "iterations": {key(c): round(v, 2) for c, v in iters.items()}}
