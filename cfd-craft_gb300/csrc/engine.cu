@@ -810,6 +810,20 @@ __global__ void k_scatter(int n, const int* __restrict__ idx, const double* __re
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) dst[idx[j]] = src[j];
 }
 
+// 1/y when y is a positive power of two whose reciprocal is a normal number, else 0. A
+// product with it is the quotient by y bit for bit (the same real value, rounded the same
+// way); FP64 division is ~20x dearer than a product on this part.
+__device__ __forceinline__ double exact_recip(double y) {
+  const long long bits = __double_as_longlong(y);
+  const int e = (int)((bits >> 52) & 0x7ff);
+  if ((bits & (long long)0x800fffffffffffffull) != 0 || e < 1 || e > 2045) return 0.0;
+  return __longlong_as_double((long long)(2046 - e) << 52);
+}
+__device__ __forceinline__ double div_exact(double x, double y) {
+  const double r = exact_recip(y);
+  return r != 0.0 ? x * r : x / y;
+}
+
 // projection_rhs (pressure.rs:440-459): b = -div(u)/dt, terms = sum(|u_lo|+|u_hi|)/dx/dt.
 __global__ void k_projection_rhs(GridDev g, const uint8_t* __restrict__ fluid, const double* __restrict__ u, double dt,
                                  double* __restrict__ b, double* __restrict__ terms, int N) {
@@ -829,8 +843,8 @@ __global__ void k_projection_rhs(GridDev g, const uint8_t* __restrict__ fluid, c
       p[a] = (g.per[a] && q[a] == g.n[a] - 1) ? 0 : q[a] + 1;
       long long fu = face_index(g, a, p[0], p[1], p[2]);
       double ul = u[fl], uu = u[fu];
-      div = div + (uu - ul) / g.dx[a];
-      scale = scale + (fabs(ul) + fabs(uu)) / g.dx[a];
+      div = div + div_exact(uu - ul, g.dx[a]);
+      scale = scale + div_exact(fabs(ul) + fabs(uu), g.dx[a]);
     }
     b[c] = -div / dt;
     terms[c] = scale / dt;
@@ -846,8 +860,8 @@ __global__ void k_correct_faces(const uint8_t* __restrict__ kind, const int* __r
   for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < F; f += (long long)gridDim.x * blockDim.x) {
     double d;
     uint8_t k = kind[f];
-    if (k == INTERIOR) d = (phi[hi[f]] - phi[lo[f]]) / dist[f];
-    else if (k == OUTLET) d = lo[f] >= 0 ? -phi[lo[f]] / dist[f] : phi[hi[f]] / dist[f];
+    if (k == INTERIOR) d = div_exact(phi[hi[f]] - phi[lo[f]], dist[f]);
+    else if (k == OUTLET) d = lo[f] >= 0 ? div_exact(-phi[lo[f]], dist[f]) : div_exact(phi[hi[f]], dist[f]);
     else d = 0.0;
     u[f] = u[f] - dt * d;
   }
