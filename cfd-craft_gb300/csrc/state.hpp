@@ -199,7 +199,7 @@ struct cfdg_grid {
   // Mixed form: V-cycle sweeps before and after the coarse correction on level 0 and on
   // the coarse levels (cfdg_grid_set_cycle); a batch takes them from its grids.
   int mx_nu0 = 2, mx_nuc = 2;
-  float mx_alpha = 1.7f;  // mixed form: coarse-correction scale on aggregation hierarchies
+  float mx_alpha = 1.8f;  // mixed form: coarse-correction scale on aggregation hierarchies
   // Laminar time stepping (cfdg_grid_set_flow / cfdg_step_device): the case flow and the
   // stage buffers (cell velocities, the two stage velocities, the stage pressure).
   bool has_flow = false;

@@ -240,7 +240,7 @@ class DeviceGrid:
 
     def set_coarse_scale(self, alpha: float):
         """Mixed form: scale of the coarse corrections on aggregation hierarchies
-        (cfdg_grid_set_coarse_scale; default 1.7, 1 is the reference's cycle)."""
+        (cfdg_grid_set_coarse_scale; default 1.8, 1 is the reference's cycle)."""
         self._check(self.L.cfdg_grid_set_coarse_scale(self.h, float(alpha)))
 
     def device_bytes(self) -> int:
@@ -519,7 +519,7 @@ class Server:
 
 # Candidate (level-0 sweeps, coarse-level sweeps) pairs of the mixed form's V-cycle.
 # (sweeps on level 0, sweeps on the coarse levels, coarse-correction scale)
-CYCLE_CANDIDATES = ((1, 1, 1.7), (1, 2, 1.5), (1, 2, 1.7), (1, 2, 1.85), (1, 3, 1.7), (2, 2, 1.7))
+CYCLE_CANDIDATES = ((1, 2, 1.7), (1, 2, 1.85), (2, 2, 1.7), (2, 2, 1.85), (2, 3, 1.85), (1, 3, 1.85))
 
 
 def autotune(device_grids, u_ptrs, p_ptrs, reset, dts, tol=1e-8, max_iter=10000, candidates=CYCLE_CANDIDATES,

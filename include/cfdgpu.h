@@ -186,9 +186,9 @@ int cfdg_debug_momentum_update(cfdg_grid *grid, const double *u, const double *p
  * The bench's autotuner picks them per case mix. No reference counterpart. */
 int cfdg_grid_set_cycle(cfdg_grid *grid, int32_t nu_fine, int32_t nu_coarse);
 /* Mixed form on aggregation (masked) hierarchies: the coarse corrections of the V-cycle are
- * scaled by alpha, 0 < alpha < 2 (default 1.7; 1 is the reference's cycle). The piecewise-
+ * scaled by alpha, 0 < alpha < 2 (default 1.8; 1 is the reference's cycle). The piecewise-
  * constant prolongation under-corrects smooth errors; on the 52-case wind-direction mix
- * 1.7 took the iterations to 1e-8 from 33 to 13. The stopping test is the FP64 true
+ * with V(2,2) 1.85 took the iterations to 1e-8 from 33 to 8. The stopping test is the FP64 true
  * residual, so the result meets the same tolerance. Batches and servers created afterwards
  * take it; grids with linear interpolation (no solid cells) are not scaled. */
 int cfdg_grid_set_coarse_scale(cfdg_grid *grid, double alpha);
