@@ -1545,6 +1545,8 @@ __device__ __forceinline__ void b_rhs(const FineCase* FC, MState* ST, const int2
       continue;
     }
     const int q[3] = {i, j, k};
+    // The round-off scale only serves the compatibility check of closed components.
+    const bool closed = F.ngroups > 0;
     double div = 0.0, scale = 0.0;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -1553,10 +1555,10 @@ __device__ __forceinline__ void b_rhs(const FineCase* FC, MState* ST, const int2
       p[a] += 1;
       const double uu = F.u[fidx(F, a, p[0], p[1], p[2])];
       div = __dadd_rn(div, div_exact(__dsub_rn(uu, ul), F.dx[a]));
-      scale = __dadd_rn(scale, div_exact(__dadd_rn(fabs(ul), fabs(uu)), F.dx[a]));
+      if (closed) scale = __dadd_rn(scale, div_exact(__dadd_rn(fabs(ul), fabs(uu)), F.dx[a]));
     }
     F.b[c] = __ddiv_rn(-div, F.dt);
-    F.terms[c] = __ddiv_rn(scale, F.dt);
+    F.terms[c] = closed ? __ddiv_rn(scale, F.dt) : 0.0;
   }
 }
 __global__ void __launch_bounds__(TILE) k_rhs(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
