@@ -444,11 +444,14 @@ class Serving:
 
     def e2e_loop(self, steps, seed=77):
         """The closed loop with the fields in host memory: each request's u* and p are copied
-        from pinned host buffers to the device before it is submitted and its projected u
-        and p back to pinned host buffers when it finishes (copies on the server's stream,
-        inside the timed region). The inputs of step s are the fields the device loop left
-        plus the seeded perturbation (prepared before the timed region). Returns
-        (milliseconds, H2D bytes, D2H bytes)."""
+        from pinned host buffers to the device before it runs and its projected u and p back
+        to pinned host buffers when it finishes, all inside the timed region. The copies run
+        on a copy stream beside the server's stream: a case's next inputs are copied into its
+        second device buffer while its current request runs (the server's stream waits for
+        that copy's event before the submission), and a finished request's results are
+        copied out after an event on the server's stream. The inputs of step s are the fields
+        the device loop left plus the seeded perturbation (prepared before the timed region).
+        Returns (milliseconds, H2D bytes, D2H bytes)."""
         import numpy as np
 
         torch = self.torch
@@ -462,26 +465,47 @@ class Serving:
             h_p.append(torch.zeros(g.count, dtype=torch.float64).pin_memory())
         o_u = [torch.empty(g.n_faces, dtype=torch.float64).pin_memory() for g in self.grids]
         o_p = [torch.empty(g.count, dtype=torch.float64).pin_memory() for g in self.grids]
+        # Second device buffers: request s of case c runs in buffer s % 2.
+        bu = [[self.d_u[c], torch.empty_like(self.d_u[c])] for c in range(self.n)]
+        bp = [[self.d_p[c], torch.empty_like(self.d_p[c])] for c in range(self.n)]
+        copy = torch.cuda.Stream(self.d_u[0].device)
+        ready = [[None, None] for _ in range(self.n)]
         srv = self.server
         torch.cuda.synchronize()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         h2d = d2h = 0
-        left = [steps] * self.n
+        nxt = [0] * self.n   # next step to submit per case
         inflight = {}
 
-        def send(c):
+        def load(c, s_):
+            """H2D of step s_'s inputs of case c into buffer s_ % 2, on the copy stream."""
             nonlocal h2d
-            s_ = steps - left[c]
-            self.d_u[c].copy_(h_in[c][s_], non_blocking=True)
-            self.d_p[c].copy_(h_p[c], non_blocking=True)
-            h2d += 8 * (self.d_u[c].numel() + self.d_p[c].numel())
-            inflight[self.submit(c)] = c
-            left[c] -= 1
+            k = s_ % 2
+            with torch.cuda.stream(copy):
+                bu[c][k].copy_(h_in[c][s_], non_blocking=True)
+                bp[c][k].copy_(h_p[c], non_blocking=True)
+                e = torch.cuda.Event()
+                e.record(copy)
+            ready[c][k] = e
+            h2d += 8 * (bu[c][k].numel() + bp[c][k].numel())
+
+        def submit(c):
+            s_ = nxt[c]
+            k = s_ % 2
+            self.stream.wait_event(ready[c][k])
+            t = srv.submit(c, bu[c][k].data_ptr(), bp[c][k].data_ptr(), DT, TOL, MAX_IT)
+            inflight[t] = (c, k)
+            nxt[c] += 1
+            if nxt[c] < steps:
+                load(c, nxt[c])  # prefetch the next inputs into the other buffer
 
         ev0.record(self.stream)
+        copy.wait_event(ev0)
         for c in range(self.n):
-            send(c)
+            load(c, 0)
+        for c in range(self.n):
+            submit(c)
         while inflight:
             if srv.progress() == 0:
                 continue
@@ -490,12 +514,17 @@ class Serving:
                 if r is None:
                     continue
                 assert r[0] == 0, r[0]
-                c = inflight.pop(t)
-                o_u[c].copy_(self.d_u[c], non_blocking=True)
-                o_p[c].copy_(self.d_p[c], non_blocking=True)
-                d2h += 8 * (self.d_u[c].numel() + self.d_p[c].numel())
-                if left[c] > 0:
-                    send(c)
+                c, k = inflight.pop(t)
+                done = torch.cuda.Event()
+                done.record(self.stream)  # after the request's epilogue
+                with torch.cuda.stream(copy):
+                    copy.wait_event(done)
+                    o_u[c].copy_(bu[c][k], non_blocking=True)
+                    o_p[c].copy_(bp[c][k], non_blocking=True)
+                d2h += 8 * (bu[c][k].numel() + bp[c][k].numel())
+                if nxt[c] < steps:
+                    submit(c)
+        self.stream.wait_stream(copy)
         ev1.record(self.stream)
         torch.cuda.synchronize()
         return ev0.elapsed_time(ev1), h2d, d2h
@@ -648,14 +677,15 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     e2e_batch = {"value": round(world * e2e_steps * n / (e2e_ms / 1e3), 4), "unit": UNIT,
                  "call": "cfdg_batch_project (host buffers) over all cases of the mix per step, lockstep"}
     # The headline end-to-end figure: the serving loop with the fields in host memory.
-    srv_steps = max(2, min(K, 3))
+    srv_steps = max(2, min(K, 4))
     srv_ms, h2d_b, d2h_b = sv.e2e_loop(srv_steps)
     if dist:
         srv_ms = max_over_ranks(srv_ms, dist, dev)
     e2e = {"value": round(world * srv_steps * n / (srv_ms / 1e3), 4), "unit": UNIT,
            "h2d_bytes_per_step": h2d_b // srv_steps, "d2h_bytes_per_step": d2h_b // srv_steps,
            "call": "cfdg_server submit/progress/result, u and p copied from and to pinned host buffers around "
-                   "every request (on the server's stream)", "steps": srv_steps}
+                   "every request on a copy stream beside the server's (a case's next inputs prefetched into a "
+                   "second device buffer, results copied out after the request's epilogue)", "steps": srv_steps}
     kernels = {}
     for name, which, reps in (("rb_half_sweep_fp32", 0, 20), ("operator_fp32", 1, 20),
                               ("coarse_levels", 2, 10), ("vcycle_fp32", 3, 5)):
