@@ -813,7 +813,7 @@ __device__ __forceinline__ void b_rb(const FineCase* FC, MState* ST, const int2 
     x[own + s] = v * id;
   }
 }
-__global__ void __launch_bounds__(TILE) k_rb(const FineCase* FC, MState* ST, const int2* tiles, const int* count, int color, int first) {
+__global__ void __launch_bounds__(TILE, 5) k_rb(const FineCase* FC, MState* ST, const int2* tiles, const int* count, int color, int first) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
   for (int ti = t0_; ti < t1_; ++ti) {
