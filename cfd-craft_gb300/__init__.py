@@ -4,8 +4,9 @@ Modules:
   grid      -- Grid.build(case): the staggered grid arrays (crates/cfd-craft/src/grid.rs)
   pressure  -- project / solve_scaled / solve / apply / center_nullspaces (pressure.rs)
   engine    -- ctypes binding of libcfdgpu.so (include/cfdgpu.h)
+  archive   -- run archives of device runs in the reference's format (output.rs write_run)
   receptors -- receptor weights (transport.rs receptor_weights) for DeviceGrid.set_receptors
   synth     -- seeded synthetic cases of the benchmark configurations
   build     -- in-tree build of libcfdgpu.so for sm_103a
 """
-from . import engine, grid, pressure, receptors, synth  # noqa: F401
+from . import archive, engine, grid, pressure, receptors, synth  # noqa: F401

@@ -1,0 +1,133 @@
+"""Run archives of device runs in CFD-craft's archive format, so that the reference's
+independent checker (validation/check_fields.py) audits fields the engine produced.
+
+Follows crates/cfd-craft/src/output.rs:162-242 (write_run): the artifacts case.json,
+summary.json, geometry.json, probes.csv and fields.json, each hashed (SHA-256) into
+manifest.json (schema cfd-craft.manifest/0.1, with the byte count before the manifest),
+then complete.json holding the manifest's hash. fields.json is the solver State
+(solver.rs:211-260: steps, time_s, velocity, pressure, k, epsilon, concentrations,
+budgets, floor_events, pressure_iterations, monitor_history) as compact JSON;
+geometry.json carries the fluid mask's hash (grid.rs:550, mask_sha256) and counts.
+
+Scope: flow-only runs (laminar stepping or projections on the device). Constituent
+archives need the mass budgets of advance_scalar (emitted, inflow, outflow), which the
+device transport does not accumulate, so a state with concentrations is refused. The
+summary holds the fields the checker and a reader need (schema, name, termination,
+assessment, model scope, steps, time, constituents), not the reference's full run
+summary (timings, profile, checks).
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import platform
+
+import numpy as np
+
+MANIFEST_SCHEMA = "cfd-craft.manifest/0.1"  # output.rs:229
+RESULT_SCHEMA = "cfd-craft.result/0.1"      # solver.rs:374
+
+
+def _sha(data: bytes) -> str:
+    return hashlib.sha256(data).hexdigest()
+
+
+def _write(path: str, data: bytes):
+    """Atomic write (output.rs atomic_write): a temporary file renamed into place."""
+    tmp = path + ".tmp"
+    with open(tmp, "wb") as f:
+        f.write(data)
+        f.flush()
+        os.fsync(f.fileno())
+    os.replace(tmp, path)
+
+
+def _floats(a):
+    return [float(v) for v in np.asarray(a, dtype=np.float64).ravel()]
+
+
+def write_run(out: str, case: dict, grid, velocity, pressure, *, steps: int, time_s: float,
+              pressure_iterations: int = 0, k=None, epsilon=None, input_sha256: str = None,
+              engine: str = "cfd-craft_gb300") -> list:
+    """Writes the archive of a flow-only run into the new directory `out`.
+
+    velocity (F) and pressure (N) are host arrays (for example the device fields after
+    cfdg_step_device, copied back). k and epsilon default to zeros (laminar). Returns the
+    names of the files written, manifest.json and complete.json last."""
+    if case.get("constituents"):
+        raise ValueError("archives with constituents need the transport budgets, which the device path does not keep")
+    n, f = int(grid.count), int(grid.n_faces)
+    velocity = np.asarray(velocity, dtype=np.float64)
+    pressure = np.asarray(pressure, dtype=np.float64)
+    if velocity.shape != (f,) or pressure.shape != (n,):
+        raise ValueError("velocity must have one value per face and pressure one per cell")
+    k = np.zeros(n) if k is None else np.asarray(k, dtype=np.float64)
+    epsilon = np.zeros(n) if epsilon is None else np.asarray(epsilon, dtype=np.float64)
+    os.makedirs(out, exist_ok=False)
+    files = {}
+    written = []
+    total = 0
+
+    def put(name, data: bytes):
+        nonlocal total
+        _write(os.path.join(out, name), data)
+        files[name] = _sha(data)
+        written.append(name)
+        total += len(data)
+
+    case_bytes = json.dumps(case, indent=2).encode()
+    put("case.json", case_bytes)
+    summary = {
+        "schema_version": RESULT_SCHEMA,
+        "name": case.get("name", ""),
+        "case_sha256": _sha(json.dumps(case, separators=(",", ":")).encode()),
+        "termination": "completed",
+        "assessment": "transient_interval_completed",
+        "error": None,
+        "model_scope": "incompressible_laminar",
+        "steps": int(steps),
+        "time_s": float(time_s),
+        "pressure_iterations": int(pressure_iterations),
+        "constituents": [],
+        "engine": engine,
+    }
+    put("summary.json", json.dumps(summary, indent=2).encode())
+    fluid = np.asarray(grid.fluid, dtype=np.uint8)
+    geometry = {
+        "mask_sha256": _sha(fluid.tobytes()),
+        "cells": [int(v) for v in grid.n],
+        "fluid_cells": int(fluid.sum()),
+        "solid_cells": int(n - fluid.sum()),
+        "components": int(grid.n_components),
+    }
+    put("geometry.json", json.dumps(geometry, indent=2).encode())
+    put("probes.csv", b"constituent,receptor,concentration_kg_m3\n")
+    fields = {
+        "steps": int(steps),
+        "time_s": float(time_s),
+        "velocity": _floats(velocity),
+        "pressure": _floats(pressure),
+        "k": _floats(k),
+        "epsilon": _floats(epsilon),
+        "concentrations": [],
+        "budgets": [],
+        "floor_events": 0,
+        "pressure_iterations": int(pressure_iterations),
+        "monitor_history": [],
+    }
+    put("fields.json", json.dumps(fields, separators=(",", ":")).encode())
+    manifest = {
+        "schema_version": MANIFEST_SCHEMA,
+        "files": files,
+        "omitted": {},
+        "input_case_sha256": input_sha256 or _sha(case_bytes),
+        "bytes_before_manifest": total,
+        "engine": engine,
+        "architecture": platform.machine(),
+        "os": platform.system().lower(),
+    }
+    manifest_bytes = json.dumps(manifest, indent=2).encode()
+    _write(os.path.join(out, "manifest.json"), manifest_bytes)
+    _write(os.path.join(out, "complete.json"), json.dumps({"manifest_sha256": _sha(manifest_bytes)}).encode())
+    return written + ["manifest.json", "complete.json"]

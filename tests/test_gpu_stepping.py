@@ -73,3 +73,33 @@ def test_ssprk2_steps_against_oracle(pkg, O, name, precision, bound):
     # The stepped flow stays divergence-free.
     assert np.max(np.abs(og.divergence(d_u.cpu().numpy()))) <= 1e-6 * 5.0 / min(g.dx)
     dg.close()
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_archive_of_device_steps(pkg, O, precision, tmp_path):
+    """Laminar steps on the device archived in CFD-craft's run-archive format (the package's
+    archive writer, output.rs:162-242): the restated checks of validation/check_fields.py
+    pass on the device fields (hashes, mask, finiteness, independent local continuity)."""
+    torch = pytest.importorskip("torch")
+    from importlib import import_module
+
+    from archive_check import check_archive
+
+    A = import_module(pkg.__name__ + ".archive")
+    case = cases(pkg)["building-open-wall"]
+    g = pkg.grid.Grid.build(case)
+    dg = pkg.pressure.DeviceGrid(g, preconditioner=case["numerics"]["pressure_preconditioner"], precision=precision)
+    dg.set_flow(case)
+    u, p = g.initial_velocity(), np.zeros(g.count)
+    its = dg.project(u, p, 0.1, 1e-8, 10000).iterations
+    dev = torch.device("cuda", 0)
+    d_u, d_p = torch.from_numpy(u).to(dev), torch.from_numpy(p).to(dev)
+    for _ in range(3):
+        its += dg.step_device(d_u.data_ptr(), d_p.data_ptr(), 0.1, 1e-8, 10000).iterations
+    torch.cuda.synchronize()
+    dg.close()
+    out = tmp_path / f"run-{precision}"
+    A.write_run(str(out), case, g, d_u.cpu().numpy(), d_p.cpu().numpy(), steps=3, time_s=0.3,
+                pressure_iterations=int(its))
+    max_div = check_archive(out, lambda c: pkg.grid.Grid.build(c).fluid.astype(bool))
+    print(f"{precision}: archived after 3 device steps, independent max |div u| {max_div:.2e} 1/s")

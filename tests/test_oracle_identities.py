@@ -266,3 +266,31 @@ def test_receptor_point_weights_match_oracle(pkg):
     # Overlaps 1.5 x 1.5 x 1.0 with cell (0,0,0) and 1.0 x 1.5 x 1.0 with cell (1,0,0).
     assert [c for c, _ in vol] == [0, 1]
     assert [v for _, v in vol] == [2.25 / 3.75, 1.5 / 3.75]
+
+
+def test_archive_of_oracle_steps_passes_restated_checker(pkg, O, tmp_path):
+    """The package's archive writer (output.rs:162-242 format) on laminar steps computed by
+    the oracle: the restated checks of validation/check_fields.py pass."""
+    from importlib import import_module
+
+    from archive_check import check_archive
+
+    A = import_module(pkg.__name__ + ".archive")
+    case = pkg.synth.case((16, 12, 8), 2.0, inflow=3.0, boxes=[((10.0, 6.0, 0.0), (16.0, 14.0, 8.0))],
+                          name="archive-probe")
+    g = pkg.grid.Grid.build(case)
+    og = O.Grid(case)
+    code, u, p, info = og.project(g.initial_velocity(), np.zeros(g.count), 0.1, 1e-10, 10000)
+    assert code == 0
+    its = info["iterations"]
+    for _ in range(3):
+        code, u, p, it = og.step(u, p, 0.1, 1e-10, 10000)
+        assert code == 0
+        its += it
+    out = tmp_path / "run"
+    names = A.write_run(str(out), case, g, u, p, steps=3, time_s=0.3, pressure_iterations=its)
+    assert names[-2:] == ["manifest.json", "complete.json"]
+    max_div = check_archive(out, lambda c: pkg.grid.Grid.build(c).fluid.astype(bool))
+    assert max_div < 1e-6
+    with pytest.raises(ValueError):
+        A.write_run(str(tmp_path / "bad"), dict(case, constituents=[{"id": "x"}]), g, u, p, steps=0, time_s=0.0)
