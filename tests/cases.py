@@ -140,3 +140,80 @@ def rough_rhs(g):
     exact = np.array([math.sin(0.73 * v) + 0.3 * math.cos(0.17 * v) for v in range(g.count)])
     exact = g.center_nullspaces(exact)
     return exact, g.apply(exact)
+
+
+def urban_case(n, open_x, blocks):
+    """tests/urban_pressure_reference.rs:15-31 `base(n, open)` with its blocks: the lid
+    cavity re-gridded to n cells of 1 m, walls in y and z, x open (inflow 1 m/s) or wall,
+    multigrid preconditioner."""
+    c = copy.deepcopy(LID_CAVITY)
+    c["grid"]["cells"] = list(n)
+    c["domain"]["size_m"] = [float(v) for v in n]
+    c["boundaries"] = {"x": "open" if open_x else "wall", "y": "wall", "z": "wall"}
+    c["flow"]["initial_velocity_m_s"] = [1.0, 0.0, 0.0]
+    c["numerics"]["pressure_preconditioner"] = "multigrid"
+    c["geometry"] = [{"id": name, "min_m": list(lo), "max_m": list(hi)} for name, lo, hi in blocks]
+    return c
+
+
+# urban_pressure_reference.rs:138-147 and :150-169
+URBAN_BARRIER = ((9, 2, 5), True, [("full-barrier", (3.0, 0.0, 0.0), (4.0, 2.0, 5.0))])
+URBAN_SINGLETON = ((7, 3, 5), True, [("left", (2.0, 1.0, 2.0), (3.0, 2.0, 3.0)), ("right", (4.0, 1.0, 2.0), (5.0, 2.0, 3.0)),
+                                     ("front", (3.0, 0.0, 2.0), (4.0, 1.0, 3.0)), ("back", (3.0, 2.0, 2.0), (4.0, 3.0, 3.0)),
+                                     ("floor", (3.0, 1.0, 1.0), (4.0, 2.0, 2.0)), ("roof", (3.0, 1.0, 3.0), (4.0, 2.0, 4.0))])
+
+
+def dense_reference(g):
+    """urban_pressure_reference.rs:52-136: the matrix assembled directly from the face
+    energies, the manufactured field sin(0.19 i) on fluid cells (centred per sealed
+    component), its image b, and an independent pivoted dense solve with one gauge cell
+    per sealed component removed, centred. Returns (exact, b, reference)."""
+    import numpy as np
+
+    n = g.count
+    a = np.zeros((n, n))
+    kind, lo, hi = np.asarray(g.face_kind), np.asarray(g.face_lo), np.asarray(g.face_hi)
+    w = np.asarray(g.face_area) / np.asarray(g.face_distance) / g.volume
+    for f in range(g.n_faces):
+        if kind[f] == 0:
+            i, j = lo[f], hi[f]
+            a[i, i] += w[f]
+            a[j, j] += w[f]
+            a[i, j] -= w[f]
+            a[j, i] -= w[f]
+        elif kind[f] == 4:
+            i = lo[f] if lo[f] >= 0 else hi[f]
+            a[i, i] += w[f]
+    comp = np.asarray(g.component)
+    sealed = [cid for cid in range(g.n_components) if not g.anchored[cid]]
+
+    def center(x):
+        x = x.copy()
+        for cid in sealed:
+            m = comp == cid
+            x[m] -= x[m].mean()
+        return x
+
+    fluid = np.asarray(g.fluid).astype(bool)
+    exact = center(np.where(fluid, np.sin(0.19 * np.arange(n)), 0.0))
+    b = a @ exact
+    gauges = [int(np.nonzero(comp == cid)[0][0]) for cid in sealed]
+    active = [i for i in range(n) if fluid[i] and i not in gauges]
+    sol = np.linalg.solve(a[np.ix_(active, active)], b[active])
+    ref = np.zeros(n)
+    ref[active] = sol
+    return exact, b, center(ref)
+
+
+def lid_case(n, boundary_x):
+    """tests/multigrid.rs:12-27 `case(n, boundary)`: the lid cavity (1 m cube, periodic y,
+    wall z) re-gridded to n cells, x boundary as given, inflow 1 m/s, multigrid."""
+    c = copy.deepcopy(LID_CAVITY)
+    c["grid"]["cells"] = list(n)
+    c["boundaries"]["x"] = boundary_x
+    c["flow"]["initial_velocity_m_s"] = [1.0, 0.0, 0.0]
+    c["numerics"]["pressure_preconditioner"] = "multigrid"
+    return c
+
+
+MANUFACTURED_SHAPES = [(9, 2, 7), (8, 5, 6), (2, 2, 2), (9, 1, 7)]

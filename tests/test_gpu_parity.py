@@ -266,3 +266,56 @@ def test_block_smoothed_cycle_matches(pkg, O, name):
         assert np.array_equal(bits(z), bits(oz))
     else:
         assert np.max(np.abs(z - oz)) <= 1e-12 * max(1.0, np.max(np.abs(oz)))
+
+
+@pytest.mark.parametrize("which", ["barrier", "singleton"])
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_sealed_components_against_pivoted_dense_reference(pkg, O, which, precision):
+    """tests/urban_pressure_reference.rs:115-183 on the device: both forms solve the sealed
+    inlet-only component and the isolated singleton within 2e-10 of an independent pivoted
+    dense solve; the singleton's incompatible RHS is E031 with x untouched."""
+    from cases import URBAN_BARRIER, URBAN_SINGLETON, dense_reference, urban_case
+
+    n, open_x, blocks = URBAN_BARRIER if which == "barrier" else URBAN_SINGLETON
+    c = urban_case(n, open_x, blocks)
+    g = pkg.grid.Grid.build(c)
+    exact, b, ref = dense_reference(g)
+    dg = pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision=precision)
+    try:
+        x, info = dg.solve_scaled(b, None, 1e-13, 2000)
+    except pkg.pressure.PressureError as e:
+        assert precision == "mixed" and e.code == pkg.engine.CFDG_ERR_UNSUPPORTED
+        dg.close()
+        pytest.skip("the mixed form needs a hierarchy of two or more levels")
+    assert info.relative_residual < 2e-12
+    assert np.max(np.abs(x - ref)) < 2e-10 and np.max(np.abs(x - exact)) < 2e-10
+    if which == "singleton":
+        single = (2 * g.n[1] + 1) * g.n[0] + 3
+        bad = np.zeros(g.count)
+        bad[single] = 1e-30
+        with pytest.raises(pkg.pressure.PressureError) as e:
+            dg.solve_scaled(bad, None, 1e-13, 2000)
+        assert e.value.code == pkg.engine.CFDG_E031
+    dg.close()
+
+
+@pytest.mark.parametrize("boundary", ["wall", "periodic", "open"])
+def test_manufactured_pressure_and_projection_on_gpu(pkg, O, boundary):
+    """tests/multigrid.rs:104-129 through the device (plain form): the manufactured solve
+    and the projection of a pure gradient."""
+    from cases import MANUFACTURED_SHAPES, lid_case
+
+    for n in MANUFACTURED_SHAPES:
+        c = lid_case(n, boundary)
+        g, og, dg = open_pair(pkg, O, c, "multigrid")
+        exact = og.center_nullspaces(np.array([math.sin(0.37 * i) for i in range(g.count)]))
+        b = -og.divergence(og.gradient(exact))
+        x, info = dg.solve_scaled(b, None, 1e-12, 2000)
+        assert info.relative_residual <= 1.1e-11, n
+        assert np.max(np.abs(x - exact)) < 1e-9, n
+        dt = 0.125
+        u, p = og.gradient(exact), np.zeros(g.count)
+        dg.project(u, p, dt, 1e-12, 2000)
+        dg.close()
+        assert np.max(np.abs(u)) < 1e-8 and np.max(np.abs(p - exact / dt)) < 1e-8, n
+        assert np.max(np.abs(og.divergence(u))) < 1e-7, n

@@ -294,3 +294,53 @@ def test_archive_of_oracle_steps_passes_restated_checker(pkg, O, tmp_path):
     assert max_div < 1e-6
     with pytest.raises(ValueError):
         A.write_run(str(tmp_path / "bad"), dict(case, constituents=[{"id": "x"}]), g, u, p, steps=0, time_s=0.0)
+
+
+@pytest.mark.parametrize("which", ["barrier", "singleton"])
+def test_sealed_components_match_pivoted_dense_reference(pkg, O, which):
+    """tests/urban_pressure_reference.rs:115-183: a sealed inlet-only component beside an
+    anchored one, and an isolated sealed singleton, solved to 1e-13 against an independent
+    pivoted dense solve (2e-10); an incompatible RHS on the singleton is E031."""
+    from cases import URBAN_BARRIER, URBAN_SINGLETON, dense_reference, urban_case
+
+    n, open_x, blocks = URBAN_BARRIER if which == "barrier" else URBAN_SINGLETON
+    c = urban_case(n, open_x, blocks)
+    g = pkg.grid.Grid.build(c)
+    og = O.Grid(c)
+    if which == "barrier":
+        assert list(g.anchored) == [0, 1]
+    else:
+        single = (2 * g.n[1] + 1) * g.n[0] + 3
+        assert np.count_nonzero(np.asarray(g.component) == g.component[single]) == 1
+        assert not g.anchored[g.component[single]] and any(g.anchored)
+    exact, b, ref = dense_reference(g)
+    code, x, info = og.solve(b, 1e-13, 2000)
+    assert code == 0 and info["relative_residual"] < 2e-12
+    assert np.max(np.abs(x - ref)) < 2e-10 and np.max(np.abs(x - exact)) < 2e-10
+    if which == "singleton":
+        bad = np.zeros(g.count)
+        bad[single] = 1e-30
+        code, _, _ = og.solve(bad, 1e-13, 2000)
+        assert code == O.E031
+
+
+@pytest.mark.parametrize("boundary", ["wall", "periodic", "open"])
+def test_manufactured_pressure_and_projection(O, boundary):
+    """tests/multigrid.rs:104-129: exact = sin(0.37 i) (centred), b = -div grad exact, solved
+    to 1e-12 (|x - exact| < 1e-9); projecting u = grad exact with dt = 0.125 leaves u ~ 0
+    (1e-8), p = exact / dt (1e-8) and div u < 1e-7."""
+    from cases import MANUFACTURED_SHAPES, lid_case
+
+    for n in MANUFACTURED_SHAPES:
+        g = O.Grid(lid_case(n, boundary))
+        g.set_preconditioner("multigrid")
+        exact = g.center_nullspaces(np.array([math.sin(0.37 * i) for i in range(g.count)]))
+        b = -g.divergence(g.gradient(exact))
+        code, x, info = g.solve(b, 1e-12, 2000)
+        assert code == 0 and info["relative_residual"] <= 1.1e-11, n
+        assert np.max(np.abs(x - exact)) < 1e-9, n
+        dt = 0.125
+        code, u, p, _ = g.project(g.gradient(exact), np.zeros(g.count), dt, 1e-12, 2000)
+        assert code == 0
+        assert np.max(np.abs(u)) < 1e-8 and np.max(np.abs(p - exact / dt)) < 1e-8, n
+        assert np.max(np.abs(g.divergence(u))) < 1e-7, n
