@@ -446,10 +446,11 @@ class Serving:
         """The closed loop with the fields in host memory: each request's u* and p are copied
         from pinned host buffers to the device before it runs and its projected u and p back
         to pinned host buffers when it finishes, all inside the timed region. The copies run
-        on a copy stream beside the server's stream: a case's next inputs are copied into its
-        second device buffer while its current request runs (the server's stream waits for
-        that copy's event before the submission), and a finished request's results are
-        copied out after an event on the server's stream. The inputs of step s are the fields
+        on two copy streams beside the server's stream: a case's next inputs are copied into
+        its second device buffer while its current request runs (the server's stream waits
+        for that copy's event before the submission; the copy waits for the results last
+        copied out of that buffer), and a finished request's results are copied out after
+        an event on the server's stream. The inputs of step s are the fields
         the device loop left plus the seeded perturbation (prepared before the timed region).
         Returns (milliseconds, H2D bytes, D2H bytes)."""
         import numpy as np
@@ -468,8 +469,10 @@ class Serving:
         # Second device buffers: request s of case c runs in buffer s % 2.
         bu = [[self.d_u[c], torch.empty_like(self.d_u[c])] for c in range(self.n)]
         bp = [[self.d_p[c], torch.empty_like(self.d_p[c])] for c in range(self.n)]
-        copy = torch.cuda.Stream(self.d_u[0].device)
+        copy = torch.cuda.Stream(self.d_u[0].device)   # host to device
+        back = torch.cuda.Stream(self.d_u[0].device)   # device to host
         ready = [[None, None] for _ in range(self.n)]
+        drained = [[None, None] for _ in range(self.n)]  # results of the buffer copied out
         srv = self.server
         torch.cuda.synchronize()
         ev0 = torch.cuda.Event(enable_timing=True)
@@ -483,6 +486,8 @@ class Serving:
             nonlocal h2d
             k = s_ % 2
             with torch.cuda.stream(copy):
+                if drained[c][k] is not None:
+                    copy.wait_event(drained[c][k])
                 bu[c][k].copy_(h_in[c][s_], non_blocking=True)
                 bp[c][k].copy_(h_p[c], non_blocking=True)
                 e = torch.cuda.Event()
@@ -502,6 +507,7 @@ class Serving:
 
         ev0.record(self.stream)
         copy.wait_event(ev0)
+        back.wait_event(ev0)
         for c in range(self.n):
             load(c, 0)
         for c in range(self.n):
@@ -517,14 +523,18 @@ class Serving:
                 c, k = inflight.pop(t)
                 done = torch.cuda.Event()
                 done.record(self.stream)  # after the request's epilogue
-                with torch.cuda.stream(copy):
-                    copy.wait_event(done)
+                with torch.cuda.stream(back):
+                    back.wait_event(done)
                     o_u[c].copy_(bu[c][k], non_blocking=True)
                     o_p[c].copy_(bp[c][k], non_blocking=True)
+                    e = torch.cuda.Event()
+                    e.record(back)
+                drained[c][k] = e
                 d2h += 8 * (bu[c][k].numel() + bp[c][k].numel())
                 if nxt[c] < steps:
                     submit(c)
         self.stream.wait_stream(copy)
+        self.stream.wait_stream(back)
         ev1.record(self.stream)
         torch.cuda.synchronize()
         return ev0.elapsed_time(ev1), h2d, d2h
@@ -684,8 +694,8 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     e2e = {"value": round(world * srv_steps * n / (srv_ms / 1e3), 4), "unit": UNIT,
            "h2d_bytes_per_step": h2d_b // srv_steps, "d2h_bytes_per_step": d2h_b // srv_steps,
            "call": "cfdg_server submit/progress/result, u and p copied from and to pinned host buffers around "
-                   "every request on a copy stream beside the server's (a case's next inputs prefetched into a "
-                   "second device buffer, results copied out after the request's epilogue)", "steps": srv_steps}
+                   "every request on two copy streams beside the server's (a case's next inputs prefetched into "
+                   "a second device buffer, results copied out after the request's epilogue)", "steps": srv_steps}
     kernels = {}
     for name, which, reps in (("rb_half_sweep_fp32", 0, 20), ("operator_fp32", 1, 20),
                               ("coarse_levels", 2, 10), ("vcycle_fp32", 3, 5)):

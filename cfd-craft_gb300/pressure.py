@@ -519,7 +519,7 @@ class Server:
 
 # Candidate (level-0 sweeps, coarse-level sweeps) pairs of the mixed form's V-cycle.
 # (sweeps on level 0, sweeps on the coarse levels, coarse-correction scale)
-CYCLE_CANDIDATES = ((1, 2, 1.7), (1, 2, 1.85), (2, 2, 1.7), (2, 2, 1.85), (2, 3, 1.85), (1, 3, 1.85))
+CYCLE_CANDIDATES = ((1, 2, 1.85), (2, 1, 1.85), (2, 2, 1.7), (2, 2, 1.85), (2, 3, 1.85), (3, 2, 1.85))
 
 
 def autotune(device_grids, u_ptrs, p_ptrs, reset, dts, tol=1e-8, max_iter=10000, candidates=CYCLE_CANDIDATES,
