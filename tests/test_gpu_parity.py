@@ -319,3 +319,25 @@ def test_manufactured_pressure_and_projection_on_gpu(pkg, O, boundary):
         dg.close()
         assert np.max(np.abs(u)) < 1e-8 and np.max(np.abs(p - exact / dt)) < 1e-8, n
         assert np.max(np.abs(og.divergence(u))) < 1e-7, n
+
+
+def test_continuum_poisson_second_order_on_gpu(pkg):
+    """tests/numerics.rs:172-200 through the device: second-order convergence of the
+    periodic solve of b = 4 pi^2 sin(2 pi x) (log2 error ratios > 1.9)."""
+    import copy
+
+    from cases import PERIODIC
+
+    errors = []
+    for n in (8, 16, 32):
+        c = copy.deepcopy(PERIODIC)
+        c["grid"]["cells"] = [n, 2, 2]
+        c["domain"]["size_m"] = [1.0, 1.0, 1.0]
+        g = pkg.grid.Grid.build(c)
+        dg = pkg.pressure.DeviceGrid(g, preconditioner="ic0")
+        x = (np.arange(g.count) % n + 0.5) / n
+        exact = np.array([math.sin(2.0 * math.pi * v) for v in x])
+        p, _ = dg.solve_scaled(4.0 * math.pi ** 2 * exact, None, 1e-12, 1000)
+        dg.close()
+        errors.append(math.sqrt(float(np.sum((p - exact) ** 2))) / math.sqrt(g.count))
+    assert math.log2(errors[1] / errors[2]) > 1.9 and math.log2(errors[0] / errors[1]) > 1.9, errors

@@ -344,3 +344,26 @@ def test_manufactured_pressure_and_projection(O, boundary):
         assert code == 0
         assert np.max(np.abs(u)) < 1e-8 and np.max(np.abs(p - exact / dt)) < 1e-8, n
         assert np.max(np.abs(g.divergence(u))) < 1e-7, n
+
+
+def test_continuum_poisson_second_order(O):
+    """tests/numerics.rs:172-200: on the periodic fixture re-gridded to [n, 2, 2] cells of a
+    1 m cube, the solve of b = 4 pi^2 sin(2 pi x) converges to sin(2 pi x) at second order
+    (log2 of successive RMS error ratios > 1.9 for n = 8, 16, 32)."""
+    import copy
+
+    from cases import PERIODIC
+
+    errors = []
+    for n in (8, 16, 32):
+        c = copy.deepcopy(PERIODIC)
+        c["grid"]["cells"] = [n, 2, 2]
+        c["domain"]["size_m"] = [1.0, 1.0, 1.0]
+        g = O.Grid(c)
+        x = (np.arange(g.count) % n + 0.5) / n
+        exact = np.array([math.sin(2.0 * math.pi * v) for v in x])
+        b = 4.0 * math.pi ** 2 * exact
+        code, p, _ = g.solve(b, 1e-12, 1000)
+        assert code == 0
+        errors.append(math.sqrt(float(np.sum((p - exact) ** 2))) / math.sqrt(g.count))
+    assert math.log2(errors[1] / errors[2]) > 1.9 and math.log2(errors[0] / errors[1]) > 1.9, errors
