@@ -53,3 +53,36 @@ def test_engine_matches_golden(pkg):
                 for got, want in ((u, ref[f"{pre}_u"]), (p, ref[f"{pre}_p"])):
                     assert np.max(np.abs(got - want)) <= 1e-10 * max(1.0, np.max(np.abs(want))), (name, pre)
             dg.close()
+
+
+def test_receptor_weights_against_reference_checker_vectors(pkg):
+    """cfd-craft_gb300/receptors.py (point, volume-average and path receptors,
+    transport.rs:202-436) against weights computed by the reference's independent archive
+    checker (validation/check_fields.py), stored by tests/golden/make_path_receptors.py.
+    The checker sums with math.fsum and math.dist, so the bar is 1e-13 relative, same cells."""
+    import json
+    import os
+    from importlib import import_module
+
+    R = import_module(pkg.__name__ + ".receptors")
+    with open(os.path.join(os.path.dirname(__file__), "golden", "path_receptors.json")) as f:
+        gold = json.load(f)
+    spec = gold["case"]
+    case = pkg.synth.case(tuple(spec["cells"]), spec["dx"], boxes=[tuple(map(tuple, b)) for b in spec["boxes"]])
+    g = pkg.grid.Grid.build(case)
+    for item in gold["receptors"]:
+        ours = R.receptor_weights(g, item["receptor"])
+        ref = item["weights"]
+        assert [c for c, _ in ours] == [c for c, _ in ref], item["receptor"]["id"]
+        for (_, a), (_, b) in zip(ours, ref):
+            assert abs(a - b) <= 1e-13 * max(abs(b), 1e-300), (item["receptor"]["id"], a, b)
+    # A path through the building is refused (CFD-E087), one leaving the domain too (E086).
+    for bad, code in (({"kind": "path", "id": "x", "polyline_m": [[2.0, 15.0], [46.0, 15.0]], "height_m": 3.0,
+                        "sample_spacing_m": 1.0}, "CFD-E087"),
+                      ({"kind": "path", "id": "y", "polyline_m": [[2.0, 5.0], [60.0, 5.0]], "height_m": 3.0,
+                        "sample_spacing_m": 1.0}, "CFD-E086")):
+        try:
+            R.receptor_weights(g, bad)
+            raise AssertionError("accepted " + bad["id"])
+        except R.ReceptorError as e:
+            assert str(e).startswith(code), str(e)
