@@ -217,3 +217,32 @@ def lid_case(n, boundary_x):
 
 
 MANUFACTURED_SHAPES = [(9, 2, 7), (8, 5, 6), (2, 2, 2), (9, 1, 7)]
+
+
+def topology_case(cells, boundaries, solid):
+    """multigrid/masked.rs:468-510 `topology`: the lid cavity re-gridded to `cells` 1 m
+    cells with the given boundaries and one 1 m block per solid cell."""
+    c = copy.deepcopy(LID_CAVITY)
+    c["grid"]["cells"] = list(cells)
+    c["domain"]["size_m"] = [float(v) for v in cells]
+    c["boundaries"] = dict(zip("xyz", boundaries))
+    c["flow"]["initial_velocity_m_s"] = [1.0, 0.0, 0.0]
+    c["numerics"]["pressure_preconditioner"] = "multigrid"
+    c["geometry"] = []
+    for z in range(cells[2]):
+        for y in range(cells[1]):
+            for x in range(cells[0]):
+                if solid((x, y, z)):
+                    c["geometry"].append({"id": f"s{x}-{y}-{z}", "min_m": [float(x), float(y), float(z)],
+                                          "max_m": [float(x + 1), float(y + 1), float(z + 1)]})
+    return c
+
+
+def porous_mask():
+    """multigrid/masked.rs:551-559: a fixed pseudo-random 45 % solid mask of 8 x 6 x 6 cells
+    from a 64-bit linear congruential generator."""
+    state, mask = 12345, []
+    for _ in range(8 * 6 * 6):
+        state = (state * 6364136223846793005 + 1442695040888963407) % (1 << 64)
+        mask.append((state >> 33) % 100 < 45)
+    return mask

@@ -367,3 +367,63 @@ def test_continuum_poisson_second_order(O):
         assert code == 0
         errors.append(math.sqrt(float(np.sum((p - exact) ** 2))) / math.sqrt(g.count))
     assert math.log2(errors[1] / errors[2]) > 1.9 and math.log2(errors[0] / errors[1]) > 1.9, errors
+
+
+def gauged_cycle_matrix(g, comp, anchored):
+    """multigrid/masked.rs:411-442: the masked V-cycle on the gauged basis (e_i - e_r0 in a
+    sealed component with first cell r0, e_i in an anchored one) as a dense matrix; each
+    image is finite, zero on solid cells and mean-free on sealed components."""
+    regions = [np.nonzero(comp == c)[0] for c in range(len(anchored))]
+    basis = []
+    for region, anch in zip(regions, anchored):
+        for i in region[0 if anch else 1:]:
+            v = np.zeros(g.count)
+            v[i] = 1.0
+            if not anch:
+                v[region[0]] = -1.0
+            basis.append(v)
+    basis = np.array(basis)
+    m = np.zeros((len(basis), len(basis)))
+    for j, b in enumerate(basis):
+        y, _ = g.mg_apply(b)
+        assert np.all(np.isfinite(y)) and np.all(y[g.fluid == 0] == 0.0)
+        for region, anch in zip(regions, anchored):
+            if not anch:
+                assert abs(y[region].mean()) < 1e-12
+        m[:, j] = basis @ y
+    return m
+
+
+def assert_spd(m):
+    """multigrid/masked.rs:443-467: symmetric to 1e-11 of the largest entry, Cholesky
+    pivots above 1e-12 of it."""
+    scale = np.max(np.abs(m))
+    assert np.max(np.abs(m - m.T)) < 1e-11 * scale
+    assert np.all(np.linalg.eigvalsh(0.5 * (m + m.T)) > 1e-12 * scale)
+    np.linalg.cholesky(m)
+
+
+@pytest.mark.parametrize("which", ["periodic-wrap", "porous-periodic"])
+def test_masked_cycle_spd_on_gauged_subspace(pkg, O, which):
+    """multigrid/masked.rs:538-574: the masked cycle is SPD on its gauged subspace for two
+    sealed periodic components joined through the wrap, and for a fixed pseudo-random
+    porous mask with sealed singletons, diagonal-only contacts and one-cell passages."""
+    from cases import porous_mask, topology_case
+
+    if which == "periodic-wrap":
+        c = topology_case((9, 1, 8), ("periodic", "periodic", "wall"), lambda q: q[0] in (2, 6))
+    else:
+        mask = porous_mask()
+        c = topology_case((8, 6, 6), ("periodic", "periodic", "periodic"),
+                          lambda q: mask[q[0] + 8 * (q[1] + 6 * q[2])])
+    g = pkg.grid.Grid.build(c)
+    comp, anchored = np.asarray(g.component), [bool(a) for a in g.anchored]
+    og = O.Grid(c)
+    og.set_preconditioner("multigrid")
+    if which == "periodic-wrap":
+        assert anchored == [False, False]
+        assert any(comp[0] == comp[8] and comp[0] == k for k in range(2))
+    else:
+        sizes = np.bincount(comp[comp >= 0])
+        assert np.any(sizes == 1) and np.any(sizes > 32) and not any(anchored)
+    assert_spd(gauged_cycle_matrix(og, comp, anchored))
