@@ -427,3 +427,42 @@ def test_masked_cycle_spd_on_gauged_subspace(pkg, O, which):
         sizes = np.bincount(comp[comp >= 0])
         assert np.any(sizes == 1) and np.any(sizes > 32) and not any(anchored)
     assert_spd(gauged_cycle_matrix(og, comp, anchored))
+
+
+def test_source_fields_integrate_to_the_declared_rates(pkg):
+    """cfd-craft_gb300/sources.py (transport.rs:90-178): point, line and volume sources give
+    density fields whose integral is the declared rate (case.rs:684-705); a source touching
+    a building is CFD-E040; a steady source in a sealed component is CFD-E043."""
+    from importlib import import_module
+
+    S = import_module(pkg.__name__ + ".sources")
+    case = pkg.synth.case((20, 12, 8), 2.0, inflow=3.0, boxes=[((24.0, 8.0, 0.0), (32.0, 16.0, 10.0))])
+    case["constituents"] = [{"id": "gas"}, {"id": "tracer"}]
+    case["sources"] = [
+        {"id": "pt", "kind": "point", "constituent": "gas", "point_m": [5.3, 7.7, 3.1], "rate_kg_s": 2e-3},
+        {"id": "ln", "kind": "line", "constituent": "gas", "from_m": [2.0, 2.0, 1.0], "to_m": [20.0, 5.5, 6.2],
+         "rate_kg_s_m": 1e-4},
+        {"id": "vol", "kind": "volume", "constituent": "tracer", "min_m": [3.0, 18.5, 0.0],
+         "max_m": [9.5, 22.0, 4.0], "rate_kg_s_m3": 5e-6},
+    ]
+    g = pkg.grid.Grid.build(case)
+    fields = S.source_fields(case, g)
+    assert len(fields) == 2
+    rates = [S.rate(case["sources"][0]) + S.rate(case["sources"][1]), S.rate(case["sources"][2])]
+    for f, r in zip(fields, rates):
+        assert abs(f.sum() * g.volume - r) <= 1e-13 * r
+        assert np.all(f[g.fluid == 0] == 0.0)
+    assert abs(S.rate(case["sources"][1]) - 1e-4 * math.sqrt(18.0 ** 2 + 3.5 ** 2 + 5.2 ** 2)) < 1e-18
+    # The point source sits in one cell; the line source spreads over the cells it crosses.
+    assert np.count_nonzero(fields[1]) == 4 * 2 * 2
+    bad = dict(case, sources=[{"id": "in-building", "kind": "point", "constituent": "gas",
+                               "point_m": [27.0, 11.0, 3.0], "rate_kg_s": 1e-3}])
+    with pytest.raises(S.SourceError, match="CFD-E040"):
+        S.source_fields(bad, g)
+    sealed = pkg.synth.case((8, 6, 4), 1.0, boundaries=("wall", "wall", "wall"), inflow=0.0)
+    sealed["constituents"] = [{"id": "gas"}]
+    sealed["sources"] = [{"id": "s", "kind": "point", "constituent": "gas", "point_m": [2.0, 2.0, 2.0],
+                          "rate_kg_s": 1e-3}]
+    sealed["run"] = dict(sealed["run"], mode="steady")
+    with pytest.raises(S.SourceError, match="CFD-E043"):
+        S.source_fields(sealed, pkg.grid.Grid.build(sealed))
