@@ -121,3 +121,15 @@ def source_fields(case: dict, g) -> list:
     if any(not np.all(np.isfinite(f)) for f in out):
         raise SourceError("CFD-E044: represented source density is nonfinite")
     return out
+
+
+def diffusivity(case: dict, constituent: int, nut=None, cells: int = None) -> np.ndarray:
+    """solver.rs:585-597: per cell the constituent's molecular diffusivity plus nu_t / Sc
+    (Sc the case's turbulent Schmidt number with neutral_rans, else 1); `nut` the eddy
+    viscosity per cell (zeros for laminar flow, then `cells` gives the count)."""
+    flow = case["flow"]
+    sc = flow["turbulent_schmidt"] if flow.get("kind") == "neutral_rans" else 1.0
+    d0 = case["constituents"][constituent]["diffusivity_m2_s"]
+    nut = np.zeros(int(cells)) if nut is None else np.asarray(nut, dtype=np.float64)
+    return np.array([d0 + n / sc for n in nut.tolist()])
+
