@@ -1752,9 +1752,12 @@ static int flow_euler(Grid& g, const double* u, const double* p, double dt, doub
 
 // transport.rs:651-699 rhs_into with linear upwind (no MUSCL slope) and a zero inlet
 // concentration (solver.rs:823-832 passes |_| 0.0), in face order.
+// Also returns the emission rate (the source densities summed, times the volume) and the
+// open-boundary inflow and outflow rates (transport.rs:717-723).
 static void scalar_rhs(const Grid& g, const double* c, const double* u, const double* d, const double* source,
-                       double* v) {
+                       double* v, double rates[3]) {
   const size_t N = g.count();
+  double inflow = 0.0, outflow = 0.0;
   for (size_t i = 0; i < N; ++i) v[i] = source[i];
   for (size_t fi = 0; fi < g.faces.size(); ++fi) {
     const Face& f = g.faces[fi];
@@ -1774,21 +1777,37 @@ static void scalar_rhs(const Grid& g, const double* c, const double* u, const do
     const double per_volume = flux / g.volume;
     if (f.lo != NONE) v[f.lo] = v[f.lo] - per_volume;
     if (f.hi != NONE) v[f.hi] = v[f.hi] + per_volume;
+    if (f.lo == NONE || f.hi == NONE) {
+      const double outward = f.lo != NONE ? flux : -flux;
+      outflow += std::fmax(outward, 0.0);
+      inflow += std::fmax(-outward, 0.0);
+    }
   }
+  double s = rsum_init();
+  for (size_t i = 0; i < N; ++i) s += source[i];
+  rates[0] = s * g.volume;
+  rates[1] = inflow;
+  rates[2] = outflow;
 }
 
 extern "C" {
 
 // solver.rs:808-855 advance_scalar: one SSPRK2 step of a constituent in place (linear
 // upwind, no particle terms; the budgets are not kept).
-void ora_scalar_step(void* gp, double* c, const double* u, const double* d, const double* source, double dt) {
+// `budget` (nullable): emitted, inflow and outflow masses in kg, incremented as
+// solver.rs:851-853 does.
+void ora_scalar_step(void* gp, double* c, const double* u, const double* d, const double* source, double dt,
+                     double* budget) {
   const Grid& g = *(Grid*)gp;
   const size_t N = g.count();
   std::vector<double> r1(N), stage(N), r2(N);
-  scalar_rhs(g, c, u, d, source, r1.data());
+  double a[3], b[3];
+  scalar_rhs(g, c, u, d, source, r1.data(), a);
   for (size_t i = 0; i < N; ++i) stage[i] = c[i] + dt * r1[i];
-  scalar_rhs(g, stage.data(), u, d, source, r2.data());
+  scalar_rhs(g, stage.data(), u, d, source, r2.data(), b);
   for (size_t i = 0; i < N; ++i) c[i] = 0.5 * (c[i] + stage[i] + dt * r2[i]);
+  if (budget)
+    for (int k = 0; k < 3; ++k) budget[k] += 0.5 * dt * (a[k] + b[k]);
 }
 
 // Laminar flow terms the projection does not need (case flow: viscosity_m2_s, acceleration_m_s2).

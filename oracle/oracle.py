@@ -116,7 +116,7 @@ def lib():
             L.ora_grid_set_flow_terms.argtypes = [P, C.c_double, dp]
             L.ora_momentum_rhs.restype = C.c_int32
             L.ora_momentum_rhs.argtypes = [P, dp, dp]
-            L.ora_scalar_step.argtypes = [P, dp, dp, dp, dp, C.c_double]
+            L.ora_scalar_step.argtypes = [P, dp, dp, dp, dp, C.c_double, C.c_void_p]
             L.ora_step.restype = C.c_int32
             L.ora_step.argtypes = [P, dp, dp, C.c_double, C.c_double, C.c_uint64, C.POINTER(C.c_uint64)]
             _lib = L
@@ -219,12 +219,18 @@ class Grid:
         code = lib().ora_step(self.h, _ptr(uu), _ptr(pp), float(dt), float(tol), int(max_iter), C.byref(it))
         return code, uu, pp, it.value
 
-    def scalar_step(self, c, u, d, source, dt):
-        """advance_scalar (solver.rs:808-855): one SSPRK2 step of a constituent, linear upwind."""
+    def scalar_step(self, c, u, d, source, dt, budget=None):
+        """advance_scalar (solver.rs:808-855): one SSPRK2 step of a constituent, linear upwind.
+        `budget` (a float64 array of 3, optional) accumulates the emitted, inflow and outflow
+        masses in kg as solver.rs:851-853 does."""
         cc = np.array(c, dtype=np.float64, copy=True)
+        bp = None
+        if budget is not None:
+            assert budget.dtype == np.float64 and budget.shape == (3,) and budget.flags.c_contiguous
+            bp = budget.ctypes.data_as(C.c_void_p)
         lib().ora_scalar_step(self.h, _ptr(cc), _ptr(np.ascontiguousarray(u, np.float64)),
                               _ptr(np.ascontiguousarray(d, np.float64)),
-                              _ptr(np.ascontiguousarray(source, np.float64)), float(dt))
+                              _ptr(np.ascontiguousarray(source, np.float64)), float(dt), bp)
         return cc
 
     def set_preconditioner(self, name):

@@ -466,3 +466,35 @@ def test_source_fields_integrate_to_the_declared_rates(pkg):
     sealed["run"] = dict(sealed["run"], mode="steady")
     with pytest.raises(S.SourceError, match="CFD-E043"):
         S.source_fields(sealed, pkg.grid.Grid.build(sealed))
+
+
+def test_scalar_budget_closes_the_mass_balance(pkg, O):
+    """advance_scalar's budget increments (solver.rs:851-853, rates of transport.rs:717-723):
+    over several steps with an inflow, an outlet and a release, mass - initial - emitted -
+    inflow + outflow stays at round-off (the reference checker's independent mass
+    accounting, validation/check_fields.py:633-651, bounds it by 1e-9 of the scale)."""
+    from importlib import import_module
+
+    S = import_module(pkg.__name__ + ".sources")
+    case = pkg.synth.case((16, 10, 6), 2.0, inflow=3.0, boxes=[((12.0, 6.0, 0.0), (18.0, 12.0, 8.0))])
+    case["constituents"] = [{"id": "gas", "diffusivity_m2_s": 0.05}]
+    case["sources"] = [{"id": "pt", "kind": "point", "constituent": "gas", "point_m": [5.0, 9.0, 3.0],
+                        "rate_kg_s": 1e-3}]
+    g = pkg.grid.Grid.build(case)
+    og = O.Grid(case)
+    code, u, _, _ = og.project(g.initial_velocity(), np.zeros(g.count), 0.1, 1e-10, 10000)
+    assert code == 0
+    src = S.source_fields(case, g)[0]
+    d = S.diffusivity(case, 0, cells=g.count)
+    rng = np.random.default_rng(4)
+    c = np.where(g.fluid == 1, rng.uniform(0.0, 1e-4, g.count), 0.0)
+    initial = c.sum() * g.volume
+    budget = np.zeros(3)
+    for _ in range(40):
+        c = og.scalar_step(c, u, d, src, 0.05, budget)
+    emitted, inflow, outflow = budget
+    assert abs(emitted - 40 * 0.05 * 1e-3) < 1e-15
+    assert outflow > 0.0
+    mass = c.sum() * g.volume
+    scale = initial + emitted + inflow + outflow
+    assert abs(mass - initial - emitted - inflow + outflow) < 1e-12 * scale
