@@ -413,6 +413,7 @@ struct Level {
   Matrix matrix;
   Transfer transfer;
   std::vector<BlockSmoother> lines;  // anisotropic levels: replaces the point sweeps
+  size_t dims[3] = {0, 0, 0};        // cells per axis of this level
   std::vector<double> rhs, x, residual, cholesky;
   bool anchored = true;
   bool terminal = false;
@@ -1106,6 +1107,7 @@ static int hierarchy_build(const Grid& g, Control& control, Hierarchy& h) {
     Level level;
     level.matrix = Matrix::build(edges, anchors);
     level.anchored = anchored;
+    for (int a = 0; a < 3; ++a) level.dims[a] = n[a];
     size_t cnt = anchors.size();
     level.rhs.assign(cnt, 0.0);
     level.x.assign(cnt, 0.0);
@@ -1877,6 +1879,43 @@ int32_t ora_mg_apply(void* gp, const double* r, double* z, ora_info* out) {
   if (c) return c;
   hierarchy_apply(*g->hierarchy, r, z, g->count(), info);
   fill_info(info, control.polls, out);
+  return OK;
+}
+// Unmasked hierarchy export of one level: its dims and the dense matrix (n*n, row major;
+// dense may be null to query the dims). Returns n, or -1 when absent.
+int64_t ora_mg_level_dense(void* gp, int32_t level, int64_t* dims, double* dense) {
+  Grid* g = (Grid*)gp;
+  if (!g->hierarchy || g->hierarchy->masked || level < 0 || level >= (int32_t)g->hierarchy->levels.size()) return -1;
+  const Level& L = g->hierarchy->levels[level];
+  const size_t n = L.matrix.diagonal.size();
+  for (int a = 0; a < 3; ++a) dims[a] = (int64_t)L.dims[a];
+  if (dense) {
+    std::fill(dense, dense + n * n, 0.0);
+    for (size_t i = 0; i < n; ++i) {
+      dense[i * n + i] = L.matrix.diagonal[i];
+      for (size_t k = L.matrix.offsets[i]; k < L.matrix.offsets[i + 1]; ++k)
+        dense[i * n + L.matrix.columns[k]] += L.matrix.values[k];
+    }
+  }
+  return (int64_t)n;
+}
+// multigrid/line.rs: a block smoother over the axes in `axes_mask` (bit a = axis a, in
+// axis order) with the periodic flags `periodic_mask`, built on an unmasked level's matrix
+// and swept once over x in place. Returns 0, or E036 / -1.
+int32_t ora_block_sweep(void* gp, int32_t level, int32_t axes_mask, int32_t periodic_mask, int32_t backward,
+                        const double* rhs, double* x) {
+  Grid* g = (Grid*)gp;
+  if (!g->hierarchy || g->hierarchy->masked || level < 0 || level >= (int32_t)g->hierarchy->levels.size()) return -1;
+  const Level& L = g->hierarchy->levels[level];
+  std::vector<int> axes;
+  for (int a = 0; a < 3; ++a)
+    if (axes_mask & (1 << a)) axes.push_back(a);
+  bool periodic[3];
+  for (int a = 0; a < 3; ++a) periodic[a] = (periodic_mask >> a) & 1;
+  Control control;
+  BlockSmoother b;
+  if (int e = b.build(L.matrix, L.dims, axes, periodic, control)) return e;
+  b.sweep(rhs, x, backward != 0);
   return OK;
 }
 // Level sizes of the current hierarchy; returns the level count (0 before the first build).

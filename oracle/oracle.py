@@ -111,6 +111,9 @@ def lib():
             L.ora_mg_apply.argtypes = [P, dp, dp, C.POINTER(Info)]
             L.ora_mg_levels.restype = C.c_int32
             L.ora_mg_levels.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int32]
+            L.ora_mg_level_dense.restype = C.c_int64
+            L.ora_mg_level_dense.argtypes = [P, C.c_int32, C.c_void_p, C.c_void_p]
+            L.ora_block_sweep.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]
             L.ora_mg_masked_level.restype = C.c_int64
             L.ora_mg_masked_level.argtypes = [P, C.c_int32] + [C.c_void_p] * 6
             L.ora_grid_set_flow_terms.argtypes = [P, C.c_double, dp]
@@ -313,6 +316,27 @@ class Grid:
         if code:
             raise OracleError(code)
         return z, info.as_dict()
+
+    def mg_level_dense(self, level):
+        """(dims, dense matrix) of an unmasked hierarchy level (after a build)."""
+        dims = np.zeros(3, np.int64)
+        n = lib().ora_mg_level_dense(self.h, int(level), _vp(dims), None)
+        if n < 0:
+            raise OracleError(-1)
+        a = np.zeros((n, n))
+        lib().ora_mg_level_dense(self.h, int(level), _vp(dims), _vp(a))
+        return tuple(int(v) for v in dims), a
+
+    def block_sweep(self, level, axes, periodic, backward, rhs, x):
+        """One block Gauss-Seidel sweep (multigrid/line.rs) over `axes` on a level's matrix."""
+        rhs = np.ascontiguousarray(rhs, np.float64)
+        xx = np.array(x, dtype=np.float64, copy=True)
+        mask = sum(1 << a for a in axes)
+        pmask = sum(1 << a for a in range(3) if periodic[a])
+        code = lib().ora_block_sweep(self.h, int(level), mask, pmask, int(bool(backward)), _vp(rhs), _vp(xx))
+        if code:
+            raise OracleError(code)
+        return xx
 
     def mg_levels(self):
         cells = np.zeros(64, np.uint64)

@@ -498,3 +498,56 @@ def test_scalar_budget_closes_the_mass_balance(pkg, O):
     mass = c.sum() * g.volume
     scale = initial + emitted + inflow + outflow
     assert abs(mass - initial - emitted - inflow + outflow) < 1e-12 * scale
+
+
+@pytest.mark.parametrize("boundary", ["wall", "periodic", "open"])
+def test_block_smoother_matches_independent_dense_sweeps(O, boundary):
+    """multigrid/line.rs:305-349: on every level of the hierarchy, line and small-plane
+    block sweeps (axes x, y, z and the x-z plane, y periodic, x periodic with a periodic x
+    boundary; forward and backward) equal an independent block Gauss-Seidel with dense
+    pivoted block solves to 1e-9."""
+    import copy
+
+    from cases import LID_CAVITY
+
+    for n in ([7, 3, 5], [2, 3, 5]):
+        c = copy.deepcopy(LID_CAVITY)
+        c["grid"]["cells"] = n
+        c["boundaries"]["x"] = boundary
+        c["flow"]["initial_velocity_m_s"] = [1.0, 0.0, 0.0]
+        g = O.Grid(c)
+        g.set_preconditioner("multigrid")
+        g.mg_apply(np.zeros(g.count))
+        levels = len(g.mg_levels()[0])
+        for level in range(levels):
+            dims, a = g.mg_level_dense(level)
+            count = a.shape[0]
+            for axes in ([0], [1], [2], [0, 2]):
+                periodic = [boundary == "periodic", True, False]
+                rhs = np.array([math.sin(i * 0.31) for i in range(count)])
+                x0 = np.array([math.cos(i * 0.19) for i in range(count)])
+                for backward in (False, True):
+                    got = g.block_sweep(level, axes, periodic, backward, rhs, x0)
+                    # line.rs:272-303 `reference`: blocks in the order of their first cell.
+                    length = int(np.prod([dims[ax] for ax in axes]))
+                    groups = []
+                    for i in range(count):
+                        q = [i % dims[0], i // dims[0] % dims[1], i // (dims[0] * dims[1])]
+                        if any(q[ax] != 0 for ax in axes):
+                            continue
+                        nodes = []
+                        for k in range(length):
+                            at, qq = k, list(q)
+                            for ax in axes:
+                                qq[ax] = at % dims[ax]
+                                at //= dims[ax]
+                            nodes.append((qq[2] * dims[1] + qq[1]) * dims[0] + qq[0])
+                        groups.append(nodes)
+                    if backward:
+                        groups.reverse()
+                    x = x0.copy()
+                    for nodes in groups:
+                        outside = np.setdiff1d(np.arange(count), nodes)
+                        b = rhs[nodes] - a[np.ix_(nodes, outside)] @ x[outside]
+                        x[nodes] = np.linalg.solve(a[np.ix_(nodes, nodes)], b)
+                    assert np.all(np.abs(got - x) < 1e-9 * np.maximum(np.abs(x), 1.0)), (n, level, axes, backward)
