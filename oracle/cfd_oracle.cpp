@@ -1899,6 +1899,23 @@ int64_t ora_mg_level_dense(void* gp, int32_t level, int64_t* dims, double* dense
   }
   return (int64_t)n;
 }
+// The prolongation of an unmasked level to the next one as a dense n x nc matrix (row
+// major; dense may be null to query nc). Returns nc, or -1 when absent.
+int64_t ora_mg_transfer_dense(void* gp, int32_t level, double* dense) {
+  Grid* g = (Grid*)gp;
+  if (!g->hierarchy || g->hierarchy->masked || level < 0 || level + 1 >= (int32_t)g->hierarchy->levels.size())
+    return -1;
+  const Level& L = g->hierarchy->levels[level];
+  const size_t n = L.matrix.diagonal.size();
+  const size_t nc = g->hierarchy->levels[level + 1].matrix.diagonal.size();
+  if (dense) {
+    std::fill(dense, dense + n * nc, 0.0);
+    for (size_t i = 0; i < n; ++i)
+      for (size_t k = L.transfer.offsets[i]; k < L.transfer.offsets[i + 1]; ++k)
+        dense[i * nc + L.transfer.columns[k]] += L.transfer.weights[k];
+  }
+  return (int64_t)nc;
+}
 // multigrid/line.rs: a block smoother over the axes in `axes_mask` (bit a = axis a, in
 // axis order) with the periodic flags `periodic_mask`, built on an unmasked level's matrix
 // and swept once over x in place. Returns 0, or E036 / -1.

@@ -113,6 +113,8 @@ def lib():
             L.ora_mg_levels.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int32]
             L.ora_mg_level_dense.restype = C.c_int64
             L.ora_mg_level_dense.argtypes = [P, C.c_int32, C.c_void_p, C.c_void_p]
+            L.ora_mg_transfer_dense.restype = C.c_int64
+            L.ora_mg_transfer_dense.argtypes = [P, C.c_int32, C.c_void_p]
             L.ora_block_sweep.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]
             L.ora_mg_masked_level.restype = C.c_int64
             L.ora_mg_masked_level.argtypes = [P, C.c_int32] + [C.c_void_p] * 6
@@ -326,6 +328,16 @@ class Grid:
         a = np.zeros((n, n))
         lib().ora_mg_level_dense(self.h, int(level), _vp(dims), _vp(a))
         return tuple(int(v) for v in dims), a
+
+    def mg_transfer_dense(self, level):
+        """The prolongation of an unmasked level to the next one, dense (n x nc)."""
+        nc = lib().ora_mg_transfer_dense(self.h, int(level), None)
+        if nc < 0:
+            raise OracleError(-1)
+        n = self.mg_level_dense(level)[1].shape[0]
+        p = np.zeros((n, nc))
+        lib().ora_mg_transfer_dense(self.h, int(level), _vp(p))
+        return p
 
     def block_sweep(self, level, axes, periodic, backward, rhs, x):
         """One block Gauss-Seidel sweep (multigrid/line.rs) over `axes` on a level's matrix."""
