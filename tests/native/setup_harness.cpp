@@ -12,6 +12,7 @@
 using namespace cfdg;
 
 static std::unique_ptr<Hierarchy> g_h;
+static std::unique_ptr<HostGrid> g_grid;
 static std::string g_err;
 
 extern "C" {
@@ -43,6 +44,7 @@ int32_t hh_build(const int32_t* n, const double* dx, double volume, const int32_
   h.anchored.assign(anchored, anchored + ncomp);
   g_err = check_layout(h);
   if (!g_err.empty()) return -1;
+  g_grid = std::make_unique<HostGrid>(h);
   g_h = std::make_unique<Hierarchy>();
   Poller poll;
   return build_hierarchy(h, poll, *g_h);
@@ -76,6 +78,26 @@ int32_t hh_level_lines(int32_t l, int32_t* out) {
   out[2] = B.count();
   out[3] = B.fwd.levels();
   return 1;
+}
+
+// IC(0) of the grid last passed to hh_build (build_ic0) applied to r, in the order of
+// pressure.rs:223-241 (forward substitution by rows, then the backward scatter).
+int32_t hh_ic0_apply(const double* r, double* z) {
+  if (!g_grid) return -1;
+  Ic0 f;
+  build_ic0(*g_grid, f);
+  const int64_t n = g_grid->cells;
+  for (int64_t i = 0; i < n; ++i) {
+    double v = r[i];
+    for (int32_t k = f.lower.off[i]; k < f.lower.off[i + 1]; ++k) v -= f.lower.val[k] * z[f.lower.col[k]];
+    z[i] = v / f.diag[i];
+  }
+  for (int64_t i = n - 1; i >= 0; --i) {
+    const double v = z[i] / f.diag[i];
+    z[i] = v;
+    for (int32_t k = f.lower.off[i]; k < f.lower.off[i + 1]; ++k) z[f.lower.col[k]] -= f.lower.val[k] * v;
+  }
+  return 0;
 }
 
 }  // extern "C"

@@ -129,3 +129,19 @@ def test_engine_block_smoothers_have_the_reference_shapes(pkg, harness, name):
         assert bw <= (4 if name == "periodic" else 10)
     if name == "plate64":
         assert any(s[0] == 16 for s in shapes[1:])  # a 4 x 4 plane block on a coarse level
+
+
+@pytest.mark.parametrize("name", ["buildings", "barrier", "porous-periodic", "unmasked-open"])
+def test_engine_ic0_factor_equals_oracle(pkg, O, harness, name):
+    """The engine's host IC(0) factor (setup.cpp build_ic0, pressure.rs:118-222) applied in
+    the reference's order equals the oracle's IC(0) application bit for bit."""
+    harness.hh_ic0_apply.argtypes = [C.c_void_p, C.c_void_p]
+    case = grids(pkg)[name]
+    g = pkg.grid.Grid.build(case)
+    og = O.Grid(case)
+    build(harness, g)
+    r = np.where(g.fluid == 1, np.sin(0.37 * np.arange(g.count)), 0.0)
+    z = np.zeros(g.count)
+    assert harness.hh_ic0_apply(vp(r), vp(z)) == 0
+    ref = og.ic0_apply(r)
+    assert np.array_equal(z.view(np.uint64), ref.view(np.uint64)), float(np.max(np.abs(z - ref)))
