@@ -13,6 +13,13 @@
 // The PCG loop runs as CUDA graphs of 8 iterations; every kernel first reads the
 // device Scalars and returns at once when the solve has finished, so the host only
 // synchronises between chunks, where it polls the caller's Control.
+//
+// Also here, on device arrays: laminar SSPRK2 time stepping (momentum right-hand side
+// and stage update, cfdg_step_device), linear-upwind scalar transport (k_scalar_pass,
+// cfdg_scalar_step_device), receptor sampling (cfdg_receptors_sample), and the
+// line/plane block smoothers of anisotropic multigrid hierarchies (line_block, in the
+// cooperative V-cycle k_plain_coarse). All of it follows the reference's operation order
+// (bit-identical results) under -fmad=false.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 

@@ -5,22 +5,26 @@
 // r = b_c - A x with the exact FP64 operator (the reference's face order, with
 // rounded-as-written products: the true residual of pressure.rs:403-415) and stops
 // once |r|/|b_c| <= tol; otherwise it solves A e = r/|r| approximately with an inner
-// FP32 PCG (vectors, operator and the multigrid V-cycle in FP32; dot products and
-// alpha/beta accumulated in FP64) and adds |r| e to x.
+// FP32 PCG (vectors, operator and the multigrid V-cycle in FP32; dot products carried
+// as compensated FP32 pairs, alpha/beta in FP64) and adds |r| e to x.
 //
-// The V(2,2) cycle keeps the reference hierarchy (multigrid.rs / masked.rs: same
-// aggregates, Galerkin coarse operators, transfers and per-component gauges) but
-// smooths with parallel orderings: red-black Gauss-Seidel on the structured fine
-// level and multicolour Gauss-Seidel (greedy colouring) on the coarse levels, colours
-// reversed on the way up so the cycle stays symmetric. The coarsest level is solved
-// in FP64 with the reference's dense Cholesky factors.
+// The V-cycle keeps the reference hierarchy (multigrid.rs / masked.rs: same aggregates,
+// Galerkin coarse operators, transfers and per-component gauges) but smooths with
+// parallel orderings: red-black Gauss-Seidel on the structured fine level (level-0 FP32
+// arrays in a colour-split row layout), two-colour Gauss-Seidel by bin parity on the
+// aggregation levels, l1-Jacobi on levels needing more than 8 colours, colours reversed
+// on the way up so the cycle stays symmetric; the coarse corrections of aggregation
+// hierarchies are scaled by the grid's over-correction factor. Sweep counts and the
+// factor are per grid (cfdg_grid_set_cycle / cfdg_grid_set_coarse_scale). The coarsest
+// level is solved in FP64 with the inverses of the reference's dense Cholesky factors.
 //
-// Batching: the fine-level kernels run over a work-list of 256-cell tiles drawn from
-// all cases of the batch; all coarse levels of one case run in one thread-block
-// cluster (cluster barriers between phases), one cluster per case in one launch. A
-// per-case state machine (outer step -> inner start -> inner iterations -> outer
-// step ... -> done) lets a fixed kernel sequence serve every case, so the whole
-// iteration is captured once as a CUDA graph and replayed in chunks.
+// Batching: the fine-level kernels are persistent and run over a device work-list of
+// row tiles (8 rows, one warp per row) drawn from all active cases; all coarse levels of
+// all cases run in one cooperative kernel (grid-wide phases for large levels, one block
+// per case for small ones). A per-case state machine (outer step -> inner start -> inner
+// iterations -> outer step ... -> done) lets a fixed kernel sequence serve every case,
+// so the whole iteration is captured once as a CUDA graph and replayed in chunks; the
+// server (continuous batching) admits and finishes requests between chunks.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
