@@ -8,8 +8,10 @@
  * the IC(0) factor and the multigrid hierarchy resident in device memory.
  *
  * Conventions
- *  - Every pointer argument is caller-owned HOST memory unless the function
- *    name ends in _device, and is only read during the call (copied in/out).
+ *  - Every pointer argument is caller-owned HOST memory, only read during the call
+ *    (copied in/out), except parameters named d_* (and those of functions whose name
+ *    ends in _device): those are DEVICE memory, used in stream order on the grid's,
+ *    batch's or server's stream.
  *  - Cell index (k*ny + j)*nx + i, x fastest (grid.rs:218-220). Face arrays hold
  *    the x-faces, then the y-faces, then the z-faces, each x fastest over its
  *    face dimensions (grid.rs:341-429).
