@@ -16,8 +16,12 @@
 //   pressure.rs:316-325  center_nullspaces
 //   pressure.rs:342-436  solve_scaled (PCG, true-residual gate, E031/E032/E033)
 //   pressure.rs:440-502  projection_rhs / project
-//   multigrid.rs:24-726  unmasked geometric multigrid (Galerkin, V(2,2), dense Cholesky)
+//   multigrid.rs:24-726  unmasked geometric multigrid (Galerkin, V(2,2), dense Cholesky,
+//                        semicoarsening of anisotropic grids)
+//   multigrid/line.rs:26-201    line/plane block smoothers (banded Cholesky block GS)
 //   multigrid/masked.rs:16-342  masked aggregation multigrid
+//   flow.rs:426-525, solver.rs:671-732,879-960  laminar momentum RHS and SSPRK2 step
+//   transport.rs:651-723, solver.rs:808-855     linear-upwind scalar step and budgets
 // Parity is pinned by the reference's published known answers (iteration counts,
 // residuals) and by its unit-test identities, re-run in tests/.
 //
@@ -1932,8 +1936,8 @@ int32_t ora_block_sweep(void* gp, int32_t level, int32_t axes_mask, int32_t peri
   Control control;
   BlockSmoother b;
   if (int e = b.build(L.matrix, L.dims, axes, periodic, control)) return e;
-  b.sweep(rhs, x, backward != 0);
-  return OK;
+  if (x) b.sweep(rhs, x, backward != 0);
+  return x ? OK : -(int32_t)b.bandwidth - 1000;  // without x: the half-bandwidth, encoded
 }
 // Level sizes of the current hierarchy; returns the level count (0 before the first build).
 int32_t ora_mg_levels(void* gp, uint64_t* cells, uint64_t* nonzeros, int32_t cap) {

@@ -4,7 +4,8 @@ Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference leg
 use this module. It loads ``oracle/_build/libcfd_oracle.so`` (built by
 ``oracle/Makefile``), a plain C++ restatement of the CFD-craft pressure
 projection (crates/cfd-craft/src/grid.rs, pressure.rs, multigrid.rs,
-multigrid/masked.rs). Cases are reference-schema case dictionaries
+multigrid/masked.rs, multigrid/line.rs) and of the steps around it (flow.rs laminar
+momentum, transport.rs scalar transport). Cases are reference-schema case dictionaries
 (``cfd-craft.case/0.1``); only the fields the projection reads are used.
 """
 from __future__ import annotations
@@ -349,6 +350,15 @@ class Grid:
         if code:
             raise OracleError(code)
         return xx
+
+    def block_bandwidth(self, level, axes, periodic):
+        """Half-bandwidth of the block factor a block smoother over `axes` gets on a level."""
+        mask = sum(1 << a for a in axes)
+        pmask = sum(1 << a for a in range(3) if periodic[a])
+        code = lib().ora_block_sweep(self.h, int(level), mask, pmask, 0, None, None)
+        if code > -1000:
+            raise OracleError(code)
+        return -code - 1000
 
     def mg_levels(self):
         cells = np.zeros(64, np.uint64)

@@ -632,3 +632,21 @@ def test_pressure_verification_fixture(pkg, O, which):
     code, xs, info = og.solve(og.apply(exact), 1e-11, 5000)
     assert code == 0
     assert math.sqrt(float(np.sum((xs - exact) ** 2)) / g.count) < 1e-9
+
+
+def test_folded_periodic_lines_keep_a_narrow_band(O):
+    """multigrid/line.rs:352-365: x lines of a periodic 17 x 3 x 3 grid, folded, have a
+    half-bandwidth of at most 2 on the fine level and 4 on the coarse ones."""
+    import copy
+
+    from cases import LID_CAVITY
+
+    c = copy.deepcopy(LID_CAVITY)
+    c["grid"]["cells"] = [17, 3, 3]
+    c["boundaries"]["x"] = "periodic"
+    g = O.Grid(c)
+    g.set_preconditioner("multigrid")
+    g.mg_apply(np.zeros(g.count))
+    for level in range(len(g.mg_levels()[0])):
+        bw = g.block_bandwidth(level, [0], [True, True, False])
+        assert bw <= (2 if level == 0 else 4), (level, bw)
