@@ -650,3 +650,23 @@ def test_folded_periodic_lines_keep_a_narrow_band(O):
     for level in range(len(g.mg_levels()[0])):
         bw = g.block_bandwidth(level, [0], [True, True, False])
         assert bw <= (2 if level == 0 else 4), (level, bw)
+
+
+def test_line_source_through_cell_corners(pkg):
+    """transport.rs:101-121: a line source along a cell diagonal crosses x and y faces at the
+    same parameters; the duplicates merge (within 1e-14) and every cell on the diagonal
+    receives an equal share of the line."""
+    from importlib import import_module
+
+    S = import_module(pkg.__name__ + ".sources")
+    case = pkg.synth.case((8, 8, 4), 1.0, inflow=1.0)
+    case["constituents"] = [{"id": "gas"}]
+    case["sources"] = [{"id": "diag", "kind": "line", "constituent": "gas", "from_m": [0.0, 0.0, 1.5],
+                        "to_m": [8.0, 8.0, 1.5], "rate_kg_s_m": 1e-3}]
+    g = pkg.grid.Grid.build(case)
+    f = S.source_fields(case, g)[0]
+    cells = np.nonzero(f)[0]
+    assert len(cells) == 8  # the eight cells (i, i, 1)
+    assert all(c % 8 == (c // 8) % 8 and c // 64 == 1 for c in cells)
+    assert np.allclose(f[cells], f[cells[0]], rtol=1e-14, atol=0.0)
+    assert abs(f.sum() * g.volume - 1e-3 * math.sqrt(128.0)) < 1e-16
