@@ -14,7 +14,9 @@ archives need the mass budgets of advance_scalar (emitted, inflow, outflow), whi
 device transport does not accumulate, so a state with concentrations is refused. The
 summary holds the fields the checker and a reader need (schema, name, termination,
 assessment, model scope, steps, time, constituents), not the reference's full run
-summary (timings, profile, checks).
+summary (timings, profile, checks). The manifest carries the reference's keys
+(output.rs:218-226); source_sha256 and executable_sha256 identify this engine's sources
+and built library rather than the reference's CLI binary.
 """
 from __future__ import annotations
 
@@ -27,6 +29,7 @@ import numpy as np
 
 MANIFEST_SCHEMA = "cfd-craft.manifest/0.1"  # output.rs:229
 RESULT_SCHEMA = "cfd-craft.result/0.1"      # solver.rs:374
+ENGINE_VERSION = "0.2.0"
 
 
 def _sha(data: bytes) -> str:
@@ -47,14 +50,34 @@ def _floats(a):
     return [float(v) for v in np.asarray(a, dtype=np.float64).ravel()]
 
 
+def _engine_identity():
+    """(source_sha256, executable_sha256) of the engine: the hash of its CUDA/C++ sources in
+    name order and of the built library, the build identity output.rs records."""
+    here = os.path.dirname(os.path.abspath(__file__))
+    src = os.path.join(here, "csrc")
+    h = hashlib.sha256()
+    if os.path.isdir(src):
+        for name in sorted(os.listdir(src)):
+            with open(os.path.join(src, name), "rb") as fh:
+                h.update(name.encode() + b"\0" + fh.read())
+    lib = os.path.join(here, "_build", "libcfdgpu.so")
+    exe = None
+    if os.path.exists(lib):
+        with open(lib, "rb") as fh:
+            exe = _sha(fh.read())
+    return h.hexdigest(), exe
+
+
 def write_run(out: str, case: dict, grid, velocity, pressure, *, steps: int, time_s: float,
               pressure_iterations: int = 0, k=None, epsilon=None, input_sha256: str = None,
-              engine: str = "cfd-craft_gb300") -> list:
+              initial_state_sha256: str = None, engine: str = "cfd-craft_gb300") -> list:
     """Writes the archive of a flow-only run into the new directory `out`.
 
     velocity (F) and pressure (N) are host arrays (for example the device fields after
-    cfdg_step_device, copied back). k and epsilon default to zeros (laminar). Returns the
-    names of the files written, manifest.json and complete.json last."""
+    cfdg_step_device, copied back). k and epsilon default to zeros (laminar). Every value
+    must be finite: the reference serialises the state with serde_json, which cannot write
+    NaN or infinity, and its checker rejects non-finite fields (ValueError here). Returns
+    the names of the files written, manifest.json and complete.json last."""
     if case.get("constituents"):
         raise ValueError("archives with constituents need the transport budgets, which the device path does not keep")
     n, f = int(grid.count), int(grid.n_faces)
@@ -64,6 +87,10 @@ def write_run(out: str, case: dict, grid, velocity, pressure, *, steps: int, tim
         raise ValueError("velocity must have one value per face and pressure one per cell")
     k = np.zeros(n) if k is None else np.asarray(k, dtype=np.float64)
     epsilon = np.zeros(n) if epsilon is None else np.asarray(epsilon, dtype=np.float64)
+    for name, a in (("velocity", velocity), ("pressure", pressure), ("k", k), ("epsilon", epsilon)):
+        if not np.all(np.isfinite(a)):
+            raise ValueError(f"non-finite {name}: a run archive holds finite fields only")
+    source_sha256, executable_sha256 = _engine_identity()
     os.makedirs(out, exist_ok=False)
     files = {}
     written = []
@@ -91,6 +118,9 @@ def write_run(out: str, case: dict, grid, velocity, pressure, *, steps: int, tim
         "pressure_iterations": int(pressure_iterations),
         "constituents": [],
         "engine": engine,
+        "source_sha256": source_sha256,
+        "build_version": f"{engine} {ENGINE_VERSION}",
+        "initial_state_sha256": initial_state_sha256,
     }
     put("summary.json", json.dumps(summary, indent=2).encode())
     fluid = np.asarray(grid.fluid, dtype=np.uint8)
@@ -116,13 +146,18 @@ def write_run(out: str, case: dict, grid, velocity, pressure, *, steps: int, tim
         "pressure_iterations": int(pressure_iterations),
         "monitor_history": [],
     }
-    put("fields.json", json.dumps(fields, separators=(",", ":")).encode())
+    put("fields.json", json.dumps(fields, separators=(",", ":"), allow_nan=False).encode())
     manifest = {
         "schema_version": MANIFEST_SCHEMA,
         "files": files,
         "omitted": {},
         "input_case_sha256": input_sha256 or _sha(case_bytes),
+        "source_sha256": source_sha256,
+        "version": f"{engine} {ENGINE_VERSION}",
+        "initial_state_sha256": initial_state_sha256,
+        "executable_sha256": executable_sha256,
         "bytes_before_manifest": total,
+        "threads": int(case.get("run", {}).get("threads", 1)),
         "engine": engine,
         "architecture": platform.machine(),
         "os": platform.system().lower(),

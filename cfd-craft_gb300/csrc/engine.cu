@@ -291,7 +291,10 @@ __global__ void k_residual_norm_noalloc(GridDev g, const double* __restrict__ x,
   double t1 = block_sum(a1, sh);
   double t2 = block_sum(a2, sh);
   if (threadIdx.x == 0) {
-    out[0] = sqrt(t1) / sqrt(t2);
+    // |b| < 1e-24: the solve returns x = 0 and LinearInfo::default(), a zero residual
+    // (pressure.rs:372-375).
+    const double nb = sqrt(t2);
+    out[0] = nb < 1e-24 ? 0.0 : sqrt(t1) / nb;
     *counter = 0;
   }
 }
@@ -932,6 +935,8 @@ WaveArgs wave_args(cfdg_grid* G, const Scalars* S) {
   A.sync = G->wave_sync;
   A.error = G->wave_err;
   A.S = S;
+  A.spin_limit = G->wave_spin_limit;
+  A.hold_tile = G->wave_hold_tile;
   return A;
 }
 
@@ -1193,13 +1198,42 @@ int build_ic0_dev(cfdg_grid* G) {
   return 0;
 }
 
-std::string stats_json_of(const DevHierarchy& H) {
+// Device bytes of one level's block smoother as uploaded (nodes, outside rows, banded
+// factor, scratch, the two dependency orders).
+uint64_t line_device_bytes(const LineBlocks& B) {
+  return 4 * (B.nodes.size() + B.outside.off.size() + B.outside.col.size() + B.fwd.order.size() +
+              B.fwd.start.size() + B.bwd.order.size() + B.bwd.start.size()) +
+         8 * (B.outside.val.size() + B.factor.size() + B.nodes.size());
+}
+
+// MultigridStats (multigrid.rs:55-72) as JSON, fields in the reference's order; the empty
+// level_dimensions and block_smoothers are omitted as serde skips them. allocated_bytes
+// counts the device arrays the hierarchy holds (the storage this engine retains).
+std::string stats_json_of(const DevHierarchy& D, const Hierarchy& H) {
   std::string s = "{\"level_cells\":[";
-  for (size_t i = 0; i < H.level_cells.size(); ++i) s += (i ? "," : "") + std::to_string(H.level_cells[i]);
-  s += "],\"level_nonzeros\":[";
-  for (size_t i = 0; i < H.level_nonzeros.size(); ++i) s += (i ? "," : "") + std::to_string(H.level_nonzeros[i]);
-  s += "],\"allocated_bytes\":" + std::to_string(H.arena.bytes) + "}";
-  return s;
+  for (size_t i = 0; i < D.level_cells.size(); ++i) s += (i ? "," : "") + std::to_string(D.level_cells[i]);
+  s += "]";
+  if (!H.level_dims.empty()) {
+    s += ",\"level_dimensions\":[";
+    for (size_t i = 0; i < H.level_dims.size(); ++i)
+      s += std::string(i ? "," : "") + "[" + std::to_string(H.level_dims[i][0]) + "," +
+           std::to_string(H.level_dims[i][1]) + "," + std::to_string(H.level_dims[i][2]) + "]";
+    s += "]";
+  }
+  s += ",\"level_nonzeros\":[";
+  for (size_t i = 0; i < D.level_nonzeros.size(); ++i) s += (i ? "," : "") + std::to_string(D.level_nonzeros[i]);
+  s += "],\"allocated_bytes\":" + std::to_string(D.arena.bytes);
+  std::string blocks;
+  for (size_t l = 0; l < H.levels.size(); ++l)
+    for (const LineBlocks& B : H.levels[l].lines) {
+      blocks += std::string(blocks.empty() ? "" : ",") + "{\"level\":" + std::to_string(l) + ",\"axes\":[";
+      for (size_t a = 0; a < B.axes.size(); ++a) blocks += (a ? "," : "") + std::to_string(B.axes[a]);
+      blocks += "],\"block_unknowns\":" + std::to_string(B.length) + ",\"block_count\":" +
+                std::to_string(B.count()) + ",\"half_bandwidth\":" + std::to_string(B.bandwidth) +
+                ",\"allocated_bytes\":" + std::to_string(line_device_bytes(B)) + "}";
+    }
+  if (!blocks.empty()) s += ",\"block_smoothers\":[" + blocks + "]";
+  return s + "}";
 }
 
 int build_mg_dev(cfdg_grid* G, const Poller& poll) {
@@ -1365,7 +1399,7 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
   G->host_mg = std::make_shared<Hierarchy>(std::move(H));
   {
     std::lock_guard<std::mutex> lk(G->stats_mu);
-    G->stats_json = stats_json_of(*D);
+    G->stats_json = stats_json_of(*D, *G->host_mg);
   }
   G->mg = std::move(D);
   return 0;
@@ -1381,6 +1415,7 @@ int prepare_mg_impl(cfdg_grid* G, const Poller& poll, cfdg_info* info) {
       info->hierarchy_levels = G->mg->level_cells.size();
       for (auto v : G->mg->level_cells) info->hierarchy_cells += v;
       for (auto v : G->mg->level_nonzeros) info->hierarchy_nonzeros += v;
+      info->hierarchy_bytes = G->mg->arena.bytes;
     }
     return 0;
   }
@@ -1403,6 +1438,7 @@ int prepare_mg_impl(cfdg_grid* G, const Poller& poll, cfdg_info* info) {
     info->hierarchy_levels = G->mg->level_cells.size();
     for (auto v : G->mg->level_cells) info->hierarchy_cells += v;
     for (auto v : G->mg->level_nonzeros) info->hierarchy_nonzeros += v;
+    info->hierarchy_bytes = G->mg->arena.bytes;
   }
   return 0;
 }
@@ -1511,12 +1547,24 @@ int solve_device(cfdg_grid* G, bool use_terms, double tol, uint64_t max_iter, co
   if (G->preconditioner == CFDG_PRECOND_MULTIGRID && G->mg) {
     uint64_t cyc = inf->preconditioner_applications;
     inf->cycles = cyc;
-    uint64_t inner = 0, smooth = 0;
+    uint64_t inner = 0, smooth = 0, bvisits = 0, bsolves = 0;
     for (size_t l = 0; l + 1 < G->mg->levels.size(); ++l) {
-      inner += G->mg->levels[l].n;
-      smooth += (G->mg->levels[l].lines ? 2 : 4) * (uint64_t)G->mg->levels[l].n;  // 2 x sweeps
+      const DevLevel& L = G->mg->levels[l];
+      // The hierarchy's unknowns (fluid cells on a masked level 0), not the full-grid
+      // layout the device may keep level 0 in (masked.rs:337-341).
+      const uint64_t n = G->mg->level_cells[l];
+      inner += n;
+      smooth += (L.lines ? 2 : 4) * n;  // 2 x sweeps
+      if (L.lines) {
+        // multigrid.rs:677-718: one block sweep each way, every block solved.
+        bvisits += n;
+        bsolves += 2 * (uint64_t)L.lcount;
+      }
     }
     inf->smoothing_cell_updates = smooth * cyc;
+    inf->block_level_cell_visits = bvisits * cyc;
+    inf->block_smoothing_cell_updates = 2 * bvisits * cyc;
+    inf->block_solves = bsolves * cyc;
     inf->residual_cell_updates = inner * cyc;
     inf->restriction_cell_updates = inner * cyc;
     inf->prolongation_cell_updates = inner * cyc;
@@ -1566,11 +1614,12 @@ int project_mixed(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol,
   cfdg_mixed_set_stream(G->solo.get(), G->stream);
   int32_t code = 0;
   uint64_t builds = inf->hierarchy_builds, levels = inf->hierarchy_levels, cells = inf->hierarchy_cells,
-           nnz = inf->hierarchy_nonzeros;
+           nnz = inf->hierarchy_nonzeros, hbytes = inf->hierarchy_bytes;
   if (int e = cfdg_mixed_project(G->solo.get(), &d_u, &d_p, &dt, tol, max_iter, poll.fn, poll.ctx, inf, &code))
     return e;
   inf->hierarchy_builds = builds, inf->hierarchy_levels = levels, inf->hierarchy_cells = cells;
   inf->hierarchy_nonzeros = nnz;
+  inf->hierarchy_bytes = hbytes;
   if (code == CFDG_E031) return fail(code, "CFD-E031: incompatible flux in a closed fluid component");
   if (code == CFDG_E032) return fail(code, "CFD-E032: pressure CG lost positive definiteness");
   if (code == CFDG_E033) return fail(code, "CFD-E033: pressure iteration limit " + std::to_string(max_iter));
@@ -2558,6 +2607,20 @@ int cfdg_debug_precondition(cfdg_grid* G, const double* r, double* z) {
   CU(cudaMemcpyAsync(z, G->z, G->h.cells * 8, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
   return check_wave(G);
+}
+
+int cfdg_debug_wave_stall(cfdg_grid* G, int32_t hold_tile, int64_t spin_limit) {
+  if (int e = check_grid(G)) return e;
+  std::lock_guard<std::mutex> lk(G->mu);
+  if (!G->structured) return fail(CFDG_ERR_UNSUPPORTED, "the grid has no wavefront sweeps (a periodic axis)");
+  if (hold_tile < -1 || hold_tile >= G->tiles_j * G->tiles_k)
+    return fail(CFDG_ERR_INVALID, "hold_tile must be -1 or a tile of the grid's wavefront");
+  if (spin_limit < 1 || spin_limit > WAVE_SPIN_LIMIT)
+    return fail(CFDG_ERR_INVALID, "spin_limit must lie in 1 .. " + std::to_string(WAVE_SPIN_LIMIT));
+  G->wave_hold_tile = hold_tile;
+  G->wave_spin_limit = spin_limit;
+  reset_chunk(G);  // captured iteration chunks hold the sweeps' arguments
+  return 0;
 }
 
 int cfdg_residual_norm_noalloc(cfdg_grid* G, const double* d_x, const double* d_b, double* d_out, void* stream) {

@@ -13,6 +13,7 @@ namespace cfdg {
 
 constexpr int BLOCK = 256;
 constexpr int MAX_BLOCKS = 152 * 8;  // fixed reduction width: deterministic sums
+constexpr long long WAVE_SPIN_LIMIT = 1LL << 22;  // polls of a wavefront wait: about a second
 
 // Per-cell face flags: bit (2a + side) interior face, bit (6 + 2a + side) outlet
 // face, side 0 = lower face, 1 = upper face of axis a.

@@ -632,6 +632,7 @@ static int build_unmasked(const HostGrid& g, const Poller& poll, Hierarchy& h) {
     if (int c = poll.check()) return c;
     MgLevel lev;
     lev.n = (int32_t)anchors.size();
+    h.level_dims.push_back({n[0], n[1], n[2]});
     matrix_build(edges, anchors, lev.a, lev.diag);
     if (!anchored) {
       std::vector<int32_t> all(lev.n);

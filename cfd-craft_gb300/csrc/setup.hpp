@@ -3,6 +3,7 @@
 // Everything here is plain C++ compiled without FMA contraction, so the numbers
 // it produces are bit-identical to the reference's (crates/cfd-craft, Rust).
 #pragma once
+#include <array>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -115,6 +116,9 @@ struct Hierarchy {
   std::vector<int32_t> fluid_indices;  // compact index -> cell (masked); empty = identity
   std::vector<MgLevel> levels;
   std::vector<uint64_t> level_cells, level_nonzeros;
+  // Cells per axis of each level of an unmasked hierarchy (multigrid.rs:561-563); empty
+  // for masked hierarchies, whose aggregates have no dimensions (masked.rs:261-262).
+  std::vector<std::array<int32_t, 3>> level_dims;
 };
 
 // multigrid.rs:530-645 / masked.rs:181-291. Returns 0 or a CFDG_* code.

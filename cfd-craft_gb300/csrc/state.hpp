@@ -190,6 +190,8 @@ struct cfdg_grid {
   int tiles_j = 0, tiles_k = 0;
   int* wave_sync = nullptr;  // ticket, abort, per-tile progress of one sweep
   int* wave_err = nullptr;   // set when a wavefront wait gave up
+  long long wave_spin_limit = WAVE_SPIN_LIMIT;  // cfdg_debug_wave_stall
+  int wave_hold_tile = -1;
   std::shared_ptr<cfdg::Hierarchy> host_mg;  // the hierarchy as uploaded (level 0 re-indexed when full0)
   std::shared_ptr<void> mixed;               // the mixed-precision form's device state (mixed.cu)
   std::shared_ptr<struct cfdg_batch> solo;   // a one-grid batch for cfdg_project in the mixed form

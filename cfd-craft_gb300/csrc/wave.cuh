@@ -23,7 +23,6 @@
 namespace cfdg {
 
 constexpr int WTJ = 8, WTK = 8;  // tile of pencils per CTA
-constexpr long long WAVE_SPIN_LIMIT = 1LL << 22;  // about a second of polling
 
 enum WaveMode { IC0_FWD = 0, IC0_BWD = 1, GS_FWD = 2, GS_BWD = 3 };
 
@@ -46,6 +45,8 @@ struct WaveArgs {
   int* sync;        // [0] ticket, [1] abort, [2 ..] progress per tile
   int* error;       // persistent: set to 1 when a wait gave up
   const Scalars* S;
+  long long spin_limit;  // polls before a wait gives up (WAVE_SPIN_LIMIT)
+  int hold_tile;         // -1; a test of the bounded waits names a tile that never publishes
 };
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(WTJ* WTK) k_wave(WaveArgs A) {
   for (int s = 0; s < nsteps; ++s) {
     if (threadIdx.x == 0) {
       // Every thread passed the barrier of step s - 1, so steps 0 .. s - 2 are stored.
-      if (s > 1) {
+      if (s > 1 && t != A.hold_tile) {
         __threadfence();
         st_release(&progress[t], s - 1);
       }
@@ -105,7 +106,7 @@ __global__ void __launch_bounds__(WTJ* WTK) k_wave(WaveArgs A) {
       if (pj >= 0 && seen_j < need_j) {
         int v;
         while ((v = ld_acquire(&progress[pj])) < need_j) {
-          if (++spins > WAVE_SPIN_LIMIT || ld_acquire(&A.sync[1])) {
+          if (++spins > A.spin_limit || ld_acquire(&A.sync[1])) {
             bail_s = 1;
             break;
           }
@@ -115,7 +116,7 @@ __global__ void __launch_bounds__(WTJ* WTK) k_wave(WaveArgs A) {
       if (!bail_s && pk >= 0 && seen_k < need_k) {
         int v;
         while ((v = ld_acquire(&progress[pk])) < need_k) {
-          if (++spins > WAVE_SPIN_LIMIT || ld_acquire(&A.sync[1])) {
+          if (++spins > A.spin_limit || ld_acquire(&A.sync[1])) {
             bail_s = 1;
             break;
           }
@@ -208,7 +209,7 @@ __global__ void __launch_bounds__(WTJ* WTK) k_wave(WaveArgs A) {
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && t != A.hold_tile) {
     __threadfence();
     st_release(&progress[t], nsteps);
   }

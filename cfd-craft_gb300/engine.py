@@ -30,6 +30,7 @@ EXPORTS = (
     "cfdg_batch_destroy", "cfdg_batch_set_stream", "cfdg_batch_size", "cfdg_batch_project", "cfdg_batch_project_device",
     "cfdg_batch_time_kernel", "cfdg_batch_stats_json", "cfdg_server_create", "cfdg_server_destroy", "cfdg_server_set_stream",
     "cfdg_server_submit", "cfdg_server_progress", "cfdg_server_result", "cfdg_server_pending", "cfdg_server_stats_json", "cfdg_server_set_chunk", "cfdg_grid_set_cycle", "cfdg_grid_set_coarse_scale", "cfdg_grid_set_flow", "cfdg_step_device", "cfdg_scalar_step_device", "cfdg_receptors_set", "cfdg_receptors_sample", "cfdg_debug_momentum_update",
+    "cfdg_debug_wave_stall",
 )
 
 
@@ -76,6 +77,10 @@ class Info(C.Structure):
         ("device_seconds", C.c_double),
         ("graph_launches", C.c_uint64),
         ("loop_seconds", C.c_double),
+        ("hierarchy_bytes", C.c_uint64),
+        ("block_smoothing_cell_updates", C.c_uint64),
+        ("block_solves", C.c_uint64),
+        ("block_level_cell_visits", C.c_uint64),
     ]
 
     def as_dict(self):
@@ -166,6 +171,7 @@ def load(path: str = LIB_PATH):
         L.cfdg_batch_project_device.argtypes = [P, PP, PP, C.POINTER(C.c_double), C.c_double, C.c_uint64, POLL, P,
                                                 C.POINTER(Info), C.POINTER(C.c_int32)]
         L.cfdg_debug_time_kernel.argtypes = [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.cfdg_debug_wave_stall.argtypes = [P, C.c_int32, C.c_int64]
         _lib = L
         return L
 

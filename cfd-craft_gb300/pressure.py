@@ -265,6 +265,12 @@ class DeviceGrid:
         self._check(self.L.cfdg_debug_time_kernel(self.h, which, reps, C.byref(ms), C.byref(b)))
         return ms.value, b.value
 
+    def wave_stall(self, hold_tile: int = -1, spin_limit: int = 1 << 22):
+        """Test hook of the bounded wavefront waits (cfdg_debug_wave_stall): tile hold_tile
+        never publishes its progress and waits give up after spin_limit polls; (-1, 1 << 22)
+        restores normal sweeps."""
+        self._check(self.L.cfdg_debug_wave_stall(self.h, int(hold_tile), int(spin_limit)))
+
     def _check(self, rc):
         if rc:
             raise PressureError(rc, E.last_error())

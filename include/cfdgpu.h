@@ -111,6 +111,11 @@ typedef struct {
   double device_seconds;        /* device time of the solve, from CUDA events */
   uint64_t graph_launches;      /* captured iteration chunks replayed by the solve */
   double loop_seconds;          /* device time of the iteration loop alone */
+  /* MultigridWork (multigrid.rs:89,103-114): */
+  uint64_t hierarchy_bytes;     /* device bytes the hierarchy retains (this engine's storage) */
+  uint64_t block_smoothing_cell_updates; /* cell updates of line/plane block sweeps */
+  uint64_t block_solves;        /* exact line or plane block solves */
+  uint64_t block_level_cell_visits; /* cells of the block-smoothed levels per visit */
 } cfdg_info;
 
 /* Control::check (solver.rs:122-140): 0 continue, 1 "cancelled", 2 "wall_time_limit".
@@ -217,8 +222,12 @@ int cfdg_apply(cfdg_grid *grid, const double *x, double *y);
 /* pressure::center_nullspaces (pressure.rs:316-325). */
 int cfdg_center_nullspaces(cfdg_grid *grid, double *x);
 
-/* pressure::multigrid_stats (pressure.rs:100-106) as JSON:
- * {"level_cells":[...],"level_nonzeros":[...],"allocated_bytes":B}. Returns
+/* pressure::multigrid_stats (pressure.rs:100-106) as JSON, MultigridStats
+ * (multigrid.rs:55-72): {"level_cells":[...],"level_dimensions":[[nx,ny,nz],...],
+ * "level_nonzeros":[...],"allocated_bytes":B,"block_smoothers":[{"level","axes",
+ * "block_unknowns","block_count","half_bandwidth","allocated_bytes"},...]}, the empty
+ * level_dimensions (masked hierarchies) and block_smoothers (point smoothing) omitted as
+ * the reference's serialisation does; the byte counts are this engine's device storage. Returns
  * CFDG_PENDING when no hierarchy was built yet. Safe to call from a poll callback. */
 int cfdg_multigrid_stats_json(cfdg_grid *grid, char *buf, size_t cap);
 
@@ -306,9 +315,12 @@ int64_t cfdg_server_stats_json(cfdg_server *server, char *buf, int64_t cap);
 uint64_t cfdg_grid_device_bytes(const cfdg_grid *grid);
 
 /* No reference counterpart: an addition for callers that cannot allocate device memory.
- * Writes |A x - b| / |b| (the relative residual of the solve's acceptance gate,
- * pressure.rs:403-415) for device vectors x[N], b[N] of an open grid to d_out[0], on
- * `stream` (NULL: the grid's stream), without waiting for it. Some callers cannot call
+ * Writes |A x - b| / |b| for device vectors x[N], b[N] of an open grid to d_out[0], on
+ * `stream` (NULL: the grid's stream), without waiting for it; 0 when |b| < 1e-24, as
+ * the solve reports for a zero right-hand side (pressure.rs:372-375). b is used as
+ * given, not centred: the value equals the relative residual of the solve's acceptance
+ * gate (pressure.rs:403-415), which uses the centred b, on grids whose fluid components
+ * all touch an outlet, or for a b whose closed components already have zero mean. Some callers cannot call
  * cudaMalloc: a host that has handed the whole HBM budget to resident serving state, a
  * step that must not block on the implicit device synchronisation an allocation can
  * cause, or code running where an allocation failure cannot be handled. This entry
@@ -333,6 +345,15 @@ int cfdg_debug_precondition(cfdg_grid *grid, const double *r, double *z);
 
 /* projection_rhs (pressure.rs:440-459): b[N], terms[N] from u[F]. */
 int cfdg_debug_projection_rhs(cfdg_grid *grid, const double *u, double dt, double *b, double *terms);
+
+/* Test hook of the bounded device waits: from the next solve on, wavefront tile
+ * hold_tile (-1: none) of the grid's structured sweeps never publishes its progress, and
+ * every wait gives up after spin_limit polls (1 .. the default of about a second). The
+ * tiles that wait for the held tile give up, raise the sweep's abort flag so the others
+ * return too, and the call reports CFDG_ERR_TIMEOUT with u, p and x unchanged; the
+ * context stays usable. hold_tile = -1 with the default limit restores normal sweeps.
+ * CFDG_ERR_UNSUPPORTED on grids with a periodic axis (no wavefront sweeps). */
+int cfdg_debug_wave_stall(cfdg_grid *grid, int32_t hold_tile, int64_t spin_limit);
 
 /* Number of kernels this library has enqueued since it was loaded (a CUDA-graph
  * launch counts its kernel nodes). */

@@ -93,6 +93,8 @@ struct Info {
            hierarchy_nonzeros = 0, cycles = 0, smoothing_cell_updates = 0,
            residual_cell_updates = 0, restriction_cell_updates = 0,
            prolongation_cell_updates = 0, coarse_solves = 0;
+  // Block (line/plane) smoothing of anisotropic levels (multigrid.rs:103-114, 677-718).
+  uint64_t block_smoothing_cell_updates = 0, block_solves = 0, block_level_cell_visits = 0;
 };
 
 typedef int (*PollFn)(void*);
@@ -1184,9 +1186,16 @@ static void cycle(std::vector<Level>& levels, size_t at, Info& w) {
   size_t n = level.x.size();
   std::fill(level.x.begin(), level.x.end(), 0.0);
   const int sweeps = level.lines.empty() ? 2 : 1;
+  if (!level.lines.empty()) w.block_level_cell_visits += n;
   for (int pass = 0; pass < sweeps; ++pass) {
-    if (level.lines.empty()) level.matrix.sweep(level.rhs.data(), level.x.data(), n, false);
-    else level.lines[pass % level.lines.size()].sweep(level.rhs.data(), level.x.data(), false);
+    if (level.lines.empty()) {
+      level.matrix.sweep(level.rhs.data(), level.x.data(), n, false);
+    } else {
+      BlockSmoother& b = level.lines[pass % level.lines.size()];
+      b.sweep(level.rhs.data(), level.x.data(), false);
+      w.block_solves += b.nodes.size() / b.length;
+      w.block_smoothing_cell_updates += n;
+    }
   }
   center_plain(level.x.data(), n, level.anchored);
   level.matrix.product(level.x.data(), level.residual.data(), n);
@@ -1207,8 +1216,14 @@ static void cycle(std::vector<Level>& levels, size_t at, Info& w) {
     level.x[i] += s;
   }
   for (int pass = 0; pass < sweeps; ++pass) {
-    if (level.lines.empty()) level.matrix.sweep(level.rhs.data(), level.x.data(), n, true);
-    else level.lines[(sweeps - 1 - pass) % level.lines.size()].sweep(level.rhs.data(), level.x.data(), true);
+    if (level.lines.empty()) {
+      level.matrix.sweep(level.rhs.data(), level.x.data(), n, true);
+    } else {
+      BlockSmoother& b = level.lines[(sweeps - 1 - pass) % level.lines.size()];
+      b.sweep(level.rhs.data(), level.x.data(), true);
+      w.block_solves += b.nodes.size() / b.length;
+      w.block_smoothing_cell_updates += n;
+    }
   }
   center_plain(level.x.data(), n, level.anchored);
   w.smoothing_cell_updates += 2 * sweeps * n;
@@ -1477,6 +1492,7 @@ typedef struct {
       smoothing_cell_updates, residual_cell_updates, restriction_cell_updates,
       prolongation_cell_updates, coarse_solves;
   uint64_t polls;
+  uint64_t block_smoothing_cell_updates, block_solves, block_level_cell_visits;
 } ora_info;
 
 static void fill_info(const Info& in, uint64_t polls, ora_info* out) {
@@ -1498,6 +1514,9 @@ static void fill_info(const Info& in, uint64_t polls, ora_info* out) {
   out->prolongation_cell_updates = in.prolongation_cell_updates;
   out->coarse_solves = in.coarse_solves;
   out->polls = polls;
+  out->block_smoothing_cell_updates = in.block_smoothing_cell_updates;
+  out->block_solves = in.block_solves;
+  out->block_level_cell_visits = in.block_level_cell_visits;
 }
 
 void* ora_grid_build(const ora_case* c, char* err, size_t cap) {
@@ -1949,6 +1968,38 @@ int32_t ora_mg_levels(void* gp, uint64_t* cells, uint64_t* nonzeros, int32_t cap
     nonzeros[i] = g->hierarchy->level_nonzeros[i];
   }
   return L;
+}
+// Cell dimensions per level of an unmasked hierarchy (MultigridStats::level_dimensions,
+// multigrid.rs:561-563,611): dims[3*i + a]. Returns the level count, 0 for a masked
+// hierarchy (its aggregates have no dimensions, masked.rs:261-262) or before a build.
+int32_t ora_mg_dims(void* gp, int64_t* dims, int32_t cap) {
+  Grid* g = (Grid*)gp;
+  if (!g->hierarchy || g->hierarchy->masked) return 0;
+  int32_t L = (int32_t)g->hierarchy->levels.size();
+  for (int32_t i = 0; i < L && i < cap; ++i)
+    for (int a = 0; a < 3; ++a) dims[3 * i + a] = (int64_t)g->hierarchy->levels[i].dims[a];
+  return L;
+}
+// The block smoothers of the hierarchy (MultigridStats::block_smoothers, multigrid.rs:
+// 612-616; BlockSmootherStats, line.rs:200-209 without the storage bytes): per smoother
+// out[5*s ..] = level, axes bit mask, unknowns per block, block count, half-bandwidth.
+// Returns the number of smoothers.
+int32_t ora_mg_blocks(void* gp, int64_t* out, int32_t cap) {
+  Grid* g = (Grid*)gp;
+  if (!g->hierarchy || g->hierarchy->masked) return 0;
+  int32_t s = 0;
+  for (size_t l = 0; l < g->hierarchy->levels.size(); ++l)
+    for (const BlockSmoother& b : g->hierarchy->levels[l].lines) {
+      if (s < cap) {
+        int64_t mask = 0;
+        for (int a : b.axes) mask |= 1 << a;
+        int64_t* o = out + 5 * s;
+        o[0] = (int64_t)l, o[1] = mask, o[2] = (int64_t)b.length;
+        o[3] = (int64_t)(b.nodes.size() / b.length), o[4] = (int64_t)b.bandwidth;
+      }
+      ++s;
+    }
+  return s;
 }
 // Masked hierarchy export of one level: parent map (cells of this level -> next), the CSR
 // matrix, and the diagonal. Returns the number of rows, or -1 when absent.

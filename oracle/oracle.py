@@ -64,6 +64,9 @@ class Info(C.Structure):
         ("prolongation_cell_updates", C.c_uint64),
         ("coarse_solves", C.c_uint64),
         ("polls", C.c_uint64),
+        ("block_smoothing_cell_updates", C.c_uint64),
+        ("block_solves", C.c_uint64),
+        ("block_level_cell_visits", C.c_uint64),
     ]
 
     def as_dict(self):
@@ -112,6 +115,10 @@ def lib():
             L.ora_mg_apply.argtypes = [P, dp, dp, C.POINTER(Info)]
             L.ora_mg_levels.restype = C.c_int32
             L.ora_mg_levels.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int32]
+            L.ora_mg_dims.restype = C.c_int32
+            L.ora_mg_dims.argtypes = [P, C.c_void_p, C.c_int32]
+            L.ora_mg_blocks.restype = C.c_int32
+            L.ora_mg_blocks.argtypes = [P, C.c_void_p, C.c_int32]
             L.ora_mg_level_dense.restype = C.c_int64
             L.ora_mg_level_dense.argtypes = [P, C.c_int32, C.c_void_p, C.c_void_p]
             L.ora_mg_transfer_dense.restype = C.c_int64
@@ -365,6 +372,25 @@ class Grid:
         nz = np.zeros(64, np.uint64)
         L = lib().ora_mg_levels(self.h, _vp(cells), _vp(nz), 64)
         return [int(v) for v in cells[:L]], [int(v) for v in nz[:L]]
+
+    def mg_stats(self):
+        """MultigridStats (multigrid.rs:55-72) of the current hierarchy without the storage
+        bytes: level_cells, level_nonzeros, level_dimensions (unmasked hierarchies; empty
+        for masked ones) and block_smoothers (level, axes, block_unknowns, block_count,
+        half_bandwidth)."""
+        cells, nz = self.mg_levels()
+        dims = np.zeros(3 * 64, np.int64)
+        nd = lib().ora_mg_dims(self.h, _vp(dims), 64)
+        blk = np.zeros(5 * 256, np.int64)
+        nb = lib().ora_mg_blocks(self.h, _vp(blk), 256)
+        smoothers = []
+        for s_ in range(min(nb, 256)):
+            lv, mask, unk, cnt, bw = (int(v) for v in blk[5 * s_:5 * s_ + 5])
+            smoothers.append({"level": lv, "axes": [a for a in range(3) if mask >> a & 1], "block_unknowns": unk,
+                              "block_count": cnt, "half_bandwidth": bw})
+        return {"level_cells": cells, "level_nonzeros": nz,
+                "level_dimensions": [[int(v) for v in dims[3 * i:3 * i + 3]] for i in range(nd)],
+                "block_smoothers": smoothers}
 
     def mg_masked_level(self, level):
         L = lib()

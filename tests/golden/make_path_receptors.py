@@ -3,9 +3,9 @@ path receptors on a small grid with a building, computed by the reference's own
 independent checker (validation/check_fields.py receptor_weights / path_weights, pure
 Python), as golden vectors for the package's restatement (cfd-craft_gb300/receptors.py).
 
-    python tests/golden/make_path_receptors.py /root/reference
+    python tests/golden/make_path_receptors.py REFERENCE_CHECKOUT
 
-The argument is the reference checkout (its validation/check_fields.py is imported).
+The argument is the CFD-craft checkout (its validation/check_fields.py is imported).
 """
 import importlib.util
 import json

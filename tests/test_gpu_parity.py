@@ -268,6 +268,61 @@ def test_block_smoothed_cycle_matches(pkg, O, name):
         assert np.max(np.abs(z - oz)) <= 1e-12 * max(1.0, np.max(np.abs(oz)))
 
 
+BLOCK_COUNTERS = ("block_smoothing_cell_updates", "block_solves", "block_level_cell_visits", "cycles",
+                  "smoothing_cell_updates", "residual_cell_updates", "coarse_solves")
+
+
+@pytest.mark.parametrize("name", ["thin100", "plate64", "periodic", "stiff-two-cell", "near-isotropic"])
+def test_multigrid_work_counters_and_stats_match_oracle(pkg, O, name):
+    """MultigridWork's block counters (multigrid.rs:103-114) and MultigridStats'
+    level_dimensions and block_smoothers (multigrid.rs:55-72) against the oracle's on the
+    anisotropic campaign shapes, with the reference's own identities
+    (tests/multigrid.rs:310-330): block smoothing = 2 x block level visits, block solves > 0,
+    and, where every smoothed level is block-smoothed, smoothing = block smoothing."""
+    c = anisotropic_case(name, "multigrid")
+    g, og, dg = open_pair(pkg, O, c, "multigrid")
+    exact, rhs = rough_rhs(og)
+    x, info = dg.solve_scaled(rhs, None, 1e-14, 1200)
+    code, ox, oinfo = og.solve(rhs, 1e-14, 1200)
+    assert code == 0
+    stats, ostats = dg.multigrid_stats(), og.mg_stats()
+    dg.close()
+    w = info.work
+    for k in ("level_cells", "level_nonzeros", "level_dimensions"):
+        assert stats.get(k, []) == ostats[k], (name, k)
+    mine = [{k: b[k] for k in ("level", "axes", "block_unknowns", "block_count", "half_bandwidth")}
+            for b in stats.get("block_smoothers", [])]
+    assert mine == ostats["block_smoothers"], name
+    assert all(b["allocated_bytes"] > 0 for b in stats.get("block_smoothers", []))
+    assert stats["allocated_bytes"] > 0 and w["hierarchy_bytes"] == stats["allocated_bytes"]
+    if info.iterations == oinfo["iterations"]:
+        for k in BLOCK_COUNTERS:
+            assert w[k] == oinfo[k], (name, k, w[k], oinfo[k])
+    assert w["block_smoothing_cell_updates"] == 2 * w["block_level_cell_visits"]
+    if ostats["block_smoothers"]:
+        assert w["block_solves"] > 0
+        smoothed = {b["level"] for b in ostats["block_smoothers"]}
+        if smoothed == set(range(len(ostats["level_cells"]) - 1)):
+            assert w["smoothing_cell_updates"] == w["block_smoothing_cell_updates"]
+    else:
+        assert w["block_solves"] == 0 and w["block_level_cell_visits"] == 0
+
+
+def test_masked_stats_omit_dimensions(pkg, O):
+    """Masked hierarchies have no level dimensions or block smoothers (masked.rs:259-262,285)."""
+    c = pkg.synth.case((24, 20, 12), 2.0, boxes=[((10, 6, 0), (20, 14, 10))], preconditioner="multigrid")
+    g, og, dg = open_pair(pkg, O, c, "multigrid")
+    u = pkg.synth.random_velocity(g, 1)
+    info = dg.project(u.copy(), np.zeros(g.count), 0.1, 1e-8, 1000)
+    og.project(u, np.zeros(g.count), 0.1, 1e-8, 1000)
+    stats = dg.multigrid_stats()
+    dg.close()
+    assert "level_dimensions" not in stats and "block_smoothers" not in stats
+    assert og.mg_stats()["level_dimensions"] == [] and og.mg_stats()["block_smoothers"] == []
+    assert stats["level_cells"] == og.mg_stats()["level_cells"]
+    assert info.work["hierarchy_bytes"] == stats["allocated_bytes"] > 0
+
+
 @pytest.mark.parametrize("which", ["barrier", "singleton"])
 @pytest.mark.parametrize("precision", ["plain", "mixed"])
 def test_sealed_components_against_pivoted_dense_reference(pkg, O, which, precision):
