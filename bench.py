@@ -697,8 +697,8 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
                    "every request on two copy streams beside the server's (a case's next inputs prefetched into "
                    "a second device buffer, results copied out after the request's epilogue)", "steps": srv_steps}
     kernels = {}
-    for name, which, reps in (("rb_half_sweep_fp32", 0, 20), ("operator_fp32", 1, 20),
-                              ("coarse_levels", 2, 10), ("vcycle_fp32", 3, 5)):
+    for name, which, reps in (("rb_half_sweep_fp32", 0, 20), ("rb_half_sweep_fp32_unstaged", 4, 20),
+                              ("operator_fp32", 1, 20), ("coarse_levels", 2, 10), ("vcycle_fp32", 3, 5)):
         ms, b = bt.time_kernel(which, reps)
         kernels[name] = {"ms": round(ms, 4), "GB/s": round(b / ms / 1e6, 1) if b else None, "algorithmic_bytes": b}
     bt.close()

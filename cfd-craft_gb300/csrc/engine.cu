@@ -2498,6 +2498,17 @@ int cfdg_grid_set_cycle(cfdg_grid* G, int32_t nu_fine, int32_t nu_coarse) {
   return 0;
 }
 
+int cfdg_grid_set_sweep_tile(cfdg_grid* G, int32_t rows, int32_t stages) {
+  if (int e = check_grid(G)) return e;
+  if (!(rows == 8 || rows == 16 || rows == 32) || stages < 2 || stages > 8)
+    return fail(CFDG_ERR_INVALID, "sweep tile: rows must be 8, 16 or 32 and stages 2..8");
+  std::lock_guard<std::mutex> lk(G->mu);
+  if (G->mx_sweep_rows != rows || G->mx_sweep_stages != stages) G->solo.reset();
+  G->mx_sweep_rows = rows;
+  G->mx_sweep_stages = stages;
+  return 0;
+}
+
 int cfdg_grid_set_coarse_scale(cfdg_grid* G, double alpha) {
   if (int e = check_grid(G)) return e;
   if (!(alpha > 0.0 && alpha < 2.0)) return fail(CFDG_ERR_INVALID, "the coarse-correction scale must lie in (0, 2)");

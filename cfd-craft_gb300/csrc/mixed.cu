@@ -26,6 +26,7 @@
 // so the whole iteration is captured once as a CUDA graph and replayed in chunks; the
 // server (continuous batching) admits and finishes requests between chunks.
 #include <cooperative_groups.h>
+#include <cuda.h>  // CUtensorMap (the encoder is fetched from the driver at run time)
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -86,6 +87,10 @@ struct FineCase {
   const float* idiag0;   // its reciprocal, 0 where the diagonal is 0
   const uint16_t* flags0;  // face flags
   int nxh, N2;           // slots per colour and row (ceil(nx/2)); slots in all (2 * rows * nxh)
+  // TMA descriptors of the level-0 arrays viewed as [rows][2 colours][nxh] (k_rb_tma):
+  // rhs0, idiag0, flags0, x0 with boxes of RT rows, x0 with RT + 2 rows; null when the
+  // case does not take the staged path (non-uniform weights or nxh not a multiple of 8).
+  const CUtensorMap* tmaps;
   // FP64 outer vectors (the grid's buffers, natural cell order)
   double *x64, *r64, *bc, *b, *terms;
   // FP32 inner vectors (split layout; padding slots stay zero)
@@ -824,6 +829,261 @@ __global__ void __launch_bounds__(TILE, 5) k_rb(const FineCase* FC, MState* ST, 
     const int2 t = tiles[ti];
     SKIP_CASE(t, S_.state == RUN || S_.state == START)
     b_rb(FC, ST, t, cached_, color, first);
+  }
+}
+
+// ----------------------------------------------------------------- staged red-black half sweep
+// The same half sweep as k_rb (uniform weights, nxh a multiple of 8), with every operand
+// brought into shared memory by the tensor memory accelerator. A stage holds SR rows of
+// one case (SR = 8, 16 or 32: one to four consecutive work-list tiles); its operands are six
+// 3-D tensor copies ([rows][colour][nxh] views of the split layout): the own colour's rhs,
+// 1/diag and flags of the SR rows, and the other colour's x of rows r0-1 .. r0+SR (y
+// neighbours and the rows themselves) and of the SR rows one z-layer below and above.
+// Rows outside the grid arrive as zeros (their faces are absent). A producer warp keeps
+// NS stages in flight, each completed by an mbarrier transaction count; the RT consumer
+// warps sweep a stage (warp w takes rows w, w + RT, ...) and release it through a second
+// mbarrier. Results are bit-identical to k_rb: the same operands in the same fmaf order.
+// The stage height and depth are the sweep's tile shape (cfdg_grid_set_sweep_tile).
+constexpr int RB_MAX_NS = 8;    // stages per block at most
+constexpr int RB_HEIGHTS = 3;   // stage heights 8, 16, 32 rows (tensor maps per height)
+
+struct RbOff {
+  int rhs, id, fl, xy, zl, zh, stage;
+};
+// Byte offsets inside one stage of sr rows for a row length of hmax slots (a multiple of
+// 16, so every region starts on a 128-byte boundary).
+__host__ __device__ __forceinline__ RbOff rb_offsets(int hmax, int sr) {
+  RbOff o;
+  o.rhs = 0;
+  o.id = o.rhs + sr * 4 * hmax;
+  o.fl = o.id + sr * 4 * hmax;
+  o.xy = o.fl + sr * 2 * hmax;
+  o.zl = o.xy + (sr + 2) * 4 * hmax;
+  o.zh = o.zl + sr * 4 * hmax;
+  o.stage = o.zh + sr * 4 * hmax;
+  return o;
+}
+__host__ __device__ __forceinline__ int rb_height_index(int sr) { return sr == 8 ? 0 : (sr == 16 ? 1 : 2); }
+constexpr long long RB_WAIT_CYCLES = 2000000000LL;  // a stage's wait gives up after ~1 s of SM clock
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for a stage's barrier for at most RB_WAIT_CYCLES SM cycles; false when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() - t0 > RB_WAIT_CYCLES) return false;
+  return true;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// What a consumer warp needs of a stage, written by the producer beside the data.
+struct RbHead {
+  float* x0;
+  float w[3];
+  int r0, nrows, ny, h, ci, pad;  // first row, valid rows (-1: end of the block's range)
+};
+constexpr int RB_THREADS = TILE + 32;  // RT consumer warps and one producer warp
+
+__global__ void __launch_bounds__(RB_THREADS, 3) k_rb_tma(const FineCase* FC, MState* ST, const int2* tiles,
+                                                          const int* count, int color, int first, int hmax, int sr,
+                                                          int ns) {
+  extern __shared__ __align__(128) unsigned char rb_dyn[];
+  // Stage base on a 128-byte boundary (the launch adds 128 bytes of slack).
+  unsigned char* const rb_smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(rb_dyn) + 127) & ~(uintptr_t)127);
+  __shared__ __align__(8) uint64_t full[RB_MAX_NS], empty[RB_MAX_NS];
+  __shared__ RbHead head[RB_MAX_NS];
+  TILE_RANGE
+  const RbOff O = rb_offsets(hmax, sr);
+  const bool skipx = first && color == 0;  // x = 0: the sweep reads no neighbour
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < ns; ++st) {
+      mbar_init(&full[st], 1);    // the producer's arrival (with the copies' byte count)
+      mbar_init(&empty[st], RT);  // one arrival per consumer warp
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (warp == RT) {
+    // Producer warp: walks the block's tile range 32 entries at a time, keeps the current
+    // case's descriptor in registers, skips the tiles of cases that are not running, joins
+    // up to sr / RT consecutive tiles of one case into a stage and fills each stage as soon
+    // as the consumers have released it.
+    int cur = -1, st = 0;
+    bool active = false;
+    const CUtensorMap* tm = nullptr;
+    RbHead hd{};
+    int rows_all = 0, run_y = 0, run_n = 0;
+    const int group = sr / RT, hi = rb_height_index(sr) * 5;
+    unsigned ephase = (1u << RB_MAX_NS) - 1;  // a fresh stage counts as released
+    bool dead = false;
+    // Issues the open run of tiles into the next released stage; false when the wait gave up.
+    auto flush = [&]() -> bool {
+      if (run_n == 0) return true;
+      int ok = 0;
+      if (lane == 0) ok = mbar_wait_bounded(&empty[st], (ephase >> st) & 1u);
+      if (!__shfl_sync(0xffffffffu, ok, 0)) return false;
+      ephase ^= 1u << st;
+      if (lane == 0) {
+        const int r0 = run_y * RT, h = hd.h, oc = color ^ 1;
+        hd.r0 = r0;
+        hd.nrows = min(run_n * RT, rows_all - r0);
+        head[st] = hd;
+        unsigned char* b = rb_smem + st * O.stage;
+        const unsigned bytes = sr * h * 8u + (skipx ? 0u : sr * h * 2u + (3 * sr + 2) * h * 4u);
+        mbar_expect_tx(&full[st], bytes);
+        tma_load_3d(b + O.rhs, &tm[hi + 0], 0, color, r0, &full[st]);
+        tma_load_3d(b + O.id, &tm[hi + 1], 0, color, r0, &full[st]);
+        if (!skipx) {
+          tma_load_3d(b + O.fl, &tm[hi + 2], 0, color, r0, &full[st]);
+          tma_load_3d(b + O.xy, &tm[hi + 4], 0, oc, r0 - 1, &full[st]);
+          tma_load_3d(b + O.zl, &tm[hi + 3], 0, oc, r0 - hd.ny, &full[st]);
+          tma_load_3d(b + O.zh, &tm[hi + 3], 0, oc, r0 + hd.ny, &full[st]);
+        }
+      }
+      __syncwarp();
+      st = st + 1 == ns ? 0 : st + 1;
+      run_n = 0;
+      return true;
+    };
+    for (int base = t0_; base < t1_ && !dead; base += 32) {
+      const int2 mine = base + lane < t1_ ? tiles[base + lane] : make_int2(-1, 0);
+      const int nq = min(32, t1_ - base);
+      for (int q = 0; q < nq; ++q) {
+        const int tx = __shfl_sync(0xffffffffu, mine.x, q), ty = __shfl_sync(0xffffffffu, mine.y, q);
+        if (tx != cur) {
+          if (!flush()) {
+            dead = true;
+            break;
+          }
+          cur = tx;
+          const int state = ST[tx].state;
+          active = state == RUN || state == START;
+          const FineCase& F = FC[tx];
+          tm = F.tmaps;
+          hd.x0 = F.x0;
+          hd.w[0] = F.w32[0], hd.w[1] = F.w32[1], hd.w[2] = F.w32[2];
+          hd.ny = F.n[1], hd.h = F.nxh, hd.ci = tx;
+          rows_all = F.n[1] * F.n[2];
+        }
+        if (!active) continue;
+        if (run_n > 0 && ty != run_y + run_n && !flush()) {
+          dead = true;
+          break;
+        }
+        if (run_n == 0) run_y = ty;
+        if (++run_n == group && !flush()) {
+          dead = true;
+          break;
+        }
+      }
+    }
+    if (!dead && flush()) {
+      // End of the range: an empty stage in the next released slot.
+      if (lane == 0 && mbar_wait_bounded(&empty[st], (ephase >> st) & 1u)) {
+        head[st].nrows = -1;
+        mbar_arrive(&full[st]);
+      }
+      return;
+    }
+    // The consumers never released a stage: fail the case at hand and stop feeding; the
+    // consumers' own bounded waits end their loop.
+    if (lane == 0 && cur >= 0) {
+      ST[cur].error = CFDG_ERR_TIMEOUT;
+      ST[cur].state = FAIL;
+    }
+    return;
+  }
+  // Consumer warps: warp w sweeps rows w, w + RT, ... of each stage, then releases it.
+  unsigned fphase = 0;  // bit st: parity of the phase stage st completes next
+  int last_ci = -1;
+  for (int st = 0;; st = st + 1 == ns ? 0 : st + 1) {
+    if (!__all_sync(0xffffffffu, mbar_wait_bounded(&full[st], (fphase >> st) & 1u))) {
+      // Never filled: fail the case last swept (if any), give the copies that may still be
+      // in flight a bounded wait, and leave.
+      if (lane == 0 && last_ci >= 0) {
+        ST[last_ci].error = CFDG_ERR_TIMEOUT;
+        ST[last_ci].state = FAIL;
+      }
+      mbar_wait_bounded(&full[st], (fphase >> st) & 1u);
+      return;
+    }
+    fphase ^= 1u << st;
+    const RbHead hd = head[st];
+    if (hd.nrows < 0) return;  // every stage before it was swept; nothing is in flight
+    last_ci = hd.ci;
+    const int h = hd.h;
+    const unsigned char* b = rb_smem + st * O.stage;
+    for (int lr = warp; lr < hd.nrows; lr += RT) {
+      const int r = hd.r0 + lr;
+      const int par = (r % hd.ny + r / hd.ny + color) & 1;
+      const float* srhs = reinterpret_cast<const float*>(b + O.rhs) + lr * h;
+      const float* sid = reinterpret_cast<const float*>(b + O.id) + lr * h;
+      const uint16_t* sfl = reinterpret_cast<const uint16_t*>(b + O.fl) + lr * h;
+      const float* sxo = reinterpret_cast<const float*>(b + O.xy) + (lr + 1) * h;
+      const float* szl = reinterpret_cast<const float*>(b + O.zl) + lr * h;
+      const float* szh = reinterpret_cast<const float*>(b + O.zh) + lr * h;
+      float* __restrict__ x = hd.x0 + lay(r, color, h, 0);
+      for (int s2 = 2 * lane; s2 < h; s2 += 64) {
+        const float2 id = *reinterpret_cast<const float2*>(sid + s2);
+        float2 v = *reinterpret_cast<const float2*>(srhs + s2);
+        if (!skipx) {
+          const unsigned fl2 = *reinterpret_cast<const unsigned*>(sfl + s2);
+          Pair P;
+          P.xo = *reinterpret_cast<const float2*>(sxo + s2);
+          P.yl = *reinterpret_cast<const float2*>(sxo - h + s2);
+          P.yh = *reinterpret_cast<const float2*>(sxo + h + s2);
+          P.zl = *reinterpret_cast<const float2*>(szl + s2);
+          P.zh = *reinterpret_cast<const float2*>(szh + s2);
+          const int e = par ? s2 + 2 : s2 - 1;
+          P.xe = (e >= 0 && e < h) ? sxo[e] : 0.0f;
+          float nb[6];
+          P.of(0, par, nb);
+#pragma unroll
+          for (int f = 0; f < 6; ++f)
+            if (fl2 & (1u << f)) v.x = fmaf(hd.w[f >> 1], nb[f], v.x);
+          P.of(1, par, nb);
+#pragma unroll
+          for (int f = 0; f < 6; ++f)
+            if (fl2 & (1u << (16 + f))) v.y = fmaf(hd.w[f >> 1], nb[f], v.y);
+        }
+        float2 out;
+        out.x = id.x == 0.0f ? 0.0f : v.x * id.x;
+        out.y = id.y == 0.0f ? 0.0f : v.y * id.y;
+        *reinterpret_cast<float2*>(x + s2) = out;
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // this warp's reads before the stage's next fill
+      mbar_arrive(&empty[st]);
+    }
   }
 }
 
@@ -1733,6 +1993,41 @@ Csr permute_csr(const Csr& a, const std::vector<int32_t>& prow, const std::vecto
   return out;
 }
 
+// cuTensorMapEncodeTiled, fetched from the driver (the library links only the runtime).
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiled tensor_map_encoder() {
+  static EncodeTiled fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// A split-layout level-0 array as a 3-D tensor [rows][2 colours][nxh] (x fastest), read in
+// boxes of one colour's half-rows of `box_rows` consecutive rows. The row length in bytes
+// must be a multiple of 16 (nxh a multiple of 8 for 16-bit flags).
+bool encode_split(CUtensorMap& m, const void* base, bool u16, int nxh, int rows, int box_rows) {
+  EncodeTiled enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t es = u16 ? 2 : 4;
+  const cuuint64_t dims[3] = {(cuuint64_t)nxh, 2, (cuuint64_t)rows};
+  const cuuint64_t strides[2] = {(cuuint64_t)nxh * es, 2 * (cuuint64_t)nxh * es};
+  const cuuint32_t box[3] = {(cuuint32_t)nxh, 1, (cuuint32_t)box_rows};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(&m, u16 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims,
+             strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // Builds the FP32 device copy of a grid's hierarchy for the mixed form (cached on the grid).
 // Each coarse level is renumbered so that the rows of every smoother colour are
 // contiguous (colour c owns rows [coff[c], coff[c+1])): sweeps then read the right-hand
@@ -1832,6 +2127,29 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     CU(cudaMemsetAsync(F.rhs0, 0, sizeof(float) * F.N2, s));
   } else {
     F.rhs0 = F.r32;
+  }
+  // Tensor maps of the staged half sweep (k_rb_tma): uniform weights, whole 16-byte rows.
+  F.tmaps = nullptr;
+  if (F.uniform && F.nxh % 8 == 0 && F.nxh <= 256) {
+    // Per stage height (8, 16, 32 rows): rhs0, idiag0, flags0 and x0 in boxes of that
+    // height, x0 in boxes of two rows more.
+    std::vector<CUtensorMap> maps(5 * RB_HEIGHTS);
+    const int rows_all = h.n[1] * h.n[2];
+    bool ok = true;
+    for (int q = 0; q < RB_HEIGHTS && ok; ++q) {
+      const int sr = RT << q;
+      CUtensorMap* m = maps.data() + 5 * q;
+      ok = encode_split(m[0], F.rhs0, false, F.nxh, rows_all, sr) &&
+           encode_split(m[1], F.idiag0, false, F.nxh, rows_all, sr) &&
+           encode_split(m[2], F.flags0, true, F.nxh, rows_all, sr) &&
+           encode_split(m[3], F.x0, false, F.nxh, rows_all, sr) &&
+           encode_split(m[4], F.x0, false, F.nxh, rows_all, sr + 2);
+    }
+    if (ok) {
+      CUtensorMap* d = nullptr;
+      if (int e = A.upload(&d, maps, s)) return e;
+      F.tmaps = d;
+    }
   }
   F.ntiles = (h.n[1] * h.n[2] + RT - 1) / RT;  // row tiles (one reduction partial each)
   if (int e = A.alloc(&F.partials, (size_t)F.ntiles * (TILE / 32))) return e;
@@ -2145,6 +2463,11 @@ struct cfdg_batch {
   int nlev_all = 0;
   int coop_blocks = 0;
   bool coop = true;
+  // Staged half sweeps (k_rb_tma): every case has its tensor maps; the largest row length
+  // (rounded up to 16 slots), the dynamic shared memory and the persistent grid.
+  bool rb_tma = false;
+  int rb_hmax = 0, rb_grid = 1, rb_sr = RT, rb_ns = 3;
+  size_t rb_smem = 0;
   int csize = CS;
   std::vector<char> active;
   cudaGraphExec_t chunk = nullptr;
@@ -2384,6 +2707,16 @@ void launch_coarse(cfdg_batch* B, cudaStream_t s) {
 #define FINE(K, W, ...) \
   K<<<grid_of(K, TILE, B->g_fine), TILE, 0, s>>>(B->d_fc, B->d_st, (W).tiles, (W).counts, ##__VA_ARGS__)
 
+// One red-black half sweep of level 0 over the work-list: the staged kernel when every case
+// has its tensor maps, else the register kernel (the same bits either way).
+void launch_rb(cfdg_batch* B, const WorkLists& W, int color, int first, cudaStream_t s) {
+  if (B->rb_tma)
+    k_rb_tma<<<B->rb_grid, RB_THREADS, B->rb_smem, s>>>(B->d_fc, B->d_st, W.tiles, W.counts, color, first,
+                                                        B->rb_hmax, B->rb_sr, B->rb_ns);
+  else
+    FINE(k_rb, W, color, first);
+}
+
 void enqueue_vcycle(cfdg_batch* B, cudaStream_t s) {
   const WorkLists& W = B->run;
   if (B->any_groups) {
@@ -2392,8 +2725,8 @@ void enqueue_vcycle(cfdg_batch* B, cudaStream_t s) {
   }
   // nu0 forward sweeps: red, black, red, black, ... (the first red starts from x = 0).
   for (int sw = 0; sw < B->nu0; ++sw) {
-    FINE(k_rb, W, 0, sw == 0 ? 1 : 0);
-    FINE(k_rb, W, 1, 0);
+    launch_rb(B, W, 0, sw == 0 ? 1 : 0, s);
+    launch_rb(B, W, 1, 0, s);
   }
   if (B->any_groups) k_center0<<<grid_of(k_center0, 256, B->g_g), 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 1);
   FINE(k_v_resid, W);
@@ -2403,8 +2736,8 @@ void enqueue_vcycle(cfdg_batch* B, cudaStream_t s) {
   FINE(k_v_prolong, W);
   // nu0 backward sweeps: black, red, ...
   for (int sw = 0; sw < B->nu0; ++sw) {
-    FINE(k_rb, W, 1, 0);
-    FINE(k_rb, W, 0, 0);
+    launch_rb(B, W, 1, 0, s);
+    launch_rb(B, W, 0, 0, s);
   }
   if (B->any_groups) k_center0<<<grid_of(k_center0, 256, B->g_g), 256, 0, s>>>(B->d_fc, B->d_st, W.gtab, W.counts + 3, 1);
 }
@@ -2581,6 +2914,33 @@ int cfdg_mixed_pack(cfdg_batch* B) {
   auto clamp = [](size_t n) { return (int)std::max<size_t>(1, std::min<size_t>(n, 1 << 30)); };
   B->g_fine = clamp(B->tiles.size());
   B->g_1 = clamp(B->tiles1.size());
+  B->rb_tma = nc > 0;
+  B->rb_hmax = 0;
+  for (int i = 0; i < nc; ++i) {
+    B->rb_tma = B->rb_tma && B->h_fc[i].tmaps != nullptr;
+    B->rb_hmax = std::max(B->rb_hmax, B->h_fc[i].nxh);
+  }
+  if (B->rb_tma) {
+    // The sweep's tile shape comes from the grids (cfdg_grid_set_sweep_tile), like the
+    // cycle's sweep counts; fewer stages are used when the requested ones do not fit.
+    B->rb_hmax = (B->rb_hmax + 15) / 16 * 16;
+    int dev = 0, sms = 0, per = 0, smem_max = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t stage = (size_t)rb_offsets(B->rb_hmax, B->rb_sr).stage;
+    while (B->rb_ns > 1 && (size_t)B->rb_ns * stage + 128 + 1024 > (size_t)smem_max) --B->rb_ns;
+    B->rb_smem = (size_t)B->rb_ns * stage + 128;
+    cudaFuncSetAttribute(k_rb_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B->rb_smem);
+    if (B->rb_ns < 2 ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rb_tma, RB_THREADS, B->rb_smem) != cudaSuccess ||
+        per < 1) {
+      cudaGetLastError();
+      B->rb_tma = false;
+    } else {
+      B->rb_grid = std::max(1, std::min(B->g_fine, sms * per));
+    }
+  }
   B->g_f = clamp(B->ftiles.size());
   B->g_g = clamp(B->gtab.size());
   if (int e = A.upload(&B->d_fc, B->h_fc, s)) return e;
@@ -2627,8 +2987,12 @@ int cfdg_mixed_add_case(cfdg_batch* B, cfdg_grid* G) {
   if (B->grids.empty()) {
     B->nu0 = G->mx_nu0;
     B->nuc = G->mx_nuc;
+    B->rb_sr = G->mx_sweep_rows;
+    B->rb_ns = G->mx_sweep_stages;
   } else if (B->nu0 != G->mx_nu0 || B->nuc != G->mx_nuc) {
     return fail(CFDG_ERR_INVALID, "the grids of a batch must share their V-cycle sweep counts");
+  } else if (B->rb_sr != G->mx_sweep_rows || B->rb_ns != G->mx_sweep_stages) {
+    return fail(CFDG_ERR_INVALID, "the grids of a batch must share their sweep tile shape");
   }
   B->grids.push_back(G);
   B->cases.push_back(cs);
@@ -2865,8 +3229,12 @@ int64_t cfdg_batch_stats_json(cfdg_batch* B, char* buf, int64_t cap) {
   if (!B) return -(int64_t)fail(CFDG_ERR_INVALID, "null batch");
   Locks locks(B->grids);
   char tmp[256];
-  snprintf(tmp, sizeof tmp, "{\"coarse_kernel\": \"%s\", \"coarse_blocks\": %d, \"cases\": [",
-           B->coop ? "cooperative" : "cluster", B->coop ? B->coop_blocks : (int)B->cases.size() * B->csize);
+  snprintf(tmp, sizeof tmp,
+           "{\"coarse_kernel\": \"%s\", \"coarse_blocks\": %d, \"staged_sweeps\": %s, \"sweep_blocks\": %d, "
+           "\"sweep_rows\": %d, \"sweep_stages\": %d, \"cases\": [",
+           B->coop ? "cooperative" : "cluster", B->coop ? B->coop_blocks : (int)B->cases.size() * B->csize,
+           B->rb_tma ? "true" : "false", B->rb_tma ? B->rb_grid : B->g_fine, B->rb_tma ? B->rb_sr : RT,
+           B->rb_tma ? B->rb_ns : 0);
   std::string out = tmp;
   for (size_t i = 0; i < B->cases.size(); ++i) {
     const CaseState& cs = *B->cases[i];
@@ -2918,6 +3286,9 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
   auto launch = [&]() {
     switch (which) {
       case 0:  // one red-black half sweep over every case's fine level
+        launch_rb(B, B->run, 1, 0, s);
+        break;
+      case 4:  // the same half sweep with the register kernel (no staging), for comparison
         FINE(k_rb, B->run, 1, 0);
         break;
       case 1:  // FP32 operator q = A p (with p.q)
@@ -2931,7 +3302,7 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
         break;
     }
   };
-  if (which == 0) bytes = 9.0 * cells;       // half the cells: rhs, 1/diag, u16 flags, x out; the other half's x in
+  if (which == 0 || which == 4) bytes = 9.0 * cells;  // half the cells: rhs, 1/diag, u16 flags, x out; the other half's x in
   else if (which == 1) bytes = 10.0 * cells; // p in, u16 flags, q out
   launch();
   launch();

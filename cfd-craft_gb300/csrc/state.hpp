@@ -202,6 +202,9 @@ struct cfdg_grid {
   // the coarse levels (cfdg_grid_set_cycle); a batch takes them from its grids.
   int mx_nu0 = 2, mx_nuc = 2;
   float mx_alpha = 1.8f;  // mixed form: coarse-correction scale on aggregation hierarchies
+  // Mixed form: tile shape of the staged level-0 half sweeps (cfdg_grid_set_sweep_tile):
+  // rows per shared-memory stage (8, 16, 32) and stages in flight per block (2..8).
+  int mx_sweep_rows = 32, mx_sweep_stages = 2;
   // Laminar time stepping (cfdg_grid_set_flow / cfdg_step_device): the case flow and the
   // stage buffers (cell velocities, the two stage velocities, the stage pressure).
   bool has_flow = false;

@@ -30,7 +30,7 @@ EXPORTS = (
     "cfdg_batch_destroy", "cfdg_batch_set_stream", "cfdg_batch_size", "cfdg_batch_project", "cfdg_batch_project_device",
     "cfdg_batch_time_kernel", "cfdg_batch_stats_json", "cfdg_server_create", "cfdg_server_destroy", "cfdg_server_set_stream",
     "cfdg_server_submit", "cfdg_server_progress", "cfdg_server_result", "cfdg_server_pending", "cfdg_server_stats_json", "cfdg_server_set_chunk", "cfdg_grid_set_cycle", "cfdg_grid_set_coarse_scale", "cfdg_grid_set_flow", "cfdg_step_device", "cfdg_scalar_step_device", "cfdg_receptors_set", "cfdg_receptors_sample", "cfdg_debug_momentum_update",
-    "cfdg_debug_wave_stall",
+    "cfdg_debug_wave_stall", "cfdg_grid_set_sweep_tile",
 )
 
 
@@ -172,6 +172,7 @@ def load(path: str = LIB_PATH):
                                                 C.POINTER(Info), C.POINTER(C.c_int32)]
         L.cfdg_debug_time_kernel.argtypes = [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.cfdg_debug_wave_stall.argtypes = [P, C.c_int32, C.c_int64]
+        L.cfdg_grid_set_sweep_tile.argtypes = [P, C.c_int32, C.c_int32]
         _lib = L
         return L
 

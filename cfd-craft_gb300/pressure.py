@@ -238,6 +238,11 @@ class DeviceGrid:
         """Mixed form: V-cycle sweeps on level 0 and on the coarse levels (cfdg_grid_set_cycle)."""
         self._check(self.L.cfdg_grid_set_cycle(self.h, int(nu_fine), int(nu_coarse)))
 
+    def set_sweep_tile(self, rows: int, stages: int):
+        """Mixed form: rows per shared-memory stage (8, 16, 32) and stages in flight of the
+        staged level-0 half sweeps (cfdg_grid_set_sweep_tile); results do not change."""
+        self._check(self.L.cfdg_grid_set_sweep_tile(self.h, int(rows), int(stages)))
+
     def set_coarse_scale(self, alpha: float):
         """Mixed form: scale of the coarse corrections on aggregation hierarchies
         (cfdg_grid_set_coarse_scale; default 1.8, 1 is the reference's cycle)."""
@@ -526,6 +531,48 @@ class Server:
 # Candidate (level-0 sweeps, coarse-level sweeps) pairs of the mixed form's V-cycle.
 # (sweeps on level 0, sweeps on the coarse levels, coarse-correction scale)
 CYCLE_CANDIDATES = ((1, 2, 1.85), (2, 1, 1.85), (2, 2, 1.7), (2, 2, 1.85), (2, 3, 1.85), (3, 2, 1.85))
+# Tile shapes of the staged level-0 half sweeps: (rows per shared-memory stage, stages in flight).
+SWEEP_TILE_CANDIDATES = ((8, 4), (16, 2), (16, 3), (16, 4), (32, 2), (32, 3))
+
+
+def autotune_sweep_tile(device_grids, u_ptrs, p_ptrs, reset, dts, tol=1e-8, max_iter=10000,
+                        candidates=SWEEP_TILE_CANDIDATES, stream_handle=None, reps=20):
+    """Picks the tile shape of the staged level-0 half sweeps (cfdg_grid_set_sweep_tile) with
+    the shortest kernel time on these grids and applies it. Taller stages halve the y-halo
+    rows per stage and the copies per byte; more stages keep more bytes in flight but hold
+    more shared memory, so fewer blocks fit an SM. The best shape depends on the row lengths
+    of the mix, which is why it is measured: for each candidate a batch of all grids
+    projects once (the inputs restored by `reset()`), then one half sweep over every case is
+    timed `reps` times with CUDA events. Results do not depend on the shape, bit for bit.
+    Returns {"choice": [rows, stages], "us": {...}}, or None when the mix does not take the
+    staged path (non-uniform weights, or ceil(nx/2) not a multiple of 8)."""
+    probe = Batch(device_grids)
+    try:
+        if not probe.stats()["staged_sweeps"]:
+            return None
+    finally:
+        probe.close()
+    timing = {}
+    for cand in candidates:
+        for d in device_grids:
+            d.set_sweep_tile(*cand)
+        b = Batch(device_grids)
+        if stream_handle:
+            b.set_stream(stream_handle)
+        try:
+            reset()
+            if any(code != 0 for code, _ in b.project_device(u_ptrs, p_ptrs, dts, tol, max_iter)):
+                continue
+            timing[cand] = b.time_kernel(0, reps)[0]
+        finally:
+            b.close()
+    if not timing:
+        return None
+    choice = min(timing, key=timing.get)
+    for d in device_grids:
+        d.set_sweep_tile(*choice)
+    reset()
+    return {"choice": list(choice), "us": {f"{r}x{n}": round(1e3 * t, 2) for (r, n), t in timing.items()}}
 
 
 def autotune(device_grids, u_ptrs, p_ptrs, reset, dts, tol=1e-8, max_iter=10000, candidates=CYCLE_CANDIDATES,
@@ -539,9 +586,12 @@ def autotune(device_grids, u_ptrs, p_ptrs, reset, dts, tol=1e-8, max_iter=10000,
     restores the inputs before every call. More sweeps make a cycle dearer and the
     iteration count smaller; the optimum depends on the case mix (stencil anisotropy,
     buildings, the share of wide-stencil coarse levels), which is why it is measured.
-    Returns {"choice": [nu_fine, nu_coarse(, scale)], "ms": {...}, "iterations": {...}}."""
+    The tile shape of the staged half sweeps is picked first (autotune_sweep_tile).
+    Returns {"choice": [nu_fine, nu_coarse(, scale)], "ms": {...}, "iterations": {...},
+    "sweep_tile": {...} | None}."""
     import time
 
+    tile = autotune_sweep_tile(device_grids, u_ptrs, p_ptrs, reset, dts, tol, max_iter, stream_handle=stream_handle)
     timing, iters = {}, {}
     def apply(cand):
         for d in device_grids:
@@ -581,4 +631,4 @@ def autotune(device_grids, u_ptrs, p_ptrs, reset, dts, tol=1e-8, max_iter=10000,
         return ",".join(str(v) for v in c)
 
     return {"choice": list(choice), "ms": {key(c): round(1e3 * t, 2) for c, t in timing.items()},
-            "iterations": {key(c): round(v, 2) for c, v in iters.items()}}
+            "iterations": {key(c): round(v, 2) for c, v in iters.items()}, "sweep_tile": tile}

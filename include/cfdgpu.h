@@ -192,6 +192,14 @@ int cfdg_debug_momentum_update(cfdg_grid *grid, const double *u, const double *p
  * grids of one batch must agree), so a grid gives the same result alone and in a batch.
  * The bench's autotuner picks them per case mix. No reference counterpart. */
 int cfdg_grid_set_cycle(cfdg_grid *grid, int32_t nu_fine, int32_t nu_coarse);
+/* Mixed form: tile shape of the level-0 red-black half sweeps, which the tensor memory
+ * accelerator stages through shared memory on grids with uniform weights and ceil(nx/2) a
+ * multiple of 8: rows per stage (8, 16 or 32; the y halo is two rows per stage) and stages
+ * in flight per block (2..8; fewer when they do not fit the shared memory). Default 32 and 2.
+ * Batches and servers created afterwards take it from their grids (all grids of one batch
+ * must agree); the results do not depend on it, bit for bit. The bench's autotuner picks it
+ * per case mix. No reference counterpart. */
+int cfdg_grid_set_sweep_tile(cfdg_grid *grid, int32_t rows, int32_t stages);
 /* Mixed form on aggregation (masked) hierarchies: the coarse corrections of the V-cycle are
  * scaled by alpha, 0 < alpha < 2 (default 1.8; 1 is the reference's cycle). The piecewise-
  * constant prolongation under-corrects smooth errors; on the 52-case wind-direction mix
@@ -262,12 +270,14 @@ int cfdg_batch_project(cfdg_batch *batch, double *const *u, double *const *p, co
 /* Times one unit of the batch's work `reps` times with CUDA events on the batch's
  * stream, every case in its inner-iteration state: which = 0 one red-black half sweep
  * over all fine levels, 1 the FP32 operator, 2 all coarse levels (one cooperative launch), 3 one
- * V-cycle. Reports the mean duration and the unit's algorithmic bytes (0 when not
+ * V-cycle, 4 the half sweep of 0 with the unstaged register kernel. Reports the mean duration and the unit's algorithmic bytes (0 when not
  * stated). Diagnostic; no reference counterpart. */
 int cfdg_batch_time_kernel(cfdg_batch *batch, int32_t which, int32_t reps, double *ms_per_launch,
                            double *algorithmic_bytes);
 /* Per case and coarse level of the batch's FP32 hierarchies, as JSON: rows, nonzeros,
- * smoother colours, ELL entries (with padding), closed groups and terminal blocks. Writes
+ * smoother colours, ELL entries (with padding), closed groups and terminal blocks; and
+ * whether the level-0 half sweeps run staged through the tensor memory accelerator
+ * ("staged_sweeps": every case with uniform weights and ceil(nx/2) a multiple of 8). Writes
  * at most cap bytes (NUL-terminated) and returns the length the full text needs, or a
  * negative error code. Diagnostic; no reference counterpart. */
 int64_t cfdg_batch_stats_json(cfdg_batch *batch, char *buf, int64_t cap);

@@ -201,3 +201,42 @@ def test_coarse_scale_keeps_accuracy_and_cuts_iterations(pkg, O):
         with pytest.raises(pkg.pressure.PressureError):
             dg.set_coarse_scale(bad)
     dg.close()
+
+
+def test_staged_half_sweeps_equal_register_sweeps(pkg):
+    """The level-0 half sweeps staged through the tensor memory accelerator (k_rb_tma) give
+    the same bits as the register kernel (k_rb): cases whose weights are uniform and whose
+    ceil(nx/2) is a multiple of 8 run staged in a batch of their own, and the register
+    kernel in a batch with a case that is not (37 x 29 x 21)."""
+    rng = np.random.default_rng(5)
+    specs = [((64, 64, 32), 6), ((48, 48, 48), 4), ((16, 10, 8), 1), ((96, 96, 48), 9)]
+    cases = [pkg.synth.case(n, 2.0, inflow=5.0, preconditioner="multigrid",
+                            boxes=pkg.synth.random_boxes(rng, nb, [2.0 * v for v in n], side=(6.0, 20.0), dx=2.0))
+             for n, nb in specs]
+    odd = mixed_cases(pkg)["odd-37x29x21"]
+    grids = [pkg.grid.Grid.build(c) for c in cases + [odd]]
+    us = [pkg.synth.random_velocity(g, 40 + i) for i, g in enumerate(grids)]
+    ps = [np.zeros(g.count) for g in grids]
+    results = {}
+    for name, idx in (("staged", [0, 1, 2, 3]), ("register", [0, 1, 2, 3, 4])):
+        dgs = [pkg.pressure.DeviceGrid(grids[i], preconditioner="multigrid", precision="mixed") for i in idx]
+        batch = pkg.pressure.Batch(dgs)
+        assert batch.stats()["staged_sweeps"] is (name == "staged")
+        bu = [us[i].copy() for i in idx]
+        bp = [ps[i].copy() for i in idx]
+        res = batch.project(bu, bp, [0.1] * len(idx), 1e-8, 10000)
+        assert all(code == 0 for code, _ in res)
+        if name == "staged":
+            ms_staged, b1 = batch.time_kernel(0, 5)
+            ms_reg, b2 = batch.time_kernel(4, 5)
+            assert b1 == b2 > 0 and ms_staged > 0 and ms_reg > 0
+            print(f"half sweep over {sum(g.count for g in grids[:4])} cells: staged {ms_staged:.4f} ms, "
+                  f"register {ms_reg:.4f} ms")
+        results[name] = (bu, bp, [info.iterations for _, info in res])
+        batch.close()
+        for d in dgs:
+            d.close()
+    for k in range(4):
+        assert results["staged"][2][k] == results["register"][2][k]
+        assert np.array_equal(bits(results["staged"][0][k]), bits(results["register"][0][k])), k
+        assert np.array_equal(bits(results["staged"][1][k]), bits(results["register"][1][k])), k
