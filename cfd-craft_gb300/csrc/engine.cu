@@ -618,6 +618,19 @@ struct PLev {
 
 namespace cg = cooperative_groups;
 
+// The barrier between the phases of the coarse-level kernel: the whole grid of a cooperative
+// launch, or the one thread-block cluster the launch consists of (gridDim.x = cluster size,
+// so blockIdx.x is the block's rank in the cluster). Clusters are scheduled as a unit, so
+// launches on several streams at once never wait on blocks that are not resident.
+struct GridBarrier {
+  cg::grid_group g;
+  __device__ void sync() { g.sync(); }
+};
+struct ClusterBarrier {
+  __device__ void sync() { cg::this_cluster().sync(); }
+};
+constexpr int PC_CLUSTER = 8;  // blocks of the plain coarse-level cluster (portable size)
+
 // The banded forward and backward substitutions of one block (multigrid/line.rs:172-185)
 // for a half-bandwidth BW: the last BW results stay in registers and the factor entries of
 // a row are independent of the chain, so only the multiply-subtract chain is serial. The
@@ -704,7 +717,8 @@ __device__ __forceinline__ void line_block(int b, const PLev& L, const double* r
   __syncwarp();  // the row is reused by the warp's next block
 }
 
-__device__ void pc_center(const PLev& L, double* v, double* sh, double* mean, cg::grid_group& grid) {
+template <class Bar>
+__device__ void pc_center(const PLev& L, double* v, double* sh, double* mean, Bar& grid) {
   if (L.ngroups == 0) return;
   for (int g = blockIdx.x; g < L.ngroups; g += gridDim.x) center_group(g, L.goff, L.gmem, v, sh, mean);
   __threadfence();
@@ -713,7 +727,8 @@ __device__ void pc_center(const PLev& L, double* v, double* sh, double* mean, cg
 
 // A block Gauss-Seidel sweep over the block dependency levels (blocks of one level share
 // no entry, so they run in parallel; the reference's block order is kept where it matters).
-__device__ void pc_lines(const PLev& L, bool backward, cg::grid_group& grid, double* lsh) {
+template <class Bar>
+__device__ void pc_lines(const PLev& L, bool backward, Bar& grid, double* lsh) {
   const int* order = backward ? L.lbo : L.lfo;
   const int* start = backward ? L.lbs : L.lfs;
   const int nlev = backward ? L.lnbwd : L.lnfwd;
@@ -738,7 +753,8 @@ __device__ void pc_lines(const PLev& L, bool backward, cg::grid_group& grid, dou
   }
 }
 
-__device__ void pc_sweep(const PLev& L, bool backward, cg::grid_group& grid, double* lsh) {
+template <class Bar>
+__device__ void pc_sweep(const PLev& L, bool backward, Bar& grid, double* lsh) {
   if (L.lines) {
     pc_lines(L, backward, grid, lsh);
     return;
@@ -766,12 +782,12 @@ __device__ void pc_sweep(const PLev& L, bool backward, cg::grid_group& grid, dou
   }
 }
 
-__global__ void __launch_bounds__(BLOCK) k_plain_coarse(const PLev* lv, int nl, const Scalars* S) {
+template <class Bar>
+__device__ void plain_coarse(const PLev* lv, int nl, const Scalars* S, Bar& grid) {
   if (S && S->done) return;  // read once; nothing in this kernel changes it
   __shared__ double sh[32];
   __shared__ double mean;
   __shared__ double lsh[(BLOCK / 32) * LSCR];  // one scratch row per warp (block smoothers)
-  cg::grid_group grid = cg::this_grid();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
   int l = 0;
   for (; l < nl; ++l) {
@@ -807,6 +823,15 @@ __global__ void __launch_bounds__(BLOCK) k_plain_coarse(const PLev* lv, int nl, 
     for (int sw = 0; sw < L.nsweep; ++sw) pc_sweep(L, true, grid, lsh);
     pc_center(L, L.x, sh, &mean, grid);
   }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_plain_coarse(const PLev* lv, int nl, const Scalars* S) {
+  GridBarrier bar{cg::this_grid()};
+  plain_coarse(lv, nl, S, bar);
+}
+__global__ void __launch_bounds__(BLOCK) k_plain_coarse_cluster(const PLev* lv, int nl, const Scalars* S) {
+  ClusterBarrier bar;
+  plain_coarse(lv, nl, S, bar);
 }
 
 __global__ void k_gather(int n, const int* __restrict__ idx, const double* __restrict__ src, double* __restrict__ dst,
@@ -1006,7 +1031,7 @@ void launch_vcycle(cfdg_grid* G, const double* r, double* z, const Scalars* S) {
   }
   const int nl = (int)H.levels.size();
   // Levels 1 .. L-1 in one cooperative launch when available, else level by level.
-  const bool coop = H.coop_blocks > 0 && nl > 1;
+  const bool coop = (H.coop_blocks > 0 || H.cluster) && nl > 1;
   const int first = H.coop0 ? 0 : 1;  // the first level of the cooperative launch
   for (int l = 0; l < (coop ? first : nl); ++l) {
     DevLevel& L = H.levels[l];
@@ -1036,16 +1061,29 @@ void launch_vcycle(cfdg_grid* G, const double* r, double* z, const Scalars* S) {
                                                   C.rhs, S); tick(G);
   }
   if (coop) {
+    // One cluster of PC_CLUSTER blocks (cluster barriers, about 0.3 us a phase), or the
+    // cooperative grid where clusters cannot be launched.
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)H.coop_blocks, 1, 1);
     cfg.blockDim = dim3(BLOCK, 1, 1);
     cfg.stream = s;
     cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeCooperative;
-    at[0].val.cooperative = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, k_plain_coarse, (const PLev*)H.d_plev, nl - first, S);
+    if (H.cluster) {
+      cfg.gridDim = dim3(PC_CLUSTER, 1, 1);
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = PC_CLUSTER;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      cudaLaunchKernelEx(&cfg, k_plain_coarse_cluster, (const PLev*)H.d_plev, nl - first, S);
+    } else {
+      cfg.gridDim = dim3((unsigned)H.coop_blocks, 1, 1);
+      at[0].id = cudaLaunchAttributeCooperative;
+      at[0].val.cooperative = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      cudaLaunchKernelEx(&cfg, k_plain_coarse, (const PLev*)H.d_plev, nl - first, S);
+    }
     tick(G);
   }
   for (int l = coop ? first - 1 : nl - 2; l >= 0; --l) {
@@ -1392,7 +1430,26 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
       per = 0;
     }
     D->coop_blocks = per > 0 ? sms : 0;
-    if (D->coop0 && D->coop_blocks == 0)
+    // A cluster of PC_CLUSTER blocks, when one fits an SM group.
+    {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(PC_CLUSTER, 1, 1);
+      cfg.blockDim = dim3(BLOCK, 1, 1);
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = PC_CLUSTER;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int clusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&clusters, k_plain_coarse_cluster, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        clusters = 0;
+      }
+      D->cluster = clusters > 0;
+    }
+    if (D->coop0 && D->coop_blocks == 0 && !D->cluster)
       return fail(CFDG_ERR_UNSUPPORTED, "block-smoothed multigrid needs a co-resident cooperative launch");
   }
   CU(cudaStreamSynchronize(s));

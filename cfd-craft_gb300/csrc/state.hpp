@@ -145,6 +145,7 @@ struct DevHierarchy {
   // (0: not co-resident, the level-by-level launches are used instead).
   void* d_plev = nullptr;
   int coop_blocks = 0;
+  bool cluster = false;  // the coarse kernel runs as one thread-block cluster (engine.cu)
   // Block-smoothed (anisotropic) hierarchies: d_plev starts at level 0 and the whole cycle
   // is the cooperative launch.
   bool coop0 = false;

@@ -396,3 +396,65 @@ def test_continuum_poisson_second_order_on_gpu(pkg):
         dg.close()
         errors.append(math.sqrt(float(np.sum((p - exact) ** 2))) / math.sqrt(g.count))
     assert math.log2(errors[1] / errors[2]) > 1.9 and math.log2(errors[0] / errors[1]) > 1.9, errors
+
+
+def test_concurrent_plain_projections_equal_alone(pkg, O):
+    """Plain FP64 projections of several grids from several host threads at once, each on
+    its own CUDA stream (the coarse levels run as one thread-block cluster per grid, the
+    fine sweeps as wavefront kernels whose blocks wait only for tiles already running),
+    give the same bits as the same projections one after another."""
+    import threading
+
+    import torch
+
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(8)
+    cases = [pkg.synth.case((40, 32, 24), 2.0, inflow=5.0, preconditioner="multigrid",
+                            boxes=pkg.synth.random_boxes(rng, 3, (80.0, 64.0, 48.0), side=(6.0, 20.0), dx=2.0)),
+             pkg.synth.case((32, 32, 16), 1.0, preconditioner="multigrid"),
+             pkg.synth.case((24, 20, 12), 2.0, preconditioner="ic0", boxes=[((10, 6, 0), (20, 14, 10))]),
+             anisotropic_case("thin100", "multigrid")]
+    grids = [pkg.grid.Grid.build(c) for c in cases]
+    pres = ["multigrid", "multigrid", "ic0", "multigrid"]
+    us = [pkg.synth.random_velocity(g, 60 + i) for i, g in enumerate(grids[:3])]
+    exact, _ = rough_rhs(O.Grid(cases[3]))
+    us.append(grids[3].gradient(exact))  # a compatible field on the closed anisotropic box
+    seq = []
+    for g, u, pre in zip(grids, us, pres):
+        dg = pkg.pressure.DeviceGrid(g, preconditioner=pre)
+        uu, pp = u.copy(), np.zeros(g.count)
+        info = dg.project(uu, pp, 0.5, 1e-10, 2000)
+        seq.append((uu, pp, info.iterations))
+        dg.close()
+    dgs, streams, d_u, d_p = [], [], [], []
+    for g, u, pre in zip(grids, us, pres):
+        dg = pkg.pressure.DeviceGrid(g, preconditioner=pre)
+        st = torch.cuda.Stream(dev)
+        dg.set_stream(st.cuda_stream)
+        dgs.append(dg)
+        streams.append(st)
+        d_u.append(torch.from_numpy(u.copy()).to(dev))
+        d_p.append(torch.zeros(g.count, dtype=torch.float64, device=dev))
+    torch.cuda.synchronize()
+    out = [None] * len(grids)
+
+    def run(i):
+        out[i] = dgs[i].project_device(d_u[i].data_ptr(), d_p[i].data_ptr(), 0.5, 1e-10, 2000)
+
+    for rep in range(2):
+        for i in range(len(grids)):
+            d_u[i].copy_(torch.from_numpy(us[i]))
+            d_p[i].zero_()
+        torch.cuda.synchronize()
+        ths = [threading.Thread(target=run, args=(i,)) for i in range(len(grids))]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        torch.cuda.synchronize()
+        for i in range(len(grids)):
+            assert out[i].iterations == seq[i][2], (i, rep)
+            assert np.array_equal(bits(d_u[i].cpu().numpy()), bits(seq[i][0])), (i, rep)
+            assert np.array_equal(bits(d_p[i].cpu().numpy()), bits(seq[i][1])), (i, rep)
+    for dg in dgs:
+        dg.close()
