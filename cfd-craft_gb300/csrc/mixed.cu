@@ -122,7 +122,11 @@ struct CLev {
   int n, terminal, ncolors, ngroups;
   // Smoother: 0 multicolour Gauss-Seidel, 1 l1-Jacobi (levels whose graph needs many
   // colours: the wide Galerkin stencils of linear-interpolation hierarchies).
-  int jacobi, pad_;
+  // res0: a two-colour Gauss-Seidel level without closed groups. The residual is taken on
+  // colour 0 only: after the last (colour-1) half sweep before it, colour 1's residual is
+  // zero up to rounding, so those rows keep res = 0 (the cycle is unchanged in exact
+  // arithmetic and stays symmetric).
+  int jacobi, res0;
   const float* il1;  // l1-Jacobi: 1 / (diag + sum |a_ij|), 0 where diag is 0
   float* x2;         // l1-Jacobi: the second iterate of a sweep pair
   const int *off, *col;
@@ -1219,6 +1223,81 @@ __global__ void k_center0(const FineCase* FC, MState* ST, const int2* gtab, cons
   }
 }
 
+// Gauss-Seidel rows of one colour, RPI consecutive rows of the colour block per work item:
+// every row's entries are loaded before any row is stored (rows of one colour never read
+// each other), entries are summed in ELL order as every other path does. skipx: the first
+// colour of the cycle's first sweep, whose neighbours are all zero, takes x = rhs / diag
+// (the same bits as summing the zero products).
+constexpr int RPI = 4;
+__device__ __forceinline__ void gs_rows(const CLev& L, int color, int k, bool skipx) {
+  const int c0 = L.coff[color];
+  const int nrow = L.coff[color + 1] - c0;
+  const int q = RPI * k;
+  if (q >= nrow) return;
+  float v[RPI], d[RPI];
+#pragma unroll
+  for (int r = 0; r < RPI; ++r) {
+    const bool ok = q + r < nrow;
+    v[r] = ok ? __ldcg(&L.rhs[c0 + q + r]) : 0.0f;
+    d[r] = ok ? L.idiag[c0 + q + r] : 0.0f;
+  }
+  if (!skipx) {
+    const int base = L.ell_off[color], w = L.ell_w[color];
+    const int* ec = L.ell_col + base + q;
+    const float* ev = L.ell_val + base + q;
+#pragma unroll 1
+    for (int a = 0; a < w; ++a) {
+      int col[RPI];
+      float wv[RPI], xv[RPI];
+#pragma unroll
+      for (int r = 0; r < RPI; ++r) {
+        const bool ok = q + r < nrow;
+        col[r] = ok ? ec[a * nrow + r] : c0 + q;
+        wv[r] = ok ? ev[a * nrow + r] : 0.0f;
+      }
+#pragma unroll
+      for (int r = 0; r < RPI; ++r) xv[r] = __ldcg(&L.x[col[r]]);
+#pragma unroll
+      for (int r = 0; r < RPI; ++r) v[r] = fmaf(-wv[r], xv[r], v[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < RPI; ++r)
+    if (q + r < nrow) L.x[c0 + q + r] = v[r] * d[r];
+}
+
+// The residual of a res0 level on colour 0, RPI rows per item through the colour's ELL
+// block: res = rhs - (diag x + sum a x) with the entries in ELL order.
+__device__ __forceinline__ void res0_rows(const CLev& L, int k) {
+  const int nrow = L.coff[1];  // colour 0 owns rows 0 .. coff[1]-1
+  const int q = RPI * k;
+  if (q >= nrow) return;
+  float v[RPI];
+#pragma unroll
+  for (int r = 0; r < RPI; ++r) v[r] = q + r < nrow ? L.diag[q + r] * __ldcg(&L.x[q + r]) : 0.0f;
+  const int base = L.ell_off[0], w = L.ell_w[0];
+  const int* ec = L.ell_col + base + q;
+  const float* ev = L.ell_val + base + q;
+#pragma unroll 2
+  for (int a = 0; a < w; ++a) {
+    int col[RPI];
+    float wv[RPI], xv[RPI];
+#pragma unroll
+    for (int r = 0; r < RPI; ++r) {
+      const bool ok = q + r < nrow;
+      col[r] = ok ? ec[a * nrow + r] : q;
+      wv[r] = ok ? ev[a * nrow + r] : 0.0f;
+    }
+#pragma unroll
+    for (int r = 0; r < RPI; ++r) xv[r] = __ldcg(&L.x[col[r]]);
+#pragma unroll
+    for (int r = 0; r < RPI; ++r) v[r] = fmaf(wv[r], xv[r], v[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < RPI; ++r)
+    if (q + r < nrow) L.res[q + r] = __ldcg(&L.rhs[q + r]) - v[r];
+}
+
 // ----------------------------------------------------------------- coarse levels, one cluster per case
 __device__ __forceinline__ void csync() { cg::this_cluster().sync(); }
 
@@ -1323,10 +1402,14 @@ __global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState*
     }
     for (int sw = 0; sw < nu + (nu & 1); ++sw) c_sweep(L, false, sw & 1, sw < nu);
     c_center(L, L.x, C.gpart, sh);
-    for (int i = tid; i < L.n; i += nth) {
-      float v = L.diag[i] * __ldcg(&L.x[i]);
-      for (int a = L.off[i]; a < L.off[i + 1]; ++a) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
-      L.res[i] = __ldcg(&L.rhs[i]) - v;
+    if (L.res0) {
+      for (int k = tid; k < (L.coff[1] + RPI - 1) / RPI; k += nth) res0_rows(L, k);
+    } else {
+      for (int i = tid; i < L.n; i += nth) {
+        float v = L.diag[i] * __ldcg(&L.x[i]);
+        for (int a = L.off[i]; a < L.off[i + 1]; ++a) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
+        L.res[i] = __ldcg(&L.rhs[i]) - v;
+      }
     }
     __threadfence();
     csync();
@@ -1449,7 +1532,7 @@ __device__ void g_center(const CLev* sl, const MState* ST, const CoarseTab& T, i
 }
 
 __device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, int l, bool backward, int pass,
-                        bool gs_on, cg::grid_group& grid) {
+                        bool gs_on, bool first, cg::grid_group& grid) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
   for (int cc = 0; cc < T.maxc[l]; ++cc) {
     const int* off = (backward ? T.bwd : T.fwd) + (l * MAXC + cc) * (T.nc + 1);
@@ -1485,43 +1568,7 @@ __device__ void g_sweep(const CLev* sl, const MState* ST, const CoarseTab& T, in
         }
         continue;
       }
-      // Two consecutive rows of the colour block per item: both rows' loads are in flight
-      // before either is stored (rows of one colour never read each other). Each row sums
-      // its entries in ELL order, as every other path does.
-      const int color = backward ? L.ncolors - 1 - cc : cc;
-      const int c0 = L.coff[color];
-      const int nrow = L.coff[color + 1] - c0;
-      const int q = 2 * k;
-      if (q >= nrow) continue;  // ranges are rounded up to multiples of eight
-      const bool two = q + 1 < nrow;
-      const int i = c0 + q;  // colour blocks are contiguous
-      const int base = L.ell_off[color], w = L.ell_w[color];
-      float v0 = __ldcg(&L.rhs[i]);
-      float v1 = two ? __ldcg(&L.rhs[i + 1]) : 0.0f;
-      const float d0 = L.idiag[i], d1 = two ? L.idiag[i + 1] : 0.0f;
-      const int* ec = L.ell_col + base + q;
-      const float* ev = L.ell_val + base + q;
-      int a = 0;
-      for (; a + 2 <= w; a += 2) {
-        const int ca0 = ec[a * nrow], ca1 = ec[(a + 1) * nrow];
-        const int cb0 = two ? ec[a * nrow + 1] : ca0, cb1 = two ? ec[(a + 1) * nrow + 1] : ca1;
-        const float wa0 = ev[a * nrow], wa1 = ev[(a + 1) * nrow];
-        const float wb0 = two ? ev[a * nrow + 1] : 0.0f, wb1 = two ? ev[(a + 1) * nrow + 1] : 0.0f;
-        const float xa0 = __ldcg(&L.x[ca0]), xa1 = __ldcg(&L.x[ca1]);
-        const float xb0 = __ldcg(&L.x[cb0]), xb1 = __ldcg(&L.x[cb1]);
-        v0 = fmaf(-wa0, xa0, v0);
-        v0 = fmaf(-wa1, xa1, v0);
-        v1 = fmaf(-wb0, xb0, v1);
-        v1 = fmaf(-wb1, xb1, v1);
-      }
-      if (a < w) {
-        const int ca = ec[a * nrow], cb = two ? ec[a * nrow + 1] : ca;
-        const float wa = ev[a * nrow], wb = two ? ev[a * nrow + 1] : 0.0f;
-        v0 = fmaf(-wa, __ldcg(&L.x[ca]), v0);
-        v1 = fmaf(-wb, __ldcg(&L.x[cb]), v1);
-      }
-      L.x[i] = v0 * d0;
-      if (two) L.x[i + 1] = v1 * d1;
+      gs_rows(L, backward ? L.ncolors - 1 - cc : cc, k, first && !backward && cc == 0);
     }
     grid.sync();
   }
@@ -1546,7 +1593,7 @@ __device__ void blk_center(const CLev& L, float* v, double* sh) {
   }
 }
 
-__device__ void blk_sweep(const CLev& L, bool backward, int pass, bool gs_on) {
+__device__ void blk_sweep(const CLev& L, bool backward, int pass, bool gs_on, bool first) {
   if (L.jacobi) {
     const float* xin = pass ? L.x2 : L.x;
     float* xout = pass ? L.x : L.x2;
@@ -1571,28 +1618,8 @@ __device__ void blk_sweep(const CLev& L, bool backward, int pass, bool gs_on) {
   if (!gs_on) return;
   for (int cc = 0; cc < L.ncolors; ++cc) {
     const int color = backward ? L.ncolors - 1 - cc : cc;
-    const int c0 = L.coff[color], nrow = L.coff[color + 1] - c0;
-    const int base = L.ell_off[color], w = L.ell_w[color];
-    for (int k = threadIdx.x; k < nrow; k += blockDim.x) {
-      const int i = c0 + k;
-      float v = __ldcg(&L.rhs[i]);
-      const int* ec = L.ell_col + base + k;
-      const float* ev = L.ell_val + base + k;
-      int a = 0;
-      for (; a + 4 <= w; a += 4) {
-        const int c_0 = ec[(a + 0) * nrow], c_1 = ec[(a + 1) * nrow], c_2 = ec[(a + 2) * nrow],
-                  c_3 = ec[(a + 3) * nrow];
-        const float v0 = ev[(a + 0) * nrow], v1 = ev[(a + 1) * nrow], v2 = ev[(a + 2) * nrow],
-                    v3 = ev[(a + 3) * nrow];
-        const float x0 = __ldcg(&L.x[c_0]), x1 = __ldcg(&L.x[c_1]), x2 = __ldcg(&L.x[c_2]), x3 = __ldcg(&L.x[c_3]);
-        v = fmaf(-v0, x0, v);
-        v = fmaf(-v1, x1, v);
-        v = fmaf(-v2, x2, v);
-        v = fmaf(-v3, x3, v);
-      }
-      for (; a < w; ++a) v = fmaf(-ev[a * nrow], __ldcg(&L.x[ec[a * nrow]]), v);
-      L.x[i] = v * L.idiag[i];
-    }
+    const int items = (L.coff[color + 1] - L.coff[color] + RPI - 1) / RPI;
+    for (int k = threadIdx.x; k < items; k += blockDim.x) gs_rows(L, color, k, first && !backward && cc == 0);
     __syncthreads();
   }
 }
@@ -1633,10 +1660,13 @@ __device__ void blk_cycle(const CCase& C, int l0, int nu, double* sh) {
       blk_center(L, L.x, sh);
       break;
     }
-    for (int sw = 0; sw < nu + (nu & 1); ++sw) blk_sweep(L, false, sw & 1, sw < nu);
+    for (int sw = 0; sw < nu + (nu & 1); ++sw) blk_sweep(L, false, sw & 1, sw < nu, sw == 0);
     blk_center(L, L.x, sh);
-    for (int k = threadIdx.x; k < (L.jacobi ? 8 : 1) * L.n; k += blockDim.x) {
-      if (L.jacobi) {
+    const int nres = L.res0 ? (L.coff[1] + RPI - 1) / RPI : (L.jacobi ? 8 : 1) * L.n;
+    for (int k = threadIdx.x; k < nres; k += blockDim.x) {
+      if (L.res0) {
+        res0_rows(L, k);
+      } else if (L.jacobi) {
         const int i = k >> 3, sub = k & 7;
         float v = 0.0f;
         for (int a = L.off[i] + sub; a < L.off[i + 1]; a += 8) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
@@ -1671,7 +1701,7 @@ __device__ void blk_cycle(const CCase& C, int l0, int nu, double* sh) {
       L.x[i] = __ldcg(&L.x[i]) + s;
     }
     __syncthreads();
-    for (int sw = 0; sw < nu + (nu & 1); ++sw) blk_sweep(L, true, sw & 1, sw < nu);
+    for (int sw = 0; sw < nu + (nu & 1); ++sw) blk_sweep(L, true, sw & 1, sw < nu, false);
     blk_center(L, L.x, sh);
   }
 }
@@ -1711,7 +1741,7 @@ __global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const
       }
       grid.sync();
     }
-    for (int sw = 0; sw < T.nu + (T.nu & 1); ++sw) g_sweep(sl, ST, T, l, false, sw & 1, sw < T.nu, grid);
+    for (int sw = 0; sw < T.nu + (T.nu & 1); ++sw) g_sweep(sl, ST, T, l, false, sw & 1, sw < T.nu, sw == 0, grid);
     if (T.anyg[l]) g_center(sl, ST, T, l, 1, sh, grid);
     {
       const int* off = T.res + l * (nc + 1);
@@ -1724,6 +1754,10 @@ __global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const
         if (!on) continue;
         const CLev& L = sl[ci];
         const int k = t - cur.lo;
+        if (L.res0) {
+          res0_rows(L, k);
+          continue;
+        }
         if (L.jacobi) {  // eight lanes per (wide) row
           const int i = k >> 3, sub = k & 7;
           float v = 0.0f;
@@ -1790,7 +1824,7 @@ __global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const
       }
     }
     grid.sync();
-    for (int sw = 0; sw < T.nu + (T.nu & 1); ++sw) g_sweep(sl, ST, T, l, true, sw & 1, sw < T.nu, grid);
+    for (int sw = 0; sw < T.nu + (T.nu & 1); ++sw) g_sweep(sl, ST, T, l, true, sw & 1, sw < T.nu, false, grid);
     if (T.anyg[l]) g_center(sl, ST, T, l, 1, sh, grid);
   }
 }
@@ -2342,7 +2376,11 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     if (int e = A.alloc(&rhs, L.n)) return e;
     if (int e = A.alloc(&x, L.n)) return e;
     if (int e = A.alloc(&res, L.n)) return e;
+    CU(cudaMemsetAsync(rhs, 0, sizeof(float) * L.n, s));
+    CU(cudaMemsetAsync(x, 0, sizeof(float) * L.n, s));
+    CU(cudaMemsetAsync(res, 0, sizeof(float) * L.n, s));  // colour-1 rows of res0 levels stay zero
     L.rhs = rhs, L.x = x, L.res = res;
+    L.res0 = !L.terminal && !L.jacobi && L.ncolors == 2 && L.ngroups == 0 ? 1 : 0;
     if (L.terminal) {
       L.nblocks = M.direct_idx.rows();
       int *io, *ix;
@@ -2641,16 +2679,18 @@ int fill_tab(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
       next[l * w + i + 1] = next[l * w + i] + (nt ? B->cases[i]->C.lv[l + 1].n : 0);
       live[l * w + i + 1] = live[l * w + i] + (nt ? L->n : 0);
       grp[l * w + i + 1] = grp[l * w + i] + (L ? L->ngroups : 0);
-      res[l * w + i + 1] = res[l * w + i] + (nt ? r8(L->jacobi ? 8 * L->n : L->n) : 0);
+      const auto& cof = B->cases[i]->colors[l];
+      const int nres = !nt ? 0 : (L->res0 ? (cof[1] + RPI - 1) / RPI : (L->jacobi ? 8 * L->n : L->n));
+      res[l * w + i + 1] = res[l * w + i] + r8(nres);
       for (int c = 0; c < MAXC; ++c) {
         int nf = 0, nb = 0;
         if (nt && L->jacobi) {
           nf = nb = c == 0 ? 8 * L->n : 0;
-        } else if (nt && c < L->ncolors) {  // two rows per item
+        } else if (nt && c < L->ncolors) {  // RPI rows per item
           const auto& co = B->cases[i]->colors[l];
-          nf = r8((co[c + 1] - co[c] + 1) / 2);
+          nf = r8((co[c + 1] - co[c] + RPI - 1) / RPI);
           const int cb = L->ncolors - 1 - c;
-          nb = r8((co[cb + 1] - co[cb] + 1) / 2);
+          nb = r8((co[cb + 1] - co[cb] + RPI - 1) / RPI);
         }
         fwd[(l * MAXC + c) * w + i + 1] = fwd[(l * MAXC + c) * w + i] + nf;
         bwd[(l * MAXC + c) * w + i + 1] = bwd[(l * MAXC + c) * w + i] + nb;

@@ -113,11 +113,15 @@ def _vp(a):
 
 
 _open_grids = weakref.WeakSet()
+_open_groups = weakref.WeakSet()  # batches and servers: closed before their grids and context
 
 
 @atexit.register
 def _close_all():
-    # Release device state before the interpreter (and then the CUDA runtime) shut down.
+    # Release device state before the interpreter (and then the CUDA runtime) shut down:
+    # batches and servers first (they use their grids' state), then grids, then contexts.
+    for b in list(_open_groups):
+        b.close()
     for dg in list(_open_grids):
         dg.close()
     if Context._default is not None:
@@ -394,6 +398,7 @@ class Batch:
             raise PressureError(rc, E.last_error())
         self.h = h
         self.L = L
+        _open_groups.add(self)
 
     def close(self):
         if getattr(self, "h", None):
@@ -469,6 +474,7 @@ class Server:
             raise PressureError(rc, E.last_error())
         self.h = h
         self.L = L
+        _open_groups.add(self)
 
     def close(self):
         if getattr(self, "h", None):
