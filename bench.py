@@ -660,9 +660,21 @@ def plain_mix(pkg, torch, dev, sv, world, flush):
     alone = dgs[0].project_device(us[0].data_ptr(), ps[0].data_ptr(), DT, TOL, MAX_IT)
     b.record(streams[0])
     torch.cuda.synchronize()
+    # The plain form's kernels on the first 128x128x64 case: the FP64 operator with p.Ap,
+    # one lexicographic Gauss-Seidel sweep of the fine level (the pipelined wavefront) and
+    # one V-cycle (all levels), algorithmic bytes over CUDA-event time.
+    peak, _ = peaks()
+    kernels = {}
+    for name, which, reps in (("operator_fp64", 0, 20), ("gs_sweep_fine_fp64", 1, 10), ("vcycle_fp64", 3, 5)):
+        ms, by = dgs[0].time_kernel(which, reps)
+        gbs = by / ms / 1e6 if by else None
+        kernels[name] = {"ms": round(ms, 4), "GB/s": round(gbs, 1) if gbs else None, "algorithmic_bytes": by,
+                         "frac": round(gbs / peak, 4) if gbs else None}
     for d in dgs:
         d.close()
-    return {"value": round(world * n / wall, 4), "unit": UNIT, "wall_s": round(wall, 3),
+    return {"value": round(world * n / wall, 4), "unit": UNIT, "wall_s": round(wall, 3), "kernels": kernels,
+            "bound": "FP64 latency and rate: every product and sum rounded in the reference's order (no FMA), "
+                     "lexicographic sweeps with a correctly rounded division per cell",
             "iterations_mean": round(statistics.mean(its), 2), "iterations_max": max(its),
             "ms_per_solve_alone_128x128x64": round(a.elapsed_time(b), 2), "iterations_alone": alone.iterations,
             "sample": f"all {n} cases of the mix projected at once (first u* of each, after an untimed cold solve), "
@@ -719,6 +731,17 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
                    "throughput": round(args.requests / span, 2), "arrival_span_s": round(last_arrival, 3),
                    "p50_ms": round(1e3 * pct(plat, 0.50), 2), "p99_ms": round(1e3 * pct(plat, 0.99), 2),
                    "max_ms": round(1e3 * max(plat), 2), "slots": args.slots or n}
+        # Latency against load: open loops at fractions of the closed-loop capacity just
+        # measured, each about 1.5 s of arrivals.
+        serving["latency_vs_load"] = []
+        for q, frac in enumerate(float(f) for f in args.load_points.split(",") if f):
+            rate = frac * value / world
+            reqs = max(200, int(rate * 1.5))
+            pl, sp, la = sv.poisson(reqs, rate, seed=11 + q)
+            serving["latency_vs_load"].append(
+                {"fraction_of_capacity": frac, "offered_per_s": round(rate, 1), "requests": reqs,
+                 "throughput": round(reqs / sp, 1), "p50_ms": round(1e3 * pct(pl, 0.50), 2),
+                 "p99_ms": round(1e3 * pct(pl, 0.99), 2)})
     # End to end through the host-buffer batch call: every case of the mix per step, H2D + D2H inside.
     bt = pkg.pressure.Batch(sv.dgs)
     bt.set_stream(stream.cuda_stream)
@@ -763,6 +786,8 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
         kernels[name] = {"ms": round(ms, 4), "GB/s": round(b / ms / 1e6, 1) if b else None, "algorithmic_bytes": b}
     bt.close()
     peak, peak_kind = peaks()
+    for kv in kernels.values():
+        kv["frac"] = round(kv["GB/s"] / peak, 4) if kv["GB/s"] else None
     k = kernels["rb_half_sweep_fp32"]
     achieved = k["algorithmic_bytes"] / (k["ms"] * 1e-3) / 1e9
     # DRAM bytes per launch from the ncu capture of the same kernel on 4 x 128x128x64
@@ -1390,6 +1415,8 @@ def main():
     ap.add_argument("--slots", type=int, default=0, help="serving: cases on the GPU at once (0: all)")
     ap.add_argument("--requests", type=int, default=520, help="serving: open-loop requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")
+    ap.add_argument("--load-points", default="0.5,0.75,0.9",
+                    help="serving: open loops at these fractions of the measured capacity ('' for none)")
     ap.add_argument("--chunk", type=int, default=0, help="serving: iterations per graph chunk (0: the engine's)")
     ap.add_argument("--no-autotune", action="store_true", help="serving: keep the default V(2,2) sweeps")
     ap.add_argument("--only-loop", action="store_true", help="serving: the closed loop only (for launch lists)")

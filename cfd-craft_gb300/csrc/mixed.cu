@@ -3301,6 +3301,36 @@ int64_t cfdg_batch_stats_json(cfdg_batch* B, char* buf, int64_t cap) {
   return (int64_t)out.size() + 1;
 }
 
+// Algorithmic bytes of one launch of the coarse levels of every case (each logical array
+// read or written once per phase): per non-terminal level of n rows, E ELL entries (8 bytes
+// each: value and column) and nnz CSR entries, the 2 nu sweeps read the ELL block, the
+// right-hand side and 1/diag and write x (8 E + 12 n each); x is zeroed (4 n); the residual
+// reads the ELL block of colour 0 with diag, x and rhs and writes res (a res0 level, about
+// half: 4 E + 8 n), or the CSR rows (8 nnz + 20 n); the restriction reads res, children and
+// weights (12 n) and writes the next level's right-hand side; the prolongation reads the
+// injection rows and updates x (20 n). The terminal blocks read their inverse (8 m^2 each).
+double coarse_bytes(const cfdg_batch* B) {
+  double total = 0.0;
+  const double nu = (double)B->nuc;
+  for (const auto& cs : B->cases) {
+    for (size_t l = 0; l < cs->stats.size(); ++l) {
+      const auto& v = cs->stats[l];
+      const double n = (double)v.rows, E = (double)v.ell, nnz = (double)v.nnz;
+      const bool terminal = (int)l == cs->C.nl - 1;
+      if (terminal) {
+        total += 8.0 * n + 8.0 * n * 32.0;  // rhs in, x out, up to 32 x 32 inverse entries per row
+        continue;
+      }
+      const bool res0 = cs->C.lv[l].res0 != 0;
+      total += 2.0 * nu * (8.0 * E + 12.0 * n) + 4.0 * n;
+      total += res0 ? 4.0 * E + 8.0 * n : 8.0 * nnz + 20.0 * n;
+      total += 12.0 * n + 4.0 * (l + 1 < cs->stats.size() ? (double)cs->stats[l + 1].rows : 0.0);
+      total += 20.0 * n;
+    }
+  }
+  return total;
+}
+
 int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* ms_per_launch,
                            double* algorithmic_bytes) {
   if (!B || reps < 1) return fail(CFDG_ERR_INVALID, "invalid arguments");
@@ -3344,6 +3374,7 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
   };
   if (which == 0 || which == 4) bytes = 9.0 * cells;  // half the cells: rhs, 1/diag, u16 flags, x out; the other half's x in
   else if (which == 1) bytes = 10.0 * cells; // p in, u16 flags, q out
+  else if (which == 2) bytes = coarse_bytes(B);
   launch();
   launch();
   CU(cudaEventRecord(B->ev0, s));
