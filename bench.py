@@ -49,8 +49,9 @@ WORKLOAD = ("128x128x64 grid, dx=2 m, 12 seeded box buildings, open x (inflow 5 
             "masked multigrid V(2,2)-PCG to 1e-8")
 
 
-# DRAM bytes per cell of one red-black half sweep (ncu: 29,417,728 B over 4,194,304 cells).
-RB_DRAM_BYTES_PER_CELL = (29406720 + 11008) / 4194304
+# DRAM bytes per cell of one staged red-black half sweep (ncu, k_rb_tma on 4 x 128x128x64:
+# 29,541,888 B read + 18,944,000 B written over 4,194,304 cells).
+RB_DRAM_BYTES_PER_CELL = (29541888 + 18944000) / 4194304
 # DRAM bytes of one scalar transport step (both passes) per cell, from one ncu capture of
 # k_scalar_pass on the 128x128x64 transport workload.
 TRANSPORT_DRAM_BYTES_PER_CELL = (54496768 + 337408 + 62883584 + 301824) / 1048576
@@ -791,13 +792,13 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     k = kernels["rb_half_sweep_fp32"]
     achieved = k["algorithmic_bytes"] / (k["ms"] * 1e-3) / 1e9
     # DRAM bytes per launch from the ncu capture of the same kernel on 4 x 128x128x64
-    # (29.42 MB read + 0.01 MB written over 4,194,304 cells), scaled by the cells of this
+    # (29.54 MB read + 18.94 MB written over 4,194,304 cells), scaled by the cells of this
     # launch (traffic grows with cells).
     traffic = round(RB_DRAM_BYTES_PER_CELL * sum(sv.cells), 0)
     roofline = {"bound": "hbm", "kernel": "fine-level red-black Gauss-Seidel half sweep, FP32, all cases of the mix",
                 "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_source": peak_kind, "traffic": traffic,
-                "traffic_source": "ncu dram__bytes_read+write of k_rb on 4x128x128x64, scaled by cells",
+                "traffic_source": "ncu dram__bytes_read+write of k_rb_tma on 4x128x128x64, scaled by cells",
                 "algorithmic_bytes": k["algorithmic_bytes"], "ms_per_launch": k["ms"]}
     # Plain FP64 on the same mix, every case at once: one host thread and one stream per
     # case (the engine serialises calls per grid only), after an untimed cold solve each.
