@@ -2557,8 +2557,9 @@ int cfdg_grid_set_cycle(cfdg_grid* G, int32_t nu_fine, int32_t nu_coarse) {
 
 int cfdg_grid_set_sweep_tile(cfdg_grid* G, int32_t rows, int32_t stages) {
   if (int e = check_grid(G)) return e;
-  if (!(rows == 8 || rows == 16 || rows == 32) || stages < 2 || stages > 8)
-    return fail(CFDG_ERR_INVALID, "sweep tile: rows must be 8, 16 or 32 and stages 2..8");
+  const bool automatic = rows == 0 && stages == 0;
+  if (!automatic && (!(rows == 8 || rows == 16 || rows == 32) || stages < 2 || stages > 8))
+    return fail(CFDG_ERR_INVALID, "sweep tile: rows must be 8, 16 or 32 and stages 2..8 (or both 0)");
   std::lock_guard<std::mutex> lk(G->mu);
   if (G->mx_sweep_rows != rows || G->mx_sweep_stages != stages) G->solo.reset();
   G->mx_sweep_rows = rows;

@@ -98,6 +98,10 @@ struct FineCase {
   double* partials;  // ntiles doubles
   // level-0 closed groups (full indices) for the gauge
   int ngroups;
+  // No closed groups on level 0: the residual before restriction is taken on colour 0
+  // only (colour 1's is zero up to rounding after the last pre-smoothing half sweep), its
+  // colour-1 slots stay zero and the restriction gathers colour-0 children only.
+  int resc0, pad_resc0;
   const int *goff, *gmem;
   // transfers level 0 <-> 1
   int n1;
@@ -826,7 +830,8 @@ __device__ __forceinline__ void b_rb(const FineCase* FC, MState* ST, const int2 
     x[own + s] = v * id;
   }
 }
-__global__ void __launch_bounds__(TILE, 5) k_rb(const FineCase* FC, MState* ST, const int2* tiles, const int* count, int color, int first) {
+__global__ void __launch_bounds__(TILE, 5)
+    k_rb(const FineCase* FC, MState* ST, const int2* tiles, const int* count, int color, int first) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
   for (int ti = t0_; ti < t1_; ++ti) {
@@ -1100,7 +1105,7 @@ __device__ __forceinline__ void b_v_resid(const FineCase* FC, MState* ST, const 
   const float* __restrict__ x = F.x0;
   if (F.uniform && !(nxh_ & 1)) {
     const bool hy0 = j > 0, hy1 = j + 1 < F.n[1], hz0 = k > 0, hz1 = k + 1 < F.n[2];
-    for (int col = 0; col < 2; ++col) {
+    for (int col = 0; col < (F.resc0 ? 1 : 2); ++col) {
       const int par = (j + k + col) & 1;
       const int own = lay(r, col, nxh_, 0), oth = lay(r, col ^ 1, nxh_, 0);
       for (int s2 = 2 * lane; s2 < nxh_; s2 += 64) {
@@ -1128,7 +1133,7 @@ __device__ __forceinline__ void b_v_resid(const FineCase* FC, MState* ST, const 
     }
     return;
   }
-  for (int col = 0; col < 2; ++col) {
+  for (int col = 0; col < (F.resc0 ? 1 : 2); ++col) {
     const int par = (j + k + col) & 1;
     const int own = lay(r, col, nxh_, 0), oth = lay(r, col ^ 1, nxh_, 0);
     for (int s = lane; s < nxh_; s += 32) {
@@ -1171,17 +1176,22 @@ __global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState*
   }
 }
 
-// x0 += P x1 (the prolongation's rows are the split layout's slots; padding rows are empty).
+// x0 += P x1 on the colour-0 slots only (the prolongation's rows are the split layout's
+// slots; padding rows are empty): the first post-smoothing half sweep (colour 1) rewrites
+// every colour-1 slot without reading it, so their coarse correction would be dead work.
 __device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
+  const int rows_t = min(RT, F.n[1] * F.n[2] - lt * RT);
   if (F.pinj) {  // x0 += x1[parent]: the same value as the weight-1 row below
-    for (int c = sb + threadIdx.x; c < se; c += TILE) {
+    for (int m = threadIdx.x; m < rows_t * nxh_; m += TILE) {
+      const int c = lay(lt * RT + m / nxh_, 0, nxh_, m % nxh_);
       const int q = F.pinj[c];
       if (q >= 0) F.x0[c] += F.pscale * F.x1[q];
     }
     return;
   }
-  for (int c = sb + threadIdx.x; c < se; c += TILE) {
+  for (int m = threadIdx.x; m < rows_t * nxh_; m += TILE) {
+    const int c = lay(lt * RT + m / nxh_, 0, nxh_, m % nxh_);
     const int b = F.p_off[c], e = F.p_off[c + 1];
     if (b == e) continue;
     float sum = 0.0f;
@@ -2249,9 +2259,27 @@ int build_case(cfdg_grid* G, CaseState& cs) {
   {
     // Restriction gathers level-0 slots; the prolongation's rows follow the slots; level
     // 1 in its colour-by-colour numbering.
-    const Csr R0 = permute_csr(M0.restrict, perm[1], {});
+    Csr R0 = permute_csr(M0.restrict, perm[1], {});
     std::vector<int32_t> child(R0.col.size());
     for (size_t q = 0; q < child.size(); ++q) child[q] = slot[R0.col[q]];
+    F.resc0 = M0.groups.rows() == 0 ? 1 : 0;
+    if (F.resc0) {
+      // Colour-0 children only (slot in the first half of its row pair); order kept.
+      Csr K;
+      std::vector<int32_t> kept;
+      K.off.assign(1, 0);
+      for (int j = 0; j < R0.rows(); ++j) {
+        for (int q = R0.off[j]; q < R0.off[j + 1]; ++q)
+          if (((child[q] / F.nxh) & 1) == 0) {
+            kept.push_back(child[q]);
+            K.val.push_back(R0.val[q]);
+          }
+        K.off.push_back((int32_t)kept.size());
+      }
+      R0.off = std::move(K.off);
+      R0.val = std::move(K.val);
+      child = std::move(kept);
+    }
     std::vector<int32_t> poff(F.N2 + 1, 0), pcol;
     std::vector<float> pw32;
     pcol.reserve(M0.prolong.col.size());
@@ -2505,6 +2533,7 @@ struct cfdg_batch {
   // (rounded up to 16 slots), the dynamic shared memory and the persistent grid.
   bool rb_tma = false;
   int rb_hmax = 0, rb_grid = 1, rb_sr = RT, rb_ns = 3;
+  int rb_sr_req = 0, rb_ns_req = 0;  // the grids' setting (0, 0: automatic)
   size_t rb_smem = 0;
   int csize = CS;
   std::vector<char> active;
@@ -2964,10 +2993,26 @@ int cfdg_mixed_pack(cfdg_batch* B) {
     // The sweep's tile shape comes from the grids (cfdg_grid_set_sweep_tile), like the
     // cycle's sweep counts; fewer stages are used when the requested ones do not fit.
     B->rb_hmax = (B->rb_hmax + 15) / 16 * 16;
-    int dev = 0, sms = 0, per = 0, smem_max = 0;
+    int dev = 0, sms = 0, per = 0, smem_max = 0, smem_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    B->rb_sr = B->rb_sr_req;
+    B->rb_ns = B->rb_ns_req;
+    if (B->rb_sr == 0) {
+      // The automatic shape: two stages of the tallest height whose blocks still fit twice
+      // per SM (on the benchmarked mixes the autotuner's choice, 32 x 2, where it fits).
+      B->rb_ns = 2;
+      B->rb_sr = 8;
+      for (int sr : {32, 16}) {
+        const size_t need = 2 * (2 * (size_t)rb_offsets(B->rb_hmax, sr).stage + 128 + 2048);
+        if (need <= (size_t)smem_sm) {
+          B->rb_sr = sr;
+          break;
+        }
+      }
+    }
     const size_t stage = (size_t)rb_offsets(B->rb_hmax, B->rb_sr).stage;
     while (B->rb_ns > 1 && (size_t)B->rb_ns * stage + 128 + 1024 > (size_t)smem_max) --B->rb_ns;
     B->rb_smem = (size_t)B->rb_ns * stage + 128;
@@ -3027,11 +3072,11 @@ int cfdg_mixed_add_case(cfdg_batch* B, cfdg_grid* G) {
   if (B->grids.empty()) {
     B->nu0 = G->mx_nu0;
     B->nuc = G->mx_nuc;
-    B->rb_sr = G->mx_sweep_rows;
-    B->rb_ns = G->mx_sweep_stages;
+    B->rb_sr_req = G->mx_sweep_rows;
+    B->rb_ns_req = G->mx_sweep_stages;
   } else if (B->nu0 != G->mx_nu0 || B->nuc != G->mx_nuc) {
     return fail(CFDG_ERR_INVALID, "the grids of a batch must share their V-cycle sweep counts");
-  } else if (B->rb_sr != G->mx_sweep_rows || B->rb_ns != G->mx_sweep_stages) {
+  } else if (B->rb_sr_req != G->mx_sweep_rows || B->rb_ns_req != G->mx_sweep_stages) {
     return fail(CFDG_ERR_INVALID, "the grids of a batch must share their sweep tile shape");
   }
   B->grids.push_back(G);

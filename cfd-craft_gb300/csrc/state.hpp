@@ -204,8 +204,9 @@ struct cfdg_grid {
   int mx_nu0 = 2, mx_nuc = 2;
   float mx_alpha = 1.8f;  // mixed form: coarse-correction scale on aggregation hierarchies
   // Mixed form: tile shape of the staged level-0 half sweeps (cfdg_grid_set_sweep_tile):
-  // rows per shared-memory stage (8, 16, 32) and stages in flight per block (2..8).
-  int mx_sweep_rows = 32, mx_sweep_stages = 2;
+  // rows per shared-memory stage (8, 16, 32) and stages in flight per block (2..8); 0 and 0
+  // choose from the row length when a batch is packed.
+  int mx_sweep_rows = 0, mx_sweep_stages = 0;
   // Laminar time stepping (cfdg_grid_set_flow / cfdg_step_device): the case flow and the
   // stage buffers (cell velocities, the two stage velocities, the stage pressure).
   bool has_flow = false;

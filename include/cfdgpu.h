@@ -195,7 +195,9 @@ int cfdg_grid_set_cycle(cfdg_grid *grid, int32_t nu_fine, int32_t nu_coarse);
 /* Mixed form: tile shape of the level-0 red-black half sweeps, which the tensor memory
  * accelerator stages through shared memory on grids with uniform weights and ceil(nx/2) a
  * multiple of 8: rows per stage (8, 16 or 32; the y halo is two rows per stage) and stages
- * in flight per block (2..8; fewer when they do not fit the shared memory). Default 32 and 2.
+ * in flight per block (2..8; fewer when they do not fit the shared memory). 0 and 0 (the
+ * default) choose from the row length: two stages of 32 rows when two blocks of them fit an
+ * SM's shared memory, else of 16 or 8 rows.
  * Batches and servers created afterwards take it from their grids (all grids of one batch
  * must agree); the results do not depend on it, bit for bit. The bench's autotuner picks it
  * per case mix. No reference counterpart. */
