@@ -1308,6 +1308,13 @@ __device__ __forceinline__ void res0_rows(const CLev& L, int k) {
     if (q + r < nrow) L.res[q + r] = __ldcg(&L.rhs[q + r]) - v[r];
 }
 
+// Rows of a level that the prolongation must update: on Gauss-Seidel levels the last colour
+// (the first one the post-smoothing sweeps, backward) is rewritten without being read, so
+// its rows (the last colour block) are skipped; l1-Jacobi levels read every row.
+__device__ __forceinline__ int prolong_rows(const CLev& L) {
+  return L.jacobi ? L.n : L.coff[L.ncolors - 1];
+}
+
 // ----------------------------------------------------------------- coarse levels, one cluster per case
 __device__ __forceinline__ void csync() { cg::this_cluster().sync(); }
 
@@ -1436,7 +1443,7 @@ __global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState*
   for (int m = min(l, C.nl - 1) - 1; m >= 0; --m) {
     const CLev& L = C.lv[m];
     const CLev& N = C.lv[m + 1];
-    for (int i = tid; i < L.n; i += nth) {
+    for (int i = tid; i < prolong_rows(L); i += nth) {
       float s = 0.0f;
       for (int k = L.poff[i]; k < L.poff[i + 1]; ++k) s = fmaf(L.pw[k], __ldcg(&N.x[L.pcol[k]]), s);
       L.x[i] = __ldcg(&L.x[i]) + s;
@@ -1705,7 +1712,7 @@ __device__ void blk_cycle(const CCase& C, int l0, int nu, double* sh) {
   for (int m = min(l, C.nl - 1) - 1; m >= l0; --m) {
     const CLev& L = C.lv[m];
     const CLev& N = C.lv[m + 1];
-    for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+    for (int i = threadIdx.x; i < prolong_rows(L); i += blockDim.x) {
       float s = 0.0f;
       for (int k = L.poff[i]; k < L.poff[i + 1]; ++k) s = fmaf(L.pw[k], __ldcg(&N.x[L.pcol[k]]), s);
       L.x[i] = __ldcg(&L.x[i]) + s;
@@ -2449,9 +2456,24 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     } else {
       int *ro, *rc, *po, *pc;
       float *rw, *pw;
-      if (int e = A.upload(&ro, M.restrict.off, s)) return e;
-      if (int e = A.upload(&rc, M.restrict.col, s)) return e;
-      if (int e = A.upload(&rw, to_f32(M.restrict.val), s)) return e;
+      Csr R = M.restrict;
+      if (L.res0) {
+        // Colour-1 residuals stay zero on this level: gather colour-0 children only.
+        Csr K;
+        K.off.assign(1, 0);
+        for (int j = 0; j < R.rows(); ++j) {
+          for (int q = R.off[j]; q < R.off[j + 1]; ++q)
+            if (R.col[q] < coff[1]) {
+              K.col.push_back(R.col[q]);
+              K.val.push_back(R.val[q]);
+            }
+          K.off.push_back((int32_t)K.col.size());
+        }
+        R = std::move(K);
+      }
+      if (int e = A.upload(&ro, R.off, s)) return e;
+      if (int e = A.upload(&rc, R.col, s)) return e;
+      if (int e = A.upload(&rw, to_f32(R.val), s)) return e;
       if (int e = A.upload(&po, M.prolong.off, s)) return e;
       if (int e = A.upload(&pc, M.prolong.col, s)) return e;
       std::vector<float> pw32 = to_f32(M.prolong.val);
@@ -2706,7 +2728,8 @@ int fill_tab(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
       rows[l * w + i + 1] = rows[l * w + i] + (L ? L->n : 0);
       term[l * w + i + 1] = term[l * w + i] + (L && L->terminal ? L->nblocks : 0);
       next[l * w + i + 1] = next[l * w + i] + (nt ? B->cases[i]->C.lv[l + 1].n : 0);
-      live[l * w + i + 1] = live[l * w + i] + (nt ? L->n : 0);
+      // Prolongation items: every row but the last colour's on Gauss-Seidel levels.
+      live[l * w + i + 1] = live[l * w + i] + (nt ? (L->jacobi ? L->n : B->cases[i]->colors[l][L->ncolors - 1]) : 0);
       grp[l * w + i + 1] = grp[l * w + i] + (L ? L->ngroups : 0);
       const auto& cof = B->cases[i]->colors[l];
       const int nres = !nt ? 0 : (L->res0 ? (cof[1] + RPI - 1) / RPI : (L->jacobi ? 8 * L->n : L->n));
