@@ -1238,7 +1238,7 @@ __global__ void k_center0(const FineCase* FC, MState* ST, const int2* gtab, cons
 // each other), entries are summed in ELL order as every other path does. skipx: the first
 // colour of the cycle's first sweep, whose neighbours are all zero, takes x = rhs / diag
 // (the same bits as summing the zero products).
-constexpr int RPI = 4;
+constexpr int RPI = 4;  // the pipelined entry loops below are written for four rows
 __device__ __forceinline__ void gs_rows(const CLev& L, int color, int k, bool skipx) {
   const int c0 = L.coff[color];
   const int nrow = L.coff[color + 1] - c0;
@@ -1255,20 +1255,33 @@ __device__ __forceinline__ void gs_rows(const CLev& L, int color, int k, bool sk
     const int base = L.ell_off[color], w = L.ell_w[color];
     const int* ec = L.ell_col + base + q;
     const float* ev = L.ell_val + base + q;
+    // Software-pipelined: entry a+1's columns and values load while entry a's x gathers.
+    int col[RPI];
+    float wv[RPI];
+#pragma unroll
+    for (int r = 0; r < RPI; ++r) {
+      const bool ok = q + r < nrow && w > 0;
+      col[r] = ok ? ec[r] : c0 + q;
+      wv[r] = ok ? ev[r] : 0.0f;
+    }
 #pragma unroll 1
     for (int a = 0; a < w; ++a) {
-      int col[RPI];
-      float wv[RPI], xv[RPI];
-#pragma unroll
-      for (int r = 0; r < RPI; ++r) {
-        const bool ok = q + r < nrow;
-        col[r] = ok ? ec[a * nrow + r] : c0 + q;
-        wv[r] = ok ? ev[a * nrow + r] : 0.0f;
-      }
+      float xv[RPI];
 #pragma unroll
       for (int r = 0; r < RPI; ++r) xv[r] = __ldcg(&L.x[col[r]]);
+      const float w0 = wv[0], w1 = wv[1], w2 = wv[2], w3 = wv[3];
+      if (a + 1 < w) {
 #pragma unroll
-      for (int r = 0; r < RPI; ++r) v[r] = fmaf(-wv[r], xv[r], v[r]);
+        for (int r = 0; r < RPI; ++r) {
+          const bool ok = q + r < nrow;
+          col[r] = ok ? ec[(a + 1) * nrow + r] : c0 + q;
+          wv[r] = ok ? ev[(a + 1) * nrow + r] : 0.0f;
+        }
+      }
+      v[0] = fmaf(-w0, xv[0], v[0]);
+      v[1] = fmaf(-w1, xv[1], v[1]);
+      v[2] = fmaf(-w2, xv[2], v[2]);
+      v[3] = fmaf(-w3, xv[3], v[3]);
     }
   }
 #pragma unroll
@@ -1288,20 +1301,32 @@ __device__ __forceinline__ void res0_rows(const CLev& L, int k) {
   const int base = L.ell_off[0], w = L.ell_w[0];
   const int* ec = L.ell_col + base + q;
   const float* ev = L.ell_val + base + q;
-#pragma unroll 2
-  for (int a = 0; a < w; ++a) {
-    int col[RPI];
-    float wv[RPI], xv[RPI];
+  int col[RPI];
+  float wv[RPI];
 #pragma unroll
-    for (int r = 0; r < RPI; ++r) {
-      const bool ok = q + r < nrow;
-      col[r] = ok ? ec[a * nrow + r] : q;
-      wv[r] = ok ? ev[a * nrow + r] : 0.0f;
-    }
+  for (int r = 0; r < RPI; ++r) {
+    const bool ok = q + r < nrow && w > 0;
+    col[r] = ok ? ec[r] : q;
+    wv[r] = ok ? ev[r] : 0.0f;
+  }
+#pragma unroll 1
+  for (int a = 0; a < w; ++a) {
+    float xv[RPI];
 #pragma unroll
     for (int r = 0; r < RPI; ++r) xv[r] = __ldcg(&L.x[col[r]]);
+    const float w0 = wv[0], w1 = wv[1], w2 = wv[2], w3 = wv[3];
+    if (a + 1 < w) {
 #pragma unroll
-    for (int r = 0; r < RPI; ++r) v[r] = fmaf(wv[r], xv[r], v[r]);
+      for (int r = 0; r < RPI; ++r) {
+        const bool ok = q + r < nrow;
+        col[r] = ok ? ec[(a + 1) * nrow + r] : q;
+        wv[r] = ok ? ev[(a + 1) * nrow + r] : 0.0f;
+      }
+    }
+    v[0] = fmaf(w0, xv[0], v[0]);
+    v[1] = fmaf(w1, xv[1], v[1]);
+    v[2] = fmaf(w2, xv[2], v[2]);
+    v[3] = fmaf(w3, xv[3], v[3]);
   }
 #pragma unroll
   for (int r = 0; r < RPI; ++r)
