@@ -1096,6 +1096,24 @@ __global__ void __launch_bounds__(RB_THREADS, 3) k_rb_tma(const FineCase* FC, MS
   }
 }
 
+// acc + sum over k in [b, e) of w[k] v[idx[k]], in k order, with four entries' index and
+// value loads in flight at a time (the transfers' rows are chains of dependent loads).
+__device__ __forceinline__ float gather_sum(const int* __restrict__ idx, const float* __restrict__ w,
+                                            const float* __restrict__ v, int b, int e, float acc) {
+  int k = b;
+  for (; k + 4 <= e; k += 4) {
+    const int i0 = idx[k], i1 = idx[k + 1], i2 = idx[k + 2], i3 = idx[k + 3];
+    const float w0 = w[k], w1 = w[k + 1], w2 = w[k + 2], w3 = w[k + 3];
+    const float x0 = __ldcg(&v[i0]), x1 = __ldcg(&v[i1]), x2 = __ldcg(&v[i2]), x3 = __ldcg(&v[i3]);
+    acc = fmaf(w0, x0, acc);
+    acc = fmaf(w1, x1, acc);
+    acc = fmaf(w2, x2, acc);
+    acc = fmaf(w3, x3, acc);
+  }
+  for (; k < e; ++k) acc = fmaf(w[k], __ldcg(&v[idx[k]]), acc);
+  return acc;
+}
+
 // res0 = rhs0 - A0 x0 (A0 = diag - sum w on interior faces).
 __device__ __forceinline__ void b_v_resid(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
@@ -1171,7 +1189,7 @@ __global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState*
     const int j = t.y * TILE + threadIdx.x;
     if (j >= F.n1) continue;
     float v = 0.0f;
-    for (int k = F.r_off[j]; k < F.r_off[j + 1]; ++k) v = fmaf(F.r_w[k], F.res0[F.r_child[k]], v);
+    v = gather_sum(F.r_child, F.r_w, F.res0, F.r_off[j], F.r_off[j + 1], v);
     F.rhs1[j] = v;
   }
 }
@@ -1238,7 +1256,7 @@ __global__ void k_center0(const FineCase* FC, MState* ST, const int2* gtab, cons
 // each other), entries are summed in ELL order as every other path does. skipx: the first
 // colour of the cycle's first sweep, whose neighbours are all zero, takes x = rhs / diag
 // (the same bits as summing the zero products).
-constexpr int RPI = 4;  // the pipelined entry loops below are written for four rows
+constexpr int RPI = 4;
 __device__ __forceinline__ void gs_rows(const CLev& L, int color, int k, bool skipx) {
   const int c0 = L.coff[color];
   const int nrow = L.coff[color + 1] - c0;
@@ -1269,7 +1287,9 @@ __device__ __forceinline__ void gs_rows(const CLev& L, int color, int k, bool sk
       float xv[RPI];
 #pragma unroll
       for (int r = 0; r < RPI; ++r) xv[r] = __ldcg(&L.x[col[r]]);
-      const float w0 = wv[0], w1 = wv[1], w2 = wv[2], w3 = wv[3];
+      float wc[RPI];
+#pragma unroll
+      for (int r = 0; r < RPI; ++r) wc[r] = wv[r];
       if (a + 1 < w) {
 #pragma unroll
         for (int r = 0; r < RPI; ++r) {
@@ -1278,10 +1298,8 @@ __device__ __forceinline__ void gs_rows(const CLev& L, int color, int k, bool sk
           wv[r] = ok ? ev[(a + 1) * nrow + r] : 0.0f;
         }
       }
-      v[0] = fmaf(-w0, xv[0], v[0]);
-      v[1] = fmaf(-w1, xv[1], v[1]);
-      v[2] = fmaf(-w2, xv[2], v[2]);
-      v[3] = fmaf(-w3, xv[3], v[3]);
+#pragma unroll
+      for (int r = 0; r < RPI; ++r) v[r] = fmaf(-wc[r], xv[r], v[r]);
     }
   }
 #pragma unroll
@@ -1314,7 +1332,9 @@ __device__ __forceinline__ void res0_rows(const CLev& L, int k) {
     float xv[RPI];
 #pragma unroll
     for (int r = 0; r < RPI; ++r) xv[r] = __ldcg(&L.x[col[r]]);
-    const float w0 = wv[0], w1 = wv[1], w2 = wv[2], w3 = wv[3];
+    float wc[RPI];
+#pragma unroll
+    for (int r = 0; r < RPI; ++r) wc[r] = wv[r];
     if (a + 1 < w) {
 #pragma unroll
       for (int r = 0; r < RPI; ++r) {
@@ -1323,10 +1343,8 @@ __device__ __forceinline__ void res0_rows(const CLev& L, int k) {
         wv[r] = ok ? ev[(a + 1) * nrow + r] : 0.0f;
       }
     }
-    v[0] = fmaf(w0, xv[0], v[0]);
-    v[1] = fmaf(w1, xv[1], v[1]);
-    v[2] = fmaf(w2, xv[2], v[2]);
-    v[3] = fmaf(w3, xv[3], v[3]);
+#pragma unroll
+    for (int r = 0; r < RPI; ++r) v[r] = fmaf(wc[r], xv[r], v[r]);
   }
 #pragma unroll
   for (int r = 0; r < RPI; ++r)
@@ -1449,7 +1467,7 @@ __global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState*
     } else {
       for (int i = tid; i < L.n; i += nth) {
         float v = L.diag[i] * __ldcg(&L.x[i]);
-        for (int a = L.off[i]; a < L.off[i + 1]; ++a) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
+        v = gather_sum(L.col, L.val, L.x, L.off[i], L.off[i + 1], v);
         L.res[i] = __ldcg(&L.rhs[i]) - v;
       }
     }
@@ -1459,7 +1477,7 @@ __global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState*
     const CLev& N = C.lv[l + 1];
     for (int j = tid; j < N.n; j += nth) {
       float v = 0.0f;
-      for (int k = L.roff[j]; k < L.roff[j + 1]; ++k) v = fmaf(L.rw[k], __ldcg(&L.res[L.rchild[k]]), v);
+      v = gather_sum(L.rchild, L.rw, L.res, L.roff[j], L.roff[j + 1], v);
       N.rhs[j] = v;
     }
     __threadfence();
@@ -1470,7 +1488,7 @@ __global__ void __launch_bounds__(CT) k_coarse(const CCase* cases, const MState*
     const CLev& N = C.lv[m + 1];
     for (int i = tid; i < prolong_rows(L); i += nth) {
       float s = 0.0f;
-      for (int k = L.poff[i]; k < L.poff[i + 1]; ++k) s = fmaf(L.pw[k], __ldcg(&N.x[L.pcol[k]]), s);
+      s = gather_sum(L.pcol, L.pw, N.x, L.poff[i], L.poff[i + 1], s);
       L.x[i] = __ldcg(&L.x[i]) + s;
     }
     __threadfence();
@@ -1720,7 +1738,7 @@ __device__ void blk_cycle(const CCase& C, int l0, int nu, double* sh) {
       } else {
         const int i = k;
         float v = L.diag[i] * __ldcg(&L.x[i]);
-        for (int a = L.off[i]; a < L.off[i + 1]; ++a) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
+        v = gather_sum(L.col, L.val, L.x, L.off[i], L.off[i + 1], v);
         L.res[i] = __ldcg(&L.rhs[i]) - v;
       }
     }
@@ -1729,7 +1747,7 @@ __device__ void blk_cycle(const CCase& C, int l0, int nu, double* sh) {
     const CLev& N = C.lv[l + 1];
     for (int j = threadIdx.x; j < N.n; j += blockDim.x) {
       float v = 0.0f;
-      for (int k = L.roff[j]; k < L.roff[j + 1]; ++k) v = fmaf(L.rw[k], __ldcg(&L.res[L.rchild[k]]), v);
+      v = gather_sum(L.rchild, L.rw, L.res, L.roff[j], L.roff[j + 1], v);
       N.rhs[j] = v;
     }
     __syncthreads();
@@ -1739,7 +1757,7 @@ __device__ void blk_cycle(const CCase& C, int l0, int nu, double* sh) {
     const CLev& N = C.lv[m + 1];
     for (int i = threadIdx.x; i < prolong_rows(L); i += blockDim.x) {
       float s = 0.0f;
-      for (int k = L.poff[i]; k < L.poff[i + 1]; ++k) s = fmaf(L.pw[k], __ldcg(&N.x[L.pcol[k]]), s);
+      s = gather_sum(L.pcol, L.pw, N.x, L.poff[i], L.poff[i + 1], s);
       L.x[i] = __ldcg(&L.x[i]) + s;
     }
     __syncthreads();
@@ -1814,7 +1832,7 @@ __global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const
         if (k >= L.n) continue;
         const int i = k;
         float v = L.diag[i] * __ldcg(&L.x[i]);
-        for (int a = L.off[i]; a < L.off[i + 1]; ++a) v = fmaf(L.val[a], __ldcg(&L.x[L.col[a]]), v);
+        v = gather_sum(L.col, L.val, L.x, L.off[i], L.off[i + 1], v);
         L.res[i] = __ldcg(&L.rhs[i]) - v;
       }
     }
@@ -1833,7 +1851,7 @@ __global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const
         const CLev& N = sl[nc + ci];
         const int j = t - cur.lo;
         float v = 0.0f;
-        for (int k = L.roff[j]; k < L.roff[j + 1]; ++k) v = fmaf(L.rw[k], __ldcg(&L.res[L.rchild[k]]), v);
+        v = gather_sum(L.rchild, L.rw, L.res, L.roff[j], L.roff[j + 1], v);
         N.rhs[j] = v;
       }
     }
@@ -1861,7 +1879,7 @@ __global__ void __launch_bounds__(512, 2) k_coarse_all(const CCase* cases, const
         const CLev& N = sl[nc + ci];
         const int i = t - cur.lo;
         float s = 0.0f;
-        for (int k = L.poff[i]; k < L.poff[i + 1]; ++k) s = fmaf(L.pw[k], __ldcg(&N.x[L.pcol[k]]), s);
+        s = gather_sum(L.pcol, L.pw, N.x, L.poff[i], L.poff[i + 1], s);
         L.x[i] = __ldcg(&L.x[i]) + s;
       }
     }
