@@ -174,8 +174,10 @@ class CpuPool:
         def work(t):
             p = self.np.zeros(self.gs[t].count)
             t0 = time.perf_counter()
-            codes[t], _, _, _ = self.grids[t].project(us[t], p, DT, TOL, MAX_IT)
+            codes[t], ou, op, info = self.grids[t].project(us[t], p, DT, TOL, MAX_IT)
             times[t] = time.perf_counter() - t0
+            if t == 0:
+                self.first = (us[0], ou, op, info)  # thread 0's input and result (the oracle check)
 
         self._each(work)
         assert all(c == 0 for c in codes), codes
@@ -200,7 +202,13 @@ def mix_sample(pkg, threads):
     return [mix[(t * len(mix)) // threads] for t in range(threads)]
 
 
-def cpu_baseline_mix(pkg):
+def cpu_baseline_mix(pkg, serve_one=None):
+    """The oracle on all host threads over the mix. With `serve_one(case_index, u)` (the
+    served path on the device), thread 0's timed input is also served and the result
+    compared with the oracle's: the error of a served case against the FP64 reference
+    algorithm (bound 1e-7 relative)."""
+    import numpy as np
+
     threads = os.cpu_count() or 1
     cases = mix_sample(pkg, threads)
     pool = CpuPool(cases, threads)
@@ -209,10 +217,21 @@ def cpu_baseline_mix(pkg):
     times = pool.solve([1000 + t for t in range(threads)])
     wall = time.perf_counter() - t0
     small = sum(1 for c in cases if c["grid"]["cells"][0] == 96)
-    return {"value": round(threads / wall, 4), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{threads} concurrent warm solves, one per host thread, over cases of the mix "
-                      f"({threads - small} at 128x128x64, {small} at 96x96x48), after one untimed cold solve "
-                      f"each; {wall:.2f} s wall, median {statistics.median(times):.2f} s per solve"}
+    out = {"value": round(threads / wall, 4), "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{threads} concurrent warm solves, one per host thread, over cases of the mix "
+                     f"({threads - small} at 128x128x64, {small} at 96x96x48), after one untimed cold solve "
+                     f"each; {wall:.2f} s wall, median {statistics.median(times):.2f} s per solve"}
+    if serve_one is not None:
+        u_in, ou, op, oinfo = pool.first
+        gu, gp, code, info = serve_one(0, u_in)
+        out["oracle_check"] = {
+            "case": cases[0]["name"], "code": code, "gpu_iterations": info.iterations,
+            "oracle_iterations": oinfo["iterations"],
+            "max_rel_err_p": float(np.max(np.abs(gp - op)) / np.max(np.abs(op))),
+            "max_rel_err_u": float(np.max(np.abs(gu - ou)) / np.max(np.abs(ou))), "bound": 1e-7,
+            "how": "thread 0's timed input (U[-1,1] faces, seed 1000, p = 0) served through cfdg_server in the "
+                   "mixed form, against the oracle's FP64 projection of the same input"}
+    return out
 
 
 def run_reference(args):
@@ -810,7 +829,16 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
         plain = plain_mix(pkg, torch, dev, sv, world, flush)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_mix(pkg)
+        def serve_one(c, u_host):
+            d_u = torch.from_numpy(u_host.copy()).to(dev)
+            d_p = torch.zeros(sv.grids[c].count, dtype=torch.float64, device=dev)
+            torch.cuda.synchronize()
+            t = sv.server.submit(c, d_u.data_ptr(), d_p.data_ptr(), DT, TOL, MAX_IT)
+            while (r := sv.server.result(t)) is None:
+                sv.server.progress()
+            return d_u.cpu().numpy(), d_p.cpu().numpy(), r[0], r[1]
+
+        cpu = cpu_baseline_mix(pkg, serve_one)
     if rank == 0:
         its = [i.iterations for _, i in infos]
         line = {
