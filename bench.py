@@ -464,101 +464,61 @@ class Serving:
         return lat, infos
 
     def e2e_loop(self, steps, seed=77):
-        """The closed loop with the fields in host memory: each request's u* and p are copied
-        from pinned host buffers to the device before it runs and its projected u and p back
-        to pinned host buffers when it finishes, all inside the timed region. The copies run
-        on two copy streams beside the server's stream: a case's next inputs are copied into
-        its second device buffer while its current request runs (the server's stream waits
-        for that copy's event before the submission; the copy waits for the results last
-        copied out of that buffer), and a finished request's results are copied out after
-        an event on the server's stream. The inputs of step s are the fields
-        the device loop left plus a seeded perturbation (two per case, used in turn, prepared
-        before the timed region).
+        """The closed loop with the fields in host memory, through cfdg_server_submit_host:
+        each request's u* and p are copied by the engine from page-locked host buffers to a
+        device slot of its grid before it runs, and its projected u and p back to host
+        buffers after it finishes; a ticket reports done once its results are in host memory.
+        Every case keeps two requests in flight (the engine's two slots per grid), so the
+        next input's copy overlaps the running solve; when one finishes the case's next is
+        submitted. The copies run on the engine's copy streams beside the solves, all inside
+        the timed region. The inputs are the fields the device loop left plus a seeded
+        perturbation (two sets per case, used in turn, prepared before the timed region).
         Returns (milliseconds, H2D bytes, D2H bytes)."""
         import numpy as np
 
         torch = self.torch
         rng = np.random.default_rng(seed)
         base = [u.cpu().numpy() for u in self.d_u]
-        h_in, h_p = [], []
+        h_in, h_p, o_u, o_p = [], [], [], []
         for c, g in enumerate(self.grids):
             m = self.free[c].cpu().numpy()
-            # Two perturbed input fields per case, used in turn (step s reads set s % 2), so
-            # the pinned host memory does not grow with the number of steps.
             h_in.append([torch.from_numpy(base[c] + m * rng.uniform(-0.05, 0.05, g.n_faces)).pin_memory()
-                         for _ in range(min(steps, 2))])
+                         for _ in range(2)])
             h_p.append(torch.zeros(g.count, dtype=torch.float64).pin_memory())
-        o_u = [torch.empty(g.n_faces, dtype=torch.float64).pin_memory() for g in self.grids]
-        o_p = [torch.empty(g.count, dtype=torch.float64).pin_memory() for g in self.grids]
-        # Second device buffers: request s of case c runs in buffer s % 2.
-        bu = [[self.d_u[c], torch.empty_like(self.d_u[c])] for c in range(self.n)]
-        bp = [[self.d_p[c], torch.empty_like(self.d_p[c])] for c in range(self.n)]
-        copy = torch.cuda.Stream(self.d_u[0].device)   # host to device
-        back = torch.cuda.Stream(self.d_u[0].device)   # device to host
-        ready = [[None, None] for _ in range(self.n)]
-        drained = [[None, None] for _ in range(self.n)]  # results of the buffer copied out
+            o_u.append([torch.empty(g.n_faces, dtype=torch.float64).pin_memory() for _ in range(2)])
+            o_p.append([torch.empty(g.count, dtype=torch.float64).pin_memory() for _ in range(2)])
         srv = self.server
         torch.cuda.synchronize()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         h2d = d2h = 0
-        nxt = [0] * self.n   # next step to submit per case
+        nxt = [0] * self.n
         inflight = {}
 
-        def load(c, s_):
-            """H2D of step s_'s inputs of case c into buffer s_ % 2, on the copy stream."""
-            nonlocal h2d
-            k = s_ % 2
-            with torch.cuda.stream(copy):
-                if drained[c][k] is not None:
-                    copy.wait_event(drained[c][k])
-                bu[c][k].copy_(h_in[c][s_ % len(h_in[c])], non_blocking=True)
-                bp[c][k].copy_(h_p[c], non_blocking=True)
-                e = torch.cuda.Event()
-                e.record(copy)
-            ready[c][k] = e
-            h2d += 8 * (bu[c][k].numel() + bp[c][k].numel())
-
         def submit(c):
-            s_ = nxt[c]
-            k = s_ % 2
-            self.stream.wait_event(ready[c][k])
-            t = srv.submit(c, bu[c][k].data_ptr(), bp[c][k].data_ptr(), DT, TOL, MAX_IT)
-            inflight[t] = (c, k)
+            nonlocal h2d
+            k = nxt[c] % 2
+            t = srv.submit_host(c, h_in[c][k].data_ptr(), h_p[c].data_ptr(), o_u[c][k].data_ptr(),
+                                o_p[c][k].data_ptr(), DT, TOL, MAX_IT)
+            inflight[t] = c
             nxt[c] += 1
-            if nxt[c] < steps:
-                load(c, nxt[c])  # prefetch the next inputs into the other buffer
+            h2d += 8 * (h_in[c][k].numel() + h_p[c].numel())
 
         ev0.record(self.stream)
-        copy.wait_event(ev0)
-        back.wait_event(ev0)
         for c in range(self.n):
-            load(c, 0)
-        for c in range(self.n):
-            submit(c)
+            for _ in range(min(2, steps)):
+                submit(c)
         while inflight:
-            if srv.progress() == 0:
-                continue
+            srv.progress()
             for t in list(inflight):
                 r = srv.result(t)
                 if r is None:
                     continue
                 assert r[0] == 0, r[0]
-                c, k = inflight.pop(t)
-                done = torch.cuda.Event()
-                done.record(self.stream)  # after the request's epilogue
-                with torch.cuda.stream(back):
-                    back.wait_event(done)
-                    o_u[c].copy_(bu[c][k], non_blocking=True)
-                    o_p[c].copy_(bp[c][k], non_blocking=True)
-                    e = torch.cuda.Event()
-                    e.record(back)
-                drained[c][k] = e
-                d2h += 8 * (bu[c][k].numel() + bp[c][k].numel())
+                c = inflight.pop(t)
+                d2h += 8 * (o_u[c][0].numel() + o_p[c][0].numel())
                 if nxt[c] < steps:
                     submit(c)
-        self.stream.wait_stream(copy)
-        self.stream.wait_stream(back)
         ev1.record(self.stream)
         torch.cuda.synchronize()
         return ev0.elapsed_time(ev1), h2d, d2h
@@ -799,9 +759,10 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
         srv_ms = max_over_ranks(srv_ms, dist, dev)
     e2e = {"value": round(world * srv_steps * n / (srv_ms / 1e3), 4), "unit": UNIT,
            "h2d_bytes_per_step": h2d_b // srv_steps, "d2h_bytes_per_step": d2h_b // srv_steps,
-           "call": "cfdg_server submit/progress/result, u and p copied from and to pinned host buffers around "
-                   "every request on two copy streams beside the server's (a case's next inputs prefetched into "
-                   "a second device buffer, results copied out after the request's epilogue)", "steps": srv_steps}
+           "call": "cfdg_server_submit_host/progress/result: the engine copies each request's u and p from "
+                   "page-locked host buffers into a device slot of its grid and the results back after the "
+                   "request, on copy streams beside the solves; a ticket is done when its results are in host "
+                   "memory; two requests per case in flight", "steps": srv_steps}
     kernels = {}
     for name, which, reps in (("rb_half_sweep_fp32", 0, 20), ("rb_half_sweep_fp32_unstaged", 4, 20),
                               ("operator_fp32", 1, 20), ("coarse_levels", 2, 10), ("vcycle_fp32", 3, 5)):

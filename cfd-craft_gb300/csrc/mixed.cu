@@ -3304,9 +3304,29 @@ struct cfdg_server {
     double *u, *p;
     double dt, tol;
     uint64_t max_iter;
+    int slot;              // host-buffer requests: the grid's device slot (0 or 1), else -1
+    double *hu, *hp;       // host-buffer requests: where the results go
   };
+  // Host-buffer requests (cfdg_server_submit_host): per grid two device slots holding a
+  // request's u and p; the input copy runs on `cin`, the chunk that admits the request
+  // waits for it (`ready`), the result copy runs on `cout` after the epilogue, and `drained`
+  // marks a slot free again once its results reached host memory.
+  struct Slots {
+    double *u[2] = {nullptr, nullptr}, *p[2] = {nullptr, nullptr};
+    cudaEvent_t ready[2] = {nullptr, nullptr}, drained[2] = {nullptr, nullptr};
+    bool used[2] = {false, false};
+    bool busy[2] = {false, false};  // held by a request whose result copy is not yet issued
+    int next = 0;
+  };
+  std::vector<Slots> slots;
+  cudaStream_t cin = nullptr, cout = nullptr;
+  struct HostDone {
+    int grid, slot;
+  };
+  std::map<uint64_t, HostDone> copying;  // finished host requests whose results are in flight
   std::deque<Req> queue;
   std::vector<uint64_t> running;  // ticket per case, 0 when idle
+  std::vector<Req> running_req;  // the running request per case
   struct Done {
     cfdg_info info;
     int32_t code;
@@ -3325,6 +3345,15 @@ struct cfdg_server {
     if (ca) cudaEventDestroy(ca);
     if (cb) cudaEventDestroy(cb);
     if (epi) cudaEventDestroy(epi);
+    for (auto& g : slots)
+      for (int k = 0; k < 2; ++k) {
+        if (g.u[k]) cudaFree(g.u[k]);
+        if (g.p[k]) cudaFree(g.p[k]);
+        if (g.ready[k]) cudaEventDestroy(g.ready[k]);
+        if (g.drained[k]) cudaEventDestroy(g.drained[k]);
+      }
+    if (cin) cudaStreamDestroy(cin);
+    if (cout) cudaStreamDestroy(cout);
   }
 };
 
@@ -3558,6 +3587,7 @@ int cfdg_server_create(cfdg_context* ctx, cfdg_grid* const* grids, int32_t n, in
     return fail(CFDG_ERR_CUDA, "could not create the server's events");
   }
   S->running.assign(n, 0);
+  S->running_req.assign(n, cfdg_server::Req{});
   B->active.assign(n, 0);
   int e = 0;
   {
@@ -3608,7 +3638,45 @@ int cfdg_server_submit(cfdg_server* S, int32_t grid, double* d_u, double* d_p, d
     return fail(CFDG_ERR_INVALID, "invalid submit arguments");
   std::lock_guard<std::mutex> lk(S->mu);
   *ticket = S->next_ticket++;
-  S->queue.push_back({*ticket, grid, d_u, d_p, dt, tol, max_iter});
+  S->queue.push_back({*ticket, grid, d_u, d_p, dt, tol, max_iter, -1, nullptr, nullptr});
+  return 0;
+}
+
+int cfdg_server_submit_host(cfdg_server* S, int32_t grid, const double* u, const double* p, double* u_out,
+                            double* p_out, double dt, double tol, uint64_t max_iter, uint64_t* ticket) {
+  if (!S || grid < 0 || grid >= (int)S->B->grids.size() || !u || !p || !u_out || !p_out || !ticket)
+    return fail(CFDG_ERR_INVALID, "invalid submit arguments");
+  std::lock_guard<std::mutex> lk(S->mu);
+  cfdg_batch* B = S->B;
+  CU(cudaSetDevice(B->ctx->device));
+  if (!S->cin) {
+    CU(cudaStreamCreateWithFlags(&S->cin, cudaStreamNonBlocking));
+    CU(cudaStreamCreateWithFlags(&S->cout, cudaStreamNonBlocking));
+  }
+  if (S->slots.empty()) S->slots.resize(B->grids.size());
+  cfdg_server::Slots& g = S->slots[grid];
+  const size_t F = (size_t)B->h_fc[grid].F, N = (size_t)B->h_fc[grid].N;
+  const int k = g.next;
+  // A grid's requests run one at a time, so two slots let the next input copy overlap the
+  // running request; a slot whose results are still being copied out is waited for on the
+  // copy stream. A third request before either earlier one has finished has no slot.
+  if (g.busy[k])
+    return fail(CFDG_ERR_INVALID, "two host requests of this grid are unfinished; collect one before submitting");
+  if (!g.u[k]) {
+    CU(cudaMalloc(&g.u[k], F * sizeof(double)));
+    CU(cudaMalloc(&g.p[k], N * sizeof(double)));
+    CU(cudaEventCreateWithFlags(&g.ready[k], cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&g.drained[k], cudaEventDisableTiming));
+  }
+  if (g.used[k]) CU(cudaStreamWaitEvent(S->cin, g.drained[k], 0));
+  CU(cudaMemcpyAsync(g.u[k], u, F * sizeof(double), cudaMemcpyHostToDevice, S->cin));
+  CU(cudaMemcpyAsync(g.p[k], p, N * sizeof(double), cudaMemcpyHostToDevice, S->cin));
+  CU(cudaEventRecord(g.ready[k], S->cin));
+  g.used[k] = true;
+  g.busy[k] = true;
+  g.next = 1 - k;
+  *ticket = S->next_ticket++;
+  S->queue.push_back({*ticket, grid, g.u[k], g.p[k], dt, tol, max_iter, k, u_out, p_out});
   return 0;
 }
 
@@ -3658,11 +3726,27 @@ int cfdg_server_progress(cfdg_server* S, int32_t* finished) {
     CU(cudaEventRecord(S->epi, s));
   }
   std::vector<std::pair<uint64_t, cfdg_server::Done>> out;
+  bool any_host = false;
+  for (int i = 0; i < nc; ++i) any_host |= fin[i] && S->running_req[i].slot >= 0;
+  if (any_host && !any_done) CU(cudaEventRecord(S->epi, s));  // failed requests: their inputs go back
   for (int i = 0; i < nc; ++i) {
     if (!fin[i]) continue;
     cfdg_server::Done d;
     fill_info(B->h_st[i], d.info);
     d.code = B->h_st[i].state == DONE ? 0 : (B->h_st[i].error ? B->h_st[i].error : CFDG_E033);
+    const cfdg_server::Req& rq = S->running_req[i];
+    if (rq.slot >= 0) {
+      // The results (or, for a failed request, its unchanged inputs) to host memory once
+      // the epilogue has run; the ticket reports done when the copy has completed.
+      cfdg_server::Slots& g = S->slots[i];
+      const size_t F = (size_t)B->h_fc[i].F, N = (size_t)B->h_fc[i].N;
+      CU(cudaStreamWaitEvent(S->cout, S->epi, 0));
+      CU(cudaMemcpyAsync(rq.hu, g.u[rq.slot], F * sizeof(double), cudaMemcpyDeviceToHost, S->cout));
+      CU(cudaMemcpyAsync(rq.hp, g.p[rq.slot], N * sizeof(double), cudaMemcpyDeviceToHost, S->cout));
+      CU(cudaEventRecord(g.drained[rq.slot], S->cout));
+      g.busy[rq.slot] = false;
+      S->copying[S->running[i]] = {i, rq.slot};
+    }
     out.push_back({S->running[i], d});
     S->running[i] = 0;
     B->active[i] = 0;
@@ -3686,6 +3770,8 @@ int cfdg_server_progress(cfdg_server* S, int32_t* finished) {
     B->h_fc[i].dt = it->dt;
     B->h_st[i] = initial_state(it->tol, it->max_iter);
     S->running[i] = it->ticket;
+    S->running_req[i] = *it;
+    if (it->slot >= 0) CU(cudaStreamWaitEvent(s, S->slots[i].ready[it->slot], 0));  // its input copy
     ++S->admitted;
     admit[i] = 1;
     any_admit = true;
@@ -3723,6 +3809,13 @@ int cfdg_server_result(cfdg_server* S, uint64_t ticket, cfdg_info* info, int32_t
   std::lock_guard<std::mutex> lk(S->mu);
   auto it = S->results.find(ticket);
   if (it == S->results.end()) return CFDG_PENDING;
+  auto hc = S->copying.find(ticket);
+  if (hc != S->copying.end()) {  // a host-buffer request: done once its results are in host memory
+    const cudaError_t q = cudaEventQuery(S->slots[hc->second.grid].drained[hc->second.slot]);
+    if (q == cudaErrorNotReady) return CFDG_PENDING;
+    if (q != cudaSuccess) return fail(CFDG_ERR_CUDA, std::string("result copy: ") + cudaGetErrorString(q));
+    S->copying.erase(hc);
+  }
   if (info) *info = it->second.info;
   if (code) *code = it->second.code;
   S->results.erase(it);

@@ -500,6 +500,18 @@ class Server:
                                               float(dt), float(tol), int(max_iter), C.byref(t)))
         return t.value
 
+    def submit_host(self, grid_index: int, u_ptr: int, p_ptr: int, u_out_ptr: int, p_out_ptr: int, dt, tol,
+                    max_iter) -> int:
+        """Queues pressure::project of grid `grid_index` on host buffers given as raw pointers
+        (cfdg_server_submit_host): u (F doubles) and p (N doubles) in, the projected fields
+        (or the unchanged inputs on failure) into u_out and p_out before the ticket reports
+        done. Page-locked buffers let the copies overlap the solves."""
+        t = C.c_uint64()
+        self._check(self.L.cfdg_server_submit_host(self.h, int(grid_index), C.c_void_p(u_ptr), C.c_void_p(p_ptr),
+                                                   C.c_void_p(u_out_ptr), C.c_void_p(p_out_ptr), float(dt),
+                                                   float(tol), int(max_iter), C.byref(t)))
+        return t.value
+
     def set_chunk(self, iterations: int):
         """Iterations per graph chunk (cfdg_server_set_chunk)."""
         self._check(self.L.cfdg_server_set_chunk(self.h, int(iterations)))

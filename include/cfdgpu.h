@@ -311,6 +311,17 @@ int cfdg_server_set_stream(cfdg_server *server, void *stream);
 int cfdg_server_set_chunk(cfdg_server *server, int32_t iterations);
 int cfdg_server_submit(cfdg_server *server, int32_t grid, double *d_u, double *d_p, double dt, double tol,
                        uint64_t max_iter, uint64_t *ticket);
+/* The same request on host buffers: the engine copies u (F doubles) and p (N doubles) to
+ * one of two device slots of the grid on a copy stream of its own (the request starts once
+ * the copy is done), and after the request copies the projected fields, or on failure the
+ * unchanged inputs, into u_out and p_out on another copy stream; cfdg_server_result reports
+ * the ticket done only when those copies have completed. All four buffers must stay valid
+ * until then; page-locked host memory lets the copies overlap the solves. A grid's next
+ * input copy waits until the results of the request that last used its slot have been
+ * copied out; a third request of a grid while two are unfinished is CFDG_ERR_INVALID. The
+ * reference-facing form of serving: the caller's fields stay in host memory. */
+int cfdg_server_submit_host(cfdg_server *server, int32_t grid, const double *u, const double *p, double *u_out,
+                            double *p_out, double dt, double tol, uint64_t max_iter, uint64_t *ticket);
 int cfdg_server_progress(cfdg_server *server, int32_t *finished);
 /* 0 and the result (consumed) when the ticket finished, CFDG_PENDING otherwise. */
 int cfdg_server_result(cfdg_server *server, uint64_t ticket, cfdg_info *info, int32_t *code);

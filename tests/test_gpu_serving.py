@@ -210,3 +210,151 @@ def test_admission_by_hbm_budget_and_failed_requests(pkg):
     server.close()
     for d in dgs:
         d.close()
+
+
+def test_host_buffer_requests_equal_device_requests(pkg):
+    """cfdg_server_submit_host: the fields stay in host memory (page-locked for two grids,
+    ordinary pageable numpy memory for the third); the engine copies them to a device slot,
+    runs the request and copies the results back before the ticket reports done. Two
+    consecutive requests per grid (both device slots, the second fed with the first's
+    results plus a perturbation) give the same bits as the same requests submitted on
+    device arrays to another server; a failing request (E031) returns its inputs unchanged."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(9)
+    shapes = [(32, 32, 16), (40, 24, 16), (24, 24, 24)]
+    cases = [pkg.synth.case(sh, 2.0, inflow=5.0, preconditioner="multigrid",
+                            boxes=pkg.synth.random_boxes(rng, 2, [v * 2.0 for v in sh], side=(6.0, 14.0),
+                                                         height=(6.0, 20.0), dx=2.0)) for sh in shapes]
+    cases.append(pkg.synth.case((24, 12, 8), 1.0, preconditioner="multigrid", boxes=[((8, 0, 0), (9, 12, 8))]))
+    grids = [pkg.grid.Grid.build(c) for c in cases]
+    n = len(grids)
+    dev = torch.device("cuda", 0)
+    u0 = [pkg.synth.random_velocity(g, 50 + i) for i, g in enumerate(grids)]
+    noise = [np.where((g.face_kind == pkg.grid.INTERIOR) | (g.face_kind == pkg.grid.OUTLET),
+                      np.random.default_rng(200 + i).uniform(-0.05, 0.05, g.n_faces), 0.0) for i, g in enumerate(grids)]
+
+    def run(server, submit):
+        us, ps = [u.copy() for u in u0], [np.zeros(g.count) for g in grids]
+        outs = []
+        for step in range(2):
+            tickets = [submit(server, i, us[i], ps[i]) for i in range(n)]
+            got = [None] * n
+            for _ in range(1_000_000):
+                server.progress()
+                for i, (t, fetch) in enumerate(tickets):
+                    if got[i] is None and (r := server.result(t)) is not None:
+                        got[i] = (r[0],) + fetch()
+                if all(x is not None for x in got):
+                    break
+            outs.append(got)
+            us = [got[i][1] + noise[i] if got[i][0] == 0 else got[i][1] for i in range(n)]
+            ps = [got[i][2] for i in range(n)]
+        return outs
+
+    keep = []
+
+    def dev_submit(server, i, u, p):
+        du, dp = torch.from_numpy(u.copy()).to(dev), torch.from_numpy(p.copy()).to(dev)
+        torch.cuda.synchronize()
+        keep.append((du, dp))
+        t = server.submit(i, du.data_ptr(), dp.data_ptr(), 0.1, 1e-8, 10000)
+        return t, lambda: (du.cpu().numpy(), dp.cpu().numpy())
+
+    def host_submit(server, i, u, p):
+        if i == 2:  # pageable numpy buffers
+            hu, hp = u.copy(), p.copy()
+            ou, op = np.empty_like(hu), np.empty_like(hp)
+            ptrs = [a.ctypes.data for a in (hu, hp, ou, op)]
+            keep.append((hu, hp, ou, op))
+            t = server.submit_host(i, *ptrs, 0.1, 1e-8, 10000)
+            return t, lambda: (ou.copy(), op.copy())
+        hu, hp = torch.from_numpy(u.copy()).pin_memory(), torch.from_numpy(p.copy()).pin_memory()
+        ou, op = torch.empty_like(hu).pin_memory(), torch.empty_like(hp).pin_memory()
+        keep.append((hu, hp, ou, op))
+        t = server.submit_host(i, hu.data_ptr(), hp.data_ptr(), ou.data_ptr(), op.data_ptr(), 0.1, 1e-8, 10000)
+        return t, lambda: (ou.numpy().copy(), op.numpy().copy())
+
+    results = []
+    for submit in (dev_submit, host_submit):
+        dgs = [pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed") for g in grids]
+        server = pkg.pressure.Server(dgs, max_active=n)
+        results.append(run(server, submit))
+        server.close()
+        for d in dgs:
+            d.close()
+    dev_out, host_out = results
+    for step in range(2):
+        for i in range(n):
+            assert dev_out[step][i][0] == host_out[step][i][0], (step, i)
+            assert np.array_equal(bits(dev_out[step][i][1]), bits(host_out[step][i][1])), (step, i)
+            assert np.array_equal(bits(dev_out[step][i][2]), bits(host_out[step][i][2])), (step, i)
+        assert host_out[step][n - 1][0] == 31
+        assert all(host_out[step][i][0] == 0 for i in range(n - 1))
+    assert np.array_equal(bits(host_out[0][n - 1][1]), bits(u0[n - 1]))  # the failed request's inputs
+
+
+def test_host_buffer_requests_two_in_flight_per_grid(pkg):
+    """Two host requests of one grid in flight at once (both device slots): the second's
+    input copy overlaps the first's solve, a third before either finished is refused
+    (CFDG_ERR_INVALID), and once the first is done its slot takes the third. Each result
+    equals the same input served alone on device arrays, bit for bit."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(31)
+    shapes = [(32, 32, 16), (24, 40, 16)]
+    cases = [pkg.synth.case(sh, 2.0, inflow=5.0, preconditioner="multigrid",
+                            boxes=pkg.synth.random_boxes(rng, 2, [v * 2.0 for v in sh], side=(6.0, 14.0),
+                                                         height=(6.0, 20.0), dx=2.0)) for sh in shapes]
+    grids = [pkg.grid.Grid.build(c) for c in cases]
+    n = len(grids)
+    dev = torch.device("cuda", 0)
+    inputs = [[pkg.synth.random_velocity(g, 300 + 10 * i + k) for k in range(3)] for i, g in enumerate(grids)]
+
+    def drain(server, tickets):
+        out = {}
+        for _ in range(1_000_000):
+            server.progress()
+            for t in tickets:
+                if t not in out and (r := server.result(t)) is not None:
+                    out[t] = r[0]
+            if len(out) == len(tickets):
+                return out
+        raise AssertionError("requests did not finish")
+
+    dgs = [pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed") for g in grids]
+    server = pkg.pressure.Server(dgs, max_active=n)
+    want = [[None] * 3 for _ in range(n)]
+    for i in range(n):
+        for k in range(3):
+            du = torch.from_numpy(inputs[i][k]).to(dev)
+            dp = torch.zeros(grids[i].count, dtype=torch.float64, device=dev)
+            torch.cuda.synchronize()
+            t = server.submit(i, du.data_ptr(), dp.data_ptr(), 0.1, 1e-8, 10000)
+            assert drain(server, [t])[t] == 0
+            want[i][k] = (du.cpu().numpy(), dp.cpu().numpy())
+    server.close()
+
+    server = pkg.pressure.Server(dgs, max_active=n)
+    bufs = [[[torch.from_numpy(inputs[i][k]).pin_memory(), torch.zeros(g.count, dtype=torch.float64).pin_memory(),
+              torch.empty(g.n_faces, dtype=torch.float64).pin_memory(),
+              torch.empty(g.count, dtype=torch.float64).pin_memory()] for k in range(3)]
+            for i, g in enumerate(grids)]
+
+    def submit(i, k):
+        return server.submit_host(i, *[b.data_ptr() for b in bufs[i][k]], 0.1, 1e-8, 10000)
+
+    first = [[submit(i, 0), submit(i, 1)] for i in range(n)]
+    for i in range(n):
+        with pytest.raises(pkg.pressure.PressureError) as e:
+            submit(i, 2)
+        assert e.value.code == 203
+    codes = drain(server, [first[i][0] for i in range(n)])
+    third = [submit(i, 2) for i in range(n)]
+    codes.update(drain(server, [first[i][1] for i in range(n)] + third))
+    assert all(c == 0 for c in codes.values())
+    server.close()
+    for d in dgs:
+        d.close()
+    for i in range(n):
+        for k in range(3):
+            assert np.array_equal(bits(bufs[i][k][2].numpy()), bits(want[i][k][0])), (i, k)
+            assert np.array_equal(bits(bufs[i][k][3].numpy()), bits(want[i][k][1])), (i, k)
