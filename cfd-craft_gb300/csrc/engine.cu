@@ -1486,9 +1486,13 @@ int prepare_mg_impl(cfdg_grid* G, const Poller& poll, cfdg_info* info) {
     G->mixed.reset();
     G->solo.reset();
     reset_chunk(G);
+    const auto t0 = std::chrono::steady_clock::now();
     if (int e = build_mg_dev(G, poll)) return e;
     G->signature = std::make_unique<Signature>(std::move(cur));
-    if (info) info->hierarchy_builds = 1;
+    if (info) {
+      info->hierarchy_builds = 1;
+      info->multigrid_setup_seconds = seconds_since(t0);
+    }
   }
   G->sig_version = G->faces_version;
   if (info) {
@@ -1505,7 +1509,9 @@ int prepare_preconditioner(cfdg_grid* G, const Poller& poll, cfdg_info* info) {
   if (G->preconditioner == CFDG_PRECOND_MULTIGRID) return prepare_mg_impl(G, poll, info);
   if (!G->ic0) {
     reset_chunk(G);
+    const auto t0 = std::chrono::steady_clock::now();
     if (int e = build_ic0_dev(G)) return e;
+    if (info) info->factor_setup_seconds = seconds_since(t0);
   }
   return 0;
 }
@@ -1660,13 +1666,16 @@ int project_mixed(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol,
   cfdg_info* inf = info ? info : &local;
   std::memset(inf, 0, sizeof(*inf));
   if (int e = prepare_mg_impl(G, poll, inf)) return e;
+  double setup = inf->multigrid_setup_seconds;
   if (!G->solo) {
+    const auto t0 = std::chrono::steady_clock::now();
     cfdg_batch* B = cfdg_mixed_new(G->ctx);
     if (!B) return fail(CFDG_ERR_CUDA, "could not create the mixed-form stream");
     std::shared_ptr<cfdg_batch> solo(B, cfdg_mixed_delete);
     if (int e = cfdg_mixed_add_case(B, G)) return e;
     if (int e = cfdg_mixed_pack(B)) return e;
     G->solo = solo;
+    setup += seconds_since(t0);
   }
   cfdg_mixed_set_stream(G->solo.get(), G->stream);
   int32_t code = 0;
@@ -1677,6 +1686,7 @@ int project_mixed(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol,
   inf->hierarchy_builds = builds, inf->hierarchy_levels = levels, inf->hierarchy_cells = cells;
   inf->hierarchy_nonzeros = nnz;
   inf->hierarchy_bytes = hbytes;
+  inf->multigrid_setup_seconds = setup;
   if (code == CFDG_E031) return fail(code, "CFD-E031: incompatible flux in a closed fluid component");
   if (code == CFDG_E032) return fail(code, "CFD-E032: pressure CG lost positive definiteness");
   if (code == CFDG_E033) return fail(code, "CFD-E033: pressure iteration limit " + std::to_string(max_iter));

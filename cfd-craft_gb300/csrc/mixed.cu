@@ -116,6 +116,7 @@ struct FineCase {
   double* u;
   double* pfield;
   double dt;
+  double rdt;  // RN(1/dt) for div_rdt, 0 when dt lies outside [2^-60, 2^60]
   const uint8_t* fkind;
   const int *flo, *fhi;
   const double* fdist;
@@ -246,9 +247,24 @@ __device__ __forceinline__ double exact_recip(double y) {
   if ((b & (long long)0x800fffffffffffffull) != 0 || e < 1 || e > 2045) return 0.0;
   return __longlong_as_double((long long)(2046 - e) << 52);
 }
-__device__ __forceinline__ double div_exact(double x, double y) {
-  const double r = exact_recip(y);
-  return r != 0.0 ? __dmul_rn(x, r) : __ddiv_rn(x, y);
+
+// x / y rounded to nearest from ry = RN(1/y), by Markstein's correction step (P. Markstein,
+// IBM J. Res. Dev. 34(1), 1990; restated as a theorem in Muller et al., Handbook of
+// Floating-Point Arithmetic): q = RN(x ry) lies within one ulp of x/y, rem = x - q y is
+// exact under one FMA, and RN(q + rem ry) is RN(x/y) when nothing underflows or overflows.
+// With y in [2^-60, 2^60] (else ry = 0) and |x| in [2^-900, 2^900] every intermediate stays
+// normal; zeros, subnormals, NaN, infinities and x outside that range take the division.
+__device__ __forceinline__ double div_rdt(double x, double y, double ry) {
+  const int e = (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+  if (ry == 0.0 || e < 123 || e > 1923) return __ddiv_rn(x, y);
+  const double q = __dmul_rn(x, ry);
+  const double rem = __fma_rn(-q, y, x);
+  return __fma_rn(rem, ry, q);
+}
+
+// The host side of div_rdt: RN(1/dt), or 0 outside the range the device step assumes.
+inline double rdt_of(double dt) {
+  return (dt >= 0x1p-60 && dt <= 0x1p60) ? 1.0 / dt : 0.0;
 }
 
 __device__ __forceinline__ long long fidx(const FineCase& F, int a, int i, int j, int k) {
@@ -272,6 +288,12 @@ __device__ __forceinline__ double mulw(double w, int k, double d) {
     if ((b & 0x7fffffffffffffffLL) == 0) return d;
   }
   return __dmul_rn(w, d);
+}
+// x / y bit for bit: for y a power of two the exponent field of x moved (mulw), else the
+// division.
+__device__ __forceinline__ double div_p2(double x, double y) {
+  const double r = exact_recip(y);
+  return r != 0.0 ? mulw(r, pow2_k(r), x) : __ddiv_rn(x, y);
 }
 
 // FP64 operator with every product and sum rounded as written, in the reference's
@@ -1912,11 +1934,11 @@ __device__ __forceinline__ void b_rhs(const FineCase* FC, MState* ST, const int2
       const double ul = F.u[fidx(F, a, p[0], p[1], p[2])];
       p[a] += 1;
       const double uu = F.u[fidx(F, a, p[0], p[1], p[2])];
-      div = __dadd_rn(div, div_exact(__dsub_rn(uu, ul), F.dx[a]));
-      if (closed) scale = __dadd_rn(scale, div_exact(__dadd_rn(fabs(ul), fabs(uu)), F.dx[a]));
+      div = __dadd_rn(div, div_p2(__dsub_rn(uu, ul), F.dx[a]));
+      if (closed) scale = __dadd_rn(scale, div_p2(__dadd_rn(fabs(ul), fabs(uu)), F.dx[a]));
     }
-    F.b[c] = __ddiv_rn(-div, F.dt);
-    F.terms[c] = closed ? __ddiv_rn(scale, F.dt) : 0.0;
+    F.b[c] = div_rdt(-div, F.dt, F.rdt);
+    F.terms[c] = closed ? div_rdt(scale, F.dt, F.rdt) : 0.0;
   }
 }
 __global__ void __launch_bounds__(TILE) k_rhs(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
@@ -1981,8 +2003,8 @@ __global__ void k_correct(const FineCase* FC, const MState* ST, const int2* ftil
       if (ff >= F.F) break;
       double d;
       const uint8_t k = F.fkind[ff];
-      if (k == INTERIOR) d = div_exact(__dsub_rn(F.x64[F.fhi[ff]], F.x64[F.flo[ff]]), F.fdist[ff]);
-      else if (k == OUTLET) d = F.flo[ff] >= 0 ? div_exact(-F.x64[F.flo[ff]], F.fdist[ff]) : div_exact(F.x64[F.fhi[ff]], F.fdist[ff]);
+      if (k == INTERIOR) d = div_p2(__dsub_rn(F.x64[F.fhi[ff]], F.x64[F.flo[ff]]), F.fdist[ff]);
+      else if (k == OUTLET) d = F.flo[ff] >= 0 ? div_p2(-F.x64[F.flo[ff]], F.fdist[ff]) : div_p2(F.x64[F.fhi[ff]], F.fdist[ff]);
       else d = 0.0;
       F.u[ff] = __dsub_rn(F.u[ff], __dmul_rn(F.dt, d));
     }
@@ -3161,6 +3183,7 @@ int cfdg_mixed_project(cfdg_batch* B, double* const* d_u, double* const* d_p, co
     B->h_fc[i].u = d_u[i];
     B->h_fc[i].pfield = d_p[i];
     B->h_fc[i].dt = dt[i];
+    B->h_fc[i].rdt = rdt_of(dt[i]);
   }
   CU(cudaMemcpyAsync(B->d_fc, B->h_fc.data(), sizeof(FineCase) * nc, cudaMemcpyHostToDevice, s));
   std::vector<MState> st(nc, initial_state(tol, max_iter));
@@ -3357,7 +3380,58 @@ struct cfdg_server {
   }
 };
 
+// Checks div_rdt against the correctly rounded division on generated numerators: mode 0
+// random significands over the exponents div_rdt takes, mode 1 products RN(y m) (quotients
+// next to a double), mode 2 quotients next to the midpoint between two doubles.
+__global__ void k_div_check(double y, double ry, unsigned long long seed, long long n, int mode,
+                            unsigned long long* bad) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    unsigned long long z = seed + 0x9e3779b97f4a7c15ull * (unsigned long long)(i + 1);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    z ^= z >> 31;
+    const unsigned long long mant = z & 0xfffffffffffffull, sign = (z >> 63) << 63;
+    const int e = 123 + (int)((z >> 52) % 1801ull);
+    double x = __longlong_as_double((long long)(sign | ((unsigned long long)e << 52) | mant));
+    if (mode > 0) {
+      // m near 1 so that x = y m stays within the exponent range for every y in [2^-60, 2^60]
+      const double m = __longlong_as_double((long long)(sign | (1023ull << 52) | mant));
+      x = mode == 1 ? __dmul_rn(y, m) : __fma_rn(y, m, __dmul_rn(y, __dmul_rn(m, 0x1p-53)));
+    }
+    const double a = div_rdt(x, y, ry), b = __ddiv_rn(x, y);
+    if (__double_as_longlong(a) != __double_as_longlong(b)) atomicAdd(bad, 1ull);
+  }
+}
+
 extern "C" {
+
+int cfdg_debug_div_check(double y, uint64_t seed, int64_t n, int32_t mode, uint64_t* mismatches) {
+  if (n < 1 || mode < 0 || mode > 2 || !mismatches) return fail(CFDG_ERR_INVALID, "invalid arguments");
+  unsigned long long* d = nullptr;
+  CU(cudaMalloc(&d, sizeof(unsigned long long)));
+  CU(cudaMemset(d, 0, sizeof(unsigned long long)));
+  k_div_check<<<4 * 152, 256>>>(y, rdt_of(y), seed, n, mode, d);
+  const cudaError_t le = cudaGetLastError();
+  unsigned long long h = 0;
+  const cudaError_t ce = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  CU(le);
+  CU(ce);
+  *mismatches = h;
+  return 0;
+}
+
+int cfdg_batch_debug_rhs(cfdg_batch* B, int32_t c, double* b, double* terms) {
+  if (!B || c < 0 || c >= (int)B->grids.size() || !b || !terms) return fail(CFDG_ERR_INVALID, "invalid arguments");
+  CU(cudaSetDevice(B->ctx->device));
+  Locks locks(B->grids);
+  const FineCase& F = B->h_fc[c];
+  if (!F.b) return fail(CFDG_ERR_INVALID, "the batch has not projected yet");
+  CU(cudaStreamSynchronize(B->stream));
+  CU(cudaMemcpy(b, F.b, sizeof(double) * F.N, cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(terms, F.terms, sizeof(double) * F.N, cudaMemcpyDeviceToHost));
+  return 0;
+}
 
 int cfdg_batch_create(cfdg_context* ctx, cfdg_grid* const* grids, int32_t n, cfdg_batch** out) {
   if (!ctx || !grids || n < 1 || !out) return fail(CFDG_ERR_INVALID, "invalid batch arguments");
@@ -3478,13 +3552,20 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
   Locks locks(B->grids);
   const int nc = (int)B->cases.size();
   cudaStream_t s = B->stream;
-  // Every case in the inner-iteration state, on the vectors of the last solve.
+  if (which == 6)
+    for (int i = 0; i < nc; ++i)
+      if (B->h_fc[i].u != B->grids[i]->u)
+        return fail(CFDG_ERR_INVALID, "time the right-hand side after a host-buffer projection of the batch");
+  // Every case in the inner-iteration state, on the vectors of the last solve (the FP64
+  // true residual: every case in an outer step with a correction; the right-hand side:
+  // every case idle, on the batch's own copy of the last inputs).
   std::vector<MState> saved(nc), run(nc);
   CU(cudaMemcpyAsync(saved.data(), B->d_st, sizeof(MState) * nc, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
   for (int i = 0; i < nc; ++i) {
     run[i] = saved[i];
-    run[i].state = RUN;
+    run[i].state = which == 5 ? OUTER : which == 6 ? IDLE : RUN;
+    run[i].has_e = 1;
     run[i].counter = 0;
   }
   CU(cudaMemcpyAsync(B->d_st, run.data(), sizeof(MState) * nc, cudaMemcpyHostToDevice, s));
@@ -3507,6 +3588,12 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
       case 2:  // all coarse levels of all cases
         launch_coarse(B, s);
         break;
+      case 5:  // FP64 true residual r = b_c - A x with |r|^2
+        FINE(k_outer_resid, B->run);
+        break;
+      case 6:  // FP64 right-hand side b = -div(u)/dt
+        FINE(k_rhs, B->run);
+        break;
       default:
         enqueue_vcycle(B, s);
         break;
@@ -3515,14 +3602,33 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
   if (which == 0 || which == 4) bytes = 9.0 * cells;  // half the cells: rhs, 1/diag, u16 flags, x out; the other half's x in
   else if (which == 1) bytes = 10.0 * cells; // p in, u16 flags, q out
   else if (which == 2) bytes = coarse_bytes(B);
-  launch();
-  launch();
-  CU(cudaEventRecord(B->ev0, s));
-  for (int r = 0; r < reps; ++r) launch();
-  CU(cudaEventRecord(B->ev1, s));
-  CU(cudaEventSynchronize(B->ev1));
+  else if (which == 5) bytes = 26.0 * cells;  // x, b_c, r out (FP64), u16 flags
+  else if (which == 6) {
+    for (auto& F : B->h_fc) bytes += 8.0 * (double)F.F + 17.0 * F.N;  // u faces, fluid, b and terms out
+  }
   float ms = 0;
-  CU(cudaEventElapsedTime(&ms, B->ev0, B->ev1));
+  if (which == 5 || which == 6) {
+    // These kernels move the cases' states on: restore them before every launch and time
+    // the launches alone.
+    for (int r = -2; r < reps; ++r) {
+      CU(cudaMemcpyAsync(B->d_st, run.data(), sizeof(MState) * nc, cudaMemcpyHostToDevice, s));
+      CU(cudaEventRecord(B->ev0, s));
+      launch();
+      CU(cudaEventRecord(B->ev1, s));
+      CU(cudaEventSynchronize(B->ev1));
+      float one = 0;
+      CU(cudaEventElapsedTime(&one, B->ev0, B->ev1));
+      if (r >= 0) ms += one;
+    }
+  } else {
+    launch();
+    launch();
+    CU(cudaEventRecord(B->ev0, s));
+    for (int r = 0; r < reps; ++r) launch();
+    CU(cudaEventRecord(B->ev1, s));
+    CU(cudaEventSynchronize(B->ev1));
+    CU(cudaEventElapsedTime(&ms, B->ev0, B->ev1));
+  }
   CU(cudaMemcpyAsync(B->d_st, saved.data(), sizeof(MState) * nc, cudaMemcpyHostToDevice, s));
   CU(cudaStreamSynchronize(s));
   CU(cudaGetLastError());
@@ -3768,6 +3874,7 @@ int cfdg_server_progress(cfdg_server* S, int32_t* finished) {
     B->h_fc[i].u = it->u;
     B->h_fc[i].pfield = it->p;
     B->h_fc[i].dt = it->dt;
+    B->h_fc[i].rdt = rdt_of(it->dt);
     B->h_st[i] = initial_state(it->tol, it->max_iter);
     S->running[i] = it->ticket;
     S->running_req[i] = *it;

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -20,6 +21,10 @@ namespace cfdg {
 extern thread_local std::string t_error;  // last error message of the calling thread
 extern std::atomic<uint64_t> g_launches;   // kernels enqueued by this library (graph launches count their nodes)
 inline void count(uint64_t k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+inline double seconds_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
 
 inline int fail(int code, const std::string& msg) {
   t_error = msg;

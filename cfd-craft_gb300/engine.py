@@ -30,7 +30,8 @@ EXPORTS = (
     "cfdg_batch_destroy", "cfdg_batch_set_stream", "cfdg_batch_size", "cfdg_batch_project", "cfdg_batch_project_device",
     "cfdg_batch_time_kernel", "cfdg_batch_stats_json", "cfdg_server_create", "cfdg_server_destroy", "cfdg_server_set_stream",
     "cfdg_server_submit", "cfdg_server_progress", "cfdg_server_result", "cfdg_server_pending", "cfdg_server_stats_json", "cfdg_server_set_chunk", "cfdg_grid_set_cycle", "cfdg_grid_set_coarse_scale", "cfdg_grid_set_flow", "cfdg_step_device", "cfdg_scalar_step_device", "cfdg_receptors_set", "cfdg_receptors_sample", "cfdg_debug_momentum_update",
-    "cfdg_debug_wave_stall", "cfdg_grid_set_sweep_tile", "cfdg_server_submit_host",
+    "cfdg_debug_wave_stall", "cfdg_grid_set_sweep_tile", "cfdg_server_submit_host", "cfdg_batch_debug_rhs",
+    "cfdg_debug_div_check",
 )
 
 
@@ -81,6 +82,8 @@ class Info(C.Structure):
         ("block_smoothing_cell_updates", C.c_uint64),
         ("block_solves", C.c_uint64),
         ("block_level_cell_visits", C.c_uint64),
+        ("factor_setup_seconds", C.c_double),
+        ("multigrid_setup_seconds", C.c_double),
     ]
 
     def as_dict(self):
@@ -154,6 +157,8 @@ def load(path: str = LIB_PATH):
         L.cfdg_server_pending.argtypes = [P]
         L.cfdg_batch_time_kernel.argtypes = [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.cfdg_batch_size.argtypes = [P]
+        L.cfdg_batch_debug_rhs.argtypes = [P, C.c_int32, P, P]
+        L.cfdg_debug_div_check.argtypes = [C.c_double, C.c_uint64, C.c_int64, C.c_int32, C.POINTER(C.c_uint64)]
         L.cfdg_batch_stats_json.argtypes = [P, C.c_char_p, C.c_int64]
         L.cfdg_batch_stats_json.restype = C.c_int64
         L.cfdg_server_stats_json.argtypes = [P, C.c_char_p, C.c_int64]

@@ -459,6 +459,14 @@ class Batch:
             raise PressureError(rc, E.last_error())
         return ms.value, b.value
 
+    def debug_rhs(self, c: int, n_cells: int):
+        """(b, terms) of case c's last projection (cfdg_batch_debug_rhs)."""
+        b, t = np.empty(n_cells), np.empty(n_cells)
+        rc = self.L.cfdg_batch_debug_rhs(self.h, int(c), _vp(b), _vp(t))
+        if rc:
+            raise PressureError(rc, E.last_error())
+        return b, t
+
 
 class Server:
     """Continuous-batching projection server over resident grids (cfdg_server)."""

@@ -116,6 +116,12 @@ typedef struct {
   uint64_t block_smoothing_cell_updates; /* cell updates of line/plane block sweeps */
   uint64_t block_solves;        /* exact line or plane block solves */
   uint64_t block_level_cell_visits; /* cells of the block-smoothed levels per visit */
+  /* The setup spans (profiling.rs Phase::PressureFactorSetup / PressureMultigridSetup,
+   * pressure.rs:60-63,79-83): host wall seconds of building the IC(0) factor, and of
+   * (re)building the multigrid hierarchy with its upload (plus, in the mixed form, the
+   * first build of its FP32 state), inside this call; 0 when the cached one was used. */
+  double factor_setup_seconds;
+  double multigrid_setup_seconds;
 } cfdg_info;
 
 /* Control::check (solver.rs:122-140): 0 continue, 1 "cancelled", 2 "wall_time_limit".
@@ -272,8 +278,11 @@ int cfdg_batch_project(cfdg_batch *batch, double *const *u, double *const *p, co
 /* Times one unit of the batch's work `reps` times with CUDA events on the batch's
  * stream, every case in its inner-iteration state: which = 0 one red-black half sweep
  * over all fine levels, 1 the FP32 operator, 2 all coarse levels (one cooperative launch), 3 one
- * V-cycle, 4 the half sweep of 0 with the unstaged register kernel. Reports the mean duration and the unit's algorithmic bytes (0 when not
- * stated). Diagnostic; no reference counterpart. */
+ * V-cycle, 4 the half sweep of 0 with the unstaged register kernel, 5 the FP64 true
+ * residual of every case, 6 the FP64 right-hand side of every case (only after a
+ * host-buffer cfdg_batch_project, whose inputs the batch keeps). Reports the mean duration
+ * and the unit's algorithmic bytes (0 when not stated). Diagnostic; no reference
+ * counterpart. */
 int cfdg_batch_time_kernel(cfdg_batch *batch, int32_t which, int32_t reps, double *ms_per_launch,
                            double *algorithmic_bytes);
 /* Per case and coarse level of the batch's FP32 hierarchies, as JSON: rows, nonzeros,
@@ -283,6 +292,15 @@ int cfdg_batch_time_kernel(cfdg_batch *batch, int32_t which, int32_t reps, doubl
  * at most cap bytes (NUL-terminated) and returns the length the full text needs, or a
  * negative error code. Diagnostic; no reference counterpart. */
 int64_t cfdg_batch_stats_json(cfdg_batch *batch, char *buf, int64_t cap);
+/* Copies case c's FP64 right-hand side b = -div(u)/dt and its round-off terms (0 unless
+ * the grid has closed components) of the batch's last projection to host arrays of N
+ * doubles. Diagnostic (parity of the mixed form's right-hand side); no reference counterpart. */
+int cfdg_batch_debug_rhs(cfdg_batch *batch, int32_t c, double *b, double *terms);
+/* Counts the numerators x, of n generated from seed (mode 0 random over 2^+-900, 1 next to
+ * y times a double, 2 next to y times a midpoint), whose quotient x / y by the engine's
+ * division from a precomputed reciprocal differs in any bit from the correctly rounded
+ * division. Diagnostic; no reference counterpart. */
+int cfdg_debug_div_check(double y, uint64_t seed, int64_t n, int32_t mode, uint64_t *mismatches);
 /* The same on device arrays d_u[i] (F_i doubles) and d_p[i] (N_i doubles). */
 int cfdg_batch_project_device(cfdg_batch *batch, double *const *d_u, double *const *d_p, const double *dt,
                               double tol, uint64_t max_iter, cfdg_poll_fn poll, void *poll_ctx, cfdg_info *infos,

@@ -243,3 +243,47 @@ def test_staged_half_sweeps_equal_register_sweeps(pkg):
         assert results["staged"][2][k] == results["register"][2][k]
         assert np.array_equal(bits(results["staged"][0][k]), bits(results["register"][0][k])), k
         assert np.array_equal(bits(results["staged"][1][k]), bits(results["register"][1][k])), k
+
+
+@pytest.mark.parametrize("y", [0.1, 0.05, 0.3, 1.0 / 3.0, 0.7, 0.037, 1.0 - 2.0 ** -53, 1.0 + 2.0 ** -52,
+                               2.0 - 2.0 ** -51, 0.25, 2.0 ** -60, 2.0 ** 60, 12345.678, 9.87e-15])
+def test_division_from_reciprocal_is_correctly_rounded(pkg, y):
+    """The mixed right-hand side divides by dt through a reciprocal and one correction step
+    (Markstein's); every quotient equals CUDA's correctly rounded division, bit for bit, on
+    random numerators and on numerators whose quotients lie next to a double or next to a
+    midpoint between two doubles."""
+    import ctypes as C
+
+    L = pkg.engine.load()
+    for mode in range(3):
+        bad = C.c_uint64()
+        assert L.cfdg_debug_div_check(y, 1234 + mode, 1 << 22, mode, C.byref(bad)) == 0, pkg.engine.last_error()
+        assert bad.value == 0, (y, mode, bad.value)
+
+
+def test_mixed_rhs_bitwise_against_oracle(pkg, O):
+    """b = -div(u)/dt of the mixed form (power-of-two face spacings as exponent shifts, the
+    division by dt from its reciprocal) equals the oracle's projection right-hand side bit
+    for bit; the round-off terms too where the grid has closed components (the mixed form
+    forms them only there)."""
+    cases = mixed_cases(pkg)
+    names = ["buildings-64x64x32", "pocket", "odd-37x29x21"]
+    grids = [pkg.grid.Grid.build(cases[n]) for n in names]
+    ogs = [O.Grid(cases[n]) for n in names]
+    dgs = [pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed") for g in grids]
+    batch = pkg.pressure.Batch(dgs)
+    for dts in ([0.1, 0.037, 0.25], [1.0 / 3.0, 0.1, 0.7]):
+        us = [pkg.synth.random_velocity(g, 70 + i) for i, g in enumerate(grids)]
+        res = batch.project([u.copy() for u in us], [np.zeros(g.count) for g in grids], dts, 1e-8, 10000)
+        for i, g in enumerate(grids):
+            b, terms = batch.debug_rhs(i, g.count)
+            ob, oterms = ogs[i].projection_rhs(us[i], dts[i])
+            assert np.array_equal(bits(b), bits(ob)), (names[i], dts[i])
+            if not all(g.anchored):
+                assert np.array_equal(bits(terms), bits(oterms)), (names[i], dts[i])
+            else:
+                assert not np.any(terms)
+        assert res[1][0] in (0, 31)  # the pocket may be incompatible for a random field
+    batch.close()
+    for d in dgs:
+        d.close()

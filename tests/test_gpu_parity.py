@@ -232,6 +232,46 @@ def test_changed_faces_rebuild_multigrid_and_keep_ic0(pkg, O):
         dg.close()
 
 
+def test_setup_spans_only_when_built(pkg, O):
+    """factor_setup_seconds / multigrid_setup_seconds (Phase::PressureFactorSetup and
+    PressureMultigridSetup, pressure.rs:60-63,79-83) are positive in the call that builds
+    the factor or (re)builds the hierarchy and 0 in calls that use the cached one; the
+    IC(0) factor survives changed faces, the hierarchy does not."""
+    c = periodic_case([5, 4, 3], "open", True)
+    for pre in ("ic0", "multigrid"):
+        g, og, dg = open_pair(pkg, O, c, pre)
+        b = og.apply(sin_field(g.count))
+        spans = []
+        for step in range(3):
+            if step == 2:
+                area = g.face_area * (1.0 + (np.arange(g.n_faces) % 5) * 0.03)
+                dg.update_faces(area=area)
+            _, info = dg.solve_scaled(b, None, 1e-10, 2000)
+            spans.append((info.work["factor_setup_seconds"], info.work["multigrid_setup_seconds"],
+                          info.work["hierarchy_builds"]))
+        dg.close()
+        if pre == "ic0":
+            assert spans[0][0] > 0 and spans[1][0] == 0 and spans[2][0] == 0, spans
+            assert all(s[1] == 0 for s in spans), spans
+        else:
+            assert [s[2] for s in spans] == [1, 0, 1], spans
+            assert spans[0][1] > 0 and spans[1][1] == 0 and spans[2][1] > 0, spans
+            assert all(s[0] == 0 for s in spans), spans
+    # The mixed form: the first projection builds the hierarchy and the FP32 state.
+    cm = pkg.synth.case((32, 16, 16), 2.0, inflow=5.0, preconditioner="multigrid",
+                        boxes=[((8, 0, 0), (12, 6, 8))])
+    gm = pkg.grid.Grid.build(cm)
+    dm = pkg.pressure.DeviceGrid(gm, preconditioner="multigrid", precision="mixed")
+    u = pkg.synth.random_velocity(gm, 3)
+    got = []
+    for _ in range(2):
+        p = np.zeros(gm.count)
+        info = dm.project(u.copy(), p, 0.1, 1e-8, 1000)
+        got.append((info.work["multigrid_setup_seconds"], info.work["hierarchy_builds"]))
+    dm.close()
+    assert got[0][0] > 0 and got[0][1] == 1 and got[1] == (0.0, 0), got
+
+
 # The 18 anisotropic shapes of docs/evidence/anisotropic-pressure.md (line/plane block
 # smoothing and semicoarsening, multigrid/line.rs) through the plain form's multigrid.
 
