@@ -379,6 +379,22 @@ __device__ __forceinline__ bool warp_row(const FineCase& F, int lt, int warp, in
 
 // FP32 error-free transformations: a running sum (hi, lo) of exact products keeps
 // about twice the FP32 significand, so a thread's few terms convert to FP64 once.
+// Compensated running sum (hi, lo) += v (Knuth's TwoSum).
+__device__ __forceinline__ void dd_add(float v, float& hi, float& lo) {
+  const float s = hi + v;
+  const float bb = s - hi;
+  lo += (hi - (s - bb)) + (v - bb);
+  hi = s;
+}
+// Sum of the outlet-face weights of a cell whose outlet bits (x-lo ... z-hi) are ob.
+template <class FC>
+__device__ __forceinline__ float outlet_sum(const FC& F, unsigned ob) {
+  float w = 0.0f;
+#pragma unroll
+  for (int f = 0; f < 6; ++f)
+    if (ob & (1u << f)) w += F.wo32[f >> 1];
+  return w;
+}
 __device__ __forceinline__ void dd_add_prod(float a, float b, float& hi, float& lo) {
   const float p = a * b;
   const float pe = fmaf(a, b, -p);
@@ -524,21 +540,19 @@ __device__ __forceinline__ void b_op(const FineCase* FC, MState* ST, const int2 
         P.load(F.p, oth, s2, par, nxh_, sy, sz, hy0, hy1, hz0, hz1);
         float nb[6];
         float2 y = make_float2(0.0f, 0.0f);
+        // Interior faces in face order, each through a selected weight (0 where the face
+        // is not interior) instead of a branch; the rare outlet faces after them.
         P.of(0, par, nb);
 #pragma unroll
-        for (int f = 0; f < 6; ++f) {
-          if (fl2 & (1u << f)) y.x = fmaf(F.w32[f >> 1], pc.x - nb[f], y.x);
-          else if (fl2 & (1u << (6 + f))) y.x = fmaf(F.wo32[f >> 1], pc.x, y.x);
-        }
+        for (int f = 0; f < 6; ++f) y.x = fmaf((fl2 & (1u << f)) ? F.w32[f >> 1] : 0.0f, pc.x - nb[f], y.x);
+        if (fl2 & 0xfc0u) y.x = fmaf(outlet_sum(F, fl2 >> 6), pc.x, y.x);
         P.of(1, par, nb);
 #pragma unroll
-        for (int f = 0; f < 6; ++f) {
-          if (fl2 & (1u << (16 + f))) y.y = fmaf(F.w32[f >> 1], pc.y - nb[f], y.y);
-          else if (fl2 & (1u << (22 + f))) y.y = fmaf(F.wo32[f >> 1], pc.y, y.y);
-        }
+        for (int f = 0; f < 6; ++f) y.y = fmaf((fl2 & (1u << (16 + f))) ? F.w32[f >> 1] : 0.0f, pc.y - nb[f], y.y);
+        if (fl2 & 0xfc00000u) y.y = fmaf(outlet_sum(F, fl2 >> 22), pc.y, y.y);
         *reinterpret_cast<float2*>(F.q + own + s2) = y;
-        dd_add_prod(pc.x, y.x, hi, lo);
-        dd_add_prod(pc.y, y.y, hi, lo);
+        // p.q: the pair's two products in one FMA, then a compensated running sum.
+        dd_add(fmaf(pc.x, y.x, pc.y * y.y), hi, lo);
       }
     }
   } else if (warp_row(F, lt, warp, j, k, rb)) {
@@ -557,7 +571,7 @@ __device__ __forceinline__ void b_op(const FineCase* FC, MState* ST, const int2 
   }
   tile_partial((double)hi + (double)lo, F, lt, sh, seg_n);
 }
-__global__ void __launch_bounds__(TILE, 6) k_op(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
+__global__ void __launch_bounds__(TILE, 5) k_op(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   __shared__ double sh[32];
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
@@ -3361,12 +3375,18 @@ struct cfdg_server {
   // Observability: graph chunks, their device time (events around each launch, read at
   // the next progress), host time inside progress, cases finished and admitted.
   cudaEvent_t ca = nullptr, cb = nullptr, epi = nullptr;
-  bool timing = false;
+  // Between consecutive chunks: the end of the earlier one (pcb) to the start of the next
+  // (ca), i.e. epilogues, prologues and the device waiting on the host.
+  cudaEvent_t pcb = nullptr;
+  bool timing = false, gap_timing = false;
+  double gap_ms = 0.0, work_ms = 0.0;
+  uint64_t gaps = 0, last_chunk_round = 0;
   uint64_t chunks = 0, finished = 0, admitted = 0, rounds = 0;
   double chunk_ms = 0.0, host_ms = 0.0;
   ~cfdg_server() {
     if (ca) cudaEventDestroy(ca);
     if (cb) cudaEventDestroy(cb);
+    if (pcb) cudaEventDestroy(pcb);
     if (epi) cudaEventDestroy(epi);
     for (auto& g : slots)
       for (int k = 0; k < 2; ++k) {
@@ -3687,6 +3707,7 @@ int cfdg_server_create(cfdg_context* ctx, cfdg_grid* const* grids, int32_t n, in
   S->B = B;
   S->max_active = max_active;
   if (cudaEventCreate(&S->ca) != cudaSuccess || cudaEventCreate(&S->cb) != cudaSuccess ||
+      cudaEventCreate(&S->pcb) != cudaSuccess ||
       cudaEventCreateWithFlags(&S->epi, cudaEventDisableTiming) != cudaSuccess) {
     cfdg_batch_destroy(B);
     delete S;
@@ -3807,9 +3828,21 @@ int cfdg_server_progress(cfdg_server* S, int32_t* finished) {
   // 1. Finish the cases that converged or failed in the last chunk.
   CU(cudaMemcpyAsync(B->h_st, B->d_st, sizeof(MState) * nc, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
+  const auto w0 = std::chrono::steady_clock::now();
+  struct WorkClock {
+    cfdg_server* S;
+    std::chrono::steady_clock::time_point t0;
+    ~WorkClock() {
+      S->work_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+  } work_clock{S, w0};
   if (S->timing) {
     float ms = 0.0f;
     if (cudaEventElapsedTime(&ms, S->ca, S->cb) == cudaSuccess) S->chunk_ms += ms;
+    if (S->gap_timing && cudaEventElapsedTime(&ms, S->pcb, S->ca) == cudaSuccess) {
+      S->gap_ms += ms;
+      ++S->gaps;
+    }
     S->timing = false;
   }
   std::vector<char> done(nc, 0), fin(nc, 0);
@@ -3898,9 +3931,13 @@ int cfdg_server_progress(cfdg_server* S, int32_t* finished) {
   if (changed)
     if (int e = set_active(B, s)) return e;
   if (nactive > 0) {
+    // pcb keeps the previous chunk's end when that chunk ran in the round just before.
+    S->gap_timing = S->chunks > 0 && S->last_chunk_round + 1 == S->rounds;
+    std::swap(S->cb, S->pcb);
     CU(cudaEventRecord(S->ca, s));
     CU(cudaGraphLaunch(B->chunk, s));
     CU(cudaEventRecord(S->cb, s));
+    S->last_chunk_round = S->rounds;
     S->timing = true;
     ++S->chunks;
     count(B->chunk_nodes);
@@ -3935,9 +3972,11 @@ int64_t cfdg_server_stats_json(cfdg_server* S, char* buf, int64_t cap) {
   char tmp[512];
   snprintf(tmp, sizeof tmp,
            "{\"rounds\": %llu, \"chunks\": %llu, \"iterations_per_chunk\": %d, \"chunk_device_ms\": %.3f, "
-           "\"progress_host_ms\": %.3f, \"finished\": %llu, \"admitted\": %llu}",
+           "\"progress_host_ms\": %.3f, \"progress_work_ms\": %.3f, \"between_chunks_ms\": %.3f, "
+           "\"chunk_pairs\": %llu, \"finished\": %llu, \"admitted\": %llu}",
            (unsigned long long)S->rounds, (unsigned long long)S->chunks, S->B->chunk_it, S->chunk_ms, S->host_ms,
-           (unsigned long long)S->finished, (unsigned long long)S->admitted);
+           S->work_ms, S->gap_ms, (unsigned long long)S->gaps, (unsigned long long)S->finished,
+           (unsigned long long)S->admitted);
   const std::string out = tmp;
   if (buf && cap > 0) {
     const size_t k = std::min((size_t)cap - 1, out.size());

@@ -347,9 +347,11 @@ int cfdg_server_result(cfdg_server *server, uint64_t ticket, cfdg_info *info, in
 int cfdg_server_pending(cfdg_server *server);
 /* Counters of the server since its creation, as JSON: progress rounds, graph chunks
  * launched and their device time (CUDA events around each launch), host time spent in
- * cfdg_server_progress (it includes waiting for the previous chunk), requests finished
- * and admitted. Same buffer convention as cfdg_batch_stats_json. No reference
- * counterpart. */
+ * cfdg_server_progress (it includes waiting for the previous chunk) and the part of it
+ * after that wait, the device time from the end of a chunk to the start of the next one
+ * launched in the following round (epilogues, prologues and the device waiting on the
+ * host) with the number of such pairs, requests finished and admitted. Same buffer
+ * convention as cfdg_batch_stats_json. No reference counterpart. */
 int64_t cfdg_server_stats_json(cfdg_server *server, char *buf, int64_t cap);
 
 /* Device memory the grid holds, in bytes (admission accounting). */
