@@ -780,7 +780,8 @@ def run_serving(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     kernels = {}
     for name, which, reps in (("rb_half_sweep_fp32", 0, 20), ("rb_half_sweep_fp32_unstaged", 4, 20),
                               ("operator_fp32", 1, 20), ("coarse_levels", 2, 10), ("vcycle_fp32", 3, 5),
-                              ("true_residual_fp64", 5, 10), ("rhs_fp64", 6, 10)):
+                              ("true_residual_fp64", 5, 10), ("rhs_fp64", 6, 10),
+                              ("level0_residual_restriction", 7, 20), ("level0_prolongation", 8, 20)):
         ms, b = bt.time_kernel(which, reps)
         kernels[name] = {"ms": round(ms, 4), "GB/s": round(b / ms / 1e6, 1) if b else None, "algorithmic_bytes": b}
     bt.close()

@@ -2589,6 +2589,18 @@ int cfdg_grid_set_coarse_scale(cfdg_grid* G, double alpha) {
   return 0;
 }
 
+int cfdg_grid_set_coarse_layout(cfdg_grid* G, int32_t bins) {
+  if (int e = check_grid(G)) return e;
+  if (bins != 0 && bins != 1) return fail(CFDG_ERR_INVALID, "the coarse layout is 0 (aggregate order) or 1 (bin grid)");
+  std::lock_guard<std::mutex> lk(G->mu);
+  if (G->mx_bins != bins) {
+    G->mixed.reset();  // the case state holds the first coarse level's numbering
+    G->solo.reset();
+  }
+  G->mx_bins = bins;
+  return 0;
+}
+
 int cfdg_project_device(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol, uint64_t max_iter,
                         cfdg_poll_fn poll, void* poll_ctx, cfdg_info* info) {
   if (int e = check_grid(G)) return e;

@@ -102,6 +102,13 @@ struct FineCase {
   // only (colour 1's is zero up to rounding after the last pre-smoothing half sweep), its
   // colour-1 slots stay zero and the restriction gathers colour-0 children only.
   int resc0, pad_resc0;
+  // Level 1 laid out as the bin grid (bin1): aggregate of bin (I, J, K) in row
+  // colour*h1 + (K*nb1[1] + J)*nbh1 + (I>>1), colour = (I+J+K)&1, nbh1 = ceil(nb1[0]/2),
+  // h1 = nb1[1]*nb1[2]*nbh1; empty bins are empty rows. Valid where every 2x2x2 bin holds at
+  // most one aggregate and prolongation is by injection; the residual of the colour-0
+  // children is then formed inside the restriction and the parent of a cell is its bin.
+  int bin1, nbh1, h1, pad_bin1;
+  int nb1[3], pad_nb1;
   const int *goff, *gmem;
   // transfers level 0 <-> 1
   int n1;
@@ -151,6 +158,13 @@ struct CLev {
   const int *ioff, *idx;
   const long long* foff;
   const double* fac;
+  // Level 1 of a bin1 grid whose rows all fit the bin stencil: per row its ELL entries in
+  // order as 7-bit codes (bits 7a..7a+2 the neighbour direction x-lo, x-hi, y-lo, y-hi,
+  // z-lo, z-hi, 7 for padding; bits 7a+3..7a+6 an index into svt, the level's distinct
+  // entry values), so a sweep computes its columns instead of loading them. Null: ELL.
+  const unsigned long long* scode;
+  const float* svt;
+  int snb1y, snbh;  // bins per column (nb1[1]) and per colour of a bin row (nbh1)
 };
 
 static_assert(sizeof(CLev) % 8 == 0, "CLev is copied to shared memory in 8-byte words");
@@ -188,6 +202,19 @@ __device__ __forceinline__ void tile_partial(double v, const FineCase& F, int lt
   (void)sh;
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) F.partials[lt * (TILE / 32) + (threadIdx.x >> 5)] = v;
+  ++seg_n;
+}
+
+// The same from a compensated FP32 pair per thread (hi, lo): the warp's pairs are summed
+// with TwoSum in FP32 and converted to FP64 once per warp (the FP64 pipe is narrow).
+__device__ __forceinline__ void tile_partial2(float hi, float lo, const FineCase& F, int lt, int& seg_n) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
+    const float s = hi + h2, bb = s - hi;
+    lo += l2 + ((hi - (s - bb)) + (h2 - bb));
+    hi = s;
+  }
+  if ((threadIdx.x & 31) == 0) F.partials[lt * (TILE / 32) + (threadIdx.x >> 5)] = (double)hi + (double)lo;
   ++seg_n;
 }
 
@@ -379,6 +406,10 @@ __device__ __forceinline__ bool warp_row(const FineCase& F, int lt, int warp, in
 
 // FP32 error-free transformations: a running sum (hi, lo) of exact products keeps
 // about twice the FP32 significand, so a thread's few terms convert to FP64 once.
+// Four consecutive slots (16-byte aligned): the level-0 arrays start on 256-byte
+// boundaries and a row tile's slots on multiples of four.
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 // Compensated running sum (hi, lo) += v (Knuth's TwoSum).
 __device__ __forceinline__ void dd_add(float v, float& hi, float& lo) {
   const float s = hi + v;
@@ -569,7 +600,7 @@ __device__ __forceinline__ void b_op(const FineCase* FC, MState* ST, const int2 
       }
     }
   }
-  tile_partial((double)hi + (double)lo, F, lt, sh, seg_n);
+  tile_partial2(hi, lo, F, lt, seg_n);
 }
 __global__ void __launch_bounds__(TILE, 5) k_op(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   __shared__ double sh[32];
@@ -603,13 +634,28 @@ __device__ __forceinline__ void b_update(const FineCase* FC, MState* ST, const i
   FINE_PROLOGUE(S.state == RUN)
   const float alpha = (float)S.alpha;
   float hi = 0.0f, lo = 0.0f;
-  for (int c = sb + threadIdx.x; c < se; c += TILE) {
-    F.e[c] = fmaf(alpha, F.p[c], F.e[c]);
-    const float r = fmaf(-alpha, F.q[c], F.r32[c]);
-    F.r32[c] = r;
-    dd_add_prod(r, r, hi, lo);
+  if (!((sb | se) & 3)) {
+    // Four slots per thread: every operand of a tile in flight at once.
+    for (int c = sb + 4 * threadIdx.x; c < se; c += 4 * TILE) {
+      float4 e = ld4(F.e + c);
+      const float4 p = ld4(F.p + c), q = ld4(F.q + c);
+      float4 r = ld4(F.r32 + c);
+      e.x = fmaf(alpha, p.x, e.x), e.y = fmaf(alpha, p.y, e.y), e.z = fmaf(alpha, p.z, e.z), e.w = fmaf(alpha, p.w, e.w);
+      r.x = fmaf(-alpha, q.x, r.x), r.y = fmaf(-alpha, q.y, r.y), r.z = fmaf(-alpha, q.z, r.z);
+      r.w = fmaf(-alpha, q.w, r.w);
+      st4(F.e + c, e);
+      st4(F.r32 + c, r);
+      dd_add(fmaf(r.x, r.x, fmaf(r.y, r.y, fmaf(r.z, r.z, r.w * r.w))), hi, lo);
+    }
+  } else {
+    for (int c = sb + threadIdx.x; c < se; c += TILE) {
+      F.e[c] = fmaf(alpha, F.p[c], F.e[c]);
+      const float r = fmaf(-alpha, F.q[c], F.r32[c]);
+      F.r32[c] = r;
+      dd_add_prod(r, r, hi, lo);
+    }
   }
-  tile_partial((double)hi + (double)lo, F, lt, sh, seg_n);
+  tile_partial2(hi, lo, F, lt, seg_n);
 }
 __global__ void __launch_bounds__(TILE) k_update(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   __shared__ double sh[32];
@@ -757,8 +803,15 @@ __device__ __forceinline__ void b_rz(const FineCase* FC, MState* ST, const int2 
                                     int& seg_n) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   float hi = 0.0f, lo = 0.0f;
-  for (int c = sb + threadIdx.x; c < se; c += TILE) dd_add_prod(F.r32[c], F.x0[c], hi, lo);
-  tile_partial((double)hi + (double)lo, F, lt, sh, seg_n);
+  if (!((sb | se) & 3)) {
+    for (int c = sb + 4 * threadIdx.x; c < se; c += 4 * TILE) {
+      const float4 r = ld4(F.r32 + c), z = ld4(F.x0 + c);
+      dd_add(fmaf(r.x, z.x, fmaf(r.y, z.y, fmaf(r.z, z.z, r.w * z.w))), hi, lo);
+    }
+  } else {
+    for (int c = sb + threadIdx.x; c < se; c += TILE) dd_add_prod(F.r32[c], F.x0[c], hi, lo);
+  }
+  tile_partial2(hi, lo, F, lt, seg_n);
 }
 __global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   __shared__ double sh[32];
@@ -781,7 +834,18 @@ __global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, con
 __device__ __forceinline__ void b_p(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == RUN)
   const float beta = (float)S.beta;
-  if (S.beta == 0.0) {
+  if (!((sb | se) & 3)) {
+    if (S.beta == 0.0) {
+      for (int c = sb + 4 * threadIdx.x; c < se; c += 4 * TILE) st4(F.p + c, ld4(F.x0 + c));
+    } else {
+      for (int c = sb + 4 * threadIdx.x; c < se; c += 4 * TILE) {
+        float4 p = ld4(F.p + c);
+        const float4 z = ld4(F.x0 + c);
+        p.x = fmaf(beta, p.x, z.x), p.y = fmaf(beta, p.y, z.y), p.z = fmaf(beta, p.z, z.z), p.w = fmaf(beta, p.w, z.w);
+        st4(F.p + c, p);
+      }
+    }
+  } else if (S.beta == 0.0) {
     for (int c = sb + threadIdx.x; c < se; c += TILE) F.p[c] = F.x0[c];
   } else {
     for (int c = sb + threadIdx.x; c < se; c += TILE) F.p[c] = fmaf(beta, F.p[c], F.x0[c]);
@@ -1213,6 +1277,31 @@ __global__ void __launch_bounds__(TILE) k_v_resid(const FineCase* FC, MState* ST
   }
 }
 
+// bin1 restriction, thread q of the case's 2*h1: bin row R = q / (2 nbh1) (J = R mod nb1[1],
+// K = R / nb1[1]), bin I = q mod (2 nbh1), so consecutive threads take consecutive bins of a
+// row and every level-1 row is written once (I >= nb1[0]: an empty row). Its right-hand
+// side is the sum, in cell order, of the level-0 residuals of the bin's colour-0 cells (one
+// per fine row: i = 2I + ((j+k)&1), slot I of the row's colour-0 half). The residual holds
+// +0 on solid cells and padding slots, and a running sum that starts at +0 never becomes
+// -0, so adding them changes no bit: the sum equals the index lists' over the members.
+__device__ __forceinline__ void bin_restrict(const FineCase& F, int q) {
+  const int nbh = F.nbh1, R = q / (2 * nbh), I = q - R * 2 * nbh;
+  const int J = R % F.nb1[1], K = R / F.nb1[1];
+  float acc = 0.0f;
+  if (I < F.nb1[0]) {
+    const int ny = F.n[1], nz = F.n[2], nxh = F.nxh;
+    float v[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {  // (dk, dj) in cell order; the loads first, then the sum
+      const int k = 2 * K + (c >> 1), j = 2 * J + (c & 1);
+      v[c] = (k < nz && j < ny) ? __ldcg(&F.res0[lay(k * ny + j, 0, nxh, I)]) : 0.0f;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc = fmaf(1.0f, v[c], acc);
+  }
+  F.rhs1[((I + J + K) & 1) * F.h1 + R * nbh + (I >> 1)] = acc;
+}
+
 // rhs1 = R res0: level-1 rows gather their level-0 children. Tiles index level-1 rows.
 __global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState* ST, const int2* tiles1,
                                                      const int* count) {
@@ -1224,6 +1313,10 @@ __global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState*
     if (!(S.state == RUN || S.state == START)) continue;
     const int j = t.y * TILE + threadIdx.x;
     if (j >= F.n1) continue;
+    if (F.bin1) {
+      bin_restrict(F, j);
+      continue;
+    }
     float v = 0.0f;
     v = gather_sum(F.r_child, F.r_w, F.res0, F.r_off[j], F.r_off[j + 1], v);
     F.rhs1[j] = v;
@@ -1236,11 +1329,26 @@ __global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState*
 __device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
   const int rows_t = min(RT, F.n[1] * F.n[2] - lt * RT);
+  if (F.bin1) {
+    // One warp per row; the parent of the cell in colour-0 slot s (i = 2s + par) is bin
+    // (s, j/2, k/2). Solid cells take a correction too: no interior face reads them and
+    // the last post-smoothing half sweep (colour 0) sets them to zero.
+    int j, k, rb;
+    if (!warp_row(F, lt, warp, j, k, rb)) return;
+    const int par = (j + k) & 1, jk = (j >> 1) + (k >> 1), h1 = F.h1;
+    const int base1 = ((k >> 1) * F.nb1[1] + (j >> 1)) * F.nbh1;
+    float* __restrict__ x = F.x0 + lay(lt * RT + warp, 0, nxh_, 0);
+    const float* __restrict__ x1 = F.x1;
+    const float a = F.pscale;
+    for (int sl = lane; sl < nxh_; sl += 32)
+      if (2 * sl + par < nx_) x[sl] = fmaf(a, x1[((sl + jk) & 1) * h1 + base1 + (sl >> 1)], x[sl]);
+    return;
+  }
   if (F.pinj) {  // x0 += x1[parent]: the same value as the weight-1 row below
     for (int m = threadIdx.x; m < rows_t * nxh_; m += TILE) {
       const int c = lay(lt * RT + m / nxh_, 0, nxh_, m % nxh_);
       const int q = F.pinj[c];
-      if (q >= 0) F.x0[c] += F.pscale * F.x1[q];
+      if (q >= 0) F.x0[c] = fmaf(F.pscale, F.x1[q], F.x0[c]);
     }
     return;
   }
@@ -1293,6 +1401,20 @@ __global__ void k_center0(const FineCase* FC, MState* ST, const int2* gtab, cons
 // colour of the cycle's first sweep, whose neighbours are all zero, takes x = rhs / diag
 // (the same bits as summing the zero products).
 constexpr int RPI = 4;
+// Entry a of a bin-stencil row (CLev::scode): its column (padding: the row `self`) and
+// value. ob: the row's slot in the other colour's half (same bin row, same slot); par:
+// the parity of the row's bin index along x.
+__device__ __forceinline__ void bin_entry(const CLev& L, unsigned long long cw, int a, int ob, int par, int self,
+                                          int& col, float& val) {
+  const unsigned e = (unsigned)(cw >> (7 * a)) & 127u;
+  const int dir = (int)(e & 7u), nbh = L.snbh, nz = L.snb1y * L.snbh;
+  const int off = dir == 0 ? par - 1 : dir == 1 ? par : dir == 2 ? -nbh : dir == 3 ? nbh : dir == 4 ? -nz : nz;
+  col = dir == 7 ? self : ob + off;
+  val = dir == 7 ? 0.0f : __ldg(&L.svt[e >> 3]);
+}
+constexpr unsigned long long BIN_PAD = 0x3870e1c387ull;  // direction 7 (padding) in all six entries
+static_assert(((BIN_PAD >> 35) & 127u) == 7u && (BIN_PAD >> 42) == 0, "six padding codes");
+
 __device__ __forceinline__ void gs_rows(const CLev& L, int color, int k, bool skipx) {
   const int c0 = L.coff[color];
   const int nrow = L.coff[color + 1] - c0;
@@ -1305,7 +1427,31 @@ __device__ __forceinline__ void gs_rows(const CLev& L, int color, int k, bool sk
     v[r] = ok ? __ldcg(&L.rhs[c0 + q + r]) : 0.0f;
     d[r] = ok ? L.idiag[c0 + q + r] : 0.0f;
   }
-  if (!skipx) {
+  if (!skipx && L.scode) {
+    // Bin stencil: the codes of the item's rows (one bin row: nbh is a multiple of RPI),
+    // then every entry's column computed and all gathers issued; the same entries, values
+    // and fmaf order as the ELL rows below.
+    const int nbh = L.snbh, R = q / nbh;
+    const int par = (color + R % L.snb1y + R / L.snb1y) & 1;
+    const int ob = (1 - color) * L.coff[1] + R * nbh + (q - R * nbh);
+    const int w = L.ell_w[color];
+    unsigned long long cw[RPI];
+#pragma unroll
+    for (int r = 0; r < RPI; ++r) cw[r] = q + r < nrow ? __ldg(&L.scode[c0 + q + r]) : BIN_PAD;
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+      if (a < w) {
+        float xv[RPI], wv[RPI];
+#pragma unroll
+        for (int r = 0; r < RPI; ++r) {
+          int col;
+          bin_entry(L, cw[r], a, ob + r, par, q + r < nrow ? c0 + q + r : c0 + q, col, wv[r]);
+          xv[r] = __ldcg(&L.x[col]);
+        }
+#pragma unroll
+        for (int r = 0; r < RPI; ++r) v[r] = fmaf(-wv[r], xv[r], v[r]);
+      }
+  } else if (!skipx) {
     const int base = L.ell_off[color], w = L.ell_w[color];
     const int* ec = L.ell_col + base + q;
     const float* ev = L.ell_val + base + q;
@@ -1352,6 +1498,32 @@ __device__ __forceinline__ void res0_rows(const CLev& L, int k) {
   float v[RPI];
 #pragma unroll
   for (int r = 0; r < RPI; ++r) v[r] = q + r < nrow ? L.diag[q + r] * __ldcg(&L.x[q + r]) : 0.0f;
+  if (L.scode) {  // bin stencil (gs_rows): the same entries in the same order
+    const int nbh = L.snbh, R = q / nbh;
+    const int par = (R % L.snb1y + R / L.snb1y) & 1;
+    const int ob = nrow + R * nbh + (q - R * nbh);
+    const int w = L.ell_w[0];
+    unsigned long long cw[RPI];
+#pragma unroll
+    for (int r = 0; r < RPI; ++r) cw[r] = q + r < nrow ? __ldg(&L.scode[q + r]) : BIN_PAD;
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+      if (a < w) {
+        float xv[RPI], wv[RPI];
+#pragma unroll
+        for (int r = 0; r < RPI; ++r) {
+          int col;
+          bin_entry(L, cw[r], a, ob + r, par, q + r < nrow ? q + r : q, col, wv[r]);
+          xv[r] = __ldcg(&L.x[col]);
+        }
+#pragma unroll
+        for (int r = 0; r < RPI; ++r) v[r] = fmaf(wv[r], xv[r], v[r]);
+      }
+#pragma unroll
+    for (int r = 0; r < RPI; ++r)
+      if (q + r < nrow) L.res[q + r] = __ldcg(&L.rhs[q + r]) - v[r];
+    return;
+  }
   const int base = L.ell_off[0], w = L.ell_w[0];
   const int* ec = L.ell_col + base + q;
   const float* ev = L.ell_val + base + q;
@@ -2105,12 +2277,15 @@ struct CaseState {
 
 // Row r of `a` becomes row prow[r] (entry order kept), columns c become pcol[c]; an
 // empty map is the identity.
-Csr permute_csr(const Csr& a, const std::vector<int32_t>& prow, const std::vector<int32_t>& pcol) {
+// Rows moved to prow[r] (of nout rows, -1: a's row count; rows no r maps to stay empty),
+// columns renamed by pcol; every row keeps its entries in their order.
+Csr permute_csr(const Csr& a, const std::vector<int32_t>& prow, const std::vector<int32_t>& pcol, int nout = -1) {
   Csr out;
   const int n = a.rows();
-  out.off.assign(n + 1, 0);
+  const int m = nout < 0 ? n : nout;
+  out.off.assign(m + 1, 0);
   for (int r = 0; r < n; ++r) out.off[(prow.empty() ? r : prow[r]) + 1] = a.off[r + 1] - a.off[r];
-  for (int r = 0; r < n; ++r) out.off[r + 1] += out.off[r];
+  for (int r = 0; r < m; ++r) out.off[r + 1] += out.off[r];
   out.col.resize(a.col.size());
   if (!a.val.empty()) out.val.resize(a.val.size());
   for (int r = 0; r < n; ++r) {
@@ -2294,8 +2469,59 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     F.goff = o;
     F.gmem = m;
   }
+  // Level 1 as the bin grid (FineCase::bin1) where the grid allows it: an aggregation
+  // hierarchy of three or more levels, no closed groups on level 0, uniform weights with
+  // whole colour pairs per row, injection prolongation and restriction with weight 1,
+  // every aggregate inside one bin and no bin holding two. bslot: aggregate -> row.
+  F.bin1 = 0;
+  std::vector<int32_t> bslot;
+  if (G->mx_bins && H.masked && M0.groups.rows() == 0 && F.uniform && !(F.nxh & 1) && H.levels.size() >= 3) {
+    const MgLevel& M1 = H.levels[1];
+    const int nb0 = (nx + 1) / 2, nb1 = (ny + 1) / 2, nb2 = (h.n[2] + 1) / 2, nbh = (nb0 + 1) / 2;
+    const int h1 = nb1 * nb2 * nbh;
+    bool ok = M0.restrict.rows() == M1.n && (int)M1.parity.size() == M1.n &&
+              (int64_t)M0.prolong.rows() == (int64_t)F.N;
+    for (int c = 0; c < F.N && ok; ++c) {
+      const int n = M0.prolong.off[c + 1] - M0.prolong.off[c];
+      ok = n == 0 || (n == 1 && M0.prolong.val[M0.prolong.off[c]] == 1.0);
+    }
+    std::vector<char> used(2 * (size_t)h1, 0);
+    bslot.assign(M1.n, -1);
+    for (int a = 0; a < M1.n && ok; ++a) {
+      int bin = -1, row = -1;
+      for (int q = M0.restrict.off[a]; q < M0.restrict.off[a + 1] && ok; ++q) {
+        const int c = M0.restrict.col[q];
+        const int I = (c % nx) >> 1, J = ((c / nx) % ny) >> 1, K = (c / (nx * ny)) >> 1;
+        const int b = (K * nb1 + J) * nb0 + I;
+        ok = M0.restrict.val[q] == 1.0 && (bin < 0 || b == bin);
+        if (bin < 0 && ok) {
+          bin = b;
+          const int col = (I + J + K) & 1;
+          row = col * h1 + (K * nb1 + J) * nbh + (I >> 1);
+          ok = M1.parity[a] == col;
+        }
+      }
+      ok = ok && row >= 0 && !used[row];
+      if (ok) {
+        used[row] = 1;
+        bslot[a] = row;
+      }
+    }
+    for (int a = 0; a < M1.n && ok; ++a)
+      for (int q = M1.a.off[a]; q < M1.a.off[a + 1] && ok; ++q)
+        ok = M1.a.col[q] == a || M1.parity[M1.a.col[q]] != M1.parity[a];
+    if (ok) {
+      F.bin1 = 1;
+      F.nb1[0] = nb0, F.nb1[1] = nb1, F.nb1[2] = nb2;
+      F.nbh1 = nbh;
+      F.h1 = h1;
+    } else {
+      bslot.clear();
+    }
+  }
   // Coarse levels 1 .. L-1: colouring (bin parity, else greedy; l1-Jacobi when more than
-  // 8 colours), then every level renumbered colour by colour.
+  // 8 colours), then every level renumbered colour by colour (level 1 of a bin1 grid by
+  // its bin rows).
   CCase& C = cs.C;
   C.nl = (int)H.levels.size() - 1;
   if (C.nl < 1 || C.nl > MAXL) return fail(CFDG_ERR_UNSUPPORTED, "mixed form: unsupported hierarchy depth");
@@ -2304,6 +2530,12 @@ int build_case(cfdg_grid* G, CaseState& cs) {
   for (int l = 1; l <= C.nl; ++l) {
     const MgLevel& M = H.levels[l];
     const bool terminal = l == C.nl;
+    if (l == 1 && F.bin1) {
+      lcoff[1] = {0, F.h1, 2 * F.h1};
+      lcolors[1] = 2;
+      perm[1] = bslot;
+      continue;
+    }
     std::vector<int32_t> rows;
     int nco = 1;
     if (terminal) {
@@ -2329,9 +2561,10 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     MgLevel& Q = PL[l];
     const std::vector<int32_t>& P = perm[l];
     const std::vector<int32_t> none;
-    Q.n = M.n;
-    Q.a = permute_csr(M.a, P, P);
-    Q.diag.assign(M.n, 0.0);
+    const int nout = (l == 1 && F.bin1) ? 2 * F.h1 : M.n;  // bin rows include empty bins
+    Q.n = nout;
+    Q.a = permute_csr(M.a, P, P, nout);
+    Q.diag.assign(nout, 0.0);
     for (int i = 0; i < M.n; ++i) Q.diag[P[i]] = M.diag[i];
     Q.groups = permute_csr(M.groups, none, P);
     Q.direct_idx = permute_csr(M.direct_idx, none, P);
@@ -2339,13 +2572,13 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     Q.direct_factor = M.direct_factor;
     if (l < C.nl) {
       Q.restrict = permute_csr(M.restrict, perm[l + 1], P);
-      Q.prolong = permute_csr(M.prolong, P, perm[l + 1]);
+      Q.prolong = permute_csr(M.prolong, P, perm[l + 1], nout);
     }
   }
   {
     // Restriction gathers level-0 slots; the prolongation's rows follow the slots; level
     // 1 in its colour-by-colour numbering.
-    Csr R0 = permute_csr(M0.restrict, perm[1], {});
+    Csr R0 = permute_csr(M0.restrict, perm[1], {}, PL[1].n);
     std::vector<int32_t> child(R0.col.size());
     for (size_t q = 0; q < child.size(); ++q) child[q] = slot[R0.col[q]];
     F.resc0 = M0.groups.rows() == 0 ? 1 : 0;
@@ -2479,6 +2712,54 @@ int build_case(cfdg_grid* G, CaseState& cs) {
       L.ell_off = eo, L.ell_w = ewp, L.ell_col = ec, L.ell_val = ev, L.idiag = idp;
       cs.stats.push_back({M.n, (long long)M.a.col.size(), (long long)ecol.size(), M.groups.rows(),
                           L.terminal ? M.direct_idx.rows() : 0, L.ncolors, L.jacobi});
+      // The bin stencil of level 1 (CLev::scode): every ELL entry of every row is one of
+      // the row's six bin neighbours or padding, at most six per row, at most 16 distinct
+      // values, and a bin row's slots per colour a multiple of the rows per sweep item.
+      L.scode = nullptr;
+      L.svt = nullptr;
+      if (l == 1 && F.bin1 && !L.jacobi && L.ncolors == 2 && F.nbh1 % RPI == 0 && ew[0] <= 6 && ew[1] <= 6) {
+        const int nbh = F.nbh1, nb1y = F.nb1[1], h1 = F.h1;
+        std::vector<unsigned long long> code(M.n, 0);
+        std::vector<float> vt;
+        bool ok = true;
+        for (int c = 0; c < 2 && ok; ++c) {
+          const int nrow = coff[c + 1] - coff[c];
+          for (int t = 0; t < nrow && ok; ++t) {
+            const int row = coff[c] + t, R = t / nbh, m = t % nbh;
+            const int par = (c + R % nb1y + R / nb1y) & 1;
+            const int other = (1 - c) * h1 + R * nbh + m;
+            const int offs[6] = {par - 1, par, -nbh, nbh, -nb1y * nbh, nb1y * nbh};
+            unsigned long long cw = 0;
+            for (int a = 0; a < ew[c] && ok; ++a) {
+              const size_t e = (size_t)eoff[c] + (size_t)a * nrow + t;
+              int dir = 7, vi = 0;
+              if (!(ecol[e] == row && eval[e] == 0.0f)) {
+                dir = -1;
+                for (int d2 = 0; d2 < 6; ++d2)
+                  if (ecol[e] == other + offs[d2]) dir = d2;
+                ok = dir >= 0;
+                if (ok) {
+                  vi = (int)(std::find(vt.begin(), vt.end(), eval[e]) - vt.begin());
+                  if (vi == (int)vt.size()) vt.push_back(eval[e]);
+                  ok = vi < 16;
+                }
+              }
+              cw |= (unsigned long long)(dir | (vi << 3)) << (7 * a);
+            }
+            code[row] = cw;
+          }
+        }
+        if (ok) {
+          unsigned long long* dc;
+          float* dv;
+          if (int e = A.upload(&dc, code, s)) return e;
+          if (int e = A.upload(&dv, vt, s)) return e;
+          L.scode = dc;
+          L.svt = dv;
+          L.snb1y = nb1y;
+          L.snbh = nbh;
+        }
+      }
     }
     if (L.ngroups) {
       int *go, *gm;
@@ -2623,6 +2904,7 @@ struct cfdg_batch {
   WorkLists run, pro, epi;
   int g_fine = 1, g_1 = 1, g_f = 1, g_g = 1;  // work items per list: caps on the persistent grids
   bool any_groups = false;
+  bool any_bin1 = false;  // some case has its level 1 as the bin grid
   // Coarse-level phase tables (device), refilled for each active set.
   CoarseTab h_tab{};
   CoarseTab* d_tab = nullptr;
@@ -3042,6 +3324,7 @@ int cfdg_mixed_pack(cfdg_batch* B) {
   std::vector<CCase> cc;
   const int nc = (int)B->cases.size();
   B->any_groups = false;
+  B->any_bin1 = false;
   B->nlev_all = 0;
   for (int i = 0; i < nc; ++i) {
     FineCase F = B->cases[i]->F;
@@ -3051,6 +3334,7 @@ int cfdg_mixed_pack(cfdg_batch* B) {
     for (int t = 0; t < F.nftiles; ++t) B->ftiles.push_back(make_int2(i, t));
     for (int g = 0; g < F.ngroups; ++g) B->gtab.push_back(make_int2(i, g));
     B->any_groups |= F.ngroups > 0;
+    B->any_bin1 |= F.bin1 != 0;
     B->nlev_all = std::max(B->nlev_all, B->cases[i]->C.nl);
     for (int l = 0; l < B->cases[i]->C.nl; ++l)
       if (!B->cases[i]->C.lv[l].terminal && B->cases[i]->C.lv[l].ncolors > MAXC)
@@ -3512,8 +3796,10 @@ int64_t cfdg_batch_stats_json(cfdg_batch* B, char* buf, int64_t cap) {
   std::string out = tmp;
   for (size_t i = 0; i < B->cases.size(); ++i) {
     const CaseState& cs = *B->cases[i];
-    snprintf(tmp, sizeof tmp, "%s{\"cells\": %d, \"groups0\": %d, \"levels\": [", i ? ", " : "", cs.F.N,
-             cs.ngroups0);
+    snprintf(tmp, sizeof tmp,
+             "%s{\"cells\": %d, \"groups0\": %d, \"level1_bins\": %s, \"level1_stencil\": %s, \"levels\": [",
+             i ? ", " : "", cs.F.N, cs.ngroups0, cs.F.bin1 ? "true" : "false",
+             cs.C.lv[0].scode ? "true" : "false");
     out += tmp;
     for (size_t l = 0; l < cs.stats.size(); ++l) {
       const auto& v = cs.stats[l];
@@ -3614,6 +3900,23 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
       case 6:  // FP64 right-hand side b = -div(u)/dt
         FINE(k_rhs, B->run);
         break;
+      case 7:  // level-0 residual and its restriction to level 1
+        FINE(k_v_resid, B->run);
+        k_v_restrict<<<grid_of(k_v_restrict, TILE, B->g_1), TILE, 0, s>>>(B->d_fc, B->d_st, B->run.tiles1,
+                                                                          B->run.counts + 1);
+        break;
+      case 9:  // e += alpha p, r -= alpha q with |r|^2
+        FINE(k_update, B->run);
+        break;
+      case 10:  // r.z
+        FINE(k_rz, B->run);
+        break;
+      case 11:  // p = z + beta p
+        FINE(k_p, B->run);
+        break;
+      case 8:  // level-1 correction prolonged to level 0
+        FINE(k_v_prolong, B->run);
+        break;
       default:
         enqueue_vcycle(B, s);
         break;
@@ -3623,11 +3926,14 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
   else if (which == 1) bytes = 10.0 * cells; // p in, u16 flags, q out
   else if (which == 2) bytes = coarse_bytes(B);
   else if (which == 5) bytes = 26.0 * cells;  // x, b_c, r out (FP64), u16 flags
+  else if (which == 9) bytes = 24.0 * cells;  // e, p, r, q in; e, r out
+  else if (which == 10) bytes = 8.0 * cells;  // r, z in
+  else if (which == 11) bytes = 12.0 * cells; // z, p in; p out
   else if (which == 6) {
     for (auto& F : B->h_fc) bytes += 8.0 * (double)F.F + 17.0 * F.N;  // u faces, fluid, b and terms out
   }
   float ms = 0;
-  if (which == 5 || which == 6) {
+  if (which == 5 || which == 6 || which == 9 || which == 10) {
     // These kernels move the cases' states on: restore them before every launch and time
     // the launches alone.
     for (int r = -2; r < reps; ++r) {

@@ -212,6 +212,9 @@ struct cfdg_grid {
   // rows per shared-memory stage (8, 16, 32) and stages in flight per block (2..8); 0 and 0
   // choose from the row length when a batch is packed.
   int mx_sweep_rows = 0, mx_sweep_stages = 0;
+  // Mixed form: first coarse level laid out as the 2x2x2 bin grid where the hierarchy
+  // allows it (cfdg_grid_set_coarse_layout); 0 keeps the aggregates' colour order.
+  int mx_bins = 1;
   // Laminar time stepping (cfdg_grid_set_flow / cfdg_step_device): the case flow and the
   // stage buffers (cell velocities, the two stage velocities, the stage pressure).
   bool has_flow = false;

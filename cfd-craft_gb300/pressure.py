@@ -252,6 +252,12 @@ class DeviceGrid:
         (cfdg_grid_set_coarse_scale; default 1.8, 1 is the reference's cycle)."""
         self._check(self.L.cfdg_grid_set_coarse_scale(self.h, float(alpha)))
 
+    def set_coarse_layout(self, bins: bool):
+        """Mixed form: the first coarse level as the 2x2x2 bin grid where the hierarchy
+        allows it (True, the default) or in the aggregates' colour order (False); the same
+        bits either way (cfdg_grid_set_coarse_layout)."""
+        self._check(self.L.cfdg_grid_set_coarse_layout(self.h, 1 if bins else 0))
+
     def device_bytes(self) -> int:
         return int(self.L.cfdg_grid_device_bytes(self.h))
 

@@ -215,6 +215,13 @@ int cfdg_grid_set_sweep_tile(cfdg_grid *grid, int32_t rows, int32_t stages);
  * residual, so the result meets the same tolerance. Batches and servers created afterwards
  * take it; grids with linear interpolation (no solid cells) are not scaled. */
 int cfdg_grid_set_coarse_scale(cfdg_grid *grid, double alpha);
+/* Mixed form: the first coarse level of an aggregation hierarchy laid out as the grid of
+ * 2x2x2 bins (bins = 1, the default) where every bin holds at most one aggregate, the
+ * level has no closed groups and the weights are uniform; the level-0 residual is then
+ * formed inside the restriction and a cell's parent is its bin. bins = 0 keeps the
+ * aggregates in colour order with index lists. Both give the same bits; a batch or server
+ * takes the layout from its grids. No reference counterpart. */
+int cfdg_grid_set_coarse_layout(cfdg_grid *grid, int32_t bins);
 
 /* ------------------------------------------------------------------ the projection */
 
@@ -280,13 +287,17 @@ int cfdg_batch_project(cfdg_batch *batch, double *const *u, double *const *p, co
  * over all fine levels, 1 the FP32 operator, 2 all coarse levels (one cooperative launch), 3 one
  * V-cycle, 4 the half sweep of 0 with the unstaged register kernel, 5 the FP64 true
  * residual of every case, 6 the FP64 right-hand side of every case (only after a
- * host-buffer cfdg_batch_project, whose inputs the batch keeps). Reports the mean duration
+ * host-buffer cfdg_batch_project, whose inputs the batch keeps), 7 the level-0 residual
+ * with its restriction to level 1, 8 the prolongation of the level-1 correction to level
+ * 0, 9 the inner update (e, r and |r|^2), 10 r.z, 11 p = z + beta p. Reports the mean duration
  * and the unit's algorithmic bytes (0 when not stated). Diagnostic; no reference
  * counterpart. */
 int cfdg_batch_time_kernel(cfdg_batch *batch, int32_t which, int32_t reps, double *ms_per_launch,
                            double *algorithmic_bytes);
 /* Per case and coarse level of the batch's FP32 hierarchies, as JSON: rows, nonzeros,
  * smoother colours, ELL entries (with padding), closed groups and terminal blocks; and
+ * whether level 1 is laid out as the bin grid ("level1_bins", per case) and swept through
+ * computed bin-stencil columns ("level1_stencil"), and
  * whether the level-0 half sweeps run staged through the tensor memory accelerator
  * ("staged_sweeps": every case with uniform weights and ceil(nx/2) a multiple of 8). Writes
  * at most cap bytes (NUL-terminated) and returns the length the full text needs, or a

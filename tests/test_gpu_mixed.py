@@ -287,3 +287,47 @@ def test_mixed_rhs_bitwise_against_oracle(pkg, O):
     batch.close()
     for d in dgs:
         d.close()
+
+
+def test_bin_grid_first_coarse_level_gives_the_same_bits(pkg):
+    """The first coarse level laid out as the 2x2x2 bin grid (restriction children and
+    prolongation parents from bin positions, sweeps and residual through computed
+    bin-stencil columns) against the aggregates' colour order with index lists: the same
+    projected bits and iterations, alone and in a batch; grids the bin layout does not fit
+    (no buildings: a geometric hierarchy) keep the index lists."""
+    rng = np.random.default_rng(23)
+    cases = [pkg.synth.case((64, 64, 32), 2.0, inflow=5.0, preconditioner="multigrid",
+                            boxes=pkg.synth.random_boxes(rng, 8, (128.0, 128.0, 64.0), dx=2.0)),
+             pkg.synth.case((48, 40, 24), 2.0, inflow=5.0, preconditioner="multigrid",
+                            boxes=pkg.synth.random_boxes(rng, 5, (96.0, 80.0, 48.0), dx=2.0)),
+             pkg.synth.case((32, 32, 16), 2.0, inflow=5.0, preconditioner="multigrid")]
+    grids = [pkg.grid.Grid.build(c) for c in cases]
+    us = [pkg.synth.random_velocity(g, 40 + i) for i, g in enumerate(grids)]
+    out = {}
+    for bins in (False, True):
+        dgs = [pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed") for g in grids]
+        for d in dgs:
+            d.set_coarse_layout(bins)
+        alone = []
+        for d, g, u in zip(dgs, grids, us):
+            uu, pp = u.copy(), np.zeros(g.count)
+            info = d.project(uu, pp, 0.1, 1e-8, 10000)
+            alone.append((uu, pp, info.iterations))
+        batch = pkg.pressure.Batch(dgs)
+        laid = [c["level1_bins"] for c in batch.stats()["cases"]]
+        assert [c["level1_stencil"] for c in batch.stats()["cases"]] == laid
+        bu, bp = [u.copy() for u in us], [np.zeros(g.count) for g in grids]
+        res = batch.project(bu, bp, [0.1] * len(grids), 1e-8, 10000)
+        assert all(code == 0 for code, _ in res)
+        batch.close()
+        for d in dgs:
+            d.close()
+        out[bins] = (alone, bu, bp, laid)
+    assert out[False][3] == [False, False, False]
+    assert out[True][3] == [True, True, False]
+    for i in range(len(grids)):
+        a0, a1 = out[False][0][i], out[True][0][i]
+        assert a0[2] == a1[2], i
+        assert np.array_equal(bits(a0[0]), bits(a1[0])) and np.array_equal(bits(a0[1]), bits(a1[1])), i
+        assert np.array_equal(bits(out[False][1][i]), bits(out[True][1][i])), i
+        assert np.array_equal(bits(out[False][2][i]), bits(out[True][2][i])), i
