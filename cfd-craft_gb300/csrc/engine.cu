@@ -1274,6 +1274,63 @@ std::string stats_json_of(const DevHierarchy& D, const Hierarchy& H) {
   return s + "}";
 }
 
+// Re-indexes level 0 of a host hierarchy from compact fluid numbering to full-grid cells
+// (structured grids whose level 0 the device keeps in the full-grid layout).
+static void reindex_level0(const cfdg_grid* G, Hierarchy& H) {
+  // Re-index level 0 from compact fluid numbering to full-grid cells.
+  MgLevel& M = H.levels[0];
+  const int32_t N = (int32_t)G->h.cells;
+  std::vector<int32_t> full(M.n);
+  for (int32_t j = 0; j < M.n; ++j) full[j] = H.masked ? H.fluid_indices[j] : j;
+  std::vector<double> diag(N, 0.0);
+  for (int32_t j = 0; j < M.n; ++j) diag[full[j]] = M.diag[j];
+  M.diag = std::move(diag);
+  for (auto& m : M.groups.col) m = full[m];
+  for (auto& m : M.restrict.col) m = full[m];
+  Csr P;
+  P.off.assign(N + 1, 0);
+  for (int32_t j = 0; j < M.n; ++j) P.off[full[j] + 1] = M.prolong.off[j + 1] - M.prolong.off[j];
+  for (int32_t c = 0; c < N; ++c) P.off[c + 1] += P.off[c];
+  P.col.resize(M.prolong.col.size());
+  P.val.resize(M.prolong.val.size());
+  for (int32_t j = 0; j < M.n; ++j)
+    for (int32_t k = 0; k < M.prolong.off[j + 1] - M.prolong.off[j]; ++k) {
+      P.col[P.off[full[j]] + k] = M.prolong.col[M.prolong.off[j] + k];
+      P.val[P.off[full[j]] + k] = M.prolong.val[M.prolong.off[j] + k];
+    }
+  M.prolong = std::move(P);
+  M.n = N;
+  M.a = Csr();  // the wavefront kernel reads the grid's faces
+  M.a.off.assign(1, 0);
+  M.fwd = Schedule();
+  M.bwd = Schedule();
+}
+
+// The host hierarchy of the mixed form: the grid's own when it is an aggregation
+// hierarchy, else (grids without solid cells, which the reference coarsens geometrically
+// with linear interpolation) an aggregation hierarchy of 2x2x2 bins built on first use.
+// Its levels are point-smoothed bin grids like those of the grids with buildings, which
+// the mixed form's fast paths and coarse-correction scale are made for.
+int mixed_host_hierarchy_impl(cfdg_grid* G, std::shared_ptr<Hierarchy>& out) {
+  if (!G->host_mg) return fail(CFDG_ERR_INVALID, "mixed form: no multigrid hierarchy");
+  if (G->host_mg->masked) {
+    out = G->host_mg;
+    return 0;
+  }
+  if (!G->host_mg_mx) {
+    Hierarchy H;
+    Poller P;
+    if (int e = build_aggregation_hierarchy(G->h, P, H)) {
+      if (e == CFDG_E035) return fail(e, "CFD-E035: numerics.pressure_preconditioner: multigrid coarse Cholesky lost positive definiteness");
+      return fail(e, "mixed form: aggregation hierarchy setup failed");
+    }
+    if (H.levels.size() > 1) reindex_level0(G, H);
+    G->host_mg_mx = std::make_shared<Hierarchy>(std::move(H));
+  }
+  out = G->host_mg_mx;
+  return 0;
+}
+
 int build_mg_dev(cfdg_grid* G, const Poller& poll) {
   Hierarchy H;
   if (int e = build_hierarchy(G->h, poll, H)) {
@@ -1296,35 +1353,7 @@ int build_mg_dev(cfdg_grid* G, const Poller& poll) {
   const bool lines = !H.levels.empty() && !H.levels[0].lines.empty();
   D->full0 = G->structured && H.levels.size() > 1 && !lines;
   D->coop0 = lines && H.levels.size() > 1;
-  if (D->full0) {
-    // Re-index level 0 from compact fluid numbering to full-grid cells.
-    MgLevel& M = H.levels[0];
-    const int32_t N = (int32_t)G->h.cells;
-    std::vector<int32_t> full(M.n);
-    for (int32_t j = 0; j < M.n; ++j) full[j] = H.masked ? H.fluid_indices[j] : j;
-    std::vector<double> diag(N, 0.0);
-    for (int32_t j = 0; j < M.n; ++j) diag[full[j]] = M.diag[j];
-    M.diag = std::move(diag);
-    for (auto& m : M.groups.col) m = full[m];
-    for (auto& m : M.restrict.col) m = full[m];
-    Csr P;
-    P.off.assign(N + 1, 0);
-    for (int32_t j = 0; j < M.n; ++j) P.off[full[j] + 1] = M.prolong.off[j + 1] - M.prolong.off[j];
-    for (int32_t c = 0; c < N; ++c) P.off[c + 1] += P.off[c];
-    P.col.resize(M.prolong.col.size());
-    P.val.resize(M.prolong.val.size());
-    for (int32_t j = 0; j < M.n; ++j)
-      for (int32_t k = 0; k < M.prolong.off[j + 1] - M.prolong.off[j]; ++k) {
-        P.col[P.off[full[j]] + k] = M.prolong.col[M.prolong.off[j] + k];
-        P.val[P.off[full[j]] + k] = M.prolong.val[M.prolong.off[j] + k];
-      }
-    M.prolong = std::move(P);
-    M.n = N;
-    M.a = Csr();  // the wavefront kernel reads the grid's faces
-    M.a.off.assign(1, 0);
-    M.fwd = Schedule();
-    M.bwd = Schedule();
-  }
+  if (D->full0) reindex_level0(G, H);
   for (size_t l = 0; l < H.levels.size(); ++l) {
     MgLevel& M = H.levels[l];
     DevLevel& L = D->levels[l];
@@ -1483,6 +1512,7 @@ int prepare_mg_impl(cfdg_grid* G, const Poller& poll, cfdg_info* info) {
     if (se)
       return fail(CFDG_E034, "CFD-E034: numerics.pressure_preconditioner: multigrid requires finite positive pressure face weights");
     G->mg.reset();
+    G->host_mg_mx.reset();
     G->mixed.reset();
     G->solo.reset();
     reset_chunk(G);
@@ -1686,6 +1716,12 @@ int project_mixed(cfdg_grid* G, double* d_u, double* d_p, double dt, double tol,
   inf->hierarchy_builds = builds, inf->hierarchy_levels = levels, inf->hierarchy_cells = cells;
   inf->hierarchy_nonzeros = nnz;
   inf->hierarchy_bytes = hbytes;
+  if (G->host_mg_mx) {  // the solve ran on the aggregation hierarchy: its levels
+    inf->hierarchy_levels = G->host_mg_mx->level_cells.size();
+    inf->hierarchy_cells = inf->hierarchy_nonzeros = 0;
+    for (auto v : G->host_mg_mx->level_cells) inf->hierarchy_cells += v;
+    for (auto v : G->host_mg_mx->level_nonzeros) inf->hierarchy_nonzeros += v;
+  }
   inf->multigrid_setup_seconds = setup;
   if (code == CFDG_E031) return fail(code, "CFD-E031: incompatible flux in a closed fluid component");
   if (code == CFDG_E032) return fail(code, "CFD-E032: pressure CG lost positive definiteness");
@@ -2086,6 +2122,8 @@ int prepare_multigrid(cfdg_grid* G) {
   Poller P;
   return prepare_mg_impl(G, P, nullptr);
 }
+
+int mixed_host_hierarchy(cfdg_grid* G, std::shared_ptr<Hierarchy>& out) { return mixed_host_hierarchy_impl(G, out); }
 
 int plain_compat_center(cfdg_grid* G, cudaStream_t s) {
   Scalars init{};

@@ -265,6 +265,23 @@ __device__ __forceinline__ void close_seg(const FineCase* FC, MState* ST, Seg& g
   const int per_ = (n_ + gridDim.x - 1) / gridDim.x; \
   const int t0_ = blockIdx.x * per_, t1_ = min(n_, t0_ + per_);
 
+// The fine-level kernels that take groups of tiles: up to PG consecutive tiles of one case
+// per step of a block's loop, so the fixed cost of a tile (its work-list entry, the case's
+// state and descriptor) is paid once per group and a warp's loads of several rows are in
+// flight together. tile_run: the length of the run of consecutive tiles of t's case that
+// starts at list entry ti (at most PG, inside the block's range).
+constexpr int PG = 4;
+__device__ __forceinline__ int tile_run(const int2* tiles, int ti, int t1, int2 t) {
+  int2 u[PG - 1];
+#pragma unroll
+  for (int m = 1; m < PG; ++m) u[m - 1] = ti + m < t1 ? tiles[ti + m] : make_int2(-1, 0);
+  int n = 1;
+#pragma unroll
+  for (int m = 1; m < PG; ++m)
+    if (n == m && u[m - 1].x == t.x && u[m - 1].y == t.y + m) n = m + 1;
+  return n;
+}
+
 // 1/y when y is a positive power of two whose reciprocal is a normal number, else 0. A
 // product with it is the quotient by y bit for bit (the same real value, rounded the same
 // way): FP64 division is ~20x dearer than a product on this part.
@@ -629,47 +646,94 @@ struct FinUpdate {
 };
 
 // B: e += alpha p, r -= alpha q; |r| decides the end of the inner solve.
-__device__ __forceinline__ void b_update(const FineCase* FC, MState* ST, const int2 t, int& cached_, double* sh,
-                                    int& seg_n) {
+// The slot ranges of the n tiles lt .. lt+n-1 hold one float4 per thread each (row
+// tiles of at most 4 * TILE slots, 16-byte aligned): the group path of the element-wise
+// kernels, every operand of the group loaded before any result is stored. Otherwise the
+// tiles run one at a time.
+__device__ __forceinline__ bool group4(const FineCase& F, int sb, int nxh) {
+  return !(sb & 3) && !(F.N2 & 3) && RT * 2 * nxh <= 4 * TILE;
+}
+
+// B: e += alpha p, r -= alpha q; |r| decides the end of the inner solve. One reduction
+// partial per tile, as in the one-tile path, so the bits do not depend on the grouping.
+__device__ __forceinline__ void b_update(const FineCase* FC, MState* ST, const int2 t, int n, int& cached_,
+                                         int& seg_n) {
   FINE_PROLOGUE(S.state == RUN)
   const float alpha = (float)S.alpha;
-  float hi = 0.0f, lo = 0.0f;
-  if (!((sb | se) & 3)) {
-    // Four slots per thread: every operand of a tile in flight at once.
-    for (int c = sb + 4 * threadIdx.x; c < se; c += 4 * TILE) {
-      float4 e = ld4(F.e + c);
-      const float4 p = ld4(F.p + c), q = ld4(F.q + c);
-      float4 r = ld4(F.r32 + c);
-      e.x = fmaf(alpha, p.x, e.x), e.y = fmaf(alpha, p.y, e.y), e.z = fmaf(alpha, p.z, e.z), e.w = fmaf(alpha, p.w, e.w);
-      r.x = fmaf(-alpha, q.x, r.x), r.y = fmaf(-alpha, q.y, r.y), r.z = fmaf(-alpha, q.z, r.z);
-      r.w = fmaf(-alpha, q.w, r.w);
-      st4(F.e + c, e);
-      st4(F.r32 + c, r);
-      dd_add(fmaf(r.x, r.x, fmaf(r.y, r.y, fmaf(r.z, r.z, r.w * r.w))), hi, lo);
+  const int T = RT * 2 * nxh_;
+  if (group4(F, sb, nxh_)) {
+    float4 e[PG], p[PG], q[PG], r[PG];
+    bool ok[PG];
+#pragma unroll
+    for (int m = 0; m < PG; ++m) {
+      const int c = sb + m * T + 4 * threadIdx.x;
+      ok[m] = m < n && 4 * (int)threadIdx.x < T && c < F.N2;
+      if (ok[m]) e[m] = ld4(F.e + c), p[m] = ld4(F.p + c), q[m] = ld4(F.q + c), r[m] = ld4(F.r32 + c);
     }
-  } else {
-    for (int c = sb + threadIdx.x; c < se; c += TILE) {
-      F.e[c] = fmaf(alpha, F.p[c], F.e[c]);
-      const float r = fmaf(-alpha, F.q[c], F.r32[c]);
-      F.r32[c] = r;
-      dd_add_prod(r, r, hi, lo);
+#pragma unroll
+    for (int m = 0; m < PG; ++m) {
+      if (m >= n) break;
+      float hi = 0.0f, lo = 0.0f;
+      if (ok[m]) {
+        const int c = sb + m * T + 4 * threadIdx.x;
+        float4 ev = e[m], rv = r[m];
+        const float4 pv = p[m], qv = q[m];
+        ev.x = fmaf(alpha, pv.x, ev.x), ev.y = fmaf(alpha, pv.y, ev.y), ev.z = fmaf(alpha, pv.z, ev.z);
+        ev.w = fmaf(alpha, pv.w, ev.w);
+        rv.x = fmaf(-alpha, qv.x, rv.x), rv.y = fmaf(-alpha, qv.y, rv.y), rv.z = fmaf(-alpha, qv.z, rv.z);
+        rv.w = fmaf(-alpha, qv.w, rv.w);
+        st4(F.e + c, ev);
+        st4(F.r32 + c, rv);
+        dd_add(fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, fmaf(rv.z, rv.z, rv.w * rv.w))), hi, lo);
+      }
+      tile_partial2(hi, lo, F, lt + m, seg_n);
     }
+    return;
   }
-  tile_partial2(hi, lo, F, lt, seg_n);
+  for (int m = 0; m < n; ++m) {
+    const int b0 = sb + m * T, b1 = min(F.N2, b0 + T);
+    float hi = 0.0f, lo = 0.0f;
+    if (!((b0 | b1) & 3)) {
+      for (int c = b0 + 4 * threadIdx.x; c < b1; c += 4 * TILE) {
+        float4 e = ld4(F.e + c);
+        const float4 p = ld4(F.p + c), q = ld4(F.q + c);
+        float4 r = ld4(F.r32 + c);
+        e.x = fmaf(alpha, p.x, e.x), e.y = fmaf(alpha, p.y, e.y), e.z = fmaf(alpha, p.z, e.z), e.w = fmaf(alpha, p.w, e.w);
+        r.x = fmaf(-alpha, q.x, r.x), r.y = fmaf(-alpha, q.y, r.y), r.z = fmaf(-alpha, q.z, r.z);
+        r.w = fmaf(-alpha, q.w, r.w);
+        st4(F.e + c, e);
+        st4(F.r32 + c, r);
+        dd_add(fmaf(r.x, r.x, fmaf(r.y, r.y, fmaf(r.z, r.z, r.w * r.w))), hi, lo);
+      }
+    } else {
+      for (int c = b0 + threadIdx.x; c < b1; c += TILE) {
+        F.e[c] = fmaf(alpha, F.p[c], F.e[c]);
+        const float r = fmaf(-alpha, F.q[c], F.r32[c]);
+        F.r32[c] = r;
+        dd_add_prod(r, r, hi, lo);
+      }
+    }
+    tile_partial2(hi, lo, F, lt + m, seg_n);
+  }
 }
 __global__ void __launch_bounds__(TILE) k_update(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   __shared__ double sh[32];
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
   Seg g;
-  for (int ti = t0_; ti < t1_; ++ti) {
+  for (int ti = t0_; ti < t1_;) {
     const int2 t = tiles[ti];
-    SKIP_CASE(t, S_.state == RUN)
+    if (ST[t.x].state != RUN) {  // the rest of this case's tiles in the range
+      ti += FC[t.x].ntiles - t.y;
+      continue;
+    }
     if (t.x != g.ci) {
       close_seg(FC, ST, g, sh, FinUpdate());
       g.ci = t.x;
     }
-    b_update(FC, ST, t, cached_, sh, g.n);
+    const int n = tile_run(tiles, ti, t1_, t);
+    b_update(FC, ST, t, n, cached_, g.n);
+    ti += n;
   }
   close_seg(FC, ST, g, sh, FinUpdate());
 }
@@ -799,65 +863,123 @@ struct FinRz {
 };
 
 // F: rz' = r.z; START: rz = rz', p = z (beta = 0) -> RUN; RUN: beta = rz'/rz.
-__device__ __forceinline__ void b_rz(const FineCase* FC, MState* ST, const int2 t, int& cached_, double* sh,
-                                    int& seg_n) {
+__device__ __forceinline__ void b_rz(const FineCase* FC, MState* ST, const int2 t, int n, int& cached_, int& seg_n) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
-  float hi = 0.0f, lo = 0.0f;
-  if (!((sb | se) & 3)) {
-    for (int c = sb + 4 * threadIdx.x; c < se; c += 4 * TILE) {
-      const float4 r = ld4(F.r32 + c), z = ld4(F.x0 + c);
-      dd_add(fmaf(r.x, z.x, fmaf(r.y, z.y, fmaf(r.z, z.z, r.w * z.w))), hi, lo);
+  const int T = RT * 2 * nxh_;
+  if (group4(F, sb, nxh_)) {
+    float4 r[PG], z[PG];
+    bool ok[PG];
+#pragma unroll
+    for (int m = 0; m < PG; ++m) {
+      const int c = sb + m * T + 4 * threadIdx.x;
+      ok[m] = m < n && 4 * (int)threadIdx.x < T && c < F.N2;
+      if (ok[m]) r[m] = ld4(F.r32 + c), z[m] = ld4(F.x0 + c);
     }
-  } else {
-    for (int c = sb + threadIdx.x; c < se; c += TILE) dd_add_prod(F.r32[c], F.x0[c], hi, lo);
+#pragma unroll
+    for (int m = 0; m < PG; ++m) {
+      if (m >= n) break;
+      float hi = 0.0f, lo = 0.0f;
+      if (ok[m]) dd_add(fmaf(r[m].x, z[m].x, fmaf(r[m].y, z[m].y, fmaf(r[m].z, z[m].z, r[m].w * z[m].w))), hi, lo);
+      tile_partial2(hi, lo, F, lt + m, seg_n);
+    }
+    return;
   }
-  tile_partial2(hi, lo, F, lt, seg_n);
+  for (int m = 0; m < n; ++m) {
+    const int b0 = sb + m * T, b1 = min(F.N2, b0 + T);
+    float hi = 0.0f, lo = 0.0f;
+    if (!((b0 | b1) & 3)) {
+      for (int c = b0 + 4 * threadIdx.x; c < b1; c += 4 * TILE) {
+        const float4 r = ld4(F.r32 + c), z = ld4(F.x0 + c);
+        dd_add(fmaf(r.x, z.x, fmaf(r.y, z.y, fmaf(r.z, z.z, r.w * z.w))), hi, lo);
+      }
+    } else {
+      for (int c = b0 + threadIdx.x; c < b1; c += TILE) dd_add_prod(F.r32[c], F.x0[c], hi, lo);
+    }
+    tile_partial2(hi, lo, F, lt + m, seg_n);
+  }
 }
 __global__ void __launch_bounds__(TILE) k_rz(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   __shared__ double sh[32];
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
   Seg g;
-  for (int ti = t0_; ti < t1_; ++ti) {
+  for (int ti = t0_; ti < t1_;) {
     const int2 t = tiles[ti];
-    SKIP_CASE(t, S_.state == RUN || S_.state == START)
+    if (!in_state(ST[t.x], RUN, START)) {  // the rest of this case's tiles in the range
+      ti += FC[t.x].ntiles - t.y;
+      continue;
+    }
     if (t.x != g.ci) {
       close_seg(FC, ST, g, sh, FinRz());
       g.ci = t.x;
     }
-    b_rz(FC, ST, t, cached_, sh, g.n);
+    const int n = tile_run(tiles, ti, t1_, t);
+    b_rz(FC, ST, t, n, cached_, g.n);
+    ti += n;
   }
   close_seg(FC, ST, g, sh, FinRz());
 }
 
 // G: p = z + beta p (z is the V-cycle's level-0 solution x0).
-__device__ __forceinline__ void b_p(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
+__device__ __forceinline__ void b_p(const FineCase* FC, MState* ST, const int2 t, int n, int& cached_) {
   FINE_PROLOGUE(S.state == RUN)
   const float beta = (float)S.beta;
-  if (!((sb | se) & 3)) {
-    if (S.beta == 0.0) {
-      for (int c = sb + 4 * threadIdx.x; c < se; c += 4 * TILE) st4(F.p + c, ld4(F.x0 + c));
-    } else {
-      for (int c = sb + 4 * threadIdx.x; c < se; c += 4 * TILE) {
+  const bool copy = S.beta == 0.0;
+  const int T = RT * 2 * nxh_;
+  if (group4(F, sb, nxh_)) {
+    float4 p[PG], z[PG];
+    bool ok[PG];
+#pragma unroll
+    for (int m = 0; m < PG; ++m) {
+      const int c = sb + m * T + 4 * threadIdx.x;
+      ok[m] = m < n && 4 * (int)threadIdx.x < T && c < F.N2;
+      if (ok[m]) {
+        z[m] = ld4(F.x0 + c);
+        if (!copy) p[m] = ld4(F.p + c);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < PG; ++m)
+      if (ok[m]) {
+        float4 v = z[m];
+        if (!copy) {
+          v.x = fmaf(beta, p[m].x, z[m].x), v.y = fmaf(beta, p[m].y, z[m].y);
+          v.z = fmaf(beta, p[m].z, z[m].z), v.w = fmaf(beta, p[m].w, z[m].w);
+        }
+        st4(F.p + sb + m * T + 4 * threadIdx.x, v);
+      }
+    return;
+  }
+  const int se_g = min(F.N2, sb + n * T);
+  if (!((sb | se_g) & 3)) {
+    for (int c = sb + 4 * threadIdx.x; c < se_g; c += 4 * TILE) {
+      if (copy) {
+        st4(F.p + c, ld4(F.x0 + c));
+      } else {
         float4 p = ld4(F.p + c);
         const float4 z = ld4(F.x0 + c);
         p.x = fmaf(beta, p.x, z.x), p.y = fmaf(beta, p.y, z.y), p.z = fmaf(beta, p.z, z.z), p.w = fmaf(beta, p.w, z.w);
         st4(F.p + c, p);
       }
     }
-  } else if (S.beta == 0.0) {
-    for (int c = sb + threadIdx.x; c < se; c += TILE) F.p[c] = F.x0[c];
+  } else if (copy) {
+    for (int c = sb + threadIdx.x; c < se_g; c += TILE) F.p[c] = F.x0[c];
   } else {
-    for (int c = sb + threadIdx.x; c < se; c += TILE) F.p[c] = fmaf(beta, F.p[c], F.x0[c]);
+    for (int c = sb + threadIdx.x; c < se_g; c += TILE) F.p[c] = fmaf(beta, F.p[c], F.x0[c]);
   }
 }
 __global__ void __launch_bounds__(TILE) k_p(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = t0_; ti < t1_; ++ti) {
+  for (int ti = t0_; ti < t1_;) {
     const int2 t = tiles[ti];
-    SKIP_CASE(t, S_.state == RUN)
-    b_p(FC, ST, t, cached_);
+    if (ST[t.x].state != RUN) {  // the rest of this case's tiles in the range
+      ti += FC[t.x].ntiles - t.y;
+      continue;
+    }
+    const int n = tile_run(tiles, ti, t1_, t);
+    b_p(FC, ST, t, n, cached_);
+    ti += n;
   }
 }
 
@@ -1326,48 +1448,89 @@ __global__ void __launch_bounds__(TILE) k_v_restrict(const FineCase* FC, MState*
 // x0 += P x1 on the colour-0 slots only (the prolongation's rows are the split layout's
 // slots; padding rows are empty): the first post-smoothing half sweep (colour 1) rewrites
 // every colour-1 slot without reading it, so their coarse correction would be dead work.
-__device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
+// One call covers the n tiles lt .. lt+n-1 of the case.
+__device__ __forceinline__ void b_v_prolong(const FineCase* FC, MState* ST, const int2 t, int n, int& cached_) {
   FINE_PROLOGUE(S.state == RUN || S.state == START)
-  const int rows_t = min(RT, F.n[1] * F.n[2] - lt * RT);
-  if (F.bin1) {
-    // One warp per row; the parent of the cell in colour-0 slot s (i = 2s + par) is bin
-    // (s, j/2, k/2). Solid cells take a correction too: no interior face reads them and
-    // the last post-smoothing half sweep (colour 0) sets them to zero.
-    int j, k, rb;
-    if (!warp_row(F, lt, warp, j, k, rb)) return;
-    const int par = (j + k) & 1, jk = (j >> 1) + (k >> 1), h1 = F.h1;
-    const int base1 = ((k >> 1) * F.nb1[1] + (j >> 1)) * F.nbh1;
-    float* __restrict__ x = F.x0 + lay(lt * RT + warp, 0, nxh_, 0);
+  const int rows = F.n[1] * F.n[2];
+  if (F.bin1 && nxh_ <= 64) {
+    // One warp per row of each tile; the parent of the cell in colour-0 slot s
+    // (i = 2s + par) is bin (s, j/2, k/2). Every load of the group before any store.
+    // Solid cells take a correction too: no interior face reads them and the last
+    // post-smoothing half sweep (colour 0) sets them to zero.
+    const int ny = F.n[1], h1 = F.h1, nb1y = F.nb1[1], nbh = F.nbh1;
     const float* __restrict__ x1 = F.x1;
+    float* __restrict__ x0 = F.x0;
     const float a = F.pscale;
-    for (int sl = lane; sl < nxh_; sl += 32)
-      if (2 * sl + par < nx_) x[sl] = fmaf(a, x1[((sl + jk) & 1) * h1 + base1 + (sl >> 1)], x[sl]);
-    return;
-  }
-  if (F.pinj) {  // x0 += x1[parent]: the same value as the weight-1 row below
-    for (int m = threadIdx.x; m < rows_t * nxh_; m += TILE) {
-      const int c = lay(lt * RT + m / nxh_, 0, nxh_, m % nxh_);
-      const int q = F.pinj[c];
-      if (q >= 0) F.x0[c] = fmaf(F.pscale, F.x1[q], F.x0[c]);
+    int idx[PG][2];
+    float v1[PG][2], v0[PG][2];
+#pragma unroll
+    for (int m = 0; m < PG; ++m) {
+      const int r = (lt + m) * RT + warp;
+      const bool rowok = m < n && r < rows;
+      const int j = r % ny, k = r / ny;
+      const int par = (j + k) & 1, jk = (j >> 1) + (k >> 1), base1 = ((k >> 1) * nb1y + (j >> 1)) * nbh;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int sl = lane + 32 * q;
+        const bool ok = rowok && sl < nxh_ && 2 * sl + par < nx_;
+        idx[m][q] = ok ? lay(r, 0, nxh_, sl) : -1;
+        v1[m][q] = ok ? x1[((sl + jk) & 1) * h1 + base1 + (sl >> 1)] : 0.0f;
+        v0[m][q] = ok ? x0[idx[m][q]] : 0.0f;
+      }
     }
+#pragma unroll
+    for (int m = 0; m < PG; ++m)
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+        if (idx[m][q] >= 0) x0[idx[m][q]] = fmaf(a, v1[m][q], v0[m][q]);
     return;
   }
-  for (int m = threadIdx.x; m < rows_t * nxh_; m += TILE) {
-    const int c = lay(lt * RT + m / nxh_, 0, nxh_, m % nxh_);
-    const int b = F.p_off[c], e = F.p_off[c + 1];
-    if (b == e) continue;
-    float sum = 0.0f;
-    for (int kk = b; kk < e; ++kk) sum = fmaf(F.p_w[kk], F.x1[F.p_col[kk]], sum);
-    F.x0[c] += sum;
+  for (int mt = 0; mt < n; ++mt) {
+    const int ltm = lt + mt;
+    const int rows_t = min(RT, rows - ltm * RT);
+    if (F.bin1) {  // rows longer than 64 slots per colour: one row per warp and tile
+      int j, k, rb;
+      if (!warp_row(F, ltm, warp, j, k, rb)) continue;
+      const int par = (j + k) & 1, jk = (j >> 1) + (k >> 1), h1 = F.h1;
+      const int base1 = ((k >> 1) * F.nb1[1] + (j >> 1)) * F.nbh1;
+      float* __restrict__ x = F.x0 + lay(ltm * RT + warp, 0, nxh_, 0);
+      const float* __restrict__ x1 = F.x1;
+      const float a = F.pscale;
+      for (int sl = lane; sl < nxh_; sl += 32)
+        if (2 * sl + par < nx_) x[sl] = fmaf(a, x1[((sl + jk) & 1) * h1 + base1 + (sl >> 1)], x[sl]);
+      continue;
+    }
+    if (F.pinj) {  // x0 += x1[parent]: the same value as the weight-1 row below
+      for (int m = threadIdx.x; m < rows_t * nxh_; m += TILE) {
+        const int c = lay(ltm * RT + m / nxh_, 0, nxh_, m % nxh_);
+        const int q = F.pinj[c];
+        if (q >= 0) F.x0[c] = fmaf(F.pscale, F.x1[q], F.x0[c]);
+      }
+      continue;
+    }
+    for (int m = threadIdx.x; m < rows_t * nxh_; m += TILE) {
+      const int c = lay(ltm * RT + m / nxh_, 0, nxh_, m % nxh_);
+      const int b = F.p_off[c], e = F.p_off[c + 1];
+      if (b == e) continue;
+      // The linear-interpolation rows (up to 8 entries) in entry order, four gathers in
+      // flight at a time (gather_sum keeps the order of the fmaf chain).
+      const float sum = gather_sum(F.p_col, F.p_w, F.x1, b, e, 0.0f);
+      F.x0[c] += sum;
+    }
   }
 }
 __global__ void __launch_bounds__(TILE) k_v_prolong(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   TILE_RANGE
   int cached_ = -1;  // case whose descriptor is in shared memory
-  for (int ti = t0_; ti < t1_; ++ti) {
+  for (int ti = t0_; ti < t1_;) {
     const int2 t = tiles[ti];
-    SKIP_CASE(t, S_.state == RUN || S_.state == START)
-    b_v_prolong(FC, ST, t, cached_);
+    if (!in_state(ST[t.x], RUN, START)) {  // the rest of this case's tiles in the range
+      ti += FC[t.x].ntiles - t.y;
+      continue;
+    }
+    const int n = tile_run(tiles, ti, t1_, t);
+    b_v_prolong(FC, ST, t, n, cached_);
+    ti += n;
   }
 }
 
@@ -2338,7 +2501,9 @@ bool encode_split(CUtensorMap& m, const void* base, bool u16, int nxh, int rows,
 // contiguous (colour c owns rows [coff[c], coff[c+1])): sweeps then read the right-hand
 // side, 1/diag and x of consecutive rows without an index list.
 int build_case(cfdg_grid* G, CaseState& cs) {
-  const Hierarchy& H = *G->host_mg;
+  std::shared_ptr<Hierarchy> Hp;
+  if (int e = mixed_host_hierarchy(G, Hp)) return e;
+  const Hierarchy& H = *Hp;
   // Coarse corrections of an aggregation (masked) hierarchy are scaled by the grid's
   // over-correction factor (cfdg_grid_set_coarse_scale): the piecewise-constant
   // prolongation under-corrects smooth errors, and the scaled correction stays symmetric

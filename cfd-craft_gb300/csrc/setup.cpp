@@ -769,12 +769,7 @@ static int build_unmasked(const HostGrid& g, const Poller& poll, Hierarchy& h) {
   return 0;
 }
 
-int build_hierarchy(const HostGrid& g, const Poller& poll, Hierarchy& h) {
-  if (g.n_components == 0) return CFDG_E034;
-  bool any_solid = false;
-  for (auto v : g.fluid) any_solid |= v == 0;
-  int e = (any_solid || g.n_components != 1) ? build_masked(g, poll, h) : build_unmasked(g, poll, h);
-  if (e) return e;
+static void finish_hierarchy(Hierarchy& h) {
   for (auto& l : h.levels) {
     Csr pattern = l.a;
     l.fwd = schedule(pattern, false);
@@ -782,6 +777,22 @@ int build_hierarchy(const HostGrid& g, const Poller& poll, Hierarchy& h) {
     h.level_cells.push_back((uint64_t)l.n);
     h.level_nonzeros.push_back((uint64_t)l.a.val.size() + (uint64_t)l.n);
   }
+}
+
+int build_hierarchy(const HostGrid& g, const Poller& poll, Hierarchy& h) {
+  if (g.n_components == 0) return CFDG_E034;
+  bool any_solid = false;
+  for (auto v : g.fluid) any_solid |= v == 0;
+  int e = (any_solid || g.n_components != 1) ? build_masked(g, poll, h) : build_unmasked(g, poll, h);
+  if (e) return e;
+  finish_hierarchy(h);
+  return 0;
+}
+
+int build_aggregation_hierarchy(const HostGrid& g, const Poller& poll, Hierarchy& h) {
+  if (g.n_components == 0) return CFDG_E034;
+  if (int e = build_masked(g, poll, h)) return e;
+  finish_hierarchy(h);
   return 0;
 }
 

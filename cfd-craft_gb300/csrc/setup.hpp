@@ -123,6 +123,9 @@ struct Hierarchy {
 
 // multigrid.rs:530-645 / masked.rs:181-291. Returns 0 or a CFDG_* code.
 int build_hierarchy(const HostGrid& g, const Poller& poll, Hierarchy& h);
+// The aggregation (masked.rs) hierarchy whether or not the grid has solid cells: the
+// mixed form's hierarchy on grids the reference coarsens geometrically.
+int build_aggregation_hierarchy(const HostGrid& g, const Poller& poll, Hierarchy& h);
 
 // The exact signature a hierarchy was built from (multigrid.rs:158-222).
 struct Signature {

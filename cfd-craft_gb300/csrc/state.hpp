@@ -199,6 +199,9 @@ struct cfdg_grid {
   long long wave_spin_limit = WAVE_SPIN_LIMIT;  // cfdg_debug_wave_stall
   int wave_hold_tile = -1;
   std::shared_ptr<cfdg::Hierarchy> host_mg;  // the hierarchy as uploaded (level 0 re-indexed when full0)
+  // Mixed form on grids without solid cells: the aggregation hierarchy it runs on (level 0
+  // re-indexed to the full grid), built on first use; null until then and for masked grids.
+  std::shared_ptr<cfdg::Hierarchy> host_mg_mx;
   std::shared_ptr<void> mixed;               // the mixed-precision form's device state (mixed.cu)
   std::shared_ptr<struct cfdg_batch> solo;   // a one-grid batch for cfdg_project in the mixed form
   // Face coefficients change only through cfdg_grid_update_faces, which bumps
@@ -241,6 +244,7 @@ struct cfdg_batch;
 namespace cfdg {
 // engine.cu helpers used by the mixed form (the grid's lock is held by the caller).
 int prepare_multigrid(cfdg_grid* G);                     // builds or reuses the hierarchy
+int mixed_host_hierarchy(cfdg_grid* G, std::shared_ptr<Hierarchy>& out);  // the mixed form's host hierarchy
 int plain_compat_center(cfdg_grid* G, cudaStream_t s);  // E031 check of G->b, then G->bc = centred b
 void plain_center(cfdg_grid* G, double* x, cudaStream_t s);
 }  // namespace cfdg

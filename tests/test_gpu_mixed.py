@@ -293,8 +293,9 @@ def test_bin_grid_first_coarse_level_gives_the_same_bits(pkg):
     """The first coarse level laid out as the 2x2x2 bin grid (restriction children and
     prolongation parents from bin positions, sweeps and residual through computed
     bin-stencil columns) against the aggregates' colour order with index lists: the same
-    projected bits and iterations, alone and in a batch; grids the bin layout does not fit
-    (no buildings: a geometric hierarchy) keep the index lists."""
+    projected bits and iterations, alone and in a batch. The grid without buildings runs
+    on the mixed form's aggregation hierarchy and takes the bin grid too; a grid with a
+    sealed pocket (closed groups on level 0) keeps the index lists."""
     rng = np.random.default_rng(23)
     cases = [pkg.synth.case((64, 64, 32), 2.0, inflow=5.0, preconditioner="multigrid",
                             boxes=pkg.synth.random_boxes(rng, 8, (128.0, 128.0, 64.0), dx=2.0)),
@@ -324,7 +325,13 @@ def test_bin_grid_first_coarse_level_gives_the_same_bits(pkg):
             d.close()
         out[bins] = (alone, bu, bp, laid)
     assert out[False][3] == [False, False, False]
-    assert out[True][3] == [True, True, False]
+    assert out[True][3] == [True, True, True]
+    gp = pkg.grid.Grid.build(mixed_cases(pkg)["pocket"])
+    dp = pkg.pressure.DeviceGrid(gp, preconditioner="multigrid", precision="mixed")
+    bp_ = pkg.pressure.Batch([dp])
+    assert [c["level1_bins"] for c in bp_.stats()["cases"]] == [False]
+    bp_.close()
+    dp.close()
     for i in range(len(grids)):
         a0, a1 = out[False][0][i], out[True][0][i]
         assert a0[2] == a1[2], i
