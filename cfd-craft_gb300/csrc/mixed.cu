@@ -81,6 +81,7 @@ struct FineCase {
   const uint16_t* flags;
   const uint8_t* fluid;
   const double* fw64;    // per-face FP64 weights (the grid's)
+  const double* diag64;  // the level-0 diagonal in FP64 (the grid's hierarchy, full-grid cells)
   const float* fw32;     // per-face FP32 weights (non-uniform grids)
   // Level-0 FP32 arrays use the colour-split row layout (slot lay(r, colour, nxh, i>>1)).
   const float* diag0;    // level-0 diagonal, 0 for solid cells
@@ -795,12 +796,40 @@ __device__ __forceinline__ void b_outer_resid(const FineCase* FC, MState* ST, co
     const double* __restrict__ bc = F.bc;
     const uint16_t* __restrict__ fl = F.flags;
     double* __restrict__ r = F.r64;
+    if (F.uniform) {
+      // A x as diag x minus the interior neighbours through one FMA each (nine FP64
+      // operations per cell against the fourteen of the reference's rounding order): on
+      // this part the FP64 pipe bounds the kernel. The rounding differs from
+      // pressure::apply's by a few ulps of diag |x|, far below the 1e-8 test.
+      const int sy = F.n[0], sz = F.n[0] * F.n[1];
+      const double mw[3] = {-F.w64[0], -F.w64[1], -F.w64[2]};
+      const double* __restrict__ d64 = F.diag64;
 #pragma unroll 4
-    for (int i = lane; i < nx_; i += 32) {
-      const int c = rb + i;
-      const double v = __dsub_rn(bc[c], op64r(F, x, c, i, j, k, fl[c]));
-      r[c] = v;
-      acc = __fma_rn(v, v, acc);
+      for (int i = lane; i < nx_; i += 32) {
+        const int c = rb + i;
+        const unsigned f = fl[c];
+        double y = 0.0;
+        if (f & 0x0fffu) {
+          y = d64[c] * x[c];
+          if (f & 1u) y = __fma_rn(mw[0], x[c - 1], y);
+          if (f & 2u) y = __fma_rn(mw[0], x[c + 1], y);
+          if (f & 4u) y = __fma_rn(mw[1], x[c - sy], y);
+          if (f & 8u) y = __fma_rn(mw[1], x[c + sy], y);
+          if (f & 16u) y = __fma_rn(mw[2], x[c - sz], y);
+          if (f & 32u) y = __fma_rn(mw[2], x[c + sz], y);
+        }
+        const double v = __dsub_rn(bc[c], y);
+        r[c] = v;
+        acc = __fma_rn(v, v, acc);
+      }
+    } else {
+#pragma unroll 4
+      for (int i = lane; i < nx_; i += 32) {
+        const int c = rb + i;
+        const double v = __dsub_rn(bc[c], op64r(F, x, c, i, j, k, fl[c]));
+        r[c] = v;
+        acc = __fma_rn(v, v, acc);
+      }
     }
   }
   tile_partial(acc, F, lt, sh, seg_n);
@@ -825,12 +854,19 @@ __global__ void __launch_bounds__(TILE) k_outer_resid(const FineCase* FC, MState
 // C2: r32 = r / |r|, e = 0.
 __device__ __forceinline__ void b_scale(const FineCase* FC, MState* ST, const int2 t, int& cached_) {
   FINE_PROLOGUE(S.state == SCALE)
+  // r / |r| in FP32: the residual converted, then scaled in FP32 (one FP64-pipe
+  // conversion per cell; the inner solve only needs its direction to FP32 precision),
+  // while |r| keeps the converted entries normal; else the FP64 product.
   const double inv = 1.0 / S.scale;
+  const bool fp32 = S.scale > 1e-25 && S.scale < 1e25;
+  const float inv32 = (float)inv;
   for (int c = sb + threadIdx.x; c < se; c += TILE) F.e[c] = 0.0f;
   int j, k, rb;
   if (!warp_row(F, lt, warp, j, k, rb)) return;
   const int r = lt * RT + warp, rp = (j + k) & 1;
-  for (int i = lane; i < nx_; i += 32) F.r32[lay(r, (i + rp) & 1, nxh_, i >> 1)] = (float)(F.r64[rb + i] * inv);
+  for (int i = lane; i < nx_; i += 32)
+    F.r32[lay(r, (i + rp) & 1, nxh_, i >> 1)] =
+        fp32 ? __double2float_rn(F.r64[rb + i]) * inv32 : (float)(F.r64[rb + i] * inv);
 }
 __global__ void __launch_bounds__(TILE) k_scale(const FineCase* FC, MState* ST, const int2* tiles, const int* count) {
   TILE_RANGE
@@ -2355,7 +2391,7 @@ __global__ void k_correct(const FineCase* FC, const MState* ST, const int2* ftil
       if (k == INTERIOR) d = div_p2(__dsub_rn(F.x64[F.fhi[ff]], F.x64[F.flo[ff]]), F.fdist[ff]);
       else if (k == OUTLET) d = F.flo[ff] >= 0 ? div_p2(-F.x64[F.flo[ff]], F.fdist[ff]) : div_p2(F.x64[F.fhi[ff]], F.fdist[ff]);
       else d = 0.0;
-      F.u[ff] = __dsub_rn(F.u[ff], __dmul_rn(F.dt, d));
+      F.u[ff] = __fma_rn(-F.dt, d, F.u[ff]);  // one rounding (the FP64 pipe bounds this kernel)
     }
   }
 }
@@ -2530,6 +2566,7 @@ int build_case(cfdg_grid* G, CaseState& cs) {
   F.flags = G->d_flags;
   F.fluid = G->d_fluid;
   F.fw64 = G->d_fw;
+  F.diag64 = G->mg->levels[0].diag;
   F.fkind = G->d_kind;
   F.flo = G->d_lo;
   F.fhi = G->d_hi;
@@ -4090,7 +4127,7 @@ int cfdg_batch_time_kernel(cfdg_batch* B, int32_t which, int32_t reps, double* m
   if (which == 0 || which == 4) bytes = 9.0 * cells;  // half the cells: rhs, 1/diag, u16 flags, x out; the other half's x in
   else if (which == 1) bytes = 10.0 * cells; // p in, u16 flags, q out
   else if (which == 2) bytes = coarse_bytes(B);
-  else if (which == 5) bytes = 26.0 * cells;  // x, b_c, r out (FP64), u16 flags
+  else if (which == 5) bytes = 34.0 * cells;  // x, b_c, diag, r out (FP64), u16 flags
   else if (which == 9) bytes = 24.0 * cells;  // e, p, r, q in; e, r out
   else if (which == 10) bytes = 8.0 * cells;  // r, z in
   else if (which == 11) bytes = 12.0 * cells; // z, p in; p out
