@@ -438,11 +438,15 @@ class Serving:
         self.drawn = [0] * self.n
         self.cells = [g.count for g in self.grids]
 
-    def perturb(self, c):
-        """u*_{s+1} = project(u*_s) + 0.05 U[-1,1] on the free faces (on the device): the
-        case's next pre-drawn noise field."""
-        self.d_u[c].add_(self.noise[c][self.drawn[c] % NOISE_POOL])
-        self.drawn[c] += 1
+    def perturb(self, cs):
+        """u*_{s+1} = project(u*_s) + 0.05 U[-1,1] on the free faces (on the device): each
+        case's next pre-drawn noise field, the cases of one round in one multi-tensor add."""
+        if not cs:
+            return
+        self.torch._foreach_add_([self.d_u[c] for c in cs],
+                                 [self.noise[c][self.drawn[c] % NOISE_POOL] for c in cs])
+        for c in cs:
+            self.drawn[c] += 1
 
     def submit(self, c):
         return self.server.submit(c, self.d_u[c].data_ptr(), self.d_p[c].data_ptr(), DT, TOL, MAX_IT)
@@ -454,13 +458,14 @@ class Serving:
         left = [steps] * self.n
         inflight = {}
         lat, infos = [], []
+        self.perturb(list(range(self.n)))
         for c in range(self.n):
-            self.perturb(c)
             inflight[self.submit(c)] = (c, time.perf_counter())
             left[c] -= 1
         while inflight:
             if srv.progress() == 0:
                 continue
+            nxt = []
             for t in list(inflight):
                 r = srv.result(t)
                 if r is None:
@@ -471,9 +476,11 @@ class Serving:
                 lat.append(time.perf_counter() - t0)
                 infos.append((c, info))
                 if left[c] > 0:
-                    self.perturb(c)
-                    inflight[self.submit(c)] = (c, time.perf_counter())
-                    left[c] -= 1
+                    nxt.append(c)
+            self.perturb(nxt)
+            for c in nxt:
+                inflight[self.submit(c)] = (c, time.perf_counter())
+                left[c] -= 1
         return lat, infos
 
     def e2e_loop(self, steps, seed=77):
@@ -559,7 +566,7 @@ class Serving:
                 nxt += 1
             for c in range(self.n):
                 if backlog[c] and not busy[c]:
-                    self.perturb(c)
+                    self.perturb([c])
                     inflight[self.submit(c)] = (c, backlog[c].pop(0))
                     busy[c] = True
             if not inflight:

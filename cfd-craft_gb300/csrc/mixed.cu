@@ -102,7 +102,8 @@ struct FineCase {
   // No closed groups on level 0: the residual before restriction is taken on colour 0
   // only (colour 1's is zero up to rounding after the last pre-smoothing half sweep), its
   // colour-1 slots stay zero and the restriction gathers colour-0 children only.
-  int resc0, pad_resc0;
+  int resc0;
+  int wbc;  // the grid has no closed components: k_rhs writes b_c (= b) itself
   // Level 1 laid out as the bin grid (bin1): aggregate of bin (I, J, K) in row
   // colour*h1 + (K*nb1[1] + J)*nbh1 + (I>>1), colour = (I+J+K)&1, nbh1 = ceil(nb1[0]/2),
   // h1 = nb1[1]*nb1[2]*nbh1; empty bins are empty rows. Valid where every 2x2x2 bin holds at
@@ -2306,6 +2307,7 @@ __device__ __forceinline__ void b_rhs(const FineCase* FC, MState* ST, const int2
     const int c = rb + i;
     if (!F.fluid[c]) {
       F.b[c] = -0.0;
+      if (F.wbc) F.bc[c] = -0.0;
       F.terms[c] = 0.0;
       continue;
     }
@@ -2322,7 +2324,9 @@ __device__ __forceinline__ void b_rhs(const FineCase* FC, MState* ST, const int2
       div = __dadd_rn(div, div_p2(__dsub_rn(uu, ul), F.dx[a]));
       if (closed) scale = __dadd_rn(scale, div_p2(__dadd_rn(fabs(ul), fabs(uu)), F.dx[a]));
     }
-    F.b[c] = div_rdt(-div, F.dt, F.rdt);
+    const double bv = div_rdt(-div, F.dt, F.rdt);
+    F.b[c] = bv;
+    if (F.wbc) F.bc[c] = bv;  // no closed components: b_c is b (no gauge)
     F.terms[c] = closed ? div_rdt(scale, F.dt, F.rdt) : 0.0;
   }
 }
@@ -2662,6 +2666,7 @@ int build_case(cfdg_grid* G, CaseState& cs) {
   if (int e = A.alloc(&F.partials, (size_t)F.ntiles * (TILE / 32))) return e;
   cs.ngroups0 = M0.groups.rows();
   F.ngroups = cs.ngroups0;
+  F.wbc = G->ncomp_groups == 0 ? 1 : 0;
   if (F.ngroups) {
     int *o, *m;
     std::vector<int32_t> mem(M0.groups.col.size());
@@ -3466,10 +3471,7 @@ int prologue(cfdg_batch* B, const std::vector<char>& on, cudaStream_t s) {
   for (size_t i = 0; i < B->cases.size(); ++i) {
     if (!on[i]) continue;
     cfdg_grid* G = B->grids[i];
-    if (G->ncomp_groups == 0) {
-      CU(cudaMemcpyAsync(G->bc, G->b, G->h.cells * 8, cudaMemcpyDeviceToDevice, s));
-      continue;
-    }
+    if (G->ncomp_groups == 0) continue;  // k_rhs wrote b_c beside b
     int rc = plain_compat_center(G, s);
     if (rc) {
       MState f = initial_state(0, 0);
