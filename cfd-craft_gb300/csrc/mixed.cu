@@ -2472,6 +2472,7 @@ struct CaseState {
   struct LevelStats {
     long long rows, nnz, ell, groups, blocks;
     int colors, jacobi;
+    int stencil = 0;  // swept through bin-stencil codes
   };
   std::vector<LevelStats> stats;  // per coarse level (diagnostics)
   int ngroups0 = 0;
@@ -2679,51 +2680,76 @@ int build_case(cfdg_grid* G, CaseState& cs) {
   // Level 1 as the bin grid (FineCase::bin1) where the grid allows it: an aggregation
   // hierarchy of three or more levels, no closed groups on level 0, uniform weights with
   // whole colour pairs per row, injection prolongation and restriction with weight 1,
-  // every aggregate inside one bin and no bin holding two. bslot: aggregate -> row.
+  // every aggregate inside one bin and no bin holding two; then the deeper non-terminal
+  // levels on the same terms, each from the bins of the level above.
   F.bin1 = 0;
-  std::vector<int32_t> bslot;
-  if (G->mx_bins && H.masked && M0.groups.rows() == 0 && F.uniform && !(F.nxh & 1) && H.levels.size() >= 3) {
-    const MgLevel& M1 = H.levels[1];
-    const int nb0 = (nx + 1) / 2, nb1 = (ny + 1) / 2, nb2 = (h.n[2] + 1) / 2, nbh = (nb0 + 1) / 2;
-    const int h1 = nb1 * nb2 * nbh;
-    bool ok = M0.restrict.rows() == M1.n && (int)M1.parity.size() == M1.n &&
-              (int64_t)M0.prolong.rows() == (int64_t)F.N;
-    for (int c = 0; c < F.N && ok; ++c) {
-      const int n = M0.prolong.off[c + 1] - M0.prolong.off[c];
-      ok = n == 0 || (n == 1 && M0.prolong.val[M0.prolong.off[c]] == 1.0);
-    }
-    std::vector<char> used(2 * (size_t)h1, 0);
-    bslot.assign(M1.n, -1);
-    for (int a = 0; a < M1.n && ok; ++a) {
-      int bin = -1, row = -1;
-      for (int q = M0.restrict.off[a]; q < M0.restrict.off[a + 1] && ok; ++q) {
-        const int c = M0.restrict.col[q];
-        const int I = (c % nx) >> 1, J = ((c / nx) % ny) >> 1, K = (c / (nx * ny)) >> 1;
-        const int b = (K * nb1 + J) * nb0 + I;
-        ok = M0.restrict.val[q] == 1.0 && (bin < 0 || b == bin);
-        if (bin < 0 && ok) {
-          bin = b;
-          const int col = (I + J + K) & 1;
-          row = col * h1 + (K * nb1 + J) * nbh + (I >> 1);
-          ok = M1.parity[a] == col;
+  // Bin levels: level l laid out as the grid of its 2x2x2 bins of level-(l-1) nodes (level
+  // 0: the cells) where every level-l aggregate lies in one bin and no bin holds two. Row
+  // of bin (I, J, K): colour*h + (K*nb[1] + J)*nbh + (I>>1), colour = (I+J+K)&1.
+  struct BinLevel {
+    bool on = false;
+    int nb[3] = {0, 0, 0}, nbh = 0, h = 0;
+    std::vector<int32_t> slot;                 // aggregate -> row
+    std::vector<std::array<int32_t, 3>> bin;   // aggregate -> bin coordinates
+  };
+  std::vector<BinLevel> binl(H.levels.size());
+  auto try_bins = [&](int l, const std::vector<std::array<int32_t, 3>>& child_xyz, const int child_n[3]) {
+    const MgLevel& Mc = H.levels[l - 1];  // restriction rows: level-l aggregates
+    const MgLevel& Ml = H.levels[l];
+    BinLevel& B = binl[l];
+    for (int a = 0; a < 3; ++a) B.nb[a] = (child_n[a] + 1) / 2;
+    B.nbh = (B.nb[0] + 1) / 2;
+    B.h = B.nb[1] * B.nb[2] * B.nbh;
+    bool ok = Mc.restrict.rows() == Ml.n && (int)Ml.parity.size() == Ml.n;
+    std::vector<char> used(2 * (size_t)B.h, 0);
+    B.slot.assign(Ml.n, -1);
+    B.bin.assign(Ml.n, {0, 0, 0});
+    for (int a = 0; a < Ml.n && ok; ++a) {
+      int row = -1;
+      std::array<int32_t, 3> bb{-1, -1, -1};
+      for (int q = Mc.restrict.off[a]; q < Mc.restrict.off[a + 1] && ok; ++q) {
+        const std::array<int32_t, 3>& xyz = child_xyz[Mc.restrict.col[q]];
+        const std::array<int32_t, 3> b{xyz[0] >> 1, xyz[1] >> 1, xyz[2] >> 1};
+        ok = row < 0 || b == bb;
+        if (row < 0 && ok) {
+          bb = b;
+          const int col = (b[0] + b[1] + b[2]) & 1;
+          row = col * B.h + (b[2] * B.nb[1] + b[1]) * B.nbh + (b[0] >> 1);
+          ok = Ml.parity[a] == col;
         }
       }
       ok = ok && row >= 0 && !used[row];
       if (ok) {
         used[row] = 1;
-        bslot[a] = row;
+        B.slot[a] = row;
+        B.bin[a] = bb;
       }
     }
-    for (int a = 0; a < M1.n && ok; ++a)
-      for (int q = M1.a.off[a]; q < M1.a.off[a + 1] && ok; ++q)
-        ok = M1.a.col[q] == a || M1.parity[M1.a.col[q]] != M1.parity[a];
+    for (int a = 0; a < Ml.n && ok; ++a)
+      for (int q = Ml.a.off[a]; q < Ml.a.off[a + 1] && ok; ++q)
+        ok = Ml.a.col[q] == a || Ml.parity[Ml.a.col[q]] != Ml.parity[a];
+    B.on = ok;
+    if (!ok) B.slot.clear(), B.bin.clear();
+  };
+  if (G->mx_bins && H.masked && M0.groups.rows() == 0 && F.uniform && !(F.nxh & 1) && H.levels.size() >= 3) {
+    bool ok = (int64_t)M0.prolong.rows() == (int64_t)F.N;
+    for (int c = 0; c < F.N && ok; ++c) {
+      const int n = M0.prolong.off[c + 1] - M0.prolong.off[c];
+      ok = n == 0 || (n == 1 && M0.prolong.val[M0.prolong.off[c]] == 1.0);
+    }
+    for (size_t q = 0; q < M0.restrict.val.size() && ok; ++q) ok = M0.restrict.val[q] == 1.0;
     if (ok) {
+      std::vector<std::array<int32_t, 3>> cells(F.N);
+      for (int c = 0; c < F.N; ++c) cells[c] = {c % nx, (c / nx) % ny, c / (nx * ny)};
+      try_bins(1, cells, h.n);
+      // Deeper non-terminal levels while the level above is a bin level.
+      for (int l = 2; l + 1 < (int)H.levels.size() && binl[l - 1].on; ++l) try_bins(l, binl[l - 1].bin, binl[l - 1].nb);
+    }
+    if (binl[1].on) {
       F.bin1 = 1;
-      F.nb1[0] = nb0, F.nb1[1] = nb1, F.nb1[2] = nb2;
-      F.nbh1 = nbh;
-      F.h1 = h1;
-    } else {
-      bslot.clear();
+      for (int a = 0; a < 3; ++a) F.nb1[a] = binl[1].nb[a];
+      F.nbh1 = binl[1].nbh;
+      F.h1 = binl[1].h;
     }
   }
   // Coarse levels 1 .. L-1: colouring (bin parity, else greedy; l1-Jacobi when more than
@@ -2737,10 +2763,10 @@ int build_case(cfdg_grid* G, CaseState& cs) {
   for (int l = 1; l <= C.nl; ++l) {
     const MgLevel& M = H.levels[l];
     const bool terminal = l == C.nl;
-    if (l == 1 && F.bin1) {
-      lcoff[1] = {0, F.h1, 2 * F.h1};
-      lcolors[1] = 2;
-      perm[1] = bslot;
+    if (binl[l].on) {
+      lcoff[l] = {0, binl[l].h, 2 * binl[l].h};
+      lcolors[l] = 2;
+      perm[l] = binl[l].slot;
       continue;
     }
     std::vector<int32_t> rows;
@@ -2768,7 +2794,7 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     MgLevel& Q = PL[l];
     const std::vector<int32_t>& P = perm[l];
     const std::vector<int32_t> none;
-    const int nout = (l == 1 && F.bin1) ? 2 * F.h1 : M.n;  // bin rows include empty bins
+    const int nout = binl[l].on ? 2 * binl[l].h : M.n;  // bin rows include empty bins
     Q.n = nout;
     Q.a = permute_csr(M.a, P, P, nout);
     Q.diag.assign(nout, 0.0);
@@ -2778,7 +2804,7 @@ int build_case(cfdg_grid* G, CaseState& cs) {
     Q.direct_off = M.direct_off;
     Q.direct_factor = M.direct_factor;
     if (l < C.nl) {
-      Q.restrict = permute_csr(M.restrict, perm[l + 1], P);
+      Q.restrict = permute_csr(M.restrict, perm[l + 1], P, binl[l + 1].on ? 2 * binl[l + 1].h : -1);
       Q.prolong = permute_csr(M.prolong, P, perm[l + 1], nout);
     }
   }
@@ -2919,13 +2945,13 @@ int build_case(cfdg_grid* G, CaseState& cs) {
       L.ell_off = eo, L.ell_w = ewp, L.ell_col = ec, L.ell_val = ev, L.idiag = idp;
       cs.stats.push_back({M.n, (long long)M.a.col.size(), (long long)ecol.size(), M.groups.rows(),
                           L.terminal ? M.direct_idx.rows() : 0, L.ncolors, L.jacobi});
-      // The bin stencil of level 1 (CLev::scode): every ELL entry of every row is one of
+      // The bin stencil of a bin level (CLev::scode): every ELL entry of every row is one of
       // the row's six bin neighbours or padding, at most six per row, at most 16 distinct
       // values, and a bin row's slots per colour a multiple of the rows per sweep item.
       L.scode = nullptr;
       L.svt = nullptr;
-      if (l == 1 && F.bin1 && !L.jacobi && L.ncolors == 2 && F.nbh1 % RPI == 0 && ew[0] <= 6 && ew[1] <= 6) {
-        const int nbh = F.nbh1, nb1y = F.nb1[1], h1 = F.h1;
+      if (binl[l].on && !L.jacobi && L.ncolors == 2 && binl[l].nbh % RPI == 0 && ew[0] <= 6 && ew[1] <= 6) {
+        const int nbh = binl[l].nbh, nb1y = binl[l].nb[1], h1 = binl[l].h;
         std::vector<unsigned long long> code(M.n, 0);
         std::vector<float> vt;
         bool ok = true;
@@ -2965,6 +2991,7 @@ int build_case(cfdg_grid* G, CaseState& cs) {
           L.svt = dv;
           L.snb1y = nb1y;
           L.snbh = nbh;
+          cs.stats.back().stencil = 1;
         }
       }
     }
@@ -4009,9 +4036,9 @@ int64_t cfdg_batch_stats_json(cfdg_batch* B, char* buf, int64_t cap) {
       const auto& v = cs.stats[l];
       snprintf(tmp, sizeof tmp,
                "%s{\"rows\": %lld, \"nnz\": %lld, \"smoother\": \"%s\", \"colors\": %d, \"ell_entries\": %lld, "
-               "\"groups\": %lld, \"blocks\": %lld}",
+               "\"groups\": %lld, \"blocks\": %lld, \"bin_stencil\": %s}",
                l ? ", " : "", v.rows, v.nnz, v.jacobi ? "l1-jacobi" : "gauss-seidel", v.colors, v.ell, v.groups,
-               v.blocks);
+               v.blocks, v.stencil ? "true" : "false");
       out += tmp;
     }
     out += "]}";

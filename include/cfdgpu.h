@@ -297,7 +297,7 @@ int cfdg_batch_time_kernel(cfdg_batch *batch, int32_t which, int32_t reps, doubl
 /* Per case and coarse level of the batch's FP32 hierarchies, as JSON: rows, nonzeros,
  * smoother colours, ELL entries (with padding), closed groups and terminal blocks; and
  * whether level 1 is laid out as the bin grid ("level1_bins", per case) and swept through
- * computed bin-stencil columns ("level1_stencil"), and
+ * computed bin-stencil columns ("level1_stencil"; per level "bin_stencil"), and
  * whether the level-0 half sweeps run staged through the tensor memory accelerator
  * ("staged_sweeps": every case with uniform weights and ceil(nx/2) a multiple of 8). Writes
  * at most cap bytes (NUL-terminated) and returns the length the full text needs, or a

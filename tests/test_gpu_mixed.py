@@ -317,6 +317,9 @@ def test_bin_grid_first_coarse_level_gives_the_same_bits(pkg):
         batch = pkg.pressure.Batch(dgs)
         laid = [c["level1_bins"] for c in batch.stats()["cases"]]
         assert [c["level1_stencil"] for c in batch.stats()["cases"]] == laid
+        # deeper levels take bin stencils too where their bins hold one aggregate each
+        deep = [sum(lv["bin_stencil"] for lv in c["levels"]) for c in batch.stats()["cases"]]
+        assert all(d >= (1 if b else 0) for d, b in zip(deep, laid)), deep
         bu, bp = [u.copy() for u in us], [np.zeros(g.count) for g in grids]
         res = batch.project(bu, bp, [0.1] * len(grids), 1e-8, 10000)
         assert all(code == 0 for code, _ in res)
