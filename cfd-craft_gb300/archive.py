@@ -9,12 +9,16 @@ then complete.json holding the manifest's hash. fields.json is the solver State
 budgets, floor_events, pressure_iterations, monitor_history) as compact JSON;
 geometry.json carries the fluid mask's hash (grid.rs:550, mask_sha256) and counts.
 
-Scope: flow-only runs (laminar stepping or projections on the device). Constituent
-archives need the mass budgets of advance_scalar (emitted, inflow, outflow), which the
-device transport does not accumulate, so a state with concentrations is refused. The
-summary holds the fields the checker and a reader need (schema, name, termination,
-assessment, model scope, steps, time, constituents), not the reference's full run
-summary (timings, profile, checks). The manifest carries the reference's keys
+Scope: laminar runs on the device, with or without constituents. A constituent carries
+its concentration field, its mass budget (solver.rs:190-202: initial, emitted, inflow and
+outflow kg, the increments kept by cfdg_scalar_step_budget), its current rates
+(cfdg_scalar_rates) and its receptor values (cfdg_receptors_sample); the writer adds the
+summary's evidence record (solver.rs ScalarEvidence: mass, budget defect, extrema,
+negative mass, rates, receptors) and the probes.csv rows. Gases only (no deposition) and
+point or volume receptors (path receptors are refused). The summary holds the fields the
+checker and a reader need (schema, name, termination, assessment, model scope, steps,
+time, constituents), not the reference's full run summary (timings, profile, checks;
+the constituent records omit steady_residual). The manifest carries the reference's keys
 (output.rs:218-226); source_sha256 and executable_sha256 identify this engine's sources
 and built library rather than the reference's CLI binary.
 """
@@ -46,6 +50,13 @@ def _write(path: str, data: bytes):
     os.replace(tmp, path)
 
 
+def _rust_e17(v: float) -> str:
+    """A float as Rust formats it with {:.17e}: 17 digits after the point and the exponent
+    without sign padding or leading zeros (1.00000000000000000e0, 2.5...e-5)."""
+    mant, exp = f"{v:.17e}".split("e")
+    return f"{mant}e{int(exp)}"
+
+
 def _floats(a):
     return [float(v) for v in np.asarray(a, dtype=np.float64).ravel()]
 
@@ -68,18 +79,61 @@ def _engine_identity():
     return h.hexdigest(), exe
 
 
+def constituent_record(sp: dict, grid, c, budget: dict, rates, receptors: dict) -> dict:
+    """The summary's evidence for one constituent (solver.rs ScalarEvidence) from its
+    archived field, budget, current rates (emitted, inflow, outflow in kg/s) and receptor
+    values: mass = Σ c over fluid cells × volume (an exact sum, math.fsum), the budget
+    defect mass - initial - emitted - inflow + outflow and its ratio to their sum, the
+    extrema (minimum over fluid cells, maximum over all cells and at least 0) and the mass
+    of negative concentrations."""
+    import math
+
+    fluid = np.asarray(grid.fluid).astype(bool)
+    c = np.asarray(c, dtype=np.float64)
+    volume = float(grid.volume)
+    mass = math.fsum(c[fluid].tolist()) * volume
+    defect = mass - budget["initial_kg"] - budget["emitted_kg"] - budget["inflow_kg"] + budget["outflow_kg"]
+    scale = max(budget["initial_kg"] + budget["emitted_kg"] + budget["inflow_kg"] + budget["outflow_kg"], 1e-30)
+    negative = -math.fsum(np.minimum(c[fluid], 0.0).tolist()) * volume
+    return {
+        "id": sp["id"],
+        "mass_kg": mass,
+        "emitted_kg": float(budget["emitted_kg"]),
+        "inflow_kg": float(budget["inflow_kg"]),
+        "outflow_kg": float(budget["outflow_kg"]),
+        "budget_defect_kg": defect,
+        "relative_budget_defect": abs(defect) / scale,
+        "minimum_kg_m3": float(c[fluid].min()) if fluid.any() else 0.0,
+        "maximum_kg_m3": max(float(c.max()), 0.0),
+        "negative_mass_kg": negative,
+        "source_rate_kg_s": float(rates[0]),
+        "boundary_inflow_rate_kg_s": float(rates[1]),
+        "boundary_outflow_rate_kg_s": float(rates[2]),
+        "receptors_kg_m3": {str(k): float(v) for k, v in sorted(receptors.items())},
+    }
+
+
 def write_run(out: str, case: dict, grid, velocity, pressure, *, steps: int, time_s: float,
-              pressure_iterations: int = 0, k=None, epsilon=None, input_sha256: str = None,
+              pressure_iterations: int = 0, k=None, epsilon=None, constituents=None, input_sha256: str = None,
               initial_state_sha256: str = None, engine: str = "cfd-craft_gb300") -> list:
-    """Writes the archive of a flow-only run into the new directory `out`.
+    """Writes the archive of a run into the new directory `out`.
 
     velocity (F) and pressure (N) are host arrays (for example the device fields after
-    cfdg_step_device, copied back). k and epsilon default to zeros (laminar). Every value
+    cfdg_step_device, copied back). k and epsilon default to zeros (laminar).
+    constituents: one dict per case constituent, in case order, with "concentration" (N),
+    "budget" (initial_kg, emitted_kg, inflow_kg, outflow_kg), "rates" (the current
+    emitted, inflow and outflow rates) and "receptors" ({receptor id: value}). Every value
     must be finite: the reference serialises the state with serde_json, which cannot write
     NaN or infinity, and its checker rejects non-finite fields (ValueError here). Returns
     the names of the files written, manifest.json and complete.json last."""
-    if case.get("constituents"):
-        raise ValueError("archives with constituents need the transport budgets, which the device path does not keep")
+    species = case.get("constituents") or []
+    constituents = constituents or []
+    if len(constituents) != len(species):
+        raise ValueError("one constituent entry per case constituent, in case order")
+    if any(r.get("kind") == "path" for r in case.get("receptors", [])) and species:
+        raise ValueError("path receptors are not written by this archive writer")
+    if any(sp.get("particle") is not None for sp in species):
+        raise ValueError("particle constituents (deposition) are not written by this archive writer")
     n, f = int(grid.count), int(grid.n_faces)
     velocity = np.asarray(velocity, dtype=np.float64)
     pressure = np.asarray(pressure, dtype=np.float64)
@@ -90,6 +144,12 @@ def write_run(out: str, case: dict, grid, velocity, pressure, *, steps: int, tim
     for name, a in (("velocity", velocity), ("pressure", pressure), ("k", k), ("epsilon", epsilon)):
         if not np.all(np.isfinite(a)):
             raise ValueError(f"non-finite {name}: a run archive holds finite fields only")
+    records = []
+    for sp, entry in zip(species, constituents):
+        conc = np.asarray(entry["concentration"], dtype=np.float64)
+        if conc.shape != (n,) or not np.all(np.isfinite(conc)):
+            raise ValueError(f"constituent {sp['id']}: one finite concentration per cell")
+        records.append(constituent_record(sp, grid, conc, entry["budget"], entry["rates"], entry["receptors"]))
     source_sha256, executable_sha256 = _engine_identity()
     os.makedirs(out, exist_ok=False)
     files = {}
@@ -116,7 +176,7 @@ def write_run(out: str, case: dict, grid, velocity, pressure, *, steps: int, tim
         "steps": int(steps),
         "time_s": float(time_s),
         "pressure_iterations": int(pressure_iterations),
-        "constituents": [],
+        "constituents": records,
         "engine": engine,
         "source_sha256": source_sha256,
         "build_version": f"{engine} {ENGINE_VERSION}",
@@ -132,7 +192,11 @@ def write_run(out: str, case: dict, grid, velocity, pressure, *, steps: int, tim
         "components": int(grid.n_components),
     }
     put("geometry.json", json.dumps(geometry, indent=2).encode())
-    put("probes.csv", b"constituent,receptor,concentration_kg_m3\n")
+    probes = "constituent,receptor,concentration_kg_m3\n"
+    for rec in records:  # output.rs:195-201: quoted fields, the value as Rust's {:.17e}
+        for rid, value in rec["receptors_kg_m3"].items():
+            probes += '"{}","{}",{}\n'.format(rec["id"].replace('"', '""'), rid.replace('"', '""'), _rust_e17(value))
+    put("probes.csv", probes.encode())
     fields = {
         "steps": int(steps),
         "time_s": float(time_s),
@@ -140,8 +204,9 @@ def write_run(out: str, case: dict, grid, velocity, pressure, *, steps: int, tim
         "pressure": _floats(pressure),
         "k": _floats(k),
         "epsilon": _floats(epsilon),
-        "concentrations": [],
-        "budgets": [],
+        "concentrations": [_floats(e["concentration"]) for e in constituents],
+        "budgets": [{k2: float(e["budget"][k2]) for k2 in ("initial_kg", "emitted_kg", "inflow_kg", "outflow_kg")}
+                    for e in constituents],
         "floor_events": 0,
         "pressure_iterations": int(pressure_iterations),
         "monitor_history": [],

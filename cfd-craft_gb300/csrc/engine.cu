@@ -2005,6 +2005,81 @@ __device__ __forceinline__ bool face_eval(const ScalarDev& D, int a, long long f
   return true;
 }
 
+// The rates transport.rs rhs_into returns with the right-hand side (solver.rs:828-833):
+// emitted = Σ source × volume, and over the faces on the domain boundary (lo or hi absent)
+// the outward flux's positive part (outflow) and negative part (inflow), in kg/s, with the
+// face flux (u donor + diffusion) area of the same transport faces. Per block, in part[3b ..
+// 3b+2]; k_scalar_budget sums the blocks in order. The sums differ from the reference's
+// sequential ones by rounding only (the budgets serve mass accounting, not bits).
+constexpr int SR_BLOCKS = 128, SR_THREADS = 256;
+__global__ void __launch_bounds__(SR_THREADS) k_scalar_rates(ScalarDev D, const double* __restrict__ x,
+                                                            const double* __restrict__ u,
+                                                            const double* __restrict__ d,
+                                                            const double* __restrict__ source, long long N,
+                                                            double* __restrict__ part) {
+  double em = 0.0, inflow = 0.0, outflow = 0.0;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x, nth = (long long)gridDim.x * blockDim.x;
+  for (long long i = tid; i < N; i += nth) em += source[i];
+  for (int a = 0; a < 3; ++a) {
+    const int b = (a + 1) % 3, cc = (a + 2) % 3, nb = D.n[b], nc = D.n[cc];
+    const long long plane = (long long)nb * nc;
+    for (long long q = tid; q < 2 * plane; q += nth) {
+      const int side = q >= plane ? 1 : 0;
+      const long long r = q - side * plane;
+      int pos[3];
+      pos[a] = side ? D.n[a] : 0;
+      pos[b] = (int)(r % nb);
+      pos[cc] = (int)(r / nb);
+      const long long f = D.face_off[a] + ((long long)pos[2] * D.fdim[a][1] + pos[1]) * D.fdim[a][0] + pos[0];
+      const int lo = D.lo[f], hi = D.hi[f];
+      if (lo >= 0 && hi >= 0) continue;  // not on the boundary (periodic wrap)
+      const uint8_t k = D.kind[f];
+      if (k != INTERIOR && k != INLET && k != OUTLET) continue;
+      const double cl = lo >= 0 ? x[lo] : 0.0, cr = hi >= 0 ? x[hi] : 0.0;
+      const double uf = u[f];
+      const double donor = uf >= 0.0 ? cl : cr;
+      const double diffusivity = lo >= 0 ? d[lo] : (hi >= 0 ? d[hi] : 0.0);
+      const double diff = k == OUTLET ? 0.0 : diffusivity * (cl - cr) / D.dist[f];
+      const double flux = (uf * donor + diff) * D.area[f];
+      const double outward = lo >= 0 ? flux : -flux;
+      outflow += fmax(outward, 0.0);
+      inflow += fmax(-outward, 0.0);
+    }
+  }
+  __shared__ double sh[3][SR_THREADS / 32];
+  double v[3] = {em, inflow, outflow};
+  for (int k = 0; k < 3; ++k) {
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if ((threadIdx.x & 31) == 0) sh[k][threadIdx.x >> 5] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int w = 0; w < SR_THREADS / 32; ++w) t += sh[threadIdx.x][w];
+    part[3 * blockIdx.x + threadIdx.x] = t;
+  }
+}
+
+// The block sums of the two stages' rates in block order; the emission is the source sum
+// times the volume. budget += dt (a + b) / 2 per quantity (solver.rs:851-853) when budget is
+// set; rates (when set) receive the first stage's rates.
+__global__ void k_scalar_budget(const double* __restrict__ pa, const double* __restrict__ pb, double volume, double dt,
+                                double* __restrict__ budget, double* __restrict__ rates) {
+  if (threadIdx.x >= 3) return;
+  const int k = threadIdx.x;
+  double a = 0.0, b = 0.0;
+  for (int blk = 0; blk < SR_BLOCKS; ++blk) {
+    a += pa[3 * blk + k];
+    if (pb) b += pb[3 * blk + k];
+  }
+  if (k == 0) {
+    a *= volume;
+    b *= volume;
+  }
+  if (rates) rates[k] = a;
+  if (budget) budget[k] += 0.5 * dt * (a + b);
+}
+
 // One pass of the SSPRK2 step over a (32, 8, 8) tile of cells. MODE 0 (solver.rs:845-847):
 // stage = c + dt rhs(c). MODE 1 (solver.rs:848-850): c = (c + stage + dt rhs(stage)) / 2, in
 // place (a thread reads c only at its own cell). Blocks are (32, 8); every thread reaches
@@ -2460,10 +2535,13 @@ static Pow2 pow2_of(double y, bool inverse) {
   return Pow2{v, k, 1};
 }
 
-int cfdg_scalar_step_device(cfdg_grid* G, const double* d_u, double* d_c, const double* d_diff, const double* d_source,
-                            double dt) {
+// mode 0: one SSPRK2 step; 1: the step and its budget increments into d_budget (device,
+// three doubles); 2: the current rates of d_c only, into the host array rates.
+static int scalar_impl(cfdg_grid* G, const double* d_u, double* d_c, const double* d_diff, const double* d_source,
+                       double dt, int mode, double* d_budget, double* rates) {
   if (int e = check_grid(G)) return e;
   if (!d_u || !d_c || !d_diff || !d_source) return fail(CFDG_ERR_INVALID, "null array");
+  if ((mode == 1 && !d_budget) || (mode == 2 && !rates)) return fail(CFDG_ERR_INVALID, "null budget or rates");
   std::lock_guard<std::mutex> lk(G->mu);
   CU(cudaSetDevice(G->ctx->device));
   for (int a = 0; a < 3; ++a)
@@ -2495,23 +2573,64 @@ int cfdg_scalar_step_device(cfdg_grid* G, const double* d_u, double* d_c, const 
     }
   double* stage = G->st_sc;
   cudaStream_t s = G->stream;
+  if (mode != 0 && !G->sc_part) {
+    if (int e = G->arena.alloc(&G->sc_part, (size_t)2 * 3 * SR_BLOCKS + 3)) return e;
+  }
+  if (mode == 2) {
+    k_scalar_rates<<<SR_BLOCKS, SR_THREADS, 0, s>>>(D, d_c, d_u, d_diff, d_source, N, G->sc_part);
+    double* dr = G->sc_part + 6 * SR_BLOCKS;
+    k_scalar_budget<<<1, 32, 0, s>>>(G->sc_part, nullptr, D.volume, 0.0, nullptr, dr);
+    count(2);
+    CU(cudaMemcpyAsync(rates, dr, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    return 0;
+  }
   const dim3 blk(STX, STY), grd((G->h.n[0] + STX - 1) / STX, (G->h.n[1] + STY - 1) / STY, (G->h.n[2] + STZ - 1) / STZ);
+  // The budget's rates: of c before the second pass overwrites it, and of the stage.
+  auto rates_of_stages = [&]() {
+    if (mode != 1) return;
+    k_scalar_rates<<<SR_BLOCKS, SR_THREADS, 0, s>>>(D, d_c, d_u, d_diff, d_source, N, G->sc_part);
+    k_scalar_rates<<<SR_BLOCKS, SR_THREADS, 0, s>>>(D, stage, d_u, d_diff, d_source, N, G->sc_part + 3 * SR_BLOCKS);
+    count(2);
+  };
   bool p2 = G->sc_uniform && D.inv_volume.ok;
   for (int a = 0; a < 3; ++a)
     for (int t = 0; t < 3; ++t)
       if (G->sc_used[a][t]) p2 = p2 && D.area_p[a][t].ok && D.inv_dist_p[a][t].ok;
   if (p2) {
     k_scalar_pass<true, true, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+    rates_of_stages();
     k_scalar_pass<true, true, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
   } else if (G->sc_uniform) {
     k_scalar_pass<true, false, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+    rates_of_stages();
     k_scalar_pass<true, false, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
   } else {
     k_scalar_pass<false, false, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+    rates_of_stages();
     k_scalar_pass<false, false, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+  }
+  if (mode == 1) {
+    k_scalar_budget<<<1, 32, 0, s>>>(G->sc_part, G->sc_part + 3 * SR_BLOCKS, D.volume, dt, d_budget, nullptr);
+    count();
   }
   CU(cudaGetLastError());
   return 0;
+}
+
+int cfdg_scalar_step_device(cfdg_grid* G, const double* d_u, double* d_c, const double* d_diff, const double* d_source,
+                            double dt) {
+  return scalar_impl(G, d_u, d_c, d_diff, d_source, dt, 0, nullptr, nullptr);
+}
+
+int cfdg_scalar_step_budget(cfdg_grid* G, const double* d_u, double* d_c, const double* d_diff, const double* d_source,
+                            double dt, double* d_budget) {
+  return scalar_impl(G, d_u, d_c, d_diff, d_source, dt, 1, d_budget, nullptr);
+}
+
+int cfdg_scalar_rates(cfdg_grid* G, const double* d_u, const double* d_c, const double* d_diff, const double* d_source,
+                      double* rates) {
+  return scalar_impl(G, d_u, const_cast<double*>(d_c), d_diff, d_source, 0.0, 2, nullptr, rates);
 }
 
 // solver.rs:1035-1037: a receptor's value is Σ c[cell] w over its weights in order, an

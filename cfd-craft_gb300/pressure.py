@@ -211,6 +211,19 @@ class DeviceGrid:
         self._check(rc)
         return LinearInfo(info.iterations, info.relative_residual, info.as_dict())
 
+    def scalar_step_budget(self, u_ptr: int, c_ptr: int, d_ptr: int, source_ptr: int, dt, budget_ptr: int):
+        """The step and its budget increments (emitted, inflow, outflow in kg) into the three
+        device doubles at budget_ptr (cfdg_scalar_step_budget)."""
+        self._check(self.L.cfdg_scalar_step_budget(self.h, C.c_void_p(u_ptr), C.c_void_p(c_ptr), C.c_void_p(d_ptr),
+                                                   C.c_void_p(source_ptr), float(dt), C.c_void_p(budget_ptr)))
+
+    def scalar_rates(self, u_ptr: int, c_ptr: int, d_ptr: int, source_ptr: int):
+        """(emitted, inflow, outflow) rates in kg/s of the device field at c_ptr (cfdg_scalar_rates)."""
+        r = (C.c_double * 3)()
+        self._check(self.L.cfdg_scalar_rates(self.h, C.c_void_p(u_ptr), C.c_void_p(c_ptr), C.c_void_p(d_ptr),
+                                             C.c_void_p(source_ptr), r))
+        return float(r[0]), float(r[1]), float(r[2])
+
     def scalar_step_device(self, u_ptr: int, c_ptr: int, d_ptr: int, source_ptr: int, dt):
         """One SSPRK2 step of a constituent on device arrays (cfdg_scalar_step_device)."""
         self._check(self.L.cfdg_scalar_step_device(self.h, C.c_void_p(u_ptr), C.c_void_p(c_ptr), C.c_void_p(d_ptr),

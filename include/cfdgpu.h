@@ -174,9 +174,22 @@ int cfdg_step_device(cfdg_grid *grid, double *d_u, double *d_p, double dt, doubl
  * velocities d_u (F), with cell diffusivities d_diff (N, m2/s: the constituent's plus
  * nu_t / Sc) and source densities d_source (N, kg/m3/s): advance_scalar
  * (solver.rs:808-855) with linear upwind (transport.rs:651-699) and zero inflow
- * concentration, bit-identical to it; the budgets are not kept. Non-periodic grids. */
+ * concentration, bit-identical to it; the budgets are not kept (cfdg_scalar_step_budget
+ * keeps them). Non-periodic grids. */
 int cfdg_scalar_step_device(cfdg_grid *grid, const double *d_u, double *d_c, const double *d_diff,
                             const double *d_source, double dt);
+/* The same step, and its mass budget (solver.rs:851-853): d_budget (device, three doubles:
+ * emitted, inflow, outflow in kg) grows by dt/2 times the sum of the two stages' rates,
+ * each the one rhs_into returns (transport.rs:651-699: source sum times the cell volume,
+ * and the positive and negative parts of the outward flux over the domain-boundary faces).
+ * The concentration gets the same bits as cfdg_scalar_step_device; the rates are summed
+ * in a fixed order of their own, within rounding of the reference's sequential sums. */
+int cfdg_scalar_step_budget(cfdg_grid *grid, const double *d_u, double *d_c, const double *d_diff,
+                            const double *d_source, double dt, double *d_budget);
+/* The current rates of d_c (kg/s) into the host array rates: emitted, inflow, outflow, as
+ * rhs_into returns them (the summary's source and boundary rates, solver.rs ScalarEvidence). */
+int cfdg_scalar_rates(cfdg_grid *grid, const double *d_u, const double *d_c, const double *d_diff,
+                      const double *d_source, double *rates);
 /* Receptors of a grid for cfdg_receptors_sample: n receptors' normalised weights as
  * receptor_weights (transport.rs:374-436) returns them, in CSR form: receptor r holds
  * cells[offsets[r] .. offsets[r+1]) with weights[...] in that order (host arrays, copied).

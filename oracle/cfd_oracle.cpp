@@ -1835,6 +1835,15 @@ void ora_scalar_step(void* gp, double* c, const double* u, const double* d, cons
     for (int k = 0; k < 3; ++k) budget[k] += 0.5 * dt * (a[k] + b[k]);
 }
 
+// transport.rs:651-699 rhs_into's returned rates of the field c: emitted (source sum times
+// the cell volume), inflow and outflow over the domain-boundary faces, in kg/s.
+void ora_scalar_rates(void* gp, const double* c, const double* u, const double* d, const double* source,
+                      double* rates) {
+  const Grid& g = *(Grid*)gp;
+  std::vector<double> r(g.count());
+  scalar_rhs(g, c, u, d, source, r.data(), rates);
+}
+
 // Laminar flow terms the projection does not need (case flow: viscosity_m2_s, acceleration_m_s2).
 void ora_grid_set_flow_terms(void* gp, double viscosity, const double* acceleration) {
   Grid* g = (Grid*)gp;

@@ -130,6 +130,7 @@ def lib():
             L.ora_momentum_rhs.restype = C.c_int32
             L.ora_momentum_rhs.argtypes = [P, dp, dp]
             L.ora_scalar_step.argtypes = [P, dp, dp, dp, dp, C.c_double, C.c_void_p]
+            L.ora_scalar_rates.argtypes = [P, dp, dp, dp, dp, dp]
             L.ora_step.restype = C.c_int32
             L.ora_step.argtypes = [P, dp, dp, C.c_double, C.c_double, C.c_uint64, C.POINTER(C.c_uint64)]
             _lib = L
@@ -245,6 +246,15 @@ class Grid:
                               _ptr(np.ascontiguousarray(d, np.float64)),
                               _ptr(np.ascontiguousarray(source, np.float64)), float(dt), bp)
         return cc
+
+    def scalar_rates(self, c, u, d, source):
+        """(emitted, inflow, outflow) in kg/s of the field c: the rates rhs_into returns
+        (transport.rs:651-699)."""
+        out = np.zeros(3)
+        lib().ora_scalar_rates(self.h, _ptr(np.ascontiguousarray(c, np.float64)),
+                               _ptr(np.ascontiguousarray(u, np.float64)), _ptr(np.ascontiguousarray(d, np.float64)),
+                               _ptr(np.ascontiguousarray(source, np.float64)), _ptr(out))
+        return float(out[0]), float(out[1]), float(out[2])
 
     def set_preconditioner(self, name):
         lib().ora_grid_set_preconditioner(self.h, PRECONDITIONER[name])

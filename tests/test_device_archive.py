@@ -2,7 +2,9 @@
 
 tests/golden/device_archive_{plain,mixed} hold archives of three laminar SSPRK2 steps
 that cfdg_step_device computed on a GB300 (plain FP64 and mixed FP32/FP64 projections),
-written by the package's archive writer; tests/golden/make_device_archive.py made them.
+written by the package's archive writer; device_archive_gas adds a gas constituent whose
+transport steps, mass budget (cfdg_scalar_step_budget), current rates and receptor values
+were computed on the device too; tests/golden/make_device_archive.py made them.
 The unmodified validation/check_fields.py of a CFD-craft checkout (its independent
 archive checker: hashes, mask, finiteness and the independent local continuity,
 validation/check_fields.py:299-530) must pass on them; it runs when a checkout is
@@ -19,7 +21,7 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
 REFERENCE = os.environ.get("CFD_CRAFT_REFERENCE", "/root/reference")
-FORMS = ("plain", "mixed")
+FORMS = ("plain", "mixed", "gas")
 
 
 def archive(form):
@@ -35,7 +37,11 @@ def test_device_archive_passes_restated_checks(pkg, form):
     path = archive(form)
     manifest = json.load(open(os.path.join(path, "manifest.json")))
     assert manifest["engine"] == "cfd-craft_gb300" and manifest["executable_sha256"]
-    max_div = check_archive(path, lambda c: pkg.grid.Grid.build(c).fluid.astype(bool))
+    from importlib import import_module
+
+    R = import_module(pkg.__name__ + ".receptors")
+    weights = lambda c, r: R.receptor_weights(pkg.grid.Grid.build(c), r)
+    max_div = check_archive(path, lambda c: pkg.grid.Grid.build(c).fluid.astype(bool), receptor_weights=weights)
     assert max_div < 1e-7
 
 
@@ -51,6 +57,8 @@ def test_device_archive_passes_reference_checker(form):
     print(form, json.dumps(result))
     assert result["passed"] is True
     assert result["max_divergence_s_inv"] < 1e-7
+    if form == "gas":  # the independent mass accounting of the device budget
+        assert len(result["scalars"]) == 1 and result["scalars"][0]["relative_defect"] < 1e-9
 
 
 def test_archive_writer_refuses_non_finite_fields(pkg, tmp_path):

@@ -185,3 +185,48 @@ def test_receptor_values_bit_identical(pkg, O):
     dg.close()
     assert np.array_equal(bits(got), bits(np.array(ref))), (got, ref)
     assert np.count_nonzero(got) >= 3
+
+
+@pytest.mark.parametrize("name", ["buildings-open-wall", "spacing-1.5m", "slip-channel"])
+def test_scalar_budget_and_rates_match_oracle(pkg, O, name):
+    """cfdg_scalar_step_budget: the concentration bit-identical to the step without budget,
+    and the budget increments (emitted, inflow, outflow; solver.rs:851-853) over several
+    steps within 1e-12 of the oracle's sequential sums; cfdg_scalar_rates: the current
+    rates of rhs_into (transport.rs:651-699) within 1e-12."""
+    torch = pytest.importorskip("torch")
+    case = flow_case(pkg, name)
+    g = pkg.grid.Grid.build(case)
+    og = O.Grid(case)
+    rng = np.random.default_rng(5)
+    code, u, _, _ = og.project(g.initial_velocity(), np.zeros(g.count), 0.1, 1e-8, 10000)
+    assert code == 0
+    u = u + np.where(g.face_kind == pkg.grid.INTERIOR, rng.uniform(-0.5, 0.5, g.n_faces), 0.0)
+    fluid = g.fluid.astype(bool)
+    d = np.where(fluid, rng.uniform(0.01, 0.3, g.count), 0.0)
+    source = np.zeros(g.count)
+    source[rng.choice(np.nonzero(fluid)[0], 4, replace=False)] = rng.uniform(1e-4, 1e-2, 4)
+    c = np.where(fluid, rng.uniform(0.0, 1e-3, g.count), 0.0)
+    dt = 0.02
+    dg = pkg.pressure.DeviceGrid(g, preconditioner=case["numerics"]["pressure_preconditioner"])
+    dev = torch.device("cuda", 0)
+    d_u, d_d, d_s = (torch.from_numpy(a.copy()).to(dev) for a in (u, d, source))
+    d_c, d_c2 = torch.from_numpy(c.copy()).to(dev), torch.from_numpy(c.copy()).to(dev)
+    d_b = torch.zeros(3, dtype=torch.float64, device=dev)
+    budget = np.zeros(3)
+    oc = c.copy()
+    for _ in range(5):
+        dg.scalar_step_budget(d_u.data_ptr(), d_c.data_ptr(), d_d.data_ptr(), d_s.data_ptr(), dt, d_b.data_ptr())
+        dg.scalar_step_device(d_u.data_ptr(), d_c2.data_ptr(), d_d.data_ptr(), d_s.data_ptr(), dt)
+        oc = og.scalar_step(oc, u, d, source, dt, budget)
+    torch.cuda.synchronize()
+    got_c = d_c.cpu().numpy()
+    assert np.array_equal(bits(got_c), bits(d_c2.cpu().numpy()))
+    assert np.array_equal(bits(got_c), bits(oc))
+    got_b = d_b.cpu().numpy()
+    scale = max(float(np.abs(budget).max()), 1e-300)
+    assert np.all(np.abs(got_b - budget) <= 1e-12 * scale), (got_b, budget)
+    rates = dg.scalar_rates(d_u.data_ptr(), d_c.data_ptr(), d_d.data_ptr(), d_s.data_ptr())
+    orates = og.scalar_rates(oc, u, d, source)
+    rscale = max(max(abs(v) for v in orates), 1e-300)
+    assert all(abs(a - b) <= 1e-12 * rscale for a, b in zip(rates, orates)), (rates, orates)
+    dg.close()
