@@ -1775,12 +1775,34 @@ static int flow_euler(Grid& g, const double* u, const double* p, double dt, doub
   return OK;
 }
 
-// transport.rs:651-699 rhs_into with linear upwind (no MUSCL slope) and a zero inlet
+// transport.rs:510-516 minmod: 0 when a b <= 0, else signum(a) min(|a|, |b|) (a is
+// nonzero then, so signum is +-1).
+static double minmod(double a, double b) {
+  if (a * b <= 0.0) return 0.0;
+  return (std::signbit(a) ? -1.0 : 1.0) * std::fmin(std::fabs(a), std::fabs(b));
+}
+// transport.rs:502-509: the cell across cell i's face on axis a, side 0 (lo) or 1 (hi),
+// when that face is interior.
+static size_t neighbor(const Grid& g, size_t i, int a, int side) {
+  const Face& f = g.faces[g.cell_faces[i][a * 2 + side]];
+  if (f.kind != K_INTERIOR) return NONE;
+  return side == 0 ? f.lo : f.hi;
+}
+// transport.rs:517-526: the monotonized-central slope of c at cell i along axis a.
+static double slope(const Grid& g, const double* c, size_t i, int a) {
+  const size_t jl = neighbor(g, i, a, 0), jh = neighbor(g, i, a, 1);
+  const double lo = jl != NONE ? c[jl] : c[i];
+  const double hi = jh != NONE ? c[jh] : c[i];
+  return minmod(0.5 * (hi - lo), minmod(2.0 * (c[i] - lo), 2.0 * (hi - c[i])));
+}
+
+// transport.rs:656-723 rhs_into with linear upwind or MUSCL (`muscl`: the donor value plus
+// or minus half the limited slope of the upwind cell along the face's axis) and a zero inlet
 // concentration (solver.rs:823-832 passes |_| 0.0), in face order.
 // Also returns the emission rate (the source densities summed, times the volume) and the
 // open-boundary inflow and outflow rates (transport.rs:717-723).
 static void scalar_rhs(const Grid& g, const double* c, const double* u, const double* d, const double* source,
-                       double* v, double rates[3]) {
+                       double* v, double rates[3], bool muscl = false) {
   const size_t N = g.count();
   double inflow = 0.0, outflow = 0.0;
   for (size_t i = 0; i < N; ++i) v[i] = source[i];
@@ -1790,8 +1812,8 @@ static void scalar_rhs(const Grid& g, const double* c, const double* u, const do
     const double cl = f.lo != NONE ? c[f.lo] : 0.0;
     const double cr = f.hi != NONE ? c[f.hi] : 0.0;
     double donor;
-    if (u[fi] >= 0.0) donor = f.lo != NONE ? cl + 0.0 : cl;
-    else donor = f.hi != NONE ? cr - 0.0 : cr;
+    if (u[fi] >= 0.0) donor = f.lo != NONE ? cl + (muscl ? 0.5 * slope(g, c, f.lo, f.axis) : 0.0) : cl;
+    else donor = f.hi != NONE ? cr - (muscl ? 0.5 * slope(g, c, f.hi, f.axis) : 0.0) : cr;
     double diffusivity;
     if (f.lo != NONE && f.hi != NONE) diffusivity = 0.5 * (d[f.lo] + d[f.hi]);
     else if (f.lo != NONE) diffusivity = d[f.lo];
@@ -1817,31 +1839,36 @@ static void scalar_rhs(const Grid& g, const double* c, const double* u, const do
 
 extern "C" {
 
-// solver.rs:808-855 advance_scalar: one SSPRK2 step of a constituent in place (linear
-// upwind, no particle terms; the budgets are not kept).
+// solver.rs:808-855 advance_scalar: one SSPRK2 step of a constituent in place (no particle
+// terms).
 // `budget` (nullable): emitted, inflow and outflow masses in kg, incremented as
 // solver.rs:851-853 does.
-void ora_scalar_step(void* gp, double* c, const double* u, const double* d, const double* source, double dt,
-                     double* budget) {
+// muscl: Advection::Muscl (transport.rs:670-694), else linear upwind.
+void ora_scalar_step_adv(void* gp, double* c, const double* u, const double* d, const double* source, double dt,
+                         double* budget, int32_t muscl) {
   const Grid& g = *(Grid*)gp;
   const size_t N = g.count();
   std::vector<double> r1(N), stage(N), r2(N);
   double a[3], b[3];
-  scalar_rhs(g, c, u, d, source, r1.data(), a);
+  scalar_rhs(g, c, u, d, source, r1.data(), a, muscl != 0);
   for (size_t i = 0; i < N; ++i) stage[i] = c[i] + dt * r1[i];
-  scalar_rhs(g, stage.data(), u, d, source, r2.data(), b);
+  scalar_rhs(g, stage.data(), u, d, source, r2.data(), b, muscl != 0);
   for (size_t i = 0; i < N; ++i) c[i] = 0.5 * (c[i] + stage[i] + dt * r2[i]);
   if (budget)
     for (int k = 0; k < 3; ++k) budget[k] += 0.5 * dt * (a[k] + b[k]);
+}
+void ora_scalar_step(void* gp, double* c, const double* u, const double* d, const double* source, double dt,
+                     double* budget) {
+  ora_scalar_step_adv(gp, c, u, d, source, dt, budget, 0);
 }
 
 // transport.rs:651-699 rhs_into's returned rates of the field c: emitted (source sum times
 // the cell volume), inflow and outflow over the domain-boundary faces, in kg/s.
 void ora_scalar_rates(void* gp, const double* c, const double* u, const double* d, const double* source,
-                      double* rates) {
+                      double* rates, int32_t muscl) {
   const Grid& g = *(Grid*)gp;
   std::vector<double> r(g.count());
-  scalar_rhs(g, c, u, d, source, r.data(), rates);
+  scalar_rhs(g, c, u, d, source, r.data(), rates, muscl != 0);
 }
 
 // Laminar flow terms the projection does not need (case flow: viscosity_m2_s, acceleration_m_s2).

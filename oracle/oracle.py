@@ -130,7 +130,8 @@ def lib():
             L.ora_momentum_rhs.restype = C.c_int32
             L.ora_momentum_rhs.argtypes = [P, dp, dp]
             L.ora_scalar_step.argtypes = [P, dp, dp, dp, dp, C.c_double, C.c_void_p]
-            L.ora_scalar_rates.argtypes = [P, dp, dp, dp, dp, dp]
+            L.ora_scalar_rates.argtypes = [P, dp, dp, dp, dp, dp, C.c_int32]
+            L.ora_scalar_step_adv.argtypes = [P, dp, dp, dp, dp, C.c_double, C.c_void_p, C.c_int32]
             L.ora_step.restype = C.c_int32
             L.ora_step.argtypes = [P, dp, dp, C.c_double, C.c_double, C.c_uint64, C.POINTER(C.c_uint64)]
             _lib = L
@@ -233,8 +234,9 @@ class Grid:
         code = lib().ora_step(self.h, _ptr(uu), _ptr(pp), float(dt), float(tol), int(max_iter), C.byref(it))
         return code, uu, pp, it.value
 
-    def scalar_step(self, c, u, d, source, dt, budget=None):
-        """advance_scalar (solver.rs:808-855): one SSPRK2 step of a constituent, linear upwind.
+    def scalar_step(self, c, u, d, source, dt, budget=None, muscl=False):
+        """advance_scalar (solver.rs:808-855): one SSPRK2 step of a constituent, linear upwind
+        or (muscl) MUSCL with the monotonized-central limiter (transport.rs:502-526,670-694).
         `budget` (a float64 array of 3, optional) accumulates the emitted, inflow and outflow
         masses in kg as solver.rs:851-853 does."""
         cc = np.array(c, dtype=np.float64, copy=True)
@@ -242,18 +244,18 @@ class Grid:
         if budget is not None:
             assert budget.dtype == np.float64 and budget.shape == (3,) and budget.flags.c_contiguous
             bp = budget.ctypes.data_as(C.c_void_p)
-        lib().ora_scalar_step(self.h, _ptr(cc), _ptr(np.ascontiguousarray(u, np.float64)),
-                              _ptr(np.ascontiguousarray(d, np.float64)),
-                              _ptr(np.ascontiguousarray(source, np.float64)), float(dt), bp)
+        lib().ora_scalar_step_adv(self.h, _ptr(cc), _ptr(np.ascontiguousarray(u, np.float64)),
+                                  _ptr(np.ascontiguousarray(d, np.float64)),
+                                  _ptr(np.ascontiguousarray(source, np.float64)), float(dt), bp, 1 if muscl else 0)
         return cc
 
-    def scalar_rates(self, c, u, d, source):
+    def scalar_rates(self, c, u, d, source, muscl=False):
         """(emitted, inflow, outflow) in kg/s of the field c: the rates rhs_into returns
         (transport.rs:651-699)."""
         out = np.zeros(3)
         lib().ora_scalar_rates(self.h, _ptr(np.ascontiguousarray(c, np.float64)),
                                _ptr(np.ascontiguousarray(u, np.float64)), _ptr(np.ascontiguousarray(d, np.float64)),
-                               _ptr(np.ascontiguousarray(source, np.float64)), _ptr(out))
+                               _ptr(np.ascontiguousarray(source, np.float64)), _ptr(out), 1 if muscl else 0)
         return float(out[0]), float(out[1]), float(out[2])
 
     def set_preconditioner(self, name):

@@ -12,6 +12,10 @@ Follows crates/cfd-craft/src/transport.rs:
     d_face (c_lo - c_hi) / distance with d_face the mean of the two cells' diffusivities
     (one cell's on a boundary face, none on outlets), flux = (u donor + diff) area, and
     flux / volume is subtracted from the lo cell and added to the hi cell;
+  * MUSCL (Advection::Muscl, transport.rs:502-526, 670-694): the donor value of a face is
+    the upwind cell's value plus (flow towards hi) or minus half its slope along the face's
+    axis, slope = minmod((c_hi - c_lo) / 2, minmod(2 (c - c_lo), 2 (c_hi - c))) with a
+    neighbour counted only through an interior face (the cell's own value otherwise);
   * receptor_weights for a point receptor (transport.rs:374-399, :428-436): trilinear
     weights between cell centres, clamped at the domain boundary, weights below 1e-14
     dropped, normalised to sum 1.
@@ -24,6 +28,11 @@ import math
 import numpy as np
 
 INTERIOR, INLET, OUTLET = 0, 3, 4
+
+
+def _minmod(a, b):
+    """minmod (transport.rs:510-516): 0 where a b <= 0, else sign(a) min(|a|, |b|)."""
+    return np.where(a * b <= 0.0, 0.0, np.sign(a) * np.minimum(np.abs(a), np.abs(b)))
 
 
 class Transport:
@@ -46,13 +55,35 @@ class Transport:
         self.dface = np.where(both, 0.5 * (dl + dh), np.where(self.lo >= 0, dl, dh))
         self.volume = float(g.volume)
 
-    def rhs(self, c, u, source, inlet_value=0.0):
-        """dc/dt (kg/m3/s) for concentrations c and face velocities u (transport.rs:651-699)."""
+    def slopes(self, c):
+        """(N, 3) monotonized-central limited slopes of c per cell and axis (MUSCL)."""
+        g = self.g
+        cf = g.cell_face_indices()
+        kind = np.asarray(g.face_kind)
+        flo, fhi = np.asarray(g.face_lo), np.asarray(g.face_hi)
+        out = np.zeros((g.count, 3))
+        for a in range(3):
+            fl, fh = cf[:, a, 0], cf[:, a, 1]
+            lo = np.where(kind[fl] == INTERIOR, c[np.maximum(flo[fl], 0)], c)
+            hi = np.where(kind[fh] == INTERIOR, c[np.maximum(fhi[fh], 0)], c)
+            out[:, a] = _minmod(0.5 * (hi - lo), _minmod(2.0 * (c - lo), 2.0 * (hi - c)))
+        return out
+
+    def rhs(self, c, u, source, inlet_value=0.0, muscl=False):
+        """dc/dt (kg/m3/s) for concentrations c and face velocities u (transport.rs:651-699),
+        linear upwind or (muscl) MUSCL donors."""
         lo, hi = self.lo, self.hi
         cl = np.where(lo >= 0, c[np.maximum(lo, 0)], inlet_value)
         cr = np.where(hi >= 0, c[np.maximum(hi, 0)], inlet_value)
         uf = u[self.faces]
-        donor = np.where(uf >= 0.0, cl, cr)
+        if muscl:
+            sl = self.slopes(c)
+            axis = np.asarray(self.g.face_axis)[self.faces].astype(np.int64)
+            dl = np.where(lo >= 0, cl + 0.5 * sl[np.maximum(lo, 0), axis], cl)
+            dh = np.where(hi >= 0, cr - 0.5 * sl[np.maximum(hi, 0), axis], cr)
+            donor = np.where(uf >= 0.0, dl, dh)
+        else:
+            donor = np.where(uf >= 0.0, cl, cr)
         diff = np.where(self.kind == OUTLET, 0.0, self.dface * (cl - cr) / self.dist)
         per_volume = (uf * donor + diff) * self.area / self.volume
         v = np.array(source, dtype=np.float64, copy=True)
