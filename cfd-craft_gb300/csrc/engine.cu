@@ -2005,6 +2005,85 @@ __device__ __forceinline__ bool face_eval(const ScalarDev& D, int a, long long f
   return true;
 }
 
+// MUSCL (transport.rs:502-526, 670-694): the donor value of a face is the upwind cell's
+// value plus (u >= 0: lo cell) or minus (hi cell) half its monotonized-central slope along
+// the face's axis; neighbours count only through interior faces. The operations are the
+// reference's, in its order (this file is compiled without FMA contraction).
+__device__ __forceinline__ double sc_minmod(double a, double b) {
+  if (a * b <= 0.0) return 0.0;
+  return (signbit(a) ? -1.0 : 1.0) * fmin(fabs(a), fabs(b));
+}
+// The face index of cell (i, j, k)'s face on axis a, side 0 (lo) or 1 (hi); on a periodic
+// axis (n faces, not n + 1) the last cell's hi face is the wrap face 0.
+__device__ __forceinline__ long long sc_face(const ScalarDev& D, int a, int i, int j, int k, int side) {
+  int p[3] = {i, j, k};
+  p[a] += side;
+  if (p[a] >= D.fdim[a][a]) p[a] -= D.fdim[a][a];
+  return D.face_off[a] + ((long long)p[2] * D.fdim[a][1] + p[1]) * D.fdim[a][0] + p[0];
+}
+__device__ __forceinline__ double sc_slope(const ScalarDev& D, const double* __restrict__ x, long long cell, int a) {
+  const int i = (int)(cell % D.n[0]), j = (int)((cell / D.n[0]) % D.n[1]), k = (int)(cell / ((long long)D.n[0] * D.n[1]));
+  const long long fl = sc_face(D, a, i, j, k, 0), fh = sc_face(D, a, i, j, k, 1);
+  const double xc = x[cell];
+  const double lo = D.kind[fl] == INTERIOR ? x[D.lo[fl]] : xc;
+  const double hi = D.kind[fh] == INTERIOR ? x[D.hi[fh]] : xc;
+  return sc_minmod(0.5 * (hi - lo), sc_minmod(2.0 * (xc - lo), 2.0 * (hi - xc)));
+}
+// The flux (kg/s) of transporting face f on axis a evaluated on x, rhs_into's arithmetic
+// from the face's own lo, hi, area and distance; false if the face does not transport.
+__device__ __forceinline__ bool sc_flux(const ScalarDev& D, int a, long long f, const double* __restrict__ x,
+                                        const double* __restrict__ u, const double* __restrict__ d, bool muscl,
+                                        double& flux) {
+  const uint8_t k = D.kind[f];
+  if (k != INTERIOR && k != INLET && k != OUTLET) return false;
+  const int lo = D.lo[f], hi = D.hi[f];
+  const double cl = lo >= 0 ? x[lo] : 0.0, cr = hi >= 0 ? x[hi] : 0.0;
+  const double uf = u[f];
+  double donor;
+  if (uf >= 0.0) donor = lo >= 0 ? cl + (muscl ? 0.5 * sc_slope(D, x, lo, a) : 0.0) : cl;
+  else donor = hi >= 0 ? cr - (muscl ? 0.5 * sc_slope(D, x, hi, a) : 0.0) : cr;
+  double diffusivity;
+  if (lo >= 0 && hi >= 0) diffusivity = 0.5 * (d[lo] + d[hi]);
+  else if (lo >= 0) diffusivity = d[lo];
+  else if (hi >= 0) diffusivity = d[hi];
+  else diffusivity = 0.0;
+  const double diff = k == OUTLET ? 0.0 : diffusivity * (cl - cr) / D.dist[f];
+  flux = (uf * donor + diff) * D.area[f];
+  return true;
+}
+
+// One pass of the SSPRK2 step with MUSCL donors, one thread per cell: the cell's six faces
+// in face order (the x faces, then y, then z; on an axis the lower face index first, the
+// periodic wrap face of the last cell before its lo face, and on a one-cell periodic axis
+// the face's lo update before its hi update), each face's flux / volume added where the
+// cell is the face's hi and subtracted where it is its lo, as rhs_into applies them, so
+// every cell receives the reference's sum; a face's flux is the same value for both cells.
+// MODE 0: stage = c + dt rhs(c); MODE 1: c = (c + stage + dt rhs(stage)) / 2.
+template <int MODE>
+__global__ void k_scalar_muscl(ScalarDev D, double* __restrict__ c, double* __restrict__ stage,
+                               const double* __restrict__ u, const double* __restrict__ d,
+                               const double* __restrict__ source, double dt, long long N) {
+  const double* __restrict__ x = MODE == 0 ? c : stage;
+  for (long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x; cell < N;
+       cell += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(cell % D.n[0]), j = (int)((cell / D.n[0]) % D.n[1]), k = (int)(cell / ((long long)D.n[0] * D.n[1]));
+    double v = source[cell];
+    for (int a = 0; a < 3; ++a) {
+      const long long fl = sc_face(D, a, i, j, k, 0), fh = sc_face(D, a, i, j, k, 1);
+      double flux;
+      if (fh <= fl) {
+        if (sc_flux(D, a, fh, x, u, d, true, flux)) v = v - flux / D.volume;
+        if (sc_flux(D, a, fl, x, u, d, true, flux)) v = v + flux / D.volume;
+      } else {
+        if (sc_flux(D, a, fl, x, u, d, true, flux)) v = v + flux / D.volume;
+        if (sc_flux(D, a, fh, x, u, d, true, flux)) v = v - flux / D.volume;
+      }
+    }
+    if (MODE == 0) stage[cell] = c[cell] + dt * v;
+    else c[cell] = 0.5 * (c[cell] + stage[cell] + dt * v);
+  }
+}
+
 // The rates transport.rs rhs_into returns with the right-hand side (solver.rs:828-833):
 // emitted = Σ source × volume, and over the faces on the domain boundary (lo or hi absent)
 // the outward flux's positive part (outflow) and negative part (inflow), in kg/s, with the
@@ -2016,7 +2095,7 @@ __global__ void __launch_bounds__(SR_THREADS) k_scalar_rates(ScalarDev D, const 
                                                             const double* __restrict__ u,
                                                             const double* __restrict__ d,
                                                             const double* __restrict__ source, long long N,
-                                                            double* __restrict__ part) {
+                                                            double* __restrict__ part, int muscl) {
   double em = 0.0, inflow = 0.0, outflow = 0.0;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x, nth = (long long)gridDim.x * blockDim.x;
   for (long long i = tid; i < N; i += nth) em += source[i];
@@ -2033,14 +2112,8 @@ __global__ void __launch_bounds__(SR_THREADS) k_scalar_rates(ScalarDev D, const 
       const long long f = D.face_off[a] + ((long long)pos[2] * D.fdim[a][1] + pos[1]) * D.fdim[a][0] + pos[0];
       const int lo = D.lo[f], hi = D.hi[f];
       if (lo >= 0 && hi >= 0) continue;  // not on the boundary (periodic wrap)
-      const uint8_t k = D.kind[f];
-      if (k != INTERIOR && k != INLET && k != OUTLET) continue;
-      const double cl = lo >= 0 ? x[lo] : 0.0, cr = hi >= 0 ? x[hi] : 0.0;
-      const double uf = u[f];
-      const double donor = uf >= 0.0 ? cl : cr;
-      const double diffusivity = lo >= 0 ? d[lo] : (hi >= 0 ? d[hi] : 0.0);
-      const double diff = k == OUTLET ? 0.0 : diffusivity * (cl - cr) / D.dist[f];
-      const double flux = (uf * donor + diff) * D.area[f];
+      double flux;
+      if (!sc_flux(D, a, f, x, u, d, muscl != 0, flux)) continue;
       const double outward = lo >= 0 ? flux : -flux;
       outflow += fmax(outward, 0.0);
       inflow += fmax(-outward, 0.0);
@@ -2577,7 +2650,7 @@ static int scalar_impl(cfdg_grid* G, const double* d_u, double* d_c, const doubl
     if (int e = G->arena.alloc(&G->sc_part, (size_t)2 * 3 * SR_BLOCKS + 3)) return e;
   }
   if (mode == 2) {
-    k_scalar_rates<<<SR_BLOCKS, SR_THREADS, 0, s>>>(D, d_c, d_u, d_diff, d_source, N, G->sc_part);
+    k_scalar_rates<<<SR_BLOCKS, SR_THREADS, 0, s>>>(D, d_c, d_u, d_diff, d_source, N, G->sc_part, G->sc_muscl);
     double* dr = G->sc_part + 6 * SR_BLOCKS;
     k_scalar_budget<<<1, 32, 0, s>>>(G->sc_part, nullptr, D.volume, 0.0, nullptr, dr);
     count(2);
@@ -2589,15 +2662,21 @@ static int scalar_impl(cfdg_grid* G, const double* d_u, double* d_c, const doubl
   // The budget's rates: of c before the second pass overwrites it, and of the stage.
   auto rates_of_stages = [&]() {
     if (mode != 1) return;
-    k_scalar_rates<<<SR_BLOCKS, SR_THREADS, 0, s>>>(D, d_c, d_u, d_diff, d_source, N, G->sc_part);
-    k_scalar_rates<<<SR_BLOCKS, SR_THREADS, 0, s>>>(D, stage, d_u, d_diff, d_source, N, G->sc_part + 3 * SR_BLOCKS);
+    k_scalar_rates<<<SR_BLOCKS, SR_THREADS, 0, s>>>(D, d_c, d_u, d_diff, d_source, N, G->sc_part, G->sc_muscl);
+    k_scalar_rates<<<SR_BLOCKS, SR_THREADS, 0, s>>>(D, stage, d_u, d_diff, d_source, N, G->sc_part + 3 * SR_BLOCKS,
+                                                    G->sc_muscl);
     count(2);
   };
   bool p2 = G->sc_uniform && D.inv_volume.ok;
   for (int a = 0; a < 3; ++a)
     for (int t = 0; t < 3; ++t)
       if (G->sc_used[a][t]) p2 = p2 && D.area_p[a][t].ok && D.inv_dist_p[a][t].ok;
-  if (p2) {
+  if (G->sc_muscl) {
+    const int nb = (int)std::min<long long>(((long long)N + 255) / 256, 152LL * 16);
+    k_scalar_muscl<0><<<nb, 256, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt, N); tick(G);
+    rates_of_stages();
+    k_scalar_muscl<1><<<nb, 256, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt, N); tick(G);
+  } else if (p2) {
     k_scalar_pass<true, true, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
     rates_of_stages();
     k_scalar_pass<true, true, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
@@ -2621,6 +2700,14 @@ static int scalar_impl(cfdg_grid* G, const double* d_u, double* d_c, const doubl
 int cfdg_scalar_step_device(cfdg_grid* G, const double* d_u, double* d_c, const double* d_diff, const double* d_source,
                             double dt) {
   return scalar_impl(G, d_u, d_c, d_diff, d_source, dt, 0, nullptr, nullptr);
+}
+
+int cfdg_grid_set_advection(cfdg_grid* G, int32_t muscl) {
+  if (int e = check_grid(G)) return e;
+  if (muscl != 0 && muscl != 1) return fail(CFDG_ERR_INVALID, "advection is 0 (linear upwind) or 1 (MUSCL)");
+  std::lock_guard<std::mutex> lk(G->mu);
+  G->sc_muscl = muscl;
+  return 0;
 }
 
 int cfdg_scalar_step_budget(cfdg_grid* G, const double* d_u, double* d_c, const double* d_diff, const double* d_source,

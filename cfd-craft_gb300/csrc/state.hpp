@@ -225,6 +225,7 @@ struct cfdg_grid {
   double flow_size[3] = {0, 0, 0}, flow_vel[3] = {0, 0, 0}, flow_nu = 0, flow_acc[3] = {0, 0, 0};
   double *st_cu = nullptr, *st_v = nullptr, *st_v2 = nullptr, *st_p1 = nullptr;
   double* sc_part = nullptr;  // scalar transport rates: two stages of per-block partials, then three rates
+  int sc_muscl = 0;           // scalar transport advection: 0 linear upwind, 1 MUSCL (cfdg_grid_set_advection)
   double* st_sc = nullptr;  // scalar transport: the SSPRK2 stage (N)
   // Receptors (cfdg_receptors_set): CSR of cells and weights, in receptor order.
   int32_t rc_n = 0, rc_cap_n = 0;

@@ -32,6 +32,7 @@ EXPORTS = (
     "cfdg_server_submit", "cfdg_server_progress", "cfdg_server_result", "cfdg_server_pending", "cfdg_server_stats_json", "cfdg_server_set_chunk", "cfdg_grid_set_cycle", "cfdg_grid_set_coarse_scale", "cfdg_grid_set_flow", "cfdg_step_device", "cfdg_scalar_step_device", "cfdg_receptors_set", "cfdg_receptors_sample", "cfdg_debug_momentum_update",
     "cfdg_debug_wave_stall", "cfdg_grid_set_sweep_tile", "cfdg_server_submit_host", "cfdg_batch_debug_rhs",
     "cfdg_debug_div_check", "cfdg_grid_set_coarse_layout", "cfdg_scalar_step_budget", "cfdg_scalar_rates",
+    "cfdg_grid_set_advection",
 )
 
 
@@ -173,6 +174,7 @@ def load(path: str = LIB_PATH):
         L.cfdg_scalar_step_device.argtypes = [P, P, P, P, P, C.c_double]
         L.cfdg_scalar_step_budget.argtypes = [P, P, P, P, P, C.c_double, P]
         L.cfdg_scalar_rates.argtypes = [P, P, P, P, P, C.POINTER(C.c_double)]
+        L.cfdg_grid_set_advection.argtypes = [P, C.c_int32]
         L.cfdg_receptors_set.argtypes = [P, C.c_int32, P, P, P]
         L.cfdg_receptors_sample.argtypes = [P, P, P]
         PP = C.POINTER(C.c_void_p)

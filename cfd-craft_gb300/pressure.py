@@ -217,6 +217,14 @@ class DeviceGrid:
         self._check(self.L.cfdg_scalar_step_budget(self.h, C.c_void_p(u_ptr), C.c_void_p(c_ptr), C.c_void_p(d_ptr),
                                                    C.c_void_p(source_ptr), float(dt), C.c_void_p(budget_ptr)))
 
+    def set_advection(self, scheme: str):
+        """Advection of the scalar steps and rates: "linear_upwind" or "muscl"
+        (cfdg_grid_set_advection; transport.rs Advection)."""
+        schemes = {"linear_upwind": 0, "muscl": 1}
+        if scheme not in schemes:
+            raise ValueError(f"advection is one of {sorted(schemes)}, not {scheme!r}")
+        self._check(self.L.cfdg_grid_set_advection(self.h, schemes[scheme]))
+
     def scalar_rates(self, u_ptr: int, c_ptr: int, d_ptr: int, source_ptr: int):
         """(emitted, inflow, outflow) rates in kg/s of the device field at c_ptr (cfdg_scalar_rates)."""
         r = (C.c_double * 3)()

@@ -190,6 +190,12 @@ int cfdg_scalar_step_budget(cfdg_grid *grid, const double *d_u, double *d_c, con
  * rhs_into returns them (the summary's source and boundary rates, solver.rs ScalarEvidence). */
 int cfdg_scalar_rates(cfdg_grid *grid, const double *d_u, const double *d_c, const double *d_diff,
                       const double *d_source, double *rates);
+/* The advection scheme of the grid's scalar steps and rates (Advection, transport.rs:
+ * 502-526, 670-694): 0 linear upwind (the default), 1 MUSCL, whose donor value is the
+ * upwind cell's value plus or minus half its monotonized-central limited slope along the
+ * face's axis (neighbours through interior faces only). Either is bit-identical to the
+ * reference's rhs_into. Other values: CFDG_ERR_INVALID. */
+int cfdg_grid_set_advection(cfdg_grid *grid, int32_t muscl);
 /* Receptors of a grid for cfdg_receptors_sample: n receptors' normalised weights as
  * receptor_weights (transport.rs:374-436) returns them, in CSR form: receptor r holds
  * cells[offsets[r] .. offsets[r+1]) with weights[...] in that order (host arrays, copied).
