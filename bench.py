@@ -1062,7 +1062,7 @@ TRANSPORT_WORKLOAD = ("128x128x64 grid, dx=2 m, 12 seeded box buildings, laminar
                       "one constituent on the flow projected from the initial velocity, linear upwind, cell "
                       "diffusivities 0.05-0.15 m2/s, a release of 1e-3 kg/m3/s in 64 cells near the inflow, "
                       "dt at CFL 0.4")
-TRANSPORT_METRIC = "scalar transport SSPRK2 steps/s (linear upwind, bit-identical to the reference arithmetic)"
+TRANSPORT_METRIC = "scalar transport SSPRK2 steps/s ({}, bit-identical to the reference arithmetic)"
 
 
 def transport_fields(pkg, g, seed):
@@ -1081,7 +1081,7 @@ def transport_fields(pkg, g, seed):
     return d, source, c
 
 
-def transport_cpu_baseline(case, u, d, source, c, dt):
+def transport_cpu_baseline(case, u, d, source, c, dt, muscl=False):
     """The oracle's advance_scalar on every host thread, each on its own grid and copy."""
     from oracle import oracle as O
 
@@ -1095,7 +1095,7 @@ def transport_cpu_baseline(case, u, d, source, c, dt):
     def work(t):
         x = c
         for _ in range(steps):
-            x = grids[t].scalar_step(x, u, d, source, dt)
+            x = grids[t].scalar_step(x, u, d, source, dt, muscl=muscl)
 
     for fn in (build, work):
         ths = [threading.Thread(target=fn, args=(t,)) for t in range(threads)]
@@ -1129,6 +1129,8 @@ def run_transport(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     d_u = torch.from_numpy(u).to(dev)
     d_d, d_s = torch.from_numpy(d).to(dev), torch.from_numpy(source).to(dev)
     d_c = torch.from_numpy(c.copy()).to(dev)
+    muscl = args.advection == "muscl"
+    dg.set_advection(args.advection)
 
     def step():
         dg.scalar_step_device(d_u.data_ptr(), d_c.data_ptr(), d_d.data_ptr(), d_s.data_ptr(), dt)
@@ -1191,22 +1193,28 @@ def run_transport(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            cpu = transport_cpu_baseline(case, u, d, source, c, dt)
-        line = {"metric": TRANSPORT_METRIC, "value": round(value, 4), "unit": "steps/s", "n_gpus": world,
+            cpu = transport_cpu_baseline(case, u, d, source, c, dt, muscl)
+        scheme = "MUSCL, monotonized-central limiter" if muscl else "linear upwind"
+        if muscl:
+            roofline_kernel = "k_scalar_pass<MUSCL> stage + combine (one step)"
+            limiter = ("FP64 pipe and gathers (each face once, with one limited slope of its upwind cell: "
+                       "one more concentration and face kind read per face)")
+        else:
+            roofline_kernel = "k_scalar_pass stage + combine (one step)"
+            limiter = "FP64 pipe (72 % active under ncu; about 24 FP64 adds and multiplies per cell and pass)"
+        line = {"metric": TRANSPORT_METRIC.format(scheme), "value": round(value, 4), "unit": "steps/s", "n_gpus": world,
                 "steps": K, "warmup": W, "ms_per_step": round(total_ms / K, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": TRANSPORT_WORKLOAD, "cells": n, "faces": f, "dt_s": dt,
+                "config": {"workload": TRANSPORT_WORKLOAD.replace("linear upwind", scheme), "cells": n, "faces": f, "dt_s": dt,
                            "l2": "256 MiB buffer written before every step", "parallelism": f"replicas x{world}"},
                 "cell_updates_per_s": round(world * K * n / (total_ms / 1e3), 1),
                 "e2e": {"value": round(world * K / (e2e_ms / 1e3), 4), "unit": "steps/s",
                         "h2d_bytes_per_step": 8 * (f + 3 * n), "d2h_bytes_per_step": 8 * n},
-                "roofline": {"bound": "hbm", "kernel": "k_scalar_pass stage + combine (one step)",
-                             "limiter": "FP64 pipe (72 % active under ncu; about 24 FP64 adds and multiplies "
-                                        "per cell and pass)",
+                "roofline": {"bound": "hbm", "kernel": roofline_kernel, "limiter": limiter,
                              "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                              "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                              "algorithmic_bytes_per_step": step_bytes, "kernel_ms_per_step": round(kern_ms, 4),
-                             "traffic": round(TRANSPORT_DRAM_BYTES_PER_CELL * n, 0)},
+                             "traffic": None if muscl else round(TRANSPORT_DRAM_BYTES_PER_CELL * n, 0)},
                 "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk}
         print(json.dumps(line), flush=True)
     return 0
@@ -1428,6 +1436,8 @@ def main():
     ap.add_argument("--form", default="serving",
                     choices=["plain", "mixed", "batched", "serving", "uneven", "large", "stepping", "transport",
                              "anisotropic"])
+    ap.add_argument("--advection", default="linear_upwind", choices=["linear_upwind", "muscl"],
+                    help="transport: the constituents' advection scheme")
     ap.add_argument("--slots", type=int, default=0, help="serving: cases on the GPU at once (0: all)")
     ap.add_argument("--requests", type=int, default=520, help="serving: open-loop requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")

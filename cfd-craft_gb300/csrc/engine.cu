@@ -31,6 +31,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/cfdgpu.h"
@@ -1950,12 +1951,39 @@ __device__ __forceinline__ bool nonneg(double x) {
 }
 __device__ __forceinline__ double half(double x) { return mul_pow2(x, Pow2{0.5, -1, 1}); }
 
+__device__ __forceinline__ double twice(double x) { return mul_pow2(x, Pow2{2.0, 1, 1}); }
+__device__ __forceinline__ bool is_nan64(double x) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+// minmod (transport.rs:510-516): 0 when a b <= 0 (the FP64 product, so an underflow to zero
+// counts), else signum(a) min(|a|, |b|). a is nonzero there, so signum(a) times the minimum
+// is the minimum with a's sign; f64::min of two magnitudes is the smaller bit pattern (a
+// NaN magnitude is above every number, and min returns the other operand); signum of a NaN
+// is NaN, and so is the product.
+__device__ __forceinline__ double minmod_bits(double a, double b) {
+  if (a * b <= 0.0) return 0.0;
+  if (is_nan64(a)) return a;
+  const long long ma = __double_as_longlong(a) & 0x7fffffffffffffffLL;
+  const long long mb = __double_as_longlong(b) & 0x7fffffffffffffffLL;
+  return __longlong_as_double((ma < mb ? ma : mb) | (__double_as_longlong(a) & (long long)0x8000000000000000ull));
+}
+// The monotonized-central slope (transport.rs:517-526) of a cell of value xc whose
+// neighbours along the axis have values lo and hi (the cell's own value where the face
+// between is not interior): minmod((hi - lo) / 2, minmod(2 (xc - lo), 2 (hi - xc))), the
+// products by 0.5 and 2 through the exponent field.
+__device__ __forceinline__ double mc_slope(double lo, double xc, double hi) {
+  return minmod_bits(half(hi - lo), minmod_bits(twice(xc - lo), twice(hi - xc)));
+}
+
 // The flux / volume of face f on axis a between cells lo_cell and hi_cell (its structural
 // neighbours, -1 outside the domain), evaluated on the field x; false if the face does not
 // transport. UNI: the layout's lo/hi (interior iff both are fluid) and per-axis constants.
 // P2 (with UNI): the volume and every transporting face's area and distance are powers of
 // two, so the products and quotients by them go through the exponent field.
-template <bool UNI, bool P2>
+// MUSCL (transport.rs:670-694): the donor is the upwind cell's value plus (flow towards hi)
+// or minus half its slope along a, whose neighbours are the cells across the upwind cell's
+// two faces on a (faces f -+ one face stride; the grid is not periodic, so both exist).
+template <bool UNI, bool P2, bool MUSCL = false>
 __device__ __forceinline__ bool face_eval(const ScalarDev& D, int a, long long f, long long lo_cell,
                                           long long hi_cell, const double* __restrict__ x,
                                           const double* __restrict__ u, const double* __restrict__ d, double& pv) {
@@ -1987,9 +2015,30 @@ __device__ __forceinline__ bool face_eval(const ScalarDev& D, int a, long long f
   }
   const double cl = hl ? x[lo_cell] : 0.0, cr = hh ? x[hi_cell] : 0.0;
   const double uf = u[f];
-  // Donor: the upwind cell's value (+ 0.0 when it exists; the inlet value 0.0 otherwise,
-  // whose + 0.0 is the same bits); `cr - 0.0` is cr for every cr.
-  const double donor = nonneg(uf) ? plus_zero(cl) : cr;
+  double donor;
+  if (MUSCL) {
+    const long long cs = a == 0 ? 1 : (a == 1 ? (long long)D.n[0] : (long long)D.n[0] * D.n[1]);
+    const long long fs = a == 0 ? 1 : (a == 1 ? (long long)D.fdim[1][0] : (long long)D.fdim[2][0] * D.fdim[2][1]);
+    // One slope per face, of the upwind cell, without a branch on the flow's sign: its
+    // value vc, the neighbour across face f (vf) and the one across its other face on a
+    // (vo, through face f -+ fs). donor = vc + h with h = +-slope / 2 equals the reference's
+    // cl + slope / 2 or cr - slope / 2 bit for bit (a - b is a + (-b)); without an upwind
+    // cell vc is the inlet value 0.0 and h = +-0.0, whose sum is 0.0 like the bare inlet value.
+    const bool up = nonneg(uf);
+    const double vc = up ? cl : cr;
+    double h = 0.0;
+    if (up ? hl : hh) {
+      const long long fo = up ? f - fs : f + fs;
+      const double vo = D.kind[fo] == INTERIOR ? x[up ? lo_cell - cs : hi_cell + cs] : vc;
+      const double vf = k == INTERIOR ? (up ? cr : cl) : vc;
+      h = half(mc_slope(up ? vo : vf, vc, up ? vf : vo));
+    }
+    donor = vc + (up ? h : -h);
+  } else {
+    // Donor: the upwind cell's value (+ 0.0 when it exists; the inlet value 0.0 otherwise,
+    // whose + 0.0 is the same bits); `cr - 0.0` is cr for every cr.
+    donor = nonneg(uf) ? plus_zero(cl) : cr;
+  }
   double diffusivity;
   if (hl && hh) diffusivity = half(d[lo_cell] + d[hi_cell]);
   else if (hl) diffusivity = d[lo_cell];
@@ -2005,14 +2054,10 @@ __device__ __forceinline__ bool face_eval(const ScalarDev& D, int a, long long f
   return true;
 }
 
-// MUSCL (transport.rs:502-526, 670-694): the donor value of a face is the upwind cell's
-// value plus (u >= 0: lo cell) or minus (hi cell) half its monotonized-central slope along
-// the face's axis; neighbours count only through interior faces. The operations are the
-// reference's, in its order (this file is compiled without FMA contraction).
-__device__ __forceinline__ double sc_minmod(double a, double b) {
-  if (a * b <= 0.0) return 0.0;
-  return (signbit(a) ? -1.0 : 1.0) * fmin(fabs(a), fabs(b));
-}
+// MUSCL from a face's own lo and hi (the budget's boundary faces): the donor value of a
+// face is the upwind cell's value plus (u >= 0: lo cell) or minus (hi cell) half its
+// monotonized-central slope along the face's axis; neighbours count only through interior
+// faces (transport.rs:502-526, 670-694).
 // The face index of cell (i, j, k)'s face on axis a, side 0 (lo) or 1 (hi); on a periodic
 // axis (n faces, not n + 1) the last cell's hi face is the wrap face 0.
 __device__ __forceinline__ long long sc_face(const ScalarDev& D, int a, int i, int j, int k, int side) {
@@ -2027,7 +2072,7 @@ __device__ __forceinline__ double sc_slope(const ScalarDev& D, const double* __r
   const double xc = x[cell];
   const double lo = D.kind[fl] == INTERIOR ? x[D.lo[fl]] : xc;
   const double hi = D.kind[fh] == INTERIOR ? x[D.hi[fh]] : xc;
-  return sc_minmod(0.5 * (hi - lo), sc_minmod(2.0 * (xc - lo), 2.0 * (hi - xc)));
+  return mc_slope(lo, xc, hi);
 }
 // The flux (kg/s) of transporting face f on axis a evaluated on x, rhs_into's arithmetic
 // from the face's own lo, hi, area and distance; false if the face does not transport.
@@ -2050,38 +2095,6 @@ __device__ __forceinline__ bool sc_flux(const ScalarDev& D, int a, long long f, 
   const double diff = k == OUTLET ? 0.0 : diffusivity * (cl - cr) / D.dist[f];
   flux = (uf * donor + diff) * D.area[f];
   return true;
-}
-
-// One pass of the SSPRK2 step with MUSCL donors, one thread per cell: the cell's six faces
-// in face order (the x faces, then y, then z; on an axis the lower face index first, the
-// periodic wrap face of the last cell before its lo face, and on a one-cell periodic axis
-// the face's lo update before its hi update), each face's flux / volume added where the
-// cell is the face's hi and subtracted where it is its lo, as rhs_into applies them, so
-// every cell receives the reference's sum; a face's flux is the same value for both cells.
-// MODE 0: stage = c + dt rhs(c); MODE 1: c = (c + stage + dt rhs(stage)) / 2.
-template <int MODE>
-__global__ void k_scalar_muscl(ScalarDev D, double* __restrict__ c, double* __restrict__ stage,
-                               const double* __restrict__ u, const double* __restrict__ d,
-                               const double* __restrict__ source, double dt, long long N) {
-  const double* __restrict__ x = MODE == 0 ? c : stage;
-  for (long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x; cell < N;
-       cell += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(cell % D.n[0]), j = (int)((cell / D.n[0]) % D.n[1]), k = (int)(cell / ((long long)D.n[0] * D.n[1]));
-    double v = source[cell];
-    for (int a = 0; a < 3; ++a) {
-      const long long fl = sc_face(D, a, i, j, k, 0), fh = sc_face(D, a, i, j, k, 1);
-      double flux;
-      if (fh <= fl) {
-        if (sc_flux(D, a, fh, x, u, d, true, flux)) v = v - flux / D.volume;
-        if (sc_flux(D, a, fl, x, u, d, true, flux)) v = v + flux / D.volume;
-      } else {
-        if (sc_flux(D, a, fl, x, u, d, true, flux)) v = v + flux / D.volume;
-        if (sc_flux(D, a, fh, x, u, d, true, flux)) v = v - flux / D.volume;
-      }
-    }
-    if (MODE == 0) stage[cell] = c[cell] + dt * v;
-    else c[cell] = 0.5 * (c[cell] + stage[cell] + dt * v);
-  }
 }
 
 // The rates transport.rs rhs_into returns with the right-hand side (solver.rs:828-833):
@@ -2157,7 +2170,7 @@ __global__ void k_scalar_budget(const double* __restrict__ pa, const double* __r
 // stage = c + dt rhs(c). MODE 1 (solver.rs:848-850): c = (c + stage + dt rhs(stage)) / 2, in
 // place (a thread reads c only at its own cell). Blocks are (32, 8); every thread reaches
 // every barrier and shuffle.
-template <bool UNI, bool P2, int MODE>
+template <bool UNI, bool P2, bool MUSCL, int MODE>
 __global__ void __launch_bounds__(STX * STY) k_scalar_pass(ScalarDev D, double* __restrict__ c,
                                                           double* __restrict__ stage, const double* __restrict__ u,
                                                           const double* __restrict__ d,
@@ -2176,7 +2189,7 @@ __global__ void __launch_bounds__(STX * STY) k_scalar_pass(ScalarDev D, double* 
   if (valid) {  // the z-lo face of the first slice
     const long long cell = z0 * sxy + j * sx + i;
     const long long f = D.face_off[2] + ((long long)z0 * D.fdim[2][1] + j) * D.fdim[2][0] + i;
-    zlo_on = face_eval<UNI, P2>(D, 2, f, z0 > 0 ? cell - sxy : -1, cell, x, u, d, zlo);
+    zlo_on = face_eval<UNI, P2, MUSCL>(D, 2, f, z0 > 0 ? cell - sxy : -1, cell, x, u, d, zlo);
   }
   for (int z = z0; z < z1; ++z) {
     const long long cell = z * sxy + j * sx + i;
@@ -2184,11 +2197,11 @@ __global__ void __launch_bounds__(STX * STY) k_scalar_pass(ScalarDev D, double* 
     bool xlo_on = false, xhi_on = false, ylo_on = false, yhi_on = false, zhi_on = false;
     if (valid) {
       const long long fx = D.face_off[0] + ((long long)z * D.fdim[0][1] + j) * D.fdim[0][0] + i;
-      xlo_on = face_eval<UNI, P2>(D, 0, fx, i > 0 ? cell - 1 : -1, cell, x, u, d, xlo);
+      xlo_on = face_eval<UNI, P2, MUSCL>(D, 0, fx, i > 0 ? cell - 1 : -1, cell, x, u, d, xlo);
       const long long fy = D.face_off[1] + ((long long)z * D.fdim[1][1] + j) * D.fdim[1][0] + i;
-      ylo_on = face_eval<UNI, P2>(D, 1, fy, j > 0 ? cell - sx : -1, cell, x, u, d, ylo);
+      ylo_on = face_eval<UNI, P2, MUSCL>(D, 1, fy, j > 0 ? cell - sx : -1, cell, x, u, d, ylo);
       const long long fz = D.face_off[2] + ((long long)(z + 1) * D.fdim[2][1] + j) * D.fdim[2][0] + i;
-      zhi_on = face_eval<UNI, P2>(D, 2, fz, cell, z + 1 < nz ? cell + sxy : -1, x, u, d, zhi);
+      zhi_on = face_eval<UNI, P2, MUSCL>(D, 2, fz, cell, z + 1 < nz ? cell + sxy : -1, x, u, d, zhi);
     }
     // x-hi: the next lane's x-lo, or computed here at the tile's or the domain's edge.
     const double nxt = __shfl_down_sync(0xffffffffu, xlo, 1);
@@ -2199,14 +2212,14 @@ __global__ void __launch_bounds__(STX * STY) k_scalar_pass(ScalarDev D, double* 
     if (valid) {
       if (tx == STX - 1 || i == nx - 1) {
         const long long fx = D.face_off[0] + ((long long)z * D.fdim[0][1] + j) * D.fdim[0][0] + i + 1;
-        xhi_on = face_eval<UNI, P2>(D, 0, fx, cell, i + 1 < nx ? cell + 1 : -1, x, u, d, xhi);
+        xhi_on = face_eval<UNI, P2, MUSCL>(D, 0, fx, cell, i + 1 < nx ? cell + 1 : -1, x, u, d, xhi);
       } else {
         xhi = nxt;
         xhi_on = nxt_on != 0;
       }
       if (ty == STY - 1 || j == ny - 1) {
         const long long fy = D.face_off[1] + ((long long)z * D.fdim[1][1] + j + 1) * D.fdim[1][0] + i;
-        yhi_on = face_eval<UNI, P2>(D, 1, fy, cell, j + 1 < ny ? cell + sx : -1, x, u, d, yhi);
+        yhi_on = face_eval<UNI, P2, MUSCL>(D, 1, fy, cell, j + 1 < ny ? cell + sx : -1, x, u, d, yhi);
       } else {
         yhi = s_pv[ty + 1][tx];
         yhi_on = s_on[ty + 1][tx] != 0;
@@ -2671,23 +2684,22 @@ static int scalar_impl(cfdg_grid* G, const double* d_u, double* d_c, const doubl
   for (int a = 0; a < 3; ++a)
     for (int t = 0; t < 3; ++t)
       if (G->sc_used[a][t]) p2 = p2 && D.area_p[a][t].ok && D.inv_dist_p[a][t].ok;
+  auto passes = [&](auto uni, auto p2c, auto muscl) {
+    constexpr bool U = decltype(uni)::value, P = decltype(p2c)::value, M = decltype(muscl)::value;
+    k_scalar_pass<U, P, M, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+    rates_of_stages();
+    k_scalar_pass<U, P, M, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+  };
+  using T = std::true_type;
+  using F = std::false_type;
   if (G->sc_muscl) {
-    const int nb = (int)std::min<long long>(((long long)N + 255) / 256, 152LL * 16);
-    k_scalar_muscl<0><<<nb, 256, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt, N); tick(G);
-    rates_of_stages();
-    k_scalar_muscl<1><<<nb, 256, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt, N); tick(G);
-  } else if (p2) {
-    k_scalar_pass<true, true, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
-    rates_of_stages();
-    k_scalar_pass<true, true, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
-  } else if (G->sc_uniform) {
-    k_scalar_pass<true, false, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
-    rates_of_stages();
-    k_scalar_pass<true, false, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+    if (p2) passes(T{}, T{}, T{});
+    else if (G->sc_uniform) passes(T{}, F{}, T{});
+    else passes(F{}, F{}, T{});
   } else {
-    k_scalar_pass<false, false, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
-    rates_of_stages();
-    k_scalar_pass<false, false, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+    if (p2) passes(T{}, T{}, F{});
+    else if (G->sc_uniform) passes(T{}, F{}, F{});
+    else passes(F{}, F{}, F{});
   }
   if (mode == 1) {
     k_scalar_budget<<<1, 32, 0, s>>>(G->sc_part, G->sc_part + 3 * SR_BLOCKS, D.volume, dt, d_budget, nullptr);

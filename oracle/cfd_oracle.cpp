@@ -1776,10 +1776,11 @@ static int flow_euler(Grid& g, const double* u, const double* p, double dt, doub
 }
 
 // transport.rs:510-516 minmod: 0 when a b <= 0, else signum(a) min(|a|, |b|) (a is
-// nonzero then, so signum is +-1).
+// nonzero then, so f64::signum is +-1, or NaN for a NaN).
 static double minmod(double a, double b) {
   if (a * b <= 0.0) return 0.0;
-  return (std::signbit(a) ? -1.0 : 1.0) * std::fmin(std::fabs(a), std::fabs(b));
+  const double signum = std::isnan(a) ? a : (std::signbit(a) ? -1.0 : 1.0);
+  return signum * std::fmin(std::fabs(a), std::fabs(b));
 }
 // transport.rs:502-509: the cell across cell i's face on axis a, side 0 (lo) or 1 (hi),
 // when that face is interior.

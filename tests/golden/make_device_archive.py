@@ -94,6 +94,7 @@ def gas_archive(pkg, out_dir):
     dev = torch.device("cuda", 0)
     dg = pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed")
     dg.set_flow(case)
+    dg.set_advection(case["numerics"]["transport"])
     u, p = g.initial_velocity(), np.zeros(g.count)
     its = dg.project(u, p, 1.0, 1e-8, 10000).iterations
     p[:] = 0.0
