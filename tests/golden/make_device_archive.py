@@ -11,7 +11,7 @@ dt = 0.1 s with cfdg_step_device (a projection per stage), copies the fields bac
 writes the archive with the package's writer (output.rs:162-242 format) into
 OUT_DIR/device_archive_<form> (default: this directory). device_archive_gas adds a gas
 constituent (a point and a volume source, a point and a volume receptor) on a 16x12x8
-case: each of four steps of dt = 0.1 s is a flow step (mixed form) and a transport step
+case, and device_archive_gas_muscl the same case with MUSCL advection: each of four steps of dt = 0.1 s is a flow step (mixed form) and a transport step
 with its budget (cfdg_scalar_step_budget), then the current rates (cfdg_scalar_rates)
 and the receptor values (cfdg_receptors_sample), all computed on the device.
 """
@@ -65,10 +65,12 @@ def main(out_dir=HERE):
         print(out)
 
 
-def gas_case(pkg):
+def gas_case(pkg, advection="linear_upwind"):
+    suffix = "" if advection == "linear_upwind" else "-" + advection
     case = pkg.synth.case((16, 12, 8), 2.0, inflow=3.0, boxes=[((10.0, 6.0, 0.0), (16.0, 14.0, 8.0))],
-                          name="device-archive-gas-16x12x8")
+                          name="device-archive-gas-16x12x8" + suffix)
     case["output"]["fields"] = True
+    case["numerics"]["transport"] = advection
     case["constituents"] = [{"id": "gas", "diffusivity_m2_s": 0.05}]
     case["sources"] = [
         {"id": "stack", "kind": "point", "constituent": "gas", "point_m": [5.0, 5.0, 3.0], "rate_kg_s": 2e-3},
@@ -82,14 +84,14 @@ def gas_case(pkg):
     return case
 
 
-def gas_archive(pkg, out_dir):
+def gas_archive(pkg, out_dir, advection="linear_upwind"):
     import torch
     from importlib import import_module
 
     A = import_module(pkg.__name__ + ".archive")
     S = import_module(pkg.__name__ + ".sources")
     R = import_module(pkg.__name__ + ".receptors")
-    case = gas_case(pkg)
+    case = gas_case(pkg, advection)
     g = pkg.grid.Grid.build(case)
     dev = torch.device("cuda", 0)
     dg = pkg.pressure.DeviceGrid(g, preconditioner="multigrid", precision="mixed")
@@ -118,7 +120,7 @@ def gas_archive(pkg, out_dir):
              "budget": {"initial_kg": 0.0, "emitted_kg": float(b[0]), "inflow_kg": float(b[1]),
                         "outflow_kg": float(b[2])}}
     dg.close()
-    out = os.path.join(out_dir, "device_archive_gas")
+    out = os.path.join(out_dir, "device_archive_gas" + ("" if advection == "linear_upwind" else "_" + advection))
     if os.path.exists(out):
         import shutil
 
@@ -133,4 +135,5 @@ if __name__ == "__main__":
     sys.path.insert(0, ROOT)
     import __graft_entry__ as entry
 
-    gas_archive(entry.package(), sys.argv[1] if len(sys.argv) > 1 else HERE)
+    for scheme in ("linear_upwind", "muscl"):
+        gas_archive(entry.package(), sys.argv[1] if len(sys.argv) > 1 else HERE, scheme)

@@ -4,7 +4,8 @@ tests/golden/device_archive_{plain,mixed} hold archives of three laminar SSPRK2 
 that cfdg_step_device computed on a GB300 (plain FP64 and mixed FP32/FP64 projections),
 written by the package's archive writer; device_archive_gas adds a gas constituent whose
 transport steps, mass budget (cfdg_scalar_step_budget), current rates and receptor values
-were computed on the device too; tests/golden/make_device_archive.py made them.
+were computed on the device too, and device_archive_gas_muscl the same with MUSCL
+advection; tests/golden/make_device_archive.py made them.
 The unmodified validation/check_fields.py of a CFD-craft checkout (its independent
 archive checker: hashes, mask, finiteness and the independent local continuity,
 validation/check_fields.py:299-530) must pass on them; it runs when a checkout is
@@ -21,7 +22,7 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
 REFERENCE = os.environ.get("CFD_CRAFT_REFERENCE", "/root/reference")
-FORMS = ("plain", "mixed", "gas")
+FORMS = ("plain", "mixed", "gas", "gas_muscl")
 
 
 def archive(form):
@@ -57,7 +58,7 @@ def test_device_archive_passes_reference_checker(form):
     print(form, json.dumps(result))
     assert result["passed"] is True
     assert result["max_divergence_s_inv"] < 1e-7
-    if form == "gas":  # the independent mass accounting of the device budget
+    if form.startswith("gas"):  # the independent mass accounting of the device budget
         assert len(result["scalars"]) == 1 and result["scalars"][0]["relative_defect"] < 1e-9
 
 
