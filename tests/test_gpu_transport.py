@@ -68,12 +68,14 @@ def test_scalar_steps_bit_identical(pkg, O, name, perturb):
     dg.close()
 
 
+@pytest.mark.parametrize("muscl", [False, True])
 @pytest.mark.parametrize("name,perturb", [("wide-tiles", False), ("buildings-open-wall", False),
                                           ("spacing-1.5m", False), ("wide-tiles", True)])
-def test_scalar_steps_extreme_values_bit_identical(pkg, O, name, perturb):
+def test_scalar_steps_extreme_values_bit_identical(pkg, O, name, perturb, muscl):
     """Signed zeros, subnormals and values near the top of the range in the concentration,
     diffusivity and source: the exponent-field products and the `+ 0.0` on bits must give
-    the FP64 operations' bits there too."""
+    the FP64 operations' bits there too; with MUSCL also the limiter's products by 0.5 and
+    2, its minimum on the bits and its products a b that underflow to zero."""
     torch = pytest.importorskip("torch")
     case = flow_case(pkg, name)
     g = pkg.grid.Grid.build(case)
@@ -92,12 +94,13 @@ def test_scalar_steps_extreme_values_bit_identical(pkg, O, name, perturb):
         dist = np.asarray(g.face_distance) * rng.uniform(0.9, 1.1, g.n_faces)
         og.set_faces(area, dist)
         dg.update_faces(area, dist)
+    dg.set_advection("muscl" if muscl else "linear_upwind")
     dev = torch.device("cuda", 0)
     d_u, d_c = torch.from_numpy(u).to(dev), torch.from_numpy(c.copy()).to(dev)
     d_d, d_s = torch.from_numpy(d).to(dev), torch.from_numpy(source).to(dev)
     ref = c.copy()
     for step in range(3):
-        ref = og.scalar_step(ref, u, d, source, dt)
+        ref = og.scalar_step(ref, u, d, source, dt, muscl=muscl)
         dg.scalar_step_device(d_u.data_ptr(), d_c.data_ptr(), d_d.data_ptr(), d_s.data_ptr(), dt)
         torch.cuda.synchronize()
         got = d_c.cpu().numpy()
