@@ -56,6 +56,9 @@ RB_DRAM_BYTES_PER_CELL = (29541888 + 18944000) / 4194304
 # DRAM bytes of one scalar transport step (both passes) per cell, from one ncu capture of
 # k_scalar_pass on the 128x128x64 transport workload.
 TRANSPORT_DRAM_BYTES_PER_CELL = (54496768 + 337408 + 62883584 + 301824) / 1048576
+# The same for the MUSCL passes (one capture, blocks of 8 slices; the per-grid split of 4
+# slices re-reads one more z face plane per block, mostly from L2).
+MUSCL_DRAM_BYTES_PER_CELL = (54467328 + 542208 + 62851072 + 452352) / 1048576
 
 
 def max_over_ranks(value, dist, device):
@@ -1197,8 +1200,8 @@ def run_transport(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
         scheme = "MUSCL, monotonized-central limiter" if muscl else "linear upwind"
         if muscl:
             roofline_kernel = "k_scalar_pass<MUSCL> stage + combine (one step)"
-            limiter = ("FP64 pipe and gathers (each face once, with one limited slope of its upwind cell: "
-                       "one more concentration and face kind read per face)")
+            limiter = ("FP64 pipe (78 % active under ncu; each face once, with one limited slope of its "
+                       "upwind cell; minmod's sign test on the bits)")
         else:
             roofline_kernel = "k_scalar_pass stage + combine (one step)"
             limiter = "FP64 pipe (72 % active under ncu; about 24 FP64 adds and multiplies per cell and pass)"
@@ -1214,7 +1217,8 @@ def run_transport(args, pkg, torch, dev, stream, flush, rank, world, dist, L):
                              "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                              "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                              "algorithmic_bytes_per_step": step_bytes, "kernel_ms_per_step": round(kern_ms, 4),
-                             "traffic": None if muscl else round(TRANSPORT_DRAM_BYTES_PER_CELL * n, 0)},
+                             "traffic": round((MUSCL_DRAM_BYTES_PER_CELL if muscl
+                                               else TRANSPORT_DRAM_BYTES_PER_CELL) * n, 0)},
                 "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk}
         print(json.dumps(line), flush=True)
     return 0

@@ -1921,7 +1921,7 @@ struct ScalarDev {
   Pow2 area_p[3][3], inv_dist_p[3][3];
 };
 
-constexpr int STX = 32, STY = 8, STZ = 8;  // cells of one transport tile (x, y, z)
+constexpr int STX = 32, STY = 8;  // cells of one transport tile in x and y (its z extent is chosen per grid)
 
 __device__ __forceinline__ int transport_slot(uint8_t k) { return k == INTERIOR ? 0 : (k == INLET ? 1 : 2); }
 
@@ -1955,13 +1955,38 @@ __device__ __forceinline__ double twice(double x) { return mul_pow2(x, Pow2{2.0,
 __device__ __forceinline__ bool is_nan64(double x) {
   return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
 }
+__device__ __noinline__ bool fp64_prod_le0(double a, double b) { return a * b <= 0.0; }
+// The exponent q of |x| = m 2^q, m in [1, 2), from its nonzero finite magnitude bits.
+__device__ __forceinline__ int exp_of(long long mag) {
+  const int e = (int)(mag >> 52);
+  return e ? e - 1023 : -1074 + (63 - __clzll(mag));
+}
+// a * b <= 0.0 as the FP64 product and comparison decide it, on the bits where the signs and
+// exponents settle it: a NaN operand or 0 * inf gives NaN (false); a zero operand a zero
+// product (true); different signs a negative product or -0 (true); an infinite operand of
+// the same sign +inf (false). Same-sign finite products are at least 2^-1074, the smallest
+// subnormal, when qa + qb >= -1074 (false) and below 2^-1075, so rounded to zero, when
+// qa + qb <= -1077 (true); the two exponent sums between go to the FP64 product.
+__device__ __forceinline__ bool prod_le_zero(double a, double b) {
+  const long long ua = __double_as_longlong(a), ub = __double_as_longlong(b);
+  const long long ma = ua & 0x7fffffffffffffffLL, mb = ub & 0x7fffffffffffffffLL;
+  const long long inf = 0x7ff0000000000000LL;
+  if (ma > inf || mb > inf) return false;
+  if (ma == 0 || mb == 0) return ma != inf && mb != inf;
+  if ((ua ^ ub) < 0) return true;
+  if (ma == inf || mb == inf) return false;
+  const int q = exp_of(ma) + exp_of(mb);
+  if (q >= -1074) return false;
+  if (q <= -1077) return true;
+  return fp64_prod_le0(a, b);
+}
 // minmod (transport.rs:510-516): 0 when a b <= 0 (the FP64 product, so an underflow to zero
-// counts), else signum(a) min(|a|, |b|). a is nonzero there, so signum(a) times the minimum
+// counts; decided by prod_le_zero), else signum(a) min(|a|, |b|). a is nonzero there, so signum(a) times the minimum
 // is the minimum with a's sign; f64::min of two magnitudes is the smaller bit pattern (a
 // NaN magnitude is above every number, and min returns the other operand); signum of a NaN
 // is NaN, and so is the product.
 __device__ __forceinline__ double minmod_bits(double a, double b) {
-  if (a * b <= 0.0) return 0.0;
+  if (prod_le_zero(a, b)) return 0.0;
   if (is_nan64(a)) return a;
   const long long ma = __double_as_longlong(a) & 0x7fffffffffffffffLL;
   const long long mb = __double_as_longlong(b) & 0x7fffffffffffffffLL;
@@ -2166,7 +2191,7 @@ __global__ void k_scalar_budget(const double* __restrict__ pa, const double* __r
   if (budget) budget[k] += 0.5 * dt * (a + b);
 }
 
-// One pass of the SSPRK2 step over a (32, 8, 8) tile of cells. MODE 0 (solver.rs:845-847):
+// One pass of the SSPRK2 step over a tile of (32, 8, zs) cells. MODE 0 (solver.rs:845-847):
 // stage = c + dt rhs(c). MODE 1 (solver.rs:848-850): c = (c + stage + dt rhs(stage)) / 2, in
 // place (a thread reads c only at its own cell). Blocks are (32, 8); every thread reaches
 // every barrier and shuffle.
@@ -2174,14 +2199,14 @@ template <bool UNI, bool P2, bool MUSCL, int MODE>
 __global__ void __launch_bounds__(STX * STY) k_scalar_pass(ScalarDev D, double* __restrict__ c,
                                                           double* __restrict__ stage, const double* __restrict__ u,
                                                           const double* __restrict__ d,
-                                                          const double* __restrict__ source, double dt) {
+                                                          const double* __restrict__ source, double dt, int zs) {
   __shared__ double s_pv[STY][STX];
   __shared__ uint8_t s_on[STY][STX];
   const double* __restrict__ x = MODE == 0 ? c : stage;  // the field the right-hand side reads
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int nx = D.n[0], ny = D.n[1], nz = D.n[2];
   const int i = blockIdx.x * STX + tx, j = blockIdx.y * STY + ty;
-  const int z0 = blockIdx.z * STZ, z1 = min(z0 + STZ, nz);
+  const int z0 = blockIdx.z * zs, z1 = min(z0 + zs, nz);
   const bool valid = i < nx && j < ny;
   const long long sx = nx, sxy = (long long)nx * ny;
   double zlo = 0.0;
@@ -2240,6 +2265,30 @@ __global__ void __launch_bounds__(STX * STY) k_scalar_pass(ScalarDev D, double* 
     zlo_on = zhi_on;
     __syncthreads();  // s_pv is rewritten by the next slice
   }
+}
+
+// Slices per block of the scalar passes: the z extent split so that the blocks' slices
+// spread evenly over the SMs (the passes are FP64-pipe bound, so an SM's time follows the
+// slices it is given: about ceil(blocks / SMs) zs), counting the z face each block
+// evaluates once more than its slices need (a third of a slice's faces), among the splits
+// that give every SM its four resident blocks (the smallest split where none does).
+int scalar_zsplit(const int32_t n[3], int device) {
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  sms = std::max(sms, 1);
+  const long long cols = (long long)((n[0] + STX - 1) / STX) * ((n[1] + STY - 1) / STY);
+  int best = 2;
+  double best_cost = 1e300;
+  for (int zs = 2; zs <= 16; ++zs) {
+    const long long blocks = cols * ((n[2] + zs - 1) / zs);
+    if (zs > 2 && blocks < 4LL * sms) continue;
+    const double cost = (double)((blocks + sms - 1) / sms) * std::min(zs, n[2]) * (1.0 + 1.0 / (3.0 * zs));
+    if (cost < best_cost - 1e-9) {
+      best_cost = cost;
+      best = zs;
+    }
+  }
+  return best;
 }
 
 FlowDev flow_dev(cfdg_grid* G) {
@@ -2671,7 +2720,8 @@ static int scalar_impl(cfdg_grid* G, const double* d_u, double* d_c, const doubl
     CU(cudaStreamSynchronize(s));
     return 0;
   }
-  const dim3 blk(STX, STY), grd((G->h.n[0] + STX - 1) / STX, (G->h.n[1] + STY - 1) / STY, (G->h.n[2] + STZ - 1) / STZ);
+  const int zs = scalar_zsplit(G->h.n, G->ctx->device);
+  const dim3 blk(STX, STY), grd((G->h.n[0] + STX - 1) / STX, (G->h.n[1] + STY - 1) / STY, (G->h.n[2] + zs - 1) / zs);
   // The budget's rates: of c before the second pass overwrites it, and of the stage.
   auto rates_of_stages = [&]() {
     if (mode != 1) return;
@@ -2686,9 +2736,9 @@ static int scalar_impl(cfdg_grid* G, const double* d_u, double* d_c, const doubl
       if (G->sc_used[a][t]) p2 = p2 && D.area_p[a][t].ok && D.inv_dist_p[a][t].ok;
   auto passes = [&](auto uni, auto p2c, auto muscl) {
     constexpr bool U = decltype(uni)::value, P = decltype(p2c)::value, M = decltype(muscl)::value;
-    k_scalar_pass<U, P, M, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+    k_scalar_pass<U, P, M, 0><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt, zs); tick(G);
     rates_of_stages();
-    k_scalar_pass<U, P, M, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt); tick(G);
+    k_scalar_pass<U, P, M, 1><<<grd, blk, 0, s>>>(D, d_c, stage, d_u, d_diff, d_source, dt, zs); tick(G);
   };
   using T = std::true_type;
   using F = std::false_type;

@@ -87,3 +87,53 @@ def test_half_and_twice_equal_fp64_products():
         for x in vals:
             assert same(mul_pow2_shift(x, -1), np.float64(0.5) * np.float64(x)), x
             assert same(mul_pow2_shift(x, 1), np.float64(2.0) * np.float64(x)), x
+
+
+def prod_le_zero_device(a, b):
+    """The device's `a * b <= 0.0` (prod_le_zero) on the bits: NaN operands and 0 * inf give
+    NaN (false); a zero operand gives a zero product (true); different signs a negative
+    product (true); an infinite operand of the same sign +inf (false). Same-sign finite
+    nonzero operands |a| = ma 2^qa, |b| = mb 2^qb (ma, mb in [1, 2)): the product is at
+    least 2^-1074, the smallest subnormal, when qa + qb >= -1074 (false) and below 2^-1075,
+    half of it, so rounding to zero, when qa + qb <= -1077 (true); in between the FP64
+    product decides."""
+    ua, ub = int(u64(a)), int(u64(b))
+    ma, mb = ua & 0x7FFFFFFFFFFFFFFF, ub & 0x7FFFFFFFFFFFFFFF
+    inf = 0x7FF0000000000000
+    if ma > inf or mb > inf:
+        return False
+    if ma == 0 or mb == 0:
+        return not (ma == inf or mb == inf)
+    if (ua ^ ub) >> 63:
+        return True
+    if ma == inf or mb == inf:
+        return False
+
+    def q(m):
+        e = m >> 52
+        return e - 1023 if e else -1074 + (m.bit_length() - 1)
+
+    s = q(ma) + q(mb)
+    if s >= -1074:
+        return False
+    if s <= -1077:
+        return True
+    with np.errstate(all="ignore"):
+        return bool(np.float64(a) * np.float64(b) <= 0.0)
+
+
+def test_product_sign_test_on_bits_equals_fp64():
+    rng = np.random.default_rng(12)
+    edge = [np.ldexp(1.0, e) for e in range(-1076, -1070)] + [np.ldexp(1.5, e) for e in range(-540, -530)]
+    vals = list(SPECIAL) + edge + [np.nextafter(np.ldexp(1.0, -537), 1.0), np.ldexp(1.0, -537), 2.0 ** -538]
+    vals += list(np.ldexp(rng.uniform(-2.0, 2.0, 3000), rng.integers(-1074, 1024, 3000)))
+    vals += list(np.ldexp(rng.uniform(0.5, 2.0, 3000), rng.integers(-545, -530, 3000)))
+    vals = np.array(vals, dtype=np.float64)
+    with np.errstate(all="ignore"):
+        for a in vals[rng.permutation(vals.size)[:400]]:
+            want = (np.float64(a) * vals) <= 0.0
+            got = np.array([prod_le_zero_device(a, b) for b in vals])
+            bad = np.nonzero(want != got)[0]
+            assert bad.size == 0, (a, vals[bad[:3]])
+        for a, b in itertools.product(SPECIAL, SPECIAL):
+            assert prod_le_zero_device(a, b) == bool(np.float64(a) * np.float64(b) <= 0.0), (a, b)
