@@ -61,7 +61,6 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 template <int MODE>
 __global__ void __launch_bounds__(WTJ* WTK) k_wave(WaveArgs A) {
   constexpr bool BWD = (MODE == IC0_BWD || MODE == GS_BWD);
-  constexpr bool GS = (MODE == GS_FWD || MODE == GS_BWD);
   __shared__ double sh[2][WTK][WTJ];
   __shared__ int tile_s, bail_s;
   __shared__ int seen_j, seen_k;
@@ -139,7 +138,6 @@ __global__ void __launch_bounds__(WTJ* WTK) k_wave(WaveArgs A) {
       const long long c = ((long long)k * ny + j) * nx + i;
       const unsigned fl = A.flags[c];
       // Neighbour values already updated in this sweep ("new") along x, y, z.
-      const bool has_nx = BWD ? i + 1 < nx : i > 0;
       const bool has_ny = BWD ? j + 1 < ny : j > 0;
       const bool has_nz = BWD ? k + 1 < nz : k > 0;
       const bool in_tile_y = BWD ? tj + 1 < WTJ : tj > 0;
