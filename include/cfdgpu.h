@@ -173,7 +173,8 @@ int cfdg_step_device(cfdg_grid *grid, double *d_u, double *d_p, double dt, doubl
 /* One SSPRK2 step of a constituent's concentration d_c (N, kg/m3) in place on the face
  * velocities d_u (F), with cell diffusivities d_diff (N, m2/s: the constituent's plus
  * nu_t / Sc) and source densities d_source (N, kg/m3/s): advance_scalar
- * (solver.rs:808-855) with linear upwind (transport.rs:651-699) and zero inflow
+ * (solver.rs:808-855) with the grid's advection scheme (linear upwind unless
+ * cfdg_grid_set_advection selects MUSCL; transport.rs:651-699) and zero inflow
  * concentration, bit-identical to it; the budgets are not kept (cfdg_scalar_step_budget
  * keeps them). Non-periodic grids. */
 int cfdg_scalar_step_device(cfdg_grid *grid, const double *d_u, double *d_c, const double *d_diff,
